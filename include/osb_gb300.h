@@ -1,0 +1,179 @@
+/*
+ * osb_gb300.h -- C ABI of the GB300 (sm_103a) residual-and-update path for OpenSBLI.
+ *
+ * The reference turns a problem script into OPS C++ (opensbli/code_generation/opsc.py:407-460)
+ * whose main() runs, per RK stage, constituent-relation loops, one characteristic
+ * WENO/TENO reconstruction loop per direction, the residual loop, the central derivative and
+ * viscous loops, the RK update loop and the halo exchanges
+ * (apps/performance_benchmark/TENO6/opensbli.cpp:206-431).  This library replaces that whole
+ * stage: the Python backend (opensbli_gb300/backend.py, standing in for OPSC(alg)) fills one
+ * osb_block_desc per OpenSBLI block and drives the steps through the calls below.
+ *
+ * Conventions
+ *  - Every function returns an int status: OSB_OK (0) or a negative OSB_E* code; the text of
+ *    the last error of the calling thread is read with osb_last_error().  No C++ exception
+ *    crosses this boundary.
+ *  - Arrays use the OPS layout the generated code declares (opsc.py:1182-1196): one array per
+ *    variable, x fastest, `halo` (=5) points on both sides of every used dimension, FP64.
+ *    Pointers in osb_block_desc are DEVICE pointers owned by the caller (borrowed until
+ *    osb_ctx_destroy).
+ *  - A context serves one host thread and owns one CUDA stream on its device.
+ */
+#ifndef OSB_GB300_H
+#define OSB_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define OSB_VERSION 100
+
+#define OSB_OK 0
+#define OSB_EINVAL -1      /* bad argument or descriptor */
+#define OSB_ECUDA -2       /* CUDA runtime error */
+#define OSB_ETIMEDOUT -3   /* osb_sync gave up waiting */
+#define OSB_ENOTSUP -4     /* configuration outside the supported path */
+#define OSB_ENAN -5        /* non-finite value detected in the state */
+
+/* Convective (shock-capturing) scheme: LFWeno/LFTeno (opensbli/schemes/spatial/weno.py:475,
+ * teno.py:480) with characteristic local Lax-Friedrichs splitting; or the central
+ * skew-symmetric (Feiereisen) form of physical_models/split_forms.py with StoreSome(4). */
+#define OSB_SCHEME_WENO5_JS 1
+#define OSB_SCHEME_WENO5_Z 2
+#define OSB_SCHEME_TENO5 3
+#define OSB_SCHEME_CENTRAL4 5
+
+/* Averaging for the characteristic system (schemes/spatial/averaging.py:31,65). */
+#define OSB_AVG_SIMPLE 0
+#define OSB_AVG_ROE 1
+
+/* Viscous terms: none (Euler), modified Sutherland law mu(T) (compressible_TGV.py:82), or
+ * constant viscosity (split_forms.py viscosity='constant'). */
+#define OSB_VISC_NONE 0
+#define OSB_VISC_SUTHERLAND 1
+#define OSB_VISC_CONSTANT 2
+
+/* Boundary conditions per face (core/boundary_conditions/). */
+#define OSB_BC_PERIODIC 0    /* PeriodicBC -> ExchangeSelf (periodic.py:25-71) */
+#define OSB_BC_ZERO_GRAD 1   /* ZeroGradientOutletBC (zero_gradient_outlet.py:11-23) */
+#define OSB_BC_INTERFACE 2   /* InterfaceBC between blocks (multi_block.py:48-107) */
+
+/* Residual precision (per context). */
+#define OSB_PREC_FP64 0          /* plain FP64 path, parity with the generated solver */
+#define OSB_PREC_FP32_RESIDUAL 1 /* FP32 residual arithmetic, FP64 state/RK/reductions */
+
+/* Time integrators (schemes/temporal/rk_LS.py, rk_sbli.py). */
+#define OSB_RK_LOW_STORAGE 0     /* RKold = A*RKold + dt*R ; q += B*RKold */
+#define OSB_RK_SBLI3 1           /* old = q at step start; q = old + dt*B*R ; old += dt*A*R */
+
+/* Reductions (osb_reduce). */
+#define OSB_RED_KE 0             /* sum 0.5*rho*|u|^2 over interior points */
+#define OSB_RED_ENSTROPHY_DISS 1 /* sum mu*|curl u|^2 (central-4 derivatives) */
+#define OSB_RED_DILATATION_DISS 2/* sum 4/3*mu*(div u)^2 */
+#define OSB_RED_RHO_SUM 3        /* sum rho */
+#define OSB_RED_CFL_DT 4         /* min over points of 1/sum_d (|u_d|+a)/Delta_d */
+#define OSB_RED_NAN_COUNT 5      /* number of non-finite values in the state */
+
+typedef struct osb_ctx osb_ctx;
+
+typedef struct osb_interface {
+  int32_t block;   /* index (osb_block_add order) of the neighbouring block */
+  int32_t dir;     /* its direction that faces this one */
+  int32_t side;    /* its side (0 = low, 1 = high) */
+  int32_t flip;    /* 1 if the transverse index runs backwards across the interface */
+} osb_interface;
+
+typedef struct osb_block_desc {
+  int32_t ndim;              /* 1, 2 or 3 */
+  int32_t size[3];           /* interior points per direction (1 for unused directions) */
+  int32_t halo;              /* halo points on each side of every used direction: 5 */
+  int32_t scheme;            /* OSB_SCHEME_* */
+  int32_t averaging;         /* OSB_AVG_* */
+  int32_t viscous;           /* OSB_VISC_* */
+  int32_t bc[3][2];          /* OSB_BC_* per direction, side */
+  int32_t bc_depth[3][2];    /* halo layers written by that boundary (4 or 5) */
+  osb_interface iface[3][2]; /* neighbour for OSB_BC_INTERFACE faces */
+  double gama, Minf, Re, Pr;
+  double mu_const;           /* OSB_VISC_CONSTANT: dimensionless viscosity (1.0 in the TGV app) */
+  double eps;                /* TENO epsilon (teno.py:369-371) */
+  double teno_ct;            /* TENO cut-off C_T (teno.py:373-377) */
+  double shock_filter_control; /* LLF wave-speed scale (shock_capturing.py:1008-1019) */
+  double delta[3];           /* grid spacing per direction */
+  double* q[5];              /* conserved variables rho, rhou0.., rhoE (device, OPS layout) */
+  double* rkold[5];          /* RK register (device, OPS layout) */
+  const double* metric[10];  /* curvilinear: D00 D01 D02 D10 D11 D12 D20 D21 D22 detJ, or NULL */
+} osb_block_desc;
+
+/* ---- library / context ------------------------------------------------------------- */
+
+/* Library version (OSB_VERSION). */
+int osb_version(void);
+
+/* Copies the calling thread's last error message into buf (NUL terminated); returns its
+ * length. */
+int osb_last_error(char* buf, size_t n);
+
+/* Creates a context on `device` with residual precision OSB_PREC_*; replaces ops_init and
+ * the generated OPS declarations (opensbli.cpp:45-160). */
+int osb_ctx_create(int device, int precision, osb_ctx** out);
+
+/* Destroys the context, its stream, graphs and workspaces. */
+int osb_ctx_destroy(osb_ctx* ctx);
+
+/* Registers one block (ops_decl_block + ops_decl_dat of q / RKold, defdec_data_set.h).
+ * Blocks of one context share the scheme, averaging, viscosity and precision; sizes,
+ * spacings, boundaries and arrays may differ.  *block_id receives the block index. */
+int osb_block_add(osb_ctx* ctx, const osb_block_desc* desc, int* block_id);
+
+/* Selects the time integrator and its coefficients (rk_LS.py:97-132 / rk_sbli.py:75-77).
+ * A = stage coefficients (rkA / rknew), B = solution coefficients (rkB / rkold). */
+int osb_set_rk(osb_ctx* ctx, int kind, int nstages, const double* A, const double* B);
+
+/* ---- time stepping (the generated time loop, opensbli.cpp:206-431) ------------------- */
+
+/* Advances every block by nsteps full RK steps of size dt.  With graphs enabled the step is
+ * captured once into a CUDA graph and replayed.  Asynchronous: returns after queueing. */
+int osb_step(osb_ctx* ctx, double dt, int nsteps);
+
+/* Runs one RK stage (index `stage`) on every block: residual, update, boundaries. */
+int osb_stage(osb_ctx* ctx, int stage, double dt);
+
+/* Applies the boundary conditions / halo exchanges of every block once
+ * (ops_halo_transfer / boundary kernels of the generated code). */
+int osb_apply_bc(osb_ctx* ctx);
+
+/* Writes the residual dq/dt of block `block` (before any update) into the caller's device
+ * arrays out[nvars] (OPS layout, FP64) -- per-kernel parity hook. */
+int osb_residual(osb_ctx* ctx, int block, double* const* out);
+
+/* FP64 global reduction over all blocks of the context (OSB_RED_*); replaces the
+ * ops_reduction_result calls of the generated post-processing (opensbli.cpp:450-453). */
+int osb_reduce(osb_ctx* ctx, int what, double* host_out);
+
+/* Waits for the context's stream, giving up after timeout_ms (OSB_ETIMEDOUT). */
+int osb_sync(osb_ctx* ctx, int timeout_ms);
+
+/* Enables (1) or disables (0) CUDA-graph capture of osb_step. */
+int osb_set_graphs(osb_ctx* ctx, int enable);
+
+/* Selects the kernel tiling variant for the reconstruction kernels (autotuner hook);
+ * variant < 0 restores the default. */
+int osb_set_variant(osb_ctx* ctx, int variant);
+
+/* Returns the number of kernel launches the context has issued so far. */
+int osb_launch_count(osb_ctx* ctx, long long* out);
+
+/* Raw CUDA stream of the context (cudaStream_t), for event timing by the caller. */
+int osb_get_stream(osb_ctx* ctx, void** stream);
+
+/* Binding check: writes sizeof(osb_block_desc) and the byte offsets of size, bc, iface, gama,
+ * delta, q, rkold and metric into out[0..8] (n >= 9).  Needs no GPU. */
+int osb_desc_layout(long long* out, int n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,186 @@
+"""ctypes mirror of ``include/osb_gb300.h`` and loader of the CUDA library.
+
+The structure layout must match the C header field for field; ``tests/test_abi.py`` checks
+the size and offsets against the compiled library (``osb_desc_layout``).
+"""
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_NAME = "libosb_gb300.so"
+
+OSB_OK = 0
+OSB_EINVAL = -1
+OSB_ECUDA = -2
+OSB_ETIMEDOUT = -3
+OSB_ENOTSUP = -4
+OSB_ENAN = -5
+
+SCHEME_WENO5_JS = 1
+SCHEME_WENO5_Z = 2
+SCHEME_TENO5 = 3
+SCHEME_CENTRAL4 = 5
+
+AVG_SIMPLE = 0
+AVG_ROE = 1
+
+VISC_NONE = 0
+VISC_SUTHERLAND = 1
+VISC_CONSTANT = 2
+
+BC_PERIODIC = 0
+BC_ZERO_GRAD = 1
+BC_INTERFACE = 2
+
+PREC_FP64 = 0
+PREC_FP32_RESIDUAL = 1
+
+RK_LOW_STORAGE = 0
+RK_SBLI3 = 1
+
+RED_KE = 0
+RED_ENSTROPHY_DISS = 1
+RED_DILATATION_DISS = 2
+RED_RHO_SUM = 3
+RED_CFL_DT = 4
+RED_NAN_COUNT = 5
+
+SCHEME_NAMES = {"weno5_js": SCHEME_WENO5_JS, "weno5_z": SCHEME_WENO5_Z, "teno5": SCHEME_TENO5,
+                "central4": SCHEME_CENTRAL4}
+
+
+class Interface(ctypes.Structure):
+    _fields_ = [("block", ctypes.c_int32), ("dir", ctypes.c_int32), ("side", ctypes.c_int32),
+                ("flip", ctypes.c_int32)]
+
+
+class BlockDesc(ctypes.Structure):
+    _fields_ = [
+        ("ndim", ctypes.c_int32),
+        ("size", ctypes.c_int32 * 3),
+        ("halo", ctypes.c_int32),
+        ("scheme", ctypes.c_int32),
+        ("averaging", ctypes.c_int32),
+        ("viscous", ctypes.c_int32),
+        ("bc", (ctypes.c_int32 * 2) * 3),
+        ("bc_depth", (ctypes.c_int32 * 2) * 3),
+        ("iface", (Interface * 2) * 3),
+        ("gama", ctypes.c_double),
+        ("Minf", ctypes.c_double),
+        ("Re", ctypes.c_double),
+        ("Pr", ctypes.c_double),
+        ("mu_const", ctypes.c_double),
+        ("eps", ctypes.c_double),
+        ("teno_ct", ctypes.c_double),
+        ("shock_filter_control", ctypes.c_double),
+        ("delta", ctypes.c_double * 3),
+        ("q", ctypes.c_void_p * 5),
+        ("rkold", ctypes.c_void_p * 5),
+        ("metric", ctypes.c_void_p * 10),
+    ]
+
+
+def layout_signature():
+    """(sizeof, offsets...) of BlockDesc, compared with the C side in the tests."""
+    offs = [BlockDesc.size.offset, BlockDesc.bc.offset, BlockDesc.iface.offset, BlockDesc.gama.offset,
+            BlockDesc.delta.offset, BlockDesc.q.offset, BlockDesc.rkold.offset, BlockDesc.metric.offset]
+    return [ctypes.sizeof(BlockDesc)] + offs
+
+
+def make_desc(spec, q_ptrs, rk_ptrs, metric_ptrs=None):
+    """Fill a BlockDesc from a BlockSpec (see backend.py) and raw array addresses."""
+    d = BlockDesc()
+    d.ndim = spec.ndim
+    for i in range(3):
+        d.size[i] = spec.size[i] if i < spec.ndim else 1
+        d.delta[i] = spec.delta[i] if i < spec.ndim else 1.0
+    d.halo = spec.halo
+    d.scheme = spec.scheme
+    d.averaging = spec.averaging
+    d.viscous = spec.viscous
+    for i in range(3):
+        for s in range(2):
+            if i < spec.ndim:
+                d.bc[i][s] = spec.bc[i][s]
+                d.bc_depth[i][s] = spec.bc_depth[i][s]
+                if spec.iface is not None and spec.iface[i][s] is not None:
+                    blk, dr, sd, fl = spec.iface[i][s]
+                    d.iface[i][s] = Interface(blk, dr, sd, fl)
+    d.gama = spec.gama
+    d.Minf = spec.Minf
+    d.Re = spec.Re
+    d.Pr = spec.Pr
+    d.mu_const = spec.mu_const
+    d.eps = spec.eps
+    d.teno_ct = spec.teno_ct
+    d.shock_filter_control = spec.shock_filter_control
+    for v, p in enumerate(q_ptrs):
+        d.q[v] = p
+    for v, p in enumerate(rk_ptrs):
+        d.rkold[v] = p
+    if metric_ptrs:
+        for i, p in enumerate(metric_ptrs):
+            d.metric[i] = p
+    return d
+
+
+class OSBError(RuntimeError):
+    pass
+
+
+_lib = None
+
+
+def lib_path():
+    return os.path.join(HERE, LIB_NAME)
+
+
+def load_library():
+    """Load the in-tree CUDA library.  There is no fallback: a missing library is an error."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = lib_path()
+    if not os.path.exists(path):
+        raise OSBError("%s is not built; run `python -c 'import __graft_entry__ as g; g.build()'`" % path)
+    lib = ctypes.CDLL(path)
+    vp = ctypes.c_void_p
+    i32 = ctypes.c_int
+    lib.osb_version.restype = i32
+    lib.osb_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
+    lib.osb_ctx_create.argtypes = [i32, i32, ctypes.POINTER(vp)]
+    lib.osb_ctx_destroy.argtypes = [vp]
+    lib.osb_block_add.argtypes = [vp, ctypes.POINTER(BlockDesc), ctypes.POINTER(i32)]
+    lib.osb_set_rk.argtypes = [vp, i32, i32, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
+    lib.osb_step.argtypes = [vp, ctypes.c_double, i32]
+    lib.osb_stage.argtypes = [vp, i32, ctypes.c_double]
+    lib.osb_apply_bc.argtypes = [vp]
+    lib.osb_residual.argtypes = [vp, i32, ctypes.POINTER(vp)]
+    lib.osb_reduce.argtypes = [vp, i32, ctypes.POINTER(ctypes.c_double)]
+    lib.osb_sync.argtypes = [vp, i32]
+    lib.osb_set_graphs.argtypes = [vp, i32]
+    lib.osb_set_variant.argtypes = [vp, i32]
+    lib.osb_launch_count.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong)]
+    lib.osb_get_stream.argtypes = [vp, ctypes.POINTER(vp)]
+    lib.osb_desc_layout.argtypes = [ctypes.POINTER(ctypes.c_longlong), i32]
+    _lib = lib
+    return lib
+
+
+def last_error(lib):
+    buf = ctypes.create_string_buffer(1024)
+    lib.osb_last_error(buf, 1024)
+    return buf.value.decode(errors="replace")
+
+
+def check(lib, rc, what):
+    if rc != OSB_OK:
+        raise OSBError("%s failed (%d): %s" % (what, rc, last_error(lib)))
+    return rc
+
+
+# Exported symbols the header declares (checked by the CPU tests without a GPU).
+EXPORTED = ["osb_version", "osb_last_error", "osb_ctx_create", "osb_ctx_destroy", "osb_block_add",
+            "osb_set_rk", "osb_step", "osb_stage", "osb_apply_bc", "osb_residual", "osb_reduce",
+            "osb_sync", "osb_set_graphs", "osb_set_variant", "osb_launch_count", "osb_get_stream",
+            "osb_desc_layout"]

@@ -1,0 +1,84 @@
+"""Block specifications and OPS-layout array helpers.
+
+A ``BlockSpec`` is the Python form of ``osb_block_desc`` (include/osb_gb300.h) minus the
+array pointers.  ``opensbli_gb300.backend`` builds one per OpenSBLI ``SimulationBlock`` (by
+walking the reference's scheme / boundary / constant objects) or takes them directly from a
+caller that does not use the OpenSBLI front end.
+"""
+from dataclasses import dataclass, field
+from typing import List, Optional, Tuple
+
+import numpy as np
+
+from . import abi
+
+HALO = 5
+
+
+@dataclass
+class BlockSpec:
+    ndim: int
+    size: Tuple[int, ...]
+    scheme: int
+    averaging: int = abi.AVG_SIMPLE
+    viscous: int = abi.VISC_NONE
+    bc: List[List[int]] = None
+    bc_depth: List[List[int]] = None
+    iface: Optional[list] = None
+    gama: float = 1.4
+    Minf: float = 1.0
+    Re: float = 1.0
+    Pr: float = 0.71
+    mu_const: float = 1.0
+    eps: float = 1e-40
+    teno_ct: float = 1e-6
+    shock_filter_control: float = 1.0
+    delta: Tuple[float, ...] = (1.0, 1.0, 1.0)
+    halo: int = HALO
+
+    def __post_init__(self):
+        self.size = tuple(int(s) for s in self.size)
+        if self.bc is None:
+            self.bc = [[abi.BC_PERIODIC, abi.BC_PERIODIC] for _ in range(self.ndim)]
+        if self.bc_depth is None:
+            self.bc_depth = [[4, 4] for _ in range(self.ndim)]
+        if len(self.delta) < 3:
+            self.delta = tuple(self.delta) + (1.0,) * (3 - len(self.delta))
+
+    @property
+    def nvars(self):
+        return self.ndim + 2
+
+    @property
+    def shape(self):
+        """numpy shape of one OPS-layout array (slowest first)."""
+        ext = [self.size[d] + 2 * self.halo for d in range(self.ndim)]
+        return tuple(reversed(ext))
+
+    @property
+    def npoints(self):
+        n = 1
+        for d in range(self.ndim):
+            n *= self.size[d]
+        return n
+
+    def interior(self):
+        """Slice tuple selecting the interior of an OPS-layout array."""
+        h = self.halo
+        return tuple(slice(h, h + self.size[d]) for d in reversed(range(self.ndim)))
+
+    def grid_index(self, d):
+        """Global index (OPS ``idx``) of every allocated point along direction d, broadcastable."""
+        n = self.size[d] + 2 * self.halo
+        idx = np.arange(n) - self.halo
+        shp = [1] * self.ndim
+        shp[self.ndim - 1 - d] = n
+        return idx.reshape(shp)
+
+    def same_discretisation(self, other):
+        return (self.ndim, self.scheme, self.averaging, self.viscous) == (
+            other.ndim, other.scheme, other.averaging, other.viscous)
+
+
+def empty_state(spec):
+    return [np.zeros(spec.shape, dtype=np.float64) for _ in range(spec.nvars)]

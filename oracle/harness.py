@@ -1,0 +1,187 @@
+"""Python side of the oracle: builds and calls the C restatement (osb_oracle.c) and runs the
+reference's generated solvers compiled against ops_compat.h.
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and bench.py's CPU
+baseline, never by the opensbli_gb300 package.
+"""
+import ctypes
+import os
+import subprocess
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+BUILD = os.path.join(HERE, "_build")
+REF = os.path.join(HERE, "_ref")
+
+import sys  # noqa: E402
+
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+from opensbli_gb300 import abi  # noqa: E402
+from opensbli_gb300.spec import BlockSpec  # noqa: E402
+
+
+def oracle_lib_path():
+    return os.path.join(BUILD, "libosb_oracle.so")
+
+
+def build_oracle(force=False):
+    """Compile oracle/osb_oracle.c (gcc, no FMA contraction) into oracle/_build."""
+    os.makedirs(BUILD, exist_ok=True)
+    out = oracle_lib_path()
+    src = os.path.join(HERE, "osb_oracle.c")
+    if not force and os.path.exists(out) and os.path.getmtime(out) >= os.path.getmtime(src):
+        return out
+    cmd = ["gcc", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-fopenmp", "-o", out, src, "-lm"]
+    subprocess.check_call(cmd)
+    return out
+
+
+_olib = None
+
+
+def oracle():
+    global _olib
+    if _olib is None:
+        lib = ctypes.CDLL(build_oracle())
+        P = ctypes.POINTER
+        lib.oracle_residual.argtypes = [P(abi.BlockDesc), P(ctypes.c_void_p)]
+        lib.oracle_apply_bc.argtypes = [P(abi.BlockDesc), ctypes.c_int, ctypes.c_int]
+        lib.oracle_stage.argtypes = [P(abi.BlockDesc), ctypes.c_int, ctypes.c_int, P(ctypes.c_double),
+                                     P(ctypes.c_double), ctypes.c_int, ctypes.c_double]
+        lib.oracle_step.argtypes = [P(abi.BlockDesc), ctypes.c_int, ctypes.c_int, ctypes.c_int, P(ctypes.c_double),
+                                    P(ctypes.c_double), ctypes.c_double, ctypes.c_int]
+        lib.oracle_reduce.argtypes = [P(abi.BlockDesc), ctypes.c_int, ctypes.c_int, P(ctypes.c_double)]
+        _olib = lib
+    return _olib
+
+
+def _ptr(a):
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data
+
+
+class OracleBlocks:
+    """Host state of several blocks plus the C descriptors that point into it."""
+
+    def __init__(self, specs_states, rkold=None):
+        self.specs = [s for s, _ in specs_states]
+        self.q = [[np.ascontiguousarray(a, dtype=np.float64).copy() for a in st] for _, st in specs_states]
+        if rkold is None:
+            self.rk = [[np.zeros(s.shape) for _ in range(s.nvars)] for s in self.specs]
+        else:
+            self.rk = [[np.ascontiguousarray(a, dtype=np.float64).copy() for a in r] for r in rkold]
+        arr = (abi.BlockDesc * len(self.specs))()
+        for i, s in enumerate(self.specs):
+            arr[i] = abi.make_desc(s, [_ptr(a) for a in self.q[i]], [_ptr(a) for a in self.rk[i]])
+        self.desc = arr
+
+    def residual(self, ib=0):
+        s = self.specs[ib]
+        R = [np.zeros(s.shape) for _ in range(s.nvars)]
+        ptrs = (ctypes.c_void_p * 5)(*[_ptr(a) for a in R])
+        oracle().oracle_residual(ctypes.byref(self.desc[ib]), ptrs)
+        return R
+
+    def apply_bc(self):
+        oracle().oracle_apply_bc(self.desc, len(self.specs), 0)
+
+    def stage(self, rk_kind, A, B, stage, dt):
+        Aa = (ctypes.c_double * len(A))(*A)
+        Bb = (ctypes.c_double * len(B))(*B)
+        oracle().oracle_stage(self.desc, len(self.specs), rk_kind, Aa, Bb, stage, dt)
+
+    def step(self, rk_kind, A, B, dt, nsteps):
+        Aa = (ctypes.c_double * len(A))(*A)
+        Bb = (ctypes.c_double * len(B))(*B)
+        oracle().oracle_step(self.desc, len(self.specs), rk_kind, len(A), Aa, Bb, dt, nsteps)
+
+    def reduce(self, what):
+        out = ctypes.c_double()
+        oracle().oracle_reduce(self.desc, len(self.specs), what, ctypes.byref(out))
+        return out.value
+
+
+# ---------------------------------------------------------------------------------------
+# Reference runs (generated OPS C++ under oracle/_ref/<case>, compiled with ops_compat.h)
+
+def ref_available(case):
+    return os.path.exists(os.path.join(REF, case, "opensbli.cpp"))
+
+
+def build_ref(case, force=False):
+    d = os.path.join(REF, case)
+    exe = os.path.join(d, "ref_case")
+    src = os.path.join(d, "opensbli.cpp")
+    if not os.path.exists(src):
+        raise FileNotFoundError("reference sources for %s not generated (oracle/ref_generate.py)" % case)
+    if not force and os.path.exists(exe) and os.path.getmtime(exe) >= os.path.getmtime(src):
+        return exe
+    cmd = ["g++", "-std=c++17", "-O2", "-fopenmp", "-ffp-contract=off", "-I", HERE, "-I", d, src, "-o", exe]
+    subprocess.check_call(cmd)
+    return exe
+
+
+def read_dump(path):
+    hdr = np.fromfile(path, dtype=np.int32, count=8)
+    nd = int(hdr[0])
+    ext = [int(x) for x in hdr[1:1 + nd]]
+    data = np.fromfile(path, dtype=np.float64, offset=32)
+    return data.reshape(tuple(reversed(ext)))
+
+
+def write_dump(path, arr, halo=5):
+    nd = arr.ndim
+    ext = list(reversed(arr.shape)) + [1] * (3 - nd)
+    dm = [-halo] * nd + [0] * (3 - nd)
+    hdr = np.array([nd] + ext + dm + [0], dtype=np.int32)
+    with open(path, "wb") as f:
+        f.write(hdr.tobytes())
+        f.write(np.ascontiguousarray(arr, dtype=np.float64).tobytes())
+
+
+def run_ref(case, env=None, init=None, stop_after_rk=None, threads=None, timeout=3600):
+    """Run a generated reference case; returns {dat_name: array} dumped at the stop point.
+
+    init: optional {dat_name: array} loaded right before the time loop (OSB_INIT_DIR)."""
+    exe = build_ref(case)
+    with tempfile.TemporaryDirectory() as td:
+        e = dict(os.environ)
+        e["OSB_QUIET"] = "1"
+        e["OSB_DUMP_DIR"] = td
+        if env:
+            e.update({k: str(v) for k, v in env.items()})
+        if threads:
+            e["OSB_THREADS"] = str(threads)
+            e["OMP_NUM_THREADS"] = str(threads)
+        if stop_after_rk is not None:
+            e["OSB_STOP_AFTER_RK"] = str(stop_after_rk)
+        if init:
+            idir = os.path.join(td, "init")
+            os.makedirs(idir)
+            for k, v in init.items():
+                write_dump(os.path.join(idir, k + ".bin"), v)
+            e["OSB_INIT_DIR"] = idir
+        subprocess.run([exe], env=e, cwd=td, check=True, timeout=timeout, stdout=subprocess.DEVNULL)
+        out = {}
+        for fn in os.listdir(td):
+            if fn.endswith(".bin"):
+                out[fn[:-4]] = read_dump(os.path.join(td, fn))
+        red = os.path.join(td, "reductions.txt")
+        if os.path.exists(red):
+            out["_reductions"] = open(red).read()
+        return out
+
+
+def state_names(ndim):
+    return ["rho_B0"] + ["rhou%d_B0" % i for i in range(ndim)] + ["rhoE_B0"]
+
+
+def rel_err(a, b):
+    """max |a-b| / max |b| (relative to the field's scale)."""
+    scale = max(float(np.max(np.abs(b))), 1e-300)
+    return float(np.max(np.abs(a - b))) / scale

@@ -1,0 +1,727 @@
+/*
+ * osb_oracle.c -- CPU restatement of OpenSBLI's explicit residual-and-update path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the checker the GPU path is compared with; it is
+ * loaded by tests/, by __graft_entry__.smoke() and by bench.py's CPU-baseline leg, never by
+ * the product.  Parity of this restatement with the reference's own generated solver is
+ * pinned by tests/test_oracle_ref.py (reference OPS C++ compiled with oracle/ops_compat.h) and
+ * by the committed golden vectors under tests/golden/.
+ *
+ * It operates on HOST arrays described by the same osb_block_desc as the CUDA library
+ * (include/osb_gb300.h): OPS layout, x fastest, 5 halo points per used direction.
+ *
+ * Algorithm (each piece cites the reference file it restates):
+ *  - constituent relations u_i = rhou_i/rho, p, a, T, mu        (compressible_TGV.py:77-83)
+ *  - characteristic LLF flux at i+1/2 per direction:
+ *      averaging (simple / Roe)                                   (schemes/spatial/averaging.py:31-124)
+ *      eigensystem LEV/REV/eigenvalues (1D, 2D, 3D; k-vector)     (physical_models/euler_eigensystem.py:19-166)
+ *      CS = LEV*Q, CF = LEV*F on points i-2..i+3                  (shock_capturing.py:440-502)
+ *      lambda_w = sfc * max(|ev_w(i)|, |ev_w(i+1)|)               (shock_capturing.py:1000-1028)
+ *      f+/- = (CF +/- lambda*CS)/2                                (shock_capturing.py:979-998)
+ *      WENO5-JS / WENO5-Z / TENO5 reconstruction                  (weno.py:36-472, teno.py:59-477)
+ *      Fhat = REV * (recon(f+) + recon(f-))                       (shock_capturing.py:859-891)
+ *  - residual R = -sum_d (Fhat(i+1/2) - Fhat(i-1/2)) / Delta_d    (shock_capturing.py:23-36)
+ *  - StoreSome(4) viscous / heat-flux terms, central-4            (optimisations/StoreSome.py, scheme.py:174-258)
+ *  - skew-symmetric (Feiereisen) central convective terms         (physical_models/split_forms.py:111-145)
+ *  - low-storage RK3 (rk_LS.py:185-215) and SBLI RK3 (rk_sbli.py:138-154)
+ *  - periodic exchange (periodic.py:53-71, opsc.py:1026-1064), zero-gradient
+ *    (zero_gradient_outlet.py:11-23), block interfaces (multi_block.py:48-107)
+ *  - TGV reductions (compressible_TGV.py:176-206)
+ */
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#include "../include/osb_gb300.h"
+
+#define NVMAX 5
+
+typedef struct {
+  int nd, n[3], hx, hy, hz;
+  long ex, ey, ez;
+  long st[3]; /* stride per direction */
+} geom_t;
+
+static geom_t geom_of(const osb_block_desc* b) {
+  geom_t g;
+  g.nd = b->ndim;
+  for (int d = 0; d < 3; ++d) g.n[d] = d < b->ndim ? b->size[d] : 1;
+  g.hx = b->halo;
+  g.hy = b->ndim > 1 ? b->halo : 0;
+  g.hz = b->ndim > 2 ? b->halo : 0;
+  g.ex = g.n[0] + 2 * g.hx;
+  g.ey = g.n[1] + 2 * g.hy;
+  g.ez = g.n[2] + 2 * g.hz;
+  g.st[0] = 1;
+  g.st[1] = g.ex;
+  g.st[2] = g.ex * g.ey;
+  return g;
+}
+
+static inline long gid(const geom_t* g, int i, int j, int k) {
+  return (long)(i + g->hx) + g->ex * ((long)(j + g->hy) + g->ey * (long)(k + g->hz));
+}
+
+static inline long npts_alloc(const geom_t* g) { return g->ex * g->ey * g->ez; }
+
+/* ---- constituent relations ---------------------------------------------------------- */
+
+typedef struct {
+  double* u[3];
+  double *p, *a, *T, *mu;
+} cr_t;
+
+static void cr_alloc(cr_t* c, long n) {
+  for (int i = 0; i < 3; ++i) c->u[i] = (double*)calloc(n, sizeof(double));
+  c->p = (double*)calloc(n, sizeof(double));
+  c->a = (double*)calloc(n, sizeof(double));
+  c->T = (double*)calloc(n, sizeof(double));
+  c->mu = (double*)calloc(n, sizeof(double));
+}
+
+static void cr_free(cr_t* c) {
+  for (int i = 0; i < 3; ++i) free(c->u[i]);
+  free(c->p); free(c->a); free(c->T); free(c->mu);
+}
+
+/* Pointwise primitives over the whole allocated extent (halo points hold whatever the
+ * boundary treatment left there; points with rho == 0 are skipped). */
+static void cr_compute(const osb_block_desc* b, const geom_t* g, cr_t* c) {
+  const int nd = b->ndim, nv = nd + 2;
+  const double gm = b->gama;
+  long n = npts_alloc(g);
+  for (long id = 0; id < n; ++id) {
+    double rho = b->q[0][id];
+    if (rho == 0.0) continue;
+    double ke = 0.0;
+    for (int i = 0; i < nd; ++i) {
+      double ui = b->q[1 + i][id] / rho;
+      c->u[i][id] = ui;
+      ke += ui * ui;
+    }
+    double p = (gm - 1.0) * (b->q[nv - 1][id] - 0.5 * rho * ke);
+    c->p[id] = p;
+    c->a[id] = sqrt(gm * p / rho);
+    double T = b->Minf * b->Minf * gm * p / rho;
+    c->T[id] = T;
+    if (b->viscous == OSB_VISC_SUTHERLAND)
+      c->mu[id] = 1.4042 * T * sqrt(T) / (0.40417 + T);
+    else
+      c->mu[id] = b->mu_const;
+  }
+}
+
+/* ---- eigensystems (euler_eigensystem.py) --------------------------------------------- */
+
+/* Left/right eigenvectors at the averaged state for unit direction kt (|kt| = 1). */
+static void eigensystem(int nd, double gm, const double kt[3], double rho, const double u[3], double a,
+                        double L[NVMAX][NVMAX], double R[NVMAX][NVMAX]) {
+  const double g1 = gm - 1.0;
+  memset(L, 0, sizeof(double) * NVMAX * NVMAX);
+  memset(R, 0, sizeof(double) * NVMAX * NVMAX);
+  if (nd == 1) {
+    /* euler_eigensystem.py:85-99 with H = a^2/(gama-1) + u^2/2 */
+    double u0 = u[0];
+    double H = a * a / g1 + 0.5 * u0 * u0;
+    double den = 2.0 * H - u0 * u0;
+    L[0][0] = u0 * (2.0 * H + a * u0 - u0 * u0) / (2.0 * a * den);
+    L[0][1] = (-H - a * u0 + 0.5 * u0 * u0) / (a * den);
+    L[0][2] = 1.0 / den;
+    L[1][0] = 2.0 * (H - u0 * u0) / den;
+    L[1][1] = 2.0 * u0 / den;
+    L[1][2] = 2.0 / (-den);
+    L[2][0] = u0 * (-2.0 * H + a * u0 + u0 * u0) / (2.0 * a * den);
+    L[2][1] = (H - a * u0 - 0.5 * u0 * u0) / (a * den);
+    L[2][2] = 1.0 / den;
+    R[0][0] = 1.0; R[0][1] = 1.0; R[0][2] = 1.0;
+    R[1][0] = u0 - a; R[1][1] = u0; R[1][2] = u0 + a;
+    R[2][0] = H - u0 * a; R[2][1] = 0.5 * u0 * u0; R[2][2] = H + u0 * a;
+    return;
+  }
+  const double s2 = sqrt(2.0);
+  const double alpha = rho / (a * s2), bta = 1.0 / (rho * a * s2);
+  const double a2 = a * a;
+  if (nd == 2) {
+    /* euler_eigensystem.py:100-135 */
+    double k0 = kt[0], k1 = kt[1], u0 = u[0], u1 = u[1];
+    double phi = g1 * 0.5 * (u0 * u0 + u1 * u1);
+    double th = k0 * u0 + k1 * u1;
+    R[0][0] = 1.0; R[0][1] = 0.0; R[0][2] = alpha; R[0][3] = alpha;
+    R[1][0] = u0; R[1][1] = k1 * rho; R[1][2] = alpha * (u0 + k0 * a); R[1][3] = alpha * (u0 - k0 * a);
+    R[2][0] = u1; R[2][1] = -k0 * rho; R[2][2] = alpha * (u1 + k1 * a); R[2][3] = alpha * (u1 - k1 * a);
+    R[3][0] = phi / g1; R[3][1] = rho * (k1 * u0 - k0 * u1);
+    R[3][2] = alpha * ((phi + a2) / g1 + a * th); R[3][3] = alpha * ((phi + a2) / g1 - a * th);
+    L[0][0] = 1.0 - phi / a2; L[0][1] = g1 * u0 / a2; L[0][2] = g1 * u1 / a2; L[0][3] = -g1 / a2;
+    L[1][0] = -(k1 * u0 - k0 * u1) / rho; L[1][1] = k1 / rho; L[1][2] = -k0 / rho; L[1][3] = 0.0;
+    L[2][0] = bta * (phi - a * th); L[2][1] = bta * (k0 * a - g1 * u0); L[2][2] = bta * (k1 * a - g1 * u1);
+    L[2][3] = bta * g1;
+    L[3][0] = bta * (phi + a * th); L[3][1] = -bta * (k0 * a + g1 * u0); L[3][2] = -bta * (k1 * a + g1 * u1);
+    L[3][3] = bta * g1;
+    return;
+  }
+  /* nd == 3: euler_eigensystem.py:137-165 */
+  double k0 = kt[0], k1 = kt[1], k2 = kt[2], u0 = u[0], u1 = u[1], u2 = u[2];
+  double phi = g1 * 0.5 * (u0 * u0 + u1 * u1 + u2 * u2);
+  double th = k0 * u0 + k1 * u1 + k2 * u2;
+  R[0][0] = k0; R[0][1] = k1; R[0][2] = k2; R[0][3] = alpha; R[0][4] = alpha;
+  R[1][0] = k0 * u0; R[1][1] = k1 * u0 - k2 * rho; R[1][2] = k2 * u0 + k1 * rho;
+  R[1][3] = alpha * (u0 + k0 * a); R[1][4] = alpha * (u0 - k0 * a);
+  R[2][0] = k0 * u1 + k2 * rho; R[2][1] = k1 * u1; R[2][2] = k2 * u1 - k0 * rho;
+  R[2][3] = alpha * (u1 + k1 * a); R[2][4] = alpha * (u1 - k1 * a);
+  R[3][0] = k0 * u2 - k1 * rho; R[3][1] = k1 * u2 + k0 * rho; R[3][2] = k2 * u2;
+  R[3][3] = alpha * (u2 + k2 * a); R[3][4] = alpha * (u2 - k2 * a);
+  R[4][0] = k0 * phi / g1 + rho * (k2 * u1 - k1 * u2);
+  R[4][1] = k1 * phi / g1 + rho * (k0 * u2 - k2 * u0);
+  R[4][2] = k2 * phi / g1 + rho * (k1 * u0 - k0 * u1);
+  R[4][3] = alpha * ((phi + a2) / g1 + th * a);
+  R[4][4] = alpha * ((phi + a2) / g1 - th * a);
+  L[0][0] = k0 * (1.0 - phi / a2) - (k2 * u1 - k1 * u2) / rho;
+  L[0][1] = k0 * g1 * u0 / a2;
+  L[0][2] = k0 * g1 * u1 / a2 + k2 / rho;
+  L[0][3] = k0 * g1 * u2 / a2 - k1 / rho;
+  L[0][4] = -k0 * g1 / a2;
+  L[1][0] = k1 * (1.0 - phi / a2) - (k0 * u2 - k2 * u0) / rho;
+  L[1][1] = k1 * g1 * u0 / a2 - k2 / rho;
+  L[1][2] = k1 * g1 * u1 / a2;
+  L[1][3] = k1 * g1 * u2 / a2 + k0 / rho;
+  L[1][4] = -k1 * g1 / a2;
+  L[2][0] = k2 * (1.0 - phi / a2) - (k1 * u0 - k0 * u1) / rho;
+  L[2][1] = k2 * g1 * u0 / a2 + k1 / rho;
+  L[2][2] = k2 * g1 * u1 / a2 - k0 / rho;
+  L[2][3] = k2 * g1 * u2 / a2;
+  L[2][4] = -k2 * g1 / a2;
+  L[3][0] = bta * (phi - th * a);
+  L[3][1] = -bta * (g1 * u0 - k0 * a);
+  L[3][2] = -bta * (g1 * u1 - k1 * a);
+  L[3][3] = -bta * (g1 * u2 - k2 * a);
+  L[3][4] = bta * g1;
+  L[4][0] = bta * (phi + th * a);
+  L[4][1] = -bta * (g1 * u0 + k0 * a);
+  L[4][2] = -bta * (g1 * u1 + k1 * a);
+  L[4][3] = -bta * (g1 * u2 + k2 * a);
+  L[4][4] = bta * g1;
+}
+
+/* Pointwise eigenvalues: 1D diag(u-a, u, u+a); 2D diag(U,U,U+ak,U-ak);
+ * 3D diag(U,U,U,U+ak,U-ak) with U = k.u (euler_eigensystem.py:88,120,150). */
+static void point_ev(int nd, const double k[3], double kmag, const double u[3], double a, double ev[NVMAX]) {
+  if (nd == 1) {
+    ev[0] = u[0] - a; ev[1] = u[0]; ev[2] = u[0] + a;
+    return;
+  }
+  double U = 0.0;
+  for (int i = 0; i < nd; ++i) U += k[i] * u[i];
+  for (int i = 0; i < nd; ++i) ev[i] = U;
+  ev[nd] = U + a * kmag;
+  ev[nd + 1] = U - a * kmag;
+}
+
+/* ---- WENO / TENO reconstruction ------------------------------------------------------- */
+
+/* Upwind-biased fifth-order reconstruction at the right face of f[2] from f[0..4] =
+ * values at i-2..i+2.  The left-biased reconstruction of the reference (side -1) is this
+ * function applied to the mirrored stencil (weno.py:123-136, teno.py:96-107). */
+static double recon5(int scheme, const double* f, double teno_eps, double teno_ct) {
+  const double fm2 = f[0], fm1 = f[1], f0 = f[2], fp1 = f[3], fp2 = f[4];
+  if (scheme == OSB_SCHEME_TENO5) {
+    /* teno.py:96-107 (points), 109-123 (ENO), 128-140 (weights), 156-165 (beta), 197-217 */
+    double b0 = 0.25 * (fm1 - fp1) * (fm1 - fp1) + (13.0 / 12.0) * (fm1 - 2.0 * f0 + fp1) * (fm1 - 2.0 * f0 + fp1);
+    double b1 = 0.25 * (3.0 * f0 - 4.0 * fp1 + fp2) * (3.0 * f0 - 4.0 * fp1 + fp2) +
+                (13.0 / 12.0) * (f0 - 2.0 * fp1 + fp2) * (f0 - 2.0 * fp1 + fp2);
+    double b2 = 0.25 * (fm2 - 4.0 * fm1 + 3.0 * f0) * (fm2 - 4.0 * fm1 + 3.0 * f0) +
+                (13.0 / 12.0) * (fm2 - 2.0 * fm1 + f0) * (fm2 - 2.0 * fm1 + f0);
+    double tau = fabs(b0 - b2);
+    double t0 = 1.0 + tau / (teno_eps + b0), t1 = 1.0 + tau / (teno_eps + b1), t2 = 1.0 + tau / (teno_eps + b2);
+    double a0 = t0 * t0 * t0 * t0 * t0 * t0, a1 = t1 * t1 * t1 * t1 * t1 * t1, a2 = t2 * t2 * t2 * t2 * t2 * t2;
+    double inv = 1.0 / (a0 + a1 + a2);
+    double d0 = (a0 * inv < teno_ct) ? 0.0 : 1.0;
+    double d1 = (a1 * inv < teno_ct) ? 0.0 : 1.0;
+    double d2 = (a2 * inv < teno_ct) ? 0.0 : 1.0;
+    double w0 = (11.0 / 20.0) * d0, w1 = (4.0 / 10.0) * d1, w2 = (1.0 / 20.0) * d2;
+    double iw = 1.0 / (w0 + w1 + w2);
+    double e0 = -(1.0 / 6.0) * fm1 + (5.0 / 6.0) * f0 + (2.0 / 6.0) * fp1;
+    double e1 = (2.0 / 6.0) * f0 + (5.0 / 6.0) * fp1 - (1.0 / 6.0) * fp2;
+    double e2 = (2.0 / 6.0) * fm2 - (7.0 / 6.0) * fm1 + (11.0 / 6.0) * f0;
+    return (w0 * e0 + w1 * e1 + w2 * e2) * iw;
+  }
+  /* WENO5: weno.py:71-121 (ENO coefficients / optimal weights), 139-206 (JS smoothness) */
+  double b0 = (13.0 / 12.0) * (f0 - 2.0 * fp1 + fp2) * (f0 - 2.0 * fp1 + fp2) +
+              0.25 * (3.0 * f0 - 4.0 * fp1 + fp2) * (3.0 * f0 - 4.0 * fp1 + fp2);
+  double b1 = (13.0 / 12.0) * (fm1 - 2.0 * f0 + fp1) * (fm1 - 2.0 * f0 + fp1) + 0.25 * (fm1 - fp1) * (fm1 - fp1);
+  double b2 = (13.0 / 12.0) * (fm2 - 2.0 * fm1 + f0) * (fm2 - 2.0 * fm1 + f0) +
+              0.25 * (fm2 - 4.0 * fm1 + 3.0 * f0) * (fm2 - 4.0 * fm1 + 3.0 * f0);
+  double a0, a1, a2;
+  if (scheme == OSB_SCHEME_WENO5_Z) {
+    /* weno.py:290-345: tau = |b0 - b2|, alpha = d (1 + (tau/(eps+b))^2), eps = 1e-40 */
+    const double eps = 1.0e-40;
+    double tau = fabs(b0 - b2);
+    double r0 = tau / (eps + b0), r1 = tau / (eps + b1), r2 = tau / (eps + b2);
+    a0 = 0.3 * (1.0 + r0 * r0);
+    a1 = 0.6 * (1.0 + r1 * r1);
+    a2 = 0.1 * (1.0 + r2 * r2);
+  } else {
+    /* weno.py:348-376: alpha = d / (eps + b)^2, eps = 1e-6 */
+    const double eps = 1.0e-6;
+    a0 = 0.3 / ((eps + b0) * (eps + b0));
+    a1 = 0.6 / ((eps + b1) * (eps + b1));
+    a2 = 0.1 / ((eps + b2) * (eps + b2));
+  }
+  double inv = 1.0 / (a0 + a1 + a2);
+  double e0 = (1.0 / 3.0) * f0 + (5.0 / 6.0) * fp1 - (1.0 / 6.0) * fp2;
+  double e1 = -(1.0 / 6.0) * fm1 + (5.0 / 6.0) * f0 + (1.0 / 3.0) * fp1;
+  double e2 = (1.0 / 3.0) * fm2 - (7.0 / 6.0) * fm1 + (11.0 / 6.0) * f0;
+  return (a0 * inv) * e0 + (a1 * inv) * e1 + (a2 * inv) * e2;
+}
+
+/* ---- characteristic flux at one interface --------------------------------------------- */
+
+/* Interface i+1/2 along direction d of a Cartesian block: idc = linear index of point i. */
+static void char_flux_cart(const osb_block_desc* b, const geom_t* g, const cr_t* c, int d, long idc,
+                           double* fhat) {
+  const int nd = b->ndim, nv = nd + 2;
+  const long s = g->st[d];
+  const double gm = b->gama;
+  double kt[3] = {0.0, 0.0, 0.0};
+  kt[d] = 1.0;
+  long iL = idc, iR = idc + s;
+  /* averaged state (averaging.py) */
+  double rho_av, u_av[3] = {0, 0, 0}, a_av;
+  if (b->averaging == OSB_AVG_ROE) {
+    double rL = b->q[0][iL], rR = b->q[0][iR];
+    double sL = sqrt(rL), sR = sqrt(rR);
+    rho_av = sqrt(rL * rR);
+    double inv = 1.0 / (sL + sR);
+    double ke = 0.0;
+    for (int i = 0; i < nd; ++i) {
+      u_av[i] = (sL * c->u[i][iL] + sR * c->u[i][iR]) * inv;
+      ke += u_av[i] * u_av[i];
+    }
+    double HL = (b->q[nv - 1][iL] + c->p[iL]) / rL, HR = (b->q[nv - 1][iR] + c->p[iR]) / rR;
+    double H = (sL * HL + sR * HR) * inv;
+    a_av = sqrt((gm - 1.0) * (H - 0.5 * ke));
+  } else {
+    rho_av = 0.5 * (b->q[0][iL] + b->q[0][iR]);
+    for (int i = 0; i < nd; ++i) u_av[i] = 0.5 * (c->u[i][iL] + c->u[i][iR]);
+    a_av = 0.5 * (c->a[iL] + c->a[iR]);
+  }
+  double L[NVMAX][NVMAX], R[NVMAX][NVMAX];
+  eigensystem(nd, gm, kt, rho_av, u_av, a_av, L, R);
+  /* LLF wave speeds over points i, i+1 only */
+  double lam[NVMAX], evL[NVMAX], evR[NVMAX];
+  double uL[3] = {0, 0, 0}, uR[3] = {0, 0, 0};
+  for (int i = 0; i < nd; ++i) { uL[i] = c->u[i][iL]; uR[i] = c->u[i][iR]; }
+  point_ev(nd, kt, 1.0, uL, c->a[iL], evL);
+  point_ev(nd, kt, 1.0, uR, c->a[iR], evR);
+  for (int w = 0; w < nv; ++w) lam[w] = b->shock_filter_control * fmax(fabs(evL[w]), fabs(evR[w]));
+  /* characteristic projections on points i-2 .. i+3 */
+  double fp[NVMAX][6], fm[NVMAX][6];
+  for (int m = 0; m < 6; ++m) {
+    long id = idc + (long)(m - 2) * s;
+    double Q[NVMAX], F[NVMAX];
+    double ud = c->u[d][id], p = c->p[id];
+    for (int v = 0; v < nv; ++v) Q[v] = b->q[v][id];
+    F[0] = Q[1 + d];
+    for (int i = 0; i < nd; ++i) F[1 + i] = ud * Q[1 + i] + (i == d ? p : 0.0);
+    F[nv - 1] = ud * (Q[nv - 1] + p);
+    for (int w = 0; w < nv; ++w) {
+      double cs = 0.0, cf = 0.0;
+      for (int v = 0; v < nv; ++v) { cs += L[w][v] * Q[v]; cf += L[w][v] * F[v]; }
+      fp[w][m] = 0.5 * (cf + lam[w] * cs);
+      fm[w][m] = 0.5 * (cf - lam[w] * cs);
+    }
+  }
+  double rec[NVMAX];
+  for (int w = 0; w < nv; ++w) {
+    double mir[5] = {fm[w][5], fm[w][4], fm[w][3], fm[w][2], fm[w][1]};
+    rec[w] = recon5(b->scheme, &fp[w][0], b->eps, b->teno_ct) + recon5(b->scheme, mir, b->eps, b->teno_ct);
+  }
+  for (int v = 0; v < nv; ++v) {
+    double acc = 0.0;
+    for (int w = 0; w < nv; ++w) acc += R[v][w] * rec[w];
+    fhat[v] = acc;
+  }
+}
+
+/* ---- central 4th-order operators (scheme.py:83-87 finite_diff_weights) --------------- */
+
+static inline double d1c(const double* f, long id, long s, double invd) {
+  return ((1.0 / 12.0) * f[id - 2 * s] - (2.0 / 3.0) * f[id - s] + (2.0 / 3.0) * f[id + s] -
+          (1.0 / 12.0) * f[id + 2 * s]) * invd;
+}
+static inline double d2c(const double* f, long id, long s, double inv2d) {
+  return (-(1.0 / 12.0) * f[id - 2 * s] + (4.0 / 3.0) * f[id - s] - 2.5 * f[id] + (4.0 / 3.0) * f[id + s] -
+          (1.0 / 12.0) * f[id + 2 * s]) * inv2d;
+}
+static const double C1[5] = {1.0 / 12.0, -2.0 / 3.0, 0.0, 2.0 / 3.0, -1.0 / 12.0};
+/* d^2 f / dx_a dx_b (a != b) as the central-4 derivative along b of the central-4 derivative
+ * along a (StoreSome stores du/dx_a and differentiates it again, StoreSome.py:47-67). */
+static inline double dmix(const double* f, long id, long sa, long sb, double inva, double invb) {
+  double acc = 0.0;
+  for (int m = 0; m < 5; ++m) {
+    if (m == 2) continue;
+    long idb = id + (long)(m - 2) * sb;
+    acc += C1[m] * d1c(f, idb, sa, inva);
+  }
+  return acc * invb;
+}
+
+/* Viscous stress and heat-flux residual terms (generated "Viscous terms" kernel of the
+ * supersonic TGV, Residual1..4 += ...). */
+static void viscous_point(const osb_block_desc* b, const geom_t* g, const cr_t* c, long id, double* r) {
+  const int nd = b->ndim;
+  double inv[3], inv2[3];
+  for (int d = 0; d < nd; ++d) { inv[d] = 1.0 / b->delta[d]; inv2[d] = 1.0 / (b->delta[d] * b->delta[d]); }
+  double du[3][3], lap[3], dmu[3], dT[3], lapT = 0.0;
+  for (int i = 0; i < nd; ++i)
+    for (int j = 0; j < nd; ++j) du[i][j] = d1c(c->u[i], id, g->st[j], inv[j]);
+  double div = 0.0;
+  for (int i = 0; i < nd; ++i) div += du[i][i];
+  for (int j = 0; j < nd; ++j) {
+    dmu[j] = d1c(c->mu, id, g->st[j], inv[j]);
+    dT[j] = d1c(c->T, id, g->st[j], inv[j]);
+    lapT += d2c(c->T, id, g->st[j], inv2[j]);
+  }
+  /* lap_i = sum_j d2u_i/dx_j^2 + 1/3 d/dx_i (div u) */
+  for (int i = 0; i < nd; ++i) {
+    double s = 0.0;
+    for (int j = 0; j < nd; ++j) s += d2c(c->u[i], id, g->st[j], inv2[j]);
+    s += (1.0 / 3.0) * d2c(c->u[i], id, g->st[i], inv2[i]);
+    for (int j = 0; j < nd; ++j) {
+      if (j == i) continue;
+      int a = i < j ? i : j, bb = i < j ? j : i;
+      s += (1.0 / 3.0) * dmix(c->u[j], id, g->st[a], g->st[bb], inv[a], inv[bb]);
+    }
+    lap[i] = s;
+  }
+  const double invRe = 1.0 / b->Re;
+  const double mu = c->mu[id];
+  double tau[3][3];
+  for (int i = 0; i < nd; ++i)
+    for (int j = 0; j < nd; ++j) tau[i][j] = du[i][j] + du[j][i] - (i == j ? (2.0 / 3.0) * div : 0.0);
+  double e = 0.0;
+  for (int i = 0; i < nd; ++i) {
+    double m = 0.0;
+    for (int j = 0; j < nd; ++j) m += tau[i][j] * dmu[j];
+    m += mu * lap[i];
+    r[1 + i] += m * invRe;
+    double ui = c->u[i][id];
+    for (int j = 0; j < nd; ++j) e += mu * tau[i][j] * du[i][j] + ui * tau[i][j] * dmu[j];
+    e += mu * ui * lap[i];
+  }
+  double kheat = 1.0 / (b->Pr * b->Re * b->Minf * b->Minf * (b->gama - 1.0));
+  double h = mu * lapT;
+  for (int j = 0; j < nd; ++j) h += dT[j] * dmu[j];
+  r[nd + 1] += e * invRe + h * kheat;
+}
+
+/* Skew-symmetric (Feiereisen) central convective terms (split_forms.py:111-145, generated
+ * "Convective terms" kernel of the low-Mach TGV):
+ *   R_rho  -= sum_j D_j(rhou_j)
+ *   R_rhou_i -= D_i p + 1/2 sum_j [ D_j(rhou_i u_j) + u_i D_j(rhou_j) + rhou_j D_j(u_i) ]
+ *   R_rhoE -= sum_j [ D_j(p u_j) + 1/2 ( D_j(rhoE u_j) + rhou_j D_j(rhoE/rho) + (rhoE/rho) D_j(rhou_j) ) ]
+ * with D_j the central 4th-order first derivative. */
+static void central_conv_point(const osb_block_desc* b, const geom_t* g, const cr_t* c, const double* const* tmp,
+                               long id, double* r);
+
+/* ---- residual ------------------------------------------------------------------------- */
+
+typedef struct {
+  int nblocks;
+  osb_block_desc* blocks;
+} set_t;
+
+int oracle_residual(const osb_block_desc* b, double* const* Rout) {
+  geom_t g = geom_of(b);
+  const int nd = b->ndim, nv = nd + 2;
+  long n = npts_alloc(&g);
+  cr_t c;
+  cr_alloc(&c, n);
+  cr_compute(b, &g, &c);
+  for (int v = 0; v < nv; ++v)
+    for (int k = 0; k < g.n[2]; ++k)
+      for (int j = 0; j < g.n[1]; ++j)
+        for (int i = 0; i < g.n[0]; ++i) Rout[v][gid(&g, i, j, k)] = 0.0;
+  if (b->scheme == OSB_SCHEME_CENTRAL4) {
+    /* quadratic products needed by the split form (precomputed over the extent) */
+    double* tmp[1] = {NULL};
+    for (int k = 0; k < g.n[2]; ++k)
+      for (int j = 0; j < g.n[1]; ++j)
+        for (int i = 0; i < g.n[0]; ++i) {
+          long id = gid(&g, i, j, k);
+          double r[NVMAX] = {0, 0, 0, 0, 0};
+          central_conv_point(b, &g, &c, (const double* const*)tmp, id, r);
+          for (int v = 0; v < nv; ++v) Rout[v][id] = r[v];
+        }
+  } else {
+    /* interface fluxes per direction, stored like the generated wk arrays */
+    double* fh[3][NVMAX];
+    for (int d = 0; d < nd; ++d)
+      for (int v = 0; v < nv; ++v) fh[d][v] = (double*)calloc(n, sizeof(double));
+    for (int d = 0; d < nd; ++d) {
+      int lo[3] = {0, 0, 0};
+      lo[d] = -1;
+      for (int k = lo[2]; k < g.n[2]; ++k)
+        for (int j = lo[1]; j < g.n[1]; ++j)
+          for (int i = lo[0]; i < g.n[0]; ++i) {
+            long id = gid(&g, i, j, k);
+            double f[NVMAX];
+            char_flux_cart(b, &g, &c, d, id, f);
+            for (int v = 0; v < nv; ++v) fh[d][v][id] = f[v];
+          }
+    }
+    for (int k = 0; k < g.n[2]; ++k)
+      for (int j = 0; j < g.n[1]; ++j)
+        for (int i = 0; i < g.n[0]; ++i) {
+          long id = gid(&g, i, j, k);
+          for (int v = 0; v < nv; ++v) {
+            double r = 0.0;
+            for (int d = 0; d < nd; ++d) r -= (fh[d][v][id] - fh[d][v][id - g.st[d]]) * (1.0 / b->delta[d]);
+            Rout[v][id] = r;
+          }
+        }
+    for (int d = 0; d < nd; ++d)
+      for (int v = 0; v < nv; ++v) free(fh[d][v]);
+  }
+  if (b->viscous != OSB_VISC_NONE) {
+    for (int k = 0; k < g.n[2]; ++k)
+      for (int j = 0; j < g.n[1]; ++j)
+        for (int i = 0; i < g.n[0]; ++i) {
+          long id = gid(&g, i, j, k);
+          double r[NVMAX] = {0, 0, 0, 0, 0};
+          viscous_point(b, &g, &c, id, r);
+          for (int v = 1; v < nv; ++v) Rout[v][id] += r[v];
+        }
+  }
+  cr_free(&c);
+  return 0;
+}
+
+static void central_conv_point(const osb_block_desc* b, const geom_t* g, const cr_t* c, const double* const* tmp,
+                               long id, double* r) {
+  (void)tmp;
+  const int nd = b->ndim, nv = nd + 2;
+  const double* rho = b->q[0];
+  const double* rhoE = b->q[nv - 1];
+  double inv[3];
+  for (int d = 0; d < nd; ++d) inv[d] = 1.0 / b->delta[d];
+  double E = rhoE[id] / rho[id];
+  double divm = 0.0; /* sum_j d(rhou_j)/dx_j */
+  for (int j = 0; j < nd; ++j) divm += d1c(b->q[1 + j], id, g->st[j], inv[j]);
+  r[0] -= divm;
+  for (int i = 0; i < nd; ++i) {
+    double acc = d1c(c->p, id, g->st[i], inv[i]);
+    double adv = 0.0, conv = 0.0;
+    for (int j = 0; j < nd; ++j) {
+      long s = g->st[j];
+      double pr = 0.0;
+      for (int m = 0; m < 5; ++m) {
+        if (m == 2) continue;
+        long im = id + (long)(m - 2) * s;
+        pr += C1[m] * b->q[1 + i][im] * c->u[j][im];
+      }
+      conv += pr * inv[j];
+      adv += b->q[1 + j][id] * d1c(c->u[i], id, s, inv[j]);
+    }
+    acc += 0.5 * (conv + c->u[i][id] * divm + adv);
+    r[1 + i] -= acc;
+  }
+  double e = 0.0;
+  for (int j = 0; j < nd; ++j) {
+    long s = g->st[j];
+    double dpu = 0.0, dEu = 0.0, dE = 0.0;
+    for (int m = 0; m < 5; ++m) {
+      if (m == 2) continue;
+      long im = id + (long)(m - 2) * s;
+      dpu += C1[m] * c->p[im] * c->u[j][im];
+      dEu += C1[m] * rhoE[im] * c->u[j][im];
+      dE += C1[m] * rhoE[im] / rho[im];
+    }
+    e += dpu * inv[j] + 0.5 * (dEu * inv[j] + b->q[1 + j][id] * dE * inv[j]);
+  }
+  e += 0.5 * divm * E;
+  r[nv - 1] -= e;
+}
+
+/* ---- boundary conditions ---------------------------------------------------------------- */
+
+/* Periodic exchange of one face, as ops_halo_transfer of the generated bc_exchanges.h:
+ * side 0 copies interior [0, depth) to the high halo [N, N+depth); side 1 copies
+ * [N-depth, N) to [-depth, 0).  Transverse extent covers -depth..N+depth of the other used
+ * directions (periodic.py:53-71 with corners). */
+static void periodic_face(osb_block_desc* b, const geom_t* g, int d, int side, int depth) {
+  const int nd = b->ndim, nv = nd + 2;
+  int lo[3], hi[3];
+  for (int e = 0; e < 3; ++e) {
+    if (e < nd) { lo[e] = -depth; hi[e] = g->n[e] + depth; } else { lo[e] = 0; hi[e] = 1; }
+  }
+  int N = g->n[d];
+  int from0 = side == 0 ? 0 : N - depth;
+  int to0 = side == 0 ? N : -depth;
+  lo[d] = 0; hi[d] = depth;
+  for (int v = 0; v < nv; ++v)
+    for (int k = lo[2]; k < hi[2]; ++k)
+      for (int j = lo[1]; j < hi[1]; ++j)
+        for (int i = lo[0]; i < hi[0]; ++i) {
+          int src[3] = {i, j, k}, dst[3] = {i, j, k};
+          src[d] += from0; dst[d] += to0;
+          b->q[v][gid(g, dst[0], dst[1], dst[2])] = b->q[v][gid(g, src[0], src[1], src[2])];
+        }
+}
+
+/* Zero-gradient outlet: q(0) = q(1), q(-m) = q(m) for m = 1..depth at side 0 (mirrored at
+ * side 1), over the full transverse extent of the boundary plane (zero_gradient_outlet.py). */
+static void zero_grad_face(osb_block_desc* b, const geom_t* g, int d, int side, int depth) {
+  const int nd = b->ndim, nv = nd + 2;
+  int lo[3], hi[3];
+  for (int e = 0; e < 3; ++e) {
+    if (e < nd) { lo[e] = 0; hi[e] = g->n[e]; } else { lo[e] = 0; hi[e] = 1; }
+  }
+  int N = g->n[d];
+  int base = side == 0 ? 0 : N - 1;
+  int sgn = side == 0 ? 1 : -1;
+  lo[d] = base; hi[d] = base + 1;
+  for (int k = lo[2]; k < hi[2]; ++k)
+    for (int j = lo[1]; j < hi[1]; ++j)
+      for (int i = lo[0]; i < hi[0]; ++i) {
+        long id = gid(g, i, j, k);
+        long s = g->st[d] * sgn;
+        for (int v = 0; v < nv; ++v) {
+          double* q = b->q[v];
+          q[id] = q[id + s];
+          for (int m = 1; m <= depth; ++m) q[id - m * s] = q[id + m * s];
+        }
+      }
+}
+
+int oracle_apply_bc(osb_block_desc* blocks, int nblocks, int zero_grad_only) {
+  for (int ib = 0; ib < nblocks; ++ib) {
+    osb_block_desc* b = &blocks[ib];
+    geom_t g = geom_of(b);
+    for (int d = 0; d < b->ndim; ++d)
+      for (int side = 0; side < 2; ++side) {
+        int kind = b->bc[d][side];
+        int depth = b->bc_depth[d][side] > 0 ? b->bc_depth[d][side] : 4;
+        if (kind == OSB_BC_PERIODIC && !zero_grad_only) periodic_face(b, &g, d, side, depth);
+        if (kind == OSB_BC_ZERO_GRAD) zero_grad_face(b, &g, d, side, depth);
+      }
+  }
+  return 0;
+}
+
+/* ---- time integration ------------------------------------------------------------------ */
+
+static double* alloc_like(const geom_t* g) { return (double*)calloc(npts_alloc(g), sizeof(double)); }
+
+int oracle_stage(osb_block_desc* blocks, int nblocks, int rk_kind, const double* A, const double* B, int stage,
+                 double dt) {
+  /* residuals of every block first (all use the pre-stage state), then the updates */
+  double** R = (double**)calloc((size_t)nblocks * NVMAX, sizeof(double*));
+  for (int ib = 0; ib < nblocks; ++ib) {
+    geom_t g = geom_of(&blocks[ib]);
+    for (int v = 0; v < blocks[ib].ndim + 2; ++v) R[ib * NVMAX + v] = alloc_like(&g);
+    oracle_residual(&blocks[ib], &R[ib * NVMAX]);
+  }
+  for (int ib = 0; ib < nblocks; ++ib) {
+    osb_block_desc* b = &blocks[ib];
+    geom_t g = geom_of(b);
+    const int nv = b->ndim + 2;
+    for (int v = 0; v < nv; ++v) {
+      double* q = b->q[v];
+      double* o = b->rkold[v];
+      const double* r = R[ib * NVMAX + v];
+      for (int k = 0; k < g.n[2]; ++k)
+        for (int j = 0; j < g.n[1]; ++j)
+          for (int i = 0; i < g.n[0]; ++i) {
+            long id = gid(&g, i, j, k);
+            if (rk_kind == OSB_RK_LOW_STORAGE) {
+              o[id] = A[stage] * o[id] + dt * r[id];
+              q[id] = B[stage] * o[id] + q[id];
+            } else {
+              q[id] = A[stage] * dt * r[id] + o[id];
+              o[id] = B[stage] * dt * r[id] + o[id];
+            }
+          }
+      free(R[ib * NVMAX + v]);
+    }
+  }
+  free(R);
+  oracle_apply_bc(blocks, nblocks, 0);
+  return 0;
+}
+
+int oracle_step(osb_block_desc* blocks, int nblocks, int rk_kind, int nstages, const double* A, const double* B,
+                double dt, int nsteps) {
+  for (int it = 0; it < nsteps; ++it) {
+    oracle_apply_bc(blocks, nblocks, 0);
+    if (rk_kind == OSB_RK_SBLI3) {
+      for (int ib = 0; ib < nblocks; ++ib) {
+        osb_block_desc* b = &blocks[ib];
+        geom_t g = geom_of(b);
+        for (int v = 0; v < b->ndim + 2; ++v)
+          for (int k = 0; k < g.n[2]; ++k)
+            for (int j = 0; j < g.n[1]; ++j)
+              for (int i = 0; i < g.n[0]; ++i) {
+                long id = gid(&g, i, j, k);
+                b->rkold[v][id] = b->q[v][id];
+              }
+      }
+    }
+    for (int s = 0; s < nstages; ++s) oracle_stage(blocks, nblocks, rk_kind, A, B, s, dt);
+  }
+  return 0;
+}
+
+/* ---- reductions (compressible_TGV.py:176-206) -------------------------------------------- */
+
+int oracle_reduce(const osb_block_desc* blocks, int nblocks, int what, double* out) {
+  double acc = (what == OSB_RED_CFL_DT) ? 1e300 : 0.0;
+  for (int ib = 0; ib < nblocks; ++ib) {
+    const osb_block_desc* b = &blocks[ib];
+    geom_t g = geom_of(b);
+    const int nd = b->ndim, nv = nd + 2;
+    long n = npts_alloc(&g);
+    cr_t c;
+    cr_alloc(&c, n);
+    cr_compute(b, &g, &c);
+    double inv[3];
+    for (int d = 0; d < nd; ++d) inv[d] = 1.0 / b->delta[d];
+    for (int k = 0; k < g.n[2]; ++k)
+      for (int j = 0; j < g.n[1]; ++j)
+        for (int i = 0; i < g.n[0]; ++i) {
+          long id = gid(&g, i, j, k);
+          double rho = b->q[0][id];
+          if (what == OSB_RED_RHO_SUM) acc += rho;
+          else if (what == OSB_RED_KE) {
+            double s = 0.0;
+            for (int e = 0; e < nd; ++e) s += c.u[e][id] * c.u[e][id];
+            acc += 0.5 * s * rho;
+          } else if (what == OSB_RED_DILATATION_DISS) {
+            double div = 0.0;
+            for (int e = 0; e < nd; ++e) div += d1c(c.u[e], id, g.st[e], inv[e]);
+            acc += (4.0 / 3.0) * div * div * c.mu[id];
+          } else if (what == OSB_RED_ENSTROPHY_DISS) {
+            double w2 = 0.0;
+            if (nd == 3) {
+              double wx = d1c(c.u[2], id, g.st[1], inv[1]) - d1c(c.u[1], id, g.st[2], inv[2]);
+              double wy = d1c(c.u[0], id, g.st[2], inv[2]) - d1c(c.u[2], id, g.st[0], inv[0]);
+              double wz = d1c(c.u[1], id, g.st[0], inv[0]) - d1c(c.u[0], id, g.st[1], inv[1]);
+              w2 = wx * wx + wy * wy + wz * wz;
+            } else if (nd == 2) {
+              double wz = d1c(c.u[1], id, g.st[0], inv[0]) - d1c(c.u[0], id, g.st[1], inv[1]);
+              w2 = wz * wz;
+            }
+            acc += w2 * c.mu[id];
+          } else if (what == OSB_RED_CFL_DT) {
+            double s = 0.0;
+            for (int e = 0; e < nd; ++e) s += (fabs(c.u[e][id]) + c.a[id]) * inv[e];
+            double dtl = 1.0 / s;
+            if (dtl < acc) acc = dtl;
+          } else if (what == OSB_RED_NAN_COUNT) {
+            for (int v = 0; v < nv; ++v)
+              if (!isfinite(b->q[v][id])) acc += 1.0;
+          }
+        }
+    cr_free(&c);
+  }
+  *out = acc;
+  return 0;
+}

@@ -1,0 +1,354 @@
+"""Generate the reference solver sources (OPS C++) for each parity case.
+
+TEST INFRASTRUCTURE ONLY.  This script imports the upstream OpenSBLI generator from a
+read-only checkout (``--reference``, default ``/root/reference``), builds the problem
+definitions below with OpenSBLI's own Python API, and writes the generated OPS C++
+(``opensbli.cpp``, ``opensbliblock00_kernels.h``, ``defdec_data_set.h``, ...) into
+``oracle/_ref/<case>/``.  Those sources are then compiled against ``oracle/ops_compat.h``
+(see ``oracle/Makefile``) and their output pins the C restatement in ``oracle/osb_oracle.c``.
+Nothing under ``oracle/_ref`` is committed; it is regenerated from the reference.
+
+The generator pins SymPy 1.1 (``environment_and_run_scripts/InstallPython.sh:50``); only
+SymPy 1.14 exists here, so three runtime shims are applied (the checkout is not edited):
+
+1. ``Indexed.is_commutative`` becomes a per-instance settable property
+   (``opensbli/core/opensblifunctions.py:31`` assigns to it).
+2. Bare integer ``0`` "equations" (zero entries of the eigenvector matrices,
+   ``opensbli/schemes/spatial/shock_capturing.py:326-340``) are dropped before
+   ``OPSC.kernel_computation_opsc`` (``opensbli/code_generation/opsc.py:629``).
+3. ``GroupedPiecewise`` (``opensbli/core/opensbliobjects.py:672``) is printed as a C ternary
+   through the printer's ``_print_Piecewise``.
+
+Run parameters that OpenSBLI leaves as ``=Input`` are substituted by calls into
+``ops_compat.h`` (``osb_env_int`` / ``osb_env_double``) so one compiled case can be run at
+several sizes, time steps and step counts from the environment.
+"""
+import argparse
+import os
+import sys
+import contextlib
+
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def apply_compat_patches():
+    import sympy
+    from sympy import Indexed
+
+    base_prop = sympy.Basic.is_commutative
+
+    def _get(self):
+        d = getattr(self, "__dict__", None)
+        if d is not None and "_osb_is_comm" in d:
+            return d["_osb_is_comm"]
+        return base_prop.fget(self)
+
+    def _set(self, value):
+        self.__dict__["_osb_is_comm"] = value
+
+    Indexed.is_commutative = property(_get, _set)
+
+    from opensbli.code_generation import opsc as opsc_mod
+    from opensbli.core.opensbliobjects import GroupedPiecewise
+
+    orig_kc = opsc_mod.OPSC.kernel_computation_opsc
+
+    def kernel_computation_opsc(self, kernel):
+        kernel.equations = [e for e in kernel.equations
+                            if not (isinstance(e, int) or (hasattr(e, "is_zero") and e is sympy.S.Zero))]
+        return orig_kc(self, kernel)
+
+    opsc_mod.OPSC.kernel_computation_opsc = kernel_computation_opsc
+
+    printer = opsc_mod.OPSCCodePrinter
+
+    def _print_GroupedPiecewise(self, expr):
+        return printer._print_Piecewise(self, sympy.Piecewise(*expr.args))
+
+    printer._print_GroupedPiecewise = _print_GroupedPiecewise
+
+
+@contextlib.contextmanager
+def in_dir(path):
+    old = os.getcwd()
+    os.makedirs(path, exist_ok=True)
+    os.chdir(path)
+    try:
+        yield
+    finally:
+        os.chdir(old)
+
+
+def _env_params(ndim, defaults):
+    """Map OpenSBLI ``Input`` constants to environment-driven C expressions."""
+    names, values = [], []
+    for k, v in defaults.items():
+        names.append(k)
+        values.append(v)
+    return names, values
+
+
+def _euler_equations(ndim, scheme_tag, viscous=False):
+    """Conservative Euler / Navier-Stokes equations in OpenSBLI's Einstein notation
+    (the forms of ``apps/compressible_taylor_green_vortex/compressible_TGV.py:43-59``)."""
+    from opensbli import EinsteinEquation, SimulationEquations
+    sc1 = "**{'scheme':'%s'}" % scheme_tag
+    constants = ["Re", "Pr", "gama", "Minf", "SuthT", "RefT"]
+    eq = EinsteinEquation()
+    mass = "Eq(Der(rho,t), - Conservative(rhou_j,x_j,%s))" % sc1
+    if viscous:
+        momentum = "Eq(Der(rhou_i,t) , -Conservative(rhou_i*u_j + KD(_i,_j)*p,x_j , %s) + Der(tau_i_j,x_j) )" % sc1
+        energy = "Eq(Der(rhoE,t), - Conservative((p+rhoE)*u_j,x_j, %s) - Der(q_j,x_j) + Der(u_i*tau_i_j ,x_j) )" % sc1
+        subs = ["Eq(tau_i_j, (mu/Re)*(Der(u_i,x_j)+ Der(u_j,x_i) - (2/3)* KD(_i,_j)* Der(u_k,x_k)))",
+                "Eq(q_j, (-mu/((gama-1)*Minf*Minf*Pr*Re))*Der(T,x_j))"]
+    else:
+        momentum = "Eq(Der(rhou_i,t) , -Conservative(rhou_i*u_j + KD(_i,_j)*p,x_j , %s))" % sc1
+        energy = "Eq(Der(rhoE,t), - Conservative((p+rhoE)*u_j,x_j, %s))" % sc1
+        subs = []
+    sim = SimulationEquations()
+    for base in (mass, momentum, energy):
+        sim.add_equations(eq.expand(base, ndim, "x", subs, constants))
+    return sim
+
+
+def _constituents(ndim, viscous=False, sutherland=True, with_T=None):
+    from opensbli import EinsteinEquation, ConstituentRelations
+    eq = EinsteinEquation()
+    constants = ["Re", "Pr", "gama", "Minf", "SuthT", "RefT"]
+    rels = ["Eq(u_i, rhou_i/rho)",
+            "Eq(p, (gama-1)*(rhoE - (1/2)*rho*(KD(_i,_j)*u_i*u_j)))"]
+    if viscous or with_T:
+        rels.append("Eq(T, p*gama*Minf*Minf/(rho))")
+    rels.append("Eq(H, (rhoE + p) / rho)")
+    if viscous and sutherland:
+        rels.append("Eq(mu, (T**(1.5)*(1.4042)/(T+0.40417)))")
+    rels.append("Eq(a, (gama*p/rho)**0.5)")
+    cr = ConstituentRelations()
+    for r in rels:
+        cr.add_equations(eq.expand(r, ndim, "x", [], constants))
+    return cr
+
+
+def _finish(block, alg_kwargs, params):
+    from opensbli import TraditionalAlgorithmRK, SimulationDataType, Double, OPSC
+    from opensbli.utilities.helperfunctions import substitute_simulation_parameters
+    alg = TraditionalAlgorithmRK(block, **alg_kwargs)
+    SimulationDataType.set_datatype(Double)
+    OPSC(alg)
+    names, values = zip(*params.items())
+    substitute_simulation_parameters(list(names), list(values))
+
+
+def case_sod_weno5js():
+    """1D Sod, WENO5-JS characteristic LLF (simple average), zero-gradient ends, RK-LS3.
+    Problem definition follows ``apps/Sod_shock_tube/Sod_shock_tube.py`` with the
+    scheme/BC/time-stepper choices of the 1D Sod parity case."""
+    import copy
+    from opensbli import (SimulationBlock, GridBasedInitialisation, GridVariable, DataObject,
+                          parse_expr, SimpleAverage, LFWeno, RungeKuttaLS, ZeroGradientOutletBC)
+    ndim = 1
+    sim = _euler_equations(ndim, "Weno")
+    cr = _constituents(ndim)
+    block = SimulationBlock(ndim, block_number=0)
+    local_dict = {"block": block, "GridVariable": GridVariable, "DataObject": DataObject}
+    eqns = ["Eq(DataObject(x0), block.deltas[0]*block.grid_indexes[0])",
+            "Eq(GridVariable(u0), Piecewise((0.0, DataObject(x0) < 0.5),(0, True)))",
+            "Eq(GridVariable(p), Piecewise((1.0, DataObject(x0) < 0.5), (0.10, True)))",
+            "Eq(GridVariable(d), Piecewise((1.0, DataObject(x0) < 0.5), (0.125, True)))",
+            "Eq(DataObject(rho), d)", "Eq(DataObject(rhou0), d*u0)",
+            "Eq(DataObject(rhoE), p/(gama-1.0) + 0.5* d *(u0**2.0))"]
+    initial = GridBasedInitialisation()
+    initial.add_equations([parse_expr(e, local_dict=local_dict) for e in eqns])
+    schemes = {}
+    LF = LFWeno(order=5, formulation="JS", averaging=SimpleAverage([0, 1]), flux_type="LLF")
+    schemes[LF.name] = LF
+    rk = RungeKuttaLS(3)
+    schemes[rk.name] = rk
+    block.set_block_boundaries([ZeroGradientOutletBC(0, 0), ZeroGradientOutletBC(0, 1)])
+    block.set_equations([copy.deepcopy(cr), copy.deepcopy(sim), initial])
+    block.set_discretisation_schemes(schemes)
+    block.discretise()
+    params = {"gama": "1.4", "dt": 'osb_env_double("OSB_DT", 0.0002)',
+              "niter": 'osb_env_int("OSB_NITER", 1)', "block0np0": 'osb_env_int("OSB_NP0", 400)',
+              "Delta0block0": "1.0/(block0np0-1)"}
+    _finish(block, {}, params)
+
+
+def _tgv_block(ndim, conservative=True):
+    from opensbli import SimulationBlock, GridBasedInitialisation, GridVariable, DataObject, parse_expr
+    block = SimulationBlock(ndim, block_number=0, conservative=conservative)
+    local_dict = {"block": block, "GridVariable": GridVariable, "DataObject": DataObject}
+    eqns = ["Eq(GridVariable(x0), block.deltas[0]*block.grid_indexes[0])",
+            "Eq(GridVariable(x1), block.deltas[1]*block.grid_indexes[1])",
+            "Eq(GridVariable(x2), block.deltas[2]*block.grid_indexes[2])",
+            "Eq(GridVariable(u0),sin(x0)*cos(x1)*cos(x2))",
+            "Eq(GridVariable(u1),-cos(x0)*sin(x1)*cos(x2))",
+            "Eq(GridVariable(u2), 0.0)",
+            "Eq(GridVariable(p), 1.0/(gama*Minf*Minf)+ (1.0/16.0) * (cos(2.0*x0)+cos(2.0*x1))*(2.0 + cos(2.0*x2)))",
+            "Eq(GridVariable(r), gama*Minf*Minf*p)",
+            "Eq(DataObject(rho), r)", "Eq(DataObject(rhou0), r*u0)", "Eq(DataObject(rhou1), r*u1)",
+            "Eq(DataObject(rhou2), r*u2)",
+            "Eq(DataObject(rhoE), p/(gama-1) + 0.5* r *(u0**2+ u1**2 + u2**2))"]
+    initial = GridBasedInitialisation()
+    initial.add_equations([parse_expr(e, local_dict=local_dict) for e in eqns])
+    return block, initial
+
+
+def _tgv_params(minf, n, dt):
+    p = {"Re": "1600.0", "gama": "1.4", "Minf": str(minf), "Pr": "0.71",
+         "dt": 'osb_env_double("OSB_DT", %s)' % dt, "niter": 'osb_env_int("OSB_NITER", 1)'}
+    for d in range(3):
+        p["block0np%d" % d] = 'osb_env_int("OSB_NP%d", %d)' % (d, n)
+        p["Delta%dblock0" % d] = "2*M_PI/block0np%d" % d
+    p["TENO_CT"] = 'osb_env_double("OSB_TENO_CT", 1e-6)'
+    return p
+
+
+def case_tgv_shock(kind):
+    """3D supersonic TGV: characteristic LLF TENO5 (Roe average) or WENO5-Z (simple average)
+    plus 4th-order central viscous terms (StoreSome), periodic, RK-LS3
+    (``apps/compressible_taylor_green_vortex/compressible_TGV.py:43-242``)."""
+    import copy
+    from opensbli import (SimpleAverage, RoeAverage, LFWeno, LFTeno, StoreSome, RungeKuttaLS, PeriodicBC)
+    ndim = 3
+    tag = "Teno" if kind.startswith("teno") else "Weno"
+    sim = _euler_equations(ndim, tag, viscous=True)
+    cr = _constituents(ndim, viscous=True)
+    block, initial = _tgv_block(ndim)
+    schemes = {}
+    if kind == "teno5":
+        LF = LFTeno(order=5, averaging=RoeAverage([0, 1]), flux_type="LLF")
+    elif kind == "teno6":
+        LF = LFTeno(order=6, averaging=RoeAverage([0, 1]), flux_type="LLF")
+    else:
+        LF = LFWeno(order=5, formulation="Z", averaging=SimpleAverage([0, 1]), flux_type="LLF")
+    schemes[LF.name] = LF
+    cent = StoreSome(4, "u0 u1 u2")
+    schemes[cent.name] = cent
+    rk = RungeKuttaLS(3)
+    schemes[rk.name] = rk
+    block.set_discretisation_schemes(schemes)
+    bcs = []
+    for d in range(ndim):
+        bcs += [PeriodicBC(d, 0, halos=[-4, 4]), PeriodicBC(d, 1, halos=[-4, 4])]
+    block.set_block_boundaries(bcs)
+    block.set_equations([copy.deepcopy(cr), copy.deepcopy(sim), initial])
+    block.discretise()
+    _finish(block, {}, _tgv_params(1.25, 16, "0.001"))
+
+
+def case_tgv_central():
+    """3D low-Mach TGV, 4th-order central Feiereisen split form with constant viscosity,
+    periodic, RK-LS3 (``apps/taylor_green_vortex/taylor_green_vortex.py:20-140``; no DRP filter)."""
+    import copy
+    from opensbli import (NS_Split, SimulationEquations, ConstituentRelations, EinsteinEquation,
+                          StoreSome, RungeKuttaLS, PeriodicBC)
+    ndim = 3
+    constants = ["Re", "Pr", "gama", "Minf", "mu"]
+    NS = NS_Split("Feiereisen", ndim, constants, coordinate_symbol="x", conservative=True,
+                  viscosity="constant")
+    sim = SimulationEquations()
+    sim.add_equations(NS.mass)
+    sim.add_equations(NS.momentum)
+    sim.add_equations(NS.energy)
+    cr = ConstituentRelations()
+    ee = EinsteinEquation()
+    for r in ["Eq(u_i, rhou_i/rho)", "Eq(p, (gama-1)*(rhoE - (1/2)*rho*(KD(_i,_j)*u_i*u_j)))",
+              "Eq(T, p*gama*Minf*Minf/(rho))"]:
+        cr.add_equations(ee.expand(r, ndim, "x", [], constants))
+    block, initial = _tgv_block(ndim)
+    schemes = {}
+    cent = StoreSome(4, "u0 u1 u2")
+    schemes[cent.name] = cent
+    rk = RungeKuttaLS(3)
+    schemes[rk.name] = rk
+    block.set_discretisation_schemes(schemes)
+    bcs = []
+    for d in range(ndim):
+        bcs += [PeriodicBC(d, 0, full_depth=True), PeriodicBC(d, 1, full_depth=True)]
+    block.set_block_boundaries(bcs)
+    block.set_equations([copy.deepcopy(cr), copy.deepcopy(sim), initial])
+    block.discretise()
+    _finish(block, {}, _tgv_params(0.1, 16, "0.003385"))
+
+
+def case_kh_weno5z():
+    """2D Kelvin-Helmholtz, Euler, characteristic LLF WENO5-Z with Roe average, periodic,
+    classic 3-register SBLI RK3 (``apps/kelvin_helmholtz/kelvin_helmholtz.py:20-130``).  The
+    HDF5 random-number perturbation of that app is replaced by a deterministic sine mode whose
+    amplitude and phase come from the environment (the ensemble draws them from a seeded rng)."""
+    import copy
+    from opensbli import (SimulationBlock, GridBasedInitialisation, GridVariable, DataObject, parse_expr,
+                          RoeAverage, LFWeno, RungeKutta, PeriodicBC)
+    ndim = 2
+    sim = _euler_equations(ndim, "Weno")
+    cr = _constituents(ndim)
+    block = SimulationBlock(ndim, block_number=0)
+    local_dict = {"block": block, "GridVariable": GridVariable, "DataObject": DataObject}
+    eqns = ["Eq(GridVariable(x0), block.deltas[0]*block.grid_indexes[0])",
+            "Eq(GridVariable(x1), block.deltas[1]*block.grid_indexes[1])",
+            "Eq(GridVariable(d), Piecewise((2.0, Abs(x1 - 0.5) < 0.25), (1.0, True)))",
+            "Eq(GridVariable(u0), Piecewise((-0.5, Abs(x1 - 0.5) < 0.25), (0.5, True)))",
+            "Eq(GridVariable(u1), 0.01*khamp*sin(4.0*pi*x0 + khphase))",
+            "Eq(GridVariable(p), 2.5)",
+            "Eq(DataObject(rho), d)", "Eq(DataObject(rhou0), d*u0)", "Eq(DataObject(rhou1), d*u1)",
+            "Eq(DataObject(rhoE), p/(gama-1.0) + 0.5*d*(u0**2 + u1**2))"]
+    from opensbli.core.opensbliobjects import ConstantObject
+    local_dict["khamp"] = ConstantObject("khamp")
+    local_dict["khphase"] = ConstantObject("khphase")
+    initial = GridBasedInitialisation()
+    initial.add_equations([parse_expr(e, local_dict=local_dict) for e in eqns])
+    schemes = {}
+    LF = LFWeno(5, formulation="Z", averaging=RoeAverage([0, 1]))
+    schemes[LF.name] = LF
+    rk = RungeKutta(3)
+    schemes[rk.name] = rk
+    block.set_discretisation_schemes(schemes)
+    bcs = []
+    for d in range(ndim):
+        bcs += [PeriodicBC(d, 0), PeriodicBC(d, 1)]
+    block.set_block_boundaries(bcs)
+    block.set_equations([copy.deepcopy(cr), copy.deepcopy(sim), initial])
+    block.discretise()
+    params = {"gama": "1.4", "dt": 'osb_env_double("OSB_DT", 0.0002)', "niter": 'osb_env_int("OSB_NITER", 1)',
+              "khamp": 'osb_env_double("OSB_KHAMP", 1.0)', "khphase": 'osb_env_double("OSB_KHPHASE", 0.0)'}
+    for d in range(2):
+        params["block0np%d" % d] = 'osb_env_int("OSB_NP%d", 32)' % d
+        params["Delta%dblock0" % d] = "1.0/block0np%d" % d
+    params["block0np2"] = "1"
+    _finish(block, {}, params)
+
+
+CASES = {
+    "sod_weno5js": case_sod_weno5js,
+    "tgv_teno5": lambda: case_tgv_shock("teno5"),
+    "tgv_weno5z": lambda: case_tgv_shock("weno5z"),
+    "tgv_teno6": lambda: case_tgv_shock("teno6"),
+    "tgv_central": case_tgv_central,
+    "kh_weno5z": case_kh_weno5z,
+}
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("cases", nargs="*", default=sorted(CASES))
+    ap.add_argument("--reference", default=os.environ.get("OSB_REFERENCE", "/root/reference"))
+    ap.add_argument("--out", default=os.path.join(HERE, "_ref"))
+    args = ap.parse_args(argv)
+    if not os.path.isdir(os.path.join(args.reference, "opensbli")):
+        print("reference checkout not found at %s; nothing generated" % args.reference)
+        return 1
+    sys.path.insert(0, args.reference)
+    apply_compat_patches()
+    for name in args.cases:
+        out = os.path.join(args.out, name)
+        print("== generating %s -> %s" % (name, out), flush=True)
+        with in_dir(out):
+            with open(os.devnull, "w") as dn, contextlib.redirect_stdout(dn):
+                CASES[name]()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())
