@@ -1,0 +1,376 @@
+"""Benchmark: Mpt-RK-stage updates/s of the explicit residual + RK3 path on the 256^3
+supersonic Taylor-Green vortex (M=1.25, Re=1600, TENO5 with Roe averaging + 4th-order central
+viscous terms, periodic, low-storage RK3, dt from CFL 0.5 at t=0), FP32 residual with FP64
+state, next to the plain FP64 path, the reference's OPS solver on the host cores, and the
+kernel roofline.
+
+    python bench.py [--gpus 1] [--steps K] [--warmup W] [--impl reference]
+
+One "step" is one full RK step (3 stages) of the whole 256^3 block.  The state (5 x 266^3
+FP64, 752 MB) is larger than L2 (129 MB), so no explicit L2 flush is needed between steps.
+Replicas only for N > 1 (independent blocks per rank, no collective on the data path).
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import faulthandler
+
+import numpy as np
+
+faulthandler.enable()
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mpt-RK-stage updates/s (FP32 residual, FP64 state)"
+UNIT = "Mpt-RK-stage/s"
+NS = 256
+MINF = 1.25
+CFL = 0.5
+BYTES_PER_PT_STAGE = 160.0  # fully fused algorithmic traffic: q and RKold read+written once, FP64
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--size", type=int, default=NS)
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """Samples nvidia-smi SM clocks and throttle reasons while the timed region runs."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.QUERY,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        if self.thread is not None:
+            self.thread.join(timeout=2)
+        return self.summary()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for i, n in enumerate(names):
+                if r[5 + i].lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+def probe_fp(device):
+    import ctypes
+    path = os.path.join(ROOT, "opensbli_gb300", "libosb_probe.so")
+    if not os.path.exists(path):
+        return None, None
+    lib = ctypes.CDLL(path)
+    lib.osb_probe_fma.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+    out = {}
+    for name, fp64 in (("fp32", 0), ("fp64", 1)):
+        v = ctypes.c_double()
+        rc = lib.osb_probe_fma(device, fp64, ctypes.byref(v))
+        out[name] = v.value / 1e12 if rc == 0 else None
+    return out["fp32"], out["fp64"]
+
+
+def log(msg):
+    sys.stderr.write("[bench] %s\n" % msg)
+    sys.stderr.flush()
+
+
+def make_problem(n):
+    from opensbli_gb300 import abi, problems
+    spec, q = problems.tgv(n, minf=MINF, scheme=abi.SCHEME_TENO5, averaging=abi.AVG_ROE)
+    dt = problems.cfl_dt(spec, q, CFL)
+    return spec, q, dt
+
+
+def time_steps(solver, dt, steps):
+    import torch
+    stream = solver.stream()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    solver.step(dt, steps)
+    e1.record(stream)
+    solver.sync()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / 1e3
+
+
+def cpu_baseline(n, stages=2):
+    """The reference's generated OPS solver (oracle/_ref/tgv_teno5, -O3 OpenMP) on the host
+    cores: seconds per RK stage on the full n^3 workload, from its per-stage timestamps."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import harness
+    cores = os.cpu_count() or 1
+    if not harness.ref_available("tgv_teno5"):
+        return None
+    env = {"OSB_NP0": n, "OSB_NP1": n, "OSB_NP2": n, "OSB_NITER": 10}
+    r = harness.run_ref("tgv_teno5", env=env, stop_after_rk=stages, threads=cores, fast=True, dump=False)
+    t = r["_rk_times"]
+    per_stage = (t[-1] - t[1]) / (len(t) - 2) if len(t) > 2 else (t[-1] - t[0])
+    rate = n ** 3 / per_stage / 1e6
+    return {"value": rate, "unit": UNIT, "cores": cores, "kind": "reference",
+            "sample": "%d RK stages of the %d^3 TENO5 TGV with the reference's generated OPS solver (OpenMP, "
+                      "-O3); rate from stage %d..%d timestamps" % (stages, n, 2, stages)}
+
+
+def reference_arm(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import harness
+    if not harness.ref_available("tgv_teno5"):
+        print(json.dumps({"impl": "reference", "unavailable": "generated reference sources (oracle/_ref) missing"}))
+        return 0
+    n = args.size
+    cores = os.cpu_count() or 1
+    total = args.warmup + args.steps
+    env = {"OSB_NP0": n, "OSB_NP1": n, "OSB_NP2": n, "OSB_NITER": total + 2}
+    # one "step" of this arm = one RK stage of the n^3 workload (a bounded sample of a step)
+    r = harness.run_ref("tgv_teno5", env=env, stop_after_rk=total, threads=cores, fast=True, dump=False,
+                        timeout=3600)
+    t = r["_rk_times"]  # start, then one stamp per stage
+    timed = t[args.warmup + 1:]
+    secs = timed[-1] - t[args.warmup]
+    k = len(timed)
+    rate = n ** 3 * k / secs / 1e6
+    line = {"metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": 0, "steps": k, "warmup": args.warmup,
+            "ms_per_step": secs / k * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (analytic TGV initial condition)", "impl": "reference",
+            "config": {"workload": "supersonic TGV %d^3 TENO5-Roe + central-4 viscous, RK-LS3; one step = one RK "
+                                   "stage (bounded sample)" % n, "l2": "inputs larger than L2"},
+            "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores, "kind": "reference",
+                             "sample": "%d RK stages of the %d^3 workload" % (k, n)},
+            "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def our_arm(args):
+    import torch
+    from opensbli_gb300 import abi, problems
+    from opensbli_gb300.solver import Solver
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    n = args.size
+    spec, q, dt = make_problem(n)
+    pts = spec.npoints
+    s32 = Solver([(spec, q)], precision="fp32", rk="ls3", device=local, graphs=True)
+    s32.apply_bc()
+    s32.step(dt, args.warmup)
+    s32.sync()
+    log("warmup done")
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    launches0 = s32.launches()
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier()
+    secs = time_steps(s32, dt, args.steps)
+    barrier()
+    clk = clocks.stop()
+    launches = s32.launches() - launches0
+    log("timed done")
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([secs], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        secs = float(t.item())
+    value = world * pts * 3 * args.steps / secs / 1e6
+
+    # per-kernel times (CUDA events per launch on the context stream) over one more step
+    s32.timing(True)
+    s32.step(dt, 1)
+    rep = s32.timing_report()
+    s32.timing(False)
+    log("kernel timing done")
+    tot = sum(v[0] for v in rep.values()) or 1.0
+    dom = max(rep, key=lambda k: rep[k][0])
+    dom_ms = rep[dom][0] / max(rep[dom][1], 1)
+    alg_bytes = {"flux_x": 80.0, "flux_y": 120.0, "flux_z": 120.0, "central": 80.0, "rk_update": 200.0,
+                 "boundary": 0.0, "reduce": 40.0}[dom] * pts
+    hbm, peak_kind = measured_peaks()
+    achieved = alg_bytes / (dom_ms * 1e-3) / 1e9
+    step_bytes_gbs = BYTES_PER_PT_STAGE * pts * 3 * args.steps / secs / 1e9
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "traffic_%s_%d.json" % (dom, n))
+    if os.path.exists(tf):
+        traffic = json.load(open(tf)).get("bytes_per_launch")
+
+    fp32_peak, fp64_peak = probe_fp(local)
+    log("probe done")
+
+    # FP64 parity path on the same workload, and the FP32-vs-FP64 error after the same steps
+    fp64 = None
+    err = None
+    if not args.no_fp64 and rank == 0:
+        s64 = Solver([(spec, q)], precision="fp64", rk="ls3", device=local, graphs=True)
+        s64.apply_bc()
+        s64.step(dt, 1)
+        s64.sync()
+        n64 = 1
+        t64 = time_steps(s64, dt, n64)
+        fp64 = pts * 3 * n64 / t64 / 1e6
+        a = Solver([(spec, q)], precision="fp32", rk="ls3", device=local, graphs=True)
+        a.apply_bc()
+        a.step(dt, 1 + n64)
+        qa = a.state(0)
+        qb = s64.state(0)
+        sl = spec.interior()
+        err = {}
+        for v, name in ((0, "rho"), (4, "rhoE")):
+            d = qa[v][sl] - qb[v][sl]
+            err[name] = {"rel_l2": float(np.linalg.norm(d) / np.linalg.norm(qb[v][sl])),
+                         "rel_linf": float(np.max(np.abs(d)) / np.max(np.abs(qb[v][sl])))}
+        ke_a = a.reduce(abi.RED_KE)
+        ke_b = s64.reduce(abi.RED_KE)
+        err["ke_rel"] = abs(ke_a - ke_b) / abs(ke_b)
+        err["steps"] = 1 + n64
+        a.close()
+        s64.close()
+        log("fp64 done")
+
+    # end to end through the public API with pinned host buffers: H2D state, one RK step, D2H state
+    host_q = torch.from_numpy(np.stack(q)).pin_memory()
+    host_out = torch.empty_like(host_q).pin_memory()
+    stream = s32.stream()
+    e2e_steps = max(1, min(args.steps, 3))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        with torch.cuda.stream(stream):
+            s32.q[0].copy_(host_q, non_blocking=True)
+        s32.apply_bc()
+        s32.step(dt, 1)
+        with torch.cuda.stream(stream):
+            host_out.copy_(s32.q[0], non_blocking=True)
+        s32.sync()
+    t_e2e = time.perf_counter() - t0
+    e2e_value = world * pts * 3 * e2e_steps / t_e2e / 1e6
+    nbytes = host_q.numel() * 8
+    s32.close()
+    del host_q, host_out, s32
+    torch.cuda.synchronize()
+
+    cpu = None
+    log("e2e done")
+    if not args.no_cpu and rank == 0 and world == 1:
+        try:
+            cpu = cpu_baseline(n)
+        except Exception as ex:  # the baseline is reported, not required
+            cpu = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "reference",
+                   "sample": "failed: %s" % str(ex)[:200]}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": secs / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 residual / f64 state",
+            "data": "synthetic (analytic TGV initial condition, dt from CFL %.1f at t=0 = %.6g)" % (CFL, dt),
+            "config": {"workload": "supersonic TGV %d^3, M=%.2f, Re=1600, TENO5 (Roe) + central-4 viscous, "
+                                   "RK-LS3, periodic" % (n, MINF),
+                       "points": pts, "stages_per_step": 3,
+                       "l2": "inputs larger than L2 (752 MB state), no flush"},
+            "fp64": {"value": fp64, "unit": UNIT,
+                     "fp32_over_fp64": (value / world / fp64) if fp64 else None},
+            "error_vs_fp64": err,
+            "clocks": clk,
+            "gpu_launches": launches,
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                         "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
+                         "per_launch_ms": dom_ms, "share": rep[dom][0] / tot,
+                         "note": "the reconstruction sweeps are FP32-pipe bound; compute roof below"},
+            "compute": {"fp32_peak_tflops": fp32_peak, "fp64_peak_tflops": fp64_peak},
+            "step_hbm_gbs_at_160B": step_bytes_gbs,
+            "kernel_ms_per_step": {k: v[0] for k, v in rep.items()},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return reference_arm(args)
+    return our_arm(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

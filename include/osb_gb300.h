@@ -163,6 +163,16 @@ int osb_set_graphs(osb_ctx* ctx, int enable);
  * variant < 0 restores the default. */
 int osb_set_variant(osb_ctx* ctx, int variant);
 
+/* Per-kernel timing, the analogue of OPS's ops_timing_output (opsc.py:826-836): while enabled
+ * every kernel launch is bracketed by CUDA events on the context stream (CUDA graphs are
+ * bypassed). */
+int osb_timing(osb_ctx* ctx, int enable);
+
+/* Writes accumulated milliseconds and launch counts per kernel family (0 flux-x, 1 flux-y,
+ * 2 flux-z, 3 central, 4 RK update, 5 boundaries, 6 reductions) into ms[0..n) / launches[0..n)
+ * and resets them. */
+int osb_timing_report(osb_ctx* ctx, double* ms, long long* launches, int n);
+
 /* Returns the number of kernel launches the context has issued so far. */
 int osb_launch_count(osb_ctx* ctx, long long* out);
 

@@ -1,0 +1,311 @@
+"""Drop-in backend: takes the algorithm object an OpenSBLI problem script builds and runs it on
+the GB300 kernels, in place of the OPS C++ printer.
+
+Reference flow (e.g. apps/compressible_taylor_green_vortex/compressible_TGV.py:231-242):
+
+    alg = TraditionalAlgorithmRK(block)
+    SimulationDataType.set_datatype(Double)
+    OPSC(alg)                                   # writes OPS C++ (opsc.py:407-460)
+    substitute_simulation_parameters(names, values)
+
+GB300 flow:
+
+    alg = TraditionalAlgorithmRK(block)
+    be = GB300Backend(alg, dict(zip(names, values)), precision="fp64")
+    be.initialise()                             # the script's GridBasedInitialisation, on the host
+    be.run(niter)                               # the generated time loop, on the GPU
+
+The backend walks ``alg.blocks`` and each block's ``discretisation_schemes`` and
+``boundary_types`` and maps them onto ``osb_block_desc`` (include/osb_gb300.h).  Anything
+outside the supported path (other flux types, other boundary conditions, filters, HLLC ...)
+raises ``NotImplementedError``; there is no fallback.
+"""
+import math
+
+import numpy as np
+
+from . import abi
+from .spec import BlockSpec
+
+
+def _num(expr, params, env=None):
+    """Evaluate a simulation-parameter string such as '2*M_PI/block0np0'."""
+    if isinstance(expr, (int, float)):
+        return float(expr)
+    scope = {"M_PI": math.pi, "pi": math.pi, "sqrt": math.sqrt, "ceil": math.ceil}
+    if env:
+        scope.update(env)
+    for k, v in params.items():
+        if k not in scope and isinstance(v, (int, float)):
+            scope[k] = v
+    return float(eval(str(expr), {"__builtins__": {}}, scope))
+
+
+def resolve_parameters(params):
+    """Turn the {name: 'expression'} dict given to substitute_simulation_parameters
+    (utilities/helperfunctions.py:150-175) into numbers, resolving cross references."""
+    out = {}
+    pending = dict(params)
+    for _ in range(len(pending) + 1):
+        progressed = False
+        for k in list(pending):
+            try:
+                out[k] = _num(pending[k], out)
+                del pending[k]
+                progressed = True
+            except (NameError, TypeError, SyntaxError, ZeroDivisionError):
+                continue
+        if not pending or not progressed:
+            break
+    if pending:
+        raise ValueError("cannot evaluate simulation parameters: %s" % sorted(pending))
+    return out
+
+
+def _const_value(name, params, default=None):
+    if name in params:
+        return params[name]
+    from opensbli.core.kernel import ConstantsToDeclare
+    for c in ConstantsToDeclare.constants:
+        if str(c) == name and getattr(c, "value", None) is not None:
+            try:
+                return float(c.value)
+            except (TypeError, ValueError):
+                pass
+    if default is None:
+        raise ValueError("value of constant %s is not known; pass it in the parameters" % name)
+    return default
+
+
+def _scheme_of(block):
+    """(scheme, averaging, has_central) from block.discretisation_schemes."""
+    from opensbli.schemes.spatial.weno import LFWeno
+    from opensbli.schemes.spatial.teno import LFTeno
+    from opensbli.schemes.spatial.scheme import Central
+    from opensbli.schemes.spatial.averaging import RoeAverage
+    scheme, avg, central = None, abi.AVG_SIMPLE, False
+    for sch in block.discretisation_schemes.values():
+        if isinstance(sch, (LFWeno, LFTeno)):
+            if getattr(sch, "flux_type", "LLF") != "LLF":
+                raise NotImplementedError("only local Lax-Friedrichs splitting is supported (got %s)" % sch.flux_type)
+            if getattr(sch, "shock_filter", False):
+                raise NotImplementedError("WENO filter steps are not supported")
+            owner = getattr(sch.average, "__self__", None)
+            avg = abi.AVG_ROE if isinstance(owner, RoeAverage) else abi.AVG_SIMPLE
+            if isinstance(sch, LFTeno):
+                if sch.order != 5:
+                    raise NotImplementedError("TENO order %d is not supported (TENO5 only)" % sch.order)
+                scheme = abi.SCHEME_TENO5
+            else:
+                if sch.order != 5:
+                    raise NotImplementedError("WENO order %d is not supported (WENO5 only)" % sch.order)
+                rv = sch.reconstruction_classes[0]
+                is_z = any("Abs" in str(a) for a in rv.alpha_evaluated)
+                scheme = abi.SCHEME_WENO5_Z if is_z else abi.SCHEME_WENO5_JS
+        elif isinstance(sch, Central):
+            if sch.order != 4:
+                raise NotImplementedError("central order %d is not supported (4th order only)" % sch.order)
+            central = True
+    if scheme is None:
+        if not central:
+            raise NotImplementedError("no supported spatial scheme on block %s" % block.blockname)
+        scheme = abi.SCHEME_CENTRAL4
+    return scheme, avg, central
+
+
+def _viscosity_of(block):
+    """OSB_VISC_* from the block's equations: a Sutherland-type mu(T) constituent relation, a
+    constant viscosity (viscous terms without a mu relation), or inviscid."""
+    from opensbli.equation_types.opensbliequations import ConstituentRelations, SimulationEquations
+    from sympy import flatten
+    has_mu = False
+    viscous = False
+    for ec in block.list_of_equation_classes:
+        if isinstance(ec, ConstituentRelations):
+            for eq in flatten(ec.equations):
+                if str(eq.lhs).startswith("mu"):
+                    rhs = str(eq.rhs)
+                    if "1.4042" not in rhs or "0.40417" not in rhs:
+                        raise NotImplementedError("viscosity law %s is not supported" % rhs)
+                    has_mu = True
+        if isinstance(ec, SimulationEquations):
+            for eq in flatten(ec.equations):
+                if "Re" in str(eq.rhs):
+                    viscous = True
+    if not viscous:
+        return abi.VISC_NONE
+    return abi.VISC_SUTHERLAND if has_mu else abi.VISC_CONSTANT
+
+
+def _rk_of(block):
+    from opensbli.schemes.temporal.rk_LS import RungeKuttaLS
+    from opensbli.schemes.temporal.rk_sbli import RungeKutta
+    for sch in block.discretisation_schemes.values():
+        if isinstance(sch, (RungeKuttaLS, RungeKutta)):
+            sch.get_coefficients  # property: fills stage_coeffs / solution_coeffs (rk_LS.py:97-132)
+        if isinstance(sch, RungeKuttaLS):
+            A = [float(x) for x in sch.stage_coeffs.value]
+            B = [float(x) for x in sch.solution_coeffs.value]
+            return (abi.RK_LOW_STORAGE, A, B)
+        if isinstance(sch, RungeKutta):
+            A = [float(x) for x in sch.stage_coeffs.value]
+            B = [float(x) for x in sch.solution_coeffs.value]
+            return (abi.RK_SBLI3, A, B)
+    raise NotImplementedError("no supported time integrator (RungeKuttaLS / RungeKutta)")
+
+
+def _bcs_of(block, central_only):
+    from opensbli.core.boundary_conditions.periodic import PeriodicBC
+    from opensbli.core.boundary_conditions.zero_gradient_outlet import ZeroGradientOutletBC
+    bc = [[None, None] for _ in range(block.ndim)]
+    depth = [[4, 4] for _ in range(block.ndim)]
+    for d, pair in enumerate(block.boundary_types):
+        for side, b in enumerate(pair):
+            if isinstance(b, PeriodicBC):
+                bc[d][side] = abi.BC_PERIODIC
+                if b.halos is not None:
+                    depth[d][side] = abs(b.halos[side])
+                else:
+                    hv = b.get_halo_values(block)
+                    depth[d][side] = abs(hv[d][side])
+            elif isinstance(b, ZeroGradientOutletBC):
+                bc[d][side] = abi.BC_ZERO_GRAD
+                hv = b.get_halo_values(block)
+                depth[d][side] = abs(hv[d][side])
+            else:
+                raise NotImplementedError("boundary condition %s is not supported" % type(b).__name__)
+    return bc, depth
+
+
+def block_spec(block, params):
+    """BlockSpec of one OpenSBLI SimulationBlock."""
+    p = resolve_parameters(params)
+    b = block.blocknumber
+    nd = block.ndim
+    size = tuple(int(_const_value("block%dnp%d" % (b, d), p)) for d in range(nd))
+    delta = tuple(float(_const_value("Delta%dblock%d" % (d, b), p)) for d in range(nd))
+    scheme, avg, central = _scheme_of(block)
+    visc = _viscosity_of(block)
+    bc, depth = _bcs_of(block, scheme == abi.SCHEME_CENTRAL4)
+    return BlockSpec(ndim=nd, size=size, scheme=scheme, averaging=avg, viscous=visc, bc=bc, bc_depth=depth,
+                     gama=_const_value("gama", p), Minf=_const_value("Minf", p, 1.0), Re=_const_value("Re", p, 1.0),
+                     Pr=_const_value("Pr", p, 0.71), mu_const=1.0, eps=_const_value("eps", p, 1e-40),
+                     teno_ct=_const_value("TENO_CT", p, 1e-6),
+                     shock_filter_control=_const_value("shock_filter_control", p, 1.0), delta=delta)
+
+
+def initial_state(block, spec, params):
+    """Evaluate the block's GridBasedInitialisation equations on the host over every allocated
+    point (the generated initialisation kernel's range -halo..N+halo), returning the
+    conserved variables in OPS layout."""
+    import sympy
+    from sympy import flatten
+    from opensbli.initialisation.gridbasedinit import GridBasedInitialisation
+    from opensbli.core.opensbliobjects import DataObject, ConstantObject
+    from opensbli.core.grid import GridVariable
+    p = resolve_parameters(params)
+    inits = [ec for ec in block.list_of_equation_classes if isinstance(ec, GridBasedInitialisation)]
+    if not inits:
+        raise NotImplementedError("block has no GridBasedInitialisation")
+    env = {}
+    idx = [spec.grid_index(d).astype(np.float64) for d in range(spec.ndim)]
+    for d in range(spec.ndim):
+        env[str(block.grid_indexes[d])] = idx[d]
+        env[str(block.deltas[d])] = spec.delta[d]
+    for k, v in p.items():
+        env.setdefault(k, v)
+    mods = [{"Abs": np.abs, "Piecewise": _np_piecewise}, "numpy"]
+    values = {}
+    for eq in flatten([e.equations for e in inits]):
+        lhs, rhs = eq.lhs, eq.rhs
+        indexed = sorted(rhs.atoms(sympy.Indexed), key=str)
+        dummies = {ix: sympy.Symbol("_ix%d" % i) for i, ix in enumerate(indexed)}
+        body = rhs.subs(dummies)
+        back = {v: k for k, v in dummies.items()}
+        syms = sorted(body.free_symbols, key=str)
+        args = []
+        for sym in syms:
+            n = str(back.get(sym, sym))
+            key = n.split("[")[0]
+            base = key[:-3] if key.endswith("_B%d" % block.blocknumber) else key
+            for cand in (n, key, base):
+                if cand in values:
+                    args.append(values[cand])
+                    break
+                if cand in env:
+                    args.append(env[cand])
+                    break
+            else:
+                raise ValueError("initial condition uses unknown symbol %s" % n)
+        f = sympy.lambdify(syms, body, modules=mods)
+        val = f(*args)
+        name = str(lhs).split("[")[0]
+        name = name[:-3] if name.endswith("_B%d" % block.blocknumber) else name
+        values[name] = np.broadcast_to(np.asarray(val, dtype=np.float64), spec.shape)
+    order = ["rho"] + ["rhou%d" % d for d in range(spec.ndim)] + ["rhoE"]
+    return [np.ascontiguousarray(values[n]) for n in order]
+
+
+def _np_piecewise(*args):
+    out = None
+    for expr, cond in reversed(args):
+        if out is None:
+            out = np.asarray(expr, dtype=np.float64) * np.ones_like(np.asarray(cond, dtype=np.float64))
+        else:
+            out = np.where(cond, expr, out)
+    return out
+
+
+class GB300Backend:
+    """Stands in for OPSC(alg): owns the GPU state of every block of ``alg`` and runs its
+    time loop on the GB300 kernels."""
+
+    def __init__(self, alg, parameters, precision="fp64", device=0, graphs=True):
+        self.alg = alg
+        self.params = dict(parameters)
+        self.numbers = resolve_parameters(self.params)
+        self.blocks = list(alg.blocks)
+        self.specs = [block_spec(b, self.params) for b in self.blocks]
+        for s in self.specs[1:]:
+            if not s.same_discretisation(self.specs[0]):
+                raise NotImplementedError("blocks with different discretisations")
+        self.rk = _rk_of(self.blocks[0])
+        self.precision = precision
+        self.device = device
+        self.graphs = graphs
+        self.dt = float(self.numbers["dt"]) if "dt" in self.numbers else None
+        self.niter = int(self.numbers["niter"]) if "niter" in self.numbers else None
+        self.solver = None
+        self.iteration = 0
+
+    def initialise(self, states=None):
+        """Upload the initial state (default: the scripts' GridBasedInitialisation evaluated on the
+        host) and apply the boundary conditions once, as the generated code does before its time loop."""
+        from .solver import Solver
+        if states is None:
+            states = [initial_state(b, s, self.params) for b, s in zip(self.blocks, self.specs)]
+        self.solver = Solver(list(zip(self.specs, states)), precision=self.precision, rk=self.rk,
+                             device=self.device, graphs=self.graphs)
+        self.solver.apply_bc()
+        return self
+
+    def run(self, niter=None, dt=None):
+        niter = self.niter if niter is None else niter
+        dt = self.dt if dt is None else dt
+        if niter is None or dt is None:
+            raise ValueError("niter and dt must be given (as parameters or arguments)")
+        self.solver.step(dt, niter)
+        self.iteration += niter
+        self.solver.sync()
+        return self
+
+    def state(self, ib=0):
+        return self.solver.state(ib)
+
+    def reduce(self, what):
+        return self.solver.reduce(what)
+
+    def close(self):
+        if self.solver is not None:
+            self.solver.close()
+            self.solver = None

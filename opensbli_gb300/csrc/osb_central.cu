@@ -1,0 +1,41 @@
+// osb_central.cu -- launches of the central 4th-order convective / viscous kernel.
+#include "osb_internal.h"
+
+namespace osb {
+namespace {
+
+template <typename T, bool CONV, int VISC>
+int launch_central_t(osb_ctx* c, Block& bl, int first) {
+  using Fd = CentralFields<T, CONV, VISC>;
+  size_t smem = (size_t)Fd::N * CPTS * sizeof(T);
+  auto kern = k_central3d<T, CONV, VISC>;
+  OSB_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  CentralParams cp{bl.d.gama, bl.d.Minf, bl.d.Re, bl.d.Pr, bl.d.mu_const};
+  const BlockK& k = bl.k;
+  dim3 grid((k.n[0] + CX - 1) / CX, (k.n[1] + CY - 1) / CY, (k.n[2] + CZ - 1) / CZ);
+  timing_begin(c, FAM_CENTRAL);
+  kern<<<grid, CX * CY, smem, c->stream>>>(k, cp, first);
+  timing_end(c);
+  c->launches++;
+  return OSB_OK;
+}
+
+template <typename T>
+int launch_central(osb_ctx* c, Block& bl, bool conv, int first) {
+  const int visc = bl.d.viscous;
+  if (conv) {
+    if (visc == OSB_VISC_SUTHERLAND) return launch_central_t<T, true, 1>(c, bl, first);
+    if (visc == OSB_VISC_CONSTANT) return launch_central_t<T, true, 2>(c, bl, first);
+    return launch_central_t<T, true, 0>(c, bl, first);
+  }
+  if (visc == OSB_VISC_SUTHERLAND) return launch_central_t<T, false, 1>(c, bl, first);
+  if (visc == OSB_VISC_CONSTANT) return launch_central_t<T, false, 2>(c, bl, first);
+  return OSB_OK;
+}
+
+}  // namespace
+
+int central_f64(osb_ctx* c, Block& bl, bool conv, int first) { return launch_central<double>(c, bl, conv, first); }
+int central_f32(osb_ctx* c, Block& bl, bool conv, int first) { return launch_central<float>(c, bl, conv, first); }
+
+}  // namespace osb

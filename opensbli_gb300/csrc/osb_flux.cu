@@ -1,0 +1,75 @@
+// osb_flux.cu -- launches of the characteristic flux sweeps, compiled once per precision
+// (OSB_T) and dimension (OSB_ND) so the instantiations build in parallel.
+#include <algorithm>
+
+#include "osb_internal.h"
+
+#ifndef OSB_T
+#define OSB_T double
+#define OSB_ND 3
+#define OSB_NAME flux_f64_3d
+#endif
+
+namespace osb {
+namespace {
+
+template <typename T, int ND, int SCH, int AVG>
+int launch_flux(osb_ctx* c, Block& bl, const SchemeParams& sp) {
+  BlockK& k = bl.k;
+  cudaStream_t st = c->stream;
+  // x sweep (writes R)
+  {
+    constexpr int NV = ND + 2;
+    size_t smem = (size_t)XWARPS * NV * 32 * XPITCH * sizeof(T);
+    auto kern = k_flux_x<T, ND, SCH, AVG>;
+    OSB_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int nrows = k.n[1] * k.n[2];
+    dim3 grid((k.n[0] + XSEG - 1) / XSEG, (nrows + 32 * XWARPS - 1) / (32 * XWARPS));
+    timing_begin(c, FAM_FLUX_X);
+    kern<<<grid, 32 * XWARPS, smem, st>>>(k, sp, 1);
+    timing_end(c);
+    c->launches++;
+  }
+  // y, z sweeps (accumulate)
+  for (int D = 1; D < ND; ++D) {
+    int N = k.n[D];
+    long lines = (long)k.n[0] * (ND == 3 ? (D == 1 ? k.n[2] : k.n[1]) : 1);
+    long target = (long)c->sm_count * 512;
+    int nseg = (int)std::max(1L, std::min((long)(N / 16 > 0 ? N / 16 : 1), (target + lines - 1) / lines));
+    int seg = (N + nseg - 1) / nseg;
+    nseg = (N + seg - 1) / seg;
+    int other = ND == 3 ? (D == 1 ? k.n[2] : k.n[1]) : 1;
+    long gy = (long)other * nseg;
+    dim3 grid((k.n[0] + 127) / 128, (unsigned)std::min(gy, 65535L), (unsigned)((gy + 65534) / 65535));
+    if (grid.z > 1) return fail(OSB_ENOTSUP, "block too large for the sweep grid");
+    timing_begin(c, D == 1 ? FAM_FLUX_Y : FAM_FLUX_Z);
+    if (D == 1) k_flux_sweep<T, ND, 1, SCH, AVG><<<grid, 128, 0, st>>>(k, sp, seg, nseg, 0);
+    else if (ND == 3) k_flux_sweep<T, ND, (ND == 3 ? 2 : 1), SCH, AVG><<<grid, 128, 0, st>>>(k, sp, seg, nseg, 0);
+    timing_end(c);
+    c->launches++;
+  }
+  return OSB_OK;
+}
+
+template <typename T, int ND>
+int dispatch_flux_nd(osb_ctx* c, Block& bl, const SchemeParams& sp) {
+  const int sch = bl.d.scheme, avg = bl.d.averaging;
+  if (avg == OSB_AVG_ROE) {
+    if (sch == OSB_SCHEME_WENO5_JS) return launch_flux<T, ND, SCH_WENO5_JS, AVG_ROE>(c, bl, sp);
+    if (sch == OSB_SCHEME_WENO5_Z) return launch_flux<T, ND, SCH_WENO5_Z, AVG_ROE>(c, bl, sp);
+    if (sch == OSB_SCHEME_TENO5) return launch_flux<T, ND, SCH_TENO5, AVG_ROE>(c, bl, sp);
+  } else {
+    if (sch == OSB_SCHEME_WENO5_JS) return launch_flux<T, ND, SCH_WENO5_JS, AVG_SIMPLE>(c, bl, sp);
+    if (sch == OSB_SCHEME_WENO5_Z) return launch_flux<T, ND, SCH_WENO5_Z, AVG_SIMPLE>(c, bl, sp);
+    if (sch == OSB_SCHEME_TENO5) return launch_flux<T, ND, SCH_TENO5, AVG_SIMPLE>(c, bl, sp);
+  }
+  return fail(OSB_ENOTSUP, "unsupported scheme/averaging %d/%d", sch, avg);
+}
+
+
+
+}  // namespace
+
+int OSB_NAME(osb_ctx* c, Block& bl, const SchemeParams& sp) { return dispatch_flux_nd<OSB_T, OSB_ND>(c, bl, sp); }
+
+}  // namespace osb

@@ -1,0 +1,724 @@
+// osb_gb300.cu -- C ABI of the GB300 residual-and-update path (include/osb_gb300.h).
+//
+// A context owns one CUDA stream, the FP64 residual workspace of each block, the reduction
+// scratch and an optional CUDA graph of one RK step.  One RK stage is
+//     for each block: flux sweeps x, y, z (characteristic LLF WENO/TENO)  | central kernel
+//                     [+ central viscous kernel]
+//     for each block: RK update
+//     for each block: boundary conditions (periodic exchange / zero gradient / interfaces)
+// which is the kernel order of the generated stage loop
+// (apps/performance_benchmark/TENO6/opensbli.cpp:216-431) with the constituent-relation,
+// derivative and residual loops folded into the sweeps and the central kernel.
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "osb_internal.h"
+
+using namespace osb;
+
+namespace osb {
+
+// ---------------------------------------------------------------------------------------
+// RK update over the interior (rk_LS.py:204-215 / rk_sbli.py:138-145); counts non-finite
+// results into *bad.
+__global__ void k_rk(BlockK b, int nv, int kind, double A, double B, double dt, unsigned long long* bad) {
+  const long npts = (long)b.n[0] * b.n[1] * b.n[2];
+  unsigned long long nb = 0;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < npts; t += (long)gridDim.x * blockDim.x) {
+    int i = (int)(t % b.n[0]);
+    long r = t / b.n[0];
+    int j = (int)(r % b.n[1]);
+    int k = (int)(r / b.n[1]);
+    long id = lin(b, i, j, k);
+    for (int v = 0; v < nv; ++v) {
+      double r0 = b.R[v][id];
+      double o = b.rk[v][id];
+      double q = b.q[v][id];
+      if (kind == 0) {
+        o = A * o + dt * r0;
+        q = B * o + q;
+      } else {
+        q = A * dt * r0 + o;
+        o = B * dt * r0 + o;
+      }
+      b.rk[v][id] = o;
+      b.q[v][id] = q;
+      if (!isfinite(q)) ++nb;
+    }
+  }
+  if (nb) atomicAdd(bad, nb);
+}
+
+// SBLI RK3 "Save equations": old = q over the interior.
+__global__ void k_save(BlockK b, int nv) {
+  const long npts = (long)b.n[0] * b.n[1] * b.n[2];
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < npts; t += (long)gridDim.x * blockDim.x) {
+    int i = (int)(t % b.n[0]);
+    long r = t / b.n[0];
+    int j = (int)(r % b.n[1]);
+    int k = (int)(r / b.n[1]);
+    long id = lin(b, i, j, k);
+    for (int v = 0; v < nv; ++v) b.rk[v][id] = b.q[v][id];
+  }
+}
+
+// Periodic exchange of both faces of direction d (ExchangeSelf, periodic.py:53-71):
+// side 0 copies [0, depth) to [N, N+depth), side 1 copies [N-depth, N) to [-depth, 0); the
+// transverse ranges include -depth..N+depth of the other used directions (corners).
+__global__ void k_periodic(BlockK b, int nv, int d, int depth0, int depth1) {
+  int ext[3], lo[3];
+  for (int e = 0; e < 3; ++e) {
+    if (e < b.ndim && e != d) { ext[e] = b.n[e] + 2 * max(depth0, depth1); lo[e] = -max(depth0, depth1); }
+    else { ext[e] = 1; lo[e] = 0; }
+  }
+  const int dmax = max(depth0, depth1);
+  ext[d] = dmax;
+  const long per_side = (long)ext[0] * ext[1] * ext[2];
+  const long total = 2 * per_side * nv;
+  const int N = b.n[d];
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+    long r = t;
+    int c[3];
+    c[0] = (int)(r % ext[0]); r /= ext[0];
+    c[1] = (int)(r % ext[1]); r /= ext[1];
+    c[2] = (int)(r % ext[2]); r /= ext[2];
+    int side = (int)(r % 2);
+    int v = (int)(r / 2);
+    int depth = side == 0 ? depth0 : depth1;
+    if (c[d] >= depth) continue;
+    int src[3], dst[3];
+    bool skip = false;
+    for (int e = 0; e < 3; ++e) {
+      src[e] = c[e] + lo[e];
+      dst[e] = src[e];
+      if (e != d && e < b.ndim && (src[e] < -depth || src[e] >= b.n[e] + depth)) skip = true;
+    }
+    if (skip) continue;
+    if (side == 0) { src[d] = c[d]; dst[d] = N + c[d]; }
+    else { src[d] = N - depth + c[d]; dst[d] = -depth + c[d]; }
+    b.q[v][lin(b, dst[0], dst[1], dst[2])] = b.q[v][lin(b, src[0], src[1], src[2])];
+  }
+}
+
+// Zero-gradient outlet (zero_gradient_outlet.py:11-23 as generated): on side 0,
+// q(0) = q(1) then q(-m) = q(m) for m = 1..depth; mirrored on side 1.  Over the interior
+// extent of the other directions.
+__global__ void k_zero_grad(BlockK b, int nv, int d, int side, int depth) {
+  int ext[3];
+  for (int e = 0; e < 3; ++e) ext[e] = (e == d) ? 1 : b.n[e];
+  const long total = (long)ext[0] * ext[1] * ext[2];
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+    long r = t;
+    int c[3];
+    c[0] = (int)(r % ext[0]); r /= ext[0];
+    c[1] = (int)(r % ext[1]); r /= ext[1];
+    c[2] = (int)r;
+    c[d] = side == 0 ? 0 : b.n[d] - 1;
+    long id = lin(b, c[0], c[1], c[2]);
+    long s = b.st[d] * (side == 0 ? 1 : -1);
+    for (int v = 0; v < nv; ++v) {
+      double* q = b.q[v];
+      q[id] = q[id + s];
+      for (int m = 1; m <= depth; ++m) q[id - m * s] = q[id + m * s];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// Reductions (compressible_TGV.py:176-206 and the CFL / NaN checks), FP64.
+__device__ __forceinline__ double uval(const BlockK& b, int v, long id) { return b.q[v][id] / b.q[0][id]; }
+
+__device__ __forceinline__ double d1g(const BlockK& b, int v, long id, int d) {
+  long s = b.st[d];
+  return ((1.0 / 12.0) * uval(b, v, id - 2 * s) - (2.0 / 3.0) * uval(b, v, id - s) + (2.0 / 3.0) * uval(b, v, id + s) -
+          (1.0 / 12.0) * uval(b, v, id + 2 * s)) * b.invd[d];
+}
+
+struct RedParams {
+  int what, nv, visc;
+  double gama, Minf, mu_const;
+};
+
+__global__ void k_reduce(BlockK b, RedParams rp, double* partial, int slot) {
+  __shared__ double sh[256];
+  const long npts = (long)b.n[0] * b.n[1] * b.n[2];
+  const bool is_min = rp.what == 4;
+  double acc = is_min ? 1e300 : 0.0;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < npts; t += (long)gridDim.x * blockDim.x) {
+    int i = (int)(t % b.n[0]);
+    long r = t / b.n[0];
+    int j = (int)(r % b.n[1]);
+    int k = (int)(r / b.n[1]);
+    long id = lin(b, i, j, k);
+    const int nd = b.ndim;
+    double rho = b.q[0][id];
+    double u[3] = {0, 0, 0}, ke = 0.0;
+    for (int e = 0; e < nd; ++e) { u[e] = b.q[1 + e][id] / rho; ke += u[e] * u[e]; }
+    double p = (rp.gama - 1.0) * (b.q[rp.nv - 1][id] - 0.5 * rho * ke);
+    double mu = rp.mu_const;
+    if (rp.visc == 1) {
+      double T = rp.Minf * rp.Minf * rp.gama * p / rho;
+      mu = 1.4042 * T * sqrt(T) / (0.40417 + T);
+    }
+    double c = 0.0;
+    switch (rp.what) {
+      case 0: c = 0.5 * ke * rho; break;
+      case 1: {
+        double w2 = 0.0;
+        if (nd == 3) {
+          double wx = d1g(b, 3, id, 1) - d1g(b, 2, id, 2);
+          double wy = d1g(b, 1, id, 2) - d1g(b, 3, id, 0);
+          double wz = d1g(b, 2, id, 0) - d1g(b, 1, id, 1);
+          w2 = wx * wx + wy * wy + wz * wz;
+        } else if (nd == 2) {
+          double wz = d1g(b, 2, id, 0) - d1g(b, 1, id, 1);
+          w2 = wz * wz;
+        }
+        c = w2 * mu;
+        break;
+      }
+      case 2: {
+        double div = 0.0;
+        for (int e = 0; e < nd; ++e) div += d1g(b, 1 + e, id, e);
+        c = (4.0 / 3.0) * div * div * mu;
+        break;
+      }
+      case 3: c = rho; break;
+      case 4: {
+        double a = sqrt(rp.gama * p / rho);
+        double s = 0.0;
+        for (int e = 0; e < nd; ++e) s += (fabs(u[e]) + a) * b.invd[e];
+        c = 1.0 / s;
+        break;
+      }
+      case 5: {
+        for (int v = 0; v < rp.nv; ++v)
+          if (!isfinite(b.q[v][id])) c += 1.0;
+        break;
+      }
+    }
+    acc = is_min ? fmin(acc, c) : acc + c;
+  }
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) sh[threadIdx.x] = is_min ? fmin(sh[threadIdx.x], sh[threadIdx.x + s]) : sh[threadIdx.x] + sh[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[slot + blockIdx.x] = sh[0];
+}
+
+__global__ void k_reduce_final(const double* partial, int n, int is_min, double* out) {
+  __shared__ double sh[256];
+  double acc = is_min ? 1e300 : 0.0;
+  for (int t = threadIdx.x; t < n; t += blockDim.x) acc = is_min ? fmin(acc, partial[t]) : acc + partial[t];
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) sh[threadIdx.x] = is_min ? fmin(sh[threadIdx.x], sh[threadIdx.x + s]) : sh[threadIdx.x] + sh[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = sh[0];
+}
+
+
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+}  // namespace osb
+
+namespace osb {
+
+void timing_begin(osb_ctx* c, int fam) {
+  if (!c->timing) return;
+  TimedEvent te;
+  te.fam = fam;
+  for (int i = 0; i < 2; ++i) {
+    cudaEvent_t e;
+    if (!c->event_pool.empty()) {
+      e = c->event_pool.back();
+      c->event_pool.pop_back();
+    } else {
+      cudaEventCreate(&e);
+    }
+    (i == 0 ? te.a : te.b) = e;
+  }
+  cudaEventRecord(te.a, c->stream);
+  c->events.push_back(te);
+}
+
+void timing_end(osb_ctx* c) {
+  if (!c->timing || c->events.empty()) return;
+  cudaEventRecord(c->events.back().b, c->stream);
+}
+
+}  // namespace osb
+
+namespace {
+
+// Folds completed timed launches into the per-family totals.
+int timing_collect(osb_ctx* c) {
+  if (c->events.empty()) return OSB_OK;
+  OSB_CK(cudaStreamSynchronize(c->stream));
+  for (auto& te : c->events) {
+    float ms = 0.f;
+    OSB_CK(cudaEventElapsedTime(&ms, te.a, te.b));
+    c->fam_ms[te.fam] += ms;
+    c->fam_count[te.fam] += 1;
+    c->event_pool.push_back(te.a);
+    c->event_pool.push_back(te.b);
+  }
+  c->events.clear();
+  return OSB_OK;
+}
+
+template <typename T>
+int residual_t(osb_ctx* c, Block& bl) {
+  SchemeParams sp{bl.d.gama, bl.d.eps, bl.d.teno_ct, bl.d.shock_filter_control, 1e-12};
+  int rc;
+  if (bl.d.scheme == OSB_SCHEME_CENTRAL4) {
+    if (bl.d.ndim != 3) return fail(OSB_ENOTSUP, "central scheme implemented for 3D blocks");
+    rc = sizeof(T) == 4 ? central_f32(c, bl, true, 1) : central_f64(c, bl, true, 1);
+  } else {
+    const int nd = bl.d.ndim;
+    if (sizeof(T) == 4) rc = nd == 1 ? flux_f32_1d(c, bl, sp) : nd == 2 ? flux_f32_2d(c, bl, sp) : flux_f32_3d(c, bl, sp);
+    else rc = nd == 1 ? flux_f64_1d(c, bl, sp) : nd == 2 ? flux_f64_2d(c, bl, sp) : flux_f64_3d(c, bl, sp);
+    if (rc == OSB_OK && bl.d.viscous != OSB_VISC_NONE) {
+      if (bl.d.ndim != 3) return fail(OSB_ENOTSUP, "viscous terms implemented for 3D blocks");
+      rc = sizeof(T) == 4 ? central_f32(c, bl, false, 0) : central_f64(c, bl, false, 0);
+    }
+  }
+  return rc;
+}
+
+int residual(osb_ctx* c, Block& bl) {
+  return c->prec == OSB_PREC_FP32_RESIDUAL ? residual_t<float>(c, bl) : residual_t<double>(c, bl);
+}
+
+int grid_for(osb_ctx* c, long n, int threads) {
+  long g = (n + threads - 1) / threads;
+  long cap = (long)c->sm_count * 8;
+  return (int)std::max(1L, std::min(g, cap));
+}
+
+int apply_bc(osb_ctx* c) {
+  for (size_t ib = 0; ib < c->blocks.size(); ++ib) {
+    Block& bl = c->blocks[ib];
+    const int nv = bl.d.ndim + 2;
+    for (int d = 0; d < bl.d.ndim; ++d) {
+      int b0 = bl.d.bc[d][0], b1 = bl.d.bc[d][1];
+      int dep0 = bl.d.bc_depth[d][0] > 0 ? bl.d.bc_depth[d][0] : 4;
+      int dep1 = bl.d.bc_depth[d][1] > 0 ? bl.d.bc_depth[d][1] : 4;
+      if (b0 == OSB_BC_PERIODIC && b1 == OSB_BC_PERIODIC) {
+        long tr = 1;
+        for (int e = 0; e < bl.d.ndim; ++e)
+          if (e != d) tr *= bl.k.n[e] + 2 * std::max(dep0, dep1);
+        long total = 2L * std::max(dep0, dep1) * tr * nv;
+        timing_begin(c, FAM_BC);
+        k_periodic<<<grid_for(c, total, 256), 256, 0, c->stream>>>(bl.k, nv, d, dep0, dep1);
+        timing_end(c);
+        c->launches++;
+      } else {
+        for (int side = 0; side < 2; ++side) {
+          int kind = bl.d.bc[d][side];
+          if (kind == OSB_BC_ZERO_GRAD) {
+            long tr = 1;
+            for (int e = 0; e < bl.d.ndim; ++e)
+              if (e != d) tr *= bl.k.n[e];
+            timing_begin(c, FAM_BC);
+            k_zero_grad<<<grid_for(c, tr, 128), 128, 0, c->stream>>>(bl.k, nv, d, side, side ? dep1 : dep0);
+            timing_end(c);
+            c->launches++;
+          } else if (kind == OSB_BC_PERIODIC) {
+            return fail(OSB_EINVAL, "periodic boundary on one side only (block %zu dir %d)", ib, d);
+          } else if (kind == OSB_BC_INTERFACE) {
+            return fail(OSB_ENOTSUP, "block interfaces are not supported by this build");
+          }
+        }
+      }
+    }
+  }
+  return OSB_OK;
+}
+
+int stage(osb_ctx* c, int s, double dt) {
+  for (auto& bl : c->blocks) {
+    int rc = residual(c, bl);
+    if (rc) return rc;
+  }
+  for (auto& bl : c->blocks) {
+    long n = (long)bl.k.n[0] * bl.k.n[1] * bl.k.n[2];
+    timing_begin(c, FAM_RK);
+    k_rk<<<grid_for(c, n, 256), 256, 0, c->stream>>>(bl.k, bl.d.ndim + 2, c->rk_kind == OSB_RK_LOW_STORAGE ? 0 : 1,
+                                                      c->A[s], c->B[s], dt, c->bad);
+    timing_end(c);
+    c->launches++;
+  }
+  return apply_bc(c);
+}
+
+int one_step(osb_ctx* c, double dt) {
+  int rc = apply_bc(c);
+  if (rc) return rc;
+  if (c->rk_kind == OSB_RK_SBLI3) {
+    for (auto& bl : c->blocks) {
+      long n = (long)bl.k.n[0] * bl.k.n[1] * bl.k.n[2];
+      k_save<<<grid_for(c, n, 256), 256, 0, c->stream>>>(bl.k, bl.d.ndim + 2);
+      c->launches++;
+    }
+  }
+  for (int s = 0; s < c->nst; ++s) {
+    rc = stage(c, s, dt);
+    if (rc) return rc;
+  }
+  return OSB_OK;
+}
+
+void drop_graph(osb_ctx* c) {
+  if (c->gexec) {
+    cudaGraphExecDestroy(c->gexec);
+    c->gexec = nullptr;
+  }
+}
+
+bool check_desc(const osb_block_desc* d, std::string& why) {
+  if (d->ndim < 1 || d->ndim > 3) { why = "ndim must be 1, 2 or 3"; return false; }
+  if (d->halo != 5) { why = "halo must be 5 (OPS layout)"; return false; }
+  for (int i = 0; i < d->ndim; ++i)
+    if (d->size[i] < 6) { why = "every used direction needs at least 6 points"; return false; }
+  for (int i = d->ndim; i < 3; ++i)
+    if (d->size[i] != 1) { why = "unused directions must have size 1"; return false; }
+  if (!(d->scheme == OSB_SCHEME_WENO5_JS || d->scheme == OSB_SCHEME_WENO5_Z || d->scheme == OSB_SCHEME_TENO5 ||
+        d->scheme == OSB_SCHEME_CENTRAL4)) { why = "unknown scheme"; return false; }
+  if (d->averaging != OSB_AVG_SIMPLE && d->averaging != OSB_AVG_ROE) { why = "unknown averaging"; return false; }
+  for (int v = 0; v < d->ndim + 2; ++v)
+    if (!d->q[v] || !d->rkold[v]) { why = "null state or RK array"; return false; }
+  for (int i = 0; i < d->ndim; ++i)
+    for (int s = 0; s < 2; ++s) {
+      int dep = d->bc_depth[i][s];
+      if (dep < 0 || dep > 5) { why = "boundary depth must be 0..5"; return false; }
+    }
+  if (d->gama <= 1.0) { why = "gama must exceed 1"; return false; }
+  return true;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------------------
+extern "C" {
+
+int osb_version(void) { return OSB_VERSION; }
+
+int osb_last_error(char* buf, size_t n) {
+  if (!buf || n == 0) return (int)g_err.size();
+  size_t m = std::min(n - 1, g_err.size());
+  memcpy(buf, g_err.data(), m);
+  buf[m] = 0;
+  return (int)m;
+}
+
+int osb_desc_layout(long long* out, int n) {
+  if (!out || n < 9) return fail(OSB_EINVAL, "need 9 slots");
+  out[0] = sizeof(osb_block_desc);
+  out[1] = offsetof(osb_block_desc, size);
+  out[2] = offsetof(osb_block_desc, bc);
+  out[3] = offsetof(osb_block_desc, iface);
+  out[4] = offsetof(osb_block_desc, gama);
+  out[5] = offsetof(osb_block_desc, delta);
+  out[6] = offsetof(osb_block_desc, q);
+  out[7] = offsetof(osb_block_desc, rkold);
+  out[8] = offsetof(osb_block_desc, metric);
+  return OSB_OK;
+}
+
+int osb_ctx_create(int device, int precision, osb_ctx** out) {
+  if (!out) return fail(OSB_EINVAL, "null out");
+  if (precision != OSB_PREC_FP64 && precision != OSB_PREC_FP32_RESIDUAL) return fail(OSB_EINVAL, "bad precision");
+  int ndev = 0;
+  OSB_CK(cudaGetDeviceCount(&ndev));
+  if (device < 0 || device >= ndev) return fail(OSB_EINVAL, "device %d out of range (%d devices)", device, ndev);
+  OSB_CK(cudaSetDevice(device));
+  osb_ctx* c = new osb_ctx;
+  c->device = device;
+  c->prec = precision;
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, device) == cudaSuccess) c->sm_count = prop.multiProcessorCount;
+  cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) { delete c; return fail(OSB_ECUDA, "stream: %s", cudaGetErrorString(e)); }
+  c->red_slots = c->sm_count * 8 + 1;
+  e = cudaMalloc(&c->red, sizeof(double) * (c->red_slots + 8) * 64);
+  if (e == cudaSuccess) e = cudaMalloc(&c->bad, sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMallocHost(&c->red_host, sizeof(double) * 8);
+  if (e == cudaSuccess) e = cudaMemset(c->bad, 0, sizeof(unsigned long long));
+  if (e != cudaSuccess) {
+    osb_ctx_destroy(c);
+    return fail(OSB_ECUDA, "workspace: %s", cudaGetErrorString(e));
+  }
+  *out = c;
+  return OSB_OK;
+}
+
+int osb_ctx_destroy(osb_ctx* c) {
+  if (!c) return OSB_OK;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  drop_graph(c);
+  for (auto& te : c->events) {
+    cudaEventDestroy(te.a);
+    cudaEventDestroy(te.b);
+  }
+  for (auto e : c->event_pool) cudaEventDestroy(e);
+  for (auto& bl : c->blocks)
+    if (bl.k.R[0]) cudaFree(bl.k.R[0]);
+  if (c->red) cudaFree(c->red);
+  if (c->bad) cudaFree(c->bad);
+  if (c->red_host) cudaFreeHost(c->red_host);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return OSB_OK;
+}
+
+int osb_block_add(osb_ctx* c, const osb_block_desc* d, int* block_id) {
+  if (!c || !d) return fail(OSB_EINVAL, "null argument");
+  std::string why;
+  if (!check_desc(d, why)) return fail(OSB_EINVAL, "invalid block descriptor: %s", why.c_str());
+  if (!c->blocks.empty()) {
+    const osb_block_desc& f = c->blocks[0].d;
+    if (f.ndim != d->ndim || f.scheme != d->scheme || f.averaging != d->averaging || f.viscous != d->viscous)
+      return fail(OSB_EINVAL, "blocks of one context must share ndim, scheme, averaging and viscosity");
+  }
+  for (int i = 0; i < 10; ++i)
+    if (d->metric[i]) return fail(OSB_ENOTSUP, "curvilinear metrics are not supported by this build");
+  OSB_CK(cudaSetDevice(c->device));
+  Block bl;
+  bl.d = *d;
+  BlockK& k = bl.k;
+  memset(&k, 0, sizeof k);
+  k.ndim = d->ndim;
+  long ext[3];
+  for (int i = 0; i < 3; ++i) {
+    k.n[i] = i < d->ndim ? d->size[i] : 1;
+    ext[i] = i < d->ndim ? d->size[i] + 2 * d->halo : 1;
+    k.invd[i] = i < d->ndim ? 1.0 / d->delta[i] : 0.0;
+    k.inv2d[i] = i < d->ndim ? 1.0 / (d->delta[i] * d->delta[i]) : 0.0;
+  }
+  k.st[0] = 1;
+  k.st[1] = ext[0];
+  k.st[2] = ext[0] * ext[1];
+  k.alloc = ext[0] * ext[1] * ext[2];
+  k.off0 = d->halo + (d->ndim > 1 ? d->halo * k.st[1] : 0) + (d->ndim > 2 ? d->halo * k.st[2] : 0);
+  const int nv = d->ndim + 2;
+  for (int v = 0; v < nv; ++v) {
+    k.q[v] = d->q[v];
+    k.rk[v] = d->rkold[v];
+  }
+  double* R = nullptr;
+  OSB_CK(cudaMalloc(&R, sizeof(double) * k.alloc * nv));
+  OSB_CK(cudaMemsetAsync(R, 0, sizeof(double) * k.alloc * nv, c->stream));
+  for (int v = 0; v < nv; ++v) k.R[v] = R + (size_t)v * k.alloc;
+  c->blocks.push_back(bl);
+  drop_graph(c);
+  if (block_id) *block_id = (int)c->blocks.size() - 1;
+  return OSB_OK;
+}
+
+int osb_set_rk(osb_ctx* c, int kind, int nstages, const double* A, const double* B) {
+  if (!c || !A || !B) return fail(OSB_EINVAL, "null argument");
+  if (kind != OSB_RK_LOW_STORAGE && kind != OSB_RK_SBLI3) return fail(OSB_EINVAL, "unknown RK kind");
+  if (nstages < 1 || nstages > 8) return fail(OSB_EINVAL, "1..8 stages");
+  c->rk_kind = kind;
+  c->nst = nstages;
+  for (int i = 0; i < nstages; ++i) {
+    c->A[i] = A[i];
+    c->B[i] = B[i];
+  }
+  drop_graph(c);
+  return OSB_OK;
+}
+
+int osb_stage(osb_ctx* c, int s, double dt) {
+  if (!c) return fail(OSB_EINVAL, "null ctx");
+  if (s < 0 || s >= c->nst) return fail(OSB_EINVAL, "stage %d out of range", s);
+  OSB_CK(cudaSetDevice(c->device));
+  int rc = stage(c, s, dt);
+  if (rc) return rc;
+  OSB_CK(cudaGetLastError());
+  return OSB_OK;
+}
+
+int osb_apply_bc(osb_ctx* c) {
+  if (!c) return fail(OSB_EINVAL, "null ctx");
+  OSB_CK(cudaSetDevice(c->device));
+  int rc = apply_bc(c);
+  if (rc) return rc;
+  OSB_CK(cudaGetLastError());
+  return OSB_OK;
+}
+
+int osb_step(osb_ctx* c, double dt, int nsteps) {
+  if (!c) return fail(OSB_EINVAL, "null ctx");
+  if (nsteps < 0) return fail(OSB_EINVAL, "nsteps < 0");
+  if (c->blocks.empty()) return fail(OSB_EINVAL, "no blocks");
+  OSB_CK(cudaSetDevice(c->device));
+  if (!c->graphs || c->timing) {
+    for (int it = 0; it < nsteps; ++it) {
+      int rc = one_step(c, dt);
+      if (rc) return rc;
+    }
+    OSB_CK(cudaGetLastError());
+    return OSB_OK;
+  }
+  if (!c->gexec || c->g_dt != dt) {
+    drop_graph(c);
+    cudaGraph_t g;
+    long long before = c->launches;
+    OSB_CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = one_step(c, dt);
+    cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+    if (rc) {
+      if (e == cudaSuccess) cudaGraphDestroy(g);
+      return rc;
+    }
+    if (e != cudaSuccess) return fail(OSB_ECUDA, "graph capture: %s", cudaGetErrorString(e));
+    c->g_kernels = c->launches - before;
+    c->launches = before;
+    e = cudaGraphInstantiate(&c->gexec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(OSB_ECUDA, "graph instantiate: %s", cudaGetErrorString(e));
+    c->g_dt = dt;
+  }
+  for (int it = 0; it < nsteps; ++it) {
+    OSB_CK(cudaGraphLaunch(c->gexec, c->stream));
+    c->launches += c->g_kernels;
+  }
+  return OSB_OK;
+}
+
+int osb_residual(osb_ctx* c, int block, double* const* out) {
+  if (!c || !out) return fail(OSB_EINVAL, "null argument");
+  if (block < 0 || block >= (int)c->blocks.size()) return fail(OSB_EINVAL, "block %d out of range", block);
+  OSB_CK(cudaSetDevice(c->device));
+  Block& bl = c->blocks[block];
+  int rc = residual(c, bl);
+  if (rc) return rc;
+  for (int v = 0; v < bl.d.ndim + 2; ++v) {
+    if (!out[v]) return fail(OSB_EINVAL, "null output array %d", v);
+    OSB_CK(cudaMemcpyAsync(out[v], bl.k.R[v], sizeof(double) * bl.k.alloc, cudaMemcpyDeviceToDevice, c->stream));
+  }
+  OSB_CK(cudaGetLastError());
+  return OSB_OK;
+}
+
+int osb_reduce(osb_ctx* c, int what, double* host_out) {
+  if (!c || !host_out) return fail(OSB_EINVAL, "null argument");
+  if (what < OSB_RED_KE || what > OSB_RED_NAN_COUNT) return fail(OSB_EINVAL, "unknown reduction %d", what);
+  if (c->blocks.empty()) return fail(OSB_EINVAL, "no blocks");
+  OSB_CK(cudaSetDevice(c->device));
+  int slot = 0;
+  const int threads = 256;
+  for (auto& bl : c->blocks) {
+    long n = (long)bl.k.n[0] * bl.k.n[1] * bl.k.n[2];
+    int grid = std::min(grid_for(c, n, threads), 64);
+    if (slot + grid > (c->red_slots + 8) * 64 - 1) return fail(OSB_ENOTSUP, "too many blocks for the reduction");
+    RedParams rp{what, bl.d.ndim + 2, bl.d.viscous, bl.d.gama, bl.d.Minf, bl.d.mu_const};
+    k_reduce<<<grid, threads, 0, c->stream>>>(bl.k, rp, c->red, slot);
+    c->launches++;
+    slot += grid;
+  }
+  double* dout = c->red + ((size_t)(c->red_slots + 8) * 64 - 1);
+  k_reduce_final<<<1, 256, 0, c->stream>>>(c->red, slot, what == OSB_RED_CFL_DT, dout);
+  c->launches++;
+  OSB_CK(cudaMemcpyAsync(c->red_host, dout, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  OSB_CK(cudaStreamSynchronize(c->stream));
+  *host_out = c->red_host[0];
+  return OSB_OK;
+}
+
+int osb_sync(osb_ctx* c, int timeout_ms) {
+  if (!c) return fail(OSB_EINVAL, "null ctx");
+  OSB_CK(cudaSetDevice(c->device));
+  auto t0 = std::chrono::steady_clock::now();
+  for (;;) {
+    cudaError_t e = cudaStreamQuery(c->stream);
+    if (e == cudaSuccess) break;
+    if (e != cudaErrorNotReady) return fail(OSB_ECUDA, "stream: %s", cudaGetErrorString(e));
+    auto ms = std::chrono::duration_cast<std::chrono::milliseconds>(std::chrono::steady_clock::now() - t0).count();
+    if (timeout_ms >= 0 && ms > timeout_ms) return fail(OSB_ETIMEDOUT, "stream not idle after %d ms", timeout_ms);
+    std::this_thread::sleep_for(std::chrono::microseconds(50));
+  }
+  unsigned long long bad = 0;
+  OSB_CK(cudaMemcpy(&bad, c->bad, sizeof bad, cudaMemcpyDeviceToHost));
+  if (bad) {
+    OSB_CK(cudaMemset(c->bad, 0, sizeof bad));
+    return fail(OSB_ENAN, "%llu non-finite values produced by the RK update", bad);
+  }
+  return OSB_OK;
+}
+
+int osb_set_graphs(osb_ctx* c, int enable) {
+  if (!c) return fail(OSB_EINVAL, "null ctx");
+  c->graphs = enable != 0;
+  if (!c->graphs) drop_graph(c);
+  return OSB_OK;
+}
+
+int osb_set_variant(osb_ctx* c, int variant) {
+  if (!c) return fail(OSB_EINVAL, "null ctx");
+  c->variant = variant;
+  drop_graph(c);
+  return OSB_OK;
+}
+
+int osb_timing(osb_ctx* c, int enable) {
+  if (!c) return fail(OSB_EINVAL, "null ctx");
+  OSB_CK(cudaSetDevice(c->device));
+  int rc = timing_collect(c);
+  if (rc) return rc;
+  c->timing = enable != 0;
+  return OSB_OK;
+}
+
+int osb_timing_report(osb_ctx* c, double* ms, long long* launches, int n) {
+  if (!c || !ms || !launches) return fail(OSB_EINVAL, "null argument");
+  OSB_CK(cudaSetDevice(c->device));
+  int rc = timing_collect(c);
+  if (rc) return rc;
+  for (int i = 0; i < n && i < FAM_N; ++i) {
+    ms[i] = c->fam_ms[i];
+    launches[i] = c->fam_count[i];
+    c->fam_ms[i] = 0.0;
+    c->fam_count[i] = 0;
+  }
+  return OSB_OK;
+}
+
+int osb_launch_count(osb_ctx* c, long long* out) {
+  if (!c || !out) return fail(OSB_EINVAL, "null argument");
+  *out = c->launches;
+  return OSB_OK;
+}
+
+int osb_get_stream(osb_ctx* c, void** stream) {
+  if (!c || !stream) return fail(OSB_EINVAL, "null argument");
+  *stream = (void*)c->stream;
+  return OSB_OK;
+}
+
+}  // extern "C"

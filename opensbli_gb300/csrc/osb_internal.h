@@ -1,0 +1,81 @@
+// osb_internal.h -- host-side types shared by the translation units of libosb_gb300.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/osb_gb300.h"
+#include "osb_kernels.cuh"
+
+namespace osb {
+
+int fail(int code, const char* fmt, ...);
+
+#define OSB_CK(call)                                                                             \
+  do {                                                                                           \
+    cudaError_t e_ = (call);                                                                     \
+    if (e_ != cudaSuccess) return ::osb::fail(OSB_ECUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+  } while (0)
+
+struct Block {
+  osb_block_desc d;
+  BlockK k;
+};
+
+// Kernel families for per-kernel timing (osb_timing_report).
+enum { FAM_FLUX_X = 0, FAM_FLUX_Y, FAM_FLUX_Z, FAM_CENTRAL, FAM_RK, FAM_BC, FAM_REDUCE, FAM_N };
+
+struct TimedEvent {
+  cudaEvent_t a, b;
+  int fam;
+};
+
+}  // namespace osb
+
+struct osb_ctx {
+  int device = 0;
+  int prec = OSB_PREC_FP64;
+  cudaStream_t stream = nullptr;
+  std::vector<osb::Block> blocks;
+  int rk_kind = OSB_RK_LOW_STORAGE;
+  int nst = 3;
+  double A[8] = {0.0, -5.0 / 9.0, -153.0 / 128.0};
+  double B[8] = {1.0 / 3.0, 15.0 / 16.0, 8.0 / 15.0};
+  bool graphs = true;
+  cudaGraphExec_t gexec = nullptr;
+  double g_dt = 0.0;
+  long long g_kernels = 0;
+  double* red = nullptr;              // device reduction partials (+ final slot)
+  double* red_host = nullptr;         // pinned
+  unsigned long long* bad = nullptr;  // non-finite counter
+  int red_slots = 0;
+  long long launches = 0;
+  int variant = -1;
+  int sm_count = 152;
+  bool timing = false;                    // per-kernel CUDA-event timing (graphs bypassed)
+  std::vector<osb::TimedEvent> events;    // pending timed launches
+  std::vector<cudaEvent_t> event_pool;
+  double fam_ms[osb::FAM_N] = {0};
+  long long fam_count[osb::FAM_N] = {0};
+};
+
+namespace osb {
+
+// Brackets one kernel launch with events when timing is enabled.
+void timing_begin(osb_ctx* c, int fam);
+void timing_end(osb_ctx* c);
+
+// Characteristic flux sweeps of one block (x writes R, y/z accumulate); one instantiation per
+// precision and dimension lives in osb_flux.cu.
+int flux_f64_1d(osb_ctx* c, Block& bl, const SchemeParams& sp);
+int flux_f64_2d(osb_ctx* c, Block& bl, const SchemeParams& sp);
+int flux_f64_3d(osb_ctx* c, Block& bl, const SchemeParams& sp);
+int flux_f32_1d(osb_ctx* c, Block& bl, const SchemeParams& sp);
+int flux_f32_2d(osb_ctx* c, Block& bl, const SchemeParams& sp);
+int flux_f32_3d(osb_ctx* c, Block& bl, const SchemeParams& sp);
+// Central convective and/or viscous terms of one 3D block (osb_central.cu).
+int central_f64(osb_ctx* c, Block& bl, bool conv, int first);
+int central_f32(osb_ctx* c, Block& bl, bool conv, int first);
+
+}  // namespace osb

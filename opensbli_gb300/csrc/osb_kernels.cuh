@@ -1,0 +1,386 @@
+// osb_kernels.cuh -- CUDA kernels of one RK stage (sm_103a).
+//
+//   k_flux_x      characteristic flux sweep along x: a warp stages 32 rows x 32 points of the
+//                 state in shared memory (coalesced), then each lane sweeps one row
+//   k_flux_sweep  characteristic flux sweep along y or z: one thread per line segment,
+//                 coalesced along x, 6-point register window, one interface per step
+//   k_central3d   central 4th-order terms on a shared-memory tile: skew-symmetric convective
+//                 terms and/or viscous stress + heat flux
+//   k_rk          low-storage / SBLI RK update, counts non-finite values
+//   k_periodic / k_zero_grad / k_interface   boundary conditions
+//   k_reduce_*    FP64 diagnostics
+#pragma once
+#include "osb_math.cuh"
+
+namespace osb {
+
+struct BlockK {
+  int n[3];        // interior points per direction (1 for unused directions)
+  int ndim;
+  long st[3];      // linear strides of the OPS-layout arrays
+  long off0;       // linear index of point (0,0,0)
+  long alloc;      // allocated points per array
+  double* q[5];
+  double* rk[5];
+  double* R[5];    // FP64 residual
+  double invd[3];  // 1/Delta
+  double inv2d[3]; // 1/Delta^2
+};
+
+__device__ __forceinline__ long lin(const BlockK& b, int i, int j, int k) {
+  return b.off0 + (long)i * b.st[0] + (long)j * b.st[1] + (long)k * b.st[2];
+}
+
+// Local-frame variable order of a sweep along direction D: global index of local variable lv.
+template <int ND, int D>
+__device__ __forceinline__ int gvar(int lv) {
+  if (lv == 0) return 0;
+  if (lv == ND + 1) return ND + 1;
+  int t = lv - 1;  // 0 = normal, 1.. = tangential
+  if (ND == 3) return 1 + (D + t) % 3;
+  if (ND == 2) return 1 + (t == 0 ? D : 1 - D);
+  return 1;
+}
+
+// Accumulates -(fnew - fold) * invd into R.  In the FP32 path the difference is formed with
+// TwoSum (Knuth) so it reaches the FP64 residual without the FP32 rounding of the
+// subtraction (the compensated flux difference).
+template <typename T>
+__device__ __forceinline__ double flux_diff(T fnew, T fold, double invd) {
+  if (sizeof(T) == 4) {
+    float s = (float)fnew - (float)fold;
+    float v = s - (float)fnew;
+    float e = ((float)fnew - (s - v)) + (-(float)fold - v);
+    return -((double)s + (double)e) * invd;
+  } else {
+    return -((double)fnew - (double)fold) * invd;
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// Sweep along y (D=1) or z (D=2): thread = (x, transverse, segment).
+template <typename T, int ND, int D, int SCH, int AVG>
+__global__ void __launch_bounds__(128) k_flux_sweep(BlockK b, SchemeParams sp, int seg, int nseg, int first) {
+  constexpr int NV = ND + 2;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int other = blockIdx.y / nseg, sidx = blockIdx.y % nseg;
+  if (x >= b.n[0]) return;
+  int c1 = 0, c2 = 0;
+  if (ND == 3) {
+    if (D == 1) c2 = other + blockIdx.z * 65535; else c1 = other + blockIdx.z * 65535;
+    if (D == 1 && c2 >= b.n[2]) return;
+    if (D == 2 && c1 >= b.n[1]) return;
+  }
+  const long s = b.st[D];
+  const long base = lin(b, x, c1, c2);
+  const int N = b.n[D];
+  const int j0 = sidx * seg;
+  const int j1 = min(N, j0 + seg);
+  if (j0 >= j1) return;
+  const T gm = (T)sp.gama;
+  const double invd = b.invd[D];
+  const double* __restrict__ qv[NV];
+  double* __restrict__ Rv[NV];
+#pragma unroll
+  for (int lv = 0; lv < NV; ++lv) {
+    qv[lv] = b.q[gvar<ND, D>(lv)];
+    Rv[lv] = b.R[gvar<ND, D>(lv)];
+  }
+  Pt<T, ND> w[6];
+#pragma unroll
+  for (int m = 1; m < 6; ++m) {
+    long id = base + (long)(j0 - 4 + m) * s;
+#pragma unroll
+    for (int lv = 0; lv < NV; ++lv) w[m].q[lv] = (T)__ldg(qv[lv] + id);
+    make_pt<T, ND>(w[m], gm);
+  }
+  T fprev[NV];
+#pragma unroll
+  for (int lv = 0; lv < NV; ++lv) fprev[lv] = L_(0.0);
+  for (int j = j0 - 1; j < j1; ++j) {
+#pragma unroll
+    for (int m = 0; m < 5; ++m) w[m] = w[m + 1];
+    {
+      long id = base + (long)(j + 3) * s;
+#pragma unroll
+      for (int lv = 0; lv < NV; ++lv) w[5].q[lv] = (T)__ldg(qv[lv] + id);
+      make_pt<T, ND>(w[5], gm);
+    }
+    T fh[NV];
+    char_flux<T, ND, SCH, AVG>(w, sp, fh);
+    if (j >= j0) {
+      long id = base + (long)j * s;
+#pragma unroll
+      for (int lv = 0; lv < NV; ++lv) {
+        double d = flux_diff<T>(fh[lv], fprev[lv], invd);
+        Rv[lv][id] = first ? d : Rv[lv][id] + d;
+      }
+    }
+#pragma unroll
+    for (int lv = 0; lv < NV; ++lv) fprev[lv] = fh[lv];
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// Sweep along x.  A warp owns 32 rows (fixed y, z) and a segment of XSEG points; the state of
+// columns s0-3 .. s0+XSEG+2 of its rows is staged in shared memory with coalesced loads, then
+// lane r sweeps row r out of shared memory.
+constexpr int XSEG = 26;
+constexpr int XPITCH = 33;
+constexpr int XWARPS = 2;
+
+template <typename T, int ND, int SCH, int AVG>
+__global__ void __launch_bounds__(32 * XWARPS) k_flux_x(BlockK b, SchemeParams sp, int first) {
+  constexpr int NV = ND + 2;
+  extern __shared__ __align__(16) unsigned char osb_smem[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  T* tile = reinterpret_cast<T*>(osb_smem) + (size_t)warp * NV * 32 * XPITCH;
+  const int nrows = b.n[1] * b.n[2];
+  const int row0 = (blockIdx.y * XWARPS + warp) * 32;
+  const int s0 = blockIdx.x * XSEG;
+  const int s1 = min(b.n[0], s0 + XSEG);
+  if (row0 >= nrows) return;
+  // stage rows
+  for (int r = 0; r < 32; ++r) {
+    int row = row0 + r;
+    if (row >= nrows) break;
+    int y = row % b.n[1], z = row / b.n[1];
+    int col = s0 - 3 + lane;
+    if (col <= s1 + 2) {
+      long id = lin(b, col, y, z);
+#pragma unroll
+      for (int v = 0; v < NV; ++v) tile[(v * 32 + r) * XPITCH + lane] = (T)__ldg(b.q[v] + id);
+    }
+  }
+  __syncwarp();
+  const int row = row0 + lane;
+  if (row >= nrows) return;
+  const int y = row % b.n[1], z = row / b.n[1];
+  const long base = lin(b, 0, y, z);
+  const T gm = (T)sp.gama;
+  const double invd = b.invd[0];
+  Pt<T, ND> w[6];
+#pragma unroll
+  for (int m = 1; m < 6; ++m) {
+    int col = m - 1;  // point s0-3+col
+#pragma unroll
+    for (int v = 0; v < NV; ++v) w[m].q[v] = tile[(v * 32 + lane) * XPITCH + col];
+    make_pt<T, ND>(w[m], gm);
+  }
+  T fprev[NV];
+#pragma unroll
+  for (int v = 0; v < NV; ++v) fprev[v] = L_(0.0);
+  for (int j = s0 - 1; j < s1; ++j) {
+#pragma unroll
+    for (int m = 0; m < 5; ++m) w[m] = w[m + 1];
+    {
+      int col = j + 3 - (s0 - 3);
+#pragma unroll
+      for (int v = 0; v < NV; ++v) w[5].q[v] = tile[(v * 32 + lane) * XPITCH + col];
+      make_pt<T, ND>(w[5], gm);
+    }
+    T fh[NV];
+    char_flux<T, ND, SCH, AVG>(w, sp, fh);
+    if (j >= s0) {
+      long id = base + j;
+#pragma unroll
+      for (int v = 0; v < NV; ++v) {
+        double d = flux_diff<T>(fh[v], fprev[v], invd);
+        b.R[v][id] = first ? d : b.R[v][id] + d;
+      }
+    }
+#pragma unroll
+    for (int v = 0; v < NV; ++v) fprev[v] = fh[v];
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// Central 4th-order terms on a 3D tile (CX x CY x CZ points, halo 2 with edges).
+//   CONV: skew-symmetric (Feiereisen) convective terms, split_forms.py:111-145 as generated
+//         for the low-Mach TGV ("Convective terms" kernel).
+//   VISC: viscous stress and heat flux (StoreSome "Viscous terms" kernel), mu from the
+//         modified Sutherland law (VISC == 1) or constant (VISC == 2).
+struct CentralParams {
+  double gama, Minf, Re, Pr, mu_const;
+};
+
+constexpr int CX = 32, CY = 4, CZ = 4, CH = 2;
+constexpr int CSX = CX + 2 * CH, CSY = CY + 2 * CH, CSZ = CZ + 2 * CH;
+constexpr int CPTS = CSX * CSY * CSZ;
+
+template <typename T, bool CONV, int VISC>
+struct CentralFields {
+  // indices into the shared-memory field array
+  static constexpr int U0 = 0, U1 = 1, U2 = 2, P = 3;
+  static constexpr int TT = 4, MU = 5;
+  static constexpr int RHO = VISC ? 6 : 4, M0 = RHO + 1, M1 = RHO + 2, M2 = RHO + 3, E = RHO + 4;
+  static constexpr int N = CONV ? (VISC ? 11 : 9) : 6;
+};
+
+template <typename T, bool CONV, int VISC>
+__global__ void __launch_bounds__(CX * CY) k_central3d(BlockK b, CentralParams cp, int first) {
+  using Fd = CentralFields<T, CONV, VISC>;
+  extern __shared__ __align__(16) unsigned char osb_smem[];
+  T* sm = reinterpret_cast<T*>(osb_smem);
+  const int tx = threadIdx.x % CX, ty = threadIdx.x / CX;
+  const int x0 = blockIdx.x * CX, y0 = blockIdx.y * CY, z0 = blockIdx.z * CZ;
+  const T gm = (T)cp.gama;
+  const T M2 = (T)(cp.Minf * cp.Minf);
+  // ---- load the halo'd tile and form primitives
+  for (int idx = threadIdx.x; idx < CPTS; idx += blockDim.x) {
+    int i = idx % CSX, jj = (idx / CSX) % CSY, k = idx / (CSX * CSY);
+    int gx = x0 - CH + i, gy = y0 - CH + jj, gz = z0 - CH + k;
+    if (gx > b.n[0] + CH || gy > b.n[1] + CH || gz > b.n[2] + CH) continue;
+    long id = lin(b, gx, gy, gz);
+    T rho = (T)b.q[0][id], m0 = (T)b.q[1][id], m1 = (T)b.q[2][id], m2 = (T)b.q[3][id], E = (T)b.q[4][id];
+    T ir = L_(1.0) / rho;
+    T u0 = m0 * ir, u1 = m1 * ir, u2 = m2 * ir;
+    T p = (gm - L_(1.0)) * (E - L_(0.5) * rho * (u0 * u0 + u1 * u1 + u2 * u2));
+    sm[Fd::U0 * CPTS + idx] = u0;
+    sm[Fd::U1 * CPTS + idx] = u1;
+    sm[Fd::U2 * CPTS + idx] = u2;
+    sm[Fd::P * CPTS + idx] = p;
+    if (VISC) {
+      T Tt = M2 * gm * p * ir;
+      sm[Fd::TT * CPTS + idx] = Tt;
+      sm[Fd::MU * CPTS + idx] = (VISC == 1) ? L_(1.4042) * Tt * sqrt(Tt) / (L_(0.40417) + Tt) : (T)cp.mu_const;
+    }
+    if (CONV) {
+      sm[Fd::RHO * CPTS + idx] = rho;
+      sm[Fd::M0 * CPTS + idx] = m0;
+      sm[Fd::M1 * CPTS + idx] = m1;
+      sm[Fd::M2 * CPTS + idx] = m2;
+      sm[Fd::E * CPTS + idx] = E;
+    }
+  }
+  __syncthreads();
+  const int gx = x0 + tx, gy = y0 + ty;
+  if (gx >= b.n[0] || gy >= b.n[1]) return;
+  const T id0 = (T)b.invd[0], id1 = (T)b.invd[1], id2 = (T)b.invd[2];
+  const T jd0 = (T)b.inv2d[0], jd1 = (T)b.inv2d[1], jd2 = (T)b.inv2d[2];
+  const int sx = 1, sy = CSX, sz = CSX * CSY;
+  for (int tz = 0; tz < CZ; ++tz) {
+    const int gz = z0 + tz;
+    if (gz >= b.n[2]) break;
+    const int c = (tz + CH) * sz + (ty + CH) * sy + (tx + CH);
+    auto F = [&](int f, int o) -> T { return sm[f * CPTS + c + o]; };
+    auto D1 = [&](int f, int s, T inv) -> T { return d1w<T>(F(f, -2 * s), F(f, -s), F(f, s), F(f, 2 * s)) * inv; };
+    auto D2 = [&](int f, int s, T inv) -> T { return d2w<T>(F(f, -2 * s), F(f, -s), F(f, 0), F(f, s), F(f, 2 * s)) * inv; };
+    // mixed derivative: central-4 along sb of the central-4 derivative along sa
+    auto DM = [&](int f, int sa, int sb, T ia, T ib) -> T {
+      const T cw[4] = {L_(1.0 / 12.0), -L_(2.0 / 3.0), L_(2.0 / 3.0), -L_(1.0 / 12.0)};
+      const int off[4] = {-2, -1, 1, 2};
+      T r = L_(0.0);
+#pragma unroll
+      for (int m = 0; m < 4; ++m) {
+        int o = off[m] * sb;
+        T dv = d1w<T>(F(f, o - 2 * sa), F(f, o - sa), F(f, o + sa), F(f, o + 2 * sa)) * ia;
+        r += cw[m] * dv;
+      }
+      return r * ib;
+    };
+    const long gid = lin(b, gx, gy, gz);
+    double racc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    const int S[3] = {sx, sy, sz};
+    const T ID[3] = {id0, id1, id2};
+    const T JD[3] = {jd0, jd1, jd2};
+    const int UF[3] = {Fd::U0, Fd::U1, Fd::U2};
+    if (CONV) {
+      // R_rho -= sum_j D_j m_j ; R_m_i -= D_i p + 1/2 sum_j [D_j(m_i u_j) + u_i D_j m_j + m_j D_j u_i]
+      // R_E -= sum_j [D_j(p u_j) + 1/2 (D_j(E u_j) + m_j D_j(E/rho) + (E/rho) D_j m_j)]
+      const int MF[3] = {Fd::M0, Fd::M1, Fd::M2};
+      T divm = L_(0.0);
+#pragma unroll
+      for (int j = 0; j < 3; ++j) divm += D1(MF[j], S[j], ID[j]);
+      racc[0] = -(double)divm;
+      T Ec = F(Fd::E, 0) / F(Fd::RHO, 0);
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        T acc = D1(Fd::P, S[i], ID[i]);
+        T conv = L_(0.0), adv = L_(0.0);
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          const int s = S[j];
+          T pr = d1w<T>(F(MF[i], -2 * s) * F(UF[j], -2 * s), F(MF[i], -s) * F(UF[j], -s), F(MF[i], s) * F(UF[j], s),
+                        F(MF[i], 2 * s) * F(UF[j], 2 * s));
+          conv += pr * ID[j];
+          adv += F(MF[j], 0) * D1(UF[i], s, ID[j]);
+        }
+        acc += L_(0.5) * (conv + F(UF[i], 0) * divm + adv);
+        racc[1 + i] = -(double)acc;
+      }
+      T e = L_(0.0);
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        const int s = S[j];
+        T dpu = d1w<T>(F(Fd::P, -2 * s) * F(UF[j], -2 * s), F(Fd::P, -s) * F(UF[j], -s), F(Fd::P, s) * F(UF[j], s),
+                       F(Fd::P, 2 * s) * F(UF[j], 2 * s));
+        T dEu = d1w<T>(F(Fd::E, -2 * s) * F(UF[j], -2 * s), F(Fd::E, -s) * F(UF[j], -s), F(Fd::E, s) * F(UF[j], s),
+                       F(Fd::E, 2 * s) * F(UF[j], 2 * s));
+        T dE = d1w<T>(F(Fd::E, -2 * s) / F(Fd::RHO, -2 * s), F(Fd::E, -s) / F(Fd::RHO, -s),
+                      F(Fd::E, s) / F(Fd::RHO, s), F(Fd::E, 2 * s) / F(Fd::RHO, 2 * s));
+        e += dpu * ID[j] + L_(0.5) * (dEu * ID[j] + F(MF[j], 0) * dE * ID[j]);
+      }
+      e += L_(0.5) * divm * Ec;
+      racc[4] = -(double)e;
+    }
+    if (VISC) {
+      T du[3][3], lap[3], dmu[3], dT[3], lapT = L_(0.0);
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) du[i][j] = D1(UF[i], S[j], ID[j]);
+      const T div = du[0][0] + du[1][1] + du[2][2];
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        dmu[j] = (VISC == 1) ? D1(Fd::MU, S[j], ID[j]) : L_(0.0);
+        dT[j] = D1(Fd::TT, S[j], ID[j]);
+        lapT += D2(Fd::TT, S[j], JD[j]);
+      }
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        T s = L_(0.0);
+#pragma unroll
+        for (int j = 0; j < 3; ++j) s += D2(UF[i], S[j], JD[j]);
+        s += L_(1.0 / 3.0) * D2(UF[i], S[i], JD[i]);
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          if (j == i) continue;
+          const int a = i < j ? i : j, bb = i < j ? j : i;
+          s += L_(1.0 / 3.0) * DM(UF[j], S[a], S[bb], ID[a], ID[bb]);
+        }
+        lap[i] = s;
+      }
+      const T invRe = (T)(1.0 / cp.Re);
+      const T mu = F(Fd::MU, 0);
+      T tau[3][3];
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) tau[i][j] = du[i][j] + du[j][i] - (i == j ? L_(2.0 / 3.0) * div : L_(0.0));
+      T e = L_(0.0);
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        T m = L_(0.0);
+#pragma unroll
+        for (int j = 0; j < 3; ++j) m += tau[i][j] * dmu[j];
+        m += mu * lap[i];
+        racc[1 + i] += (double)(m * invRe);
+        const T ui = F(UF[i], 0);
+#pragma unroll
+        for (int j = 0; j < 3; ++j) e += mu * tau[i][j] * du[i][j] + ui * tau[i][j] * dmu[j];
+        e += mu * ui * lap[i];
+      }
+      const T kheat = (T)(1.0 / (cp.Pr * cp.Re * cp.Minf * cp.Minf * (cp.gama - 1.0)));
+      T h = mu * lapT;
+#pragma unroll
+      for (int j = 0; j < 3; ++j) h += dT[j] * dmu[j];
+      racc[4] += (double)(e * invRe + h * kheat);
+    }
+    const int v0 = CONV ? 0 : 1;
+#pragma unroll
+    for (int v = v0; v < 5; ++v) b.R[v][gid] = first ? racc[v] : b.R[v][gid] + racc[v];
+  }
+}
+
+}  // namespace osb

@@ -1,0 +1,297 @@
+// osb_math.cuh -- device numerics of the residual path (characteristic LLF WENO/TENO flux,
+// central-4 operators), templated on the arithmetic type T (double: FP64 path, float: FP32
+// residual path).
+//
+// Everything is written in the local frame of the sweep direction: the conserved state of a
+// point is (rho, m_n, m_t1[, m_t2], E) with m_n the momentum along the sweep.  For a Cartesian
+// direction the eigensystem of physical_models/euler_eigensystem.py:53-166 with k = e_d is the
+// k = e_0 system with the momentum components permuted (a cyclic permutation in 3D, a swap in
+// 2D, which only flips the sign of one vorticity eigenvector); the characteristic flux is
+// invariant under those relabelings, so one set of formulas serves every direction.
+#pragma once
+#include <cuda_runtime.h>
+#include <math.h>
+
+namespace osb {
+
+enum { SCH_WENO5_JS = 1, SCH_WENO5_Z = 2, SCH_TENO5 = 3, SCH_CENTRAL4 = 5 };
+enum { AVG_SIMPLE = 0, AVG_ROE = 1 };
+
+template <typename T> struct Lit;
+template <> struct Lit<double> {
+  static __device__ __forceinline__ double c(double x) { return x; }
+};
+template <> struct Lit<float> {
+  static __device__ __forceinline__ float c(double x) { return (float)x; }
+};
+#define L_(x) Lit<T>::c(x)
+
+struct SchemeParams {
+  double gama;
+  double teno_eps;   // TENO epsilon (reference value 1e-40)
+  double teno_ct;    // TENO cut-off
+  double sfc;        // shock_filter_control
+  double eps32_rel;  // FP32 path: epsilon relative to the stencil's mean square
+};
+
+// ---------------------------------------------------------------------------------------
+// Fifth-order reconstruction at the right face of f2 from f0..f4 (offsets -2..+2).
+//   WENO5-JS / WENO5-Z: weno.py:71-121 (ENO coefficients, optimal weights 3/10, 3/5, 1/10),
+//     139-206 (Jiang-Shu smoothness), 290-376 (JS alpha = d/(1e-6+b)^2; Z alpha =
+//     d(1+(|b0-b2|/(1e-40+b))^2)).
+//   TENO5: teno.py:96-217, 419-477 (stencils [-1,0,1],[0,1,2],[-2,-1,0], weights 11/20, 4/10,
+//     1/20, tau = |b0-b2|, alpha = (1+tau/(eps+b))^6, cut-off alpha/sum < C_T).
+// In the FP32 path the epsilon of WENO-Z / TENO (1e-40, below the FP32 normal range) is
+// replaced by eps32_rel * mean(f^2) + 1e-30, and TENO's alpha ratios are formed from
+// t_r/t_max so that (1+tau/(eps+b))^6 cannot overflow.
+template <typename T, int SCH>
+__device__ __forceinline__ T recon5(T fm2, T fm1, T f0, T fp1, T fp2, const SchemeParams& sp) {
+  constexpr bool F32 = sizeof(T) == 4;
+  if (SCH == SCH_TENO5) {
+    T s0 = fm1 - fp1, c0 = fm1 - L_(2.0) * f0 + fp1;
+    T s1 = L_(3.0) * f0 - L_(4.0) * fp1 + fp2, c1 = f0 - L_(2.0) * fp1 + fp2;
+    T s2 = fm2 - L_(4.0) * fm1 + L_(3.0) * f0, c2 = fm2 - L_(2.0) * fm1 + f0;
+    T b0 = L_(0.25) * s0 * s0 + L_(13.0 / 12.0) * c0 * c0;
+    T b1 = L_(0.25) * s1 * s1 + L_(13.0 / 12.0) * c1 * c1;
+    T b2 = L_(0.25) * s2 * s2 + L_(13.0 / 12.0) * c2 * c2;
+    T tau = fabs(b0 - b2);
+    T d0, d1, d2;
+    if (F32) {
+      T eps = (T)sp.eps32_rel * (fm2 * fm2 + fm1 * fm1 + f0 * f0 + fp1 * fp1 + fp2 * fp2) * L_(0.2) + L_(1e-30);
+      T t0 = L_(1.0) + tau / (eps + b0), t1 = L_(1.0) + tau / (eps + b1), t2 = L_(1.0) + tau / (eps + b2);
+      T tm = fmax(t0, fmax(t1, t2));
+      T r0 = t0 / tm, r1 = t1 / tm, r2 = t2 / tm;
+      r0 = r0 * r0 * r0; r0 = r0 * r0;
+      r1 = r1 * r1 * r1; r1 = r1 * r1;
+      r2 = r2 * r2 * r2; r2 = r2 * r2;
+      T inv = L_(1.0) / (r0 + r1 + r2);
+      T ct = (T)sp.teno_ct;
+      d0 = (r0 * inv < ct) ? L_(0.0) : L_(1.0);
+      d1 = (r1 * inv < ct) ? L_(0.0) : L_(1.0);
+      d2 = (r2 * inv < ct) ? L_(0.0) : L_(1.0);
+    } else {
+      T eps = (T)sp.teno_eps;
+      T t0 = L_(1.0) + tau / (eps + b0), t1 = L_(1.0) + tau / (eps + b1), t2 = L_(1.0) + tau / (eps + b2);
+      T a0 = t0 * t0 * t0 * t0 * t0 * t0;
+      T a1 = t1 * t1 * t1 * t1 * t1 * t1;
+      T a2 = t2 * t2 * t2 * t2 * t2 * t2;
+      T inv = L_(1.0) / (a0 + a1 + a2);
+      T ct = (T)sp.teno_ct;
+      d0 = (a0 * inv < ct) ? L_(0.0) : L_(1.0);
+      d1 = (a1 * inv < ct) ? L_(0.0) : L_(1.0);
+      d2 = (a2 * inv < ct) ? L_(0.0) : L_(1.0);
+    }
+    T w0 = L_(11.0 / 20.0) * d0, w1 = L_(4.0 / 10.0) * d1, w2 = L_(1.0 / 20.0) * d2;
+    T iw = L_(1.0) / (w0 + w1 + w2);
+    T e0 = -L_(1.0 / 6.0) * fm1 + L_(5.0 / 6.0) * f0 + L_(2.0 / 6.0) * fp1;
+    T e1 = L_(2.0 / 6.0) * f0 + L_(5.0 / 6.0) * fp1 - L_(1.0 / 6.0) * fp2;
+    T e2 = L_(2.0 / 6.0) * fm2 - L_(7.0 / 6.0) * fm1 + L_(11.0 / 6.0) * f0;
+    return (w0 * e0 + w1 * e1 + w2 * e2) * iw;
+  } else {
+    T c0 = f0 - L_(2.0) * fp1 + fp2, s0 = L_(3.0) * f0 - L_(4.0) * fp1 + fp2;
+    T c1 = fm1 - L_(2.0) * f0 + fp1, s1 = fm1 - fp1;
+    T c2 = fm2 - L_(2.0) * fm1 + f0, s2 = fm2 - L_(4.0) * fm1 + L_(3.0) * f0;
+    T b0 = L_(13.0 / 12.0) * c0 * c0 + L_(0.25) * s0 * s0;
+    T b1 = L_(13.0 / 12.0) * c1 * c1 + L_(0.25) * s1 * s1;
+    T b2 = L_(13.0 / 12.0) * c2 * c2 + L_(0.25) * s2 * s2;
+    T a0, a1, a2;
+    if (SCH == SCH_WENO5_Z) {
+      T eps = F32 ? (T)sp.eps32_rel * (fm2 * fm2 + fm1 * fm1 + f0 * f0 + fp1 * fp1 + fp2 * fp2) * L_(0.2) + L_(1e-30)
+                  : L_(1.0e-40);
+      T tau = fabs(b0 - b2);
+      T r0 = tau / (eps + b0), r1 = tau / (eps + b1), r2 = tau / (eps + b2);
+      a0 = L_(0.3) * (L_(1.0) + r0 * r0);
+      a1 = L_(0.6) * (L_(1.0) + r1 * r1);
+      a2 = L_(0.1) * (L_(1.0) + r2 * r2);
+    } else {
+      T eps = L_(1.0e-6);
+      a0 = L_(0.3) / ((eps + b0) * (eps + b0));
+      a1 = L_(0.6) / ((eps + b1) * (eps + b1));
+      a2 = L_(0.1) / ((eps + b2) * (eps + b2));
+    }
+    T inv = L_(1.0) / (a0 + a1 + a2);
+    T e0 = L_(1.0 / 3.0) * f0 + L_(5.0 / 6.0) * fp1 - L_(1.0 / 6.0) * fp2;
+    T e1 = -L_(1.0 / 6.0) * fm1 + L_(5.0 / 6.0) * f0 + L_(1.0 / 3.0) * fp1;
+    T e2 = L_(1.0 / 3.0) * fm2 - L_(7.0 / 6.0) * fm1 + L_(11.0 / 6.0) * f0;
+    return (a0 * inv) * e0 + (a1 * inv) * e1 + (a2 * inv) * e2;
+  }
+}
+
+// Point data carried through a sweep: conserved state in the local frame plus primitives.
+template <typename T, int ND>
+struct Pt {
+  T q[ND + 2];  // rho, m_n, m_t.., E
+  T u[ND];      // u_n, u_t..
+  T p, a;
+};
+
+template <typename T, int ND>
+__device__ __forceinline__ void make_pt(Pt<T, ND>& s, T gm) {
+  T rho = s.q[0];
+  T ir = L_(1.0) / rho;
+  T ke = L_(0.0);
+#pragma unroll
+  for (int i = 0; i < ND; ++i) {
+    s.u[i] = s.q[1 + i] * ir;
+    ke += s.u[i] * s.u[i];
+  }
+  s.p = (gm - L_(1.0)) * (s.q[ND + 1] - L_(0.5) * rho * ke);
+  s.a = sqrt(gm * s.p * ir);
+}
+
+// Characteristic LLF flux at the interface between w[2] and w[3] of a 6-point window
+// (offsets -2..+3), local frame.  Restates shock_capturing.py:786-891 and 979-1028 with the
+// eigensystems of euler_eigensystem.py for k = e_0.
+template <typename T, int ND, int SCH, int AVG>
+__device__ __forceinline__ void char_flux(const Pt<T, ND> (&w)[6], const SchemeParams& sp, T (&fh)[ND + 2]) {
+  constexpr int NV = ND + 2;
+  const T gm = (T)sp.gama;
+  const T g1 = gm - L_(1.0);
+  const Pt<T, ND>& L = w[2];
+  const Pt<T, ND>& R = w[3];
+  // ---- averaged state (averaging.py:31-124)
+  T rho, u[ND], a;
+  if (AVG == AVG_ROE) {
+    T sL = sqrt(L.q[0]), sR = sqrt(R.q[0]);
+    rho = sqrt(L.q[0] * R.q[0]);
+    T inv = L_(1.0) / (sL + sR);
+    T ke = L_(0.0);
+#pragma unroll
+    for (int i = 0; i < ND; ++i) {
+      u[i] = (sL * L.u[i] + sR * R.u[i]) * inv;
+      ke += u[i] * u[i];
+    }
+    T H = ((L.q[NV - 1] + L.p) / sL + (R.q[NV - 1] + R.p) / sR) * inv;
+    a = sqrt(g1 * (H - L_(0.5) * ke));
+  } else {
+    rho = L_(0.5) * (L.q[0] + R.q[0]);
+#pragma unroll
+    for (int i = 0; i < ND; ++i) u[i] = L_(0.5) * (L.u[i] + R.u[i]);
+    a = L_(0.5) * (L.a + R.a);
+  }
+  // ---- LLF wave speeds over points i, i+1 (shock_capturing.py:1000-1028)
+  T sfc = (T)sp.sfc;
+  T lam_u = sfc * fmax(fabs(L.u[0]), fabs(R.u[0]));
+  T lam_p = sfc * fmax(fabs(L.u[0] + L.a), fabs(R.u[0] + R.a));
+  T lam_m = sfc * fmax(fabs(L.u[0] - L.a), fabs(R.u[0] - R.a));
+
+  T rec[NV];
+  if (ND == 1) {
+    // 1D system, euler_eigensystem.py:85-99, H = a^2/(gama-1) + u^2/2, waves (u-a, u, u+a)
+    const T u0 = u[0];
+    const T H = a * a / g1 + L_(0.5) * u0 * u0;
+    const T den = L_(2.0) * H - u0 * u0;
+    const T iden = L_(1.0) / den, ia = L_(1.0) / a;
+    T Lm[3][3];
+    Lm[0][0] = u0 * (L_(2.0) * H + a * u0 - u0 * u0) * L_(0.5) * ia * iden;
+    Lm[0][1] = (-H - a * u0 + L_(0.5) * u0 * u0) * ia * iden;
+    Lm[0][2] = iden;
+    Lm[1][0] = L_(2.0) * (H - u0 * u0) * iden;
+    Lm[1][1] = L_(2.0) * u0 * iden;
+    Lm[1][2] = -L_(2.0) * iden;
+    Lm[2][0] = u0 * (-L_(2.0) * H + a * u0 + u0 * u0) * L_(0.5) * ia * iden;
+    Lm[2][1] = (H - a * u0 - L_(0.5) * u0 * u0) * ia * iden;
+    Lm[2][2] = iden;
+    const T lam[3] = {lam_m, lam_u, lam_p};
+    T fp[3][6], fmn[3][6];
+#pragma unroll
+    for (int m = 0; m < 6; ++m) {
+      const T F0 = w[m].q[1];
+      const T F1 = w[m].u[0] * w[m].q[1] + w[m].p;
+      const T F2 = w[m].u[0] * (w[m].q[2] + w[m].p);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        T cs = Lm[k][0] * w[m].q[0] + Lm[k][1] * w[m].q[1] + Lm[k][2] * w[m].q[2];
+        T cf = Lm[k][0] * F0 + Lm[k][1] * F1 + Lm[k][2] * F2;
+        fp[k][m] = L_(0.5) * (cf + lam[k] * cs);
+        fmn[k][m] = L_(0.5) * (cf - lam[k] * cs);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+      rec[k] = recon5<T, SCH>(fp[k][0], fp[k][1], fp[k][2], fp[k][3], fp[k][4], sp) +
+               recon5<T, SCH>(fmn[k][5], fmn[k][4], fmn[k][3], fmn[k][2], fmn[k][1], sp);
+    fh[0] = rec[0] + rec[1] + rec[2];
+    fh[1] = (u0 - a) * rec[0] + u0 * rec[1] + (u0 + a) * rec[2];
+    fh[2] = (H - u0 * a) * rec[0] + L_(0.5) * u0 * u0 * rec[1] + (H + u0 * a) * rec[2];
+    return;
+  }
+  // ---- 2D / 3D with k = e_0: waves 0..ND-1 move with u_n, ND with u_n + a, ND+1 with u_n - a
+  const T ia = L_(1.0) / a, ia2 = ia * ia, irho = L_(1.0) / rho;
+  T ke = L_(0.0);
+#pragma unroll
+  for (int i = 0; i < ND; ++i) ke += u[i] * u[i];
+  const T phi = g1 * L_(0.5) * ke;
+  const T bta = ia * irho * L_(0.70710678118654752440);   // 1/(rho a sqrt 2)
+  const T alf = rho * ia * L_(0.70710678118654752440);    // rho/(a sqrt 2)
+  // projections L*v of a conserved-like vector v (rows of LEV, euler_eigensystem.py):
+  //   S = phi*v0 - g1*(u.vm) + g1*vE ; D = v_n - u_n v0
+  //   row0 = v0 - S/a^2, row_{1..ND-1} = vorticity rows, row ND = bta(S + a D), row ND+1 = bta(S - a D)
+  T fp[NV][6], fmn[NV][6];
+#pragma unroll
+  for (int m = 0; m < 6; ++m) {
+    const Pt<T, ND>& s = w[m];
+    T Fv[NV];
+    Fv[0] = s.q[1];
+    Fv[1] = s.u[0] * s.q[1] + s.p;
+#pragma unroll
+    for (int i = 1; i < ND; ++i) Fv[1 + i] = s.u[0] * s.q[1 + i];
+    Fv[NV - 1] = s.u[0] * (s.q[NV - 1] + s.p);
+    T cs[NV], cf[NV];
+#pragma unroll
+    for (int pass = 0; pass < 2; ++pass) {
+      const T* v = pass == 0 ? s.q : Fv;
+      T* o = pass == 0 ? cs : cf;
+      T um = L_(0.0);
+#pragma unroll
+      for (int i = 0; i < ND; ++i) um += u[i] * v[1 + i];
+      T S = phi * v[0] - g1 * um + g1 * v[NV - 1];
+      T D = v[1] - u[0] * v[0];
+      o[0] = v[0] - S * ia2;
+      if (ND == 2) {
+        o[1] = (u[1] * v[0] - v[2]) * irho;
+      } else {
+        o[1] = (v[3] - u[2] * v[0]) * irho;
+        o[2] = (u[1] * v[0] - v[2]) * irho;
+      }
+      o[ND] = bta * (S + a * D);
+      o[ND + 1] = bta * (S - a * D);
+    }
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      const T lk = (k < ND) ? lam_u : (k == ND ? lam_p : lam_m);
+      fp[k][m] = L_(0.5) * (cf[k] + lk * cs[k]);
+      fmn[k][m] = L_(0.5) * (cf[k] - lk * cs[k]);
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < NV; ++k)
+    rec[k] = recon5<T, SCH>(fp[k][0], fp[k][1], fp[k][2], fp[k][3], fp[k][4], sp) +
+             recon5<T, SCH>(fmn[k][5], fmn[k][4], fmn[k][3], fmn[k][2], fmn[k][1], sp);
+  // back to physical space with the REV columns (k = e_0)
+  const T rp = rec[ND] + rec[ND + 1], rm = rec[ND] - rec[ND + 1];
+  const T F0 = rec[0] + alf * rp;
+  fh[0] = F0;
+  fh[1] = u[0] * F0 + alf * a * rm;
+  const T h0 = (phi + a * a) / g1;
+  if (ND == 2) {
+    fh[2] = u[1] * F0 - rho * rec[1];
+    fh[3] = phi / g1 * rec[0] - rho * u[1] * rec[1] + alf * h0 * rp + alf * u[0] * a * rm;
+  } else {
+    fh[2] = u[1] * F0 - rho * rec[2];
+    fh[3] = u[2] * F0 + rho * rec[1];
+    fh[4] = phi / g1 * rec[0] + rho * u[2] * rec[1] - rho * u[1] * rec[2] + alf * h0 * rp + alf * u[0] * a * rm;
+  }
+}
+
+// Central 4th-order first / second derivative weights (scheme.py:83-87).
+template <typename T>
+__device__ __forceinline__ T d1w(T fm2, T fm1, T fp1, T fp2) {
+  return L_(1.0 / 12.0) * fm2 - L_(2.0 / 3.0) * fm1 + L_(2.0 / 3.0) * fp1 - L_(1.0 / 12.0) * fp2;
+}
+template <typename T>
+__device__ __forceinline__ T d2w(T fm2, T fm1, T f0, T fp1, T fp2) {
+  return -L_(1.0 / 12.0) * fm2 + L_(4.0 / 3.0) * fm1 - L_(2.5) * f0 + L_(4.0 / 3.0) * fp1 - L_(1.0 / 12.0) * fp2;
+}
+
+}  // namespace osb

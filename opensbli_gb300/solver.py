@@ -1,0 +1,150 @@
+"""Device-side engine: owns the FP64 state of every block in HBM (torch tensors used only as
+allocations) and drives libosb_gb300 through its C ABI.
+
+This is the runtime the backend (``backend.GB300Backend``) hands an OpenSBLI algorithm to,
+and what tests and the benchmark call directly with ``BlockSpec`` objects.  There is no CPU
+path: constructing a ``Solver`` without the CUDA library or without a GPU raises.
+"""
+import ctypes
+
+import numpy as np
+
+from . import abi
+from .problems import RK3_LS_A, RK3_LS_B, RK3_SBLI_NEW, RK3_SBLI_OLD
+
+
+def _torch():
+    import torch
+    if not torch.cuda.is_available():
+        raise abi.OSBError("no CUDA device: the GB300 path has no CPU fallback")
+    return torch
+
+
+class Solver:
+    """Advance one or more blocks with the GB300 kernels.
+
+    specs_states: list of (BlockSpec, [nv arrays in OPS layout]) pairs.
+    precision: "fp64" (parity path) or "fp32" (FP32 residual, FP64 state).
+    rk: "ls3" (RungeKuttaLS(3)), "sbli3" (RungeKutta(3)) or (kind, A, B).
+    """
+
+    def __init__(self, specs_states, precision="fp64", rk="ls3", device=0, graphs=True, rkold=None):
+        torch = _torch()
+        self.torch = torch
+        self.lib = abi.load_library()
+        self.device = torch.device("cuda", device)
+        self.precision = precision
+        prec = abi.PREC_FP64 if precision == "fp64" else abi.PREC_FP32_RESIDUAL
+        ctx = ctypes.c_void_p()
+        abi.check(self.lib, self.lib.osb_ctx_create(device, prec, ctypes.byref(ctx)), "osb_ctx_create")
+        self.ctx = ctx
+        self.specs = []
+        self.q = []
+        self.rk = []
+        self._descs = []
+        try:
+            for i, (spec, state) in enumerate(specs_states):
+                q = torch.empty((spec.nvars,) + spec.shape, dtype=torch.float64, device=self.device)
+                q.copy_(torch.from_numpy(np.ascontiguousarray(np.stack([np.asarray(a, dtype=np.float64) for a in state]))))
+                r = torch.zeros_like(q)
+                if rkold is not None:
+                    r.copy_(torch.from_numpy(np.ascontiguousarray(np.stack(rkold[i]))))
+                self.specs.append(spec)
+                self.q.append(q)
+                self.rk.append(r)
+                d = abi.make_desc(spec, [q[v].data_ptr() for v in range(spec.nvars)],
+                                  [r[v].data_ptr() for v in range(spec.nvars)])
+                self._descs.append(d)
+                bid = ctypes.c_int()
+                torch.cuda.synchronize(self.device)
+                abi.check(self.lib, self.lib.osb_block_add(self.ctx, ctypes.byref(d), ctypes.byref(bid)), "osb_block_add")
+            self.set_rk(rk)
+            abi.check(self.lib, self.lib.osb_set_graphs(self.ctx, 1 if graphs else 0), "osb_set_graphs")
+        except Exception:
+            self.close()
+            raise
+
+    # -- configuration -------------------------------------------------------------------
+    def set_rk(self, rk):
+        if rk == "ls3":
+            kind, A, B = abi.RK_LOW_STORAGE, RK3_LS_A, RK3_LS_B
+        elif rk == "sbli3":
+            kind, A, B = abi.RK_SBLI3, RK3_SBLI_NEW, RK3_SBLI_OLD
+        else:
+            kind, A, B = rk
+        self.rk_kind, self.A, self.B = kind, tuple(A), tuple(B)
+        Aa = (ctypes.c_double * len(A))(*A)
+        Bb = (ctypes.c_double * len(B))(*B)
+        abi.check(self.lib, self.lib.osb_set_rk(self.ctx, kind, len(A), Aa, Bb), "osb_set_rk")
+
+    # -- time stepping -------------------------------------------------------------------
+    def apply_bc(self):
+        abi.check(self.lib, self.lib.osb_apply_bc(self.ctx), "osb_apply_bc")
+
+    def step(self, dt, nsteps=1):
+        abi.check(self.lib, self.lib.osb_step(self.ctx, float(dt), int(nsteps)), "osb_step")
+
+    def stage(self, s, dt):
+        abi.check(self.lib, self.lib.osb_stage(self.ctx, int(s), float(dt)), "osb_stage")
+
+    def save_sbli(self):
+        """Copy q into the RK register (the SBLI RK3 start-of-step save) for stage-level use."""
+        for q, r in zip(self.q, self.rk):
+            r.copy_(q)
+
+    def sync(self, timeout_ms=600000):
+        abi.check(self.lib, self.lib.osb_sync(self.ctx, int(timeout_ms)), "osb_sync")
+
+    # -- outputs -------------------------------------------------------------------------
+    def residual(self, ib=0):
+        spec = self.specs[ib]
+        out = self.torch.zeros_like(self.q[ib])
+        ptrs = (ctypes.c_void_p * 5)(*([out[v].data_ptr() for v in range(spec.nvars)] + [None] * (5 - spec.nvars)))
+        abi.check(self.lib, self.lib.osb_residual(self.ctx, ib, ptrs), "osb_residual")
+        self.sync()
+        return [out[v].cpu().numpy() for v in range(spec.nvars)]
+
+    def reduce(self, what):
+        out = ctypes.c_double()
+        abi.check(self.lib, self.lib.osb_reduce(self.ctx, int(what), ctypes.byref(out)), "osb_reduce")
+        return out.value
+
+    def state(self, ib=0):
+        self.sync()
+        return [a.cpu().numpy() for a in self.q[ib]]
+
+    def rk_register(self, ib=0):
+        self.sync()
+        return [a.cpu().numpy() for a in self.rk[ib]]
+
+    def launches(self):
+        n = ctypes.c_longlong()
+        abi.check(self.lib, self.lib.osb_launch_count(self.ctx, ctypes.byref(n)), "osb_launch_count")
+        return n.value
+
+    def stream(self):
+        s = ctypes.c_void_p()
+        abi.check(self.lib, self.lib.osb_get_stream(self.ctx, ctypes.byref(s)), "osb_get_stream")
+        return self.torch.cuda.ExternalStream(s.value, device=self.device)
+
+    def timing(self, enable):
+        abi.check(self.lib, self.lib.osb_timing(self.ctx, 1 if enable else 0), "osb_timing")
+
+    def timing_report(self):
+        """{family: (milliseconds, launches)} accumulated since the last report."""
+        n = len(abi.KERNEL_FAMILIES)
+        ms = (ctypes.c_double * n)()
+        cnt = (ctypes.c_longlong * n)()
+        abi.check(self.lib, self.lib.osb_timing_report(self.ctx, ms, cnt, n), "osb_timing_report")
+        return {f: (ms[i], cnt[i]) for i, f in enumerate(abi.KERNEL_FAMILIES)}
+
+    def close(self):
+        if getattr(self, "ctx", None) is not None and self.ctx.value:
+            self.lib.osb_ctx_destroy(self.ctx)
+            self.ctx = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -113,15 +113,19 @@ def ref_available(case):
     return os.path.exists(os.path.join(REF, case, "opensbli.cpp"))
 
 
-def build_ref(case, force=False):
+def build_ref(case, force=False, fast=False):
+    """Compile a generated reference case.  The parity build uses -O2 -ffp-contract=off; the
+    timing build (fast=True, CPU baseline) uses -O3 with the compiler's default contraction."""
     d = os.path.join(REF, case)
-    exe = os.path.join(d, "ref_case")
+    exe = os.path.join(d, "ref_case_O3" if fast else "ref_case")
     src = os.path.join(d, "opensbli.cpp")
     if not os.path.exists(src):
         raise FileNotFoundError("reference sources for %s not generated (oracle/ref_generate.py)" % case)
-    if not force and os.path.exists(exe) and os.path.getmtime(exe) >= os.path.getmtime(src):
+    deps = max(os.path.getmtime(src), os.path.getmtime(os.path.join(HERE, "ops_compat.h")))
+    if not force and os.path.exists(exe) and os.path.getmtime(exe) >= deps:
         return exe
-    cmd = ["g++", "-std=c++17", "-O2", "-fopenmp", "-ffp-contract=off", "-I", HERE, "-I", d, src, "-o", exe]
+    flags = ["-O3"] if fast else ["-O2", "-ffp-contract=off"]
+    cmd = ["g++", "-std=c++17"] + flags + ["-fopenmp", "-I", HERE, "-I", d, src, "-o", exe]
     subprocess.check_call(cmd)
     return exe
 
@@ -144,11 +148,12 @@ def write_dump(path, arr, halo=5):
         f.write(np.ascontiguousarray(arr, dtype=np.float64).tobytes())
 
 
-def run_ref(case, env=None, init=None, stop_after_rk=None, threads=None, timeout=3600):
-    """Run a generated reference case; returns {dat_name: array} dumped at the stop point.
+def run_ref(case, env=None, init=None, stop_after_rk=None, threads=None, timeout=3600, fast=False, dump=True):
+    """Run a generated reference case; returns {dat_name: array} dumped at the stop point
+    plus "_rk_times" (wall-clock stamps: start of the time loop, then every RK update).
 
     init: optional {dat_name: array} loaded right before the time loop (OSB_INIT_DIR)."""
-    exe = build_ref(case)
+    exe = build_ref(case, fast=fast)
     with tempfile.TemporaryDirectory() as td:
         e = dict(os.environ)
         e["OSB_QUIET"] = "1"
@@ -160,6 +165,8 @@ def run_ref(case, env=None, init=None, stop_after_rk=None, threads=None, timeout
             e["OMP_NUM_THREADS"] = str(threads)
         if stop_after_rk is not None:
             e["OSB_STOP_AFTER_RK"] = str(stop_after_rk)
+        if not dump:
+            e["OSB_NO_DUMP"] = "1"
         if init:
             idir = os.path.join(td, "init")
             os.makedirs(idir)
@@ -174,6 +181,9 @@ def run_ref(case, env=None, init=None, stop_after_rk=None, threads=None, timeout
         red = os.path.join(td, "reductions.txt")
         if os.path.exists(red):
             out["_reductions"] = open(red).read()
+        tim = os.path.join(td, "rk_times.txt")
+        if os.path.exists(tim):
+            out["_rk_times"] = [float(l.split()[1]) for l in open(tim) if l.strip()]
         return out
 
 

@@ -292,20 +292,36 @@ static inline void ops_exit() {
   osb_dump_all("exit");
 }
 
+static inline double osb_now() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+// Wall-clock timestamp of every completed RK update (plus the start of the time loop) in
+// <OSB_DUMP_DIR>/rk_times.txt, for the CPU-baseline timing.
+static inline void osb_stamp(const char* what) {
+  const char* dir = getenv("OSB_DUMP_DIR");
+  if (!dir) return;
+  std::string fn = std::string(dir) + "/rk_times.txt";
+  FILE* f = fopen(fn.c_str(), "a");
+  if (f) { fprintf(f, "%s %.9f\n", what, osb_now()); fclose(f); }
+}
+
 static inline void osb_before_loop(const char* name) {
   osb_run_state& st = osb_state();
   if (!st.init_loaded && !osb_is_init(name)) {
     st.init_loaded = true;
     osb_load_init();
+    osb_stamp("start");
   }
   if (st.stop_pending && !osb_is_bc(name)) {
-    osb_dump_all("stop");
+    if (!osb_env_int("OSB_NO_DUMP", 0)) osb_dump_all("stop");
     exit(0);
   }
 }
 static inline void osb_after_loop(const char* name) {
   osb_run_state& st = osb_state();
   if (strstr(name, "Temporal solution advancement")) {
+    osb_stamp("rk");
     st.rk_updates++;
     if (st.stop_after >= 0 && st.rk_updates >= st.stop_after) st.stop_pending = true;
   }

@@ -172,7 +172,7 @@ def case_sod_weno5js():
     params = {"gama": "1.4", "dt": 'osb_env_double("OSB_DT", 0.0002)',
               "niter": 'osb_env_int("OSB_NITER", 1)', "block0np0": 'osb_env_int("OSB_NP0", 400)',
               "Delta0block0": "1.0/(block0np0-1)"}
-    _finish(block, {}, params)
+    return block, params
 
 
 def _tgv_block(ndim, conservative=True):
@@ -235,7 +235,7 @@ def case_tgv_shock(kind):
     block.set_block_boundaries(bcs)
     block.set_equations([copy.deepcopy(cr), copy.deepcopy(sim), initial])
     block.discretise()
-    _finish(block, {}, _tgv_params(1.25, 16, "0.001"))
+    return block, _tgv_params(1.25, 16, "0.001")
 
 
 def case_tgv_central():
@@ -270,7 +270,7 @@ def case_tgv_central():
     block.set_block_boundaries(bcs)
     block.set_equations([copy.deepcopy(cr), copy.deepcopy(sim), initial])
     block.discretise()
-    _finish(block, {}, _tgv_params(0.1, 16, "0.003385"))
+    return block, _tgv_params(0.1, 16, "0.003385")
 
 
 def case_kh_weno5z():
@@ -317,7 +317,7 @@ def case_kh_weno5z():
         params["block0np%d" % d] = 'osb_env_int("OSB_NP%d", 32)' % d
         params["Delta%dblock0" % d] = "1.0/block0np%d" % d
     params["block0np2"] = "1"
-    _finish(block, {}, params)
+    return block, params
 
 
 CASES = {
@@ -328,6 +328,17 @@ CASES = {
     "tgv_central": case_tgv_central,
     "kh_weno5z": case_kh_weno5z,
 }
+
+
+def build_case(name, reference=None):
+    """Build the OpenSBLI block of one case (discretised, no code printed); for tests of the
+    drop-in backend.  Returns (block, generator parameter dict)."""
+    reference = reference or os.environ.get("OSB_REFERENCE", "/root/reference")
+    if reference not in sys.path:
+        sys.path.insert(0, reference)
+    apply_compat_patches()
+    with open(os.devnull, "w") as dn, contextlib.redirect_stdout(dn):
+        return CASES[name]()
 
 
 def main(argv=None):
@@ -346,7 +357,8 @@ def main(argv=None):
         print("== generating %s -> %s" % (name, out), flush=True)
         with in_dir(out):
             with open(os.devnull, "w") as dn, contextlib.redirect_stdout(dn):
-                CASES[name]()
+                block, params = CASES[name]()
+                _finish(block, {}, params)
     return 0
 
 

@@ -1,0 +1,82 @@
+"""Generate the golden vectors in tests/golden/ from the reference's own generated solvers.
+
+Needs the reference checkout (to regenerate oracle/_ref) and g++.  For every case the
+initial state and the states after 1 stage, 1 step and several steps are written from the
+output of the reference solver (OPS C++ generated by OpenSBLI, compiled with
+oracle/ops_compat.h), interior points only, FP64, as a compressed .npz:
+
+    python tests/golden/make_golden.py            # all cases
+"""
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+import harness  # noqa: E402
+from opensbli_gb300 import abi, problems  # noqa: E402
+
+
+def perturb(q, amp, seed):
+    rng = np.random.default_rng(seed)
+    return [a * (1.0 + amp * rng.standard_normal(a.shape)) for a in q]
+
+
+CASES = {
+    # name: (reference case, problem builder, env, dt, stage counts, perturbation)
+    "sod_weno5js_400": ("sod_weno5js", lambda: problems.sod(400), {"OSB_NP0": 400}, 2e-4, [1, 3, 30, 3000], None),
+    "tgv_teno5_12": ("tgv_teno5", lambda: problems.tgv(12, minf=1.25, scheme=abi.SCHEME_TENO5, averaging=abi.AVG_ROE),
+                     {"OSB_NP0": 12, "OSB_NP1": 12, "OSB_NP2": 12}, 1e-3, [1, 3, 12], None),
+    "tgv_weno5z_12_perturbed": ("tgv_weno5z",
+                                lambda: problems.tgv(12, minf=1.25, scheme=abi.SCHEME_WENO5_Z),
+                                {"OSB_NP0": 12, "OSB_NP1": 12, "OSB_NP2": 12}, 1e-3, [1, 3], (1e-3, 11)),
+    "tgv_central_12": ("tgv_central", lambda: problems.tgv(12, minf=0.1, scheme=abi.SCHEME_CENTRAL4),
+                       {"OSB_NP0": 12, "OSB_NP1": 12, "OSB_NP2": 12}, 3.385e-3, [1, 3, 30], None),
+    "kh_weno5z_24_perturbed": ("kh_weno5z", lambda: problems.kh(24, amp=1.0, phase=0.0),
+                               {"OSB_NP0": 24, "OSB_NP1": 24}, 2e-4, [1, 3, 6], (1e-3, 12)),
+}
+
+
+def make(name):
+    case, mk, env, dt, counts, pert = CASES[name]
+    spec, q = mk()
+    if pert is not None:
+        q = perturb(q, *pert)
+    ob = harness.OracleBlocks([(spec, q)])
+    ob.apply_bc()  # periodic images / boundary values exactly as the reference's exchanges
+    names = harness.state_names(spec.ndim)
+    init = {n: ob.q[0][v] for v, n in enumerate(names)}
+    sl = spec.interior()
+    out = {"ic": np.stack([ob.q[0][v][sl] for v in range(spec.nvars)]), "dt": dt,
+           "counts": np.array(counts)}
+    e = dict(env)
+    e["OSB_DT"] = repr(dt)
+    e["OSB_NITER"] = max(counts) // 3 + 1
+    for n in counts:
+        r = harness.run_ref(case, env=e, init=init, stop_after_rk=n)
+        out["after_%d" % n] = np.stack([r[nm][sl] for nm in names])
+        if n == 1:
+            out["residual_1"] = np.stack([r["Residual%d_B0" % v][sl] for v in range(spec.nvars)])
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    print("wrote", name)
+
+
+def main():
+    missing = sorted({c for c in harness_cases() if not harness.ref_available(c)})
+    if missing:
+        subprocess.check_call([sys.executable, os.path.join(ROOT, "oracle", "ref_generate.py")] + missing)
+    for name in (sys.argv[1:] or CASES):
+        make(name)
+
+
+def harness_cases():
+    return [c[0] for c in CASES.values()]
+
+
+if __name__ == "__main__":
+    main()

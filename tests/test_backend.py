@@ -1,0 +1,75 @@
+"""The drop-in backend maps OpenSBLI's own problem objects onto block descriptors.  Uses the
+upstream generator when its checkout is importable (OSB_REFERENCE), otherwise skips."""
+import os
+
+import numpy as np
+import pytest
+
+from opensbli_gb300 import abi, problems
+
+REF = os.environ.get("OSB_REFERENCE", "/root/reference")
+needs_ref = pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "opensbli")),
+                               reason="upstream OpenSBLI checkout not available")
+
+
+def _backend_for(case, numbers):
+    import ref_generate
+    block, _ = ref_generate.build_case(case, REF)
+    from opensbli import TraditionalAlgorithmRK
+    from opensbli_gb300.backend import GB300Backend
+    import contextlib
+    with open(os.devnull, "w") as dn, contextlib.redirect_stdout(dn):
+        alg = TraditionalAlgorithmRK(block)
+    return GB300Backend(alg, numbers)
+
+
+TGV_NUMBERS = {"Re": "1600.0", "gama": "1.4", "Pr": "0.71", "dt": "0.001", "niter": "3",
+               "block0np0": "16", "block0np1": "16", "block0np2": "16", "Delta0block0": "2*M_PI/block0np0",
+               "Delta1block0": "2*M_PI/block0np1", "Delta2block0": "2*M_PI/block0np2", "TENO_CT": "1e-6"}
+
+
+@needs_ref
+@pytest.mark.parametrize("case,scheme,avg,minf", [("tgv_teno5", abi.SCHEME_TENO5, abi.AVG_ROE, 1.25),
+                                                  ("tgv_weno5z", abi.SCHEME_WENO5_Z, abi.AVG_SIMPLE, 1.25),
+                                                  ("tgv_central", abi.SCHEME_CENTRAL4, abi.AVG_SIMPLE, 0.1)])
+def test_tgv_spec_and_initial_state(case, scheme, avg, minf):
+    nums = dict(TGV_NUMBERS, Minf=str(minf))
+    be = _backend_for(case, nums)
+    spec = be.specs[0]
+    ref_spec, ref_q = problems.tgv(16, minf=minf, scheme=scheme, averaging=avg)
+    assert spec.scheme == ref_spec.scheme and spec.averaging == ref_spec.averaging
+    assert spec.viscous == ref_spec.viscous
+    assert spec.size == ref_spec.size and np.allclose(spec.delta, ref_spec.delta, rtol=0, atol=0)
+    assert spec.bc == ref_spec.bc and spec.bc_depth == ref_spec.bc_depth
+    assert be.rk[0] == abi.RK_LOW_STORAGE
+    assert np.allclose(be.rk[1], problems.RK3_LS_A) and np.allclose(be.rk[2], problems.RK3_LS_B)
+    from opensbli_gb300.backend import initial_state
+    q = initial_state(be.blocks[0], spec, nums)
+    for v in range(5):
+        assert np.allclose(q[v], ref_q[v], rtol=1e-13, atol=1e-13), v
+
+
+@needs_ref
+def test_sod_spec():
+    be = _backend_for("sod_weno5js", {"gama": "1.4", "dt": "0.0002", "niter": "1000", "block0np0": "400",
+                                      "Delta0block0": "1.0/(block0np0-1)"})
+    spec = be.specs[0]
+    ref_spec, ref_q = problems.sod(400)
+    assert spec.scheme == abi.SCHEME_WENO5_JS and spec.averaging == abi.AVG_SIMPLE
+    assert spec.bc == [[abi.BC_ZERO_GRAD, abi.BC_ZERO_GRAD]] and spec.bc_depth == [[4, 4]]
+    assert spec.delta[0] == ref_spec.delta[0]
+    from opensbli_gb300.backend import initial_state
+    q = initial_state(be.blocks[0], spec, {"gama": "1.4", "block0np0": "400", "Delta0block0": "1.0/(block0np0-1)"})
+    for v in range(3):
+        assert np.array_equal(q[v], ref_q[v]), v
+
+
+@needs_ref
+def test_kh_spec():
+    nums = {"gama": "1.4", "dt": "0.0002", "niter": "2", "block0np0": "32", "block0np1": "32",
+            "Delta0block0": "1.0/block0np0", "Delta1block0": "1.0/block0np1", "khamp": "1.0", "khphase": "0.0"}
+    be = _backend_for("kh_weno5z", nums)
+    spec = be.specs[0]
+    assert spec.scheme == abi.SCHEME_WENO5_Z and spec.averaging == abi.AVG_ROE
+    assert be.rk[0] == abi.RK_SBLI3
+    assert spec.bc_depth == [[4, 4], [4, 4]]

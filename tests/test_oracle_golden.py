@@ -1,0 +1,91 @@
+"""The C oracle against the golden vectors produced by the reference's own generated solvers
+(tests/golden/make_golden.py).  CPU only."""
+import os
+
+import numpy as np
+import pytest
+
+import harness
+from opensbli_gb300 import abi, problems
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+CASES = {
+    "sod_weno5js_400": (lambda: problems.sod(400), "ls3", None, 1e-12),
+    "tgv_teno5_12": (lambda: problems.tgv(12, minf=1.25, scheme=abi.SCHEME_TENO5, averaging=abi.AVG_ROE), "ls3",
+                     None, 1e-12),
+    "tgv_weno5z_12_perturbed": (lambda: problems.tgv(12, minf=1.25, scheme=abi.SCHEME_WENO5_Z), "ls3", (1e-3, 11),
+                                1e-11),
+    "tgv_central_12": (lambda: problems.tgv(12, minf=0.1, scheme=abi.SCHEME_CENTRAL4), "ls3", None, 1e-12),
+    "kh_weno5z_24_perturbed": (lambda: problems.kh(24, amp=1.0, phase=0.0), "sbli3", (1e-3, 12), 1e-9),
+}
+
+
+def perturb(q, amp, seed):
+    rng = np.random.default_rng(seed)
+    return [a * (1.0 + amp * rng.standard_normal(a.shape)) for a in q]
+
+
+def load_case(name):
+    mk, rk, pert, tol = CASES[name]
+    spec, q = mk()
+    if pert is not None:
+        q = perturb(q, *pert)
+    return spec, q, rk, tol, np.load(os.path.join(GOLD, name + ".npz"))
+
+
+def rk_params(rk):
+    if rk == "ls3":
+        return abi.RK_LOW_STORAGE, problems.RK3_LS_A, problems.RK3_LS_B
+    return abi.RK_SBLI3, problems.RK3_SBLI_NEW, problems.RK3_SBLI_OLD
+
+
+def advance(ob, spec, rk, dt, nstages):
+    kind, A, B = rk_params(rk)
+    nsteps, rest = divmod(nstages, 3)
+    if nsteps:
+        ob.step(kind, A, B, dt, nsteps)
+    if rest:
+        if kind == abi.RK_SBLI3:
+            for v in range(spec.nvars):
+                ob.rk[0][v][...] = ob.q[0][v]
+        for st in range(rest):
+            ob.stage(kind, A, B, st, dt)
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_initial_state_matches_golden(oracle_lib, name):
+    spec, q, rk, tol, g = load_case(name)
+    ob = harness.OracleBlocks([(spec, q)])
+    ob.apply_bc()
+    sl = spec.interior()
+    ic = np.stack([ob.q[0][v][sl] for v in range(spec.nvars)])
+    assert np.array_equal(ic, g["ic"])
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_oracle_residual_matches_reference(oracle_lib, name):
+    spec, q, rk, tol, g = load_case(name)
+    ob = harness.OracleBlocks([(spec, q)])
+    ob.apply_bc()
+    R = ob.residual(0)
+    sl = spec.interior()
+    for v in range(spec.nvars):
+        assert harness.rel_err(R[v][sl], g["residual_1"][v]) < 10 * tol, v
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_oracle_states_match_reference(oracle_lib, name):
+    spec, q, rk, tol, g = load_case(name)
+    dt = float(g["dt"])
+    sl = spec.interior()
+    for n in g["counts"]:
+        n = int(n)
+        if n > 300 and os.environ.get("OSB_FAST_TESTS"):
+            continue
+        ob = harness.OracleBlocks([(spec, q)])
+        ob.apply_bc()
+        advance(ob, spec, rk, dt, n)
+        ref = g["after_%d" % n]
+        errs = [harness.rel_err(ob.q[0][v][sl], ref[v]) for v in range(spec.nvars)]
+        assert max(errs) < (tol if n < 300 else 100 * tol), (n, errs)
