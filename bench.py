@@ -320,9 +320,11 @@ def our_arm(args):
     t_e2e = time.perf_counter() - t0
     e2e_value = world * pts * 3 * e2e_steps / t_e2e / 1e6
     nbytes = host_q.numel() * 8
-    s32.close()
-    del host_q, host_out, s32
+    # the pinned buffers were used on the solver's stream: release them before the stream goes
     torch.cuda.synchronize()
+    del host_q, host_out
+    s32.close()
+    del s32
 
     cpu = None
     log("e2e done")

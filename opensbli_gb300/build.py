@@ -20,12 +20,17 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-cudart", "shared", "-I", CSRC, "-I", INCLUDE]
 
 # (object name, source, extra defines)
+# The FP32-residual units are compiled with --use_fast_math (approximate reciprocal/sqrt,
+# flush-to-zero, FMA contraction); the FP64 parity units keep IEEE division and square root.
+FAST = ["--use_fast_math"]
 UNITS = [
     ("api", "osb_gb300.cu", []),
-    ("central", "osb_central.cu", []),
+    ("central_f64", "osb_central.cu", ["-DOSB_CENTRAL_T=double", "-DOSB_CENTRAL_NAME=central_f64"]),
+    ("central_f32", "osb_central.cu", ["-DOSB_CENTRAL_T=float", "-DOSB_CENTRAL_NAME=central_f32"] + FAST),
 ] + [
     ("flux_%s_%dd" % (p, nd), "osb_flux.cu",
-     ["-DOSB_T=%s" % ("double" if p == "f64" else "float"), "-DOSB_ND=%d" % nd, "-DOSB_NAME=flux_%s_%dd" % (p, nd)])
+     ["-DOSB_T=%s" % ("double" if p == "f64" else "float"), "-DOSB_ND=%d" % nd, "-DOSB_NAME=flux_%s_%dd" % (p, nd)]
+     + (FAST if p == "f32" else []))
     for p in ("f64", "f32") for nd in (1, 2, 3)
 ]
 

@@ -1,4 +1,5 @@
-// osb_central.cu -- launches of the central 4th-order convective / viscous kernel.
+// osb_central.cu -- launches of the central 4th-order convective / viscous kernel, compiled
+// once per precision (OSB_CENTRAL_T).
 #include "osb_internal.h"
 
 namespace osb {
@@ -35,7 +36,13 @@ int launch_central(osb_ctx* c, Block& bl, bool conv, int first) {
 
 }  // namespace
 
-int central_f64(osb_ctx* c, Block& bl, bool conv, int first) { return launch_central<double>(c, bl, conv, first); }
-int central_f32(osb_ctx* c, Block& bl, bool conv, int first) { return launch_central<float>(c, bl, conv, first); }
+#ifndef OSB_CENTRAL_T
+#define OSB_CENTRAL_T double
+#define OSB_CENTRAL_NAME central_f64
+#endif
+
+int OSB_CENTRAL_NAME(osb_ctx* c, Block& bl, bool conv, int first) {
+  return launch_central<OSB_CENTRAL_T>(c, bl, conv, first);
+}
 
 }  // namespace osb
