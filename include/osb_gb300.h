@@ -179,6 +179,25 @@ int osb_launch_count(osb_ctx* ctx, long long* out);
 /* Raw CUDA stream of the context (cudaStream_t), for event timing by the caller. */
 int osb_get_stream(osb_ctx* ctx, void** stream);
 
+/* ---- allocation-free variant ---------------------------------------------------------- */
+
+/* Size, in doubles, of the static residual workspace behind osb_stage_noalloc (32 MB). */
+#define OSB_NOALLOC_MAX_DOUBLES (4u * 1024u * 1024u)
+
+/* One RK stage (index-free: coefficients A, B given directly) of one block on the caller's
+ * stream, for callers that cannot allocate device memory: an application that owns all GPU
+ * memory through its own pool, or one that must not call cudaMalloc after start-up.  It calls
+ * no cudaMalloc / cudaFree and creates no stream, graph or context; the FP64 residual workspace
+ * is a file-scope __device__ array of OSB_NOALLOC_MAX_DOUBLES doubles that every GPU loading
+ * the library holds until exit, and blocks whose nvars x allocated points exceed it are
+ * rejected with OSB_EINVAL.  The caller passes the state and RK arrays in the descriptor (FP64
+ * path only) and, for OSB_RK_SBLI3, copies q into rkold at the start of each step itself.  The
+ * first call on a device looks up the workspace address (cudaGetSymbolAddress) and should come
+ * before any stream capture on that device.  All calls share the workspace: calls that overlap
+ * on the GPU race.  Asynchronous on `stream` (a cudaStream_t, NULL for the default stream).
+ * No counterpart in the reference (OPS always allocates its own datasets). */
+int osb_stage_noalloc(const osb_block_desc* desc, int rk_kind, double A, double B, double dt, void* stream);
+
 /* Binding check: writes sizeof(osb_block_desc) and the byte offsets of size, bc, iface, gama,
  * delta, q, rkold and metric into out[0..8] (n >= 9).  Needs no GPU. */
 int osb_desc_layout(long long* out, int n);

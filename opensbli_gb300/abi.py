@@ -163,6 +163,8 @@ def load_library():
     lib.osb_launch_count.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong)]
     lib.osb_get_stream.argtypes = [vp, ctypes.POINTER(vp)]
     lib.osb_desc_layout.argtypes = [ctypes.POINTER(ctypes.c_longlong), i32]
+    lib.osb_stage_noalloc.argtypes = [ctypes.POINTER(BlockDesc), i32, ctypes.c_double, ctypes.c_double,
+                                      ctypes.c_double, vp]
     lib.osb_timing.argtypes = [vp, i32]
     lib.osb_timing_report.argtypes = [vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong), i32]
     _lib = lib
@@ -185,6 +187,8 @@ def check(lib, rc, what):
 EXPORTED = ["osb_version", "osb_last_error", "osb_ctx_create", "osb_ctx_destroy", "osb_block_add",
             "osb_set_rk", "osb_step", "osb_stage", "osb_apply_bc", "osb_residual", "osb_reduce",
             "osb_sync", "osb_set_graphs", "osb_set_variant", "osb_launch_count", "osb_get_stream",
-            "osb_desc_layout", "osb_timing", "osb_timing_report"]
+            "osb_desc_layout", "osb_timing", "osb_timing_report", "osb_stage_noalloc"]
+
+NOALLOC_MAX_DOUBLES = 4 * 1024 * 1024
 
 KERNEL_FAMILIES = ["flux_x", "flux_y", "flux_z", "central", "rk_update", "boundary", "reduce"]

@@ -16,6 +16,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <mutex>
 #include <thread>
 #include <vector>
 
@@ -722,3 +723,127 @@ int osb_get_stream(osb_ctx* c, void** stream) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------------------
+// One RK stage without any device allocation (osb_stage_noalloc).
+//
+// For hosts that cannot call cudaMalloc -- a solver embedded in an application that owns all
+// device memory through its own pool, or a caller that must not allocate once it is running --
+// the FP64 residual workspace of this variant is a fixed file-scope device array instead of a
+// per-context cudaMalloc.  Every GPU that loads this library holds the array until the process
+// exits.  All calls share it, so calls that overlap on the GPU (several streams, several host
+// threads) race on it; serialise them.  The residual part of the array is fully written by the
+// first residual kernel of every call; the non-finite counter at its end is cleared by each call.
+namespace {
+
+constexpr size_t kNoAllocDoubles = (size_t)OSB_NOALLOC_MAX_DOUBLES;
+// residual workspace followed by the non-finite counter (8 bytes, 256-byte aligned slot)
+static __device__ __align__(256) double osb_noalloc_scratch[kNoAllocDoubles + 32];
+
+std::mutex g_noalloc_mu;
+double* g_noalloc_ptr[64] = {nullptr};
+
+// Device address of the scratch array on the current device: host code must not use the
+// symbol itself (it names a host-side stand-in), so look it up once per device.
+int noalloc_scratch(int device, double** out) {
+  if (device < 0 || device >= 64) return fail(OSB_EINVAL, "device %d out of range", device);
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_ptr[device]) {
+    void* ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&ptr, osb_noalloc_scratch);
+    if (e != cudaSuccess) return fail(OSB_ECUDA, "cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+    g_noalloc_ptr[device] = static_cast<double*>(ptr);
+  }
+  *out = g_noalloc_ptr[device];
+  return OSB_OK;
+}
+
+}  // namespace
+
+extern "C" int osb_stage_noalloc(const osb_block_desc* d, int rk_kind, double A, double B, double dt,
+                                 void* stream) {
+  if (!d) return fail(OSB_EINVAL, "null descriptor");
+  std::string why;
+  if (!check_desc(d, why)) return fail(OSB_EINVAL, "invalid block descriptor: %s", why.c_str());
+  if (rk_kind != OSB_RK_LOW_STORAGE && rk_kind != OSB_RK_SBLI3) return fail(OSB_EINVAL, "unknown RK kind");
+  for (int i = 0; i < 10; ++i)
+    if (d->metric[i]) return fail(OSB_ENOTSUP, "curvilinear metrics are not supported by this build");
+  const int nv = d->ndim + 2;
+  size_t alloc = 1;
+  for (int i = 0; i < d->ndim; ++i) alloc *= (size_t)(d->size[i] + 2 * d->halo);
+  if ((size_t)nv * alloc > kNoAllocDoubles)
+    return fail(OSB_EINVAL,
+                "block needs %zu doubles of residual workspace; the static workspace of osb_stage_noalloc "
+                "holds %zu (OSB_NOALLOC_MAX_DOUBLES)", (size_t)nv * alloc, kNoAllocDoubles);
+  int device = 0;
+  OSB_CK(cudaGetDevice(&device));
+  double* scratch = nullptr;
+  int rc = noalloc_scratch(device, &scratch);
+  if (rc) return rc;
+  // a context on the stack: no streams, graphs or workspaces are created
+  osb_ctx c;
+  c.device = device;
+  c.prec = OSB_PREC_FP64;
+  c.stream = static_cast<cudaStream_t>(stream);
+  c.graphs = false;
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) == cudaSuccess && sms > 0)
+    c.sm_count = sms;
+  c.bad = reinterpret_cast<unsigned long long*>(scratch + kNoAllocDoubles);
+  Block bl;
+  bl.d = *d;
+  BlockK& k = bl.k;
+  memset(&k, 0, sizeof k);
+  k.ndim = d->ndim;
+  long ext[3];
+  for (int i = 0; i < 3; ++i) {
+    k.n[i] = i < d->ndim ? d->size[i] : 1;
+    ext[i] = i < d->ndim ? d->size[i] + 2 * d->halo : 1;
+    k.invd[i] = i < d->ndim ? 1.0 / d->delta[i] : 0.0;
+    k.inv2d[i] = i < d->ndim ? 1.0 / (d->delta[i] * d->delta[i]) : 0.0;
+  }
+  k.st[0] = 1;
+  k.st[1] = ext[0];
+  k.st[2] = ext[0] * ext[1];
+  k.alloc = ext[0] * ext[1] * ext[2];
+  k.off0 = d->halo + (d->ndim > 1 ? d->halo * k.st[1] : 0) + (d->ndim > 2 ? d->halo * k.st[2] : 0);
+  for (int v = 0; v < nv; ++v) {
+    k.q[v] = d->q[v];
+    k.rk[v] = d->rkold[v];
+    k.R[v] = scratch + (size_t)v * k.alloc;
+  }
+  OSB_CK(cudaMemsetAsync(c.bad, 0, sizeof(unsigned long long), c.stream));
+  rc = residual(&c, bl);
+  if (rc) return rc;
+  long n = (long)k.n[0] * k.n[1] * k.n[2];
+  k_rk<<<grid_for(&c, n, 256), 256, 0, c.stream>>>(k, nv, rk_kind == OSB_RK_LOW_STORAGE ? 0 : 1, A, B, dt, c.bad);
+  // boundary conditions of this block (the same kernels osb_apply_bc launches)
+  for (int dd = 0; dd < d->ndim; ++dd) {
+    int b0 = d->bc[dd][0], b1 = d->bc[dd][1];
+    int dep0 = d->bc_depth[dd][0] > 0 ? d->bc_depth[dd][0] : 4;
+    int dep1 = d->bc_depth[dd][1] > 0 ? d->bc_depth[dd][1] : 4;
+    if (b0 == OSB_BC_PERIODIC && b1 == OSB_BC_PERIODIC) {
+      long tr = 1;
+      for (int e = 0; e < d->ndim; ++e)
+        if (e != dd) tr *= k.n[e] + 2 * std::max(dep0, dep1);
+      long total = 2L * std::max(dep0, dep1) * tr * nv;
+      k_periodic<<<grid_for(&c, total, 256), 256, 0, c.stream>>>(k, nv, dd, dep0, dep1);
+    } else {
+      for (int side = 0; side < 2; ++side) {
+        int kind = d->bc[dd][side];
+        if (kind == OSB_BC_ZERO_GRAD) {
+          long tr = 1;
+          for (int e = 0; e < d->ndim; ++e)
+            if (e != dd) tr *= k.n[e];
+          k_zero_grad<<<grid_for(&c, tr, 128), 128, 0, c.stream>>>(k, nv, dd, side, side ? dep1 : dep0);
+        } else if (kind == OSB_BC_PERIODIC) {
+          return fail(OSB_EINVAL, "periodic boundary on one side only (dir %d)", dd);
+        } else if (kind == OSB_BC_INTERFACE) {
+          return fail(OSB_ENOTSUP, "block interfaces need osb_step on a context");
+        }
+      }
+    }
+  }
+  OSB_CK(cudaGetLastError());
+  return OSB_OK;
+}
