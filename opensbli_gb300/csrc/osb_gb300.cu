@@ -70,6 +70,55 @@ __global__ void k_save(BlockK b, int nv) {
   }
 }
 
+// FP32-residual path RK update: the residual arrives as a float-float pair, the state and
+// register stay FP64, and the FP32 shadow of q is rewritten; conversions use integer
+// operations so only the update itself runs on the FP64 pipe.
+__global__ void k_rk32(BlockK b, int nv, int kind, double A, double B, double dt, unsigned long long* bad) {
+  const long npts = (long)b.n[0] * b.n[1] * b.n[2];
+  const double Adt = A * dt, Bdt = B * dt;
+  unsigned long long nb = 0;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < npts; t += (long)gridDim.x * blockDim.x) {
+    int i = (int)(t % b.n[0]);
+    long r = t / b.n[0];
+    int j = (int)(r % b.n[1]);
+    int k = (int)(r / b.n[1]);
+    long id = lin(b, i, j, k);
+    for (int v = 0; v < nv; ++v) {
+      double r0 = f2d_exact(b.Rh[v][id]) + f2d_exact(b.Rl[v][id]);
+      double o = b.rk[v][id];
+      double q = b.q[v][id];
+      if (kind == 0) {
+        o = A * o + dt * r0;
+        q = B * o + q;
+      } else {
+        q = Adt * r0 + o;
+        o = Bdt * r0 + o;
+      }
+      b.rk[v][id] = o;
+      b.q[v][id] = q;
+      b.qf[v][id] = d2f_rn(q);
+      if ((((unsigned)__double2hiint(q) >> 20) & 0x7ffu) == 0x7ffu) ++nb;
+    }
+  }
+  if (nb) atomicAdd(bad, nb);
+}
+
+// (hi + lo) float-float residual -> FP64 array (osb_residual of the FP32-residual path).
+__global__ void k_ff_to_double(const float* hi, const float* lo, double* out, long n) {
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x)
+    out[t] = f2d_exact(hi[t]) + f2d_exact(lo[t]);
+}
+
+// FP32 shadow <- FP64 state over the whole allocation (halos included).
+__global__ void k_q2qf(BlockK b, int nv) {
+  const long total = b.alloc * nv;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+    int v = (int)(t / b.alloc);
+    long id = t % b.alloc;
+    b.qf[v][id] = d2f_rn(b.q[v][id]);
+  }
+}
+
 // Periodic exchange of both faces of direction d (ExchangeSelf, periodic.py:53-71):
 // side 0 copies [0, depth) to [N, N+depth), side 1 copies [N-depth, N) to [-depth, 0); the
 // transverse ranges include -depth..N+depth of the other used directions (corners).
@@ -104,7 +153,9 @@ __global__ void k_periodic(BlockK b, int nv, int d, int depth0, int depth1) {
     if (skip) continue;
     if (side == 0) { src[d] = c[d]; dst[d] = N + c[d]; }
     else { src[d] = N - depth + c[d]; dst[d] = -depth + c[d]; }
-    b.q[v][lin(b, dst[0], dst[1], dst[2])] = b.q[v][lin(b, src[0], src[1], src[2])];
+    long di = lin(b, dst[0], dst[1], dst[2]), si = lin(b, src[0], src[1], src[2]);
+    b.q[v][di] = b.q[v][si];
+    if (b.qf[0]) b.qf[v][di] = b.qf[v][si];
   }
 }
 
@@ -128,6 +179,11 @@ __global__ void k_zero_grad(BlockK b, int nv, int d, int side, int depth) {
       double* q = b.q[v];
       q[id] = q[id + s];
       for (int m = 1; m <= depth; ++m) q[id - m * s] = q[id + m * s];
+      if (b.qf[0]) {
+        float* f = b.qf[v];
+        f[id] = f[id + s];
+        for (int m = 1; m <= depth; ++m) f[id - m * s] = f[id + m * s];
+      }
     }
   }
 }
@@ -367,12 +423,27 @@ int stage(osb_ctx* c, int s, double dt) {
   for (auto& bl : c->blocks) {
     long n = (long)bl.k.n[0] * bl.k.n[1] * bl.k.n[2];
     timing_begin(c, FAM_RK);
-    k_rk<<<grid_for(c, n, 256), 256, 0, c->stream>>>(bl.k, bl.d.ndim + 2, c->rk_kind == OSB_RK_LOW_STORAGE ? 0 : 1,
-                                                      c->A[s], c->B[s], dt, c->bad);
+    if (c->prec == OSB_PREC_FP32_RESIDUAL)
+      k_rk32<<<grid_for(c, n, 256), 256, 0, c->stream>>>(bl.k, bl.d.ndim + 2, c->rk_kind == OSB_RK_LOW_STORAGE ? 0 : 1,
+                                                          c->A[s], c->B[s], dt, c->bad);
+    else
+      k_rk<<<grid_for(c, n, 256), 256, 0, c->stream>>>(bl.k, bl.d.ndim + 2, c->rk_kind == OSB_RK_LOW_STORAGE ? 0 : 1,
+                                                        c->A[s], c->B[s], dt, c->bad);
     timing_end(c);
     c->launches++;
   }
   return apply_bc(c);
+}
+
+// FP32-residual path: refresh the FP32 shadow from the caller's FP64 state (the caller may
+// have written q between calls).
+int sync_shadow(osb_ctx* c) {
+  if (c->prec != OSB_PREC_FP32_RESIDUAL) return OSB_OK;
+  for (auto& bl : c->blocks) {
+    k_q2qf<<<grid_for(c, bl.k.alloc * (bl.d.ndim + 2), 256), 256, 0, c->stream>>>(bl.k, bl.d.ndim + 2);
+    c->launches++;
+  }
+  return OSB_OK;
 }
 
 int one_step(osb_ctx* c, double dt) {
@@ -486,8 +557,10 @@ int osb_ctx_destroy(osb_ctx* c) {
     cudaEventDestroy(te.b);
   }
   for (auto e : c->event_pool) cudaEventDestroy(e);
-  for (auto& bl : c->blocks)
+  for (auto& bl : c->blocks) {
     if (bl.k.R[0]) cudaFree(bl.k.R[0]);
+    if (bl.k.qf[0]) cudaFree(bl.k.qf[0]);
+  }
   if (c->red) cudaFree(c->red);
   if (c->bad) cudaFree(c->bad);
   if (c->red_host) cudaFreeHost(c->red_host);
@@ -534,6 +607,21 @@ int osb_block_add(osb_ctx* c, const osb_block_desc* d, int* block_id) {
   OSB_CK(cudaMalloc(&R, sizeof(double) * k.alloc * nv));
   OSB_CK(cudaMemsetAsync(R, 0, sizeof(double) * k.alloc * nv, c->stream));
   for (int v = 0; v < nv; ++v) k.R[v] = R + (size_t)v * k.alloc;
+  if (c->prec == OSB_PREC_FP32_RESIDUAL) {
+    // the float-float residual reuses the FP64 residual bytes; the FP32 shadow of q is extra
+    float* Rf = reinterpret_cast<float*>(R);
+    for (int v = 0; v < nv; ++v) {
+      k.Rh[v] = Rf + (size_t)(2 * v) * k.alloc;
+      k.Rl[v] = Rf + (size_t)(2 * v + 1) * k.alloc;
+    }
+    float* qf = nullptr;
+    cudaError_t e = cudaMalloc(&qf, sizeof(float) * k.alloc * nv);
+    if (e != cudaSuccess) {
+      cudaFree(R);
+      return fail(OSB_ECUDA, "FP32 shadow: %s", cudaGetErrorString(e));
+    }
+    for (int v = 0; v < nv; ++v) k.qf[v] = qf + (size_t)v * k.alloc;
+  }
   c->blocks.push_back(bl);
   drop_graph(c);
   if (block_id) *block_id = (int)c->blocks.size() - 1;
@@ -558,7 +646,9 @@ int osb_stage(osb_ctx* c, int s, double dt) {
   if (!c) return fail(OSB_EINVAL, "null ctx");
   if (s < 0 || s >= c->nst) return fail(OSB_EINVAL, "stage %d out of range", s);
   OSB_CK(cudaSetDevice(c->device));
-  int rc = stage(c, s, dt);
+  int rc = sync_shadow(c);
+  if (rc) return rc;
+  rc = stage(c, s, dt);
   if (rc) return rc;
   OSB_CK(cudaGetLastError());
   return OSB_OK;
@@ -567,7 +657,9 @@ int osb_stage(osb_ctx* c, int s, double dt) {
 int osb_apply_bc(osb_ctx* c) {
   if (!c) return fail(OSB_EINVAL, "null ctx");
   OSB_CK(cudaSetDevice(c->device));
-  int rc = apply_bc(c);
+  int rc = sync_shadow(c);
+  if (rc) return rc;
+  rc = apply_bc(c);
   if (rc) return rc;
   OSB_CK(cudaGetLastError());
   return OSB_OK;
@@ -578,6 +670,8 @@ int osb_step(osb_ctx* c, double dt, int nsteps) {
   if (nsteps < 0) return fail(OSB_EINVAL, "nsteps < 0");
   if (c->blocks.empty()) return fail(OSB_EINVAL, "no blocks");
   OSB_CK(cudaSetDevice(c->device));
+  int src = sync_shadow(c);
+  if (src) return src;
   if (!c->graphs || c->timing) {
     for (int it = 0; it < nsteps; ++it) {
       int rc = one_step(c, dt);
@@ -617,11 +711,18 @@ int osb_residual(osb_ctx* c, int block, double* const* out) {
   if (block < 0 || block >= (int)c->blocks.size()) return fail(OSB_EINVAL, "block %d out of range", block);
   OSB_CK(cudaSetDevice(c->device));
   Block& bl = c->blocks[block];
-  int rc = residual(c, bl);
+  int rc = sync_shadow(c);
+  if (rc) return rc;
+  rc = residual(c, bl);
   if (rc) return rc;
   for (int v = 0; v < bl.d.ndim + 2; ++v) {
     if (!out[v]) return fail(OSB_EINVAL, "null output array %d", v);
-    OSB_CK(cudaMemcpyAsync(out[v], bl.k.R[v], sizeof(double) * bl.k.alloc, cudaMemcpyDeviceToDevice, c->stream));
+    if (c->prec == OSB_PREC_FP32_RESIDUAL) {
+      k_ff_to_double<<<grid_for(c, bl.k.alloc, 256), 256, 0, c->stream>>>(bl.k.Rh[v], bl.k.Rl[v], out[v], bl.k.alloc);
+      c->launches++;
+    } else {
+      OSB_CK(cudaMemcpyAsync(out[v], bl.k.R[v], sizeof(double) * bl.k.alloc, cudaMemcpyDeviceToDevice, c->stream));
+    }
   }
   OSB_CK(cudaGetLastError());
   return OSB_OK;

@@ -22,10 +22,121 @@ struct BlockK {
   long alloc;      // allocated points per array
   double* q[5];
   double* rk[5];
-  double* R[5];    // FP64 residual
+  double* R[5];    // FP64 residual (FP64 path)
+  float* qf[5];    // FP32 shadow of q (FP32-residual path; null otherwise)
+  float* Rh[5];    // FP32-residual path: residual as a float-float pair (hi + lo) ...
+  float* Rl[5];    // ... stored in the same bytes as the FP64 residual
   double invd[3];  // 1/Delta
   double inv2d[3]; // 1/Delta^2
 };
+
+// ---- FP32-path helpers: no FP64 arithmetic (the FP64 pipe is 1/64 of FP32 on GB300) ----
+
+// Exact float -> double with integer operations (zero and FTZ-flushed denormals map to zero).
+__device__ __forceinline__ double f2d_exact(float f) {
+  unsigned b = __float_as_uint(f);
+  unsigned sign = b & 0x80000000u;
+  unsigned e = (b >> 23) & 0xffu;
+  unsigned m = b & 0x7fffffu;
+  unsigned hi, lo;
+  if (e == 0u) {
+    hi = sign;
+    lo = 0u;
+  } else if (e == 255u) {
+    hi = sign | 0x7ff00000u | (m >> 3) | (m ? 0x80000u : 0u);
+    lo = 0u;
+  } else {
+    hi = sign | ((e + 896u) << 20) | (m >> 3);
+    lo = m << 29;
+  }
+  return __hiloint2double((int)hi, (int)lo);
+}
+
+// double -> float rounded to nearest even with integer operations; results below the FP32
+// normal range flush to signed zero (the FP32 path runs flush-to-zero anyway).
+__device__ __forceinline__ float d2f_rn(double x) {
+  unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+  unsigned sign = hi & 0x80000000u;
+  int e = (int)((hi >> 20) & 0x7ffu);
+  if (e == 0x7ff) return __uint_as_float(sign | 0x7f800000u | ((((hi & 0xfffffu) | lo) != 0u) ? 0x400000u : 0u));
+  int fe = e - 896;
+  unsigned m = ((hi & 0xfffffu) << 3) | (lo >> 29);
+  unsigned rest = lo & 0x1fffffffu;
+  if (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) {
+    m += 1u;
+    if (m == 0x800000u) {
+      m = 0u;
+      fe += 1;
+    }
+  }
+  if (fe <= 0) return __uint_as_float(sign);
+  if (fe >= 255) return __uint_as_float(sign | 0x7f800000u);
+  return __uint_as_float(sign | ((unsigned)fe << 23) | m);
+}
+
+// (hi, lo) += a (TwoSum, Knuth), non-contracted operations.
+__device__ __forceinline__ void ff_add(float& hi, float& lo, float a, float alo) {
+  float S = __fadd_rn(hi, a);
+  float w = __fsub_rn(S, hi);
+  float E = __fadd_rn(__fsub_rn(hi, __fsub_rn(S, w)), __fsub_rn(a, w));
+  E = __fadd_rn(E, __fadd_rn(lo, alo));
+  hi = __fadd_rn(S, E);
+  lo = __fsub_rn(E, __fsub_rn(hi, S));
+}
+
+// -(fnew - fold) * invd as a float-float pair: the difference is exact (TwoSum), the product
+// carries its rounding error (FMA).
+__device__ __forceinline__ void ff_flux_diff(float fnew, float fold, float invd, float& p, float& pe) {
+  float s = __fsub_rn(fnew, fold);
+  float v = __fsub_rn(s, fnew);
+  float e = __fadd_rn(__fsub_rn(fnew, __fsub_rn(s, v)), __fsub_rn(-fold, v));
+  p = __fmul_rn(-s, invd);
+  pe = __fadd_rn(__fmaf_rn(-s, invd, -p), __fmul_rn(-e, invd));
+}
+
+template <typename T>
+__device__ __forceinline__ T ld_q(const BlockK& b, int v, long id);
+template <>
+__device__ __forceinline__ double ld_q<double>(const BlockK& b, int v, long id) { return __ldg(b.q[v] + id); }
+template <>
+__device__ __forceinline__ float ld_q<float>(const BlockK& b, int v, long id) { return __ldg(b.qf[v] + id); }
+
+// Residual update of one variable at linear index id with -(fnew - fold)*invd.
+__device__ __forceinline__ void acc_flux(const BlockK& b, int v, long id, double fnew, double fold, double invd,
+                                         int first) {
+  double d = -(fnew - fold) * invd;
+  b.R[v][id] = first ? d : b.R[v][id] + d;
+}
+__device__ __forceinline__ void acc_flux(const BlockK& b, int v, long id, float fnew, float fold, float invd,
+                                         int first) {
+  float p, pe;
+  ff_flux_diff(fnew, fold, invd, p, pe);
+  if (first) {
+    float h = __fadd_rn(p, pe);
+    b.Rh[v][id] = h;
+    b.Rl[v][id] = __fsub_rn(pe, __fsub_rn(h, p));
+  } else {
+    float h = b.Rh[v][id], l = b.Rl[v][id];
+    ff_add(h, l, p, pe);
+    b.Rh[v][id] = h;
+    b.Rl[v][id] = l;
+  }
+}
+// Residual update with a pointwise contribution c.
+__device__ __forceinline__ void acc_point(const BlockK& b, int v, long id, double c, int first) {
+  b.R[v][id] = first ? c : b.R[v][id] + c;
+}
+__device__ __forceinline__ void acc_point(const BlockK& b, int v, long id, float c, int first) {
+  if (first) {
+    b.Rh[v][id] = c;
+    b.Rl[v][id] = 0.f;
+  } else {
+    float h = b.Rh[v][id], l = b.Rl[v][id];
+    ff_add(h, l, c, 0.f);
+    b.Rh[v][id] = h;
+    b.Rl[v][id] = l;
+  }
+}
 
 __device__ __forceinline__ long lin(const BlockK& b, int i, int j, int k) {
   return b.off0 + (long)i * b.st[0] + (long)j * b.st[1] + (long)k * b.st[2];
@@ -42,26 +153,12 @@ __device__ __forceinline__ int gvar(int lv) {
   return 1;
 }
 
-// Accumulates -(fnew - fold) * invd into R.  In the FP32 path the difference is formed with
-// TwoSum (Knuth) so it reaches the FP64 residual without the FP32 rounding of the
-// subtraction (the compensated flux difference).
-template <typename T>
-__device__ __forceinline__ double flux_diff(T fnew, T fold, double invd) {
-  if (sizeof(T) == 4) {
-    float s = (float)fnew - (float)fold;
-    float v = s - (float)fnew;
-    float e = ((float)fnew - (s - v)) + (-(float)fold - v);
-    return -((double)s + (double)e) * invd;
-  } else {
-    return -((double)fnew - (double)fold) * invd;
-  }
-}
-
 // ---------------------------------------------------------------------------------------
 // Sweep along y (D=1) or z (D=2): thread = (x, transverse, segment).
 template <typename T, int ND, int D, int SCH, int AVG>
-__global__ void __launch_bounds__(128) k_flux_sweep(BlockK b, SchemeParams sp, int seg, int nseg, int first) {
+__global__ void __launch_bounds__(128) k_flux_sweep(BlockK b, SchemeParams spd, int seg, int nseg, int first) {
   constexpr int NV = ND + 2;
+  const SP<T> sp(spd);
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int other = blockIdx.y / nseg, sidx = blockIdx.y % nseg;
   if (x >= b.n[0]) return;
@@ -77,21 +174,14 @@ __global__ void __launch_bounds__(128) k_flux_sweep(BlockK b, SchemeParams sp, i
   const int j0 = sidx * seg;
   const int j1 = min(N, j0 + seg);
   if (j0 >= j1) return;
-  const T gm = (T)sp.gama;
-  const double invd = b.invd[D];
-  const double* __restrict__ qv[NV];
-  double* __restrict__ Rv[NV];
-#pragma unroll
-  for (int lv = 0; lv < NV; ++lv) {
-    qv[lv] = b.q[gvar<ND, D>(lv)];
-    Rv[lv] = b.R[gvar<ND, D>(lv)];
-  }
+  const T gm = sp.gama;
+  const T invd = (T)b.invd[D];
   Pt<T, ND> w[6];
 #pragma unroll
   for (int m = 1; m < 6; ++m) {
     long id = base + (long)(j0 - 4 + m) * s;
 #pragma unroll
-    for (int lv = 0; lv < NV; ++lv) w[m].q[lv] = (T)__ldg(qv[lv] + id);
+    for (int lv = 0; lv < NV; ++lv) w[m].q[lv] = ld_q<T>(b, gvar<ND, D>(lv), id);
     make_pt<T, ND>(w[m], gm);
   }
   T fprev[NV];
@@ -103,7 +193,7 @@ __global__ void __launch_bounds__(128) k_flux_sweep(BlockK b, SchemeParams sp, i
     {
       long id = base + (long)(j + 3) * s;
 #pragma unroll
-      for (int lv = 0; lv < NV; ++lv) w[5].q[lv] = (T)__ldg(qv[lv] + id);
+      for (int lv = 0; lv < NV; ++lv) w[5].q[lv] = ld_q<T>(b, gvar<ND, D>(lv), id);
       make_pt<T, ND>(w[5], gm);
     }
     T fh[NV];
@@ -111,10 +201,7 @@ __global__ void __launch_bounds__(128) k_flux_sweep(BlockK b, SchemeParams sp, i
     if (j >= j0) {
       long id = base + (long)j * s;
 #pragma unroll
-      for (int lv = 0; lv < NV; ++lv) {
-        double d = flux_diff<T>(fh[lv], fprev[lv], invd);
-        Rv[lv][id] = first ? d : Rv[lv][id] + d;
-      }
+      for (int lv = 0; lv < NV; ++lv) acc_flux(b, gvar<ND, D>(lv), id, fh[lv], fprev[lv], invd, first);
     }
 #pragma unroll
     for (int lv = 0; lv < NV; ++lv) fprev[lv] = fh[lv];
@@ -130,8 +217,9 @@ constexpr int XPITCH = 33;
 constexpr int XWARPS = 2;
 
 template <typename T, int ND, int SCH, int AVG>
-__global__ void __launch_bounds__(32 * XWARPS) k_flux_x(BlockK b, SchemeParams sp, int first) {
+__global__ void __launch_bounds__(32 * XWARPS) k_flux_x(BlockK b, SchemeParams spd, int first) {
   constexpr int NV = ND + 2;
+  const SP<T> sp(spd);
   extern __shared__ __align__(16) unsigned char osb_smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   T* tile = reinterpret_cast<T*>(osb_smem) + (size_t)warp * NV * 32 * XPITCH;
@@ -149,7 +237,7 @@ __global__ void __launch_bounds__(32 * XWARPS) k_flux_x(BlockK b, SchemeParams s
     if (col <= s1 + 2) {
       long id = lin(b, col, y, z);
 #pragma unroll
-      for (int v = 0; v < NV; ++v) tile[(v * 32 + r) * XPITCH + lane] = (T)__ldg(b.q[v] + id);
+      for (int v = 0; v < NV; ++v) tile[(v * 32 + r) * XPITCH + lane] = ld_q<T>(b, v, id);
     }
   }
   __syncwarp();
@@ -157,8 +245,8 @@ __global__ void __launch_bounds__(32 * XWARPS) k_flux_x(BlockK b, SchemeParams s
   if (row >= nrows) return;
   const int y = row % b.n[1], z = row / b.n[1];
   const long base = lin(b, 0, y, z);
-  const T gm = (T)sp.gama;
-  const double invd = b.invd[0];
+  const T gm = sp.gama;
+  const T invd = (T)b.invd[0];
   Pt<T, ND> w[6];
 #pragma unroll
   for (int m = 1; m < 6; ++m) {
@@ -184,10 +272,7 @@ __global__ void __launch_bounds__(32 * XWARPS) k_flux_x(BlockK b, SchemeParams s
     if (j >= s0) {
       long id = base + j;
 #pragma unroll
-      for (int v = 0; v < NV; ++v) {
-        double d = flux_diff<T>(fh[v], fprev[v], invd);
-        b.R[v][id] = first ? d : b.R[v][id] + d;
-      }
+      for (int v = 0; v < NV; ++v) acc_flux(b, v, id, fh[v], fprev[v], invd, first);
     }
 #pragma unroll
     for (int v = 0; v < NV; ++v) fprev[v] = fh[v];
@@ -226,13 +311,17 @@ __global__ void __launch_bounds__(CX * CY) k_central3d(BlockK b, CentralParams c
   const int x0 = blockIdx.x * CX, y0 = blockIdx.y * CY, z0 = blockIdx.z * CZ;
   const T gm = (T)cp.gama;
   const T M2 = (T)(cp.Minf * cp.Minf);
+  const T mu_c = (T)cp.mu_const;
+  const T invRe = (T)(1.0 / cp.Re);
+  const T kheat = (T)(1.0 / (cp.Pr * cp.Re * cp.Minf * cp.Minf * (cp.gama - 1.0)));
   // ---- load the halo'd tile and form primitives
   for (int idx = threadIdx.x; idx < CPTS; idx += blockDim.x) {
     int i = idx % CSX, jj = (idx / CSX) % CSY, k = idx / (CSX * CSY);
     int gx = x0 - CH + i, gy = y0 - CH + jj, gz = z0 - CH + k;
     if (gx > b.n[0] + CH || gy > b.n[1] + CH || gz > b.n[2] + CH) continue;
     long id = lin(b, gx, gy, gz);
-    T rho = (T)b.q[0][id], m0 = (T)b.q[1][id], m1 = (T)b.q[2][id], m2 = (T)b.q[3][id], E = (T)b.q[4][id];
+    T rho = ld_q<T>(b, 0, id), m0 = ld_q<T>(b, 1, id), m1 = ld_q<T>(b, 2, id), m2 = ld_q<T>(b, 3, id),
+      E = ld_q<T>(b, 4, id);
     T ir = L_(1.0) / rho;
     T u0 = m0 * ir, u1 = m1 * ir, u2 = m2 * ir;
     T p = (gm - L_(1.0)) * (E - L_(0.5) * rho * (u0 * u0 + u1 * u1 + u2 * u2));
@@ -243,7 +332,7 @@ __global__ void __launch_bounds__(CX * CY) k_central3d(BlockK b, CentralParams c
     if (VISC) {
       T Tt = M2 * gm * p * ir;
       sm[Fd::TT * CPTS + idx] = Tt;
-      sm[Fd::MU * CPTS + idx] = (VISC == 1) ? L_(1.4042) * Tt * sqrt(Tt) / (L_(0.40417) + Tt) : (T)cp.mu_const;
+      sm[Fd::MU * CPTS + idx] = (VISC == 1) ? L_(1.4042) * Tt * sqrt(Tt) / (L_(0.40417) + Tt) : mu_c;
     }
     if (CONV) {
       sm[Fd::RHO * CPTS + idx] = rho;
@@ -280,7 +369,7 @@ __global__ void __launch_bounds__(CX * CY) k_central3d(BlockK b, CentralParams c
       return r * ib;
     };
     const long gid = lin(b, gx, gy, gz);
-    double racc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    T racc[5] = {L_(0.0), L_(0.0), L_(0.0), L_(0.0), L_(0.0)};
     const int S[3] = {sx, sy, sz};
     const T ID[3] = {id0, id1, id2};
     const T JD[3] = {jd0, jd1, jd2};
@@ -292,7 +381,7 @@ __global__ void __launch_bounds__(CX * CY) k_central3d(BlockK b, CentralParams c
       T divm = L_(0.0);
 #pragma unroll
       for (int j = 0; j < 3; ++j) divm += D1(MF[j], S[j], ID[j]);
-      racc[0] = -(double)divm;
+      racc[0] = -divm;
       T Ec = F(Fd::E, 0) / F(Fd::RHO, 0);
 #pragma unroll
       for (int i = 0; i < 3; ++i) {
@@ -307,7 +396,7 @@ __global__ void __launch_bounds__(CX * CY) k_central3d(BlockK b, CentralParams c
           adv += F(MF[j], 0) * D1(UF[i], s, ID[j]);
         }
         acc += L_(0.5) * (conv + F(UF[i], 0) * divm + adv);
-        racc[1 + i] = -(double)acc;
+        racc[1 + i] = -acc;
       }
       T e = L_(0.0);
 #pragma unroll
@@ -322,7 +411,7 @@ __global__ void __launch_bounds__(CX * CY) k_central3d(BlockK b, CentralParams c
         e += dpu * ID[j] + L_(0.5) * (dEu * ID[j] + F(MF[j], 0) * dE * ID[j]);
       }
       e += L_(0.5) * divm * Ec;
-      racc[4] = -(double)e;
+      racc[4] = -e;
     }
     if (VISC) {
       T du[3][3], lap[3], dmu[3], dT[3], lapT = L_(0.0);
@@ -351,7 +440,6 @@ __global__ void __launch_bounds__(CX * CY) k_central3d(BlockK b, CentralParams c
         }
         lap[i] = s;
       }
-      const T invRe = (T)(1.0 / cp.Re);
       const T mu = F(Fd::MU, 0);
       T tau[3][3];
 #pragma unroll
@@ -365,21 +453,20 @@ __global__ void __launch_bounds__(CX * CY) k_central3d(BlockK b, CentralParams c
 #pragma unroll
         for (int j = 0; j < 3; ++j) m += tau[i][j] * dmu[j];
         m += mu * lap[i];
-        racc[1 + i] += (double)(m * invRe);
+        racc[1 + i] += m * invRe;
         const T ui = F(UF[i], 0);
 #pragma unroll
         for (int j = 0; j < 3; ++j) e += mu * tau[i][j] * du[i][j] + ui * tau[i][j] * dmu[j];
         e += mu * ui * lap[i];
       }
-      const T kheat = (T)(1.0 / (cp.Pr * cp.Re * cp.Minf * cp.Minf * (cp.gama - 1.0)));
       T h = mu * lapT;
 #pragma unroll
       for (int j = 0; j < 3; ++j) h += dT[j] * dmu[j];
-      racc[4] += (double)(e * invRe + h * kheat);
+      racc[4] += e * invRe + h * kheat;
     }
     const int v0 = CONV ? 0 : 1;
 #pragma unroll
-    for (int v = v0; v < 5; ++v) b.R[v][gid] = first ? racc[v] : b.R[v][gid] + racc[v];
+    for (int v = v0; v < 5; ++v) acc_point(b, v, gid, racc[v], first);
   }
 }
 

@@ -34,6 +34,16 @@ struct SchemeParams {
   double eps32_rel;  // FP32 path: epsilon relative to the stencil's mean square
 };
 
+// The same constants in the arithmetic type, converted once per thread (a conversion from
+// double runs on the FP64 pipe).
+template <typename T>
+struct SP {
+  T gama, g1, teno_eps, teno_ct, sfc, eps32_rel;
+  __device__ __forceinline__ explicit SP(const SchemeParams& p)
+      : gama((T)p.gama), g1((T)(p.gama - 1.0)), teno_eps((T)p.teno_eps), teno_ct((T)p.teno_ct), sfc((T)p.sfc),
+        eps32_rel((T)p.eps32_rel) {}
+};
+
 // ---------------------------------------------------------------------------------------
 // Fifth-order reconstruction at the right face of f2 from f0..f4 (offsets -2..+2).
 //   WENO5-JS / WENO5-Z: weno.py:71-121 (ENO coefficients, optimal weights 3/10, 3/5, 1/10),
@@ -45,7 +55,7 @@ struct SchemeParams {
 // replaced by eps32_rel * mean(f^2) + 1e-30, and TENO's alpha ratios are formed from
 // t_r/t_max so that (1+tau/(eps+b))^6 cannot overflow.
 template <typename T, int SCH>
-__device__ __forceinline__ T recon5(T fm2, T fm1, T f0, T fp1, T fp2, const SchemeParams& sp) {
+__device__ __forceinline__ T recon5(T fm2, T fm1, T f0, T fp1, T fp2, const SP<T>& sp) {
   constexpr bool F32 = sizeof(T) == 4;
   if (SCH == SCH_TENO5) {
     T s0 = fm1 - fp1, c0 = fm1 - L_(2.0) * f0 + fp1;
@@ -57,7 +67,7 @@ __device__ __forceinline__ T recon5(T fm2, T fm1, T f0, T fp1, T fp2, const Sche
     T tau = fabs(b0 - b2);
     T d0, d1, d2;
     if (F32) {
-      T eps = (T)sp.eps32_rel * (fm2 * fm2 + fm1 * fm1 + f0 * f0 + fp1 * fp1 + fp2 * fp2) * L_(0.2) + L_(1e-30);
+      T eps = sp.eps32_rel * (fm2 * fm2 + fm1 * fm1 + f0 * f0 + fp1 * fp1 + fp2 * fp2) * L_(0.2) + L_(1e-30);
       T t0 = L_(1.0) + tau / (eps + b0), t1 = L_(1.0) + tau / (eps + b1), t2 = L_(1.0) + tau / (eps + b2);
       T tm = fmax(t0, fmax(t1, t2));
       T r0 = t0 / tm, r1 = t1 / tm, r2 = t2 / tm;
@@ -65,18 +75,18 @@ __device__ __forceinline__ T recon5(T fm2, T fm1, T f0, T fp1, T fp2, const Sche
       r1 = r1 * r1 * r1; r1 = r1 * r1;
       r2 = r2 * r2 * r2; r2 = r2 * r2;
       T inv = L_(1.0) / (r0 + r1 + r2);
-      T ct = (T)sp.teno_ct;
+      T ct = sp.teno_ct;
       d0 = (r0 * inv < ct) ? L_(0.0) : L_(1.0);
       d1 = (r1 * inv < ct) ? L_(0.0) : L_(1.0);
       d2 = (r2 * inv < ct) ? L_(0.0) : L_(1.0);
     } else {
-      T eps = (T)sp.teno_eps;
+      T eps = sp.teno_eps;
       T t0 = L_(1.0) + tau / (eps + b0), t1 = L_(1.0) + tau / (eps + b1), t2 = L_(1.0) + tau / (eps + b2);
       T a0 = t0 * t0 * t0 * t0 * t0 * t0;
       T a1 = t1 * t1 * t1 * t1 * t1 * t1;
       T a2 = t2 * t2 * t2 * t2 * t2 * t2;
       T inv = L_(1.0) / (a0 + a1 + a2);
-      T ct = (T)sp.teno_ct;
+      T ct = sp.teno_ct;
       d0 = (a0 * inv < ct) ? L_(0.0) : L_(1.0);
       d1 = (a1 * inv < ct) ? L_(0.0) : L_(1.0);
       d2 = (a2 * inv < ct) ? L_(0.0) : L_(1.0);
@@ -96,7 +106,7 @@ __device__ __forceinline__ T recon5(T fm2, T fm1, T f0, T fp1, T fp2, const Sche
     T b2 = L_(13.0 / 12.0) * c2 * c2 + L_(0.25) * s2 * s2;
     T a0, a1, a2;
     if (SCH == SCH_WENO5_Z) {
-      T eps = F32 ? (T)sp.eps32_rel * (fm2 * fm2 + fm1 * fm1 + f0 * f0 + fp1 * fp1 + fp2 * fp2) * L_(0.2) + L_(1e-30)
+      T eps = F32 ? sp.eps32_rel * (fm2 * fm2 + fm1 * fm1 + f0 * f0 + fp1 * fp1 + fp2 * fp2) * L_(0.2) + L_(1e-30)
                   : L_(1.0e-40);
       T tau = fabs(b0 - b2);
       T r0 = tau / (eps + b0), r1 = tau / (eps + b1), r2 = tau / (eps + b2);
@@ -143,10 +153,9 @@ __device__ __forceinline__ void make_pt(Pt<T, ND>& s, T gm) {
 // (offsets -2..+3), local frame.  Restates shock_capturing.py:786-891 and 979-1028 with the
 // eigensystems of euler_eigensystem.py for k = e_0.
 template <typename T, int ND, int SCH, int AVG>
-__device__ __forceinline__ void char_flux(const Pt<T, ND> (&w)[6], const SchemeParams& sp, T (&fh)[ND + 2]) {
+__device__ __forceinline__ void char_flux(const Pt<T, ND> (&w)[6], const SP<T>& sp, T (&fh)[ND + 2]) {
   constexpr int NV = ND + 2;
-  const T gm = (T)sp.gama;
-  const T g1 = gm - L_(1.0);
+  const T g1 = sp.g1;
   const Pt<T, ND>& L = w[2];
   const Pt<T, ND>& R = w[3];
   // ---- averaged state (averaging.py:31-124)
@@ -170,7 +179,7 @@ __device__ __forceinline__ void char_flux(const Pt<T, ND> (&w)[6], const SchemeP
     a = L_(0.5) * (L.a + R.a);
   }
   // ---- LLF wave speeds over points i, i+1 (shock_capturing.py:1000-1028)
-  T sfc = (T)sp.sfc;
+  const T sfc = sp.sfc;
   T lam_u = sfc * fmax(fabs(L.u[0]), fabs(R.u[0]));
   T lam_p = sfc * fmax(fabs(L.u[0] + L.a), fabs(R.u[0] + R.a));
   T lam_m = sfc * fmax(fabs(L.u[0] - L.a), fabs(R.u[0] - R.a));
