@@ -74,15 +74,15 @@ __global__ void k_save(BlockK b, int nv) {
 // register stay FP64, and the FP32 shadow of q is rewritten; conversions use integer
 // operations so only the update itself runs on the FP64 pipe.
 __global__ void k_rk32(BlockK b, int nv, int kind, double A, double B, double dt, unsigned long long* bad) {
-  const long npts = (long)b.n[0] * b.n[1] * b.n[2];
+  const int npts = b.n[0] * b.n[1] * b.n[2];
   const double Adt = A * dt, Bdt = B * dt;
   unsigned long long nb = 0;
-  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < npts; t += (long)gridDim.x * blockDim.x) {
-    int i = (int)(t % b.n[0]);
-    long r = t / b.n[0];
-    int j = (int)(r % b.n[1]);
-    int k = (int)(r / b.n[1]);
-    long id = lin(b, i, j, k);
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < npts; t += gridDim.x * blockDim.x) {
+    int i = t % b.n[0];
+    int r = t / b.n[0];
+    int j = r % b.n[1];
+    int k = r / b.n[1];
+    int id = lin(b, i, j, k);
     for (int v = 0; v < nv; ++v) {
       double r0 = f2d_exact(b.Rh[v][id]) + f2d_exact(b.Rl[v][id]);
       double o = b.rk[v][id];
@@ -111,12 +111,10 @@ __global__ void k_ff_to_double(const float* hi, const float* lo, double* out, lo
 
 // FP32 shadow <- FP64 state over the whole allocation (halos included).
 __global__ void k_q2qf(BlockK b, int nv) {
-  const long total = b.alloc * nv;
-  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
-    int v = (int)(t / b.alloc);
-    long id = t % b.alloc;
-    b.qf[v][id] = d2f_rn(b.q[v][id]);
-  }
+  const int n = (int)b.alloc;
+  const int v = blockIdx.y;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x)
+    b.qf[v][t] = d2f_rn(b.q[v][t]);
 }
 
 // Periodic exchange of both faces of direction d (ExchangeSelf, periodic.py:53-71):
@@ -153,7 +151,7 @@ __global__ void k_periodic(BlockK b, int nv, int d, int depth0, int depth1) {
     if (skip) continue;
     if (side == 0) { src[d] = c[d]; dst[d] = N + c[d]; }
     else { src[d] = N - depth + c[d]; dst[d] = -depth + c[d]; }
-    long di = lin(b, dst[0], dst[1], dst[2]), si = lin(b, src[0], src[1], src[2]);
+    int di = lin(b, dst[0], dst[1], dst[2]), si = lin(b, src[0], src[1], src[2]);
     b.q[v][di] = b.q[v][si];
     if (b.qf[0]) b.qf[v][di] = b.qf[v][si];
   }
@@ -173,8 +171,8 @@ __global__ void k_zero_grad(BlockK b, int nv, int d, int side, int depth) {
     c[1] = (int)(r % ext[1]); r /= ext[1];
     c[2] = (int)r;
     c[d] = side == 0 ? 0 : b.n[d] - 1;
-    long id = lin(b, c[0], c[1], c[2]);
-    long s = b.st[d] * (side == 0 ? 1 : -1);
+    int id = lin(b, c[0], c[1], c[2]);
+    int s = b.st[d] * (side == 0 ? 1 : -1);
     for (int v = 0; v < nv; ++v) {
       double* q = b.q[v];
       q[id] = q[id + s];
@@ -440,7 +438,8 @@ int stage(osb_ctx* c, int s, double dt) {
 int sync_shadow(osb_ctx* c) {
   if (c->prec != OSB_PREC_FP32_RESIDUAL) return OSB_OK;
   for (auto& bl : c->blocks) {
-    k_q2qf<<<grid_for(c, bl.k.alloc * (bl.d.ndim + 2), 256), 256, 0, c->stream>>>(bl.k, bl.d.ndim + 2);
+    dim3 grid(grid_for(c, bl.k.alloc, 256), bl.d.ndim + 2);
+    k_q2qf<<<grid, 256, 0, c->stream>>>(bl.k, bl.d.ndim + 2);
     c->launches++;
   }
   return OSB_OK;
@@ -593,9 +592,10 @@ int osb_block_add(osb_ctx* c, const osb_block_desc* d, int* block_id) {
     k.invd[i] = i < d->ndim ? 1.0 / d->delta[i] : 0.0;
     k.inv2d[i] = i < d->ndim ? 1.0 / (d->delta[i] * d->delta[i]) : 0.0;
   }
+  if (ext[0] * ext[1] * ext[2] >= (1L << 31)) return fail(OSB_EINVAL, "block too large for 32-bit indexing");
   k.st[0] = 1;
-  k.st[1] = ext[0];
-  k.st[2] = ext[0] * ext[1];
+  k.st[1] = (int)ext[0];
+  k.st[2] = (int)(ext[0] * ext[1]);
   k.alloc = ext[0] * ext[1] * ext[2];
   k.off0 = d->halo + (d->ndim > 1 ? d->halo * k.st[1] : 0) + (d->ndim > 2 ? d->halo * k.st[2] : 0);
   const int nv = d->ndim + 2;
@@ -904,8 +904,8 @@ extern "C" int osb_stage_noalloc(const osb_block_desc* d, int rk_kind, double A,
     k.inv2d[i] = i < d->ndim ? 1.0 / (d->delta[i] * d->delta[i]) : 0.0;
   }
   k.st[0] = 1;
-  k.st[1] = ext[0];
-  k.st[2] = ext[0] * ext[1];
+  k.st[1] = (int)ext[0];
+  k.st[2] = (int)(ext[0] * ext[1]);
   k.alloc = ext[0] * ext[1] * ext[2];
   k.off0 = d->halo + (d->ndim > 1 ? d->halo * k.st[1] : 0) + (d->ndim > 2 ? d->halo * k.st[2] : 0);
   for (int v = 0; v < nv; ++v) {

@@ -17,9 +17,9 @@ namespace osb {
 struct BlockK {
   int n[3];        // interior points per direction (1 for unused directions)
   int ndim;
-  long st[3];      // linear strides of the OPS-layout arrays
-  long off0;       // linear index of point (0,0,0)
-  long alloc;      // allocated points per array
+  int st[3];       // linear strides of the OPS-layout arrays (32-bit: 64-bit integer multiplies
+  int off0;        // would compete for the FP64 pipe); linear index of point (0,0,0)
+  long alloc;      // allocated points per array (< 2^31, checked at osb_block_add)
   double* q[5];
   double* rk[5];
   double* R[5];    // FP64 residual (FP64 path)
@@ -95,19 +95,19 @@ __device__ __forceinline__ void ff_flux_diff(float fnew, float fold, float invd,
 }
 
 template <typename T>
-__device__ __forceinline__ T ld_q(const BlockK& b, int v, long id);
+__device__ __forceinline__ T ld_q(const BlockK& b, int v, int id);
 template <>
-__device__ __forceinline__ double ld_q<double>(const BlockK& b, int v, long id) { return __ldg(b.q[v] + id); }
+__device__ __forceinline__ double ld_q<double>(const BlockK& b, int v, int id) { return __ldg(b.q[v] + id); }
 template <>
-__device__ __forceinline__ float ld_q<float>(const BlockK& b, int v, long id) { return __ldg(b.qf[v] + id); }
+__device__ __forceinline__ float ld_q<float>(const BlockK& b, int v, int id) { return __ldg(b.qf[v] + id); }
 
 // Residual update of one variable at linear index id with -(fnew - fold)*invd.
-__device__ __forceinline__ void acc_flux(const BlockK& b, int v, long id, double fnew, double fold, double invd,
+__device__ __forceinline__ void acc_flux(const BlockK& b, int v, int id, double fnew, double fold, double invd,
                                          int first) {
   double d = -(fnew - fold) * invd;
   b.R[v][id] = first ? d : b.R[v][id] + d;
 }
-__device__ __forceinline__ void acc_flux(const BlockK& b, int v, long id, float fnew, float fold, float invd,
+__device__ __forceinline__ void acc_flux(const BlockK& b, int v, int id, float fnew, float fold, float invd,
                                          int first) {
   float p, pe;
   ff_flux_diff(fnew, fold, invd, p, pe);
@@ -123,10 +123,10 @@ __device__ __forceinline__ void acc_flux(const BlockK& b, int v, long id, float 
   }
 }
 // Residual update with a pointwise contribution c.
-__device__ __forceinline__ void acc_point(const BlockK& b, int v, long id, double c, int first) {
+__device__ __forceinline__ void acc_point(const BlockK& b, int v, int id, double c, int first) {
   b.R[v][id] = first ? c : b.R[v][id] + c;
 }
-__device__ __forceinline__ void acc_point(const BlockK& b, int v, long id, float c, int first) {
+__device__ __forceinline__ void acc_point(const BlockK& b, int v, int id, float c, int first) {
   if (first) {
     b.Rh[v][id] = c;
     b.Rl[v][id] = 0.f;
@@ -138,8 +138,8 @@ __device__ __forceinline__ void acc_point(const BlockK& b, int v, long id, float
   }
 }
 
-__device__ __forceinline__ long lin(const BlockK& b, int i, int j, int k) {
-  return b.off0 + (long)i * b.st[0] + (long)j * b.st[1] + (long)k * b.st[2];
+__device__ __forceinline__ int lin(const BlockK& b, int i, int j, int k) {
+  return b.off0 + i * b.st[0] + j * b.st[1] + k * b.st[2];
 }
 
 // Local-frame variable order of a sweep along direction D: global index of local variable lv.
@@ -168,8 +168,8 @@ __global__ void __launch_bounds__(128) k_flux_sweep(BlockK b, SchemeParams spd, 
     if (D == 1 && c2 >= b.n[2]) return;
     if (D == 2 && c1 >= b.n[1]) return;
   }
-  const long s = b.st[D];
-  const long base = lin(b, x, c1, c2);
+  const int s = b.st[D];
+  const int base = lin(b, x, c1, c2);
   const int N = b.n[D];
   const int j0 = sidx * seg;
   const int j1 = min(N, j0 + seg);
@@ -179,10 +179,17 @@ __global__ void __launch_bounds__(128) k_flux_sweep(BlockK b, SchemeParams spd, 
   Pt<T, ND> w[6];
 #pragma unroll
   for (int m = 1; m < 6; ++m) {
-    long id = base + (long)(j0 - 4 + m) * s;
+    int id = base + (j0 - 4 + m) * s;
 #pragma unroll
     for (int lv = 0; lv < NV; ++lv) w[m].q[lv] = ld_q<T>(b, gvar<ND, D>(lv), id);
     make_pt<T, ND>(w[m], gm);
+  }
+  // the state of point j+3 is loaded one step ahead (point j+4 <= N+3 stays inside the halo)
+  T nxt[NV];
+  {
+    int id = base + (j0 + 2) * s;
+#pragma unroll
+    for (int lv = 0; lv < NV; ++lv) nxt[lv] = ld_q<T>(b, gvar<ND, D>(lv), id);
   }
   T fprev[NV];
 #pragma unroll
@@ -190,16 +197,18 @@ __global__ void __launch_bounds__(128) k_flux_sweep(BlockK b, SchemeParams spd, 
   for (int j = j0 - 1; j < j1; ++j) {
 #pragma unroll
     for (int m = 0; m < 5; ++m) w[m] = w[m + 1];
-    {
-      long id = base + (long)(j + 3) * s;
 #pragma unroll
-      for (int lv = 0; lv < NV; ++lv) w[5].q[lv] = ld_q<T>(b, gvar<ND, D>(lv), id);
-      make_pt<T, ND>(w[5], gm);
+    for (int lv = 0; lv < NV; ++lv) w[5].q[lv] = nxt[lv];
+    {
+      int id = base + (j + 4) * s;
+#pragma unroll
+      for (int lv = 0; lv < NV; ++lv) nxt[lv] = ld_q<T>(b, gvar<ND, D>(lv), id);
     }
+    make_pt<T, ND>(w[5], gm);
     T fh[NV];
     char_flux<T, ND, SCH, AVG>(w, sp, fh);
     if (j >= j0) {
-      long id = base + (long)j * s;
+      int id = base + j * s;
 #pragma unroll
       for (int lv = 0; lv < NV; ++lv) acc_flux(b, gvar<ND, D>(lv), id, fh[lv], fprev[lv], invd, first);
     }
@@ -235,7 +244,7 @@ __global__ void __launch_bounds__(32 * XWARPS) k_flux_x(BlockK b, SchemeParams s
     int y = row % b.n[1], z = row / b.n[1];
     int col = s0 - 3 + lane;
     if (col <= s1 + 2) {
-      long id = lin(b, col, y, z);
+      int id = lin(b, col, y, z);
 #pragma unroll
       for (int v = 0; v < NV; ++v) tile[(v * 32 + r) * XPITCH + lane] = ld_q<T>(b, v, id);
     }
@@ -244,7 +253,7 @@ __global__ void __launch_bounds__(32 * XWARPS) k_flux_x(BlockK b, SchemeParams s
   const int row = row0 + lane;
   if (row >= nrows) return;
   const int y = row % b.n[1], z = row / b.n[1];
-  const long base = lin(b, 0, y, z);
+  const int base = lin(b, 0, y, z);
   const T gm = sp.gama;
   const T invd = (T)b.invd[0];
   Pt<T, ND> w[6];
@@ -270,7 +279,7 @@ __global__ void __launch_bounds__(32 * XWARPS) k_flux_x(BlockK b, SchemeParams s
     T fh[NV];
     char_flux<T, ND, SCH, AVG>(w, sp, fh);
     if (j >= s0) {
-      long id = base + j;
+      int id = base + j;
 #pragma unroll
       for (int v = 0; v < NV; ++v) acc_flux(b, v, id, fh[v], fprev[v], invd, first);
     }
@@ -319,7 +328,7 @@ __global__ void __launch_bounds__(CX * CY) k_central3d(BlockK b, CentralParams c
     int i = idx % CSX, jj = (idx / CSX) % CSY, k = idx / (CSX * CSY);
     int gx = x0 - CH + i, gy = y0 - CH + jj, gz = z0 - CH + k;
     if (gx > b.n[0] + CH || gy > b.n[1] + CH || gz > b.n[2] + CH) continue;
-    long id = lin(b, gx, gy, gz);
+    int id = lin(b, gx, gy, gz);
     T rho = ld_q<T>(b, 0, id), m0 = ld_q<T>(b, 1, id), m1 = ld_q<T>(b, 2, id), m2 = ld_q<T>(b, 3, id),
       E = ld_q<T>(b, 4, id);
     T ir = L_(1.0) / rho;
@@ -368,7 +377,7 @@ __global__ void __launch_bounds__(CX * CY) k_central3d(BlockK b, CentralParams c
       }
       return r * ib;
     };
-    const long gid = lin(b, gx, gy, gz);
+    const int gid = lin(b, gx, gy, gz);
     T racc[5] = {L_(0.0), L_(0.0), L_(0.0), L_(0.0), L_(0.0)};
     const int S[3] = {sx, sy, sz};
     const T ID[3] = {id0, id1, id2};

@@ -320,6 +320,68 @@ def case_kh_weno5z():
     return block, params
 
 
+def case_curv_weno5z():
+    """2D curvilinear wavy-mesh Euler wave, characteristic LLF WENO5-Z (Roe average) with
+    4th-order central metrics, periodic, RK-LS3: the reference's verification case
+    tests/verification_apps/euler_wave_curvilinear/verify_euler_wave_curvilinear.py (its
+    known answer: rho_B0[69,69] = 0.9984292346559068 after 10 steps of dt 5e-4 on 128^2)."""
+    from sympy import pi, sin, Eq
+    from opensbli import (MetricsEquation, EinsteinEquation, SimulationEquations, ConstituentRelations,
+                          SimulationBlock, RoeAverage, LFWeno, StoreSome, RungeKuttaLS, GridVariable, DataObject,
+                          ConstantObject, parse_expr, GridBasedInitialisation, PeriodicBC)
+    ndim = 2
+    metriceq = MetricsEquation()
+    metriceq.generate_transformations(ndim, "x", [(True, True), (True, True)], 2)
+    sc1 = "**{'scheme':'Weno'}"
+    mass = "Eq(Der(rho,t), - Conservative(detJ * rho*U_j,xi_j,%s)/detJ)" % sc1
+    momentum = "Eq(Der(rhou_i,t) , -  Conservative(detJ * (rhou_i*U_j + p*D_j_i), xi_j , %s)/detJ)" % sc1
+    energy = "Eq(Der(rhoE,t), - Conservative(detJ * (p+rhoE)*U_j,xi_j, %s)/detJ)" % sc1
+    constants_eqns = ["gama", "Minf"]
+    einstein = EinsteinEquation()
+    einstein.optional_subs_dict = metriceq.metric_subs
+    sim = SimulationEquations()
+    cr = ConstituentRelations()
+    for base in (mass, momentum, energy):
+        e = einstein.expand(base, ndim, "xi", [], constants_eqns)
+        if base == momentum:
+            e = [Eq(x.lhs, x.rhs) for x in e]
+        elif base == energy:
+            e = Eq(e.lhs, e.rhs)
+        sim.add_equations(e)
+    for c in ["Eq(u_i, rhou_i/rho)", "Eq(p, (gama-1)*(rhoE-rho*(1/2)*(KD(_i,_j)*u_i*u_j)))",
+              "Eq(a, (gama*p/rho)**0.5)", "Eq(U_i, D_i_j*u_j)"]:
+        cr.add_equations(einstein.expand(c, ndim, "xi", [], constants_eqns))
+    block = SimulationBlock(ndim, block_number=0)
+    schemes = {}
+    LF = LFWeno(5, formulation="Z", averaging=RoeAverage([0, 1]))
+    schemes[LF.name] = LF
+    cent = StoreSome(4, "u0 u1 T")
+    schemes[cent.name] = cent
+    rk = RungeKuttaLS(3)
+    schemes[rk.name] = rk
+    block.set_discretisation_schemes(schemes)
+    local_dict = {"block": block, "GridVariable": GridVariable, "DataObject": DataObject,
+                  "gama": ConstantObject("gama")}
+    (i, j) = block.grid_indexes
+    (dx, dy) = block.deltas
+    x0 = Eq(DataObject("x0"), i * dx + 0.04 * sin(2.0 * pi * 0.25) * sin(6.0 * pi * j * dy / 2.0), evaluate=False)
+    x1 = Eq(DataObject("x1"), j * dy + 0.04 * sin(2.0 * pi * 0.25) * sin(6.0 * pi * i * dx / 2.0), evaluate=False)
+    eqs = [parse_expr(e, local_dict=local_dict) for e in [
+        "Eq(GridVariable(d), 1+0.2*sin(pi*(DataObject(x0)+DataObject(x1))))", "Eq(GridVariable(u0), 1.0)",
+        "Eq(GridVariable(u1), -0.5)", "Eq(GridVariable(p), 1.0)", "Eq(DataObject(rho), d)",
+        "Eq(DataObject(rhou0), d*u0)", "Eq(DataObject(rhou1), d*u1)",
+        "Eq(DataObject(rhoE), p/(gama-1) + 0.5* d *(u0**2+u1**2))"]]
+    initial = GridBasedInitialisation()
+    initial.add_equations([x0, x1] + eqs)
+    block.set_block_boundaries([[PeriodicBC(d, 0), PeriodicBC(d, 1)] for d in range(ndim)])
+    block.set_equations([cr, initial, sim, metriceq])
+    block.discretise()
+    params = {"gama": "1.4", "dt": 'osb_env_double("OSB_DT", 0.0005)', "niter": 'osb_env_int("OSB_NITER", 10)',
+              "block0np0": 'osb_env_int("OSB_NP0", 128)', "block0np1": 'osb_env_int("OSB_NP1", 128)',
+              "Delta0block0": "2.0/(block0np0)", "Delta1block0": "2.0/(block0np1)", "block0np2": "1"}
+    return block, params
+
+
 CASES = {
     "sod_weno5js": case_sod_weno5js,
     "tgv_teno5": lambda: case_tgv_shock("teno5"),
@@ -327,6 +389,7 @@ CASES = {
     "tgv_teno6": lambda: case_tgv_shock("teno6"),
     "tgv_central": case_tgv_central,
     "kh_weno5z": case_kh_weno5z,
+    "curv_weno5z": case_curv_weno5z,
 }
 
 
