@@ -121,3 +121,109 @@ def cfl_dt(spec, q, cfl):
     for d in range(spec.ndim):
         s = s + (np.abs(us[d]) + a) / spec.delta[d]
     return float(cfl / np.max(s))
+
+
+# ---------------------------------------------------------------------------------------
+# Curvilinear blocks.  The metric arrays follow the layout of osb_block_desc.metric:
+# index 3*d + i holds D_di = d xi_d / d x_i, index 9 holds det J = det(d x / d xi).
+
+def _d1_central4(f, axis, inv_delta):
+    """4th-order central first derivative along a numpy axis, the operator order of the
+    generated metric kernel ((-2/3 f[-1] - 1/12 f[+2]) + 1/12 f[-2] + 2/3 f[+1]) * 1/Delta;
+    the outer two layers are left at zero."""
+    out = np.zeros_like(f)
+    n = f.shape[axis]
+
+    def sl(o):
+        s = [slice(None)] * f.ndim
+        s[axis] = slice(2 + o, n - 2 + o)
+        return tuple(s)
+    out[sl(0)] = ((-(2.0 / 3.0) * f[sl(-1)] - (1.0 / 12.0) * f[sl(2)]) + (1.0 / 12.0) * f[sl(-2)]
+                  + (2.0 / 3.0) * f[sl(1)]) * inv_delta
+    return out
+
+
+def _periodic_fill(spec, a, depth):
+    """Periodic halo fill of one OPS-layout array, direction by direction, over the full
+    transverse extent (the order of the generated halo exchanges)."""
+    h = spec.halo
+    for d in range(spec.ndim):
+        ax = spec.ndim - 1 - d
+        n = spec.size[d]
+        lo_dst = [slice(None)] * spec.ndim
+        lo_src = [slice(None)] * spec.ndim
+        hi_dst = [slice(None)] * spec.ndim
+        hi_src = [slice(None)] * spec.ndim
+        lo_dst[ax] = slice(h - depth, h)
+        lo_src[ax] = slice(h + n - depth, h + n)
+        hi_dst[ax] = slice(h + n, h + n + depth)
+        hi_src[ax] = slice(h, h + depth)
+        a[tuple(lo_dst)] = a[tuple(lo_src)]
+        a[tuple(hi_dst)] = a[tuple(hi_src)]
+
+
+def metrics_central4(spec, x, periodic_from_interior=False):
+    """Metric arrays of a block from its grid coordinates x[0..ndim-1] (OPS layout, known at
+    every allocated point), with 4th-order central derivatives (the reference's
+    MetricsEquation with central differences, opensbli/equation_types/metric.py).
+
+    periodic_from_interior=True evaluates them on the interior only and fills the halos by a
+    depth-5 periodic exchange, as the generated solver of a periodic curvilinear block does;
+    otherwise they are evaluated wherever the stencil fits and the outer two halo layers
+    repeat the nearest evaluated layer."""
+    nd = spec.ndim
+    J = [[_d1_central4(x[i], nd - 1 - j, 1.0 / spec.delta[j]) for j in range(nd)] for i in range(nd)]
+    met = [None] * 10
+    if nd == 2:
+        det = J[0][0] * J[1][1] - J[0][1] * J[1][0]
+        with np.errstate(divide="ignore", invalid="ignore"):
+            met[0] = J[1][1] / det
+            met[1] = -J[0][1] / det
+            met[3] = -J[1][0] / det
+            met[4] = J[0][0] / det
+        met[9] = det
+    else:
+        M = np.stack([np.stack(r, axis=-1) for r in J], axis=-2)  # [..., i, j] = d x_i / d xi_j
+        det = np.linalg.det(M)
+        good = det != 0.0
+        inv = np.zeros_like(M)
+        inv[good] = np.linalg.inv(M[good])  # [..., d, i] = d xi_d / d x_i
+        for d in range(3):
+            for i in range(3):
+                met[3 * d + i] = np.ascontiguousarray(inv[..., d, i])
+        met[9] = det
+    h = spec.halo
+    for k in range(10):
+        if met[k] is None:
+            continue
+        a = np.ascontiguousarray(met[k])
+        if periodic_from_interior:
+            b = np.zeros_like(a)
+            b[spec.interior()] = a[spec.interior()]
+            _periodic_fill(spec, b, h)
+            a = b
+        else:
+            core = tuple(slice(2, s - 2) for s in a.shape)
+            pad = [(2, 2)] * a.ndim
+            a = np.pad(a[core], pad, mode="edge")
+        met[k] = np.ascontiguousarray(a, dtype=np.float64)
+    return met
+
+
+def curvilinear_wave_2d(n=128, scheme=abi.SCHEME_WENO5_Z, averaging=abi.AVG_ROE):
+    """Density wave on a periodic wavy 2D mesh (the reference's curvilinear Euler verification
+    case, tests/verification_apps/euler_wave_curvilinear): Delta = 2/N,
+    x0 = i Delta + 0.04 sin(3 pi j Delta), x1 = j Delta + 0.04 sin(3 pi i Delta),
+    rho = 1 + 0.2 sin(pi (x0 + x1)), u = (1, -0.5), p = 1; metrics from 4th-order central
+    differences on the interior, exchanged periodically.  Returns (spec, state, metrics)."""
+    spec = BlockSpec(ndim=2, size=(n, n), scheme=scheme, averaging=averaging,
+                     bc=[[abi.BC_PERIODIC] * 2 for _ in range(2)], bc_depth=[[4, 4], [4, 4]],
+                     delta=(2.0 / n, 2.0 / n), gama=1.4)
+    i = spec.grid_index(0).astype(np.float64)
+    j = spec.grid_index(1).astype(np.float64)
+    d0, d1 = spec.delta[0], spec.delta[1]
+    x0 = np.broadcast_to(0.04 * np.sin(3 * math.pi * d1 * j) + d0 * i, spec.shape).copy()
+    x1 = np.broadcast_to(0.04 * np.sin(3 * math.pi * d0 * i) + d1 * j, spec.shape).copy()
+    rho = 1.0 + 0.2 * np.sin(math.pi * (x0 + x1))
+    q = _cons(spec, rho, [np.full(spec.shape, 1.0), np.full(spec.shape, -0.5)], 1.0)
+    return spec, q, metrics_central4(spec, [x0, x1], periodic_from_interior=True)

@@ -69,15 +69,21 @@ class OracleBlocks:
     """Host state of several blocks plus the C descriptors that point into it."""
 
     def __init__(self, specs_states, rkold=None):
-        self.specs = [s for s, _ in specs_states]
-        self.q = [[np.ascontiguousarray(a, dtype=np.float64).copy() for a in st] for _, st in specs_states]
+        """specs_states: (spec, state) or (spec, state, metrics) per block; metrics is the list
+        of 10 metric arrays of osb_block_desc.metric (None where unused)."""
+        self.specs = [t[0] for t in specs_states]
+        self.q = [[np.ascontiguousarray(a, dtype=np.float64).copy() for a in t[1]] for t in specs_states]
+        self.met = [None if len(t) < 3 or t[2] is None else
+                    [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in t[2]]
+                    for t in specs_states]
         if rkold is None:
             self.rk = [[np.zeros(s.shape) for _ in range(s.nvars)] for s in self.specs]
         else:
             self.rk = [[np.ascontiguousarray(a, dtype=np.float64).copy() for a in r] for r in rkold]
         arr = (abi.BlockDesc * len(self.specs))()
         for i, s in enumerate(self.specs):
-            arr[i] = abi.make_desc(s, [_ptr(a) for a in self.q[i]], [_ptr(a) for a in self.rk[i]])
+            mp = None if self.met[i] is None else [None if a is None else _ptr(a) for a in self.met[i]]
+            arr[i] = abi.make_desc(s, [_ptr(a) for a in self.q[i]], [_ptr(a) for a in self.rk[i]], mp)
         self.desc = arr
 
     def residual(self, ib=0):

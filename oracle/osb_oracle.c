@@ -341,6 +341,84 @@ static void char_flux_cart(const osb_block_desc* b, const geom_t* g, const cr_t*
   }
 }
 
+/* Curvilinear interface flux (k = D_d averaged, contravariant flux scaled by det J), as the
+ * generated "LFWeno_reconstruction" kernel of the curvilinear verification case
+ * (euler_eigensystem.py:19-51 apply_direction with metrics; metric.py). */
+static void char_flux_curv(const osb_block_desc* b, const geom_t* g, const cr_t* c, int d, long idc, double* fhat) {
+  const int nd = b->ndim, nv = nd + 2;
+  const long s = g->st[d];
+  const double gm = b->gama;
+  long iL = idc, iR = idc + s;
+  const double* J = b->metric[9];
+  double rho_av, u_av[3] = {0, 0, 0}, a_av;
+  if (b->averaging == OSB_AVG_ROE) {
+    double rL = b->q[0][iL], rR = b->q[0][iR];
+    double sL = sqrt(rL), sR = sqrt(rR);
+    rho_av = sqrt(rL * rR);
+    double inv = 1.0 / (sL + sR);
+    double ke = 0.0;
+    for (int i = 0; i < nd; ++i) {
+      u_av[i] = (sL * c->u[i][iL] + sR * c->u[i][iR]) * inv;
+      ke += u_av[i] * u_av[i];
+    }
+    double HL = (b->q[nv - 1][iL] + c->p[iL]) / rL, HR = (b->q[nv - 1][iR] + c->p[iR]) / rR;
+    a_av = sqrt((gm - 1.0) * ((sL * HL + sR * HR) * inv - 0.5 * ke));
+  } else {
+    rho_av = 0.5 * (b->q[0][iL] + b->q[0][iR]);
+    for (int i = 0; i < nd; ++i) u_av[i] = 0.5 * (c->u[i][iL] + c->u[i][iR]);
+    a_av = 0.5 * (c->a[iL] + c->a[iR]);
+  }
+  double kav[3] = {0, 0, 0}, kn = 0.0;
+  for (int i = 0; i < nd; ++i) {
+    kav[i] = 0.5 * (b->metric[3 * d + i][iL] + b->metric[3 * d + i][iR]);
+    kn += kav[i] * kav[i];
+  }
+  kn = 1.0 / sqrt(kn);
+  double kt[3] = {kav[0] * kn, kav[1] * kn, kav[2] * kn};
+  double L[NVMAX][NVMAX], R[NVMAX][NVMAX];
+  eigensystem(nd, gm, kt, rho_av, u_av, a_av, L, R);
+  double lam[NVMAX], evL[NVMAX], evR[NVMAX];
+  for (int side = 0; side < 2; ++side) {
+    long id = side ? iR : iL;
+    double k[3] = {0, 0, 0}, km = 0.0, u[3] = {0, 0, 0};
+    for (int i = 0; i < nd; ++i) {
+      k[i] = J[id] * b->metric[3 * d + i][id];
+      km += k[i] * k[i];
+      u[i] = c->u[i][id];
+    }
+    point_ev(nd, k, sqrt(km), u, c->a[id], side ? evR : evL);
+  }
+  for (int w = 0; w < nv; ++w) lam[w] = b->shock_filter_control * fmax(fabs(evL[w]), fabs(evR[w]));
+  double fp[NVMAX][6], fm[NVMAX][6];
+  for (int m = 0; m < 6; ++m) {
+    long id = idc + (long)(m - 2) * s;
+    double Q[NVMAX], F[NVMAX];
+    double U = 0.0;
+    for (int i = 0; i < nd; ++i) U += b->metric[3 * d + i][id] * c->u[i][id];
+    double p = c->p[id], dj = J[id];
+    for (int v = 0; v < nv; ++v) Q[v] = b->q[v][id];
+    F[0] = dj * (Q[0] * U);
+    for (int i = 0; i < nd; ++i) F[1 + i] = dj * (Q[1 + i] * U + p * b->metric[3 * d + i][id]);
+    F[nv - 1] = dj * ((Q[nv - 1] + p) * U);
+    for (int w = 0; w < nv; ++w) {
+      double cs = 0.0, cf = 0.0;
+      for (int v = 0; v < nv; ++v) { cs += L[w][v] * Q[v]; cf += L[w][v] * F[v]; }
+      fp[w][m] = 0.5 * (cf + lam[w] * cs);
+      fm[w][m] = 0.5 * (cf - lam[w] * cs);
+    }
+  }
+  double rec[NVMAX];
+  for (int w = 0; w < nv; ++w) {
+    double mir[5] = {fm[w][5], fm[w][4], fm[w][3], fm[w][2], fm[w][1]};
+    rec[w] = recon5(b->scheme, &fp[w][0], b->eps, b->teno_ct) + recon5(b->scheme, mir, b->eps, b->teno_ct);
+  }
+  for (int v = 0; v < nv; ++v) {
+    double acc = 0.0;
+    for (int w = 0; w < nv; ++w) acc += R[v][w] * rec[w];
+    fhat[v] = acc;
+  }
+}
+
 /* ---- central 4th-order operators (scheme.py:83-87 finite_diff_weights) --------------- */
 
 static inline double d1c(const double* f, long id, long s, double invd) {
@@ -464,7 +542,8 @@ int oracle_residual(const osb_block_desc* b, double* const* Rout) {
           for (int i = lo[0]; i < g.n[0]; ++i) {
             long id = gid(&g, i, j, k);
             double f[NVMAX];
-            char_flux_cart(b, &g, &c, d, id, f);
+            if (b->metric[9]) char_flux_curv(b, &g, &c, d, id, f);
+            else char_flux_cart(b, &g, &c, d, id, f);
             for (int v = 0; v < nv; ++v) fh[d][v][id] = f[v];
           }
     }
@@ -474,7 +553,13 @@ int oracle_residual(const osb_block_desc* b, double* const* Rout) {
           long id = gid(&g, i, j, k);
           for (int v = 0; v < nv; ++v) {
             double r = 0.0;
-            for (int d = 0; d < nd; ++d) r -= (fh[d][v][id] - fh[d][v][id - g.st[d]]) * (1.0 / b->delta[d]);
+            if (b->metric[9]) {
+              /* curvilinear: R = -(sum_d dF_d / Delta_d) / det J */
+              for (int d = 0; d < nd; ++d) r += (fh[d][v][id] - fh[d][v][id - g.st[d]]) * (1.0 / b->delta[d]);
+              r = -r / b->metric[9][id];
+            } else {
+              for (int d = 0; d < nd; ++d) r -= (fh[d][v][id] - fh[d][v][id - g.st[d]]) * (1.0 / b->delta[d]);
+            }
             Rout[v][id] = r;
           }
         }
@@ -592,18 +677,54 @@ static void zero_grad_face(osb_block_desc* b, const geom_t* g, int d, int side, 
       }
 }
 
-int oracle_apply_bc(osb_block_desc* blocks, int nblocks, int zero_grad_only) {
-  for (int ib = 0; ib < nblocks; ++ib) {
-    osb_block_desc* b = &blocks[ib];
-    geom_t g = geom_of(b);
-    for (int d = 0; d < b->ndim; ++d)
-      for (int side = 0; side < 2; ++side) {
-        int kind = b->bc[d][side];
-        int depth = b->bc_depth[d][side] > 0 ? b->bc_depth[d][side] : 4;
-        if (kind == OSB_BC_PERIODIC && !zero_grad_only) periodic_face(b, &g, d, side, depth);
-        if (kind == OSB_BC_ZERO_GRAD) zero_grad_face(b, &g, d, side, depth);
-      }
+/* Block interface (multi_block.py:11-107, identity orientation, matching faces normal to the
+ * same direction): the halo layers of face (d, side) receive the neighbour's layers adjacent to
+ * its face (d, f->side).  `full` = 0 copies the interior of the face only; `full` = 1 also the
+ * transverse halos (depth of this face), which the neighbour has filled by then. */
+static void interface_face(osb_block_desc* blocks, osb_block_desc* b, const geom_t* g, int d, int side, int depth,
+                           int full) {
+  const osb_interface* f = &b->iface[d][side];
+  osb_block_desc* nb = &blocks[f->block];
+  geom_t ng = geom_of(nb);
+  const int nv = b->ndim + 2;
+  int lo[3] = {0, 0, 0}, hi[3] = {1, 1, 1};
+  for (int e = 0; e < b->ndim; ++e) {
+    lo[e] = full ? -depth : 0;
+    hi[e] = g->n[e] + (full ? depth : 0);
   }
+  lo[d] = 0; hi[d] = depth;
+  const int Nn = ng.n[d];
+  for (int v = 0; v < nv; ++v)
+    for (int k = lo[2]; k < hi[2]; ++k)
+      for (int j = lo[1]; j < hi[1]; ++j)
+        for (int i = lo[0]; i < hi[0]; ++i) {
+          int dst[3] = {i, j, k}, src[3] = {i, j, k};
+          int layer = (d == 0 ? i : (d == 1 ? j : k));
+          dst[d] = side == 0 ? -depth + layer : g->n[d] + layer;
+          src[d] = f->side == 1 ? Nn - depth + layer : layer;
+          b->q[v][gid(g, dst[0], dst[1], dst[2])] = nb->q[v][gid(&ng, src[0], src[1], src[2])];
+        }
+}
+
+/* Boundary conditions of all blocks, in three passes: (A) interface faces, interior of the
+ * face; (B) per block, per direction, periodic and zero-gradient faces (their transverse
+ * ranges include the halos, so corners come from the layers filled before); (C) interface
+ * faces again with their transverse halos, now filled by the neighbour's own pass (B). */
+int oracle_apply_bc(osb_block_desc* blocks, int nblocks, int zero_grad_only) {
+  for (int pass = 0; pass < 3; ++pass)
+    for (int ib = 0; ib < nblocks; ++ib) {
+      osb_block_desc* b = &blocks[ib];
+      geom_t g = geom_of(b);
+      for (int d = 0; d < b->ndim; ++d)
+        for (int side = 0; side < 2; ++side) {
+          int kind = b->bc[d][side];
+          int depth = b->bc_depth[d][side] > 0 ? b->bc_depth[d][side] : 4;
+          if (pass == 1 && kind == OSB_BC_PERIODIC && !zero_grad_only) periodic_face(b, &g, d, side, depth);
+          if (pass == 1 && kind == OSB_BC_ZERO_GRAD) zero_grad_face(b, &g, d, side, depth);
+          if (pass != 1 && kind == OSB_BC_INTERFACE && !zero_grad_only)
+            interface_face(blocks, b, &g, d, side, depth, pass == 2);
+        }
+    }
   return 0;
 }
 

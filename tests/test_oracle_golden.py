@@ -18,6 +18,7 @@ CASES = {
                                 1e-11),
     "tgv_central_12": (lambda: problems.tgv(12, minf=0.1, scheme=abi.SCHEME_CENTRAL4), "ls3", None, 1e-12),
     "kh_weno5z_24_perturbed": (lambda: problems.kh(24, amp=1.0, phase=0.0), "sbli3", (1e-3, 12), 1e-9),
+    "curv_weno5z_32": (lambda: problems.curvilinear_wave_2d(32), "ls3", None, 1e-12),
 }
 
 
@@ -28,10 +29,10 @@ def perturb(q, amp, seed):
 
 def load_case(name):
     mk, rk, pert, tol = CASES[name]
-    spec, q = mk()
+    spec, q, *met = mk()
     if pert is not None:
         q = perturb(q, *pert)
-    return spec, q, rk, tol, np.load(os.path.join(GOLD, name + ".npz"))
+    return (spec, q) + tuple(met), rk, tol, np.load(os.path.join(GOLD, name + ".npz"))
 
 
 def rk_params(rk):
@@ -55,8 +56,9 @@ def advance(ob, spec, rk, dt, nstages):
 
 @pytest.mark.parametrize("name", sorted(CASES))
 def test_initial_state_matches_golden(oracle_lib, name):
-    spec, q, rk, tol, g = load_case(name)
-    ob = harness.OracleBlocks([(spec, q)])
+    blk, rk, tol, g = load_case(name)
+    spec = blk[0]
+    ob = harness.OracleBlocks([blk])
     ob.apply_bc()
     sl = spec.interior()
     ic = np.stack([ob.q[0][v][sl] for v in range(spec.nvars)])
@@ -65,9 +67,12 @@ def test_initial_state_matches_golden(oracle_lib, name):
 
 @pytest.mark.parametrize("name", sorted(CASES))
 def test_oracle_residual_matches_reference(oracle_lib, name):
-    spec, q, rk, tol, g = load_case(name)
-    ob = harness.OracleBlocks([(spec, q)])
+    blk, rk, tol, g = load_case(name)
+    spec = blk[0]
+    ob = harness.OracleBlocks([blk])
     ob.apply_bc()
+    if "residual_1" not in g:
+        pytest.skip("the reference solver of this case keeps no residual arrays")
     R = ob.residual(0)
     sl = spec.interior()
     for v in range(spec.nvars):
@@ -76,16 +81,30 @@ def test_oracle_residual_matches_reference(oracle_lib, name):
 
 @pytest.mark.parametrize("name", sorted(CASES))
 def test_oracle_states_match_reference(oracle_lib, name):
-    spec, q, rk, tol, g = load_case(name)
+    blk, rk, tol, g = load_case(name)
+    spec = blk[0]
     dt = float(g["dt"])
     sl = spec.interior()
     for n in g["counts"]:
         n = int(n)
         if n > 300 and os.environ.get("OSB_FAST_TESTS"):
             continue
-        ob = harness.OracleBlocks([(spec, q)])
+        ob = harness.OracleBlocks([blk])
         ob.apply_bc()
         advance(ob, spec, rk, dt, n)
         ref = g["after_%d" % n]
         errs = [harness.rel_err(ob.q[0][v][sl], ref[v]) for v in range(spec.nvars)]
         assert max(errs) < (tol if n < 300 else 100 * tol), (n, errs)
+
+
+def test_curvilinear_known_answer(oracle_lib):
+    """The reference's own known answer for its curvilinear Euler verification case
+    (tests/verification_apps/euler_wave_curvilinear/check_opensbli_output.py): rho at array
+    index [69, 69] of the halo-inclusive 138 x 138 output, after 10 steps of dt 5e-4 on 128^2,
+    is 0.9984292346559068 to 1e-9 relative."""
+    spec, q, met = problems.curvilinear_wave_2d(128)
+    ob = harness.OracleBlocks([(spec, q, met)])
+    ob.apply_bc()
+    ob.step(abi.RK_LOW_STORAGE, problems.RK3_LS_A, problems.RK3_LS_B, 5e-4, 10)
+    rho = ob.q[0][0][69, 69]
+    assert abs(rho - 0.9984292346559068) < 1e-9 * 0.9984292346559068, rho
