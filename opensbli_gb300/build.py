@@ -1,6 +1,7 @@
 """In-tree build of libosb_gb300.so for sm_103a.
 
-The flux sweeps are compiled once per (precision, dimension) into separate objects so the
+The flux sweeps are compiled once per (precision, dimension, Cartesian or curvilinear) into
+separate objects so the
 translation units build in parallel; the objects go to opensbli_gb300/_build and the library
 to opensbli_gb300/libosb_gb300.so (both git-ignored).
 """
@@ -32,6 +33,11 @@ UNITS = [
      ["-DOSB_T=%s" % ("double" if p == "f64" else "float"), "-DOSB_ND=%d" % nd, "-DOSB_NAME=flux_%s_%dd" % (p, nd)]
      + (FAST if p == "f32" else []))
     for p in ("f64", "f32") for nd in (1, 2, 3)
+] + [
+    ("flux_curv_%s_%dd" % (p, nd), "osb_flux.cu",
+     ["-DOSB_T=%s" % ("double" if p == "f64" else "float"), "-DOSB_ND=%d" % nd, "-DOSB_CURV=true",
+      "-DOSB_NAME=flux_curv_%s_%dd" % (p, nd)] + (FAST if p == "f32" else []))
+    for p in ("f64", "f32") for nd in (2, 3)
 ]
 
 

@@ -1,5 +1,6 @@
 // osb_flux.cu -- launches of the characteristic flux sweeps, compiled once per precision
-// (OSB_T) and dimension (OSB_ND) so the instantiations build in parallel.
+// (OSB_T), dimension (OSB_ND) and grid kind (OSB_CURV: curvilinear metrics) so the
+// instantiations build in parallel.
 #include <algorithm>
 
 #include "osb_internal.h"
@@ -9,19 +10,22 @@
 #define OSB_ND 3
 #define OSB_NAME flux_f64_3d
 #endif
+#ifndef OSB_CURV
+#define OSB_CURV false
+#endif
 
 namespace osb {
 namespace {
 
-template <typename T, int ND, int SCH, int AVG>
+template <typename T, int ND, int SCH, int AVG, bool CURV>
 int launch_flux(osb_ctx* c, Block& bl, const SchemeParams& sp) {
   BlockK& k = bl.k;
   cudaStream_t st = c->stream;
   // x sweep (writes R)
   {
-    constexpr int NV = ND + 2;
-    size_t smem = (size_t)XWARPS * NV * 32 * XPITCH * sizeof(T);
-    auto kern = k_flux_x<T, ND, SCH, AVG>;
+    constexpr int NF = SweepFields<ND, CURV>::N;
+    size_t smem = (size_t)XWARPS * NF * 32 * XPITCH * sizeof(T);
+    auto kern = k_flux_x<T, ND, SCH, AVG, CURV>;
     OSB_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int nrows = k.n[1] * k.n[2];
     dim3 grid((k.n[0] + XSEG - 1) / XSEG, (nrows + 32 * XWARPS - 1) / (32 * XWARPS));
@@ -43,25 +47,25 @@ int launch_flux(osb_ctx* c, Block& bl, const SchemeParams& sp) {
     dim3 grid((k.n[0] + 127) / 128, (unsigned)std::min(gy, 65535L), (unsigned)((gy + 65534) / 65535));
     if (grid.z > 1) return fail(OSB_ENOTSUP, "block too large for the sweep grid");
     timing_begin(c, D == 1 ? FAM_FLUX_Y : FAM_FLUX_Z);
-    if (D == 1) k_flux_sweep<T, ND, 1, SCH, AVG><<<grid, 128, 0, st>>>(k, sp, seg, nseg, 0);
-    else if (ND == 3) k_flux_sweep<T, ND, (ND == 3 ? 2 : 1), SCH, AVG><<<grid, 128, 0, st>>>(k, sp, seg, nseg, 0);
+    if (D == 1) k_flux_sweep<T, ND, 1, SCH, AVG, CURV><<<grid, 128, 0, st>>>(k, sp, seg, nseg, 0);
+    else if (ND == 3) k_flux_sweep<T, ND, (ND == 3 ? 2 : 1), SCH, AVG, CURV><<<grid, 128, 0, st>>>(k, sp, seg, nseg, 0);
     timing_end(c);
     c->launches++;
   }
   return OSB_OK;
 }
 
-template <typename T, int ND>
+template <typename T, int ND, bool CURV>
 int dispatch_flux_nd(osb_ctx* c, Block& bl, const SchemeParams& sp) {
   const int sch = bl.d.scheme, avg = bl.d.averaging;
   if (avg == OSB_AVG_ROE) {
-    if (sch == OSB_SCHEME_WENO5_JS) return launch_flux<T, ND, SCH_WENO5_JS, AVG_ROE>(c, bl, sp);
-    if (sch == OSB_SCHEME_WENO5_Z) return launch_flux<T, ND, SCH_WENO5_Z, AVG_ROE>(c, bl, sp);
-    if (sch == OSB_SCHEME_TENO5) return launch_flux<T, ND, SCH_TENO5, AVG_ROE>(c, bl, sp);
+    if (sch == OSB_SCHEME_WENO5_JS) return launch_flux<T, ND, SCH_WENO5_JS, AVG_ROE, CURV>(c, bl, sp);
+    if (sch == OSB_SCHEME_WENO5_Z) return launch_flux<T, ND, SCH_WENO5_Z, AVG_ROE, CURV>(c, bl, sp);
+    if (sch == OSB_SCHEME_TENO5) return launch_flux<T, ND, SCH_TENO5, AVG_ROE, CURV>(c, bl, sp);
   } else {
-    if (sch == OSB_SCHEME_WENO5_JS) return launch_flux<T, ND, SCH_WENO5_JS, AVG_SIMPLE>(c, bl, sp);
-    if (sch == OSB_SCHEME_WENO5_Z) return launch_flux<T, ND, SCH_WENO5_Z, AVG_SIMPLE>(c, bl, sp);
-    if (sch == OSB_SCHEME_TENO5) return launch_flux<T, ND, SCH_TENO5, AVG_SIMPLE>(c, bl, sp);
+    if (sch == OSB_SCHEME_WENO5_JS) return launch_flux<T, ND, SCH_WENO5_JS, AVG_SIMPLE, CURV>(c, bl, sp);
+    if (sch == OSB_SCHEME_WENO5_Z) return launch_flux<T, ND, SCH_WENO5_Z, AVG_SIMPLE, CURV>(c, bl, sp);
+    if (sch == OSB_SCHEME_TENO5) return launch_flux<T, ND, SCH_TENO5, AVG_SIMPLE, CURV>(c, bl, sp);
   }
   return fail(OSB_ENOTSUP, "unsupported scheme/averaging %d/%d", sch, avg);
 }
@@ -70,6 +74,8 @@ int dispatch_flux_nd(osb_ctx* c, Block& bl, const SchemeParams& sp) {
 
 }  // namespace
 
-int OSB_NAME(osb_ctx* c, Block& bl, const SchemeParams& sp) { return dispatch_flux_nd<OSB_T, OSB_ND>(c, bl, sp); }
+int OSB_NAME(osb_ctx* c, Block& bl, const SchemeParams& sp) {
+  return dispatch_flux_nd<OSB_T, OSB_ND, OSB_CURV>(c, bl, sp);
+}
 
 }  // namespace osb

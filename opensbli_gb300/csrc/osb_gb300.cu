@@ -186,6 +186,46 @@ __global__ void k_zero_grad(BlockK b, int nv, int d, int side, int depth) {
   }
 }
 
+// Block interface (multi_block.py:11-107, InterfaceBC with identity orientation): the halo
+// layers of face (d, side) of dst receive the `depth` layers of src next to its face
+// (d, sside).  The transverse range is the interior of the face (full = 0) or that plus
+// `depth` halo points on each side (full = 1).
+__global__ void k_interface(BlockK dst, BlockK src, int nv, int d, int side, int sside, int depth, int full) {
+  int ext[3], lo[3];
+  for (int e = 0; e < 3; ++e) {
+    if (e < dst.ndim && e != d) {
+      lo[e] = full ? -depth : 0;
+      ext[e] = dst.n[e] + (full ? 2 * depth : 0);
+    } else {
+      lo[e] = 0;
+      ext[e] = 1;
+    }
+  }
+  ext[d] = depth;
+  const long total = (long)ext[0] * ext[1] * ext[2] * nv;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+    long r = t;
+    int c[3];
+    c[0] = (int)(r % ext[0]); r /= ext[0];
+    c[1] = (int)(r % ext[1]); r /= ext[1];
+    c[2] = (int)(r % ext[2]);
+    const int v = (int)(r / ext[2]);
+    int di[3], si[3];
+    for (int e = 0; e < 3; ++e) di[e] = si[e] = c[e] + lo[e];
+    di[d] = side == 0 ? -depth + c[d] : dst.n[d] + c[d];
+    si[d] = sside == 1 ? src.n[d] - depth + c[d] : c[d];
+    const int a = lin(dst, di[0], di[1], di[2]), bsrc = lin(src, si[0], si[1], si[2]);
+    dst.q[v][a] = src.q[v][bsrc];
+    if (dst.qf[0]) dst.qf[v][a] = src.qf[v][bsrc];
+  }
+}
+
+// FP32 copy of a metric array (rounded to nearest).
+__global__ void k_metric_f32(const double* m, float* out, long n) {
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x)
+    out[t] = d2f_rn(m[t]);
+}
+
 // ---------------------------------------------------------------------------------------
 // Reductions (compressible_TGV.py:176-206 and the CFL / NaN checks), FP64.
 __device__ __forceinline__ double uval(const BlockK& b, int v, long id) { return b.q[v][id] / b.q[0][id]; }
@@ -353,8 +393,14 @@ int residual_t(osb_ctx* c, Block& bl) {
     rc = sizeof(T) == 4 ? central_f32(c, bl, true, 1) : central_f64(c, bl, true, 1);
   } else {
     const int nd = bl.d.ndim;
-    if (sizeof(T) == 4) rc = nd == 1 ? flux_f32_1d(c, bl, sp) : nd == 2 ? flux_f32_2d(c, bl, sp) : flux_f32_3d(c, bl, sp);
-    else rc = nd == 1 ? flux_f64_1d(c, bl, sp) : nd == 2 ? flux_f64_2d(c, bl, sp) : flux_f64_3d(c, bl, sp);
+    if (bl.k.m[9]) {
+      if (sizeof(T) == 4) rc = nd == 2 ? flux_curv_f32_2d(c, bl, sp) : flux_curv_f32_3d(c, bl, sp);
+      else rc = nd == 2 ? flux_curv_f64_2d(c, bl, sp) : flux_curv_f64_3d(c, bl, sp);
+    } else if (sizeof(T) == 4) {
+      rc = nd == 1 ? flux_f32_1d(c, bl, sp) : nd == 2 ? flux_f32_2d(c, bl, sp) : flux_f32_3d(c, bl, sp);
+    } else {
+      rc = nd == 1 ? flux_f64_1d(c, bl, sp) : nd == 2 ? flux_f64_2d(c, bl, sp) : flux_f64_3d(c, bl, sp);
+    }
     if (rc == OSB_OK && bl.d.viscous != OSB_VISC_NONE) {
       if (bl.d.ndim != 3) return fail(OSB_ENOTSUP, "viscous terms implemented for 3D blocks");
       rc = sizeof(T) == 4 ? central_f32(c, bl, false, 0) : central_f64(c, bl, false, 0);
@@ -373,7 +419,54 @@ int grid_for(osb_ctx* c, long n, int threads) {
   return (int)std::max(1L, std::min(g, cap));
 }
 
+// Interface faces of every block: the interior of each face (full = 0) or the face with its
+// transverse halos (full = 1).
+int apply_interfaces(osb_ctx* c, int full) {
+  for (size_t ib = 0; ib < c->blocks.size(); ++ib) {
+    Block& bl = c->blocks[ib];
+    const int nv = bl.d.ndim + 2;
+    for (int d = 0; d < bl.d.ndim; ++d)
+      for (int side = 0; side < 2; ++side) {
+        if (bl.d.bc[d][side] != OSB_BC_INTERFACE) continue;
+        const osb_interface& f = bl.d.iface[d][side];
+        if (f.block < 0 || f.block >= (int)c->blocks.size())
+          return fail(OSB_EINVAL, "interface of block %zu dir %d side %d names block %d of %zu", ib, d, side, f.block,
+                      c->blocks.size());
+        const Block& nb = c->blocks[f.block];
+        for (int e = 0; e < bl.d.ndim; ++e)
+          if (e != d && nb.k.n[e] != bl.k.n[e])
+            return fail(OSB_EINVAL, "interface of block %zu dir %d: transverse size %d != %d of block %d", ib, d,
+                        bl.k.n[e], nb.k.n[e], f.block);
+        const int depth = bl.d.bc_depth[d][side] > 0 ? bl.d.bc_depth[d][side] : 4;
+        if (depth > nb.k.n[d])
+          return fail(OSB_EINVAL, "interface depth %d exceeds the %d points of block %d", depth, nb.k.n[d], f.block);
+        if ((bl.k.qf[0] != nullptr) != (nb.k.qf[0] != nullptr))
+          return fail(OSB_EINVAL, "interface between blocks of different precision");
+        long total = (long)depth * nv;
+        for (int e = 0; e < bl.d.ndim; ++e)
+          if (e != d) total *= bl.k.n[e] + (full ? 2 * depth : 0);
+        timing_begin(c, FAM_BC);
+        k_interface<<<grid_for(c, total, 256), 256, 0, c->stream>>>(bl.k, nb.k, nv, d, side, f.side, depth, full);
+        timing_end(c);
+        c->launches++;
+      }
+  }
+  return OSB_OK;
+}
+
+// Boundary conditions of all blocks: interface faces (interior of the face), then each
+// block's periodic and zero-gradient faces direction by direction (transverse ranges include
+// the halos, so corners come from layers filled before), then the interface faces again with
+// their transverse halos, which the neighbour has filled by then.
 int apply_bc(osb_ctx* c) {
+  bool any_iface = false;
+  for (auto& bl : c->blocks)
+    for (int d = 0; d < bl.d.ndim; ++d)
+      any_iface = any_iface || bl.d.bc[d][0] == OSB_BC_INTERFACE || bl.d.bc[d][1] == OSB_BC_INTERFACE;
+  if (any_iface) {
+    int rc = apply_interfaces(c, 0);
+    if (rc) return rc;
+  }
   for (size_t ib = 0; ib < c->blocks.size(); ++ib) {
     Block& bl = c->blocks[ib];
     const int nv = bl.d.ndim + 2;
@@ -403,13 +496,12 @@ int apply_bc(osb_ctx* c) {
             c->launches++;
           } else if (kind == OSB_BC_PERIODIC) {
             return fail(OSB_EINVAL, "periodic boundary on one side only (block %zu dir %d)", ib, d);
-          } else if (kind == OSB_BC_INTERFACE) {
-            return fail(OSB_ENOTSUP, "block interfaces are not supported by this build");
           }
         }
       }
     }
   }
+  if (any_iface) return apply_interfaces(c, 1);
   return OSB_OK;
 }
 
@@ -487,6 +579,29 @@ bool check_desc(const osb_block_desc* d, std::string& why) {
       if (dep < 0 || dep > 5) { why = "boundary depth must be 0..5"; return false; }
     }
   if (d->gama <= 1.0) { why = "gama must exceed 1"; return false; }
+  bool curv = false;
+  for (int i = 0; i < 10; ++i) curv = curv || d->metric[i] != nullptr;
+  if (curv) {
+    if (d->ndim < 2) { why = "curvilinear blocks are 2D or 3D"; return false; }
+    for (int dd = 0; dd < d->ndim; ++dd)
+      for (int i = 0; i < d->ndim; ++i)
+        if (!d->metric[3 * dd + i]) { why = "metric D" + std::to_string(dd) + std::to_string(i) + " missing"; return false; }
+    if (!d->metric[9]) { why = "metric detJ missing"; return false; }
+    if (d->scheme == OSB_SCHEME_CENTRAL4 || d->viscous != OSB_VISC_NONE) {
+      why = "curvilinear blocks take the characteristic Euler flux only (no central or viscous terms)";
+      return false;
+    }
+  }
+  for (int i = 0; i < d->ndim; ++i)
+    for (int s = 0; s < 2; ++s) {
+      if (d->bc[i][s] != OSB_BC_INTERFACE) continue;
+      const osb_interface& f = d->iface[i][s];
+      if (f.dir != i || f.flip != 0) {
+        why = "interfaces connect faces normal to the same direction without flips";
+        return false;
+      }
+      if (f.side != 0 && f.side != 1) { why = "interface side must be 0 or 1"; return false; }
+    }
   return true;
 }
 
@@ -559,6 +674,7 @@ int osb_ctx_destroy(osb_ctx* c) {
   for (auto& bl : c->blocks) {
     if (bl.k.R[0]) cudaFree(bl.k.R[0]);
     if (bl.k.qf[0]) cudaFree(bl.k.qf[0]);
+    if (bl.mf_buf) cudaFree(bl.mf_buf);
   }
   if (c->red) cudaFree(c->red);
   if (c->bad) cudaFree(c->bad);
@@ -577,8 +693,6 @@ int osb_block_add(osb_ctx* c, const osb_block_desc* d, int* block_id) {
     if (f.ndim != d->ndim || f.scheme != d->scheme || f.averaging != d->averaging || f.viscous != d->viscous)
       return fail(OSB_EINVAL, "blocks of one context must share ndim, scheme, averaging and viscosity");
   }
-  for (int i = 0; i < 10; ++i)
-    if (d->metric[i]) return fail(OSB_ENOTSUP, "curvilinear metrics are not supported by this build");
   OSB_CK(cudaSetDevice(c->device));
   Block bl;
   bl.d = *d;
@@ -621,6 +735,26 @@ int osb_block_add(osb_ctx* c, const osb_block_desc* d, int* block_id) {
       return fail(OSB_ECUDA, "FP32 shadow: %s", cudaGetErrorString(e));
     }
     for (int v = 0; v < nv; ++v) k.qf[v] = qf + (size_t)v * k.alloc;
+  }
+  for (int i = 0; i < 10; ++i) k.m[i] = d->metric[i];
+  if (k.m[9] && c->prec == OSB_PREC_FP32_RESIDUAL) {
+    int nm = 0;
+    for (int i = 0; i < 10; ++i) nm += k.m[i] ? 1 : 0;
+    float* mf = nullptr;
+    cudaError_t e = cudaMalloc(&mf, sizeof(float) * k.alloc * nm);
+    if (e != cudaSuccess) {
+      cudaFree(R);
+      cudaFree(k.qf[0]);
+      return fail(OSB_ECUDA, "FP32 metrics: %s", cudaGetErrorString(e));
+    }
+    bl.mf_buf = mf;
+    for (int i = 0, j = 0; i < 10; ++i) {
+      if (!k.m[i]) continue;
+      k.mf[i] = mf + (size_t)(j++) * k.alloc;
+      k_metric_f32<<<grid_for(c, k.alloc, 256), 256, 0, c->stream>>>(k.m[i], const_cast<float*>(k.mf[i]), k.alloc);
+      c->launches++;
+    }
+    OSB_CK(cudaGetLastError());
   }
   c->blocks.push_back(bl);
   drop_graph(c);
@@ -868,7 +1002,7 @@ extern "C" int osb_stage_noalloc(const osb_block_desc* d, int rk_kind, double A,
   if (!check_desc(d, why)) return fail(OSB_EINVAL, "invalid block descriptor: %s", why.c_str());
   if (rk_kind != OSB_RK_LOW_STORAGE && rk_kind != OSB_RK_SBLI3) return fail(OSB_EINVAL, "unknown RK kind");
   for (int i = 0; i < 10; ++i)
-    if (d->metric[i]) return fail(OSB_ENOTSUP, "curvilinear metrics are not supported by this build");
+    if (d->metric[i]) return fail(OSB_ENOTSUP, "osb_stage_noalloc takes Cartesian blocks only");
   const int nv = d->ndim + 2;
   size_t alloc = 1;
   for (int i = 0; i < d->ndim; ++i) alloc *= (size_t)(d->size[i] + 2 * d->halo);

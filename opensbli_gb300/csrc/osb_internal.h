@@ -21,6 +21,7 @@ int fail(int code, const char* fmt, ...);
 struct Block {
   osb_block_desc d;
   BlockK k;
+  float* mf_buf = nullptr;  // FP32 copies of the metrics (FP32-residual path, curvilinear)
 };
 
 // Kernel families for per-kernel timing (osb_timing_report).
@@ -74,6 +75,11 @@ int flux_f64_3d(osb_ctx* c, Block& bl, const SchemeParams& sp);
 int flux_f32_1d(osb_ctx* c, Block& bl, const SchemeParams& sp);
 int flux_f32_2d(osb_ctx* c, Block& bl, const SchemeParams& sp);
 int flux_f32_3d(osb_ctx* c, Block& bl, const SchemeParams& sp);
+// The same for curvilinear blocks (metric arrays present).
+int flux_curv_f64_2d(osb_ctx* c, Block& bl, const SchemeParams& sp);
+int flux_curv_f64_3d(osb_ctx* c, Block& bl, const SchemeParams& sp);
+int flux_curv_f32_2d(osb_ctx* c, Block& bl, const SchemeParams& sp);
+int flux_curv_f32_3d(osb_ctx* c, Block& bl, const SchemeParams& sp);
 // Central convective and/or viscous terms of one 3D block (osb_central.cu).
 int central_f64(osb_ctx* c, Block& bl, bool conv, int first);
 int central_f32(osb_ctx* c, Block& bl, bool conv, int first);

@@ -26,6 +26,8 @@ struct BlockK {
   float* qf[5];    // FP32 shadow of q (FP32-residual path; null otherwise)
   float* Rh[5];    // FP32-residual path: residual as a float-float pair (hi + lo) ...
   float* Rl[5];    // ... stored in the same bytes as the FP64 residual
+  const double* m[10];  // curvilinear metrics (D_di at 3*d+i, det J at 9); null: Cartesian
+  const float* mf[10];  // FP32 copies of the metrics (FP32-residual path)
   double invd[3];  // 1/Delta
   double inv2d[3]; // 1/Delta^2
 };
@@ -101,6 +103,54 @@ __device__ __forceinline__ double ld_q<double>(const BlockK& b, int v, int id) {
 template <>
 __device__ __forceinline__ float ld_q<float>(const BlockK& b, int v, int id) { return __ldg(b.qf[v] + id); }
 
+// Local-frame variable order of a sweep along direction D: global index of local variable lv.
+template <int ND, int D>
+__device__ __forceinline__ int gvar_fwd(int lv) {
+  if (lv == 0) return 0;
+  if (lv == ND + 1) return ND + 1;
+  int t = lv - 1;  // 0 = normal, 1.. = tangential
+  if (ND == 3) return 1 + (D + t) % 3;
+  if (ND == 2) return 1 + (t == 0 ? D : 1 - D);
+  return 1;
+}
+
+template <typename T>
+__device__ __forceinline__ T ld_m(const BlockK& b, int c, int id);
+template <>
+__device__ __forceinline__ double ld_m<double>(const BlockK& b, int c, int id) { return __ldg(b.m[c] + id); }
+template <>
+__device__ __forceinline__ float ld_m<float>(const BlockK& b, int c, int id) { return __ldg(b.mf[c] + id); }
+
+// Fields a sweep along D reads per point: the conserved variables, plus (curvilinear) the
+// metric row D_D0..D_D(ND-1) and det J.  gfield maps a field to its local-frame variable
+// (Cartesian sweeps) or to a metric component.
+template <int ND, bool CURV>
+struct SweepFields {
+  static constexpr int NV = ND + 2;
+  static constexpr int N = CURV ? NV + ND + 1 : NV;
+};
+template <typename T, int ND, int D, bool CURV>
+__device__ __forceinline__ T ld_field(const BlockK& b, int f, int id) {
+  constexpr int NV = ND + 2;
+  if (!CURV) return ld_q<T>(b, gvar_fwd<ND, D>(f), id);
+  if (f < NV) return ld_q<T>(b, f, id);
+  if (f < NV + ND) return ld_m<T>(b, 3 * D + (f - NV), id);
+  return ld_m<T>(b, 9, id);
+}
+template <typename T, int ND>
+__device__ __forceinline__ void set_field(Pt<T, ND>& s, int f, T v) { s.q[f] = v; }
+template <typename T, int ND>
+__device__ __forceinline__ void set_field(PtC<T, ND>& s, int f, T v) {
+  constexpr int NV = ND + 2;
+  if (f < NV) s.q[f] = v;
+  else if (f < NV + ND) s.k[f - NV] = v;
+  else s.J = v;
+}
+template <typename T, int ND, bool CURV>
+struct SweepPt { using type = Pt<T, ND>; };
+template <typename T, int ND>
+struct SweepPt<T, ND, true> { using type = PtC<T, ND>; };
+
 // Residual update of one variable at linear index id with -(fnew - fold)*invd.
 __device__ __forceinline__ void acc_flux(const BlockK& b, int v, int id, double fnew, double fold, double invd,
                                          int first) {
@@ -142,22 +192,19 @@ __device__ __forceinline__ int lin(const BlockK& b, int i, int j, int k) {
   return b.off0 + i * b.st[0] + j * b.st[1] + k * b.st[2];
 }
 
-// Local-frame variable order of a sweep along direction D: global index of local variable lv.
-template <int ND, int D>
+// Global variable of local variable lv of a sweep along D (identity for curvilinear sweeps).
+template <int ND, int D, bool CURV>
 __device__ __forceinline__ int gvar(int lv) {
-  if (lv == 0) return 0;
-  if (lv == ND + 1) return ND + 1;
-  int t = lv - 1;  // 0 = normal, 1.. = tangential
-  if (ND == 3) return 1 + (D + t) % 3;
-  if (ND == 2) return 1 + (t == 0 ? D : 1 - D);
-  return 1;
+  return CURV ? lv : gvar_fwd<ND, D>(lv);
 }
 
 // ---------------------------------------------------------------------------------------
 // Sweep along y (D=1) or z (D=2): thread = (x, transverse, segment).
-template <typename T, int ND, int D, int SCH, int AVG>
+template <typename T, int ND, int D, int SCH, int AVG, bool CURV>
 __global__ void __launch_bounds__(128) k_flux_sweep(BlockK b, SchemeParams spd, int seg, int nseg, int first) {
   constexpr int NV = ND + 2;
+  constexpr int NF = SweepFields<ND, CURV>::N;
+  using P = typename SweepPt<T, ND, CURV>::type;
   const SP<T> sp(spd);
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int other = blockIdx.y / nseg, sidx = blockIdx.y % nseg;
@@ -176,20 +223,20 @@ __global__ void __launch_bounds__(128) k_flux_sweep(BlockK b, SchemeParams spd, 
   if (j0 >= j1) return;
   const T gm = sp.gama;
   const T invd = (T)b.invd[D];
-  Pt<T, ND> w[6];
+  P w[6];
 #pragma unroll
   for (int m = 1; m < 6; ++m) {
     int id = base + (j0 - 4 + m) * s;
 #pragma unroll
-    for (int lv = 0; lv < NV; ++lv) w[m].q[lv] = ld_q<T>(b, gvar<ND, D>(lv), id);
+    for (int f = 0; f < NF; ++f) set_field(w[m], f, ld_field<T, ND, D, CURV>(b, f, id));
     make_pt<T, ND>(w[m], gm);
   }
-  // the state of point j+3 is loaded one step ahead (point j+4 <= N+3 stays inside the halo)
-  T nxt[NV];
+  // the fields of point j+3 are loaded one step ahead (point j+4 <= N+3 stays inside the halo)
+  T nxt[NF];
   {
     int id = base + (j0 + 2) * s;
 #pragma unroll
-    for (int lv = 0; lv < NV; ++lv) nxt[lv] = ld_q<T>(b, gvar<ND, D>(lv), id);
+    for (int f = 0; f < NF; ++f) nxt[f] = ld_field<T, ND, D, CURV>(b, f, id);
   }
   T fprev[NV];
 #pragma unroll
@@ -198,19 +245,25 @@ __global__ void __launch_bounds__(128) k_flux_sweep(BlockK b, SchemeParams spd, 
 #pragma unroll
     for (int m = 0; m < 5; ++m) w[m] = w[m + 1];
 #pragma unroll
-    for (int lv = 0; lv < NV; ++lv) w[5].q[lv] = nxt[lv];
+    for (int f = 0; f < NF; ++f) set_field(w[5], f, nxt[f]);
     {
       int id = base + (j + 4) * s;
 #pragma unroll
-      for (int lv = 0; lv < NV; ++lv) nxt[lv] = ld_q<T>(b, gvar<ND, D>(lv), id);
+      for (int f = 0; f < NF; ++f) nxt[f] = ld_field<T, ND, D, CURV>(b, f, id);
     }
     make_pt<T, ND>(w[5], gm);
     T fh[NV];
-    char_flux<T, ND, SCH, AVG>(w, sp, fh);
+    T sc = invd;
+    if constexpr (CURV) {
+      char_flux_curv<T, ND, SCH, AVG>(w, sp, fh);
+      sc = invd / w[2].J;
+    } else {
+      char_flux<T, ND, SCH, AVG>(w, sp, fh);
+    }
     if (j >= j0) {
       int id = base + j * s;
 #pragma unroll
-      for (int lv = 0; lv < NV; ++lv) acc_flux(b, gvar<ND, D>(lv), id, fh[lv], fprev[lv], invd, first);
+      for (int lv = 0; lv < NV; ++lv) acc_flux(b, gvar<ND, D, CURV>(lv), id, fh[lv], fprev[lv], sc, first);
     }
 #pragma unroll
     for (int lv = 0; lv < NV; ++lv) fprev[lv] = fh[lv];
@@ -225,13 +278,15 @@ constexpr int XSEG = 26;
 constexpr int XPITCH = 33;
 constexpr int XWARPS = 2;
 
-template <typename T, int ND, int SCH, int AVG>
+template <typename T, int ND, int SCH, int AVG, bool CURV>
 __global__ void __launch_bounds__(32 * XWARPS) k_flux_x(BlockK b, SchemeParams spd, int first) {
   constexpr int NV = ND + 2;
+  constexpr int NF = SweepFields<ND, CURV>::N;
+  using P = typename SweepPt<T, ND, CURV>::type;
   const SP<T> sp(spd);
   extern __shared__ __align__(16) unsigned char osb_smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  T* tile = reinterpret_cast<T*>(osb_smem) + (size_t)warp * NV * 32 * XPITCH;
+  T* tile = reinterpret_cast<T*>(osb_smem) + (size_t)warp * NF * 32 * XPITCH;
   const int nrows = b.n[1] * b.n[2];
   const int row0 = (blockIdx.y * XWARPS + warp) * 32;
   const int s0 = blockIdx.x * XSEG;
@@ -246,7 +301,7 @@ __global__ void __launch_bounds__(32 * XWARPS) k_flux_x(BlockK b, SchemeParams s
     if (col <= s1 + 2) {
       int id = lin(b, col, y, z);
 #pragma unroll
-      for (int v = 0; v < NV; ++v) tile[(v * 32 + r) * XPITCH + lane] = ld_q<T>(b, v, id);
+      for (int f = 0; f < NF; ++f) tile[(f * 32 + r) * XPITCH + lane] = ld_field<T, ND, 0, CURV>(b, f, id);
     }
   }
   __syncwarp();
@@ -256,12 +311,12 @@ __global__ void __launch_bounds__(32 * XWARPS) k_flux_x(BlockK b, SchemeParams s
   const int base = lin(b, 0, y, z);
   const T gm = sp.gama;
   const T invd = (T)b.invd[0];
-  Pt<T, ND> w[6];
+  P w[6];
 #pragma unroll
   for (int m = 1; m < 6; ++m) {
     int col = m - 1;  // point s0-3+col
 #pragma unroll
-    for (int v = 0; v < NV; ++v) w[m].q[v] = tile[(v * 32 + lane) * XPITCH + col];
+    for (int f = 0; f < NF; ++f) set_field(w[m], f, tile[(f * 32 + lane) * XPITCH + col]);
     make_pt<T, ND>(w[m], gm);
   }
   T fprev[NV];
@@ -273,15 +328,21 @@ __global__ void __launch_bounds__(32 * XWARPS) k_flux_x(BlockK b, SchemeParams s
     {
       int col = j + 3 - (s0 - 3);
 #pragma unroll
-      for (int v = 0; v < NV; ++v) w[5].q[v] = tile[(v * 32 + lane) * XPITCH + col];
+      for (int f = 0; f < NF; ++f) set_field(w[5], f, tile[(f * 32 + lane) * XPITCH + col]);
       make_pt<T, ND>(w[5], gm);
     }
     T fh[NV];
-    char_flux<T, ND, SCH, AVG>(w, sp, fh);
+    T sc = invd;
+    if constexpr (CURV) {
+      char_flux_curv<T, ND, SCH, AVG>(w, sp, fh);
+      sc = invd / w[2].J;
+    } else {
+      char_flux<T, ND, SCH, AVG>(w, sp, fh);
+    }
     if (j >= s0) {
       int id = base + j;
 #pragma unroll
-      for (int v = 0; v < NV; ++v) acc_flux(b, v, id, fh[v], fprev[v], invd, first);
+      for (int v = 0; v < NV; ++v) acc_flux(b, v, id, fh[v], fprev[v], sc, first);
     }
 #pragma unroll
     for (int v = 0; v < NV; ++v) fprev[v] = fh[v];

@@ -293,6 +293,193 @@ __device__ __forceinline__ void char_flux(const Pt<T, ND> (&w)[6], const SP<T>& 
   }
 }
 
+// ---------------------------------------------------------------------------------------
+// Curvilinear sweeps work in the global frame.  A point carries its conserved state and
+// primitives plus the metric row of the sweep direction d, k_i = D_di = d xi_d / d x_i, and
+// det J.
+template <typename T, int ND>
+struct PtC {
+  T q[ND + 2];  // rho, rho u_0.., E (global frame)
+  T u[ND];
+  T p, a;
+  T k[ND];      // D_d0 .. D_d(ND-1)
+  T J;          // det(d x / d xi)
+};
+
+template <typename T, int ND>
+__device__ __forceinline__ void make_pt(PtC<T, ND>& s, T gm) {
+  T rho = s.q[0];
+  T ir = L_(1.0) / rho;
+  T ke = L_(0.0);
+#pragma unroll
+  for (int i = 0; i < ND; ++i) {
+    s.u[i] = s.q[1 + i] * ir;
+    ke += s.u[i] * s.u[i];
+  }
+  s.p = (gm - L_(1.0)) * (s.q[ND + 1] - L_(0.5) * rho * ke);
+  s.a = sqrt(gm * s.p * ir);
+}
+
+// Characteristic LLF flux of the curvilinear form at the interface between w[2] and w[3]:
+// contravariant flux F = J [rho U, rho u_i U + p D_di, (E + p) U] with U = D_d . u
+// (the conservative metric form of the reference's curvilinear Euler equations,
+// equation_types/metric.py with the generated "LFWeno_reconstruction" kernels), eigensystem of
+// euler_eigensystem.py:100-165 for the unit direction k = avg(D_d) / |avg(D_d)|, LLF speeds
+// from the pointwise J (U +- a |D_d|) over points i, i+1.  The eigenvector matrices are
+// applied in factored form: with S = phi v0 - g1 (u . v_m) + g1 v_E, E = v0 - S/a^2,
+// w = (v_m - u v0)/rho and Dn = k . v_m - (k . u) v0 the rows of LEV are
+//   2D: E, k1 w0 - k0 w1, bta (S + a Dn), bta (S - a Dn)
+//   3D: k_i E + (w x k)_i (i = 0..2), bta (S + a Dn), bta (S - a Dn)
+// and REV is applied column-wise (see the back-projection below).
+template <typename T, int ND, int SCH, int AVG>
+__device__ __forceinline__ void char_flux_curv(const PtC<T, ND> (&w)[6], const SP<T>& sp, T (&fh)[ND + 2]) {
+  static_assert(ND == 2 || ND == 3, "curvilinear sweeps are 2D or 3D");
+  constexpr int NV = ND + 2;
+  const T g1 = sp.g1;
+  const PtC<T, ND>& L = w[2];
+  const PtC<T, ND>& R = w[3];
+  T rho, u[ND], a;
+  if (AVG == AVG_ROE) {
+    T sL = sqrt(L.q[0]), sR = sqrt(R.q[0]);
+    rho = sqrt(L.q[0] * R.q[0]);
+    T inv = L_(1.0) / (sL + sR);
+    T ke = L_(0.0);
+#pragma unroll
+    for (int i = 0; i < ND; ++i) {
+      u[i] = (sL * L.u[i] + sR * R.u[i]) * inv;
+      ke += u[i] * u[i];
+    }
+    T H = ((L.q[NV - 1] + L.p) / sL + (R.q[NV - 1] + R.p) / sR) * inv;
+    a = sqrt(g1 * (H - L_(0.5) * ke));
+  } else {
+    rho = L_(0.5) * (L.q[0] + R.q[0]);
+#pragma unroll
+    for (int i = 0; i < ND; ++i) u[i] = L_(0.5) * (L.u[i] + R.u[i]);
+    a = L_(0.5) * (L.a + R.a);
+  }
+  // unit direction of the averaged metric row
+  T k[ND];
+  {
+    T kn = L_(0.0);
+#pragma unroll
+    for (int i = 0; i < ND; ++i) {
+      k[i] = L_(0.5) * (L.k[i] + R.k[i]);
+      kn += k[i] * k[i];
+    }
+    kn = L_(1.0) / sqrt(kn);
+#pragma unroll
+    for (int i = 0; i < ND; ++i) k[i] *= kn;
+  }
+  // LLF speeds: J U and J U +- a |J D_d| at i and i+1
+  const T sfc = sp.sfc;
+  T lam_u, lam_p, lam_m;
+  {
+    T UL = L_(0.0), UR = L_(0.0), mL = L_(0.0), mR = L_(0.0);
+#pragma unroll
+    for (int i = 0; i < ND; ++i) {
+      T kl = L.J * L.k[i], kr = R.J * R.k[i];
+      UL += kl * L.u[i];
+      UR += kr * R.u[i];
+      mL += kl * kl;
+      mR += kr * kr;
+    }
+    mL = sqrt(mL);
+    mR = sqrt(mR);
+    lam_u = sfc * fmax(fabs(UL), fabs(UR));
+    lam_p = sfc * fmax(fabs(UL + L.a * mL), fabs(UR + R.a * mR));
+    lam_m = sfc * fmax(fabs(UL - L.a * mL), fabs(UR - R.a * mR));
+  }
+  const T ia = L_(1.0) / a, ia2 = ia * ia, irho = L_(1.0) / rho;
+  T ke = L_(0.0), th = L_(0.0);
+#pragma unroll
+  for (int i = 0; i < ND; ++i) {
+    ke += u[i] * u[i];
+    th += k[i] * u[i];
+  }
+  const T phi = g1 * L_(0.5) * ke;
+  const T bta = ia * irho * L_(0.70710678118654752440);
+  const T alf = rho * ia * L_(0.70710678118654752440);
+  T fp[NV][6], fmn[NV][6];
+#pragma unroll
+  for (int m = 0; m < 6; ++m) {
+    const PtC<T, ND>& s = w[m];
+    T U = L_(0.0);
+#pragma unroll
+    for (int i = 0; i < ND; ++i) U += s.k[i] * s.u[i];
+    T Fv[NV];
+    Fv[0] = s.J * (s.q[0] * U);
+#pragma unroll
+    for (int i = 0; i < ND; ++i) Fv[1 + i] = s.J * (s.q[1 + i] * U + s.p * s.k[i]);
+    Fv[NV - 1] = s.J * ((s.q[NV - 1] + s.p) * U);
+    T cs[NV], cf[NV];
+#pragma unroll
+    for (int pass = 0; pass < 2; ++pass) {
+      const T* v = pass == 0 ? s.q : Fv;
+      T* o = pass == 0 ? cs : cf;
+      T um = L_(0.0), kv = L_(0.0);
+#pragma unroll
+      for (int i = 0; i < ND; ++i) {
+        um += u[i] * v[1 + i];
+        kv += k[i] * v[1 + i];
+      }
+      T S = phi * v[0] - g1 * um + g1 * v[NV - 1];
+      T E = v[0] - S * ia2;
+      T Dn = kv - th * v[0];
+      T wv[ND];
+#pragma unroll
+      for (int i = 0; i < ND; ++i) wv[i] = (v[1 + i] - u[i] * v[0]) * irho;
+      if (ND == 2) {
+        o[0] = E;
+        o[1] = k[1] * wv[0] - k[0] * wv[1];
+      } else {
+        o[0] = k[0] * E + (wv[1] * k[2] - wv[2] * k[1]);
+        o[1] = k[1] * E + (wv[2] * k[0] - wv[0] * k[2]);
+        o[2] = k[2] * E + (wv[0] * k[1] - wv[1] * k[0]);
+      }
+      o[ND] = bta * (S + a * Dn);
+      o[ND + 1] = bta * (S - a * Dn);
+    }
+#pragma unroll
+    for (int c = 0; c < NV; ++c) {
+      const T lk = (c < ND) ? lam_u : (c == ND ? lam_p : lam_m);
+      fp[c][m] = L_(0.5) * (cf[c] + lk * cs[c]);
+      fmn[c][m] = L_(0.5) * (cf[c] - lk * cs[c]);
+    }
+  }
+  T rec[NV];
+#pragma unroll
+  for (int c = 0; c < NV; ++c)
+    rec[c] = recon5<T, SCH>(fp[c][0], fp[c][1], fp[c][2], fp[c][3], fp[c][4], sp) +
+             recon5<T, SCH>(fmn[c][5], fmn[c][4], fmn[c][3], fmn[c][2], fmn[c][1], sp);
+  // REV: 2D columns (1, u, phi/g1), rho (0, t, t.u) with t = (k1, -k0), and the acoustic
+  // pair alf (1, u +- a k, h0 +- a th); 3D vorticity columns give u (k.r) + rho (k x r) and
+  // phi/g1 (k.r) + rho (u x k).r.
+  const T rp = rec[ND] + rec[ND + 1], rm = rec[ND] - rec[ND + 1];
+  const T h0 = (phi + a * a) / g1;
+  if (ND == 2) {
+    const T t0 = k[1], t1 = -k[0];
+    const T F0 = rec[0] + alf * rp;
+    fh[0] = F0;
+    fh[1] = u[0] * F0 + alf * a * k[0] * rm + rho * rec[1] * t0;
+    fh[2] = u[1] * F0 + alf * a * k[ND - 1] * rm + rho * rec[1] * t1;
+    fh[NV - 1] = phi / g1 * rec[0] + rho * (t0 * u[0] + t1 * u[1]) * rec[1] + alf * h0 * rp + alf * a * th * rm;
+  } else {
+    const T kr = k[0] * rec[0] + k[1] * rec[1] + k[ND - 1] * rec[2];
+    const T c0 = k[1] * rec[2] - k[ND - 1] * rec[1];
+    const T c1 = k[ND - 1] * rec[0] - k[0] * rec[2];
+    const T c2 = k[0] * rec[1] - k[1] * rec[0];
+    const T F0 = kr + alf * rp;
+    fh[0] = F0;
+    fh[1] = u[0] * F0 + rho * c0 + alf * a * k[0] * rm;
+    fh[2] = u[1] * F0 + rho * c1 + alf * a * k[1] * rm;
+    fh[3] = u[ND - 1] * F0 + rho * c2 + alf * a * k[ND - 1] * rm;
+    const T x0 = u[1] * k[ND - 1] - u[ND - 1] * k[1];
+    const T x1 = u[ND - 1] * k[0] - u[0] * k[ND - 1];
+    const T x2 = u[0] * k[1] - u[1] * k[0];
+    fh[NV - 1] = phi / g1 * kr + rho * (x0 * rec[0] + x1 * rec[1] + x2 * rec[2]) + alf * (h0 * rp + a * th * rm);
+  }
+}
+
 // Central 4th-order first / second derivative weights (scheme.py:83-87).
 template <typename T>
 __device__ __forceinline__ T d1w(T fm2, T fm1, T fp1, T fp2) {

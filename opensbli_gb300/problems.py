@@ -162,15 +162,16 @@ def _periodic_fill(spec, a, depth):
         a[tuple(hi_dst)] = a[tuple(hi_src)]
 
 
-def metrics_central4(spec, x, periodic_from_interior=False):
+def metrics_central4(spec, x, periodic_from_interior=False, extended=False):
     """Metric arrays of a block from its grid coordinates x[0..ndim-1] (OPS layout, known at
     every allocated point), with 4th-order central derivatives (the reference's
     MetricsEquation with central differences, opensbli/equation_types/metric.py).
 
     periodic_from_interior=True evaluates them on the interior only and fills the halos by a
-    depth-5 periodic exchange, as the generated solver of a periodic curvilinear block does;
-    otherwise they are evaluated wherever the stencil fits and the outer two halo layers
-    repeat the nearest evaluated layer."""
+    depth-5 periodic exchange, as the generated solver of a periodic curvilinear block does.
+    extended=True takes coordinates on the allocation grown by two points on every side and
+    evaluates the metrics at every allocated point.  Otherwise they are evaluated wherever the
+    stencil fits and the outer two halo layers repeat the nearest evaluated layer."""
     nd = spec.ndim
     J = [[_d1_central4(x[i], nd - 1 - j, 1.0 / spec.delta[j]) for j in range(nd)] for i in range(nd)]
     met = [None] * 10
@@ -197,7 +198,9 @@ def metrics_central4(spec, x, periodic_from_interior=False):
         if met[k] is None:
             continue
         a = np.ascontiguousarray(met[k])
-        if periodic_from_interior:
+        if extended:
+            a = a[tuple(slice(2, n - 2) for n in a.shape)]
+        elif periodic_from_interior:
             b = np.zeros_like(a)
             b[spec.interior()] = a[spec.interior()]
             _periodic_fill(spec, b, h)
@@ -227,3 +230,135 @@ def curvilinear_wave_2d(n=128, scheme=abi.SCHEME_WENO5_Z, averaging=abi.AVG_ROE)
     rho = 1.0 + 0.2 * np.sin(math.pi * (x0 + x1))
     q = _cons(spec, rho, [np.full(spec.shape, 1.0), np.full(spec.shape, -0.5)], 1.0)
     return spec, q, metrics_central4(spec, [x0, x1], periodic_from_interior=True)
+
+
+# ---------------------------------------------------------------------------------------
+# Multi-block topologies
+
+def split_block(spec, state, cuts, d=0, metrics=None):
+    """Split one block along direction d at the interior indices `cuts` into blocks joined by
+    interfaces (periodic faces along d become an interface between the last and the first
+    piece).  Returns [(spec, state[, metrics])] in OPS layout; each piece's arrays are the
+    matching window of the original allocation, halos included."""
+    h = spec.halo
+    edges = [0] + list(cuts) + [spec.size[d]]
+    nb = len(edges) - 1
+    ax = spec.ndim - 1 - d
+    out = []
+    for b in range(nb):
+        lo, hi = edges[b], edges[b + 1]
+        size = list(spec.size)
+        size[d] = hi - lo
+        bc = [list(x) for x in spec.bc]
+        iface = [[None, None] for _ in range(spec.ndim)]
+        if spec.iface is not None:
+            iface = [list(x) for x in spec.iface]
+        periodic = spec.bc[d][0] == abi.BC_PERIODIC
+        if b > 0 or periodic:
+            bc[d][0] = abi.BC_INTERFACE
+            iface[d][0] = ((b - 1) % nb, d, 1, 0)
+        if b < nb - 1 or periodic:
+            bc[d][1] = abi.BC_INTERFACE
+            iface[d][1] = ((b + 1) % nb, d, 0, 0)
+        ps = BlockSpec(**{**spec.__dict__, "size": tuple(size), "bc": bc, "iface": iface})
+        win = [slice(None)] * spec.ndim
+        win[ax] = slice(lo, hi + 2 * h)
+        win = tuple(win)
+        st = [np.ascontiguousarray(a[win]) for a in state]
+        if metrics is None:
+            out.append((ps, st))
+        else:
+            out.append((ps, st, [None if m is None else np.ascontiguousarray(m[win]) for m in metrics]))
+    return out
+
+
+MB_SIZES = {"A": (512, 256, 32), "B": (384, 256, 32), "C": (512, 192, 32), "D": (256, 256, 32)}
+
+
+def curvilinear_multiblock_3d(sizes=None, seed=0, amp=0.05, mach=0.7, pulse=1e-2, sigma=0.1,
+                              scheme=abi.SCHEME_TENO5, averaging=abi.AVG_ROE):
+    """Four curvilinear 3D Euler blocks joined by interfaces (blocks A, B, C, D in that order):
+    A, B, D form a chain along x (D's high-x face wraps to A), C sits on A's high-y face and
+    wraps to A's low-y face, B and D are periodic in y, C in x, every block in z.  The grid is
+    uniform in index space with Delta = 1/nz,
+        x = xi   + amp sin(2 pi eta / L_eta) sin(2 pi zeta / L_zeta)
+        y = eta  + amp sin(2 pi xi / L_xi)   sin(2 pi zeta / L_zeta)
+        z = zeta + amp sin(2 pi xi / L_xi)   sin(2 pi eta / L_eta)
+    with the periods chosen so that every periodic wrap and interface meets a continuous mesh
+    (L_xi: gcd of the x chain and C's x length, L_eta: gcd of the A-C chain and B's y length,
+    L_zeta: nz).  Metrics come from 4th-order central differences of the analytic mesh at every
+    allocated point.  Initial state: uniform flow at Mach `mach` along x (rho = 1, p = 1/gama,
+    so a = 1) plus a Gaussian pulse g = exp(-r^2 / (2 sigma^2)) of relative amplitude `pulse`
+    in density and gama * pulse in pressure (isentropic to first order), centred at a seeded
+    point of block A.  Returns [(spec, state, metrics)] for A, B, C, D."""
+    sizes = dict(MB_SIZES if sizes is None else sizes)
+    A, B, C, D = (sizes[k] for k in "ABCD")
+    nz = A[2]
+    assert all(s[2] == nz for s in (A, B, C, D)) and B[1] == A[1] and D[1] == A[1] and C[0] == A[0]
+    dl = 1.0 / nz
+    Lxi = math.gcd(A[0] + B[0] + D[0], C[0]) * dl
+    Leta = math.gcd(A[1] + C[1], B[1]) * dl
+    Lzeta = nz * dl
+    g = 1.4
+    P, I = abi.BC_PERIODIC, abi.BC_INTERFACE
+    # origin (in points) and faces of every block
+    layout = {
+        "A": ((0, 0, 0), [[I, I], [I, I], [P, P]], [[(3, 0, 1, 0), (1, 0, 0, 0)], [(2, 1, 1, 0), (2, 1, 0, 0)], [None, None]]),
+        "B": ((A[0], 0, 0), [[I, I], [P, P], [P, P]], [[(0, 0, 1, 0), (3, 0, 0, 0)], [None, None], [None, None]]),
+        "C": ((0, A[1], 0), [[P, P], [I, I], [P, P]], [[None, None], [(0, 1, 1, 0), (0, 1, 0, 0)], [None, None]]),
+        "D": ((A[0] + B[0], 0, 0), [[I, I], [P, P], [P, P]], [[(1, 0, 1, 0), (0, 0, 0, 0)], [None, None], [None, None]]),
+    }
+    rng = np.random.default_rng(seed)
+    centre = [rng.uniform(0.25, 0.75) * A[d] * dl for d in range(3)]
+    out = []
+    for name in "ABCD":
+        size = sizes[name]
+        org, bc, iface = layout[name]
+        spec = BlockSpec(ndim=3, size=size, scheme=scheme, averaging=averaging, viscous=abi.VISC_NONE,
+                         bc=bc, bc_depth=[[4, 4] for _ in range(3)], iface=iface, delta=(dl, dl, dl), gama=g)
+        # index coordinates on the allocation grown by 2 (for the metric stencil)
+        grids = []
+        for d in range(3):
+            n = size[d] + 2 * spec.halo + 4
+            idx = (np.arange(n) - spec.halo - 2 + org[d]) * dl
+            shp = [1, 1, 1]
+            shp[2 - d] = n
+            grids.append(idx.reshape(shp))
+        xi, eta, zeta = grids
+        ext_shape = tuple(s + 4 for s in spec.shape)
+        two_pi = 2.0 * math.pi
+        x0 = np.broadcast_to(xi + amp * np.sin(two_pi * eta / Leta) * np.sin(two_pi * zeta / Lzeta), ext_shape)
+        x1 = np.broadcast_to(eta + amp * np.sin(two_pi * xi / Lxi) * np.sin(two_pi * zeta / Lzeta), ext_shape)
+        x2 = np.broadcast_to(zeta + amp * np.sin(two_pi * xi / Lxi) * np.sin(two_pi * eta / Leta), ext_shape)
+        met = metrics_central4(spec, [np.ascontiguousarray(x0), np.ascontiguousarray(x1), np.ascontiguousarray(x2)],
+                               extended=True)
+        core = tuple(slice(2, n - 2) for n in ext_shape)
+        r2 = (x0[core] - centre[0]) ** 2 + (x1[core] - centre[1]) ** 2 + (x2[core] - centre[2]) ** 2
+        gs = np.exp(-r2 / (2.0 * sigma * sigma))
+        rho = 1.0 + pulse * gs
+        p = (1.0 / g) * (1.0 + g * pulse * gs)
+        zero = np.zeros(spec.shape)
+        q = _cons(spec, rho, [np.full(spec.shape, mach), zero, zero], p)
+        out.append((spec, q, met))
+    return out
+
+
+def multiblock_cfl_dt(blocks, cfl):
+    """CFL time step over curvilinear blocks: cfl / max sum_d (|U_d| + a |D_d|) with
+    U_d = D_d . u (physical speeds mapped to index space), FP64 on the host."""
+    worst = 0.0
+    for spec, q, met in blocks:
+        sl = spec.interior()
+        rho = q[0][sl]
+        u = [q[1 + i][sl] / rho for i in range(spec.ndim)]
+        ke = sum(ui * ui for ui in u)
+        p = (spec.gama - 1.0) * (q[-1][sl] - 0.5 * rho * ke)
+        a = np.sqrt(spec.gama * p / rho)
+        s = 0.0
+        for d in range(spec.ndim):
+            Dd = [met[3 * d + i][sl] for i in range(spec.ndim)]
+            U = sum(Dd[i] * u[i] for i in range(spec.ndim))
+            nrm = np.sqrt(sum(x * x for x in Dd))
+            s = s + (np.abs(U) + a * nrm) / spec.delta[d]
+        worst = max(worst, float(np.max(s)))
+    return cfl / worst

@@ -23,7 +23,9 @@ def _torch():
 class Solver:
     """Advance one or more blocks with the GB300 kernels.
 
-    specs_states: list of (BlockSpec, [nv arrays in OPS layout]) pairs.
+    specs_states: list of (BlockSpec, [nv arrays in OPS layout]) pairs, or triples whose third
+        item is the list of 10 metric arrays of a curvilinear block (osb_block_desc.metric
+        order: D_di at 3*d + i, det J at 9; None where unused).
     precision: "fp64" (parity path) or "fp32" (FP32 residual, FP64 state).
     rk: "ls3" (RungeKuttaLS(3)), "sbli3" (RungeKutta(3)) or (kind, A, B).
     """
@@ -41,9 +43,12 @@ class Solver:
         self.specs = []
         self.q = []
         self.rk = []
+        self.met = []
         self._descs = []
         try:
-            for i, (spec, state) in enumerate(specs_states):
+            for i, item in enumerate(specs_states):
+                spec, state = item[0], item[1]
+                met = item[2] if len(item) > 2 else None
                 q = torch.empty((spec.nvars,) + spec.shape, dtype=torch.float64, device=self.device)
                 q.copy_(torch.from_numpy(np.ascontiguousarray(np.stack([np.asarray(a, dtype=np.float64) for a in state]))))
                 r = torch.zeros_like(q)
@@ -52,8 +57,18 @@ class Solver:
                 self.specs.append(spec)
                 self.q.append(q)
                 self.rk.append(r)
+                mt, mp = None, None
+                if met is not None:
+                    for a in met:
+                        if a is not None and tuple(np.shape(a)) != tuple(spec.shape):
+                            raise abi.OSBError("metric array of shape %s, block allocation is %s"
+                                               % (np.shape(a), spec.shape))
+                    mt = [None if a is None else torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).to(self.device)
+                          for a in met]
+                    mp = [None if a is None else a.data_ptr() for a in mt]
+                self.met.append(mt)
                 d = abi.make_desc(spec, [q[v].data_ptr() for v in range(spec.nvars)],
-                                  [r[v].data_ptr() for v in range(spec.nvars)])
+                                  [r[v].data_ptr() for v in range(spec.nvars)], mp)
                 self._descs.append(d)
                 bid = ctypes.c_int()
                 torch.cuda.synchronize(self.device)
