@@ -44,6 +44,12 @@ def parse():
     ap.add_argument("--size", type=int, default=NS)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="tgv", choices=["tgv", "kh_ensemble", "curv4"],
+                    help="tgv: the 256^3 supersonic TGV (headline); kh_ensemble: 64 uneven 2D "
+                         "Kelvin-Helmholtz instances in one persistent launch per stage; curv4: the "
+                         "4-block 3D curvilinear TENO5 case")
+    ap.add_argument("--ensemble", type=int, default=64)
+    ap.add_argument("--no-tune", action="store_true")
     return ap.parse_args()
 
 
@@ -367,10 +373,126 @@ def our_arm(args):
     return 0
 
 
+def _errors(spec, qa, qb):
+    sl = spec.interior()
+    out = {}
+    for v, name in ((0, "rho"), (spec.nvars - 1, "rhoE")):
+        d = qa[v][sl] - qb[v][sl]
+        out[name] = {"rel_l2": float(np.linalg.norm(d) / np.linalg.norm(qb[v][sl])),
+                     "rel_linf": float(np.max(np.abs(d)) / np.max(np.abs(qb[v][sl])))}
+    return out
+
+
+def _merge_errors(per_block):
+    """Worst relative error over blocks (L2 over the union of points)."""
+    out = {}
+    for name in ("rho", "rhoE"):
+        out[name] = {"rel_l2": max(e[name]["rel_l2"] for e in per_block),
+                     "rel_linf": max(e[name]["rel_linf"] for e in per_block)}
+    return out
+
+
+def secondary_arm(args):
+    """kh_ensemble / curv4 workloads: FP32-residual throughput (whole batch per step), the FP64
+    per-block path beside it, the FP32-vs-FP64 error after the timed steps' count, launches."""
+    import torch
+    from opensbli_gb300 import abi, autotune, problems
+    from opensbli_gb300.solver import Solver
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if args.workload == "kh_ensemble":
+        blocks = problems.kh_ensemble(args.ensemble, seed=0)
+        dt = 2e-4
+        rk = "ls3"
+        work = ("%d Kelvin-Helmholtz 2D instances, sizes drawn by seed 0 from {128,192,256,384,512}^2, "
+                "WENO5-Z (Roe), RK-LS3, periodic" % args.ensemble)
+        bytes_pt = 4 * 8 * 4 + 2 * 4 * 4  # q, rk read+write FP64 (4 vars) + FP32 state in/out
+    else:
+        blocks = problems.curvilinear_multiblock_3d(seed=0)
+        dt = problems.multiblock_cfl_dt(blocks, CFL)
+        rk = "ls3"
+        work = ("4-block 3D curvilinear Euler (512x256x32, 384x256x32, 512x192x32, 256x256x32), TENO5 (Roe), "
+                "interfaces + periodic, Mach 0.7 + Gaussian pulse, RK-LS3, CFL %.1f" % CFL)
+        bytes_pt = 4 * 5 * 8
+    pts = sum(b[0].npoints for b in blocks)
+    log("problem ready: %d blocks, %d points" % (len(blocks), pts))
+    s32 = Solver(blocks, precision="fp32", rk=rk, device=local)
+    s32.apply_bc()
+    tuned = None
+    if args.workload == "kh_ensemble" and not args.no_tune:
+        best, trials = autotune.tune(s32, dt, steps=2, warmup=1, cache=os.path.join(ROOT, "gpurun_out",
+                                                                                     "autotune.json"))
+        tuned = {"schedule": best, "trials": len(trials),
+                 "per_block_ms": next((t for t, c in trials if c["mode"] == abi.SCHED_PER_BLOCK), None),
+                 "best_ms": min((t for t, _ in trials), default=None)}
+        log("autotune: %s" % json.dumps(tuned))
+    mode = s32.schedule()[0]
+    s32.step(dt, args.warmup)
+    s32.sync()
+    launches0 = s32.launches()
+    clocks = ClockSampler(local)
+    clocks.start()
+    secs = time_steps(s32, dt, args.steps)
+    clk = clocks.stop()
+    launches = s32.launches() - launches0
+    value = pts * 3 * args.steps / secs / 1e6
+    s32.timing(True)
+    s32.step(dt, 1)
+    rep = s32.timing_report()
+    s32.timing(False)
+    dom = max(rep, key=lambda k: rep[k][0])
+    dom_ms = rep[dom][0] / max(rep[dom][1], 1)
+    hbm, peak_kind = measured_peaks()
+    launches_per_stage = rep[dom][1] / 3.0
+    achieved = bytes_pt * pts / launches_per_stage / (dom_ms * 1e-3) / 1e9 if dom == "persistent_stage" else None
+    # FP64 per-block path and the error after the same number of steps from the same state
+    s64 = Solver(blocks, precision="fp64", rk=rk, device=local)
+    s64.apply_bc()
+    s64.step(dt, 1)
+    s64.sync()
+    t64 = time_steps(s64, dt, 1)
+    fp64 = pts * 3 / t64 / 1e6
+    s64.close()
+    nerr = 3
+    a = Solver(blocks, precision="fp32", rk=rk, device=local)
+    if tuned:
+        a.set_schedule(**tuned["schedule"])
+    a.apply_bc()
+    a.step(dt, nerr)
+    b = Solver(blocks, precision="fp64", rk=rk, device=local)
+    b.apply_bc()
+    b.step(dt, nerr)
+    errs = [_errors(blk[0], a.state(i), b.state(i)) for i, blk in enumerate(blocks)]
+    ke_a, ke_b = a.reduce(abi.RED_KE), b.reduce(abi.RED_KE)
+    a.close()
+    b.close()
+    err = _merge_errors(errs)
+    err["ke_rel"] = abs(ke_a - ke_b) / abs(ke_b)
+    err["steps"] = nerr
+    s32.close()
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": secs / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 residual / f64 state", "data": "synthetic",
+            "config": {"workload": work, "points": pts, "blocks": len(blocks),
+                       "schedule": "persistent" if mode == abi.SCHED_PERSISTENT else "per-block",
+                       "l2": "inputs larger than L2, no flush"},
+            "autotune": tuned, "fp64": {"value": fp64, "unit": UNIT, "fp32_over_fp64": value / fp64},
+            "error_vs_fp64": err, "clocks": clk, "gpu_launches": launches,
+            "kernel_ms_per_step": {k: v[0] for k, v in rep.items() if v[1]},
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                         "frac": achieved / hbm if achieved else None, "peak_kind": peak_kind,
+                         "per_launch_ms": dom_ms}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return reference_arm(args)
+    if args.workload != "tgv":
+        return secondary_arm(args)
     return our_arm(args)
 
 

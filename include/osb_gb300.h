@@ -163,14 +163,40 @@ int osb_set_graphs(osb_ctx* ctx, int enable);
  * variant < 0 restores the default. */
 int osb_set_variant(osb_ctx* ctx, int variant);
 
+/* Stage schedule.  OSB_SCHED_PER_BLOCK runs every block's sweeps, RK update and boundary
+ * kernels as separate launches; OSB_SCHED_PERSISTENT runs one fused persistent launch per RK
+ * stage over all blocks (FP32-residual path, 2D fully periodic blocks with the characteristic
+ * flux: residual kept on chip, periodic images read in place, FP32 state ping-ponged between
+ * two buffers); OSB_SCHED_AUTO picks the persistent stage whenever the blocks qualify.  The
+ * remaining fields tune the persistent stage: tile height (8, 16 or 32 points; tiles are 32
+ * wide), resident CTAs per SM, dynamic (atomic) or static tile claiming, and the tile order
+ * (0 block order, 1 largest blocks first, 2 interleaved across blocks).  The analogue of
+ * OPS's cache-blocking tiling parameters (OPS_TILING, OPS_TILESIZE_X / _Y). */
+#define OSB_SCHED_AUTO (-1)
+#define OSB_SCHED_PER_BLOCK 0
+#define OSB_SCHED_PERSISTENT 1
+typedef struct osb_schedule {
+  int32_t mode;
+  int32_t tile_y;
+  int32_t ctas_per_sm;
+  int32_t dynamic;
+  int32_t order;
+} osb_schedule;
+
+int osb_set_schedule(osb_ctx* ctx, const osb_schedule* sched);
+
+/* The schedule in effect: *mode_out receives OSB_SCHED_PER_BLOCK or OSB_SCHED_PERSISTENT as
+ * resolved for the current blocks (AUTO resolved), *sched_out (optional) the settings. */
+int osb_get_schedule(osb_ctx* ctx, int* mode_out, osb_schedule* sched_out);
+
 /* Per-kernel timing, the analogue of OPS's ops_timing_output (opsc.py:826-836): while enabled
  * every kernel launch is bracketed by CUDA events on the context stream (CUDA graphs are
  * bypassed). */
 int osb_timing(osb_ctx* ctx, int enable);
 
 /* Writes accumulated milliseconds and launch counts per kernel family (0 flux-x, 1 flux-y,
- * 2 flux-z, 3 central, 4 RK update, 5 boundaries, 6 reductions) into ms[0..n) / launches[0..n)
- * and resets them. */
+ * 2 flux-z, 3 central, 4 RK update, 5 boundaries, 6 reductions, 7 persistent stage) into
+ * ms[0..n) / launches[0..n) and resets them. */
 int osb_timing_report(osb_ctx* ctx, double* ms, long long* launches, int n);
 
 /* Returns the number of kernel launches the context has issued so far. */

@@ -45,6 +45,20 @@ RED_RHO_SUM = 3
 RED_CFL_DT = 4
 RED_NAN_COUNT = 5
 
+SCHED_AUTO = -1
+SCHED_PER_BLOCK = 0
+SCHED_PERSISTENT = 1
+
+
+class Schedule(ctypes.Structure):
+    """osb_schedule: stage schedule and persistent-stage tiling knobs."""
+    _fields_ = [("mode", ctypes.c_int32), ("tile_y", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32),
+                ("dynamic", ctypes.c_int32), ("order", ctypes.c_int32)]
+
+    def as_dict(self):
+        return {f: int(getattr(self, f)) for f, _ in self._fields_}
+
+
 SCHEME_NAMES = {"weno5_js": SCHEME_WENO5_JS, "weno5_z": SCHEME_WENO5_Z, "teno5": SCHEME_TENO5,
                 "central4": SCHEME_CENTRAL4}
 
@@ -165,6 +179,8 @@ def load_library():
     lib.osb_desc_layout.argtypes = [ctypes.POINTER(ctypes.c_longlong), i32]
     lib.osb_stage_noalloc.argtypes = [ctypes.POINTER(BlockDesc), i32, ctypes.c_double, ctypes.c_double,
                                       ctypes.c_double, vp]
+    lib.osb_set_schedule.argtypes = [vp, ctypes.POINTER(Schedule)]
+    lib.osb_get_schedule.argtypes = [vp, ctypes.POINTER(i32), ctypes.POINTER(Schedule)]
     lib.osb_timing.argtypes = [vp, i32]
     lib.osb_timing_report.argtypes = [vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong), i32]
     _lib = lib
@@ -187,8 +203,9 @@ def check(lib, rc, what):
 EXPORTED = ["osb_version", "osb_last_error", "osb_ctx_create", "osb_ctx_destroy", "osb_block_add",
             "osb_set_rk", "osb_step", "osb_stage", "osb_apply_bc", "osb_residual", "osb_reduce",
             "osb_sync", "osb_set_graphs", "osb_set_variant", "osb_launch_count", "osb_get_stream",
-            "osb_desc_layout", "osb_timing", "osb_timing_report", "osb_stage_noalloc"]
+            "osb_desc_layout", "osb_timing", "osb_timing_report", "osb_stage_noalloc", "osb_set_schedule",
+            "osb_get_schedule"]
 
 NOALLOC_MAX_DOUBLES = 4 * 1024 * 1024
 
-KERNEL_FAMILIES = ["flux_x", "flux_y", "flux_z", "central", "rk_update", "boundary", "reduce"]
+KERNEL_FAMILIES = ["flux_x", "flux_y", "flux_z", "central", "rk_update", "boundary", "reduce", "persistent_stage"]

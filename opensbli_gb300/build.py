@@ -28,6 +28,7 @@ UNITS = [
     ("api", "osb_gb300.cu", []),
     ("central_f64", "osb_central.cu", ["-DOSB_CENTRAL_T=double", "-DOSB_CENTRAL_NAME=central_f64"]),
     ("central_f32", "osb_central.cu", ["-DOSB_CENTRAL_T=float", "-DOSB_CENTRAL_NAME=central_f32"] + FAST),
+    ("batch", "osb_batch.cu", FAST),
 ] + [
     ("flux_%s_%dd" % (p, nd), "osb_flux.cu",
      ["-DOSB_T=%s" % ("double" if p == "f64" else "float"), "-DOSB_ND=%d" % nd, "-DOSB_NAME=flux_%s_%dd" % (p, nd)]

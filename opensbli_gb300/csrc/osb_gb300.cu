@@ -505,7 +505,14 @@ int apply_bc(osb_ctx* c) {
   return OSB_OK;
 }
 
+// Whether stages run as the persistent fused launch (osb_batch.cu).
+bool use_batch(const osb_ctx* c) {
+  if (c->sched.mode == OSB_SCHED_PER_BLOCK) return false;
+  return batch_eligible(c, nullptr);
+}
+
 int stage(osb_ctx* c, int s, double dt) {
+  if (use_batch(c)) return batch_stage(c, s, dt);
   for (auto& bl : c->blocks) {
     int rc = residual(c, bl);
     if (rc) return rc;
@@ -538,6 +545,14 @@ int sync_shadow(osb_ctx* c) {
 }
 
 int one_step(osb_ctx* c, double dt) {
+  if (use_batch(c)) {
+    // periodic images are read in place and the SBLI save is folded into stage 0
+    for (int s = 0; s < c->nst; ++s) {
+      int rc = batch_stage(c, s, dt);
+      if (rc) return rc;
+    }
+    return OSB_OK;
+  }
   int rc = apply_bc(c);
   if (rc) return rc;
   if (c->rk_kind == OSB_RK_SBLI3) {
@@ -559,6 +574,11 @@ void drop_graph(osb_ctx* c) {
     cudaGraphExecDestroy(c->gexec);
     c->gexec = nullptr;
   }
+  for (int p = 0; p < 2; ++p)
+    if (c->gexec_p[p]) {
+      cudaGraphExecDestroy(c->gexec_p[p]);
+      c->gexec_p[p] = nullptr;
+    }
 }
 
 bool check_desc(const osb_block_desc* d, std::string& why) {
@@ -673,9 +693,11 @@ int osb_ctx_destroy(osb_ctx* c) {
   for (auto e : c->event_pool) cudaEventDestroy(e);
   for (auto& bl : c->blocks) {
     if (bl.k.R[0]) cudaFree(bl.k.R[0]);
-    if (bl.k.qf[0]) cudaFree(bl.k.qf[0]);
+    if (bl.qf_base) cudaFree(bl.qf_base);  // k.qf may point at either ping-pong buffer
     if (bl.mf_buf) cudaFree(bl.mf_buf);
+    if (bl.qf_alt) cudaFree(bl.qf_alt);
   }
+  batch_free(c);
   if (c->red) cudaFree(c->red);
   if (c->bad) cudaFree(c->bad);
   if (c->red_host) cudaFreeHost(c->red_host);
@@ -735,6 +757,7 @@ int osb_block_add(osb_ctx* c, const osb_block_desc* d, int* block_id) {
       return fail(OSB_ECUDA, "FP32 shadow: %s", cudaGetErrorString(e));
     }
     for (int v = 0; v < nv; ++v) k.qf[v] = qf + (size_t)v * k.alloc;
+    bl.qf_base = qf;
   }
   for (int i = 0; i < 10; ++i) k.m[i] = d->metric[i];
   if (k.m[9] && c->prec == OSB_PREC_FP32_RESIDUAL) {
@@ -756,6 +779,8 @@ int osb_block_add(osb_ctx* c, const osb_block_desc* d, int* block_id) {
     }
     OSB_CK(cudaGetLastError());
   }
+  if (c->qf_parity) batch_set_parity(c, 0);  // new tables start from the original buffers
+  batch_free(c);
   c->blocks.push_back(bl);
   drop_graph(c);
   if (block_id) *block_id = (int)c->blocks.size() - 1;
@@ -784,6 +809,10 @@ int osb_stage(osb_ctx* c, int s, double dt) {
   if (rc) return rc;
   rc = stage(c, s, dt);
   if (rc) return rc;
+  if (use_batch(c)) {
+    rc = apply_bc(c);  // halos of q and of the current FP32 buffer for observers
+    if (rc) return rc;
+  }
   OSB_CK(cudaGetLastError());
   return OSB_OK;
 }
@@ -806,11 +835,55 @@ int osb_step(osb_ctx* c, double dt, int nsteps) {
   OSB_CK(cudaSetDevice(c->device));
   int src = sync_shadow(c);
   if (src) return src;
+  const bool batch = use_batch(c);
+  if (batch && !c->batch.ready) {
+    int rc = batch_build(c);  // allocates: never inside a capture
+    if (rc) return rc;
+  }
   if (!c->graphs || c->timing) {
     for (int it = 0; it < nsteps; ++it) {
       int rc = one_step(c, dt);
       if (rc) return rc;
     }
+    if (batch) {
+      int rc = apply_bc(c);
+      if (rc) return rc;
+    }
+    OSB_CK(cudaGetLastError());
+    return OSB_OK;
+  }
+  if (batch) {
+    // one graph per FP32-buffer parity; a step flips the parity when the stage count is odd
+    if (c->g_dt != dt) {
+      drop_graph(c);
+      c->g_dt = dt;
+    }
+    for (int it = 0; it < nsteps; ++it) {
+      const int p = c->qf_parity;
+      if (!c->gexec_p[p]) {
+        cudaGraph_t g;
+        long long before = c->launches;
+        OSB_CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        int rc = one_step(c, dt);
+        cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+        batch_set_parity(c, p);  // nothing ran yet
+        if (rc) {
+          if (e == cudaSuccess) cudaGraphDestroy(g);
+          return rc;
+        }
+        if (e != cudaSuccess) return fail(OSB_ECUDA, "graph capture: %s", cudaGetErrorString(e));
+        c->g_kernels = c->launches - before;
+        c->launches = before;
+        e = cudaGraphInstantiate(&c->gexec_p[p], g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return fail(OSB_ECUDA, "graph instantiate: %s", cudaGetErrorString(e));
+      }
+      OSB_CK(cudaGraphLaunch(c->gexec_p[p], c->stream));
+      c->launches += c->g_kernels;
+      batch_set_parity(c, p ^ (c->nst & 1));
+    }
+    int rc = apply_bc(c);  // halos of q and of the current FP32 buffer for observers
+    if (rc) return rc;
     OSB_CK(cudaGetLastError());
     return OSB_OK;
   }
@@ -912,6 +985,32 @@ int osb_set_graphs(osb_ctx* c, int enable) {
   if (!c) return fail(OSB_EINVAL, "null ctx");
   c->graphs = enable != 0;
   if (!c->graphs) drop_graph(c);
+  return OSB_OK;
+}
+
+int osb_set_schedule(osb_ctx* c, const osb_schedule* sched) {
+  if (!c || !sched) return fail(OSB_EINVAL, "null argument");
+  if (sched->mode < OSB_SCHED_AUTO || sched->mode > OSB_SCHED_PERSISTENT) return fail(OSB_EINVAL, "unknown mode");
+  if (sched->tile_y != 8 && sched->tile_y != 16 && sched->tile_y != 32)
+    return fail(OSB_EINVAL, "tile_y must be 8, 16 or 32");
+  if (sched->ctas_per_sm < 1 || sched->ctas_per_sm > 16) return fail(OSB_EINVAL, "ctas_per_sm must be 1..16");
+  if (sched->order < 0 || sched->order > 2) return fail(OSB_EINVAL, "order must be 0, 1 or 2");
+  if (sched->mode == OSB_SCHED_PERSISTENT) {
+    std::string why;
+    if (!batch_eligible(c, &why)) return fail(OSB_ENOTSUP, "%s", why.c_str());
+  }
+  OSB_CK(cudaSetDevice(c->device));
+  OSB_CK(cudaStreamSynchronize(c->stream));
+  c->sched = *sched;
+  batch_free(c);
+  drop_graph(c);
+  return OSB_OK;
+}
+
+int osb_get_schedule(osb_ctx* c, int* mode_out, osb_schedule* sched_out) {
+  if (!c || !mode_out) return fail(OSB_EINVAL, "null argument");
+  *mode_out = use_batch(c) ? OSB_SCHED_PERSISTENT : OSB_SCHED_PER_BLOCK;
+  if (sched_out) *sched_out = c->sched;
   return OSB_OK;
 }
 

@@ -21,11 +21,24 @@ int fail(int code, const char* fmt, ...);
 struct Block {
   osb_block_desc d;
   BlockK k;
-  float* mf_buf = nullptr;  // FP32 copies of the metrics (FP32-residual path, curvilinear)
+  float* mf_buf = nullptr;   // FP32 copies of the metrics (FP32-residual path, curvilinear)
+  float* qf_base = nullptr;  // FP32 state buffer allocated with the block (FP32-residual path)
+  float* qf_alt = nullptr;   // second FP32 state buffer of the persistent stage's ping-pong
 };
 
 // Kernel families for per-kernel timing (osb_timing_report).
-enum { FAM_FLUX_X = 0, FAM_FLUX_Y, FAM_FLUX_Z, FAM_CENTRAL, FAM_RK, FAM_BC, FAM_REDUCE, FAM_N };
+enum { FAM_FLUX_X = 0, FAM_FLUX_Y, FAM_FLUX_Z, FAM_CENTRAL, FAM_RK, FAM_BC, FAM_REDUCE, FAM_PERSISTENT, FAM_N };
+
+struct BatchBlock;
+
+// Device tables of the persistent stage (osb_batch.cu).
+struct BatchState {
+  BatchBlock* tab[2] = {nullptr, nullptr};  // per FP32-buffer parity
+  int4* work = nullptr;                     // tiles: (block, x0, y0, -)
+  int* counter = nullptr;                   // dynamic tile claiming
+  int nwork = 0;
+  bool ready = false;
+};
 
 struct TimedEvent {
   cudaEvent_t a, b;
@@ -45,6 +58,10 @@ struct osb_ctx {
   double B[8] = {1.0 / 3.0, 15.0 / 16.0, 8.0 / 15.0};
   bool graphs = true;
   cudaGraphExec_t gexec = nullptr;
+  cudaGraphExec_t gexec_p[2] = {nullptr, nullptr};  // persistent stage: one graph per FP32 parity
+  osb_schedule sched = {OSB_SCHED_AUTO, 16, 2, 1, 0};
+  osb::BatchState batch;
+  int qf_parity = 0;
   double g_dt = 0.0;
   long long g_kernels = 0;
   double* red = nullptr;              // device reduction partials (+ final slot)
@@ -80,6 +97,13 @@ int flux_curv_f64_2d(osb_ctx* c, Block& bl, const SchemeParams& sp);
 int flux_curv_f64_3d(osb_ctx* c, Block& bl, const SchemeParams& sp);
 int flux_curv_f32_2d(osb_ctx* c, Block& bl, const SchemeParams& sp);
 int flux_curv_f32_3d(osb_ctx* c, Block& bl, const SchemeParams& sp);
+// Persistent fused stage for batches of 2D periodic blocks (osb_batch.cu).
+bool batch_eligible(const osb_ctx* c, std::string* why);
+int batch_build(osb_ctx* c);
+void batch_free(osb_ctx* c);
+void batch_set_parity(osb_ctx* c, int parity);
+int batch_stage(osb_ctx* c, int s, double dt);
+size_t batch_smem(int ty);
 // Central convective and/or viscous terms of one 3D block (osb_central.cu).
 int central_f64(osb_ctx* c, Block& bl, bool conv, int first);
 int central_f32(osb_ctx* c, Block& bl, bool conv, int first);

@@ -137,6 +137,40 @@ __device__ __forceinline__ T ld_field(const BlockK& b, int f, int id) {
   if (f < NV + ND) return ld_m<T>(b, 3 * D + (f - NV), id);
   return ld_m<T>(b, 9, id);
 }
+// Source array of field f (see ld_field).
+template <typename T>
+__device__ __forceinline__ const T* qptr(const BlockK& b, int v);
+template <>
+__device__ __forceinline__ const double* qptr<double>(const BlockK& b, int v) { return b.q[v]; }
+template <>
+__device__ __forceinline__ const float* qptr<float>(const BlockK& b, int v) { return b.qf[v]; }
+template <typename T>
+__device__ __forceinline__ const T* mptr(const BlockK& b, int c);
+template <>
+__device__ __forceinline__ const double* mptr<double>(const BlockK& b, int c) { return b.m[c]; }
+template <>
+__device__ __forceinline__ const float* mptr<float>(const BlockK& b, int c) { return b.mf[c]; }
+template <typename T, int ND, int D, bool CURV>
+__device__ __forceinline__ const T* field_ptr(const BlockK& b, int f) {
+  constexpr int NV = ND + 2;
+  if (!CURV) return qptr<T>(b, gvar_fwd<ND, D>(f));
+  if (f < NV) return qptr<T>(b, f);
+  if (f < NV + ND) return mptr<T>(b, 3 * D + (f - NV));
+  return mptr<T>(b, 9);
+}
+
+// Asynchronous global -> shared copy of one element (cp.async, sm_80+): many copies stay in
+// flight at once instead of one load latency per staged row.
+template <typename T>
+__device__ __forceinline__ void cp_async_el(T* dst_smem, const T* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst_smem);
+  if (sizeof(T) == 8)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 template <typename T, int ND>
 __device__ __forceinline__ void set_field(Pt<T, ND>& s, int f, T v) { s.q[f] = v; }
 template <typename T, int ND>
@@ -172,6 +206,39 @@ __device__ __forceinline__ void acc_flux(const BlockK& b, int v, int id, float f
     b.Rl[v][id] = l;
   }
 }
+// Split form of acc_flux for sweeps that prefetch the residual they update: r_load reads the
+// current value early (its latency hidden behind the flux computation), r_store adds the flux
+// difference and writes it back.
+__device__ __forceinline__ void r_load(const BlockK& b, int v, int id, double& h, double& l) {
+  h = b.R[v][id];
+  l = 0.0;
+}
+__device__ __forceinline__ void r_load(const BlockK& b, int v, int id, float& h, float& l) {
+  h = b.Rh[v][id];
+  l = b.Rl[v][id];
+}
+__device__ __forceinline__ void r_store(const BlockK& b, int v, int id, double fnew, double fold, double invd,
+                                        double h, double) {
+  b.R[v][id] = h + -(fnew - fold) * invd;
+}
+__device__ __forceinline__ void r_store(const BlockK& b, int v, int id, float fnew, float fold, float invd,
+                                        float h, float l) {
+  float p, pe;
+  ff_flux_diff(fnew, fold, invd, p, pe);
+  ff_add(h, l, p, pe);
+  b.Rh[v][id] = h;
+  b.Rl[v][id] = l;
+}
+
+__device__ __forceinline__ void rp_store(const BlockK& b, int v, int id, double c, double h, double) {
+  b.R[v][id] = h + c;
+}
+__device__ __forceinline__ void rp_store(const BlockK& b, int v, int id, float c, float h, float l) {
+  ff_add(h, l, c, 0.f);
+  b.Rh[v][id] = h;
+  b.Rl[v][id] = l;
+}
+
 // Residual update with a pointwise contribution c.
 __device__ __forceinline__ void acc_point(const BlockK& b, int v, int id, double c, int first) {
   b.R[v][id] = first ? c : b.R[v][id] + c;
@@ -201,7 +268,7 @@ __device__ __forceinline__ int gvar(int lv) {
 // ---------------------------------------------------------------------------------------
 // Sweep along y (D=1) or z (D=2): thread = (x, transverse, segment).
 template <typename T, int ND, int D, int SCH, int AVG, bool CURV>
-__global__ void __launch_bounds__(128) k_flux_sweep(BlockK b, SchemeParams spd, int seg, int nseg, int first) {
+__global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 1) k_flux_sweep(BlockK b, SchemeParams spd, int seg, int nseg, int first) {
   constexpr int NV = ND + 2;
   constexpr int NF = SweepFields<ND, CURV>::N;
   using P = typename SweepPt<T, ND, CURV>::type;
@@ -252,6 +319,12 @@ __global__ void __launch_bounds__(128) k_flux_sweep(BlockK b, SchemeParams spd, 
       for (int f = 0; f < NF; ++f) nxt[f] = ld_field<T, ND, D, CURV>(b, f, id);
     }
     make_pt<T, ND>(w[5], gm);
+    const int id = base + j * s;
+    T oh[NV], ol[NV];
+    if (!first && j >= j0) {
+#pragma unroll
+      for (int lv = 0; lv < NV; ++lv) r_load(b, gvar<ND, D, CURV>(lv), id, oh[lv], ol[lv]);
+    }
     T fh[NV];
     T sc = invd;
     if constexpr (CURV) {
@@ -261,9 +334,13 @@ __global__ void __launch_bounds__(128) k_flux_sweep(BlockK b, SchemeParams spd, 
       char_flux<T, ND, SCH, AVG>(w, sp, fh);
     }
     if (j >= j0) {
-      int id = base + j * s;
+      if (first) {
 #pragma unroll
-      for (int lv = 0; lv < NV; ++lv) acc_flux(b, gvar<ND, D, CURV>(lv), id, fh[lv], fprev[lv], sc, first);
+        for (int lv = 0; lv < NV; ++lv) acc_flux(b, gvar<ND, D, CURV>(lv), id, fh[lv], fprev[lv], sc, 1);
+      } else {
+#pragma unroll
+        for (int lv = 0; lv < NV; ++lv) r_store(b, gvar<ND, D, CURV>(lv), id, fh[lv], fprev[lv], sc, oh[lv], ol[lv]);
+      }
     }
 #pragma unroll
     for (int lv = 0; lv < NV; ++lv) fprev[lv] = fh[lv];
@@ -301,9 +378,10 @@ __global__ void __launch_bounds__(32 * XWARPS) k_flux_x(BlockK b, SchemeParams s
     if (col <= s1 + 2) {
       int id = lin(b, col, y, z);
 #pragma unroll
-      for (int f = 0; f < NF; ++f) tile[(f * 32 + r) * XPITCH + lane] = ld_field<T, ND, 0, CURV>(b, f, id);
+      for (int f = 0; f < NF; ++f) cp_async_el(tile + (f * 32 + r) * XPITCH + lane, field_ptr<T, ND, 0, CURV>(b, f) + id);
     }
   }
+  cp_async_wait_all();
   __syncwarp();
   const int row = row0 + lane;
   if (row >= nrows) return;
@@ -385,31 +463,47 @@ __global__ void __launch_bounds__(CX * CY) k_central3d(BlockK b, CentralParams c
   const T invRe = (T)(1.0 / cp.Re);
   const T kheat = (T)(1.0 / (cp.Pr * cp.Re * cp.Minf * cp.Minf * (cp.gama - 1.0)));
   // ---- load the halo'd tile and form primitives
-  for (int idx = threadIdx.x; idx < CPTS; idx += blockDim.x) {
-    int i = idx % CSX, jj = (idx / CSX) % CSY, k = idx / (CSX * CSY);
-    int gx = x0 - CH + i, gy = y0 - CH + jj, gz = z0 - CH + k;
-    if (gx > b.n[0] + CH || gy > b.n[1] + CH || gz > b.n[2] + CH) continue;
-    int id = lin(b, gx, gy, gz);
-    T rho = ld_q<T>(b, 0, id), m0 = ld_q<T>(b, 1, id), m1 = ld_q<T>(b, 2, id), m2 = ld_q<T>(b, 3, id),
-      E = ld_q<T>(b, 4, id);
-    T ir = L_(1.0) / rho;
-    T u0 = m0 * ir, u1 = m1 * ir, u2 = m2 * ir;
-    T p = (gm - L_(1.0)) * (E - L_(0.5) * rho * (u0 * u0 + u1 * u1 + u2 * u2));
-    sm[Fd::U0 * CPTS + idx] = u0;
-    sm[Fd::U1 * CPTS + idx] = u1;
-    sm[Fd::U2 * CPTS + idx] = u2;
-    sm[Fd::P * CPTS + idx] = p;
-    if (VISC) {
-      T Tt = M2 * gm * p * ir;
-      sm[Fd::TT * CPTS + idx] = Tt;
-      sm[Fd::MU * CPTS + idx] = (VISC == 1) ? L_(1.4042) * Tt * sqrt(Tt) / (L_(0.40417) + Tt) : mu_c;
+  // loads of CU points per thread are issued together before any of them is used
+  constexpr int CU = 6;
+  for (int base = threadIdx.x; base < CPTS; base += CU * CX * CY) {
+    T qv[CU][5];
+    bool ok[CU];
+#pragma unroll
+    for (int u = 0; u < CU; ++u) {
+      const int idx = base + u * CX * CY;
+      const int i = idx % CSX, jj = (idx / CSX) % CSY, k = idx / (CSX * CSY);
+      const int gx = x0 - CH + i, gy = y0 - CH + jj, gz = z0 - CH + k;
+      ok[u] = idx < CPTS && gx <= b.n[0] + CH && gy <= b.n[1] + CH && gz <= b.n[2] + CH;
+      if (ok[u]) {
+        const int id = lin(b, gx, gy, gz);
+#pragma unroll
+        for (int v = 0; v < 5; ++v) qv[u][v] = ld_q<T>(b, v, id);
+      }
     }
-    if (CONV) {
-      sm[Fd::RHO * CPTS + idx] = rho;
-      sm[Fd::M0 * CPTS + idx] = m0;
-      sm[Fd::M1 * CPTS + idx] = m1;
-      sm[Fd::M2 * CPTS + idx] = m2;
-      sm[Fd::E * CPTS + idx] = E;
+#pragma unroll
+    for (int u = 0; u < CU; ++u) {
+      if (!ok[u]) continue;
+      const int idx = base + u * CX * CY;
+      const T rho = qv[u][0], m0 = qv[u][1], m1 = qv[u][2], m2 = qv[u][3], E = qv[u][4];
+      T ir = L_(1.0) / rho;
+      T u0 = m0 * ir, u1 = m1 * ir, u2 = m2 * ir;
+      T p = (gm - L_(1.0)) * (E - L_(0.5) * rho * (u0 * u0 + u1 * u1 + u2 * u2));
+      sm[Fd::U0 * CPTS + idx] = u0;
+      sm[Fd::U1 * CPTS + idx] = u1;
+      sm[Fd::U2 * CPTS + idx] = u2;
+      sm[Fd::P * CPTS + idx] = p;
+      if (VISC) {
+        T Tt = M2 * gm * p * ir;
+        sm[Fd::TT * CPTS + idx] = Tt;
+        sm[Fd::MU * CPTS + idx] = (VISC == 1) ? L_(1.4042) * Tt * sqrt(Tt) / (L_(0.40417) + Tt) : mu_c;
+      }
+      if (CONV) {
+        sm[Fd::RHO * CPTS + idx] = rho;
+        sm[Fd::M0 * CPTS + idx] = m0;
+        sm[Fd::M1 * CPTS + idx] = m1;
+        sm[Fd::M2 * CPTS + idx] = m2;
+        sm[Fd::E * CPTS + idx] = E;
+      }
     }
   }
   __syncthreads();
@@ -439,6 +533,11 @@ __global__ void __launch_bounds__(CX * CY) k_central3d(BlockK b, CentralParams c
       return r * ib;
     };
     const int gid = lin(b, gx, gy, gz);
+    T oh[5], ol[5];
+    if (!first) {
+#pragma unroll
+      for (int v = CONV ? 0 : 1; v < 5; ++v) r_load(b, v, gid, oh[v], ol[v]);
+    }
     T racc[5] = {L_(0.0), L_(0.0), L_(0.0), L_(0.0), L_(0.0)};
     const int S[3] = {sx, sy, sz};
     const T ID[3] = {id0, id1, id2};
@@ -535,8 +634,13 @@ __global__ void __launch_bounds__(CX * CY) k_central3d(BlockK b, CentralParams c
       racc[4] += e * invRe + h * kheat;
     }
     const int v0 = CONV ? 0 : 1;
+    if (first) {
 #pragma unroll
-    for (int v = v0; v < 5; ++v) acc_point(b, v, gid, racc[v], first);
+      for (int v = v0; v < 5; ++v) acc_point(b, v, gid, racc[v], 1);
+    } else {
+#pragma unroll
+      for (int v = v0; v < 5; ++v) rp_store(b, v, gid, racc[v], oh[v], ol[v]);
+    }
   }
 }
 

@@ -92,6 +92,20 @@ class Solver:
         Bb = (ctypes.c_double * len(B))(*B)
         abi.check(self.lib, self.lib.osb_set_rk(self.ctx, kind, len(A), Aa, Bb), "osb_set_rk")
 
+    def set_schedule(self, mode=abi.SCHED_AUTO, tile_y=16, ctas_per_sm=2, dynamic=1, order=0):
+        """Stage schedule (osb_set_schedule): per-block launches or one persistent launch per
+        stage, with the persistent stage's tiling knobs."""
+        sc = abi.Schedule(mode, tile_y, ctas_per_sm, dynamic, order)
+        abi.check(self.lib, self.lib.osb_set_schedule(self.ctx, ctypes.byref(sc)), "osb_set_schedule")
+
+    def schedule(self):
+        """(resolved mode, settings dict) of osb_get_schedule."""
+        mode = ctypes.c_int()
+        sc = abi.Schedule()
+        abi.check(self.lib, self.lib.osb_get_schedule(self.ctx, ctypes.byref(mode), ctypes.byref(sc)),
+                  "osb_get_schedule")
+        return mode.value, sc.as_dict()
+
     # -- time stepping -------------------------------------------------------------------
     def apply_bc(self):
         abi.check(self.lib, self.lib.osb_apply_bc(self.ctx), "osb_apply_bc")
