@@ -44,6 +44,7 @@ extern "C" {
 #define OSB_SCHEME_WENO5_JS 1
 #define OSB_SCHEME_WENO5_Z 2
 #define OSB_SCHEME_TENO5 3
+#define OSB_SCHEME_TENO6 4
 #define OSB_SCHEME_CENTRAL4 5
 
 /* Averaging for the characteristic system (schemes/spatial/averaging.py:31,65). */
@@ -170,7 +171,9 @@ int osb_set_variant(osb_ctx* ctx, int variant);
  * two buffers); OSB_SCHED_AUTO picks the persistent stage whenever the blocks qualify.  The
  * remaining fields tune the persistent stage: tile height (8, 16 or 32 points; tiles are 32
  * wide), resident CTAs per SM, dynamic (atomic) or static tile claiming, and the tile order
- * (0 block order, 1 largest blocks first, 2 interleaved across blocks).  The analogue of
+ * (0 block order, 1 largest blocks first, 2 interleaved across blocks).  fuse_update selects,
+ * for the per-block FP32-residual path, whether the last residual kernel (the central kernel of
+ * a viscous or central block) applies the RK update itself.  The analogue of
  * OPS's cache-blocking tiling parameters (OPS_TILING, OPS_TILESIZE_X / _Y). */
 #define OSB_SCHED_AUTO (-1)
 #define OSB_SCHED_PER_BLOCK 0
@@ -181,6 +184,7 @@ typedef struct osb_schedule {
   int32_t ctas_per_sm;
   int32_t dynamic;
   int32_t order;
+  int32_t fuse_update; /* per-block FP32 path: 1 = the central kernel applies the RK update */
 } osb_schedule;
 
 int osb_set_schedule(osb_ctx* ctx, const osb_schedule* sched);

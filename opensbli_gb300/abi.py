@@ -19,6 +19,7 @@ OSB_ENAN = -5
 SCHEME_WENO5_JS = 1
 SCHEME_WENO5_Z = 2
 SCHEME_TENO5 = 3
+SCHEME_TENO6 = 4
 SCHEME_CENTRAL4 = 5
 
 AVG_SIMPLE = 0
@@ -53,13 +54,13 @@ SCHED_PERSISTENT = 1
 class Schedule(ctypes.Structure):
     """osb_schedule: stage schedule and persistent-stage tiling knobs."""
     _fields_ = [("mode", ctypes.c_int32), ("tile_y", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32),
-                ("dynamic", ctypes.c_int32), ("order", ctypes.c_int32)]
+                ("dynamic", ctypes.c_int32), ("order", ctypes.c_int32), ("fuse_update", ctypes.c_int32)]
 
     def as_dict(self):
         return {f: int(getattr(self, f)) for f, _ in self._fields_}
 
 
-SCHEME_NAMES = {"weno5_js": SCHEME_WENO5_JS, "weno5_z": SCHEME_WENO5_Z, "teno5": SCHEME_TENO5,
+SCHEME_NAMES = {"weno5_js": SCHEME_WENO5_JS, "weno5_z": SCHEME_WENO5_Z, "teno5": SCHEME_TENO5, "teno6": SCHEME_TENO6,
                 "central4": SCHEME_CENTRAL4}
 
 

@@ -1,8 +1,9 @@
 """Autotuner of the stage schedule (osb_set_schedule).
 
-For a solver holding its blocks, times every candidate schedule -- per-block launches, and the
-persistent fused stage over tile heights, resident CTAs per SM, static or dynamic tile claiming
-and tile orders -- on the caller's own workload (CUDA-graph replays timed with CUDA events on the
+For a solver holding its blocks, times every candidate schedule -- per-block launches with and
+without the RK update fused into the last residual kernel, and the persistent fused stage over
+tile heights, resident CTAs per SM, static or dynamic tile claiming and tile orders -- on the
+caller's own workload (CUDA-graph replays timed with CUDA events on the
 solver's stream), restores the state after every trial, applies the fastest schedule and caches
 it in a JSON file keyed by the device, the precision and the blocks' shapes and schemes, so a
 later solver with the same workload picks it up without timing.
@@ -25,14 +26,15 @@ DEFAULT_CACHE = os.environ.get("OSB_AUTOTUNE_CACHE",
 
 def candidates(persistent):
     """Candidate schedules: the per-block path, plus the persistent stage's knob grid."""
-    out = [{"mode": abi.SCHED_PER_BLOCK, "tile_y": 16, "ctas_per_sm": 2, "dynamic": 1, "order": 0}]
+    out = [{"mode": abi.SCHED_PER_BLOCK, "tile_y": 16, "ctas_per_sm": 2, "dynamic": 1, "order": 0, "fuse_update": f}
+           for f in (1, 0)]
     if persistent:
         for ty in (8, 16, 32):
             for cps in (1, 2, 3, 4):
                 for dyn in (1, 0):
                     for order in (0, 1, 2):
                         out.append({"mode": abi.SCHED_PERSISTENT, "tile_y": ty, "ctas_per_sm": cps,
-                                    "dynamic": dyn, "order": order})
+                                    "dynamic": dyn, "order": order, "fuse_update": 1})
     return out
 
 

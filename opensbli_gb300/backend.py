@@ -93,9 +93,9 @@ def _scheme_of(block):
             owner = getattr(sch.average, "__self__", None)
             avg = abi.AVG_ROE if isinstance(owner, RoeAverage) else abi.AVG_SIMPLE
             if isinstance(sch, LFTeno):
-                if sch.order != 5:
-                    raise NotImplementedError("TENO order %d is not supported (TENO5 only)" % sch.order)
-                scheme = abi.SCHEME_TENO5
+                if sch.order not in (5, 6):
+                    raise NotImplementedError("TENO order %d is not supported (TENO5 and TENO6)" % sch.order)
+                scheme = abi.SCHEME_TENO5 if sch.order == 5 else abi.SCHEME_TENO6
             else:
                 if sch.order != 5:
                     raise NotImplementedError("WENO order %d is not supported (WENO5 only)" % sch.order)

@@ -238,10 +238,7 @@ int batch_build(osb_ctx* c) {
   std::vector<BatchBlock> tab[2];
   for (int ib = 0; ib < nb; ++ib) {
     Block& bl = c->blocks[ib];
-    if (!bl.qf_alt) {
-      OSB_CK(cudaMalloc(&bl.qf_alt, sizeof(float) * bl.k.alloc * 4));
-      OSB_CK(cudaMemsetAsync(bl.qf_alt, 0, sizeof(float) * bl.k.alloc * 4, c->stream));
-    }
+    if (!bl.qf_alt) return fail(OSB_EINVAL, "block %d has no FP32 state buffers", ib);
     float* buf[2] = {bl.qf_base, bl.qf_alt};
     for (int p = 0; p < 2; ++p) {
       BatchBlock b;
@@ -337,10 +334,12 @@ int batch_stage(osb_ctx* c, int s, double dt) {
   if (avg == OSB_AVG_ROE) {
     if (sch == OSB_SCHEME_WENO5_JS) rc = launch_batch_t<SCH_WENO5_JS, AVG_ROE>(c, tab, sp, kind, c->A[s], c->B[s], dt, save);
     else if (sch == OSB_SCHEME_WENO5_Z) rc = launch_batch_t<SCH_WENO5_Z, AVG_ROE>(c, tab, sp, kind, c->A[s], c->B[s], dt, save);
+    else if (sch == OSB_SCHEME_TENO6) rc = launch_batch_t<SCH_TENO6, AVG_ROE>(c, tab, sp, kind, c->A[s], c->B[s], dt, save);
     else rc = launch_batch_t<SCH_TENO5, AVG_ROE>(c, tab, sp, kind, c->A[s], c->B[s], dt, save);
   } else {
     if (sch == OSB_SCHEME_WENO5_JS) rc = launch_batch_t<SCH_WENO5_JS, AVG_SIMPLE>(c, tab, sp, kind, c->A[s], c->B[s], dt, save);
     else if (sch == OSB_SCHEME_WENO5_Z) rc = launch_batch_t<SCH_WENO5_Z, AVG_SIMPLE>(c, tab, sp, kind, c->A[s], c->B[s], dt, save);
+    else if (sch == OSB_SCHEME_TENO6) rc = launch_batch_t<SCH_TENO6, AVG_SIMPLE>(c, tab, sp, kind, c->A[s], c->B[s], dt, save);
     else rc = launch_batch_t<SCH_TENO5, AVG_SIMPLE>(c, tab, sp, kind, c->A[s], c->B[s], dt, save);
   }
   if (rc) return rc;

@@ -5,32 +5,41 @@
 namespace osb {
 namespace {
 
-template <typename T, bool CONV, int VISC>
-int launch_central_t(osb_ctx* c, Block& bl, int first) {
+template <typename T, bool CONV, int VISC, bool FUSE>
+int launch_central_k(osb_ctx* c, Block& bl, int first, const RkFuse& rf) {
   using Fd = CentralFields<T, CONV, VISC>;
   size_t smem = (size_t)Fd::N * CPTS * sizeof(T);
-  auto kern = k_central3d<T, CONV, VISC>;
+  auto kern = k_central3d<T, CONV, VISC, FUSE>;
   OSB_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   CentralParams cp{bl.d.gama, bl.d.Minf, bl.d.Re, bl.d.Pr, bl.d.mu_const};
   const BlockK& k = bl.k;
   dim3 grid((k.n[0] + CX - 1) / CX, (k.n[1] + CY - 1) / CY, (k.n[2] + CZ - 1) / CZ);
   timing_begin(c, FAM_CENTRAL);
-  kern<<<grid, CX * CY, smem, c->stream>>>(k, cp, first);
+  kern<<<grid, CX * CY, smem, c->stream>>>(k, cp, first, rf);
   timing_end(c);
   c->launches++;
   return OSB_OK;
 }
 
+// With rf (FP32 path) the kernel applies the RK update instead of storing the residual.
+template <typename T, bool CONV, int VISC>
+int launch_central_t(osb_ctx* c, Block& bl, int first, const RkFuse* rf) {
+  if constexpr (sizeof(T) == 4) {
+    if (rf) return launch_central_k<T, CONV, VISC, true>(c, bl, first, *rf);
+  }
+  return launch_central_k<T, CONV, VISC, false>(c, bl, first, RkFuse{});
+}
+
 template <typename T>
-int launch_central(osb_ctx* c, Block& bl, bool conv, int first) {
+int launch_central(osb_ctx* c, Block& bl, bool conv, int first, const RkFuse* rf) {
   const int visc = bl.d.viscous;
   if (conv) {
-    if (visc == OSB_VISC_SUTHERLAND) return launch_central_t<T, true, 1>(c, bl, first);
-    if (visc == OSB_VISC_CONSTANT) return launch_central_t<T, true, 2>(c, bl, first);
-    return launch_central_t<T, true, 0>(c, bl, first);
+    if (visc == OSB_VISC_SUTHERLAND) return launch_central_t<T, true, 1>(c, bl, first, rf);
+    if (visc == OSB_VISC_CONSTANT) return launch_central_t<T, true, 2>(c, bl, first, rf);
+    return launch_central_t<T, true, 0>(c, bl, first, rf);
   }
-  if (visc == OSB_VISC_SUTHERLAND) return launch_central_t<T, false, 1>(c, bl, first);
-  if (visc == OSB_VISC_CONSTANT) return launch_central_t<T, false, 2>(c, bl, first);
+  if (visc == OSB_VISC_SUTHERLAND) return launch_central_t<T, false, 1>(c, bl, first, rf);
+  if (visc == OSB_VISC_CONSTANT) return launch_central_t<T, false, 2>(c, bl, first, rf);
   return OSB_OK;
 }
 
@@ -41,8 +50,8 @@ int launch_central(osb_ctx* c, Block& bl, bool conv, int first) {
 #define OSB_CENTRAL_NAME central_f64
 #endif
 
-int OSB_CENTRAL_NAME(osb_ctx* c, Block& bl, bool conv, int first) {
-  return launch_central<OSB_CENTRAL_T>(c, bl, conv, first);
+int OSB_CENTRAL_NAME(osb_ctx* c, Block& bl, bool conv, int first, const RkFuse* rf) {
+  return launch_central<OSB_CENTRAL_T>(c, bl, conv, first, rf);
 }
 
 }  // namespace osb

@@ -13,12 +13,28 @@
 #ifndef OSB_CURV
 #define OSB_CURV false
 #endif
+// 1D blocks have no second sweep to carry the RK update
+#define ND_FUSABLE(nd) ((nd) >= 2)
 
 namespace osb {
 namespace {
 
+template <typename T, int ND, int D, int SCH, int AVG, bool CURV>
+void launch_sweep(osb_ctx* c, const BlockK& k, const SchemeParams& sp, dim3 grid, int seg, int nseg,
+                  const RkFuse* rf) {
+  if constexpr (sizeof(T) == 4) {
+    if (rf) {
+      k_flux_sweep<T, ND, D, SCH, AVG, CURV, true><<<grid, 128, 0, c->stream>>>(k, sp, seg, nseg, 0, *rf);
+      return;
+    }
+  }
+  k_flux_sweep<T, ND, D, SCH, AVG, CURV, false><<<grid, 128, 0, c->stream>>>(k, sp, seg, nseg, 0, RkFuse{});
+}
+
+// x sweep (writes R), then y[, z] sweeps (accumulate); with rf (FP32 path, 2D/3D) the last
+// sweep applies the RK update instead of storing the residual.
 template <typename T, int ND, int SCH, int AVG, bool CURV>
-int launch_flux(osb_ctx* c, Block& bl, const SchemeParams& sp) {
+int launch_flux(osb_ctx* c, Block& bl, const SchemeParams& sp, const RkFuse* rf) {
   BlockK& k = bl.k;
   cudaStream_t st = c->stream;
   // x sweep (writes R)
@@ -47,8 +63,9 @@ int launch_flux(osb_ctx* c, Block& bl, const SchemeParams& sp) {
     dim3 grid((k.n[0] + 127) / 128, (unsigned)std::min(gy, 65535L), (unsigned)((gy + 65534) / 65535));
     if (grid.z > 1) return fail(OSB_ENOTSUP, "block too large for the sweep grid");
     timing_begin(c, D == 1 ? FAM_FLUX_Y : FAM_FLUX_Z);
-    if (D == 1) k_flux_sweep<T, ND, 1, SCH, AVG, CURV><<<grid, 128, 0, st>>>(k, sp, seg, nseg, 0);
-    else if (ND == 3) k_flux_sweep<T, ND, (ND == 3 ? 2 : 1), SCH, AVG, CURV><<<grid, 128, 0, st>>>(k, sp, seg, nseg, 0);
+    const RkFuse* f = D == ND - 1 ? rf : nullptr;
+    if (D == 1) launch_sweep<T, ND, 1, SCH, AVG, CURV>(c, k, sp, grid, seg, nseg, f);
+    else if (ND == 3) launch_sweep<T, ND, (ND == 3 ? 2 : 1), SCH, AVG, CURV>(c, k, sp, grid, seg, nseg, f);
     timing_end(c);
     c->launches++;
   }
@@ -56,16 +73,18 @@ int launch_flux(osb_ctx* c, Block& bl, const SchemeParams& sp) {
 }
 
 template <typename T, int ND, bool CURV>
-int dispatch_flux_nd(osb_ctx* c, Block& bl, const SchemeParams& sp) {
+int dispatch_flux_nd(osb_ctx* c, Block& bl, const SchemeParams& sp, const RkFuse* rf) {
   const int sch = bl.d.scheme, avg = bl.d.averaging;
   if (avg == OSB_AVG_ROE) {
-    if (sch == OSB_SCHEME_WENO5_JS) return launch_flux<T, ND, SCH_WENO5_JS, AVG_ROE, CURV>(c, bl, sp);
-    if (sch == OSB_SCHEME_WENO5_Z) return launch_flux<T, ND, SCH_WENO5_Z, AVG_ROE, CURV>(c, bl, sp);
-    if (sch == OSB_SCHEME_TENO5) return launch_flux<T, ND, SCH_TENO5, AVG_ROE, CURV>(c, bl, sp);
+    if (sch == OSB_SCHEME_WENO5_JS) return launch_flux<T, ND, SCH_WENO5_JS, AVG_ROE, CURV>(c, bl, sp, rf);
+    if (sch == OSB_SCHEME_WENO5_Z) return launch_flux<T, ND, SCH_WENO5_Z, AVG_ROE, CURV>(c, bl, sp, rf);
+    if (sch == OSB_SCHEME_TENO5) return launch_flux<T, ND, SCH_TENO5, AVG_ROE, CURV>(c, bl, sp, rf);
+    if (sch == OSB_SCHEME_TENO6) return launch_flux<T, ND, SCH_TENO6, AVG_ROE, CURV>(c, bl, sp, rf);
   } else {
-    if (sch == OSB_SCHEME_WENO5_JS) return launch_flux<T, ND, SCH_WENO5_JS, AVG_SIMPLE, CURV>(c, bl, sp);
-    if (sch == OSB_SCHEME_WENO5_Z) return launch_flux<T, ND, SCH_WENO5_Z, AVG_SIMPLE, CURV>(c, bl, sp);
-    if (sch == OSB_SCHEME_TENO5) return launch_flux<T, ND, SCH_TENO5, AVG_SIMPLE, CURV>(c, bl, sp);
+    if (sch == OSB_SCHEME_WENO5_JS) return launch_flux<T, ND, SCH_WENO5_JS, AVG_SIMPLE, CURV>(c, bl, sp, rf);
+    if (sch == OSB_SCHEME_WENO5_Z) return launch_flux<T, ND, SCH_WENO5_Z, AVG_SIMPLE, CURV>(c, bl, sp, rf);
+    if (sch == OSB_SCHEME_TENO5) return launch_flux<T, ND, SCH_TENO5, AVG_SIMPLE, CURV>(c, bl, sp, rf);
+    if (sch == OSB_SCHEME_TENO6) return launch_flux<T, ND, SCH_TENO6, AVG_SIMPLE, CURV>(c, bl, sp, rf);
   }
   return fail(OSB_ENOTSUP, "unsupported scheme/averaging %d/%d", sch, avg);
 }
@@ -74,8 +93,8 @@ int dispatch_flux_nd(osb_ctx* c, Block& bl, const SchemeParams& sp) {
 
 }  // namespace
 
-int OSB_NAME(osb_ctx* c, Block& bl, const SchemeParams& sp) {
-  return dispatch_flux_nd<OSB_T, OSB_ND, OSB_CURV>(c, bl, sp);
+int OSB_NAME(osb_ctx* c, Block& bl, const SchemeParams& sp, const RkFuse* rf) {
+  return dispatch_flux_nd<OSB_T, OSB_ND, OSB_CURV>(c, bl, sp, ND_FUSABLE(OSB_ND) ? rf : nullptr);
 }
 
 }  // namespace osb

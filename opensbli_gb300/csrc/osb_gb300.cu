@@ -70,37 +70,21 @@ __global__ void k_save(BlockK b, int nv) {
   }
 }
 
-// FP32-residual path RK update: the residual arrives as a float-float pair, the state and
-// register stay FP64, and the FP32 shadow of q is rewritten; conversions use integer
-// operations so only the update itself runs on the FP64 pipe.
-__global__ void k_rk32(BlockK b, int nv, int kind, double A, double B, double dt, unsigned long long* bad) {
+// FP32-residual path RK update (blocks whose residual kernels do not carry it): the residual
+// arrives as a float-float pair, the state and register stay FP64, and the next FP32 state goes
+// to rf.qout; conversions use integer operations so only the update runs on the FP64 pipe.
+__global__ void k_rk32(BlockK b, int nv, RkFuse rf) {
   const int npts = b.n[0] * b.n[1] * b.n[2];
-  const double Adt = A * dt, Bdt = B * dt;
-  unsigned long long nb = 0;
+  unsigned nb = 0;
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < npts; t += gridDim.x * blockDim.x) {
     int i = t % b.n[0];
     int r = t / b.n[0];
     int j = r % b.n[1];
     int k = r / b.n[1];
     int id = lin(b, i, j, k);
-    for (int v = 0; v < nv; ++v) {
-      double r0 = f2d_exact(b.Rh[v][id]) + f2d_exact(b.Rl[v][id]);
-      double o = b.rk[v][id];
-      double q = b.q[v][id];
-      if (kind == 0) {
-        o = A * o + dt * r0;
-        q = B * o + q;
-      } else {
-        q = Adt * r0 + o;
-        o = Bdt * r0 + o;
-      }
-      b.rk[v][id] = o;
-      b.q[v][id] = q;
-      b.qf[v][id] = d2f_rn(q);
-      if ((((unsigned)__double2hiint(q) >> 20) & 0x7ffu) == 0x7ffu) ++nb;
-    }
+    for (int v = 0; v < nv; ++v) nb += rk_point(b, rf, v, id, f2d_exact(b.Rh[v][id]) + f2d_exact(b.Rl[v][id]));
   }
-  if (nb) atomicAdd(bad, nb);
+  if (nb) atomicAdd(rf.bad, (unsigned long long)nb);
 }
 
 // (hi + lo) float-float residual -> FP64 array (osb_residual of the FP32-residual path).
@@ -384,33 +368,46 @@ int timing_collect(osb_ctx* c) {
   return OSB_OK;
 }
 
+// Residual kernels of one block.  With rf (FP32 path) the last of them applies the RK update
+// itself (*fused = true): the central kernel when there is one, else the last sweep of a 2D/3D
+// block.
 template <typename T>
-int residual_t(osb_ctx* c, Block& bl) {
+int residual_t(osb_ctx* c, Block& bl, const RkFuse* rf, bool* fused) {
   SchemeParams sp{bl.d.gama, bl.d.eps, bl.d.teno_ct, bl.d.shock_filter_control, 1e-12};
+  if (fused) *fused = false;
   int rc;
   if (bl.d.scheme == OSB_SCHEME_CENTRAL4) {
     if (bl.d.ndim != 3) return fail(OSB_ENOTSUP, "central scheme implemented for 3D blocks");
-    rc = sizeof(T) == 4 ? central_f32(c, bl, true, 1) : central_f64(c, bl, true, 1);
+    rc = sizeof(T) == 4 ? central_f32(c, bl, true, 1, rf) : central_f64(c, bl, true, 1, nullptr);
+    if (fused) *fused = rf != nullptr;
   } else {
     const int nd = bl.d.ndim;
+    const bool visc = bl.d.viscous != OSB_VISC_NONE;
+    // the sweeps do not carry the update: at their 128-register cap the extra FP64 state and
+    // register loads cannot be hidden (measured slower than the separate k_rk32)
+    const RkFuse* rs = nullptr;
     if (bl.k.m[9]) {
-      if (sizeof(T) == 4) rc = nd == 2 ? flux_curv_f32_2d(c, bl, sp) : flux_curv_f32_3d(c, bl, sp);
-      else rc = nd == 2 ? flux_curv_f64_2d(c, bl, sp) : flux_curv_f64_3d(c, bl, sp);
+      if (sizeof(T) == 4) rc = nd == 2 ? flux_curv_f32_2d(c, bl, sp, rs) : flux_curv_f32_3d(c, bl, sp, rs);
+      else rc = nd == 2 ? flux_curv_f64_2d(c, bl, sp, nullptr) : flux_curv_f64_3d(c, bl, sp, nullptr);
     } else if (sizeof(T) == 4) {
-      rc = nd == 1 ? flux_f32_1d(c, bl, sp) : nd == 2 ? flux_f32_2d(c, bl, sp) : flux_f32_3d(c, bl, sp);
+      rc = nd == 1 ? flux_f32_1d(c, bl, sp, nullptr) : nd == 2 ? flux_f32_2d(c, bl, sp, rs) : flux_f32_3d(c, bl, sp, rs);
     } else {
-      rc = nd == 1 ? flux_f64_1d(c, bl, sp) : nd == 2 ? flux_f64_2d(c, bl, sp) : flux_f64_3d(c, bl, sp);
+      rc = nd == 1 ? flux_f64_1d(c, bl, sp, nullptr) : nd == 2 ? flux_f64_2d(c, bl, sp, nullptr)
+                                                          : flux_f64_3d(c, bl, sp, nullptr);
     }
-    if (rc == OSB_OK && bl.d.viscous != OSB_VISC_NONE) {
+    if (fused) *fused = rs != nullptr;
+    if (rc == OSB_OK && visc) {
       if (bl.d.ndim != 3) return fail(OSB_ENOTSUP, "viscous terms implemented for 3D blocks");
-      rc = sizeof(T) == 4 ? central_f32(c, bl, false, 0) : central_f64(c, bl, false, 0);
+      rc = sizeof(T) == 4 ? central_f32(c, bl, false, 0, rf) : central_f64(c, bl, false, 0, nullptr);
+      if (fused) *fused = rf != nullptr;
     }
   }
   return rc;
 }
 
 int residual(osb_ctx* c, Block& bl) {
-  return c->prec == OSB_PREC_FP32_RESIDUAL ? residual_t<float>(c, bl) : residual_t<double>(c, bl);
+  return c->prec == OSB_PREC_FP32_RESIDUAL ? residual_t<float>(c, bl, nullptr, nullptr)
+                                           : residual_t<double>(c, bl, nullptr, nullptr);
 }
 
 int grid_for(osb_ctx* c, long n, int threads) {
@@ -513,6 +510,33 @@ bool use_batch(const osb_ctx* c) {
 
 int stage(osb_ctx* c, int s, double dt) {
   if (use_batch(c)) return batch_stage(c, s, dt);
+  const int kind = c->rk_kind == OSB_RK_LOW_STORAGE ? 0 : 1;
+  if (c->prec == OSB_PREC_FP32_RESIDUAL) {
+    // the last residual kernel of each block applies the RK update and writes the next FP32
+    // state into the other buffer; blocks without such a kernel (1D) use k_rk32
+    for (auto& bl : c->blocks) {
+      RkFuse rf{};
+      rf.kind = kind;
+      rf.A = c->A[s];
+      rf.B = c->B[s];
+      rf.dt = dt;
+      rf.bad = c->bad;
+      float* out = c->qf_parity ? bl.qf_base : bl.qf_alt;
+      for (int v = 0; v < bl.d.ndim + 2; ++v) rf.qout[v] = out + (size_t)v * bl.k.alloc;
+      bool fused = false;
+      int rc = residual_t<float>(c, bl, c->sched.fuse_update ? &rf : nullptr, &fused);
+      if (rc) return rc;
+      if (!fused) {
+        long n = (long)bl.k.n[0] * bl.k.n[1] * bl.k.n[2];
+        timing_begin(c, FAM_RK);
+        k_rk32<<<grid_for(c, n, 256), 256, 0, c->stream>>>(bl.k, bl.d.ndim + 2, rf);
+        timing_end(c);
+        c->launches++;
+      }
+    }
+    batch_set_parity(c, c->qf_parity ^ 1);
+    return apply_bc(c);
+  }
   for (auto& bl : c->blocks) {
     int rc = residual(c, bl);
     if (rc) return rc;
@@ -520,12 +544,7 @@ int stage(osb_ctx* c, int s, double dt) {
   for (auto& bl : c->blocks) {
     long n = (long)bl.k.n[0] * bl.k.n[1] * bl.k.n[2];
     timing_begin(c, FAM_RK);
-    if (c->prec == OSB_PREC_FP32_RESIDUAL)
-      k_rk32<<<grid_for(c, n, 256), 256, 0, c->stream>>>(bl.k, bl.d.ndim + 2, c->rk_kind == OSB_RK_LOW_STORAGE ? 0 : 1,
-                                                          c->A[s], c->B[s], dt, c->bad);
-    else
-      k_rk<<<grid_for(c, n, 256), 256, 0, c->stream>>>(bl.k, bl.d.ndim + 2, c->rk_kind == OSB_RK_LOW_STORAGE ? 0 : 1,
-                                                        c->A[s], c->B[s], dt, c->bad);
+    k_rk<<<grid_for(c, n, 256), 256, 0, c->stream>>>(bl.k, bl.d.ndim + 2, kind, c->A[s], c->B[s], dt, c->bad);
     timing_end(c);
     c->launches++;
   }
@@ -589,7 +608,7 @@ bool check_desc(const osb_block_desc* d, std::string& why) {
   for (int i = d->ndim; i < 3; ++i)
     if (d->size[i] != 1) { why = "unused directions must have size 1"; return false; }
   if (!(d->scheme == OSB_SCHEME_WENO5_JS || d->scheme == OSB_SCHEME_WENO5_Z || d->scheme == OSB_SCHEME_TENO5 ||
-        d->scheme == OSB_SCHEME_CENTRAL4)) { why = "unknown scheme"; return false; }
+        d->scheme == OSB_SCHEME_TENO6 || d->scheme == OSB_SCHEME_CENTRAL4)) { why = "unknown scheme"; return false; }
   if (d->averaging != OSB_AVG_SIMPLE && d->averaging != OSB_AVG_ROE) { why = "unknown averaging"; return false; }
   for (int v = 0; v < d->ndim + 2; ++v)
     if (!d->q[v] || !d->rkold[v]) { why = "null state or RK array"; return false; }
@@ -758,6 +777,13 @@ int osb_block_add(osb_ctx* c, const osb_block_desc* d, int* block_id) {
     }
     for (int v = 0; v < nv; ++v) k.qf[v] = qf + (size_t)v * k.alloc;
     bl.qf_base = qf;
+    e = cudaMalloc(&bl.qf_alt, sizeof(float) * k.alloc * nv);  // ping-pong partner
+    if (e != cudaSuccess) {
+      cudaFree(R);
+      cudaFree(qf);
+      return fail(OSB_ECUDA, "FP32 state: %s", cudaGetErrorString(e));
+    }
+    OSB_CK(cudaMemsetAsync(bl.qf_alt, 0, sizeof(float) * k.alloc * nv, c->stream));
   }
   for (int i = 0; i < 10; ++i) k.m[i] = d->metric[i];
   if (k.m[9] && c->prec == OSB_PREC_FP32_RESIDUAL) {
@@ -767,7 +793,8 @@ int osb_block_add(osb_ctx* c, const osb_block_desc* d, int* block_id) {
     cudaError_t e = cudaMalloc(&mf, sizeof(float) * k.alloc * nm);
     if (e != cudaSuccess) {
       cudaFree(R);
-      cudaFree(k.qf[0]);
+      cudaFree(bl.qf_base);
+      cudaFree(bl.qf_alt);
       return fail(OSB_ECUDA, "FP32 metrics: %s", cudaGetErrorString(e));
     }
     bl.mf_buf = mf;
@@ -852,7 +879,7 @@ int osb_step(osb_ctx* c, double dt, int nsteps) {
     OSB_CK(cudaGetLastError());
     return OSB_OK;
   }
-  if (batch) {
+  if (c->prec == OSB_PREC_FP32_RESIDUAL) {
     // one graph per FP32-buffer parity; a step flips the parity when the stage count is odd
     if (c->g_dt != dt) {
       drop_graph(c);
@@ -882,8 +909,10 @@ int osb_step(osb_ctx* c, double dt, int nsteps) {
       c->launches += c->g_kernels;
       batch_set_parity(c, p ^ (c->nst & 1));
     }
-    int rc = apply_bc(c);  // halos of q and of the current FP32 buffer for observers
-    if (rc) return rc;
+    if (batch) {
+      int rc = apply_bc(c);  // halos of q and of the current FP32 buffer for observers
+      if (rc) return rc;
+    }
     OSB_CK(cudaGetLastError());
     return OSB_OK;
   }
@@ -995,6 +1024,7 @@ int osb_set_schedule(osb_ctx* c, const osb_schedule* sched) {
     return fail(OSB_EINVAL, "tile_y must be 8, 16 or 32");
   if (sched->ctas_per_sm < 1 || sched->ctas_per_sm > 16) return fail(OSB_EINVAL, "ctas_per_sm must be 1..16");
   if (sched->order < 0 || sched->order > 2) return fail(OSB_EINVAL, "order must be 0, 1 or 2");
+  if (sched->fuse_update != 0 && sched->fuse_update != 1) return fail(OSB_EINVAL, "fuse_update must be 0 or 1");
   if (sched->mode == OSB_SCHED_PERSISTENT) {
     std::string why;
     if (!batch_eligible(c, &why)) return fail(OSB_ENOTSUP, "%s", why.c_str());

@@ -59,7 +59,7 @@ struct osb_ctx {
   bool graphs = true;
   cudaGraphExec_t gexec = nullptr;
   cudaGraphExec_t gexec_p[2] = {nullptr, nullptr};  // persistent stage: one graph per FP32 parity
-  osb_schedule sched = {OSB_SCHED_AUTO, 16, 2, 1, 0};
+  osb_schedule sched = {OSB_SCHED_AUTO, 16, 2, 1, 0, 1};
   osb::BatchState batch;
   int qf_parity = 0;
   double g_dt = 0.0;
@@ -84,19 +84,20 @@ namespace osb {
 void timing_begin(osb_ctx* c, int fam);
 void timing_end(osb_ctx* c);
 
-// Characteristic flux sweeps of one block (x writes R, y/z accumulate); one instantiation per
-// precision and dimension lives in osb_flux.cu.
-int flux_f64_1d(osb_ctx* c, Block& bl, const SchemeParams& sp);
-int flux_f64_2d(osb_ctx* c, Block& bl, const SchemeParams& sp);
-int flux_f64_3d(osb_ctx* c, Block& bl, const SchemeParams& sp);
-int flux_f32_1d(osb_ctx* c, Block& bl, const SchemeParams& sp);
-int flux_f32_2d(osb_ctx* c, Block& bl, const SchemeParams& sp);
-int flux_f32_3d(osb_ctx* c, Block& bl, const SchemeParams& sp);
+// Characteristic flux sweeps of one block (x writes R, y/z accumulate; with rf the last sweep
+// applies the RK update, FP32 path, 2D/3D); one instantiation per precision and dimension lives
+// in osb_flux.cu.
+int flux_f64_1d(osb_ctx* c, Block& bl, const SchemeParams& sp, const RkFuse* rf);
+int flux_f64_2d(osb_ctx* c, Block& bl, const SchemeParams& sp, const RkFuse* rf);
+int flux_f64_3d(osb_ctx* c, Block& bl, const SchemeParams& sp, const RkFuse* rf);
+int flux_f32_1d(osb_ctx* c, Block& bl, const SchemeParams& sp, const RkFuse* rf);
+int flux_f32_2d(osb_ctx* c, Block& bl, const SchemeParams& sp, const RkFuse* rf);
+int flux_f32_3d(osb_ctx* c, Block& bl, const SchemeParams& sp, const RkFuse* rf);
 // The same for curvilinear blocks (metric arrays present).
-int flux_curv_f64_2d(osb_ctx* c, Block& bl, const SchemeParams& sp);
-int flux_curv_f64_3d(osb_ctx* c, Block& bl, const SchemeParams& sp);
-int flux_curv_f32_2d(osb_ctx* c, Block& bl, const SchemeParams& sp);
-int flux_curv_f32_3d(osb_ctx* c, Block& bl, const SchemeParams& sp);
+int flux_curv_f64_2d(osb_ctx* c, Block& bl, const SchemeParams& sp, const RkFuse* rf);
+int flux_curv_f64_3d(osb_ctx* c, Block& bl, const SchemeParams& sp, const RkFuse* rf);
+int flux_curv_f32_2d(osb_ctx* c, Block& bl, const SchemeParams& sp, const RkFuse* rf);
+int flux_curv_f32_3d(osb_ctx* c, Block& bl, const SchemeParams& sp, const RkFuse* rf);
 // Persistent fused stage for batches of 2D periodic blocks (osb_batch.cu).
 bool batch_eligible(const osb_ctx* c, std::string* why);
 int batch_build(osb_ctx* c);
@@ -105,7 +106,7 @@ void batch_set_parity(osb_ctx* c, int parity);
 int batch_stage(osb_ctx* c, int s, double dt);
 size_t batch_smem(int ty);
 // Central convective and/or viscous terms of one 3D block (osb_central.cu).
-int central_f64(osb_ctx* c, Block& bl, bool conv, int first);
-int central_f32(osb_ctx* c, Block& bl, bool conv, int first);
+int central_f64(osb_ctx* c, Block& bl, bool conv, int first, const RkFuse* rf);
+int central_f32(osb_ctx* c, Block& bl, bool conv, int first, const RkFuse* rf);
 
 }  // namespace osb

@@ -239,6 +239,53 @@ __device__ __forceinline__ void rp_store(const BlockK& b, int v, int id, float c
   b.Rl[v][id] = l;
 }
 
+// Fused RK epilogue of the last residual kernel of a stage (FP32-residual path).  There the
+// residual of a point is complete, so the kernel applies the FP64 RK update (rk_LS.py:204-215,
+// rk_sbli.py:138-145) itself and writes the next stage's FP32 state into the other buffer of a
+// ping-pong pair: the kernel reads the current buffer, so no thread sees a partial update.
+struct RkFuse {
+  int kind;  // 0 low-storage, 1 SBLI
+  double A, B, dt;
+  float* qout[5];
+  unsigned long long* bad;
+};
+
+__device__ __forceinline__ unsigned rk_point_qo(const BlockK& b, const RkFuse& rf, int v, int id, double r0, double q,
+                                                double o) {
+  if (rf.kind == 0) {
+    o = rf.A * o + rf.dt * r0;
+    q = rf.B * o + q;
+  } else {
+    q = (rf.A * rf.dt) * r0 + o;
+    o = (rf.B * rf.dt) * r0 + o;
+  }
+  b.rk[v][id] = o;
+  b.q[v][id] = q;
+  rf.qout[v][id] = d2f_rn(q);
+  return ((((unsigned)__double2hiint(q) >> 20) & 0x7ffu) == 0x7ffu) ? 1u : 0u;
+}
+__device__ __forceinline__ unsigned rk_point(const BlockK& b, const RkFuse& rf, int v, int id, double r0) {
+  return rk_point_qo(b, rf, v, id, r0, b.q[v][id], b.rk[v][id]);
+}
+
+// Final residual of a point from its prefetched partial value plus the last contribution.
+__device__ __forceinline__ double r_final(float fnew, float fold, float invd, float h, float l) {
+  float p, pe;
+  ff_flux_diff(fnew, fold, invd, p, pe);
+  ff_add(h, l, p, pe);
+  return f2d_exact(h) + f2d_exact(l);
+}
+__device__ __forceinline__ double r_final(double fnew, double fold, double invd, double h, double) {
+  return h + -(fnew - fold) * invd;
+}
+__device__ __forceinline__ double rp_final(float c, float h, float l) {
+  ff_add(h, l, c, 0.f);
+  return f2d_exact(h) + f2d_exact(l);
+}
+__device__ __forceinline__ double rp_final(double c, double h, double) { return h + c; }
+__device__ __forceinline__ double to_d(float x) { return f2d_exact(x); }
+__device__ __forceinline__ double to_d(double x) { return x; }
+
 // Residual update with a pointwise contribution c.
 __device__ __forceinline__ void acc_point(const BlockK& b, int v, int id, double c, int first) {
   b.R[v][id] = first ? c : b.R[v][id] + c;
@@ -267,8 +314,9 @@ __device__ __forceinline__ int gvar(int lv) {
 
 // ---------------------------------------------------------------------------------------
 // Sweep along y (D=1) or z (D=2): thread = (x, transverse, segment).
-template <typename T, int ND, int D, int SCH, int AVG, bool CURV>
-__global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 1) k_flux_sweep(BlockK b, SchemeParams spd, int seg, int nseg, int first) {
+template <typename T, int ND, int D, int SCH, int AVG, bool CURV, bool FUSE>
+__global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 1)
+    k_flux_sweep(BlockK b, SchemeParams spd, int seg, int nseg, int first, RkFuse rf) {
   constexpr int NV = ND + 2;
   constexpr int NF = SweepFields<ND, CURV>::N;
   using P = typename SweepPt<T, ND, CURV>::type;
@@ -308,6 +356,7 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 1) k_flux_sweep(Bloc
   T fprev[NV];
 #pragma unroll
   for (int lv = 0; lv < NV; ++lv) fprev[lv] = L_(0.0);
+  unsigned nbad = 0;
   for (int j = j0 - 1; j < j1; ++j) {
 #pragma unroll
     for (int m = 0; m < 5; ++m) w[m] = w[m + 1];
@@ -334,7 +383,11 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 1) k_flux_sweep(Bloc
       char_flux<T, ND, SCH, AVG>(w, sp, fh);
     }
     if (j >= j0) {
-      if (first) {
+      if (FUSE) {
+#pragma unroll
+        for (int lv = 0; lv < NV; ++lv)
+          nbad += rk_point(b, rf, gvar<ND, D, CURV>(lv), id, r_final(fh[lv], fprev[lv], sc, oh[lv], ol[lv]));
+      } else if (first) {
 #pragma unroll
         for (int lv = 0; lv < NV; ++lv) acc_flux(b, gvar<ND, D, CURV>(lv), id, fh[lv], fprev[lv], sc, 1);
       } else {
@@ -345,14 +398,15 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 1) k_flux_sweep(Bloc
 #pragma unroll
     for (int lv = 0; lv < NV; ++lv) fprev[lv] = fh[lv];
   }
+  if (FUSE && nbad) atomicAdd(rf.bad, (unsigned long long)nbad);
 }
 
 // ---------------------------------------------------------------------------------------
 // Sweep along x.  A warp owns 32 rows (fixed y, z) and a segment of XSEG points; the state of
 // columns s0-3 .. s0+XSEG+2 of its rows is staged in shared memory with coalesced loads, then
 // lane r sweeps row r out of shared memory.
-constexpr int XSEG = 26;
-constexpr int XPITCH = 33;
+constexpr int XSEG = 14;   // interfaces per segment: 20 staged columns, 16 warps per SM
+constexpr int XPITCH = 21; // odd pitch: lanes (rows) hit distinct banks
 constexpr int XWARPS = 2;
 
 template <typename T, int ND, int SCH, int AVG, bool CURV>
@@ -450,8 +504,8 @@ struct CentralFields {
   static constexpr int N = CONV ? (VISC ? 11 : 9) : 6;
 };
 
-template <typename T, bool CONV, int VISC>
-__global__ void __launch_bounds__(CX * CY) k_central3d(BlockK b, CentralParams cp, int first) {
+template <typename T, bool CONV, int VISC, bool FUSE>
+__global__ void __launch_bounds__(CX * CY) k_central3d(BlockK b, CentralParams cp, int first, RkFuse rf) {
   using Fd = CentralFields<T, CONV, VISC>;
   extern __shared__ __align__(16) unsigned char osb_smem[];
   T* sm = reinterpret_cast<T*>(osb_smem);
@@ -536,7 +590,16 @@ __global__ void __launch_bounds__(CX * CY) k_central3d(BlockK b, CentralParams c
     T oh[5], ol[5];
     if (!first) {
 #pragma unroll
-      for (int v = CONV ? 0 : 1; v < 5; ++v) r_load(b, v, gid, oh[v], ol[v]);
+      for (int v = (CONV || FUSE) ? 0 : 1; v < 5; ++v) r_load(b, v, gid, oh[v], ol[v]);
+    }
+    // the fused update's state and register, loaded before the derivative work hides them
+    double fq[5], fo[5];
+    if (FUSE) {
+#pragma unroll
+      for (int v = 0; v < 5; ++v) {
+        fq[v] = b.q[v][gid];
+        fo[v] = b.rk[v][gid];
+      }
     }
     T racc[5] = {L_(0.0), L_(0.0), L_(0.0), L_(0.0), L_(0.0)};
     const int S[3] = {sx, sy, sz};
@@ -634,7 +697,16 @@ __global__ void __launch_bounds__(CX * CY) k_central3d(BlockK b, CentralParams c
       racc[4] += e * invRe + h * kheat;
     }
     const int v0 = CONV ? 0 : 1;
-    if (first) {
+    if (FUSE) {
+      // a first (only) residual kernel starts from zero; otherwise from the partial residual
+      unsigned nb = 0;
+#pragma unroll
+      for (int v = 0; v < 5; ++v) {
+        const double r0 = first ? to_d(racc[v]) : rp_final(v < v0 ? L_(0.0) : racc[v], oh[v], ol[v]);
+        nb += rk_point_qo(b, rf, v, gid, r0, fq[v], fo[v]);
+      }
+      if (nb) atomicAdd(rf.bad, (unsigned long long)nb);
+    } else if (first) {
 #pragma unroll
       for (int v = v0; v < 5; ++v) acc_point(b, v, gid, racc[v], 1);
     } else {

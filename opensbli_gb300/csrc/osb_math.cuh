@@ -14,7 +14,7 @@
 
 namespace osb {
 
-enum { SCH_WENO5_JS = 1, SCH_WENO5_Z = 2, SCH_TENO5 = 3, SCH_CENTRAL4 = 5 };
+enum { SCH_WENO5_JS = 1, SCH_WENO5_Z = 2, SCH_TENO5 = 3, SCH_TENO6 = 4, SCH_CENTRAL4 = 5 };
 enum { AVG_SIMPLE = 0, AVG_ROE = 1 };
 
 template <typename T> struct Lit;
@@ -127,6 +127,89 @@ __device__ __forceinline__ T recon5(T fm2, T fm1, T f0, T fp1, T fp2, const SP<T
   }
 }
 
+// Sixth-order TENO at the interface i+1/2 from six points f0..f5 = i-2..i+3 (teno.py:59-194 for
+// sides +1 / -1, 220-240 tau_6 = |b3 - (b0 + b2 - 4 b1)/6|, 419-477 cut-off and weights with
+// optimal weights 231/500, 3/10, 27/500, 23/125).  Side +1 reconstructs the positive split
+// flux, side -1 the negative one.  The reference's side +1 fourth smoothness indicator has its
+// 781/720 term unsquared (teno.py:160-161, squared on side -1), and so does this: its generated
+// solvers compute it that way.  The FP32 path uses the rescaled epsilon of recon5 and forms
+// the cut-off from t_r / max|t|.
+template <typename T, int SIDE>
+__device__ __forceinline__ T recon6(T fm2, T fm1, T f0, T fp1, T fp2, T fp3, const SP<T>& sp) {
+  constexpr bool F32 = sizeof(T) == 4;
+  T b0, b1, b2, b3, e0, e1, e2, e3;
+  if (SIDE > 0) {
+    T s0 = fm1 - fp1, c0 = fm1 - L_(2.0) * f0 + fp1;
+    T s1 = L_(3.0) * f0 - L_(4.0) * fp1 + fp2, c1 = f0 - L_(2.0) * fp1 + fp2;
+    T s2 = fm2 - L_(4.0) * fm1 + L_(3.0) * f0, c2 = fm2 - L_(2.0) * fm1 + f0;
+    b0 = L_(0.25) * s0 * s0 + L_(13.0 / 12.0) * c0 * c0;
+    b1 = L_(0.25) * s1 * s1 + L_(13.0 / 12.0) * c1 * c1;
+    b2 = L_(0.25) * s2 * s2 + L_(13.0 / 12.0) * c2 * c2;
+    T u1 = -L_(11.0) * f0 + L_(18.0) * fp1 - L_(9.0) * fp2 + L_(2.0) * fp3;
+    T u2 = L_(2.0) * f0 - L_(5.0) * fp1 + L_(4.0) * fp2 - fp3;
+    T u3 = -f0 + L_(3.0) * fp1 - L_(3.0) * fp2 + fp3;
+    b3 = L_(1.0 / 36.0) * u1 * u1 + L_(13.0 / 12.0) * u2 * u2 + L_(781.0 / 720.0) * u3;
+    e0 = -L_(1.0 / 6.0) * fm1 + L_(5.0 / 6.0) * f0 + L_(2.0 / 6.0) * fp1;
+    e1 = L_(2.0 / 6.0) * f0 + L_(5.0 / 6.0) * fp1 - L_(1.0 / 6.0) * fp2;
+    e2 = L_(2.0 / 6.0) * fm2 - L_(7.0 / 6.0) * fm1 + L_(11.0 / 6.0) * f0;
+    e3 = L_(3.0 / 12.0) * f0 + L_(13.0 / 12.0) * fp1 - L_(5.0 / 12.0) * fp2 + L_(1.0 / 12.0) * fp3;
+  } else {
+    T s0 = f0 - fp2, c0 = f0 - L_(2.0) * fp1 + fp2;
+    T s1 = fm1 - L_(4.0) * f0 + L_(3.0) * fp1, c1 = fm1 - L_(2.0) * f0 + fp1;
+    T s2 = L_(3.0) * fp1 - L_(4.0) * fp2 + fp3, c2 = fp1 - L_(2.0) * fp2 + fp3;
+    b0 = L_(0.25) * s0 * s0 + L_(13.0 / 12.0) * c0 * c0;
+    b1 = L_(0.25) * s1 * s1 + L_(13.0 / 12.0) * c1 * c1;
+    b2 = L_(0.25) * s2 * s2 + L_(13.0 / 12.0) * c2 * c2;
+    T u1 = -L_(2.0) * fm2 + L_(9.0) * fm1 - L_(18.0) * f0 + L_(11.0) * fp1;
+    T u2 = -fm2 + L_(4.0) * fm1 - L_(5.0) * f0 + L_(2.0) * fp1;
+    T u3 = -fm2 + L_(3.0) * fm1 - L_(3.0) * f0 + fp1;
+    b3 = L_(1.0 / 36.0) * u1 * u1 + L_(13.0 / 12.0) * u2 * u2 + L_(781.0 / 720.0) * u3 * u3;
+    e0 = L_(2.0 / 6.0) * f0 + L_(5.0 / 6.0) * fp1 - L_(1.0 / 6.0) * fp2;
+    e1 = -L_(1.0 / 6.0) * fm1 + L_(5.0 / 6.0) * f0 + L_(2.0 / 6.0) * fp1;
+    e2 = L_(11.0 / 6.0) * fp1 - L_(7.0 / 6.0) * fp2 + L_(1.0 / 3.0) * fp3;
+    e3 = L_(1.0 / 12.0) * fm2 - L_(5.0 / 12.0) * fm1 + L_(13.0 / 12.0) * f0 + L_(3.0 / 12.0) * fp1;
+  }
+  const T tau = fabs(b3 - L_(1.0 / 6.0) * (b0 + b2 - L_(4.0) * b1));
+  T a0, a1, a2, a3;
+  if (F32) {
+    T eps = sp.eps32_rel * (fm2 * fm2 + fm1 * fm1 + f0 * f0 + fp1 * fp1 + fp2 * fp2 + fp3 * fp3) * L_(1.0 / 6.0) +
+            L_(1e-30);
+    T t0 = L_(1.0) + tau / (eps + b0), t1 = L_(1.0) + tau / (eps + b1), t2 = L_(1.0) + tau / (eps + b2),
+      t3 = L_(1.0) + tau / (eps + b3);
+    T im = L_(1.0) / fmax(fmax(fabs(t0), fabs(t1)), fmax(fabs(t2), fabs(t3)));
+    t0 *= im; t1 *= im; t2 *= im; t3 *= im;
+    a0 = t0 * t0 * t0; a0 = a0 * a0;
+    a1 = t1 * t1 * t1; a1 = a1 * a1;
+    a2 = t2 * t2 * t2; a2 = a2 * a2;
+    a3 = t3 * t3 * t3; a3 = a3 * a3;
+  } else {
+    const T eps = sp.teno_eps;
+    T t0 = L_(1.0) + tau / (eps + b0), t1 = L_(1.0) + tau / (eps + b1), t2 = L_(1.0) + tau / (eps + b2),
+      t3 = L_(1.0) + tau / (eps + b3);
+    a0 = t0 * t0 * t0 * t0 * t0 * t0;
+    a1 = t1 * t1 * t1 * t1 * t1 * t1;
+    a2 = t2 * t2 * t2 * t2 * t2 * t2;
+    a3 = t3 * t3 * t3 * t3 * t3 * t3;
+  }
+  const T inv = L_(1.0) / (a0 + a1 + a2 + a3);
+  const T ct = sp.teno_ct;
+  const T w0 = (a0 * inv < ct) ? L_(0.0) : L_(231.0 / 500.0);
+  const T w1 = (a1 * inv < ct) ? L_(0.0) : L_(3.0 / 10.0);
+  const T w2 = (a2 * inv < ct) ? L_(0.0) : L_(27.0 / 500.0);
+  const T w3 = (a3 * inv < ct) ? L_(0.0) : L_(23.0 / 125.0);
+  return (w0 * e0 + w1 * e1 + w2 * e2 + w3 * e3) * (L_(1.0) / (w0 + w1 + w2 + w3));
+}
+
+// Reconstruction of one characteristic wave at i+1/2 from the positive and negative split
+// fluxes at points i-2..i+3.
+template <typename T, int SCH>
+__device__ __forceinline__ T recon_wave(const T (&fp)[6], const T (&fm)[6], const SP<T>& sp) {
+  if (SCH == SCH_TENO6)
+    return recon6<T, 1>(fp[0], fp[1], fp[2], fp[3], fp[4], fp[5], sp) +
+           recon6<T, -1>(fm[0], fm[1], fm[2], fm[3], fm[4], fm[5], sp);
+  return recon5<T, SCH>(fp[0], fp[1], fp[2], fp[3], fp[4], sp) + recon5<T, SCH>(fm[5], fm[4], fm[3], fm[2], fm[1], sp);
+}
+
 // Point data carried through a sweep: conserved state in the local frame plus primitives.
 template <typename T, int ND>
 struct Pt {
@@ -217,9 +300,7 @@ __device__ __forceinline__ void char_flux(const Pt<T, ND> (&w)[6], const SP<T>& 
       }
     }
 #pragma unroll
-    for (int k = 0; k < 3; ++k)
-      rec[k] = recon5<T, SCH>(fp[k][0], fp[k][1], fp[k][2], fp[k][3], fp[k][4], sp) +
-               recon5<T, SCH>(fmn[k][5], fmn[k][4], fmn[k][3], fmn[k][2], fmn[k][1], sp);
+    for (int k = 0; k < 3; ++k) rec[k] = recon_wave<T, SCH>(fp[k], fmn[k], sp);
     fh[0] = rec[0] + rec[1] + rec[2];
     fh[1] = (u0 - a) * rec[0] + u0 * rec[1] + (u0 + a) * rec[2];
     fh[2] = (H - u0 * a) * rec[0] + L_(0.5) * u0 * u0 * rec[1] + (H + u0 * a) * rec[2];
@@ -274,9 +355,7 @@ __device__ __forceinline__ void char_flux(const Pt<T, ND> (&w)[6], const SP<T>& 
     }
   }
 #pragma unroll
-  for (int k = 0; k < NV; ++k)
-    rec[k] = recon5<T, SCH>(fp[k][0], fp[k][1], fp[k][2], fp[k][3], fp[k][4], sp) +
-             recon5<T, SCH>(fmn[k][5], fmn[k][4], fmn[k][3], fmn[k][2], fmn[k][1], sp);
+  for (int k = 0; k < NV; ++k) rec[k] = recon_wave<T, SCH>(fp[k], fmn[k], sp);
   // back to physical space with the REV columns (k = e_0)
   const T rp = rec[ND] + rec[ND + 1], rm = rec[ND] - rec[ND + 1];
   const T F0 = rec[0] + alf * rp;
@@ -448,9 +527,7 @@ __device__ __forceinline__ void char_flux_curv(const PtC<T, ND> (&w)[6], const S
   }
   T rec[NV];
 #pragma unroll
-  for (int c = 0; c < NV; ++c)
-    rec[c] = recon5<T, SCH>(fp[c][0], fp[c][1], fp[c][2], fp[c][3], fp[c][4], sp) +
-             recon5<T, SCH>(fmn[c][5], fmn[c][4], fmn[c][3], fmn[c][2], fmn[c][1], sp);
+  for (int c = 0; c < NV; ++c) rec[c] = recon_wave<T, SCH>(fp[c], fmn[c], sp);
   // REV: 2D columns (1, u, phi/g1), rho (0, t, t.u) with t = (k1, -k0), and the acoustic
   // pair alf (1, u +- a k, h0 +- a th); 3D vorticity columns give u (k.r) + rho (k x r) and
   // phi/g1 (k.r) + rho (u x k).r.

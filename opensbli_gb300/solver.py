@@ -92,10 +92,10 @@ class Solver:
         Bb = (ctypes.c_double * len(B))(*B)
         abi.check(self.lib, self.lib.osb_set_rk(self.ctx, kind, len(A), Aa, Bb), "osb_set_rk")
 
-    def set_schedule(self, mode=abi.SCHED_AUTO, tile_y=16, ctas_per_sm=2, dynamic=1, order=0):
+    def set_schedule(self, mode=abi.SCHED_AUTO, tile_y=16, ctas_per_sm=2, dynamic=1, order=0, fuse_update=1):
         """Stage schedule (osb_set_schedule): per-block launches or one persistent launch per
-        stage, with the persistent stage's tiling knobs."""
-        sc = abi.Schedule(mode, tile_y, ctas_per_sm, dynamic, order)
+        stage, with the persistent stage's tiling knobs and the per-block path's RK fusion."""
+        sc = abi.Schedule(mode, tile_y, ctas_per_sm, dynamic, order, fuse_update)
         abi.check(self.lib, self.lib.osb_set_schedule(self.ctx, ctypes.byref(sc)), "osb_set_schedule")
 
     def schedule(self):

@@ -272,6 +272,70 @@ static double recon5(int scheme, const double* f, double teno_eps, double teno_c
   return (a0 * inv) * e0 + (a1 * inv) * e1 + (a2 * inv) * e2;
 }
 
+/* Sixth-order TENO (teno.py:59-194 configuration for sides +1 / -1, 220-240 tau_6, 419-477
+ * cut-off and weights) at interface i+1/2 from the six points f[0..5] = i-2..i+3.  Side +1
+ * reconstructs the positive split flux, side -1 the negative one.  The reference's side +1
+ * fourth smoothness indicator carries its 781/720 term unsquared (teno.py:160-161, unlike side
+ * -1 at teno.py:169-171); its generated solver computes it that way and so does this. */
+static double recon6(int side, const double* f, double teno_eps, double teno_ct) {
+  const double fm2 = f[0], fm1 = f[1], f0 = f[2], fp1 = f[3], fp2 = f[4], fp3 = f[5];
+  double b0, b1, b2, b3, e0, e1, e2, e3;
+  if (side > 0) {
+    b0 = 0.25 * (fm1 - fp1) * (fm1 - fp1) + (13.0 / 12.0) * (fm1 - 2.0 * f0 + fp1) * (fm1 - 2.0 * f0 + fp1);
+    b1 = 0.25 * (3.0 * f0 - 4.0 * fp1 + fp2) * (3.0 * f0 - 4.0 * fp1 + fp2) +
+         (13.0 / 12.0) * (f0 - 2.0 * fp1 + fp2) * (f0 - 2.0 * fp1 + fp2);
+    b2 = 0.25 * (fm2 - 4.0 * fm1 + 3.0 * f0) * (fm2 - 4.0 * fm1 + 3.0 * f0) +
+         (13.0 / 12.0) * (fm2 - 2.0 * fm1 + f0) * (fm2 - 2.0 * fm1 + f0);
+    double s1 = -11.0 * f0 + 18.0 * fp1 - 9.0 * fp2 + 2.0 * fp3;
+    double s2 = 2.0 * f0 - 5.0 * fp1 + 4.0 * fp2 - fp3;
+    double s3 = -f0 + 3.0 * fp1 - 3.0 * fp2 + fp3;
+    b3 = (1.0 / 36.0) * s1 * s1 + (13.0 / 12.0) * s2 * s2 + (781.0 / 720.0) * s3;
+    e0 = -(1.0 / 6.0) * fm1 + (5.0 / 6.0) * f0 + (2.0 / 6.0) * fp1;
+    e1 = (2.0 / 6.0) * f0 + (5.0 / 6.0) * fp1 - (1.0 / 6.0) * fp2;
+    e2 = (2.0 / 6.0) * fm2 - (7.0 / 6.0) * fm1 + (11.0 / 6.0) * f0;
+    e3 = (3.0 / 12.0) * f0 + (13.0 / 12.0) * fp1 - (5.0 / 12.0) * fp2 + (1.0 / 12.0) * fp3;
+  } else {
+    b0 = 0.25 * (f0 - fp2) * (f0 - fp2) + (13.0 / 12.0) * (f0 - 2.0 * fp1 + fp2) * (f0 - 2.0 * fp1 + fp2);
+    b1 = 0.25 * (fm1 - 4.0 * f0 + 3.0 * fp1) * (fm1 - 4.0 * f0 + 3.0 * fp1) +
+         (13.0 / 12.0) * (fm1 - 2.0 * f0 + fp1) * (fm1 - 2.0 * f0 + fp1);
+    b2 = 0.25 * (3.0 * fp1 - 4.0 * fp2 + fp3) * (3.0 * fp1 - 4.0 * fp2 + fp3) +
+         (13.0 / 12.0) * (fp1 - 2.0 * fp2 + fp3) * (fp1 - 2.0 * fp2 + fp3);
+    double s1 = -2.0 * fm2 + 9.0 * fm1 - 18.0 * f0 + 11.0 * fp1;
+    double s2 = -fm2 + 4.0 * fm1 - 5.0 * f0 + 2.0 * fp1;
+    double s3 = -fm2 + 3.0 * fm1 - 3.0 * f0 + fp1;
+    b3 = (1.0 / 36.0) * s1 * s1 + (13.0 / 12.0) * s2 * s2 + (781.0 / 720.0) * s3 * s3;
+    e0 = (2.0 / 6.0) * f0 + (5.0 / 6.0) * fp1 - (1.0 / 6.0) * fp2;
+    e1 = -(1.0 / 6.0) * fm1 + (5.0 / 6.0) * f0 + (2.0 / 6.0) * fp1;
+    e2 = (11.0 / 6.0) * fp1 - (7.0 / 6.0) * fp2 + (1.0 / 3.0) * fp3;
+    e3 = (1.0 / 12.0) * fm2 - (5.0 / 12.0) * fm1 + (13.0 / 12.0) * f0 + (3.0 / 12.0) * fp1;
+  }
+  double tau = fabs(b3 - (1.0 / 6.0) * (b0 + b2 - 4.0 * b1));
+  double t[4] = {1.0 + tau / (teno_eps + b0), 1.0 + tau / (teno_eps + b1), 1.0 + tau / (teno_eps + b2),
+                 1.0 + tau / (teno_eps + b3)};
+  double a[4], sum = 0.0;
+  for (int r = 0; r < 4; ++r) {
+    a[r] = t[r] * t[r] * t[r] * t[r] * t[r] * t[r];
+    sum += a[r];
+  }
+  const double dopt[4] = {231.0 / 500.0, 3.0 / 10.0, 27.0 / 500.0, 23.0 / 125.0};
+  const double e[4] = {e0, e1, e2, e3};
+  double inv = 1.0 / sum, wsum = 0.0, acc = 0.0;
+  for (int r = 0; r < 4; ++r) {
+    double w = (a[r] * inv < teno_ct) ? 0.0 : dopt[r];
+    wsum += w;
+    acc += w * e[r];
+  }
+  return acc * (1.0 / wsum);
+}
+
+/* Reconstruction of one characteristic wave at i+1/2: the positive split flux fp[0..5] and the
+ * negative one fm[0..5] (points i-2..i+3). */
+static double recon_wave(int scheme, const double* fp, const double* fm, double teno_eps, double teno_ct) {
+  if (scheme == OSB_SCHEME_TENO6) return recon6(1, fp, teno_eps, teno_ct) + recon6(-1, fm, teno_eps, teno_ct);
+  double mir[5] = {fm[5], fm[4], fm[3], fm[2], fm[1]};
+  return recon5(scheme, fp, teno_eps, teno_ct) + recon5(scheme, mir, teno_eps, teno_ct);
+}
+
 /* ---- characteristic flux at one interface --------------------------------------------- */
 
 /* Interface i+1/2 along direction d of a Cartesian block: idc = linear index of point i. */
@@ -331,8 +395,7 @@ static void char_flux_cart(const osb_block_desc* b, const geom_t* g, const cr_t*
   }
   double rec[NVMAX];
   for (int w = 0; w < nv; ++w) {
-    double mir[5] = {fm[w][5], fm[w][4], fm[w][3], fm[w][2], fm[w][1]};
-    rec[w] = recon5(b->scheme, &fp[w][0], b->eps, b->teno_ct) + recon5(b->scheme, mir, b->eps, b->teno_ct);
+    rec[w] = recon_wave(b->scheme, fp[w], fm[w], b->eps, b->teno_ct);
   }
   for (int v = 0; v < nv; ++v) {
     double acc = 0.0;
@@ -409,8 +472,7 @@ static void char_flux_curv(const osb_block_desc* b, const geom_t* g, const cr_t*
   }
   double rec[NVMAX];
   for (int w = 0; w < nv; ++w) {
-    double mir[5] = {fm[w][5], fm[w][4], fm[w][3], fm[w][2], fm[w][1]};
-    rec[w] = recon5(b->scheme, &fp[w][0], b->eps, b->teno_ct) + recon5(b->scheme, mir, b->eps, b->teno_ct);
+    rec[w] = recon_wave(b->scheme, fp[w], fm[w], b->eps, b->teno_ct);
   }
   for (int v = 0; v < nv; ++v) {
     double acc = 0.0;

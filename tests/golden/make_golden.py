@@ -32,6 +32,8 @@ CASES = {
     "sod_weno5js_400": ("sod_weno5js", lambda: problems.sod(400), {"OSB_NP0": 400}, 2e-4, [1, 3, 30, 3000], None),
     "tgv_teno5_12": ("tgv_teno5", lambda: problems.tgv(12, minf=1.25, scheme=abi.SCHEME_TENO5, averaging=abi.AVG_ROE),
                      {"OSB_NP0": 12, "OSB_NP1": 12, "OSB_NP2": 12}, 1e-3, [1, 3, 12], None),
+    "tgv_teno6_12": ("tgv_teno6", lambda: problems.tgv(12, minf=1.25, scheme=abi.SCHEME_TENO6, averaging=abi.AVG_ROE),
+                     {"OSB_NP0": 12, "OSB_NP1": 12, "OSB_NP2": 12}, 1e-3, [1, 3, 12], None),
     "tgv_weno5z_12_perturbed": ("tgv_weno5z",
                                 lambda: problems.tgv(12, minf=1.25, scheme=abi.SCHEME_WENO5_Z),
                                 {"OSB_NP0": 12, "OSB_NP1": 12, "OSB_NP2": 12}, 1e-3, [1, 3], (1e-3, 11)),

@@ -76,6 +76,71 @@ def test_sod_1000_steps_fp64(built_lib, oracle_lib):
 
 
 @pytest.mark.parametrize("nstages", [1, 3, 9])
+def test_tgv_teno6_fp64(built_lib, oracle_lib, nstages):
+    spec, q = problems.tgv(16, minf=1.25, scheme=abi.SCHEME_TENO6, averaging=abi.AVG_ROE)
+    errs, _, _ = _run_pair(spec, q, "ls3", 1e-3, nstages)
+    assert max(errs) < 1e-12, errs
+
+
+def _benchmark_reductions(spec, q_last_stage, rho_final):
+    """The reference benchmark's post-processing sums (apps/performance_benchmark/TENO6/
+    opensbli.cpp:435-457 with its kernel 048): velocities, viscosity and their 4th-order
+    derivatives come from the constituent-relation arrays of the last RK stage (the state at
+    the start of that stage, halos exchanged), density from the final state."""
+    g, minf = spec.gama, spec.Minf
+    rho_s = q_last_stage[0]
+    u = [q_last_stage[1 + i] / rho_s for i in range(3)]
+    p = (g - 1.0) * (q_last_stage[4] - 0.5 * rho_s * (u[0] ** 2 + u[1] ** 2 + u[2] ** 2))
+    T = minf * minf * g * p / rho_s
+    mu = 1.4042 * T * np.sqrt(T) / (0.40417 + T)
+    h = spec.halo
+    n = spec.size
+
+    def d1(f, axis, d):
+        inv = 1.0 / spec.delta[d]
+        return ((-(2.0 / 3.0)) * np.roll(f, 1, axis) - (1.0 / 12.0) * np.roll(f, -2, axis)
+                + (1.0 / 12.0) * np.roll(f, 2, axis) + (2.0 / 3.0) * np.roll(f, -1, axis)) * inv
+    # arrays are (z, y, x); the interior is away from the wrap of np.roll by the 5 halo layers
+    du = [[d1(u[i], 2 - d, d) for d in range(3)] for i in range(3)]
+    sl = spec.interior()
+    wx = du[2][1] - du[1][2]
+    wy = du[0][2] - du[2][0]
+    wz = du[1][0] - du[0][1]
+    div = du[0][0] + du[1][1] + du[2][2]
+    return {"KE": float(np.sum((0.5 * (u[0] ** 2 + u[1] ** 2 + u[2] ** 2) * rho_final)[sl])),
+            "dilatation": float(np.sum(((4.0 / 3.0) * div * div * mu)[sl])),
+            "enstrophy": float(np.sum(((wx * wx + wy * wy + wz * wz) * mu)[sl])),
+            "rhom": float(np.sum(rho_final[sl]))}
+
+
+def test_teno6_benchmark_known_answer(built_lib):
+    """The reference's TENO6 performance benchmark validation (apps/performance_benchmark/
+    README.MD, "va" mode): supersonic TGV, 128^3, M=1.25, Re=1600, TENO6 with Roe averaging +
+    central-4 viscous terms, RK-LS3, 500 steps of dt = 2 x 0.00084625, printed to 6 digits:
+    KE 2.65363e+05, dilatation dissipation 1.16991e+05, enstrophy dissipation 1.79666e+06,
+    rhom 2.09715e+06 -- evaluated as that benchmark does (velocities and viscosity of the last
+    RK stage, final density)."""
+    from opensbli_gb300.solver import Solver
+    spec, q = problems.tgv(128, minf=1.25, scheme=abi.SCHEME_TENO6, averaging=abi.AVG_ROE)
+    dt = 2 * 0.00084625
+    s = Solver([(spec, q)], precision="fp64", rk="ls3")
+    s.apply_bc()
+    s.step(dt, 499)
+    s.stage(0, dt)
+    s.stage(1, dt)
+    q_last = s.state(0)
+    s.stage(2, dt)
+    rho_final = s.state(0)[0]
+    s.close()
+    got = _benchmark_reductions(spec, q_last, rho_final)
+    want = {"KE": 2.65363e+05, "dilatation": 1.16991e+05, "enstrophy": 1.79666e+06, "rhom": 2.09715e+06}
+    for k in want:
+        # the printed value is the exact result rounded to 6 significant digits
+        half_ulp = 0.5 * 10.0 ** (np.floor(np.log10(abs(want[k]))) - 5)
+        assert abs(got[k] - want[k]) <= half_ulp * (1 + 1e-9), (k, got[k], want[k])
+
+
+@pytest.mark.parametrize("nstages", [1, 3, 9])
 def test_tgv_teno5_fp64(built_lib, oracle_lib, nstages):
     spec, q = problems.tgv(16, minf=1.25, scheme=abi.SCHEME_TENO5, averaging=abi.AVG_ROE)
     errs, _, _ = _run_pair(spec, q, "ls3", 1e-3, nstages)

@@ -14,6 +14,8 @@ CASES = {
     "sod_weno5js_400": (lambda: problems.sod(400), "ls3", None, 1e-12),
     "tgv_teno5_12": (lambda: problems.tgv(12, minf=1.25, scheme=abi.SCHEME_TENO5, averaging=abi.AVG_ROE), "ls3",
                      None, 1e-12),
+    "tgv_teno6_12": (lambda: problems.tgv(12, minf=1.25, scheme=abi.SCHEME_TENO6, averaging=abi.AVG_ROE), "ls3",
+                     None, 1e-12),
     "tgv_weno5z_12_perturbed": (lambda: problems.tgv(12, minf=1.25, scheme=abi.SCHEME_WENO5_Z), "ls3", (1e-3, 11),
                                 1e-11),
     "tgv_central_12": (lambda: problems.tgv(12, minf=0.1, scheme=abi.SCHEME_CENTRAL4), "ls3", None, 1e-12),
