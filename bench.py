@@ -49,6 +49,9 @@ def parse():
                          "Kelvin-Helmholtz instances in one persistent launch per stage; curv4: the "
                          "4-block 3D curvilinear TENO5 case")
     ap.add_argument("--ensemble", type=int, default=64)
+    ap.add_argument("--fuse", default="auto", choices=["auto", "0", "1"],
+                    help="RK update inside the central kernel (1), as its own kernel (0), or the faster of "
+                         "the two as timed by the autotuner (auto)")
     ap.add_argument("--no-tune", action="store_true")
     return ap.parse_args()
 
@@ -151,6 +154,18 @@ def make_problem(n):
     return spec, q, dt
 
 
+def kernel_bytes(fused):
+    """Algorithmic bytes per point of one launch of each FP32-path kernel of the 3D block: its
+    own minimal inputs and outputs (FP32 state 5 x 4 B, float-float residual 5 x 8 B, FP64
+    state and RK register 5 x 8 B each)."""
+    return {"flux_x": 20.0 + 40.0,                 # read FP32 state, write residual
+            "flux_y": 20.0 + 80.0,                 # read FP32 state, read + write residual
+            "flux_z": 20.0 + 80.0,
+            "central": (20.0 + 40.0 + 160.0 + 20.0) if fused else (20.0 + 80.0),
+            "rk_update": 40.0 + 160.0 + 20.0,      # residual, state + register read/write, FP32 out
+            "boundary": 0.0, "reduce": 40.0, "persistent_stage": 0.0}
+
+
 def time_steps(solver, dt, steps):
     import torch
     stream = solver.stream()
@@ -231,6 +246,13 @@ def our_arm(args):
     pts = spec.npoints
     s32 = Solver([(spec, q)], precision="fp32", rk="ls3", device=local, graphs=True)
     s32.apply_bc()
+    from opensbli_gb300 import autotune
+    if args.fuse == "auto":
+        sched, _ = autotune.tune(s32, dt, steps=2, warmup=1, cache=None)
+    else:
+        s32.set_schedule(mode=abi.SCHED_PER_BLOCK, fuse_update=int(args.fuse))
+        sched = s32.schedule()[1]
+    log("schedule %s" % json.dumps(sched))
     s32.step(dt, args.warmup)
     s32.sync()
     log("warmup done")
@@ -265,8 +287,8 @@ def our_arm(args):
     tot = sum(v[0] for v in rep.values()) or 1.0
     dom = max(rep, key=lambda k: rep[k][0])
     dom_ms = rep[dom][0] / max(rep[dom][1], 1)
-    alg_bytes = {"flux_x": 80.0, "flux_y": 120.0, "flux_z": 120.0, "central": 80.0, "rk_update": 200.0,
-                 "boundary": 0.0, "reduce": 40.0}[dom] * pts
+    fused = rep["rk_update"][1] == 0
+    alg_bytes = kernel_bytes(fused)[dom] * pts
     hbm, peak_kind = measured_peaks()
     achieved = alg_bytes / (dom_ms * 1e-3) / 1e9
     step_bytes_gbs = BYTES_PER_PT_STAGE * pts * 3 * args.steps / secs / 1e9
@@ -356,6 +378,7 @@ def our_arm(args):
             "error_vs_fp64": err,
             "clocks": clk,
             "gpu_launches": launches,
+            "schedule": sched,
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
                          "per_launch_ms": dom_ms, "share": rep[dom][0] / tot,
@@ -427,7 +450,7 @@ def secondary_arm(args):
                  "per_block_ms": next((t for t, c in trials if c["mode"] == abi.SCHED_PER_BLOCK), None),
                  "best_ms": min((t for t, _ in trials), default=None)}
         log("autotune: %s" % json.dumps(tuned))
-    mode = s32.schedule()[0]
+    mode, sched = s32.schedule()
     s32.step(dt, args.warmup)
     s32.sync()
     launches0 = s32.launches()
@@ -480,6 +503,7 @@ def secondary_arm(args):
             "autotune": tuned, "fp64": {"value": fp64, "unit": UNIT, "fp32_over_fp64": value / fp64},
             "error_vs_fp64": err, "clocks": clk, "gpu_launches": launches,
             "kernel_ms_per_step": {k: v[0] for k, v in rep.items() if v[1]},
+            "schedule": sched,
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm if achieved else None, "peak_kind": peak_kind,
                          "per_launch_ms": dom_ms}}

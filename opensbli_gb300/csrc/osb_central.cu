@@ -11,7 +11,24 @@ int launch_central_k(osb_ctx* c, Block& bl, int first, const RkFuse& rf) {
   size_t smem = (size_t)Fd::N * CPTS * sizeof(T);
   auto kern = k_central3d<T, CONV, VISC, FUSE>;
   OSB_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  CentralParams cp{bl.d.gama, bl.d.Minf, bl.d.Re, bl.d.Pr, bl.d.mu_const};
+  CentralParams cp{};
+  const osb_block_desc& d = bl.d;
+  cp.gama = d.gama;
+  cp.M2 = d.Minf * d.Minf;
+  cp.mu_c = d.mu_const;
+  cp.invRe = 1.0 / d.Re;
+  cp.kheat = 1.0 / (d.Pr * d.Re * d.Minf * d.Minf * (d.gama - 1.0));
+  cp.gama_f = (float)cp.gama;
+  cp.M2_f = (float)cp.M2;
+  cp.mu_c_f = (float)cp.mu_c;
+  cp.invRe_f = (float)cp.invRe;
+  cp.kheat_f = (float)cp.kheat;
+  for (int i = 0; i < 3; ++i) {
+    cp.invd[i] = bl.k.invd[i];
+    cp.inv2d[i] = bl.k.inv2d[i];
+    cp.invd_f[i] = (float)cp.invd[i];
+    cp.inv2d_f[i] = (float)cp.inv2d[i];
+  }
   const BlockK& k = bl.k;
   dim3 grid((k.n[0] + CX - 1) / CX, (k.n[1] + CY - 1) / CY, (k.n[2] + CZ - 1) / CZ);
   timing_begin(c, FAM_CENTRAL);

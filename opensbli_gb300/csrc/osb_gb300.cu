@@ -517,6 +517,7 @@ int stage(osb_ctx* c, int s, double dt) {
     for (auto& bl : c->blocks) {
       RkFuse rf{};
       rf.kind = kind;
+      rf.a_zero = (kind == 0 && c->A[s] == 0.0) ? 1 : 0;
       rf.A = c->A[s];
       rf.B = c->B[s];
       rf.dt = dt;

@@ -244,7 +244,8 @@ __device__ __forceinline__ void rp_store(const BlockK& b, int v, int id, float c
 // rk_sbli.py:138-145) itself and writes the next stage's FP32 state into the other buffer of a
 // ping-pong pair: the kernel reads the current buffer, so no thread sees a partial update.
 struct RkFuse {
-  int kind;  // 0 low-storage, 1 SBLI
+  int kind;    // 0 low-storage, 1 SBLI
+  int a_zero;  // low-storage stage with A = 0 (the first): the register is not read
   double A, B, dt;
   float* qout[5];
   unsigned long long* bad;
@@ -253,7 +254,7 @@ struct RkFuse {
 __device__ __forceinline__ unsigned rk_point_qo(const BlockK& b, const RkFuse& rf, int v, int id, double r0, double q,
                                                 double o) {
   if (rf.kind == 0) {
-    o = rf.A * o + rf.dt * r0;
+    o = rf.a_zero ? rf.dt * r0 : rf.A * o + rf.dt * r0;
     q = rf.B * o + q;
   } else {
     q = (rf.A * rf.dt) * r0 + o;
@@ -265,7 +266,7 @@ __device__ __forceinline__ unsigned rk_point_qo(const BlockK& b, const RkFuse& r
   return ((((unsigned)__double2hiint(q) >> 20) & 0x7ffu) == 0x7ffu) ? 1u : 0u;
 }
 __device__ __forceinline__ unsigned rk_point(const BlockK& b, const RkFuse& rf, int v, int id, double r0) {
-  return rk_point_qo(b, rf, v, id, r0, b.q[v][id], b.rk[v][id]);
+  return rk_point_qo(b, rf, v, id, r0, b.q[v][id], rf.a_zero ? 0.0 : b.rk[v][id]);
 }
 
 // Final residual of a point from its prefetched partial value plus the last contribution.
@@ -487,9 +488,20 @@ __global__ void __launch_bounds__(32 * XWARPS) k_flux_x(BlockK b, SchemeParams s
 //         for the low-Mach TGV ("Convective terms" kernel).
 //   VISC: viscous stress and heat flux (StoreSome "Viscous terms" kernel), mu from the
 //         modified Sutherland law (VISC == 1) or constant (VISC == 2).
+// Constants of the central kernel, derived once on the host in FP64 and handed over in both
+// precisions (a conversion or division in FP64 inside an FP32 kernel runs on the FP64 pipe).
 struct CentralParams {
-  double gama, Minf, Re, Pr, mu_const;
+  double gama, M2, mu_c, invRe, kheat;  // M2 = Minf^2, kheat = 1 / (Pr Re Minf^2 (gama - 1))
+  float gama_f, M2_f, mu_c_f, invRe_f, kheat_f;
+  double invd[3], inv2d[3];
+  float invd_f[3], inv2d_f[3];
 };
+template <typename T>
+__device__ __forceinline__ T cpar(double d, float f);
+template <>
+__device__ __forceinline__ double cpar<double>(double d, float) { return d; }
+template <>
+__device__ __forceinline__ float cpar<float>(double, float f) { return f; }
 
 constexpr int CX = 32, CY = 4, CZ = 4, CH = 2;
 constexpr int CSX = CX + 2 * CH, CSY = CY + 2 * CH, CSZ = CZ + 2 * CH;
@@ -511,11 +523,11 @@ __global__ void __launch_bounds__(CX * CY) k_central3d(BlockK b, CentralParams c
   T* sm = reinterpret_cast<T*>(osb_smem);
   const int tx = threadIdx.x % CX, ty = threadIdx.x / CX;
   const int x0 = blockIdx.x * CX, y0 = blockIdx.y * CY, z0 = blockIdx.z * CZ;
-  const T gm = (T)cp.gama;
-  const T M2 = (T)(cp.Minf * cp.Minf);
-  const T mu_c = (T)cp.mu_const;
-  const T invRe = (T)(1.0 / cp.Re);
-  const T kheat = (T)(1.0 / (cp.Pr * cp.Re * cp.Minf * cp.Minf * (cp.gama - 1.0)));
+  const T gm = cpar<T>(cp.gama, cp.gama_f);
+  const T M2 = cpar<T>(cp.M2, cp.M2_f);
+  const T mu_c = cpar<T>(cp.mu_c, cp.mu_c_f);
+  const T invRe = cpar<T>(cp.invRe, cp.invRe_f);
+  const T kheat = cpar<T>(cp.kheat, cp.kheat_f);
   // ---- load the halo'd tile and form primitives
   // loads of CU points per thread are issued together before any of them is used
   constexpr int CU = 6;
@@ -563,8 +575,10 @@ __global__ void __launch_bounds__(CX * CY) k_central3d(BlockK b, CentralParams c
   __syncthreads();
   const int gx = x0 + tx, gy = y0 + ty;
   if (gx >= b.n[0] || gy >= b.n[1]) return;
-  const T id0 = (T)b.invd[0], id1 = (T)b.invd[1], id2 = (T)b.invd[2];
-  const T jd0 = (T)b.inv2d[0], jd1 = (T)b.inv2d[1], jd2 = (T)b.inv2d[2];
+  const T id0 = cpar<T>(cp.invd[0], cp.invd_f[0]), id1 = cpar<T>(cp.invd[1], cp.invd_f[1]),
+          id2 = cpar<T>(cp.invd[2], cp.invd_f[2]);
+  const T jd0 = cpar<T>(cp.inv2d[0], cp.inv2d_f[0]), jd1 = cpar<T>(cp.inv2d[1], cp.inv2d_f[1]),
+          jd2 = cpar<T>(cp.inv2d[2], cp.inv2d_f[2]);
   const int sx = 1, sy = CSX, sz = CSX * CSY;
   for (int tz = 0; tz < CZ; ++tz) {
     const int gz = z0 + tz;
@@ -598,7 +612,7 @@ __global__ void __launch_bounds__(CX * CY) k_central3d(BlockK b, CentralParams c
 #pragma unroll
       for (int v = 0; v < 5; ++v) {
         fq[v] = b.q[v][gid];
-        fo[v] = b.rk[v][gid];
+        fo[v] = rf.a_zero ? 0.0 : b.rk[v][gid];
       }
     }
     T racc[5] = {L_(0.0), L_(0.0), L_(0.0), L_(0.0), L_(0.0)};

@@ -136,6 +136,47 @@ def build_ref(case, force=False, fast=False):
     return exe
 
 
+SHIPPED_TENO6 = os.path.join("apps", "performance_benchmark", "TENO6")
+
+
+def build_shipped_teno6(reference=None, force=False):
+    """Compile the reference's shipped TENO6 benchmark solver (bit-exact generated code, from
+    where it lies in the reference checkout) against ops_compat.h into oracle/_ref/bench_teno6.
+    -O1: at -O2 the benchmark's own out-of-bounds read of its run-mode string (see
+    shipped_compat.h) is miscompiled; the floating-point semantics are the same (no FMA
+    contraction, no fast math)."""
+    reference = reference or os.environ.get("OSB_REFERENCE", "/root/reference")
+    src_dir = os.path.join(reference, SHIPPED_TENO6)
+    out_dir = os.path.join(REF, "bench_teno6")
+    exe = os.path.join(out_dir, "ref_case")
+    if not force and os.path.exists(exe):
+        return exe
+    if not os.path.exists(os.path.join(src_dir, "opensbli.cpp")):
+        raise FileNotFoundError("shipped benchmark sources not found under %s" % src_dir)
+    os.makedirs(out_dir, exist_ok=True)
+    cmd = ["g++", "-std=c++17", "-O1", "-ffp-contract=off", "-fopenmp", "-include",
+           os.path.join(HERE, "shipped_compat.h"), "-I", HERE, "-I", src_dir, os.path.join(src_dir, "opensbli.cpp"),
+           "-o", exe]
+    subprocess.check_call(cmd, stderr=subprocess.DEVNULL)
+    return exe
+
+
+def run_shipped_teno6(n, iters, stop_after_rk=None, timeout=3600):
+    """Run the shipped TENO6 benchmark in its strong-scaling mode (n^3 points, dt =
+    0.00084625 * 256 / n) and return its dumped arrays."""
+    exe = build_shipped_teno6()
+    with tempfile.TemporaryDirectory() as td:
+        with open(os.path.join(td, "input"), "w") as f:
+            f.write("ss %d %d 1 0\n" % (n, iters))  # the run-mode string is read into 2 bytes
+        e = dict(os.environ)
+        e["OSB_QUIET"] = "1"
+        e["OSB_DUMP_DIR"] = td
+        if stop_after_rk is not None:
+            e["OSB_STOP_AFTER_RK"] = str(stop_after_rk)
+        subprocess.run([exe], env=e, cwd=td, check=True, timeout=timeout, stdout=subprocess.DEVNULL)
+        return {fn[:-4]: read_dump(os.path.join(td, fn)) for fn in os.listdir(td) if fn.endswith(".bin")}
+
+
 def read_dump(path):
     hdr = np.fromfile(path, dtype=np.int32, count=8)
     nd = int(hdr[0])

@@ -72,7 +72,24 @@ def make(name):
     print("wrote", name)
 
 
+def make_shipped_teno6(n=12, counts=(1, 3, 15)):
+    """Golden states from the reference's shipped TENO6 benchmark solver itself (bit-exact
+    generated code, apps/performance_benchmark/TENO6), strong-scaling mode at n^3."""
+    spec, q = problems.tgv(n, minf=1.25, scheme=abi.SCHEME_TENO6, averaging=abi.AVG_ROE)
+    names = harness.state_names(3)
+    sl = spec.interior()
+    out = {"dt": 0.00084625 * 256 / n, "counts": np.array(counts)}
+    for c in counts:
+        r = harness.run_shipped_teno6(n, c // 3 + 1, stop_after_rk=c)
+        out["after_%d" % c] = np.stack([r[nm][sl] for nm in names])
+    np.savez_compressed(os.path.join(HERE, "shipped_teno6_%d.npz" % n), **out)
+    print("wrote shipped_teno6_%d" % n)
+
+
 def main():
+    if sys.argv[1:] == ["shipped_teno6"]:
+        make_shipped_teno6()
+        return
     missing = sorted({c for c in harness_cases() if not harness.ref_available(c)})
     if missing:
         subprocess.check_call([sys.executable, os.path.join(ROOT, "oracle", "ref_generate.py")] + missing)

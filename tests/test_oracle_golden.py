@@ -110,3 +110,20 @@ def test_curvilinear_known_answer(oracle_lib):
     ob.step(abi.RK_LOW_STORAGE, problems.RK3_LS_A, problems.RK3_LS_B, 5e-4, 10)
     rho = ob.q[0][0][69, 69]
     assert abs(rho - 0.9984292346559068) < 1e-9 * 0.9984292346559068, rho
+
+
+def test_oracle_matches_shipped_teno6_benchmark(oracle_lib):
+    """The oracle's TENO6 path against the reference's shipped benchmark solver itself
+    (apps/performance_benchmark/TENO6, bit-exact generated code, run in its strong-scaling mode
+    at 12^3 by tests/golden/make_golden.py shipped_teno6): 1 stage, 1 step, 5 steps."""
+    g = np.load(os.path.join(GOLD, "shipped_teno6_12.npz"))
+    spec, q = problems.tgv(12, minf=1.25, scheme=abi.SCHEME_TENO6, averaging=abi.AVG_ROE)
+    dt = float(g["dt"])
+    sl = spec.interior()
+    for n in g["counts"]:
+        ob = harness.OracleBlocks([(spec, q)])
+        ob.apply_bc()
+        advance(ob, spec, "ls3", dt, int(n))
+        ref = g["after_%d" % int(n)]
+        errs = [harness.rel_err(ob.q[0][v][sl], ref[v]) for v in range(spec.nvars)]
+        assert max(errs) < 1e-12, (int(n), errs)
