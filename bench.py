@@ -57,10 +57,8 @@ def parse():
 
 
 def dist_env():
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return rank, world, local
+    from opensbli_gb300.replicas import dist_env as env
+    return env()
 
 
 class ClockSampler:
@@ -272,10 +270,8 @@ def our_arm(args):
     launches = s32.launches() - launches0
     log("timed done")
     if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([secs], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        secs = float(t.item())
+        from opensbli_gb300.replicas import max_over_ranks
+        secs = max_over_ranks(secs)
     value = world * pts * 3 * args.steps / secs / 1e6
 
     # per-kernel times (CUDA events per launch on the context stream) over one more step
