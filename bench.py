@@ -50,8 +50,8 @@ def parse():
                          "4-block 3D curvilinear TENO5 case")
     ap.add_argument("--ensemble", type=int, default=64)
     ap.add_argument("--fuse", default="auto", choices=["auto", "0", "1"],
-                    help="RK update inside the central kernel (1), as its own kernel (0), or the faster of "
-                         "the two as timed by the autotuner (auto)")
+                    help="RK update inside the central kernel (1), as its own kernel (0), or the fastest "
+                         "schedule (fusion and x-sweep tiling) as timed by the autotuner (auto)")
     ap.add_argument("--no-tune", action="store_true")
     return ap.parse_args()
 
@@ -115,6 +115,21 @@ class ClockSampler:
                     reasons.add(n)
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def measured_traffic(kernel, fused):
+    """DRAM bytes (read + write) per point of one launch of `kernel`, from the ncu capture
+    summarised in profiles/dram_traffic_tgv_fp32.txt (captured at 160^3, above L2; traffic
+    scales with the points of the block), or None."""
+    path = os.path.join(ROOT, "profiles", "dram_traffic_tgv_fp32.txt")
+    if not os.path.exists(path):
+        return None
+    key = kernel + ("_fused" if kernel == "central" and fused else "")
+    for line in open(path):
+        parts = line.split()
+        if len(parts) >= 2 and not line.startswith("#") and parts[0] == key:
+            return float(parts[1])
+    return None
 
 
 def measured_peaks():
@@ -249,7 +264,7 @@ def our_arm(args):
         sched, _ = autotune.tune(s32, dt, steps=2, warmup=1, cache=None)
     else:
         s32.set_schedule(mode=abi.SCHED_PER_BLOCK, fuse_update=int(args.fuse))
-        sched = s32.schedule()[1]
+        sched = dict(s32.schedule()[1], variant=0)
     log("schedule %s" % json.dumps(sched))
     s32.step(dt, args.warmup)
     s32.sync()
@@ -288,10 +303,9 @@ def our_arm(args):
     hbm, peak_kind = measured_peaks()
     achieved = alg_bytes / (dom_ms * 1e-3) / 1e9
     step_bytes_gbs = BYTES_PER_PT_STAGE * pts * 3 * args.steps / secs / 1e9
-    traffic = None
-    tf = os.path.join(ROOT, "profiles", "traffic_%s_%d.json" % (dom, n))
-    if os.path.exists(tf):
-        traffic = json.load(open(tf)).get("bytes_per_launch")
+    traffic = measured_traffic(dom, fused)
+    if traffic is not None:
+        traffic *= pts
 
     fp32_peak, fp64_peak = probe_fp(local)
     log("probe done")
@@ -476,7 +490,7 @@ def secondary_arm(args):
     nerr = 3
     a = Solver(blocks, precision="fp32", rk=rk, device=local)
     if tuned:
-        a.set_schedule(**tuned["schedule"])
+        autotune.apply(a, tuned["schedule"])
     a.apply_bc()
     a.step(dt, nerr)
     b = Solver(blocks, precision="fp64", rk=rk, device=local)

@@ -160,8 +160,8 @@ int osb_sync(osb_ctx* ctx, int timeout_ms);
 /* Enables (1) or disables (0) CUDA-graph capture of osb_step. */
 int osb_set_graphs(osb_ctx* ctx, int enable);
 
-/* Selects the kernel tiling variant for the reconstruction kernels (autotuner hook);
- * variant < 0 restores the default. */
+/* Selects the tiling variant of the x reconstruction sweep (autotuner hook): 0 or < 0 the
+ * default segment of 14 interfaces per warp row, 1 = 12, 2 = 10, 3 = 18. */
 int osb_set_variant(osb_ctx* ctx, int variant);
 
 /* Stage schedule.  OSB_SCHED_PER_BLOCK runs every block's sweeps, RK update and boundary

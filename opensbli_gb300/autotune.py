@@ -1,7 +1,8 @@
 """Autotuner of the stage schedule (osb_set_schedule).
 
 For a solver holding its blocks, times every candidate schedule -- per-block launches with and
-without the RK update fused into the last residual kernel, and the persistent fused stage over
+without the RK update fused into the last residual kernel and with each x-sweep segment length
+(osb_set_variant), and the persistent fused stage over
 tile heights, resident CTAs per SM, static or dynamic tile claiming and tile orders -- on the
 caller's own workload (CUDA-graph replays timed with CUDA events on the
 solver's stream), restores the state after every trial, applies the fastest schedule and caches
@@ -26,16 +27,23 @@ DEFAULT_CACHE = os.environ.get("OSB_AUTOTUNE_CACHE",
 
 def candidates(persistent):
     """Candidate schedules: the per-block path, plus the persistent stage's knob grid."""
-    out = [{"mode": abi.SCHED_PER_BLOCK, "tile_y": 16, "ctas_per_sm": 2, "dynamic": 1, "order": 0, "fuse_update": f}
-           for f in (1, 0)]
+    out = [{"mode": abi.SCHED_PER_BLOCK, "tile_y": 16, "ctas_per_sm": 2, "dynamic": 1, "order": 0, "fuse_update": f,
+            "variant": v} for f in (1, 0) for v in (0, 1, 2, 3)]
     if persistent:
         for ty in (8, 16, 32):
             for cps in (1, 2, 3, 4):
                 for dyn in (1, 0):
                     for order in (0, 1, 2):
                         out.append({"mode": abi.SCHED_PERSISTENT, "tile_y": ty, "ctas_per_sm": cps,
-                                    "dynamic": dyn, "order": order, "fuse_update": 1})
+                                    "dynamic": dyn, "order": order, "fuse_update": 1, "variant": 0})
     return out
+
+
+def apply(solver, cand):
+    """Apply one candidate: the osb_schedule fields plus the x-sweep variant."""
+    sched = {k: v for k, v in cand.items() if k != "variant"}
+    solver.set_schedule(**sched)
+    solver.set_variant(cand.get("variant", 0))
 
 
 def signature(solver):
@@ -88,7 +96,7 @@ def tune(solver, dt, steps=3, warmup=1, cache=DEFAULT_CACHE, force=False, cands=
     table = _load(cache) if cache else {}
     if not force and key in table:
         best = table[key]["schedule"]
-        solver.set_schedule(**best)
+        apply(solver, best)
         return best, []
     torch = solver.torch
     solver.sync()
@@ -103,7 +111,7 @@ def tune(solver, dt, steps=3, warmup=1, cache=DEFAULT_CACHE, force=False, cands=
     trials = []
     for cand in (cands or candidates(persistent_ok)):
         try:
-            solver.set_schedule(**cand)
+            apply(solver, cand)
         except abi.OSBError:
             continue
         for q, s in zip(solver.q, saved_q):
@@ -118,7 +126,7 @@ def tune(solver, dt, steps=3, warmup=1, cache=DEFAULT_CACHE, force=False, cands=
         r.copy_(s)
     torch.cuda.synchronize(solver.device)
     ms, best = min(trials, key=lambda t: t[0])
-    solver.set_schedule(**best)
+    apply(solver, best)
     solver.apply_bc()
     if cache:
         table = _load(cache)

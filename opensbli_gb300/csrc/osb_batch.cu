@@ -10,7 +10,8 @@
 //   2. computes the characteristic LLF fluxes of the 33 x-interfaces of every row and the
 //      ty + 1 y-interfaces of every column into shared memory (char_flux, each flux once),
 //   3. forms -(dF_x/dx + dF_y/dy) per point as a float-float pair (exact flux differences),
-//      applies the FP64 low-storage / SBLI RK update to the caller's state and register, and
+//      applies the FP64 low-storage / SBLI RK update to the caller's state and register (the
+//      first low-storage stage, A = 0, does not read the register), and
 //      writes the FP32 state of the next stage into the other buffer of a ping-pong pair.
 // The residual never goes to HBM.  Tiles read one FP32 buffer and write the other, so a stage
 // has no intra-launch dependencies and needs no grid-wide barrier.
@@ -47,7 +48,7 @@ template <int SCH, int AVG>
 __global__ void __launch_bounds__(BTHREADS) k_batch2d(const BatchBlock* __restrict__ blocks,
                                                       const int4* __restrict__ work, int nwork, int* counter,
                                                       int ty, SchemeParams spd, int kind, double A, double B,
-                                                      double dt, int save, unsigned long long* bad) {
+                                                      float dt_h, float dt_l, int save, unsigned long long* bad) {
   constexpr int NV = 4;
   const SP<float> sp(spd);
   extern __shared__ __align__(16) unsigned char osb_smem[];
@@ -156,15 +157,20 @@ __global__ void __launch_bounds__(BTHREADS) k_batch2d(const BatchBlock* __restri
         float h = __fadd_rn(p1, e1);
         float l = __fsub_rn(e1, __fsub_rn(h, p1));
         ff_add(h, l, p2, e2);
-        const double r0 = f2d_exact(h) + f2d_exact(l);
+        // dt * residual as a float-float product, one conversion (as rk_point_ff)
+        const float pp = __fmul_rn(h, dt_h);
+        float ee = __fmaf_rn(h, dt_h, -pp);
+        ee = __fmaf_rn(h, dt_l, __fmaf_rn(l, dt_h, ee));
+        const double x = f2d_exact(pp) + f2d_exact(ee);
         double q = bk.q[v][id];
-        double o = save ? q : bk.rk[v][id];
+        double o;
         if (kind == 0) {
-          o = A * o + dt * r0;
-          q = B * o + q;
+          o = A == 0.0 ? x : __fma_rn(A, bk.rk[v][id], x);
+          q = __fma_rn(B, o, q);
         } else {
-          q = (A * dt) * r0 + o;
-          o = (B * dt) * r0 + o;
+          o = save ? q : bk.rk[v][id];
+          q = __fma_rn(A, x, o);
+          o = __fma_rn(B, x, o);
         }
         bk.rk[v][id] = o;
         bk.q[v][id] = q;
@@ -188,6 +194,7 @@ namespace {
 template <int SCH, int AVG>
 int launch_batch_t(osb_ctx* c, const BatchBlock* tab, const SchemeParams& sp, int kind, double A, double B, double dt,
                    int save) {
+  const float dt_h = (float)dt, dt_l = (float)(dt - (double)dt_h);
   auto kern = k_batch2d<SCH, AVG>;
   const int ty = c->sched.tile_y;
   const size_t smem = batch_smem(ty);
@@ -199,8 +206,8 @@ int launch_batch_t(osb_ctx* c, const BatchBlock* tab, const SchemeParams& sp, in
   }
   const int grid = std::max(1, std::min(c->batch.nwork, c->sched.ctas_per_sm * c->sm_count));
   timing_begin(c, FAM_PERSISTENT);
-  kern<<<grid, BTHREADS, smem, c->stream>>>(tab, c->batch.work, c->batch.nwork, counter, ty, sp, kind, A, B, dt,
-                                            save, c->bad);
+  kern<<<grid, BTHREADS, smem, c->stream>>>(tab, c->batch.work, c->batch.nwork, counter, ty, sp, kind, A, B, dt_h,
+                                            dt_l, save, c->bad);
   timing_end(c);
   c->launches++;
   OSB_CK(cudaGetLastError());

@@ -40,13 +40,15 @@ int launch_flux(osb_ctx* c, Block& bl, const SchemeParams& sp, const RkFuse* rf)
   // x sweep (writes R)
   {
     constexpr int NF = SweepFields<ND, CURV>::N;
-    size_t smem = (size_t)XWARPS * NF * 32 * XPITCH * sizeof(T);
+    // osb_set_variant: 0 = default segment, 1..3 = 12, 10, 18 interfaces per segment
+    const int xseg = c->variant == 1 ? 12 : c->variant == 2 ? 10 : c->variant == 3 ? 18 : XSEG;
+    size_t smem = (size_t)XWARPS * NF * 32 * xpitch_of(xseg) * sizeof(T);
     auto kern = k_flux_x<T, ND, SCH, AVG, CURV>;
     OSB_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int nrows = k.n[1] * k.n[2];
-    dim3 grid((k.n[0] + XSEG - 1) / XSEG, (nrows + 32 * XWARPS - 1) / (32 * XWARPS));
+    dim3 grid((k.n[0] + xseg - 1) / xseg, (nrows + 32 * XWARPS - 1) / (32 * XWARPS));
     timing_begin(c, FAM_FLUX_X);
-    kern<<<grid, 32 * XWARPS, smem, st>>>(k, sp, 1);
+    kern<<<grid, 32 * XWARPS, smem, st>>>(k, sp, 1, xseg);
     timing_end(c);
     c->launches++;
   }

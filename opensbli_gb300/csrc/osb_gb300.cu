@@ -82,7 +82,7 @@ __global__ void k_rk32(BlockK b, int nv, RkFuse rf) {
     int j = r % b.n[1];
     int k = r / b.n[1];
     int id = lin(b, i, j, k);
-    for (int v = 0; v < nv; ++v) nb += rk_point(b, rf, v, id, f2d_exact(b.Rh[v][id]) + f2d_exact(b.Rl[v][id]));
+    for (int v = 0; v < nv; ++v) nb += rk_point(b, rf, v, id, b.Rh[v][id], b.Rl[v][id]);
   }
   if (nb) atomicAdd(rf.bad, (unsigned long long)nb);
 }
@@ -101,29 +101,36 @@ __global__ void k_q2qf(BlockK b, int nv) {
     b.qf[v][t] = d2f_rn(b.q[v][t]);
 }
 
+// Halo arrays a boundary kernel writes: the FP64 state, the FP32 state, or both.
+enum { BC_Q = 1, BC_QF = 2, BC_BOTH = 3 };
+
 // Periodic exchange of both faces of direction d (ExchangeSelf, periodic.py:53-71):
 // side 0 copies [0, depth) to [N, N+depth), side 1 copies [N-depth, N) to [-depth, 0); the
 // transverse ranges include -depth..N+depth of the other used directions (corners).
-__global__ void k_periodic(BlockK b, int nv, int d, int depth0, int depth1) {
+// blockIdx.y = 2 * variable + side; 32-bit index arithmetic.
+__global__ void k_periodic(BlockK b, int nv, int d, int depth0, int depth1, int fields) {
+  const int dmax = max(depth0, depth1);
   int ext[3], lo[3];
   for (int e = 0; e < 3; ++e) {
-    if (e < b.ndim && e != d) { ext[e] = b.n[e] + 2 * max(depth0, depth1); lo[e] = -max(depth0, depth1); }
-    else { ext[e] = 1; lo[e] = 0; }
+    if (e < b.ndim && e != d) {
+      ext[e] = b.n[e] + 2 * dmax;
+      lo[e] = -dmax;
+    } else {
+      ext[e] = 1;
+      lo[e] = 0;
+    }
   }
-  const int dmax = max(depth0, depth1);
   ext[d] = dmax;
-  const long per_side = (long)ext[0] * ext[1] * ext[2];
-  const long total = 2 * per_side * nv;
+  const int side = blockIdx.y & 1, v = blockIdx.y >> 1;
+  const int depth = side == 0 ? depth0 : depth1;
   const int N = b.n[d];
-  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
-    long r = t;
+  const int per = ext[0] * ext[1] * ext[2];
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < per; t += gridDim.x * blockDim.x) {
     int c[3];
-    c[0] = (int)(r % ext[0]); r /= ext[0];
-    c[1] = (int)(r % ext[1]); r /= ext[1];
-    c[2] = (int)(r % ext[2]); r /= ext[2];
-    int side = (int)(r % 2);
-    int v = (int)(r / 2);
-    int depth = side == 0 ? depth0 : depth1;
+    c[0] = t % ext[0];
+    const int r = t / ext[0];
+    c[1] = r % ext[1];
+    c[2] = r / ext[1];
     if (c[d] >= depth) continue;
     int src[3], dst[3];
     bool skip = false;
@@ -133,18 +140,23 @@ __global__ void k_periodic(BlockK b, int nv, int d, int depth0, int depth1) {
       if (e != d && e < b.ndim && (src[e] < -depth || src[e] >= b.n[e] + depth)) skip = true;
     }
     if (skip) continue;
-    if (side == 0) { src[d] = c[d]; dst[d] = N + c[d]; }
-    else { src[d] = N - depth + c[d]; dst[d] = -depth + c[d]; }
-    int di = lin(b, dst[0], dst[1], dst[2]), si = lin(b, src[0], src[1], src[2]);
-    b.q[v][di] = b.q[v][si];
-    if (b.qf[0]) b.qf[v][di] = b.qf[v][si];
+    if (side == 0) {
+      src[d] = c[d];
+      dst[d] = N + c[d];
+    } else {
+      src[d] = N - depth + c[d];
+      dst[d] = -depth + c[d];
+    }
+    const int di = lin(b, dst[0], dst[1], dst[2]), si = lin(b, src[0], src[1], src[2]);
+    if (fields & BC_Q) b.q[v][di] = b.q[v][si];
+    if ((fields & BC_QF) && b.qf[0]) b.qf[v][di] = b.qf[v][si];
   }
 }
 
 // Zero-gradient outlet (zero_gradient_outlet.py:11-23 as generated): on side 0,
 // q(0) = q(1) then q(-m) = q(m) for m = 1..depth; mirrored on side 1.  Over the interior
 // extent of the other directions.
-__global__ void k_zero_grad(BlockK b, int nv, int d, int side, int depth) {
+__global__ void k_zero_grad(BlockK b, int nv, int d, int side, int depth, int fields) {
   int ext[3];
   for (int e = 0; e < 3; ++e) ext[e] = (e == d) ? 1 : b.n[e];
   const long total = (long)ext[0] * ext[1] * ext[2];
@@ -158,10 +170,12 @@ __global__ void k_zero_grad(BlockK b, int nv, int d, int side, int depth) {
     int id = lin(b, c[0], c[1], c[2]);
     int s = b.st[d] * (side == 0 ? 1 : -1);
     for (int v = 0; v < nv; ++v) {
-      double* q = b.q[v];
-      q[id] = q[id + s];
-      for (int m = 1; m <= depth; ++m) q[id - m * s] = q[id + m * s];
-      if (b.qf[0]) {
+      if (fields & BC_Q) {
+        double* q = b.q[v];
+        q[id] = q[id + s];
+        for (int m = 1; m <= depth; ++m) q[id - m * s] = q[id + m * s];
+      }
+      if ((fields & BC_QF) && b.qf[0]) {
         float* f = b.qf[v];
         f[id] = f[id + s];
         for (int m = 1; m <= depth; ++m) f[id - m * s] = f[id + m * s];
@@ -174,7 +188,8 @@ __global__ void k_zero_grad(BlockK b, int nv, int d, int side, int depth) {
 // layers of face (d, side) of dst receive the `depth` layers of src next to its face
 // (d, sside).  The transverse range is the interior of the face (full = 0) or that plus
 // `depth` halo points on each side (full = 1).
-__global__ void k_interface(BlockK dst, BlockK src, int nv, int d, int side, int sside, int depth, int full) {
+__global__ void k_interface(BlockK dst, BlockK src, int nv, int d, int side, int sside, int depth, int full,
+                            int fields) {
   int ext[3], lo[3];
   for (int e = 0; e < 3; ++e) {
     if (e < dst.ndim && e != d) {
@@ -199,8 +214,8 @@ __global__ void k_interface(BlockK dst, BlockK src, int nv, int d, int side, int
     di[d] = side == 0 ? -depth + c[d] : dst.n[d] + c[d];
     si[d] = sside == 1 ? src.n[d] - depth + c[d] : c[d];
     const int a = lin(dst, di[0], di[1], di[2]), bsrc = lin(src, si[0], si[1], si[2]);
-    dst.q[v][a] = src.q[v][bsrc];
-    if (dst.qf[0]) dst.qf[v][a] = src.qf[v][bsrc];
+    if (fields & BC_Q) dst.q[v][a] = src.q[v][bsrc];
+    if ((fields & BC_QF) && dst.qf[0]) dst.qf[v][a] = src.qf[v][bsrc];
   }
 }
 
@@ -418,7 +433,7 @@ int grid_for(osb_ctx* c, long n, int threads) {
 
 // Interface faces of every block: the interior of each face (full = 0) or the face with its
 // transverse halos (full = 1).
-int apply_interfaces(osb_ctx* c, int full) {
+int apply_interfaces(osb_ctx* c, int full, int fields) {
   for (size_t ib = 0; ib < c->blocks.size(); ++ib) {
     Block& bl = c->blocks[ib];
     const int nv = bl.d.ndim + 2;
@@ -443,7 +458,8 @@ int apply_interfaces(osb_ctx* c, int full) {
         for (int e = 0; e < bl.d.ndim; ++e)
           if (e != d) total *= bl.k.n[e] + (full ? 2 * depth : 0);
         timing_begin(c, FAM_BC);
-        k_interface<<<grid_for(c, total, 256), 256, 0, c->stream>>>(bl.k, nb.k, nv, d, side, f.side, depth, full);
+        k_interface<<<grid_for(c, total, 256), 256, 0, c->stream>>>(bl.k, nb.k, nv, d, side, f.side, depth, full,
+                                                                     fields);
         timing_end(c);
         c->launches++;
       }
@@ -455,13 +471,13 @@ int apply_interfaces(osb_ctx* c, int full) {
 // block's periodic and zero-gradient faces direction by direction (transverse ranges include
 // the halos, so corners come from layers filled before), then the interface faces again with
 // their transverse halos, which the neighbour has filled by then.
-int apply_bc(osb_ctx* c) {
+int apply_bc(osb_ctx* c, int fields = BC_BOTH) {
   bool any_iface = false;
   for (auto& bl : c->blocks)
     for (int d = 0; d < bl.d.ndim; ++d)
       any_iface = any_iface || bl.d.bc[d][0] == OSB_BC_INTERFACE || bl.d.bc[d][1] == OSB_BC_INTERFACE;
   if (any_iface) {
-    int rc = apply_interfaces(c, 0);
+    int rc = apply_interfaces(c, 0, fields);
     if (rc) return rc;
   }
   for (size_t ib = 0; ib < c->blocks.size(); ++ib) {
@@ -475,9 +491,10 @@ int apply_bc(osb_ctx* c) {
         long tr = 1;
         for (int e = 0; e < bl.d.ndim; ++e)
           if (e != d) tr *= bl.k.n[e] + 2 * std::max(dep0, dep1);
-        long total = 2L * std::max(dep0, dep1) * tr * nv;
+        long per = (long)std::max(dep0, dep1) * tr;
         timing_begin(c, FAM_BC);
-        k_periodic<<<grid_for(c, total, 256), 256, 0, c->stream>>>(bl.k, nv, d, dep0, dep1);
+        k_periodic<<<dim3(std::max(1, grid_for(c, per, 256) / (2 * nv) + 1), 2 * nv), 256, 0, c->stream>>>(
+            bl.k, nv, d, dep0, dep1, fields);
         timing_end(c);
         c->launches++;
       } else {
@@ -488,7 +505,7 @@ int apply_bc(osb_ctx* c) {
             for (int e = 0; e < bl.d.ndim; ++e)
               if (e != d) tr *= bl.k.n[e];
             timing_begin(c, FAM_BC);
-            k_zero_grad<<<grid_for(c, tr, 128), 128, 0, c->stream>>>(bl.k, nv, d, side, side ? dep1 : dep0);
+            k_zero_grad<<<grid_for(c, tr, 128), 128, 0, c->stream>>>(bl.k, nv, d, side, side ? dep1 : dep0, fields);
             timing_end(c);
             c->launches++;
           } else if (kind == OSB_BC_PERIODIC) {
@@ -498,7 +515,7 @@ int apply_bc(osb_ctx* c) {
       }
     }
   }
-  if (any_iface) return apply_interfaces(c, 1);
+  if (any_iface) return apply_interfaces(c, 1, fields);
   return OSB_OK;
 }
 
@@ -519,6 +536,8 @@ int stage(osb_ctx* c, int s, double dt) {
       rf.kind = kind;
       rf.a_zero = (kind == 0 && c->A[s] == 0.0) ? 1 : 0;
       rf.A = c->A[s];
+      rf.dt_h = (float)dt;
+      rf.dt_l = (float)(dt - (double)rf.dt_h);
       rf.B = c->B[s];
       rf.dt = dt;
       rf.bad = c->bad;
@@ -536,7 +555,9 @@ int stage(osb_ctx* c, int s, double dt) {
       }
     }
     batch_set_parity(c, c->qf_parity ^ 1);
-    return apply_bc(c);
+    // between stages the FP32 kernels read only the FP32 state; the FP64 halos are refreshed
+    // when a call returns (osb_step / osb_stage)
+    return apply_bc(c, BC_QF);
   }
   for (auto& bl : c->blocks) {
     int rc = residual(c, bl);
@@ -573,7 +594,7 @@ int one_step(osb_ctx* c, double dt) {
     }
     return OSB_OK;
   }
-  int rc = apply_bc(c);
+  int rc = apply_bc(c, c->prec == OSB_PREC_FP32_RESIDUAL ? BC_QF : BC_BOTH);
   if (rc) return rc;
   if (c->rk_kind == OSB_RK_SBLI3) {
     for (auto& bl : c->blocks) {
@@ -837,8 +858,8 @@ int osb_stage(osb_ctx* c, int s, double dt) {
   if (rc) return rc;
   rc = stage(c, s, dt);
   if (rc) return rc;
-  if (use_batch(c)) {
-    rc = apply_bc(c);  // halos of q and of the current FP32 buffer for observers
+  if (c->prec == OSB_PREC_FP32_RESIDUAL) {
+    rc = apply_bc(c, use_batch(c) ? BC_BOTH : BC_Q);  // halos for observers
     if (rc) return rc;
   }
   OSB_CK(cudaGetLastError());
@@ -873,8 +894,8 @@ int osb_step(osb_ctx* c, double dt, int nsteps) {
       int rc = one_step(c, dt);
       if (rc) return rc;
     }
-    if (batch) {
-      int rc = apply_bc(c);
+    if (c->prec == OSB_PREC_FP32_RESIDUAL) {
+      int rc = apply_bc(c, batch ? BC_BOTH : BC_Q);  // halos for observers
       if (rc) return rc;
     }
     OSB_CK(cudaGetLastError());
@@ -910,8 +931,8 @@ int osb_step(osb_ctx* c, double dt, int nsteps) {
       c->launches += c->g_kernels;
       batch_set_parity(c, p ^ (c->nst & 1));
     }
-    if (batch) {
-      int rc = apply_bc(c);  // halos of q and of the current FP32 buffer for observers
+    {
+      int rc = apply_bc(c, batch ? BC_BOTH : BC_Q);  // halos of the FP64 (and FP32) state for observers
       if (rc) return rc;
     }
     OSB_CK(cudaGetLastError());
@@ -1191,8 +1212,9 @@ extern "C" int osb_stage_noalloc(const osb_block_desc* d, int rk_kind, double A,
       long tr = 1;
       for (int e = 0; e < d->ndim; ++e)
         if (e != dd) tr *= k.n[e] + 2 * std::max(dep0, dep1);
-      long total = 2L * std::max(dep0, dep1) * tr * nv;
-      k_periodic<<<grid_for(&c, total, 256), 256, 0, c.stream>>>(k, nv, dd, dep0, dep1);
+      long per = (long)std::max(dep0, dep1) * tr;
+      k_periodic<<<dim3(std::max(1, grid_for(&c, per, 256) / (2 * nv) + 1), 2 * nv), 256, 0, c.stream>>>(
+          k, nv, dd, dep0, dep1, BC_BOTH);
     } else {
       for (int side = 0; side < 2; ++side) {
         int kind = d->bc[dd][side];
@@ -1200,7 +1222,7 @@ extern "C" int osb_stage_noalloc(const osb_block_desc* d, int rk_kind, double A,
           long tr = 1;
           for (int e = 0; e < d->ndim; ++e)
             if (e != dd) tr *= k.n[e];
-          k_zero_grad<<<grid_for(&c, tr, 128), 128, 0, c.stream>>>(k, nv, dd, side, side ? dep1 : dep0);
+          k_zero_grad<<<grid_for(&c, tr, 128), 128, 0, c.stream>>>(k, nv, dd, side, side ? dep1 : dep0, BC_BOTH);
         } else if (kind == OSB_BC_PERIODIC) {
           return fail(OSB_EINVAL, "periodic boundary on one side only (dir %d)", dd);
         } else if (kind == OSB_BC_INTERFACE) {

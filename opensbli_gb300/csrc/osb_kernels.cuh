@@ -247,45 +247,45 @@ struct RkFuse {
   int kind;    // 0 low-storage, 1 SBLI
   int a_zero;  // low-storage stage with A = 0 (the first): the register is not read
   double A, B, dt;
+  float dt_h, dt_l;  // dt as a float-float pair
   float* qout[5];
   unsigned long long* bad;
 };
 
-__device__ __forceinline__ unsigned rk_point_qo(const BlockK& b, const RkFuse& rf, int v, int id, double r0, double q,
-                                                double o) {
+// RK update of one variable from the float-float residual (h, l): dt * (h + l) is formed as a
+// float-float product (exact TwoProduct plus the cross terms, relative error ~2^-48, the
+// precision of the residual itself) and converted once, so the update costs three FP64
+// operations (two on the first low-storage stage) instead of four.
+__device__ __forceinline__ unsigned rk_point_ff(const BlockK& b, const RkFuse& rf, int v, int id, float h, float l,
+                                                double q, double o) {
+  const float p = __fmul_rn(h, rf.dt_h);
+  float e = __fmaf_rn(h, rf.dt_h, -p);
+  e = __fmaf_rn(h, rf.dt_l, __fmaf_rn(l, rf.dt_h, e));
+  const double x = f2d_exact(p) + f2d_exact(e);  // dt * residual
   if (rf.kind == 0) {
-    o = rf.a_zero ? rf.dt * r0 : rf.A * o + rf.dt * r0;
-    q = rf.B * o + q;
+    o = rf.a_zero ? x : __fma_rn(rf.A, o, x);
+    q = __fma_rn(rf.B, o, q);
   } else {
-    q = (rf.A * rf.dt) * r0 + o;
-    o = (rf.B * rf.dt) * r0 + o;
+    q = __fma_rn(rf.A, x, o);
+    o = __fma_rn(rf.B, x, o);
   }
   b.rk[v][id] = o;
   b.q[v][id] = q;
   rf.qout[v][id] = d2f_rn(q);
   return ((((unsigned)__double2hiint(q) >> 20) & 0x7ffu) == 0x7ffu) ? 1u : 0u;
 }
-__device__ __forceinline__ unsigned rk_point(const BlockK& b, const RkFuse& rf, int v, int id, double r0) {
-  return rk_point_qo(b, rf, v, id, r0, b.q[v][id], rf.a_zero ? 0.0 : b.rk[v][id]);
+__device__ __forceinline__ unsigned rk_point(const BlockK& b, const RkFuse& rf, int v, int id, float h, float l) {
+  return rk_point_ff(b, rf, v, id, h, l, b.q[v][id], rf.a_zero ? 0.0 : b.rk[v][id]);
 }
 
-// Final residual of a point from its prefetched partial value plus the last contribution.
-__device__ __forceinline__ double r_final(float fnew, float fold, float invd, float h, float l) {
+// Final residual of a point (float-float) from its prefetched partial value plus the last
+// flux difference / pointwise contribution.
+__device__ __forceinline__ void r_final(float fnew, float fold, float invd, float& h, float& l) {
   float p, pe;
   ff_flux_diff(fnew, fold, invd, p, pe);
   ff_add(h, l, p, pe);
-  return f2d_exact(h) + f2d_exact(l);
 }
-__device__ __forceinline__ double r_final(double fnew, double fold, double invd, double h, double) {
-  return h + -(fnew - fold) * invd;
-}
-__device__ __forceinline__ double rp_final(float c, float h, float l) {
-  ff_add(h, l, c, 0.f);
-  return f2d_exact(h) + f2d_exact(l);
-}
-__device__ __forceinline__ double rp_final(double c, double h, double) { return h + c; }
-__device__ __forceinline__ double to_d(float x) { return f2d_exact(x); }
-__device__ __forceinline__ double to_d(double x) { return x; }
+__device__ __forceinline__ void rp_final(float c, float& h, float& l) { ff_add(h, l, c, 0.f); }
 
 // Residual update with a pointwise contribution c.
 __device__ __forceinline__ void acc_point(const BlockK& b, int v, int id, double c, int first) {
@@ -384,10 +384,12 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 1)
       char_flux<T, ND, SCH, AVG>(w, sp, fh);
     }
     if (j >= j0) {
-      if (FUSE) {
+      if constexpr (FUSE) {
 #pragma unroll
-        for (int lv = 0; lv < NV; ++lv)
-          nbad += rk_point(b, rf, gvar<ND, D, CURV>(lv), id, r_final(fh[lv], fprev[lv], sc, oh[lv], ol[lv]));
+        for (int lv = 0; lv < NV; ++lv) {
+          r_final(fh[lv], fprev[lv], sc, oh[lv], ol[lv]);
+          nbad += rk_point(b, rf, gvar<ND, D, CURV>(lv), id, oh[lv], ol[lv]);
+        }
       } else if (first) {
 #pragma unroll
         for (int lv = 0; lv < NV; ++lv) acc_flux(b, gvar<ND, D, CURV>(lv), id, fh[lv], fprev[lv], sc, 1);
@@ -406,23 +408,27 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 1)
 // Sweep along x.  A warp owns 32 rows (fixed y, z) and a segment of XSEG points; the state of
 // columns s0-3 .. s0+XSEG+2 of its rows is staged in shared memory with coalesced loads, then
 // lane r sweeps row r out of shared memory.
-constexpr int XSEG = 14;   // interfaces per segment: 20 staged columns, 16 warps per SM
-constexpr int XPITCH = 21; // odd pitch: lanes (rows) hit distinct banks
+// The segment length is a launch parameter (osb_set_variant): shorter segments need less shared
+// memory per warp (more resident warps) at the price of one extra interface per segment.  The
+// row pitch is odd so the 32 lanes (rows) of a warp hit distinct banks.
+constexpr int XSEG = 14;  // default: 20 staged columns, 14 warps per SM (FP32, 3D)
+__host__ __device__ constexpr int xpitch_of(int xseg) { return (xseg + 6) | 1; }
 constexpr int XWARPS = 2;
 
 template <typename T, int ND, int SCH, int AVG, bool CURV>
-__global__ void __launch_bounds__(32 * XWARPS) k_flux_x(BlockK b, SchemeParams spd, int first) {
+__global__ void __launch_bounds__(32 * XWARPS) k_flux_x(BlockK b, SchemeParams spd, int first, int xseg) {
   constexpr int NV = ND + 2;
   constexpr int NF = SweepFields<ND, CURV>::N;
   using P = typename SweepPt<T, ND, CURV>::type;
   const SP<T> sp(spd);
   extern __shared__ __align__(16) unsigned char osb_smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int XPITCH = xpitch_of(xseg);
   T* tile = reinterpret_cast<T*>(osb_smem) + (size_t)warp * NF * 32 * XPITCH;
   const int nrows = b.n[1] * b.n[2];
   const int row0 = (blockIdx.y * XWARPS + warp) * 32;
-  const int s0 = blockIdx.x * XSEG;
-  const int s1 = min(b.n[0], s0 + XSEG);
+  const int s0 = blockIdx.x * xseg;
+  const int s1 = min(b.n[0], s0 + xseg);
   if (row0 >= nrows) return;
   // stage rows
   for (int r = 0; r < 32; ++r) {
@@ -608,7 +614,7 @@ __global__ void __launch_bounds__(CX * CY) k_central3d(BlockK b, CentralParams c
     }
     // the fused update's state and register, loaded before the derivative work hides them
     double fq[5], fo[5];
-    if (FUSE) {
+    if constexpr (FUSE) {
 #pragma unroll
       for (int v = 0; v < 5; ++v) {
         fq[v] = b.q[v][gid];
@@ -711,13 +717,14 @@ __global__ void __launch_bounds__(CX * CY) k_central3d(BlockK b, CentralParams c
       racc[4] += e * invRe + h * kheat;
     }
     const int v0 = CONV ? 0 : 1;
-    if (FUSE) {
+    if constexpr (FUSE) {
       // a first (only) residual kernel starts from zero; otherwise from the partial residual
       unsigned nb = 0;
 #pragma unroll
       for (int v = 0; v < 5; ++v) {
-        const double r0 = first ? to_d(racc[v]) : rp_final(v < v0 ? L_(0.0) : racc[v], oh[v], ol[v]);
-        nb += rk_point_qo(b, rf, v, gid, r0, fq[v], fo[v]);
+        float h = first ? racc[v] : oh[v], l = first ? 0.f : ol[v];
+        if (!first && v >= v0) rp_final(racc[v], h, l);
+        nb += rk_point_ff(b, rf, v, gid, h, l, fq[v], fo[v]);
       }
       if (nb) atomicAdd(rf.bad, (unsigned long long)nb);
     } else if (first) {

@@ -98,6 +98,10 @@ class Solver:
         sc = abi.Schedule(mode, tile_y, ctas_per_sm, dynamic, order, fuse_update)
         abi.check(self.lib, self.lib.osb_set_schedule(self.ctx, ctypes.byref(sc)), "osb_set_schedule")
 
+    def set_variant(self, variant):
+        """Tiling variant of the x reconstruction sweep (osb_set_variant)."""
+        abi.check(self.lib, self.lib.osb_set_variant(self.ctx, int(variant)), "osb_set_variant")
+
     def schedule(self):
         """(resolved mode, settings dict) of osb_get_schedule."""
         mode = ctypes.c_int()
