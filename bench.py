@@ -49,6 +49,7 @@ def parse():
                          "Kelvin-Helmholtz instances in one persistent launch per stage; curv4: the "
                          "4-block 3D curvilinear TENO5 case")
     ap.add_argument("--ensemble", type=int, default=64)
+    ap.add_argument("--variant", type=int, default=0, help="x-sweep tiling variant when --fuse is given")
     ap.add_argument("--fuse", default="auto", choices=["auto", "0", "1"],
                     help="RK update inside the central kernel (1), as its own kernel (0), or the fastest "
                          "schedule (fusion and x-sweep tiling) as timed by the autotuner (auto)")
@@ -126,8 +127,8 @@ def measured_traffic(kernel, fused):
         return None
     key = kernel + ("_fused" if kernel == "central" and fused else "")
     for line in open(path):
-        parts = line.split()
-        if len(parts) >= 2 and not line.startswith("#") and parts[0] == key:
+        parts = line.split("#")[0].split()
+        if len(parts) >= 2 and parts[0] == key:
             return float(parts[1])
     return None
 
@@ -263,8 +264,8 @@ def our_arm(args):
     if args.fuse == "auto":
         sched, _ = autotune.tune(s32, dt, steps=2, warmup=1, cache=None)
     else:
-        s32.set_schedule(mode=abi.SCHED_PER_BLOCK, fuse_update=int(args.fuse))
-        sched = dict(s32.schedule()[1], variant=0)
+        sched = dict(s32.schedule()[1], mode=abi.SCHED_PER_BLOCK, fuse_update=int(args.fuse), variant=args.variant)
+        autotune.apply(s32, sched)
     log("schedule %s" % json.dumps(sched))
     s32.step(dt, args.warmup)
     s32.sync()
