@@ -61,6 +61,8 @@ extern "C" {
 #define OSB_BC_PERIODIC 0    /* PeriodicBC -> ExchangeSelf (periodic.py:25-71) */
 #define OSB_BC_ZERO_GRAD 1   /* ZeroGradientOutletBC (zero_gradient_outlet.py:11-23) */
 #define OSB_BC_INTERFACE 2   /* InterfaceBC between blocks (multi_block.py:48-107) */
+#define OSB_BC_EXTRAP0 3     /* ExtrapolationBC order 0 (extrapolation.py:29-38), halo fill only */
+#define OSB_BC_EXTRAP1 4     /* ExtrapolationBC order 1 (extrapolation.py:39-53), halo fill only */
 
 /* Residual precision (per context). */
 #define OSB_PREC_FP64 0          /* plain FP64 path, parity with the generated solver */

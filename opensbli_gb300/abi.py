@@ -32,6 +32,8 @@ VISC_CONSTANT = 2
 BC_PERIODIC = 0
 BC_ZERO_GRAD = 1
 BC_INTERFACE = 2
+BC_EXTRAP0 = 3
+BC_EXTRAP1 = 4
 
 PREC_FP64 = 0
 PREC_FP32_RESIDUAL = 1

@@ -157,6 +157,7 @@ def _rk_of(block):
 def _bcs_of(block, central_only):
     from opensbli.core.boundary_conditions.periodic import PeriodicBC
     from opensbli.core.boundary_conditions.zero_gradient_outlet import ZeroGradientOutletBC
+    from opensbli.core.boundary_conditions.extrapolation import ExtrapolationBC
     bc = [[None, None] for _ in range(block.ndim)]
     depth = [[4, 4] for _ in range(block.ndim)]
     for d, pair in enumerate(block.boundary_types):
@@ -170,6 +171,12 @@ def _bcs_of(block, central_only):
                     depth[d][side] = abs(hv[d][side])
             elif isinstance(b, ZeroGradientOutletBC):
                 bc[d][side] = abi.BC_ZERO_GRAD
+                hv = b.get_halo_values(block)
+                depth[d][side] = abs(hv[d][side])
+            elif isinstance(b, ExtrapolationBC):
+                if b.order not in (0, 1):
+                    raise NotImplementedError("extrapolation of order %s is not supported" % b.order)
+                bc[d][side] = abi.BC_EXTRAP0 if b.order == 0 else abi.BC_EXTRAP1
                 hv = b.get_halo_values(block)
                 depth[d][side] = abs(hv[d][side])
             else:

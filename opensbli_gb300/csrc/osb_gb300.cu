@@ -184,6 +184,46 @@ __global__ void k_zero_grad(BlockK b, int nv, int d, int side, int depth, int fi
   }
 }
 
+// Extrapolation boundary (extrapolation.py:29-53 as generated): boundary point b = 0 on side 0,
+// N-1 on side 1, outward step o.  Order 0: q(b) = q(b-o), q(b+m o) = q(b-o), m = 1..depth.
+// Order 1: q(b+m o) = 2 q(b+(m-1) o) - q(b+(m-2) o), m = 1..depth in order.  Over the interior
+// extent of the other directions.
+__global__ void k_extrap(BlockK b, int nv, int d, int side, int depth, int order, int fields) {
+  int ext[3];
+  for (int e = 0; e < 3; ++e) ext[e] = (e == d) ? 1 : b.n[e];
+  const int total = ext[0] * ext[1] * ext[2];
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+    int c[3];
+    c[0] = t % ext[0];
+    const int r = t / ext[0];
+    c[1] = r % ext[1];
+    c[2] = r / ext[1];
+    c[d] = side == 0 ? 0 : b.n[d] - 1;
+    const int id = lin(b, c[0], c[1], c[2]);
+    const int o = b.st[d] * (side == 0 ? -1 : 1);
+    for (int v = 0; v < nv; ++v) {
+      if (fields & BC_Q) {
+        double* q = b.q[v];
+        if (order == 0) {
+          q[id] = q[id - o];
+          for (int m = 1; m <= depth; ++m) q[id + m * o] = q[id - o];
+        } else {
+          for (int m = 1; m <= depth; ++m) q[id + m * o] = -q[id + (m - 2) * o] + 2.0 * q[id + (m - 1) * o];
+        }
+      }
+      if ((fields & BC_QF) && b.qf[0]) {
+        float* f = b.qf[v];
+        if (order == 0) {
+          f[id] = f[id - o];
+          for (int m = 1; m <= depth; ++m) f[id + m * o] = f[id - o];
+        } else {
+          for (int m = 1; m <= depth; ++m) f[id + m * o] = -f[id + (m - 2) * o] + 2.0f * f[id + (m - 1) * o];
+        }
+      }
+    }
+  }
+}
+
 // Block interface (multi_block.py:11-107, InterfaceBC with identity orientation): the halo
 // layers of face (d, side) of dst receive the `depth` layers of src next to its face
 // (d, sside).  The transverse range is the interior of the face (full = 0) or that plus
@@ -508,6 +548,15 @@ int apply_bc(osb_ctx* c, int fields = BC_BOTH) {
             k_zero_grad<<<grid_for(c, tr, 128), 128, 0, c->stream>>>(bl.k, nv, d, side, side ? dep1 : dep0, fields);
             timing_end(c);
             c->launches++;
+          } else if (kind == OSB_BC_EXTRAP0 || kind == OSB_BC_EXTRAP1) {
+            long tr = 1;
+            for (int e = 0; e < bl.d.ndim; ++e)
+              if (e != d) tr *= bl.k.n[e];
+            timing_begin(c, FAM_BC);
+            k_extrap<<<grid_for(c, tr, 128), 128, 0, c->stream>>>(bl.k, nv, d, side, side ? dep1 : dep0,
+                                                                  kind == OSB_BC_EXTRAP1, fields);
+            timing_end(c);
+            c->launches++;
           } else if (kind == OSB_BC_PERIODIC) {
             return fail(OSB_EINVAL, "periodic boundary on one side only (block %zu dir %d)", ib, d);
           }
@@ -653,6 +702,16 @@ bool check_desc(const osb_block_desc* d, std::string& why) {
       return false;
     }
   }
+  for (int i = 0; i < d->ndim; ++i)
+    for (int s = 0; s < 2; ++s) {
+      const int k = d->bc[i][s];
+      if (k < OSB_BC_PERIODIC || k > OSB_BC_EXTRAP1) { why = "unknown boundary kind"; return false; }
+      if ((k == OSB_BC_EXTRAP0 || k == OSB_BC_EXTRAP1) &&
+          (d->scheme == OSB_SCHEME_CENTRAL4 || d->viscous != OSB_VISC_NONE)) {
+        why = "extrapolation boundaries with central derivatives need the Carpenter boundary closures";
+        return false;
+      }
+    }
   for (int i = 0; i < d->ndim; ++i)
     for (int s = 0; s < 2; ++s) {
       if (d->bc[i][s] != OSB_BC_INTERFACE) continue;
@@ -1223,6 +1282,12 @@ extern "C" int osb_stage_noalloc(const osb_block_desc* d, int rk_kind, double A,
           for (int e = 0; e < d->ndim; ++e)
             if (e != dd) tr *= k.n[e];
           k_zero_grad<<<grid_for(&c, tr, 128), 128, 0, c.stream>>>(k, nv, dd, side, side ? dep1 : dep0, BC_BOTH);
+        } else if (kind == OSB_BC_EXTRAP0 || kind == OSB_BC_EXTRAP1) {
+          long tr = 1;
+          for (int e = 0; e < d->ndim; ++e)
+            if (e != dd) tr *= k.n[e];
+          k_extrap<<<grid_for(&c, tr, 128), 128, 0, c.stream>>>(k, nv, dd, side, side ? dep1 : dep0,
+                                                                kind == OSB_BC_EXTRAP1, BC_BOTH);
         } else if (kind == OSB_BC_PERIODIC) {
           return fail(OSB_EINVAL, "periodic boundary on one side only (dir %d)", dd);
         } else if (kind == OSB_BC_INTERFACE) {

@@ -35,10 +35,11 @@ def _cons(spec, rho, u, p):
     return [np.ascontiguousarray(np.broadcast_to(x, spec.shape), dtype=np.float64) for x in q]
 
 
-def sod(n=400, scheme=abi.SCHEME_WENO5_JS):
-    """1D Sod shock tube on [0,1] with Delta = 1/(N-1), zero-gradient ends."""
+def sod(n=400, scheme=abi.SCHEME_WENO5_JS, bc=(abi.BC_ZERO_GRAD, abi.BC_ZERO_GRAD)):
+    """1D Sod shock tube on [0,1] with Delta = 1/(N-1); zero-gradient ends unless `bc` names
+    other boundary kinds (left, right)."""
     spec = BlockSpec(ndim=1, size=(n,), scheme=scheme, averaging=abi.AVG_SIMPLE,
-                     bc=[[abi.BC_ZERO_GRAD, abi.BC_ZERO_GRAD]], bc_depth=[[4, 4]],
+                     bc=[list(bc)], bc_depth=[[4, 4]],
                      delta=(1.0 / (n - 1),), gama=1.4)
     x = spec.delta[0] * spec.grid_index(0)
     left = x < 0.5

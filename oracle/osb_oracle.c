@@ -739,6 +739,36 @@ static void zero_grad_face(osb_block_desc* b, const geom_t* g, int d, int side, 
       }
 }
 
+/* Extrapolation boundary (extrapolation.py:29-53 as generated), boundary point b = 0 on side 0,
+ * N-1 on side 1, outward step o = -1 / +1.  Order 0: q(b) = q(b-o), then q(b+m o) = q(b-o) for
+ * m = 1..depth.  Order 1: q(b+m o) = 2 q(b+(m-1) o) - q(b+(m-2) o) for m = 1..depth, in that
+ * order (each layer from the two before it).  Over the interior transverse extent. */
+static void extrap_face(osb_block_desc* b, const geom_t* g, int d, int side, int depth, int order) {
+  const int nd = b->ndim, nv = nd + 2;
+  int lo[3], hi[3];
+  for (int e = 0; e < 3; ++e) {
+    if (e < nd) { lo[e] = 0; hi[e] = g->n[e]; } else { lo[e] = 0; hi[e] = 1; }
+  }
+  const int N = g->n[d];
+  const int base = side == 0 ? 0 : N - 1;
+  lo[d] = base; hi[d] = base + 1;
+  const long o = g->st[d] * (side == 0 ? -1 : 1);
+  for (int k = lo[2]; k < hi[2]; ++k)
+    for (int j = lo[1]; j < hi[1]; ++j)
+      for (int i = lo[0]; i < hi[0]; ++i) {
+        long id = gid(g, i, j, k);
+        for (int v = 0; v < nv; ++v) {
+          double* q = b->q[v];
+          if (order == 0) {
+            q[id] = q[id - o];
+            for (int m = 1; m <= depth; ++m) q[id + m * o] = q[id - o];
+          } else {
+            for (int m = 1; m <= depth; ++m) q[id + m * o] = -q[id + (m - 2) * o] + 2.0 * q[id + (m - 1) * o];
+          }
+        }
+      }
+}
+
 /* Block interface (multi_block.py:11-107, identity orientation, matching faces normal to the
  * same direction): the halo layers of face (d, side) receive the neighbour's layers adjacent to
  * its face (d, f->side).  `full` = 0 copies the interior of the face only; `full` = 1 also the
@@ -783,6 +813,8 @@ int oracle_apply_bc(osb_block_desc* blocks, int nblocks, int zero_grad_only) {
           int depth = b->bc_depth[d][side] > 0 ? b->bc_depth[d][side] : 4;
           if (pass == 1 && kind == OSB_BC_PERIODIC && !zero_grad_only) periodic_face(b, &g, d, side, depth);
           if (pass == 1 && kind == OSB_BC_ZERO_GRAD) zero_grad_face(b, &g, d, side, depth);
+          if (pass == 1 && (kind == OSB_BC_EXTRAP0 || kind == OSB_BC_EXTRAP1))
+            extrap_face(b, &g, d, side, depth, kind == OSB_BC_EXTRAP1);
           if (pass != 1 && kind == OSB_BC_INTERFACE && !zero_grad_only)
             interface_face(blocks, b, &g, d, side, depth, pass == 2);
         }

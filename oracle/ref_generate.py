@@ -140,7 +140,15 @@ def _finish(block, alg_kwargs, params):
     substitute_simulation_parameters(list(names), list(values))
 
 
-def case_sod_weno5js():
+def case_sod_extrap():
+    """1D Sod as case_sod_weno5js but with extrapolation boundaries: linear (order 1) on the
+    left, zeroth order on the right (core/boundary_conditions/extrapolation.py)."""
+    from opensbli import ExtrapolationBC
+    block, params = case_sod_weno5js(bcs=[ExtrapolationBC(0, 0, order=1), ExtrapolationBC(0, 1, order=0)])
+    return block, params
+
+
+def case_sod_weno5js(bcs=None):
     """1D Sod, WENO5-JS characteristic LLF (simple average), zero-gradient ends, RK-LS3.
     Problem definition follows ``apps/Sod_shock_tube/Sod_shock_tube.py`` with the
     scheme/BC/time-stepper choices of the 1D Sod parity case."""
@@ -165,7 +173,7 @@ def case_sod_weno5js():
     schemes[LF.name] = LF
     rk = RungeKuttaLS(3)
     schemes[rk.name] = rk
-    block.set_block_boundaries([ZeroGradientOutletBC(0, 0), ZeroGradientOutletBC(0, 1)])
+    block.set_block_boundaries(bcs or [ZeroGradientOutletBC(0, 0), ZeroGradientOutletBC(0, 1)])
     block.set_equations([copy.deepcopy(cr), copy.deepcopy(sim), initial])
     block.set_discretisation_schemes(schemes)
     block.discretise()
@@ -384,6 +392,7 @@ def case_curv_weno5z():
 
 CASES = {
     "sod_weno5js": case_sod_weno5js,
+    "sod_extrap": case_sod_extrap,
     "tgv_teno5": lambda: case_tgv_shock("teno5"),
     "tgv_weno5z": lambda: case_tgv_shock("weno5z"),
     "tgv_teno6": lambda: case_tgv_shock("teno6"),

@@ -29,6 +29,8 @@ def perturb(q, amp, seed):
 
 CASES = {
     # name: (reference case, problem builder, env, dt, stage counts, perturbation)
+    "sod_extrap_200_perturbed": ("sod_extrap", lambda: problems.sod(200, bc=(abi.BC_EXTRAP1, abi.BC_EXTRAP0)),
+                                 {"OSB_NP0": 200}, 2e-4, [1, 3, 30], (1e-2, 13)),
     "sod_weno5js_400": ("sod_weno5js", lambda: problems.sod(400), {"OSB_NP0": 400}, 2e-4, [1, 3, 30, 3000], None),
     "tgv_teno5_12": ("tgv_teno5", lambda: problems.tgv(12, minf=1.25, scheme=abi.SCHEME_TENO5, averaging=abi.AVG_ROE),
                      {"OSB_NP0": 12, "OSB_NP1": 12, "OSB_NP2": 12}, 1e-3, [1, 3, 12], None),

@@ -73,3 +73,13 @@ def test_kh_spec():
     assert spec.scheme == abi.SCHEME_WENO5_Z and spec.averaging == abi.AVG_ROE
     assert be.rk[0] == abi.RK_SBLI3
     assert spec.bc_depth == [[4, 4], [4, 4]]
+
+
+@needs_ref
+def test_extrapolation_and_teno6_specs():
+    be = _backend_for("sod_extrap", {"gama": "1.4", "dt": "0.0002", "niter": "10", "block0np0": "200",
+                                     "Delta0block0": "1.0/(block0np0-1)"})
+    spec = be.specs[0]
+    assert spec.bc == [[abi.BC_EXTRAP1, abi.BC_EXTRAP0]] and spec.bc_depth == [[4, 4]]
+    be = _backend_for("tgv_teno6", dict(TGV_NUMBERS, Minf="1.25"))
+    assert be.specs[0].scheme == abi.SCHEME_TENO6 and be.specs[0].averaging == abi.AVG_ROE

@@ -69,6 +69,14 @@ def test_sod_weno5js_fp64(built_lib, oracle_lib, nstages):
     assert max(errs) < 1e-12, errs
 
 
+@pytest.mark.parametrize("nstages", [1, 3, 30])
+def test_sod_extrapolation_fp64(built_lib, oracle_lib, nstages):
+    """Linear extrapolation on the left, zeroth order on the right, perturbed state."""
+    spec, q = problems.sod(200, bc=(abi.BC_EXTRAP1, abi.BC_EXTRAP0))
+    errs, _, _ = _run_pair(spec, _perturb(q, 1e-2, 13), "ls3", 2e-4, nstages)
+    assert max(errs) < 1e-12, errs
+
+
 def test_sod_1000_steps_fp64(built_lib, oracle_lib):
     spec, q = problems.sod(400)
     errs, got, _ = _run_pair(spec, q, "ls3", 2e-4, 3000)

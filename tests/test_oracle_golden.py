@@ -12,6 +12,8 @@ GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 CASES = {
     "sod_weno5js_400": (lambda: problems.sod(400), "ls3", None, 1e-12),
+    "sod_extrap_200_perturbed": (lambda: problems.sod(200, bc=(abi.BC_EXTRAP1, abi.BC_EXTRAP0)), "ls3", (1e-2, 13),
+                                 1e-12),
     "tgv_teno5_12": (lambda: problems.tgv(12, minf=1.25, scheme=abi.SCHEME_TENO5, averaging=abi.AVG_ROE), "ls3",
                      None, 1e-12),
     "tgv_teno6_12": (lambda: problems.tgv(12, minf=1.25, scheme=abi.SCHEME_TENO6, averaging=abi.AVG_ROE), "ls3",
