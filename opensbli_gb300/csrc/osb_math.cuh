@@ -74,11 +74,11 @@ __device__ __forceinline__ T recon5(T fm2, T fm1, T f0, T fp1, T fp2, const SP<T
       r0 = r0 * r0 * r0; r0 = r0 * r0;
       r1 = r1 * r1 * r1; r1 = r1 * r1;
       r2 = r2 * r2 * r2; r2 = r2 * r2;
-      T inv = L_(1.0) / (r0 + r1 + r2);
-      T ct = sp.teno_ct;
-      d0 = (r0 * inv < ct) ? L_(0.0) : L_(1.0);
-      d1 = (r1 * inv < ct) ? L_(0.0) : L_(1.0);
-      d2 = (r2 * inv < ct) ? L_(0.0) : L_(1.0);
+      // alpha_r / sum < C_T  <=>  alpha_r < C_T * sum (sum > 0)
+      const T cs = sp.teno_ct * (r0 + r1 + r2);
+      d0 = (r0 < cs) ? L_(0.0) : L_(1.0);
+      d1 = (r1 < cs) ? L_(0.0) : L_(1.0);
+      d2 = (r2 < cs) ? L_(0.0) : L_(1.0);
     } else {
       T eps = sp.teno_eps;
       T t0 = L_(1.0) + tau / (eps + b0), t1 = L_(1.0) + tau / (eps + b1), t2 = L_(1.0) + tau / (eps + b2);
@@ -328,8 +328,12 @@ __device__ __forceinline__ void char_flux(const Pt<T, ND> (&w)[6], const SP<T>& 
     for (int i = 1; i < ND; ++i) Fv[1 + i] = s.u[0] * s.q[1 + i];
     Fv[NV - 1] = s.u[0] * (s.q[NV - 1] + s.p);
     T cs[NV], cf[NV];
+    // FP32 path: the flux is F = u_n q + p (0, 1, 0.., u_n), so L.F = u_n (L.q) + p (L e_1 + u_n L e_E)
+    // with the two LEV columns in closed form; the FP64 path projects F itself (the reference's
+    // operation order).
+    constexpr int NPASS = sizeof(T) == 4 ? 1 : 2;
 #pragma unroll
-    for (int pass = 0; pass < 2; ++pass) {
+    for (int pass = 0; pass < NPASS; ++pass) {
       const T* v = pass == 0 ? s.q : Fv;
       T* o = pass == 0 ? cs : cf;
       T um = L_(0.0);
@@ -346,6 +350,15 @@ __device__ __forceinline__ void char_flux(const Pt<T, ND> (&w)[6], const SP<T>& 
       }
       o[ND] = bta * (S + a * D);
       o[ND + 1] = bta * (S - a * D);
+    }
+    if (NPASS == 1) {
+      const T un = s.u[0], du = un - u[0];
+      const T pb = s.p * bta, gd = g1 * du;
+      cf[0] = un * cs[0] - s.p * g1 * ia2 * du;
+#pragma unroll
+      for (int k = 1; k < ND; ++k) cf[k] = un * cs[k];
+      cf[ND] = un * cs[ND] + pb * (a + gd);
+      cf[ND + 1] = un * cs[ND + 1] + pb * (gd - a);
     }
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
