@@ -44,10 +44,10 @@ def parse():
     ap.add_argument("--size", type=int, default=NS)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="tgv", choices=["tgv", "kh_ensemble", "curv4"],
-                    help="tgv: the 256^3 supersonic TGV (headline); kh_ensemble: 64 uneven 2D "
-                         "Kelvin-Helmholtz instances in one persistent launch per stage; curv4: the "
-                         "4-block 3D curvilinear TENO5 case")
+    ap.add_argument("--workload", default="tgv", choices=["tgv", "sod", "tgv64", "kh_ensemble", "curv4"],
+                    help="tgv: the 256^3 supersonic TGV (headline); sod: the 400-point Sod tube; tgv64: the "
+                         "64^3 central TGV; kh_ensemble: 64 uneven 2D Kelvin-Helmholtz instances in one "
+                         "persistent launch per stage; curv4: the 4-block 3D curvilinear TENO5 case")
     ap.add_argument("--ensemble", type=int, default=64)
     ap.add_argument("--variant", type=int, default=0, help="x-sweep tiling variant when --fuse is given")
     ap.add_argument("--fuse", default="auto", choices=["auto", "0", "1"],
@@ -212,6 +212,23 @@ def cpu_baseline(n, stages=2):
                       "-O3); rate from stage %d..%d timestamps" % (stages, n, 2, stages)}
 
 
+def cpu_reference_rate(case, env, points, stages, what):
+    """The reference's generated OPS solver for `case` (oracle/_ref/<case>, -O3, OpenMP on all
+    host cores): Mpt-RK-stage/s from its per-stage timestamps after the first stage."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import harness
+    cores = os.cpu_count() or 1
+    if not harness.ref_available(case):
+        return None
+    r = harness.run_ref(case, env=dict(env, OSB_NITER=stages // 3 + 2), stop_after_rk=stages, threads=cores,
+                        fast=True, dump=False)
+    t = r["_rk_times"]
+    per_stage = (t[-1] - t[1]) / (len(t) - 2)
+    return {"value": points / per_stage / 1e6, "unit": UNIT, "cores": cores, "kind": "reference",
+            "sample": "%d RK stages of %s with the reference's generated OPS solver (OpenMP, -O3); rate from "
+                      "the stage timestamps after the first" % (stages, what)}
+
+
 def reference_arm(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -342,21 +359,32 @@ def our_arm(args):
         log("fp64 done")
 
     # end to end through the public API with pinned host buffers: H2D state, one RK step, D2H state
-    host_q = torch.from_numpy(np.stack(q)).pin_memory()
-    host_out = torch.empty_like(host_q).pin_memory()
+    host_q = torch.empty(s32.q[0].shape, dtype=torch.float64, pin_memory=True)
+    host_q.copy_(torch.from_numpy(np.stack(q)))
+    host_out = torch.empty_like(host_q, pin_memory=True)
     stream = s32.stream()
-    e2e_steps = max(1, min(args.steps, 3))
+    e2e_steps = max(1, min(args.steps, 5))
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    parts = [0.0, 0.0, 0.0]
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
+        ev[0].record(stream)
         with torch.cuda.stream(stream):
             s32.q[0].copy_(host_q, non_blocking=True)
+        ev[1].record(stream)
         s32.apply_bc()
         s32.step(dt, 1)
+        ev[2].record(stream)
         with torch.cuda.stream(stream):
             host_out.copy_(s32.q[0], non_blocking=True)
+        ev[3].record(stream)
         s32.sync()
+        for k in range(3):
+            parts[k] += ev[k].elapsed_time(ev[k + 1])
     t_e2e = time.perf_counter() - t0
+    log("e2e per step: H2D %.2f ms, step %.2f ms, D2H %.2f ms, wall %.2f ms"
+        % tuple([x / e2e_steps for x in parts] + [t_e2e / e2e_steps * 1e3]))
     e2e_value = world * pts * 3 * e2e_steps / t_e2e / 1e6
     nbytes = host_q.numel() * 8
     # the pinned buffers were used on the solver's stream: release them before the stream goes
@@ -435,13 +463,30 @@ def secondary_arm(args):
 
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
-    if args.workload == "kh_ensemble":
+    cpu = None
+    if args.workload == "sod":
+        blocks = [problems.sod(400)]
+        dt = 2e-4
+        rk = "ls3"
+        work = "Sod shock tube, 400 points, WENO5-JS (simple average), RK-LS3, zero-gradient ends"
+        bytes_pt = 4 * 3 * 8
+        cpu_args = ("sod_weno5js", {"OSB_NP0": 400}, 400, 600, "the 400-point Sod case")
+    elif args.workload == "tgv64":
+        blocks = [problems.tgv(64, minf=0.1, scheme=abi.SCHEME_CENTRAL4)]
+        dt = 3.385e-3
+        rk = "ls3"
+        work = "TGV 64^3, M=0.1, Re=1600, central-4 Feiereisen + viscous, RK-LS3, periodic"
+        bytes_pt = 4 * 5 * 8
+        cpu_args = ("tgv_central", {"OSB_NP0": 64, "OSB_NP1": 64, "OSB_NP2": 64}, 64 ** 3, 12, "the 64^3 central TGV")
+    elif args.workload == "kh_ensemble":
         blocks = problems.kh_ensemble(args.ensemble, seed=0)
         dt = 2e-4
         rk = "ls3"
         work = ("%d Kelvin-Helmholtz 2D instances, sizes drawn by seed 0 from {128,192,256,384,512}^2, "
                 "WENO5-Z (Roe), RK-LS3, periodic" % args.ensemble)
         bytes_pt = 4 * 8 * 4 + 2 * 4 * 4  # q, rk read+write FP64 (4 vars) + FP32 state in/out
+        cpu_args = ("kh_weno5z", {"OSB_NP0": 320, "OSB_NP1": 320}, 320 ** 2, 12,
+                    "one 320^2 Kelvin-Helmholtz instance (the ensemble's mean size)")
     else:
         blocks = problems.curvilinear_multiblock_3d(seed=0)
         dt = problems.multiblock_cfl_dt(blocks, CFL)
@@ -449,8 +494,17 @@ def secondary_arm(args):
         work = ("4-block 3D curvilinear Euler (512x256x32, 384x256x32, 512x192x32, 256x256x32), TENO5 (Roe), "
                 "interfaces + periodic, Mach 0.7 + Gaussian pulse, RK-LS3, CFL %.1f" % CFL)
         bytes_pt = 4 * 5 * 8
+        cpu_args = ("curv_weno5z", {"OSB_NP0": 1024, "OSB_NP1": 1024}, 1024 ** 2, 12,
+                    "the reference's 2D curvilinear WENO5-Z case at 1024^2 (no 3D multi-block curvilinear "
+                    "reference case is generated)")
     pts = sum(b[0].npoints for b in blocks)
     log("problem ready: %d blocks, %d points" % (len(blocks), pts))
+    if not args.no_cpu:
+        try:
+            cpu = cpu_reference_rate(*cpu_args)
+        except Exception as ex:  # the baseline is reported, not required
+            cpu = {"value": None, "unit": UNIT, "kind": "reference", "sample": "failed: %s" % str(ex)[:200]}
+        log("cpu baseline %s" % json.dumps(cpu))
     s32 = Solver(blocks, precision="fp32", rk=rk, device=local)
     s32.apply_bc()
     tuned = None
@@ -512,7 +566,7 @@ def secondary_arm(args):
                        "schedule": "persistent" if mode == abi.SCHED_PERSISTENT else "per-block",
                        "l2": "inputs larger than L2, no flush"},
             "autotune": tuned, "fp64": {"value": fp64, "unit": UNIT, "fp32_over_fp64": value / fp64},
-            "error_vs_fp64": err, "clocks": clk, "gpu_launches": launches,
+            "error_vs_fp64": err, "clocks": clk, "gpu_launches": launches, "cpu_baseline": cpu,
             "kernel_ms_per_step": {k: v[0] for k, v in rep.items() if v[1]},
             "schedule": sched,
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",

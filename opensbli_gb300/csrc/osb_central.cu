@@ -8,7 +8,7 @@ namespace {
 template <typename T, bool CONV, int VISC, bool FUSE>
 int launch_central_k(osb_ctx* c, Block& bl, int first, const RkFuse& rf) {
   using Fd = CentralFields<T, CONV, VISC>;
-  size_t smem = (size_t)Fd::N * CPTS * sizeof(T);
+  size_t smem = (size_t)Fd::N * CRING * CPL * sizeof(T);
   auto kern = k_central3d<T, CONV, VISC, FUSE>;
   OSB_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   CentralParams cp{};
@@ -30,7 +30,7 @@ int launch_central_k(osb_ctx* c, Block& bl, int first, const RkFuse& rf) {
     cp.inv2d_f[i] = (float)cp.inv2d[i];
   }
   const BlockK& k = bl.k;
-  dim3 grid((k.n[0] + CX - 1) / CX, (k.n[1] + CY - 1) / CY, (k.n[2] + CZ - 1) / CZ);
+  dim3 grid((k.n[0] + CX - 1) / CX, (k.n[1] + CY - 1) / CY, (k.n[2] + CZC - 1) / CZC);
   timing_begin(c, FAM_CENTRAL);
   kern<<<grid, CX * CY, smem, c->stream>>>(k, cp, first, rf);
   timing_end(c);

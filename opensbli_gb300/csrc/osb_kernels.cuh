@@ -509,9 +509,14 @@ __device__ __forceinline__ double cpar<double>(double d, float) { return d; }
 template <>
 __device__ __forceinline__ float cpar<float>(double, float f) { return f; }
 
-constexpr int CX = 32, CY = 4, CZ = 4, CH = 2;
-constexpr int CSX = CX + 2 * CH, CSY = CY + 2 * CH, CSZ = CZ + 2 * CH;
-constexpr int CPTS = CSX * CSY * CSZ;
+// A CTA owns a 32 x 4 column of points and streams it through CZC planes of z: the planes
+// z-2 .. z+2 around the current one sit in a 5-plane ring in shared memory (halo 2 in x and y,
+// edges included), the raw state of plane z+3 is loaded into registers while plane z is
+// computed, then converted to primitives into the slot plane z-2 vacates.
+constexpr int CX = 32, CY = 4, CH = 2, CZC = 32, CRING = 5;
+constexpr int CSX = CX + 2 * CH, CSY = CY + 2 * CH;
+constexpr int CPL = CSX * CSY;  // points of one staged plane
+constexpr int CPP = (CPL + CX * CY - 1) / (CX * CY);  // staged points per thread and plane
 
 template <typename T, bool CONV, int VISC>
 struct CentralFields {
@@ -525,72 +530,89 @@ struct CentralFields {
 template <typename T, bool CONV, int VISC, bool FUSE>
 __global__ void __launch_bounds__(CX * CY) k_central3d(BlockK b, CentralParams cp, int first, RkFuse rf) {
   using Fd = CentralFields<T, CONV, VISC>;
+  constexpr int FS = CRING * CPL;  // field stride in shared memory
   extern __shared__ __align__(16) unsigned char osb_smem[];
   T* sm = reinterpret_cast<T*>(osb_smem);
   const int tx = threadIdx.x % CX, ty = threadIdx.x / CX;
-  const int x0 = blockIdx.x * CX, y0 = blockIdx.y * CY, z0 = blockIdx.z * CZ;
+  const int x0 = blockIdx.x * CX, y0 = blockIdx.y * CY;
+  const int zb = blockIdx.z * CZC, ze = min(b.n[2], zb + CZC);
   const T gm = cpar<T>(cp.gama, cp.gama_f);
   const T M2 = cpar<T>(cp.M2, cp.M2_f);
   const T mu_c = cpar<T>(cp.mu_c, cp.mu_c_f);
   const T invRe = cpar<T>(cp.invRe, cp.invRe_f);
   const T kheat = cpar<T>(cp.kheat, cp.kheat_f);
-  // ---- load the halo'd tile and form primitives
-  // loads of CU points per thread are issued together before any of them is used
-  constexpr int CU = 6;
-  for (int base = threadIdx.x; base < CPTS; base += CU * CX * CY) {
-    T qv[CU][5];
-    bool ok[CU];
+  // raw state of one plane, CPP points per thread
+  T qv[CPP][5];
+  auto load_plane = [&](int gz) {
 #pragma unroll
-    for (int u = 0; u < CU; ++u) {
-      const int idx = base + u * CX * CY;
-      const int i = idx % CSX, jj = (idx / CSX) % CSY, k = idx / (CSX * CSY);
-      const int gx = x0 - CH + i, gy = y0 - CH + jj, gz = z0 - CH + k;
-      ok[u] = idx < CPTS && gx <= b.n[0] + CH && gy <= b.n[1] + CH && gz <= b.n[2] + CH;
-      if (ok[u]) {
+    for (int u = 0; u < CPP; ++u) {
+      const int idx = threadIdx.x + u * CX * CY;
+      const int gx = x0 - CH + idx % CSX, gy = y0 - CH + idx / CSX;
+      if (idx < CPL && gx <= b.n[0] + CH && gy <= b.n[1] + CH) {
         const int id = lin(b, gx, gy, gz);
 #pragma unroll
         for (int v = 0; v < 5; ++v) qv[u][v] = ld_q<T>(b, v, id);
       }
     }
+  };
+  // primitives of the loaded plane into ring slot `slot`
+  auto store_plane = [&](int slot) {
 #pragma unroll
-    for (int u = 0; u < CU; ++u) {
-      if (!ok[u]) continue;
-      const int idx = base + u * CX * CY;
+    for (int u = 0; u < CPP; ++u) {
+      const int idx = threadIdx.x + u * CX * CY;
+      const int gx = x0 - CH + idx % CSX, gy = y0 - CH + idx / CSX;
+      if (!(idx < CPL && gx <= b.n[0] + CH && gy <= b.n[1] + CH)) continue;
+      const int at = slot * CPL + idx;
       const T rho = qv[u][0], m0 = qv[u][1], m1 = qv[u][2], m2 = qv[u][3], E = qv[u][4];
       T ir = L_(1.0) / rho;
       T u0 = m0 * ir, u1 = m1 * ir, u2 = m2 * ir;
       T p = (gm - L_(1.0)) * (E - L_(0.5) * rho * (u0 * u0 + u1 * u1 + u2 * u2));
-      sm[Fd::U0 * CPTS + idx] = u0;
-      sm[Fd::U1 * CPTS + idx] = u1;
-      sm[Fd::U2 * CPTS + idx] = u2;
-      sm[Fd::P * CPTS + idx] = p;
+      sm[Fd::U0 * FS + at] = u0;
+      sm[Fd::U1 * FS + at] = u1;
+      sm[Fd::U2 * FS + at] = u2;
+      sm[Fd::P * FS + at] = p;
       if (VISC) {
         T Tt = M2 * gm * p * ir;
-        sm[Fd::TT * CPTS + idx] = Tt;
-        sm[Fd::MU * CPTS + idx] = (VISC == 1) ? L_(1.4042) * Tt * sqrt(Tt) / (L_(0.40417) + Tt) : mu_c;
+        sm[Fd::TT * FS + at] = Tt;
+        sm[Fd::MU * FS + at] = (VISC == 1) ? L_(1.4042) * Tt * sqrt(Tt) / (L_(0.40417) + Tt) : mu_c;
       }
       if (CONV) {
-        sm[Fd::RHO * CPTS + idx] = rho;
-        sm[Fd::M0 * CPTS + idx] = m0;
-        sm[Fd::M1 * CPTS + idx] = m1;
-        sm[Fd::M2 * CPTS + idx] = m2;
-        sm[Fd::E * CPTS + idx] = E;
+        sm[Fd::RHO * FS + at] = rho;
+        sm[Fd::M0 * FS + at] = m0;
+        sm[Fd::M1 * FS + at] = m1;
+        sm[Fd::M2 * FS + at] = m2;
+        sm[Fd::E * FS + at] = E;
       }
     }
+  };
+  auto slot_of = [](int gz) { return (gz + 2 * CRING) % CRING; };
+  // prologue: planes zb-2 .. zb+1 into the ring, plane zb+2 into registers
+  for (int gz = zb - CH; gz < zb + CH; ++gz) {
+    load_plane(gz);
+    store_plane(slot_of(gz));
   }
-  __syncthreads();
+  load_plane(zb + CH);
   const int gx = x0 + tx, gy = y0 + ty;
-  if (gx >= b.n[0] || gy >= b.n[1]) return;
+  const bool active = gx < b.n[0] && gy < b.n[1];
   const T id0 = cpar<T>(cp.invd[0], cp.invd_f[0]), id1 = cpar<T>(cp.invd[1], cp.invd_f[1]),
           id2 = cpar<T>(cp.invd[2], cp.invd_f[2]);
   const T jd0 = cpar<T>(cp.inv2d[0], cp.inv2d_f[0]), jd1 = cpar<T>(cp.inv2d[1], cp.inv2d_f[1]),
           jd2 = cpar<T>(cp.inv2d[2], cp.inv2d_f[2]);
-  const int sx = 1, sy = CSX, sz = CSX * CSY;
-  for (int tz = 0; tz < CZ; ++tz) {
-    const int gz = z0 + tz;
-    if (gz >= b.n[2]) break;
-    const int c = (tz + CH) * sz + (ty + CH) * sy + (tx + CH);
-    auto F = [&](int f, int o) -> T { return sm[f * CPTS + c + o]; };
+  // offsets are written as linear offsets of a virtual (x, y, z) tile with z stride CPL and
+  // decoded into (plane, in-plane) parts; they are compile-time constants after unrolling
+  const int sx = 1, sy = CSX, sz = CPL;
+  const int cxy = (ty + CH) * CSX + (tx + CH);
+  for (int gz = zb; gz < ze; ++gz) {
+    store_plane(slot_of(gz + CH));  // plane gz+2, loaded during the previous iteration
+    __syncthreads();
+    if (gz + CH + 1 < ze + CH) load_plane(gz + CH + 1);
+    int pbase[2 * CH + 1];
+#pragma unroll
+    for (int k = 0; k <= 2 * CH; ++k) pbase[k] = slot_of(gz + k - CH) * CPL;
+    auto F = [&](int f, int o) -> T {
+      const int dz = (o + 2 * sz + sz / 2) / sz - 2;
+      return sm[f * FS + pbase[dz + CH] + cxy + (o - dz * sz)];
+    };
     auto D1 = [&](int f, int s, T inv) -> T { return d1w<T>(F(f, -2 * s), F(f, -s), F(f, s), F(f, 2 * s)) * inv; };
     auto D2 = [&](int f, int s, T inv) -> T { return d2w<T>(F(f, -2 * s), F(f, -s), F(f, 0), F(f, s), F(f, 2 * s)) * inv; };
     // mixed derivative: central-4 along sb of the central-4 derivative along sa
@@ -606,6 +628,9 @@ __global__ void __launch_bounds__(CX * CY) k_central3d(BlockK b, CentralParams c
       }
       return r * ib;
     };
+    // every thread reaches both barriers of an iteration at the same call sites: the point
+    // update is guarded, never skipped with a jump past a barrier
+    if (active) {
     const int gid = lin(b, gx, gy, gz);
     T oh[5], ol[5];
     if (!first) {
@@ -734,6 +759,8 @@ __global__ void __launch_bounds__(CX * CY) k_central3d(BlockK b, CentralParams c
 #pragma unroll
       for (int v = v0; v < 5; ++v) rp_store(b, v, gid, racc[v], oh[v], ol[v]);
     }
+    }  // active
+    __syncthreads();  // the next iteration overwrites the slot of plane gz-2
   }
 }
 
