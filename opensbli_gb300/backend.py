@@ -11,7 +11,7 @@ Reference flow (e.g. apps/compressible_taylor_green_vortex/compressible_TGV.py:2
 GB300 flow:
 
     alg = TraditionalAlgorithmRK(block)
-    be = GB300Backend(alg, dict(zip(names, values)), precision="fp64")
+    be = GB300Backend(alg, dict(zip(names, values)))   # precision from SimulationDataType
     be.initialise()                             # the script's GridBasedInitialisation, on the host
     be.run(niter)                               # the generated time loop, on the GPU
 
@@ -263,11 +263,53 @@ def _np_piecewise(*args):
     return out
 
 
+PRECISION_STRATEGIES = ("q_vector", "wk_arrays", "residuals", "RK_arrays", "custom")
+
+
+def precision_of(mixed_precision_config=None):
+    """Precision mode implied by the reference's own precision knobs.
+
+    The reference stores every dataset in one global type (``SimulationDataType.set_datatype``,
+    core/datatypes.py:3-17: Double or FloatC; Half exists as a type) and can lower the storage
+    of groups of arrays (``OPSC(..., mixed_precision_config={strategy: (arrays, type)})``,
+    code_generation/opsc.py:462-534, strategies q_vector, wk_arrays, residuals, RK_arrays,
+    custom).  Here the state, the RK registers and the reductions are always FP64 and what can
+    be lowered is the arithmetic of the residual, so:
+
+    * Double everywhere (or nothing set) -> "fp64";
+    * FloatC globally or for any strategy -> "fp32" (FP32 residual; no array ends up with
+      less precision than the script asked for);
+    * Half anywhere -> NotImplementedError;
+    * an unknown strategy -> ValueError, as opsc.py:523 raises (the keyword itself is
+      OPSC.__init__, opsc.py:408).
+    """
+    from opensbli.core.datatypes import DataType, FloatC, Half, SimulationDataType
+    types = []
+    glob = SimulationDataType.__dict__.get("dtype")
+    if isinstance(glob, type) and issubclass(glob, DataType):
+        types.append(glob)
+    for strategy, inputs in (mixed_precision_config or {}).items():
+        if strategy not in PRECISION_STRATEGIES:
+            raise ValueError("Unknown mixed precision preset: {}. Please choose from: {}."
+                             .format(strategy, ", ".join(PRECISION_STRATEGIES)))
+        types.append(inputs[1])
+    for t in types:
+        if isinstance(t, type) and issubclass(t, Half):
+            raise NotImplementedError("half-precision storage is not supported (FP32 residual is the lowest)")
+    return "fp32" if any(isinstance(t, type) and issubclass(t, FloatC) for t in types) else "fp64"
+
+
 class GB300Backend:
     """Stands in for OPSC(alg): owns the GPU state of every block of ``alg`` and runs its
-    time loop on the GB300 kernels."""
+    time loop on the GB300 kernels.  ``precision`` is "fp64" or "fp32" (FP32 residual, FP64
+    state); left as None it follows the script's SimulationDataType and the optional
+    ``mixed_precision_config`` of OPSC (see precision_of)."""
 
-    def __init__(self, alg, parameters, precision="fp64", device=0, graphs=True):
+    def __init__(self, alg, parameters, precision=None, device=0, graphs=True, mixed_precision_config=None):
+        if precision is None:
+            precision = precision_of(mixed_precision_config)
+        if precision not in ("fp64", "fp32"):
+            raise ValueError("precision must be 'fp64' or 'fp32', not %r" % (precision,))
         self.alg = alg
         self.params = dict(parameters)
         self.numbers = resolve_parameters(self.params)

@@ -30,9 +30,15 @@ int launch_central_k(osb_ctx* c, Block& bl, int first, const RkFuse& rf) {
     cp.inv2d_f[i] = (float)cp.inv2d[i];
   }
   const BlockK& k = bl.k;
-  dim3 grid((k.n[0] + CX - 1) / CX, (k.n[1] + CY - 1) / CY, (k.n[2] + CZC - 1) / CZC);
+  // z chunks per column: whole waves of resident CTAs; a chunk starts by staging four planes
+  // (two of halo) at about a third of the cost of a computed plane each
+  const long cols = (long)((k.n[0] + CX - 1) / CX) * ((k.n[1] + CY - 1) / CY);
+  const long slots = (long)resident_ctas(kern, CX * CY, smem) * c->sm_count;
+  const int nz = wave_chunks(k.n[2], cols, slots, 1.4, 8);
+  const int czc = (k.n[2] + nz - 1) / nz;
+  dim3 grid((k.n[0] + CX - 1) / CX, (k.n[1] + CY - 1) / CY, (k.n[2] + czc - 1) / czc);
   timing_begin(c, FAM_CENTRAL);
-  kern<<<grid, CX * CY, smem, c->stream>>>(k, cp, first, rf);
+  kern<<<grid, CX * CY, smem, c->stream>>>(k, cp, first, czc, rf);
   timing_end(c);
   c->launches++;
   return OSB_OK;

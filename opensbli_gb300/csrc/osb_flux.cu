@@ -19,16 +19,30 @@
 namespace osb {
 namespace {
 
+// One y or z sweep over `lines` lines of N interfaces: the lines are cut into segments so the
+// CTAs fill the resident slots in nearly whole waves (a segment costs one extra interface and
+// the start of its 6-point window, about 1.5 interfaces).
+template <typename T, int ND, int D, int SCH, int AVG, bool CURV, bool FUSE>
+int launch_sweep_k(osb_ctx* c, const BlockK& k, const SchemeParams& sp, int N, int other, const RkFuse& rf) {
+  auto kern = k_flux_sweep<T, ND, D, SCH, AVG, CURV, FUSE>;
+  const long slots = (long)resident_ctas(kern, SWEEP_THREADS, 0) * c->sm_count;
+  const long gx = (k.n[0] + SWEEP_THREADS - 1) / SWEEP_THREADS;
+  int nseg = wave_chunks(N, gx * other, slots, 1.5, 8);
+  const int seg = (N + nseg - 1) / nseg;
+  nseg = (N + seg - 1) / seg;
+  const long gy = (long)other * nseg;
+  dim3 grid((unsigned)gx, (unsigned)std::min(gy, 65535L), (unsigned)((gy + 65534) / 65535));
+  if (grid.z > 1) return fail(OSB_ENOTSUP, "block too large for the sweep grid");
+  kern<<<grid, SWEEP_THREADS, 0, c->stream>>>(k, sp, seg, nseg, 0, rf);
+  return OSB_OK;
+}
+
 template <typename T, int ND, int D, int SCH, int AVG, bool CURV>
-void launch_sweep(osb_ctx* c, const BlockK& k, const SchemeParams& sp, dim3 grid, int seg, int nseg,
-                  const RkFuse* rf) {
+int launch_sweep(osb_ctx* c, const BlockK& k, const SchemeParams& sp, int N, int other, const RkFuse* rf) {
   if constexpr (sizeof(T) == 4) {
-    if (rf) {
-      k_flux_sweep<T, ND, D, SCH, AVG, CURV, true><<<grid, 128, 0, c->stream>>>(k, sp, seg, nseg, 0, *rf);
-      return;
-    }
+    if (rf) return launch_sweep_k<T, ND, D, SCH, AVG, CURV, true>(c, k, sp, N, other, *rf);
   }
-  k_flux_sweep<T, ND, D, SCH, AVG, CURV, false><<<grid, 128, 0, c->stream>>>(k, sp, seg, nseg, 0, RkFuse{});
+  return launch_sweep_k<T, ND, D, SCH, AVG, CURV, false>(c, k, sp, N, other, RkFuse{});
 }
 
 // x sweep (writes R), then y[, z] sweeps (accumulate); with rf (FP32 path, 2D/3D) the last
@@ -54,21 +68,15 @@ int launch_flux(osb_ctx* c, Block& bl, const SchemeParams& sp, const RkFuse* rf)
   }
   // y, z sweeps (accumulate)
   for (int D = 1; D < ND; ++D) {
-    int N = k.n[D];
-    long lines = (long)k.n[0] * (ND == 3 ? (D == 1 ? k.n[2] : k.n[1]) : 1);
-    long target = (long)c->sm_count * 512;
-    int nseg = (int)std::max(1L, std::min((long)(N / 16 > 0 ? N / 16 : 1), (target + lines - 1) / lines));
-    int seg = (N + nseg - 1) / nseg;
-    nseg = (N + seg - 1) / seg;
-    int other = ND == 3 ? (D == 1 ? k.n[2] : k.n[1]) : 1;
-    long gy = (long)other * nseg;
-    dim3 grid((k.n[0] + 127) / 128, (unsigned)std::min(gy, 65535L), (unsigned)((gy + 65534) / 65535));
-    if (grid.z > 1) return fail(OSB_ENOTSUP, "block too large for the sweep grid");
+    const int N = k.n[D];
+    const int other = ND == 3 ? (D == 1 ? k.n[2] : k.n[1]) : 1;
     timing_begin(c, D == 1 ? FAM_FLUX_Y : FAM_FLUX_Z);
     const RkFuse* f = D == ND - 1 ? rf : nullptr;
-    if (D == 1) launch_sweep<T, ND, 1, SCH, AVG, CURV>(c, k, sp, grid, seg, nseg, f);
-    else if (ND == 3) launch_sweep<T, ND, (ND == 3 ? 2 : 1), SCH, AVG, CURV>(c, k, sp, grid, seg, nseg, f);
+    int rc = OSB_OK;
+    if (D == 1) rc = launch_sweep<T, ND, 1, SCH, AVG, CURV>(c, k, sp, N, other, f);
+    else if (ND == 3) rc = launch_sweep<T, ND, (ND == 3 ? 2 : 1), SCH, AVG, CURV>(c, k, sp, N, other, f);
     timing_end(c);
+    if (rc != OSB_OK) return rc;
     c->launches++;
   }
   return OSB_OK;

@@ -106,6 +106,39 @@ void batch_set_parity(osb_ctx* c, int parity);
 int batch_stage(osb_ctx* c, int s, double dt);
 size_t batch_smem(int ty);
 // Central convective and/or viscous terms of one 3D block (osb_central.cu).
+// Resident CTAs per SM of a kernel at a launch shape (occupancy calculator; 1 if it fails).
+template <typename K>
+inline int resident_ctas(K kern, int threads, size_t smem) {
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, threads, smem) != cudaSuccess) {
+    cudaGetLastError();
+    nb = 1;
+  }
+  return nb > 0 ? nb : 1;
+}
+
+// Number of chunks a line of n work units (interfaces, planes) is cut into when each chunk
+// count k gives ctas_per_chunk * k CTAs over `slots` resident CTA slots: minimises
+// waves * (chunk length + overhead), where overhead is the start-up cost of a chunk in work
+// units, so the last wave is nearly full without paying for many short chunks.  Chunks are at
+// least min_len long unless the line is shorter.
+inline int wave_chunks(int n, long ctas_per_chunk, long slots, double overhead, int min_len) {
+  int best = 1;
+  double best_cost = 1e300;
+  for (int k = 1; k <= n; ++k) {
+    const int len = (n + k - 1) / k;
+    if (k > 1 && len < min_len) break;
+    if ((n + len - 1) / len != k) continue;  // the same split as a smaller k
+    const long waves = (ctas_per_chunk * k + slots - 1) / slots;
+    const double cost = (double)waves * (len + overhead);
+    if (cost < best_cost * (1.0 - 1e-9)) {
+      best_cost = cost;
+      best = k;
+    }
+  }
+  return best;
+}
+
 int central_f64(osb_ctx* c, Block& bl, bool conv, int first, const RkFuse* rf);
 int central_f32(osb_ctx* c, Block& bl, bool conv, int first, const RkFuse* rf);
 

@@ -315,14 +315,26 @@ __device__ __forceinline__ int gvar(int lv) {
 
 // ---------------------------------------------------------------------------------------
 // Sweep along y (D=1) or z (D=2): thread = (x, transverse, segment).
+// The fields of point j+3 and the residual of point j that iteration j needs are copied with
+// cp.async into a per-thread ring of shared-memory slots one iteration ahead, so their latency
+// overlaps a whole interface's arithmetic without holding registers (the register file is the
+// occupancy limit of these kernels).  A slot is refilled two iterations after it was read.
+constexpr int SWEEP_THREADS = 128, SWEEP_RING = 3;
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+
 template <typename T, int ND, int D, int SCH, int AVG, bool CURV, bool FUSE>
-__global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 1)
+__global__ void __launch_bounds__(SWEEP_THREADS, sizeof(T) == 4 ? 4 : 1)
     k_flux_sweep(BlockK b, SchemeParams spd, int seg, int nseg, int first, RkFuse rf) {
   constexpr int NV = ND + 2;
   constexpr int NF = SweepFields<ND, CURV>::N;
+  constexpr int NR = sizeof(T) == 4 ? 2 * NV : NV;  // residual words of a point: float-float pairs or doubles
+  constexpr int NS = NF + NR;
   using P = typename SweepPt<T, ND, CURV>::type;
+  __shared__ T ring[SWEEP_RING][NS][SWEEP_THREADS];
   const SP<T> sp(spd);
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int tid = threadIdx.x;
+  const int x = blockIdx.x * blockDim.x + tid;
   const int other = blockIdx.y / nseg, sidx = blockIdx.y % nseg;
   if (x >= b.n[0]) return;
   int c1 = 0, c2 = 0;
@@ -339,6 +351,30 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 1)
   if (j0 >= j1) return;
   const T gm = sp.gama;
   const T invd = (T)b.invd[D];
+  const bool rd = !first;
+  // iteration it (interface j = j0 - 1 + it) reads the fields of point j + 3 and, for j >= j0,
+  // the residual of point j (both inside the 5-point halo / the interior)
+  auto issue = [&](int it, int slot) {
+    const int j = j0 - 1 + it;
+    const int idf = base + (j + 3) * s;
+#pragma unroll
+    for (int f = 0; f < NF; ++f) cp_async_el(&ring[slot][f][tid], field_ptr<T, ND, D, CURV>(b, f) + idf);
+    if (rd && j >= j0) {
+      const int idr = base + j * s;
+#pragma unroll
+      for (int lv = 0; lv < NV; ++lv) {
+        const int v = gvar<ND, D, CURV>(lv);
+        if constexpr (sizeof(T) == 4) {
+          cp_async_el(&ring[slot][NF + 2 * lv][tid], b.Rh[v] + idr);
+          cp_async_el(&ring[slot][NF + 2 * lv + 1][tid], b.Rl[v] + idr);
+        } else {
+          cp_async_el(&ring[slot][NF + lv][tid], b.R[v] + idr);
+        }
+      }
+    }
+    cp_async_commit();
+  };
+  issue(0, 0);
   P w[6];
 #pragma unroll
   for (int m = 1; m < 6; ++m) {
@@ -347,33 +383,35 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 1)
     for (int f = 0; f < NF; ++f) set_field(w[m], f, ld_field<T, ND, D, CURV>(b, f, id));
     make_pt<T, ND>(w[m], gm);
   }
-  // the fields of point j+3 are loaded one step ahead (point j+4 <= N+3 stays inside the halo)
-  T nxt[NF];
-  {
-    int id = base + (j0 + 2) * s;
-#pragma unroll
-    for (int f = 0; f < NF; ++f) nxt[f] = ld_field<T, ND, D, CURV>(b, f, id);
-  }
   T fprev[NV];
 #pragma unroll
   for (int lv = 0; lv < NV; ++lv) fprev[lv] = L_(0.0);
   unsigned nbad = 0;
-  for (int j = j0 - 1; j < j1; ++j) {
+  const int nit = j1 - j0 + 1;
+  int cur = 0;
+  for (int it = 0; it < nit; ++it) {
+    const int j = j0 - 1 + it;
+    const int nxt = cur == SWEEP_RING - 1 ? 0 : cur + 1;
+    if (it + 1 < nit) issue(it + 1, nxt); else cp_async_commit();
+    cp_async_wait_prev();  // the group of iteration it has landed
 #pragma unroll
     for (int m = 0; m < 5; ++m) w[m] = w[m + 1];
 #pragma unroll
-    for (int f = 0; f < NF; ++f) set_field(w[5], f, nxt[f]);
-    {
-      int id = base + (j + 4) * s;
-#pragma unroll
-      for (int f = 0; f < NF; ++f) nxt[f] = ld_field<T, ND, D, CURV>(b, f, id);
-    }
+    for (int f = 0; f < NF; ++f) set_field(w[5], f, ring[cur][f][tid]);
     make_pt<T, ND>(w[5], gm);
     const int id = base + j * s;
     T oh[NV], ol[NV];
-    if (!first && j >= j0) {
+    if (rd && j >= j0) {
 #pragma unroll
-      for (int lv = 0; lv < NV; ++lv) r_load(b, gvar<ND, D, CURV>(lv), id, oh[lv], ol[lv]);
+      for (int lv = 0; lv < NV; ++lv) {
+        if constexpr (sizeof(T) == 4) {
+          oh[lv] = ring[cur][NF + 2 * lv][tid];
+          ol[lv] = ring[cur][NF + 2 * lv + 1][tid];
+        } else {
+          oh[lv] = ring[cur][NF + lv][tid];
+          ol[lv] = L_(0.0);
+        }
+      }
     }
     T fh[NV];
     T sc = invd;
@@ -400,6 +438,7 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 1)
     }
 #pragma unroll
     for (int lv = 0; lv < NV; ++lv) fprev[lv] = fh[lv];
+    cur = nxt;
   }
   if (FUSE && nbad) atomicAdd(rf.bad, (unsigned long long)nbad);
 }
@@ -509,11 +548,12 @@ __device__ __forceinline__ double cpar<double>(double d, float) { return d; }
 template <>
 __device__ __forceinline__ float cpar<float>(double, float f) { return f; }
 
-// A CTA owns a 32 x 4 column of points and streams it through CZC planes of z: the planes
+// A CTA owns a 32 x 4 column of points and streams it through czc planes of z (a launch
+// argument, chosen on the host so the CTAs fill whole waves): the planes
 // z-2 .. z+2 around the current one sit in a 5-plane ring in shared memory (halo 2 in x and y,
 // edges included), the raw state of plane z+3 is loaded into registers while plane z is
 // computed, then converted to primitives into the slot plane z-2 vacates.
-constexpr int CX = 32, CY = 4, CH = 2, CZC = 32, CRING = 5;
+constexpr int CX = 32, CY = 4, CH = 2, CRING = 5;
 constexpr int CSX = CX + 2 * CH, CSY = CY + 2 * CH;
 constexpr int CPL = CSX * CSY;  // points of one staged plane
 constexpr int CPP = (CPL + CX * CY - 1) / (CX * CY);  // staged points per thread and plane
@@ -528,14 +568,14 @@ struct CentralFields {
 };
 
 template <typename T, bool CONV, int VISC, bool FUSE>
-__global__ void __launch_bounds__(CX * CY) k_central3d(BlockK b, CentralParams cp, int first, RkFuse rf) {
+__global__ void __launch_bounds__(CX * CY) k_central3d(BlockK b, CentralParams cp, int first, int czc, RkFuse rf) {
   using Fd = CentralFields<T, CONV, VISC>;
   constexpr int FS = CRING * CPL;  // field stride in shared memory
   extern __shared__ __align__(16) unsigned char osb_smem[];
   T* sm = reinterpret_cast<T*>(osb_smem);
   const int tx = threadIdx.x % CX, ty = threadIdx.x / CX;
   const int x0 = blockIdx.x * CX, y0 = blockIdx.y * CY;
-  const int zb = blockIdx.z * CZC, ze = min(b.n[2], zb + CZC);
+  const int zb = blockIdx.z * czc, ze = min(b.n[2], zb + czc);
   const T gm = cpar<T>(cp.gama, cp.gama_f);
   const T M2 = cpar<T>(cp.M2, cp.M2_f);
   const T mu_c = cpar<T>(cp.mu_c, cp.mu_c_f);

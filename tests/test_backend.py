@@ -83,3 +83,35 @@ def test_extrapolation_and_teno6_specs():
     assert spec.bc == [[abi.BC_EXTRAP1, abi.BC_EXTRAP0]] and spec.bc_depth == [[4, 4]]
     be = _backend_for("tgv_teno6", dict(TGV_NUMBERS, Minf="1.25"))
     assert be.specs[0].scheme == abi.SCHEME_TENO6 and be.specs[0].averaging == abi.AVG_ROE
+
+
+@needs_ref
+def test_precision_follows_reference_datatype_knobs():
+    """SimulationDataType (core/datatypes.py:3-17) and OPSC's mixed_precision_config
+    (opsc.py:462-534) select the precision mode when none is given."""
+    import sys
+    import ref_generate
+    if REF not in sys.path:
+        sys.path.insert(0, REF)
+    ref_generate.apply_compat_patches()
+    from opensbli.core.datatypes import Double, FloatC, Half, SimulationDataType
+    from opensbli_gb300.backend import precision_of
+    saved = SimulationDataType.__dict__["dtype"]
+    try:
+        SimulationDataType.set_datatype(Double)
+        assert precision_of() == "fp64"
+        assert precision_of({"residuals": ([], FloatC)}) == "fp32"
+        assert precision_of({"wk_arrays": ([], FloatC), "RK_arrays": ([], Double)}) == "fp32"
+        assert precision_of({"q_vector": ([], Double)}) == "fp64"
+        with pytest.raises(NotImplementedError):
+            precision_of({"custom": ([], Half)})
+        with pytest.raises(ValueError):
+            precision_of({"bogus": ([], FloatC)})
+        SimulationDataType.set_datatype(FloatC)
+        assert precision_of() == "fp32"
+        SimulationDataType.set_datatype(Double)
+        be = _backend_for("sod_weno5js", {"gama": "1.4", "dt": "0.0002", "niter": "10", "block0np0": "400",
+                                          "Delta0block0": "1.0/(block0np0-1)"})
+        assert be.precision == "fp64"
+    finally:
+        setattr(SimulationDataType, "dtype", saved)
