@@ -162,8 +162,9 @@ int osb_sync(osb_ctx* ctx, int timeout_ms);
 /* Enables (1) or disables (0) CUDA-graph capture of osb_step. */
 int osb_set_graphs(osb_ctx* ctx, int enable);
 
-/* Selects the tiling variant of the x reconstruction sweep (autotuner hook): 0 or < 0 the
- * default segment of 14 interfaces per warp row, 1 = 12, 2 = 10, 3 = 18. */
+/* Selects the segment length of the x reconstruction sweep (autotuner hook): 0, < 0 or > 5 the
+ * length that fills whole waves of resident CTAs, 1 = whole rows, 2 = 64, 3 = 32, 4 = 16,
+ * 5 = 48 points. */
 int osb_set_variant(osb_ctx* ctx, int variant);
 
 /* Stage schedule.  OSB_SCHED_PER_BLOCK runs every block's sweeps, RK update and boundary

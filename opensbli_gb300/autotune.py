@@ -2,7 +2,8 @@
 
 For a solver holding its blocks, times every candidate schedule -- per-block launches with and
 without the RK update fused into the last residual kernel and with each x-sweep segment length
-(osb_set_variant), and the persistent fused stage over
+(osb_set_variant: the wave-model length, whole rows, 64, 32, 16, 48 points), and the persistent
+fused stage over
 tile heights, resident CTAs per SM, static or dynamic tile claiming and tile orders -- on the
 caller's own workload (CUDA-graph replays timed with CUDA events on the
 solver's stream), restores the state after every trial, applies the fastest schedule and caches
@@ -28,7 +29,7 @@ DEFAULT_CACHE = os.environ.get("OSB_AUTOTUNE_CACHE",
 def candidates(persistent):
     """Candidate schedules: the per-block path, plus the persistent stage's knob grid."""
     out = [{"mode": abi.SCHED_PER_BLOCK, "tile_y": 16, "ctas_per_sm": 2, "dynamic": 1, "order": 0, "fuse_update": f,
-            "variant": v} for f in (1, 0) for v in (0, 1, 2, 3)]
+            "variant": v} for f in (1, 0) for v in range(6)]
     if persistent:
         for ty in (8, 16, 32):
             for cps in (1, 2, 3, 4):

@@ -54,13 +54,25 @@ int launch_flux(osb_ctx* c, Block& bl, const SchemeParams& sp, const RkFuse* rf)
   // x sweep (writes R)
   {
     constexpr int NF = SweepFields<ND, CURV>::N;
-    // osb_set_variant: 0 = default segment, 1..3 = 12, 10, 18 interfaces per segment
-    const int xseg = c->variant == 1 ? 12 : c->variant == 2 ? 10 : c->variant == 3 ? 18 : XSEG;
-    size_t smem = (size_t)XWARPS * NF * 32 * xpitch_of(xseg) * sizeof(T);
+    const size_t smem = (size_t)XWARPS * sizeof(XTile<T, NF, CURV ? ND + 3 : ND + 2>);
     auto kern = k_flux_x<T, ND, SCH, AVG, CURV>;
     OSB_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    int nrows = k.n[1] * k.n[2];
-    dim3 grid((k.n[0] + xseg - 1) / xseg, (nrows + 32 * XWARPS - 1) / (32 * XWARPS));
+    const int nrows = k.n[1] * k.n[2];
+    const long gy = (nrows + 32 * XWARPS - 1) / (32 * XWARPS);
+    // osb_set_variant: 0 = segments from the wave model (a segment start costs about four
+    // interfaces: the extra interface, the window start and the first chunk's copy), 1 = whole
+    // rows, 2 = 64, 3 = 32, 4 = 16, 5 = 48 points per segment
+    static const int fixed_seg[6] = {0, 0, 64, 32, 16, 48};
+    int xseg;
+    if (c->variant == 1) xseg = k.n[0];
+    else if (c->variant >= 2 && c->variant <= 5) xseg = fixed_seg[c->variant];
+    else {
+      const long slots = (long)resident_ctas(kern, 32 * XWARPS, smem) * c->sm_count;
+      const int nx = wave_chunks(k.n[0], gy, slots, 4.0, 16);
+      xseg = (k.n[0] + nx - 1) / nx;
+    }
+    xseg = std::max(1, std::min(xseg, k.n[0]));
+    dim3 grid((k.n[0] + xseg - 1) / xseg, (unsigned)gy);
     timing_begin(c, FAM_FLUX_X);
     kern<<<grid, 32 * XWARPS, smem, st>>>(k, sp, 1, xseg);
     timing_end(c);

@@ -444,86 +444,136 @@ __global__ void __launch_bounds__(SWEEP_THREADS, sizeof(T) == 4 ? 4 : 1)
 }
 
 // ---------------------------------------------------------------------------------------
-// Sweep along x.  A warp owns 32 rows (fixed y, z) and a segment of XSEG points; the state of
-// columns s0-3 .. s0+XSEG+2 of its rows is staged in shared memory with coalesced loads, then
-// lane r sweeps row r out of shared memory.
-// The segment length is a launch parameter (osb_set_variant): shorter segments need less shared
-// memory per warp (more resident warps) at the price of one extra interface per segment.  The
-// row pitch is odd so the 32 lanes (rows) of a warp hit distinct banks.
-constexpr int XSEG = 14;  // default: 20 staged columns, 14 warps per SM (FP32, 3D)
-__host__ __device__ constexpr int xpitch_of(int xseg) { return (xseg + 6) | 1; }
+// Sweep along x.  A warp owns 32 rows (fixed y, z; lane = row) and a segment [s0, s1) of x.
+// Input: the state of its rows streams through a ring of XRING chunks of XCH columns in shared
+// memory; the warp copies chunk k+1 with cp.async (one instruction moves XCH consecutive
+// columns of 32 / XCH rows) while its lanes sweep chunk k with a 6-point register window.
+// Output: each lane puts the flux of its interfaces into a tile of XOUT columns plus a carry
+// column (the interface left of the tile); every XOUT points the warp forms the residual
+// differences and stores them row by row in whole 32-byte sectors.  Stores straight from the
+// sweep (lane = row) would leave every sector partially written for many iterations and send
+// read-modify-write traffic to DRAM.  Segments can be long: each costs one extra interface and
+// one window start; the length is chosen on the host (whole waves of resident CTAs) or fixed by
+// osb_set_variant.  Row pitches are odd, so the 32 lanes (rows) of a warp hit distinct banks.
+constexpr int XCH = 4, XRING = 2, XCOLS = XCH * XRING, XPITCH = XCOLS + 1, XOUT = 8, XOPITCH = XOUT + 1;
 constexpr int XWARPS = 2;
+
+template <typename T, int NF, int NO>
+struct XTile {
+  T in[NF][32][XPITCH];
+  T out[NO][32][XOPITCH];  // column 0: carry, 1..XOUT: fluxes at the right faces of the tile's points
+  int rowbase[32];
+};
 
 template <typename T, int ND, int SCH, int AVG, bool CURV>
 __global__ void __launch_bounds__(32 * XWARPS) k_flux_x(BlockK b, SchemeParams spd, int first, int xseg) {
   constexpr int NV = ND + 2;
   constexpr int NF = SweepFields<ND, CURV>::N;
+  constexpr int NO = CURV ? NV + 1 : NV;  // curvilinear: the point's 1 / (dx J) rides along
+  constexpr int RPI = 32 / XCH;           // rows per copy instruction
+  constexpr int OPI = 32 / XOUT;          // rows per store instruction
   using P = typename SweepPt<T, ND, CURV>::type;
   const SP<T> sp(spd);
   extern __shared__ __align__(16) unsigned char osb_smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int XPITCH = xpitch_of(xseg);
-  T* tile = reinterpret_cast<T*>(osb_smem) + (size_t)warp * NF * 32 * XPITCH;
+  XTile<T, NF, NO>& t = reinterpret_cast<XTile<T, NF, NO>*>(osb_smem)[warp];
   const int nrows = b.n[1] * b.n[2];
   const int row0 = (blockIdx.y * XWARPS + warp) * 32;
+  if (row0 >= nrows) return;  // whole warps only: the lanes below stay converged
   const int s0 = blockIdx.x * xseg;
   const int s1 = min(b.n[0], s0 + xseg);
-  if (row0 >= nrows) return;
-  // stage rows
-  for (int r = 0; r < 32; ++r) {
-    int row = row0 + r;
-    if (row >= nrows) break;
-    int y = row % b.n[1], z = row / b.n[1];
-    int col = s0 - 3 + lane;
-    if (col <= s1 + 2) {
-      int id = lin(b, col, y, z);
-#pragma unroll
-      for (int f = 0; f < NF; ++f) cp_async_el(tile + (f * 32 + r) * XPITCH + lane, field_ptr<T, ND, 0, CURV>(b, f) + id);
-    }
+  {
+    // rows past the block end repeat the last row (computed, never stored)
+    const int row = min(row0 + lane, nrows - 1);
+    const int y = row % b.n[1], z = row / b.n[1];
+    t.rowbase[lane] = lin(b, 0, y, z);
   }
-  cp_async_wait_all();
   __syncwarp();
-  const int row = row0 + lane;
-  if (row >= nrows) return;
-  const int y = row % b.n[1], z = row / b.n[1];
-  const int base = lin(b, 0, y, z);
-  const T gm = sp.gama;
+  const int c0 = s0 - 3;          // global x of input column 0
+  const int ncols = s1 - s0 + 6;  // columns s0-3 .. s1+2
+  auto issue = [&](int k) {       // input chunk k: columns c0 + XCH k .. c0 + XCH k + XCH - 1
+    const int rc = k * XCH + (lane % XCH);
+    if (rc < ncols) {
+      const int pos = rc % XCOLS;
+#pragma unroll
+      for (int rb = 0; rb < XCH; ++rb) {
+        const int r = rb * RPI + lane / XCH;
+        const int id = t.rowbase[r] + c0 + rc;
+#pragma unroll
+        for (int f = 0; f < NF; ++f) cp_async_el(&t.in[f][r][pos], field_ptr<T, ND, 0, CURV>(b, f) + id);
+      }
+    }
+    cp_async_commit();
+  };
   const T invd = (T)b.invd[0];
+  // residuals of the points s0 + pb .. s0 + pb + XOUT - 1 (those below s1) from the out tile
+  auto flush = [&](int pb) {
+    __syncwarp();
+    const int cc = lane % XOUT;
+    const int p = s0 + pb + cc;
+    if (p < s1) {
+#pragma unroll
+      for (int rb = 0; rb < XOUT; ++rb) {
+        const int r = rb * OPI + lane / XOUT;
+        if (row0 + r < nrows) {
+          const int id = t.rowbase[r] + p;
+          const T sc = CURV ? t.out[NO - 1][r][cc + 1] : invd;
+#pragma unroll
+          for (int v = 0; v < NV; ++v) acc_flux(b, v, id, t.out[v][r][cc + 1], t.out[v][r][cc], sc, first);
+        }
+      }
+    }
+    __syncwarp();
+#pragma unroll
+    for (int v = 0; v < NV; ++v) t.out[v][lane][0] = t.out[v][lane][XOUT];
+  };
+  const int nchunks = (ncols + XCH - 1) / XCH;
+  issue(0);
+  if (nchunks > 1) issue(1); else cp_async_commit();
+  cp_async_wait_prev();  // chunk 0 landed
+  __syncwarp();
+  const T gm = sp.gama;
   P w[6];
 #pragma unroll
-  for (int m = 1; m < 6; ++m) {
-    int col = m - 1;  // point s0-3+col
+  for (int m = 1; m < 6; ++m) {  // columns 0..4: points s0-3 .. s0+1
+    if (m - 1 == XCH) {          // column XCH opens chunk 1
+      __syncwarp();
+      if (2 < nchunks) issue(2); else cp_async_commit();
+      cp_async_wait_prev();
+      __syncwarp();
+    }
 #pragma unroll
-    for (int f = 0; f < NF; ++f) set_field(w[m], f, tile[(f * 32 + lane) * XPITCH + col]);
+    for (int f = 0; f < NF; ++f) set_field(w[m], f, t.in[f][lane][(m - 1) % XCOLS]);
     make_pt<T, ND>(w[m], gm);
   }
-  T fprev[NV];
-#pragma unroll
-  for (int v = 0; v < NV; ++v) fprev[v] = L_(0.0);
   for (int j = s0 - 1; j < s1; ++j) {
+    const int rc = j - s0 + 6;  // input column of the new point j + 3
+    if (rc % XCH == 0) {
+      // entering chunk k = rc / XCH: every lane has read chunk k-1, whose slots take chunk k+1
+      const int k = rc / XCH;
+      __syncwarp();
+      if (k + 1 < nchunks) issue(k + 1); else cp_async_commit();
+      cp_async_wait_prev();  // chunk k landed
+      __syncwarp();
+    }
 #pragma unroll
     for (int m = 0; m < 5; ++m) w[m] = w[m + 1];
-    {
-      int col = j + 3 - (s0 - 3);
 #pragma unroll
-      for (int f = 0; f < NF; ++f) set_field(w[5], f, tile[(f * 32 + lane) * XPITCH + col]);
-      make_pt<T, ND>(w[5], gm);
-    }
+    for (int f = 0; f < NF; ++f) set_field(w[5], f, t.in[f][lane][rc % XCOLS]);
+    make_pt<T, ND>(w[5], gm);
     T fh[NV];
-    T sc = invd;
     if constexpr (CURV) {
       char_flux_curv<T, ND, SCH, AVG>(w, sp, fh);
-      sc = invd / w[2].J;
     } else {
       char_flux<T, ND, SCH, AVG>(w, sp, fh);
     }
-    if (j >= s0) {
-      int id = base + j;
+    // interface j + 1/2 is the right face of point j: out column (j - s0) % XOUT + 1, or the
+    // carry column for the face left of the segment
+    const int oc = j < s0 ? 0 : (j - s0) % XOUT + 1;
 #pragma unroll
-      for (int v = 0; v < NV; ++v) acc_flux(b, v, id, fh[v], fprev[v], sc, first);
-    }
-#pragma unroll
-    for (int v = 0; v < NV; ++v) fprev[v] = fh[v];
+    for (int v = 0; v < NV; ++v) t.out[v][lane][oc] = fh[v];
+    if constexpr (CURV) t.out[NO - 1][lane][oc] = invd / w[2].J;
+    if (j >= s0 && (oc == XOUT || j == s1 - 1)) flush(j - s0 - (oc - 1));
   }
 }
 

@@ -68,11 +68,12 @@ def test_fused_stage_matches_residual_plus_update(built_lib, name):
             assert float(np.max(np.abs(q1[i][v][sl] - qn))) / scale_q < 1e-14, (name, i, v, "state")
 
 
-@pytest.mark.parametrize("variant", [1, 2, 3])
+@pytest.mark.parametrize("variant", [1, 2, 3, 4, 5])
 def test_x_sweep_variants_are_bit_identical(built_lib, variant):
-    """The x-sweep segment length (osb_set_variant) changes only the tiling: same states."""
+    """The x-sweep segment length (osb_set_variant) changes only the tiling: same states.
+    70^3: 4 900 rows leave a partial last warp, segments of 64 and 32 leave ragged ends."""
     from opensbli_gb300.solver import Solver
-    spec, q = problems.tgv(20, minf=1.25, scheme=abi.SCHEME_TENO5, averaging=abi.AVG_ROE)
+    spec, q = problems.tgv(70, minf=1.25, scheme=abi.SCHEME_TENO5, averaging=abi.AVG_ROE)
     out = []
     for var in (0, variant):
         s = Solver([(spec, q)], precision="fp32", rk="ls3")
