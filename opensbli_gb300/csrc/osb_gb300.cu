@@ -153,6 +153,76 @@ __global__ void k_periodic(BlockK b, int nv, int d, int depth0, int depth1, int 
   }
 }
 
+// Periodic halos of a block whose faces are all periodic with one depth D: every point of
+// [-D, N+D) per used direction outside the interior receives the interior point at the
+// wrapped coordinates -- what the direction-by-direction exchange (k_periodic for x, then y,
+// then z, transverse ranges including the halos) leaves there -- in one launch.  The shell is
+// walked as three disjoint regions (z faces with full x-y extent, y faces over the interior z,
+// x faces over the interior y-z), x fastest, 32-bit indices.
+__global__ void k_periodic_shell(BlockK b, int nv, int D, int fields) {
+  const int nd = b.ndim;
+  const int n0 = b.n[0], n1 = nd > 1 ? b.n[1] : 1, n2 = nd > 2 ? b.n[2] : 1;
+  const int e0 = n0 + 2 * D, e1 = nd > 1 ? n1 + 2 * D : 1;
+  const int cz = nd > 2 ? 2 * D * e1 * e0 : 0;
+  const int cy = nd > 1 ? n2 * 2 * D * e0 : 0;
+  const int cx = n2 * n1 * 2 * D;
+  const int total = cz + cy + cx;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+    int x, y = 0, z = 0;
+    if (t < cz) {
+      x = t % e0 - D;
+      const int r = t / e0;
+      y = r % e1 - D;
+      const int zz = r / e1;
+      z = zz < D ? zz - D : n2 + zz - D;
+    } else if (t < cz + cy) {
+      const int u = t - cz;
+      x = u % e0 - D;
+      const int r = u / e0;
+      const int yy = r % (2 * D);
+      y = yy < D ? yy - D : n1 + yy - D;
+      z = r / (2 * D);
+    } else {
+      const int u = t - cz - cy;
+      const int xx = u % (2 * D);
+      x = xx < D ? xx - D : n0 + xx - D;
+      const int r = u / (2 * D);
+      y = r % n1;
+      z = r / n1;
+    }
+    const int sx = x < 0 ? x + n0 : (x >= n0 ? x - n0 : x);
+    const int sy = y < 0 ? y + n1 : (y >= n1 ? y - n1 : y);
+    const int sz = z < 0 ? z + n2 : (z >= n2 ? z - n2 : z);
+    const int di = lin(b, x, y, z), si = lin(b, sx, sy, sz);
+    if (fields & BC_Q) {
+      double vq[5];
+      for (int v = 0; v < nv; ++v) vq[v] = b.q[v][si];
+      for (int v = 0; v < nv; ++v) b.q[v][di] = vq[v];
+    }
+    if ((fields & BC_QF) && b.qf[0]) {
+      float vf[5];
+      for (int v = 0; v < nv; ++v) vf[v] = b.qf[v][si];
+      for (int v = 0; v < nv; ++v) b.qf[v][di] = vf[v];
+    }
+  }
+}
+
+// Depth of a block whose faces are all periodic with one depth D not above any of its
+// extents (so one wrap lands in the interior), else 0.
+static int uniform_periodic_depth(const Block& bl) {
+  int D = 0;
+  for (int d = 0; d < bl.d.ndim; ++d)
+    for (int side = 0; side < 2; ++side) {
+      if (bl.d.bc[d][side] != OSB_BC_PERIODIC) return 0;
+      const int dep = bl.d.bc_depth[d][side] > 0 ? bl.d.bc_depth[d][side] : 4;
+      if (D == 0) D = dep;
+      else if (dep != D) return 0;
+    }
+  for (int d = 0; d < bl.d.ndim; ++d)
+    if (bl.k.n[d] < D) return 0;
+  return D;
+}
+
 // Zero-gradient outlet (zero_gradient_outlet.py:11-23 as generated): on side 0,
 // q(0) = q(1) then q(-m) = q(m) for m = 1..depth; mirrored on side 1.  Over the interior
 // extent of the other directions.
@@ -523,6 +593,19 @@ int apply_bc(osb_ctx* c, int fields = BC_BOTH) {
   for (size_t ib = 0; ib < c->blocks.size(); ++ib) {
     Block& bl = c->blocks[ib];
     const int nv = bl.d.ndim + 2;
+    if (const int D = uniform_periodic_depth(bl)) {
+      // all faces periodic: the whole halo shell in one launch
+      long shell = 1, inner = 1;
+      for (int e = 0; e < bl.d.ndim; ++e) {
+        shell *= bl.k.n[e] + 2 * D;
+        inner *= bl.k.n[e];
+      }
+      timing_begin(c, FAM_BC);
+      k_periodic_shell<<<grid_for(c, shell - inner, 256), 256, 0, c->stream>>>(bl.k, nv, D, fields);
+      timing_end(c);
+      c->launches++;
+      continue;
+    }
     for (int d = 0; d < bl.d.ndim; ++d) {
       int b0 = bl.d.bc[d][0], b1 = bl.d.bc[d][1];
       int dep0 = bl.d.bc_depth[d][0] > 0 ? bl.d.bc_depth[d][0] : 4;
