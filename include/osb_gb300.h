@@ -64,6 +64,14 @@ extern "C" {
 #define OSB_BC_EXTRAP0 3     /* ExtrapolationBC order 0 (extrapolation.py:29-38), halo fill only */
 #define OSB_BC_EXTRAP1 4     /* ExtrapolationBC order 1 (extrapolation.py:39-53), halo fill only */
 
+/* Convective split form of OSB_SCHEME_CENTRAL4 (physical_models/split_forms.py). */
+#define OSB_SPLIT_FEIEREISEN 0 /* skew-symmetric form, split_forms.py:111-145 */
+#define OSB_SPLIT_KGP 1        /* Kennedy-Gruber-Pirozzoli form, split_forms.py:178-236 */
+
+/* Filter applied after every full RK step (filters/WENO_filter.py). */
+#define OSB_FILTER_NONE 0
+#define OSB_FILTER_WENO3 1     /* non-linear characteristic WENO3-Z filter with a Ducros sensor */
+
 /* Residual precision (per context). */
 #define OSB_PREC_FP64 0          /* plain FP64 path, parity with the generated solver */
 #define OSB_PREC_FP32_RESIDUAL 1 /* FP32 residual arithmetic, FP64 state/RK/reductions */
@@ -108,6 +116,10 @@ typedef struct osb_block_desc {
   double* q[5];              /* conserved variables rho, rhou0.., rhoE (device, OPS layout) */
   double* rkold[5];          /* RK register (device, OPS layout) */
   const double* metric[10];  /* curvilinear: D00 D01 D02 D10 D11 D12 D20 D21 D22 detJ, or NULL */
+  int32_t split_form;        /* OSB_SPLIT_* (central scheme only; 0 = Feiereisen) */
+  int32_t filter;            /* OSB_FILTER_* (3D central scheme only; 0 = none) */
+  double ducros_check;       /* filter flux where max kappa over the interface stencil > this */
+  double ducros_select;      /* filter applied where max kappa around the point >= this */
 } osb_block_desc;
 
 /* ---- library / context ------------------------------------------------------------- */
@@ -232,7 +244,8 @@ int osb_get_stream(osb_ctx* ctx, void** stream);
 int osb_stage_noalloc(const osb_block_desc* desc, int rk_kind, double A, double B, double dt, void* stream);
 
 /* Binding check: writes sizeof(osb_block_desc) and the byte offsets of size, bc, iface, gama,
- * delta, q, rkold and metric into out[0..8] (n >= 9).  Needs no GPU. */
+ * delta, q, rkold, metric, split_form and ducros_check into out[0..10] (n >= 11).  Needs no
+ * GPU. */
 int osb_desc_layout(long long* out, int n);
 
 #ifdef __cplusplus

@@ -34,6 +34,10 @@ BC_ZERO_GRAD = 1
 BC_INTERFACE = 2
 BC_EXTRAP0 = 3
 BC_EXTRAP1 = 4
+SPLIT_FEIEREISEN = 0
+SPLIT_KGP = 1
+FILTER_NONE = 0
+FILTER_WENO3 = 1
 
 PREC_FP64 = 0
 PREC_FP32_RESIDUAL = 1
@@ -94,13 +98,18 @@ class BlockDesc(ctypes.Structure):
         ("q", ctypes.c_void_p * 5),
         ("rkold", ctypes.c_void_p * 5),
         ("metric", ctypes.c_void_p * 10),
+        ("split_form", ctypes.c_int32),
+        ("filter", ctypes.c_int32),
+        ("ducros_check", ctypes.c_double),
+        ("ducros_select", ctypes.c_double),
     ]
 
 
 def layout_signature():
     """(sizeof, offsets...) of BlockDesc, compared with the C side in the tests."""
     offs = [BlockDesc.size.offset, BlockDesc.bc.offset, BlockDesc.iface.offset, BlockDesc.gama.offset,
-            BlockDesc.delta.offset, BlockDesc.q.offset, BlockDesc.rkold.offset, BlockDesc.metric.offset]
+            BlockDesc.delta.offset, BlockDesc.q.offset, BlockDesc.rkold.offset, BlockDesc.metric.offset,
+            BlockDesc.split_form.offset, BlockDesc.ducros_check.offset]
     return [ctypes.sizeof(BlockDesc)] + offs
 
 
@@ -131,6 +140,10 @@ def make_desc(spec, q_ptrs, rk_ptrs, metric_ptrs=None):
     d.eps = spec.eps
     d.teno_ct = spec.teno_ct
     d.shock_filter_control = spec.shock_filter_control
+    d.split_form = spec.split_form
+    d.filter = spec.filter
+    d.ducros_check = spec.ducros_check
+    d.ducros_select = spec.ducros_select
     for v, p in enumerate(q_ptrs):
         d.q[v] = p
     for v, p in enumerate(rk_ptrs):

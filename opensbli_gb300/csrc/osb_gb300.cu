@@ -824,7 +824,7 @@ int osb_last_error(char* buf, size_t n) {
 }
 
 int osb_desc_layout(long long* out, int n) {
-  if (!out || n < 9) return fail(OSB_EINVAL, "need 9 slots");
+  if (!out || n < 11) return fail(OSB_EINVAL, "need 11 slots");
   out[0] = sizeof(osb_block_desc);
   out[1] = offsetof(osb_block_desc, size);
   out[2] = offsetof(osb_block_desc, bc);
@@ -834,6 +834,8 @@ int osb_desc_layout(long long* out, int n) {
   out[6] = offsetof(osb_block_desc, q);
   out[7] = offsetof(osb_block_desc, rkold);
   out[8] = offsetof(osb_block_desc, metric);
+  out[9] = offsetof(osb_block_desc, split_form);
+  out[10] = offsetof(osb_block_desc, ducros_check);
   return OSB_OK;
 }
 

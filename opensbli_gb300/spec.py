@@ -35,6 +35,10 @@ class BlockSpec:
     shock_filter_control: float = 1.0
     delta: Tuple[float, ...] = (1.0, 1.0, 1.0)
     halo: int = HALO
+    split_form: int = abi.SPLIT_FEIEREISEN
+    filter: int = abi.FILTER_NONE
+    ducros_check: float = 0.05
+    ducros_select: float = 0.05
 
     def __post_init__(self):
         self.size = tuple(int(s) for s in self.size)
@@ -76,8 +80,8 @@ class BlockSpec:
         return idx.reshape(shp)
 
     def same_discretisation(self, other):
-        return (self.ndim, self.scheme, self.averaging, self.viscous) == (
-            other.ndim, other.scheme, other.averaging, other.viscous)
+        return (self.ndim, self.scheme, self.averaging, self.viscous, self.split_form, self.filter) == (
+            other.ndim, other.scheme, other.averaging, other.viscous, other.split_form, other.filter)
 
 
 def empty_state(spec):

@@ -56,6 +56,7 @@ def oracle():
         lib.oracle_step.argtypes = [P(abi.BlockDesc), ctypes.c_int, ctypes.c_int, ctypes.c_int, P(ctypes.c_double),
                                     P(ctypes.c_double), ctypes.c_double, ctypes.c_int]
         lib.oracle_reduce.argtypes = [P(abi.BlockDesc), ctypes.c_int, ctypes.c_int, P(ctypes.c_double)]
+        lib.oracle_filter.argtypes = [P(abi.BlockDesc), ctypes.c_int, ctypes.c_double]
         _olib = lib
     return _olib
 
@@ -106,6 +107,10 @@ class OracleBlocks:
         Bb = (ctypes.c_double * len(B))(*B)
         oracle().oracle_step(self.desc, len(self.specs), rk_kind, len(A), Aa, Bb, dt, nsteps)
 
+    def filter(self, dt):
+        """The WENO filter step of the filtered blocks (halos must be filled)."""
+        oracle().oracle_filter(self.desc, len(self.specs), dt)
+
     def reduce(self, what):
         out = ctypes.c_double()
         oracle().oracle_reduce(self.desc, len(self.specs), what, ctypes.byref(out))
@@ -139,15 +144,19 @@ def build_ref(case, force=False, fast=False):
 SHIPPED_TENO6 = os.path.join("apps", "performance_benchmark", "TENO6")
 
 
-def build_shipped_teno6(reference=None, force=False):
-    """Compile the reference's shipped TENO6 benchmark solver (bit-exact generated code, from
-    where it lies in the reference checkout) against ops_compat.h into oracle/_ref/bench_teno6.
+SHIPPED = {"teno6": SHIPPED_TENO6, "c4w5": os.path.join("apps", "performance_benchmark", "Central4-WENO5")}
+
+
+def build_shipped(name, reference=None, force=False):
+    """Compile one of the reference's shipped performance-benchmark solvers (bit-exact
+    generated code, from where it lies in the reference checkout: TENO6 or Central4-WENO5)
+    against ops_compat.h into oracle/_ref/bench_<name>.
     -O1: at -O2 the benchmark's own out-of-bounds read of its run-mode string (see
     shipped_compat.h) is miscompiled; the floating-point semantics are the same (no FMA
     contraction, no fast math)."""
     reference = reference or os.environ.get("OSB_REFERENCE", "/root/reference")
-    src_dir = os.path.join(reference, SHIPPED_TENO6)
-    out_dir = os.path.join(REF, "bench_teno6")
+    src_dir = os.path.join(reference, SHIPPED[name])
+    out_dir = os.path.join(REF, "bench_" + name)
     exe = os.path.join(out_dir, "ref_case")
     if not force and os.path.exists(exe):
         return exe
@@ -161,20 +170,37 @@ def build_shipped_teno6(reference=None, force=False):
     return exe
 
 
-def run_shipped_teno6(n, iters, stop_after_rk=None, timeout=3600):
-    """Run the shipped TENO6 benchmark in its strong-scaling mode (n^3 points, dt =
-    0.00084625 * 256 / n) and return its dumped arrays."""
-    exe = build_shipped_teno6()
+def build_shipped_teno6(reference=None, force=False):
+    return build_shipped("teno6", reference, force)
+
+
+def run_shipped(name, n, iters, stop_after_rk=None, init=None, timeout=3600):
+    """Run a shipped benchmark in its strong-scaling mode (n^3 points, dt =
+    0.00084625 * 256 / n) and return its dumped arrays (at exit, or after stop_after_rk RK
+    updates).  init: optional {dat_name: array} loaded right before the time loop.  The input
+    line carries five tokens: the run-mode string is read into 2 bytes, and a sixth (HDF5)
+    token would land in the byte after it."""
+    exe = build_shipped(name)
     with tempfile.TemporaryDirectory() as td:
         with open(os.path.join(td, "input"), "w") as f:
-            f.write("ss %d %d 1 0\n" % (n, iters))  # the run-mode string is read into 2 bytes
+            f.write("ss %d %d 1 0\n" % (n, iters))
         e = dict(os.environ)
         e["OSB_QUIET"] = "1"
         e["OSB_DUMP_DIR"] = td
         if stop_after_rk is not None:
             e["OSB_STOP_AFTER_RK"] = str(stop_after_rk)
+        if init:
+            idir = os.path.join(td, "init")
+            os.makedirs(idir)
+            for k, a in init.items():
+                write_dump(os.path.join(idir, k + ".bin"), a)
+            e["OSB_INIT_DIR"] = idir
         subprocess.run([exe], env=e, cwd=td, check=True, timeout=timeout, stdout=subprocess.DEVNULL)
         return {fn[:-4]: read_dump(os.path.join(td, fn)) for fn in os.listdir(td) if fn.endswith(".bin")}
+
+
+def run_shipped_teno6(n, iters, stop_after_rk=None, timeout=3600):
+    return run_shipped("teno6", n, iters, stop_after_rk=stop_after_rk, timeout=timeout)
 
 
 def read_dump(path):

@@ -88,9 +88,41 @@ def make_shipped_teno6(n=12, counts=(1, 3, 15)):
     print("wrote shipped_teno6_%d" % n)
 
 
+def c4w5_spec(n):
+    """The Central4-WENO5 benchmark's block: supersonic TGV, central-4 KGP convective terms,
+    Sutherland viscosity, WENO3 filter with Ducros_check = Ducros_select = 0.05."""
+    spec, q = problems.tgv(n, minf=1.25, scheme=abi.SCHEME_CENTRAL4, viscous=abi.VISC_SUTHERLAND)
+    spec.split_form = abi.SPLIT_KGP
+    spec.filter = abi.FILTER_WENO3
+    spec.ducros_check = 0.05
+    spec.ducros_select = 0.05
+    return spec, q
+
+
+def make_shipped_c4w5(n=16, steps=(1, 2, 5)):
+    """Golden states from the reference's shipped Central4-WENO5 benchmark solver itself
+    (bit-exact generated code, apps/performance_benchmark/Central4-WENO5), strong-scaling mode
+    at n^3, dumped at exit after whole filtered steps; also the filter mask of the first step."""
+    spec, q = c4w5_spec(n)
+    names = harness.state_names(3)
+    sl = spec.interior()
+    out = {"dt": 0.00084625 * 256 / n, "steps": np.array(steps)}
+    for c in steps:
+        r = harness.run_shipped("c4w5", n, c)
+        out["after_%d" % c] = np.stack([r[nm][sl] for nm in names])
+        if c == 1:
+            out["mask_1"] = r["WENO_filter_B0"][sl]
+            out["kappa_1"] = r["kappa_B0"][sl]
+    np.savez_compressed(os.path.join(HERE, "shipped_c4w5_%d.npz" % n), **out)
+    print("wrote shipped_c4w5_%d" % n)
+
+
 def main():
     if sys.argv[1:] == ["shipped_teno6"]:
         make_shipped_teno6()
+        return
+    if sys.argv[1:] == ["shipped_c4w5"]:
+        make_shipped_c4w5()
         return
     missing = sorted({c for c in harness_cases() if not harness.ref_available(c)})
     if missing:

@@ -26,8 +26,8 @@ def test_library_exports_every_symbol(built_lib):
 
 def test_descriptor_layout(built_lib):
     lib = abi.load_library()
-    out = (ctypes.c_longlong * 9)()
-    assert lib.osb_desc_layout(out, 9) == 0
+    out = (ctypes.c_longlong * 11)()
+    assert lib.osb_desc_layout(out, 11) == 0
     assert list(out) == abi.layout_signature()
 
 
