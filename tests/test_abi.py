@@ -35,4 +35,4 @@ def test_version_and_errors(built_lib):
     lib = abi.load_library()
     assert lib.osb_version() == 100
     assert lib.osb_desc_layout(None, 0) == abi.OSB_EINVAL
-    assert "9 slots" in abi.last_error(lib)
+    assert "11 slots" in abi.last_error(lib)
