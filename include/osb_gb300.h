@@ -214,7 +214,7 @@ int osb_get_schedule(osb_ctx* ctx, int* mode_out, osb_schedule* sched_out);
 int osb_timing(osb_ctx* ctx, int enable);
 
 /* Writes accumulated milliseconds and launch counts per kernel family (0 flux-x, 1 flux-y,
- * 2 flux-z, 3 central, 4 RK update, 5 boundaries, 6 reductions, 7 persistent stage) into
+ * 2 flux-z, 3 central, 4 RK update, 5 boundaries, 6 reductions, 7 persistent stage, 8 filter) into
  * ms[0..n) / launches[0..n) and resets them. */
 int osb_timing_report(osb_ctx* ctx, double* ms, long long* launches, int n);
 

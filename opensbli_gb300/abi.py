@@ -224,4 +224,5 @@ EXPORTED = ["osb_version", "osb_last_error", "osb_ctx_create", "osb_ctx_destroy"
 
 NOALLOC_MAX_DOUBLES = 4 * 1024 * 1024
 
-KERNEL_FAMILIES = ["flux_x", "flux_y", "flux_z", "central", "rk_update", "boundary", "reduce", "persistent_stage"]
+KERNEL_FAMILIES = ["flux_x", "flux_y", "flux_z", "central", "rk_update", "boundary", "reduce", "persistent_stage",
+                   "filter"]

@@ -29,6 +29,8 @@ UNITS = [
     ("central_f64", "osb_central.cu", ["-DOSB_CENTRAL_T=double", "-DOSB_CENTRAL_NAME=central_f64"]),
     ("central_f32", "osb_central.cu", ["-DOSB_CENTRAL_T=float", "-DOSB_CENTRAL_NAME=central_f32"] + FAST),
     ("batch", "osb_batch.cu", FAST),
+    ("filter_f64", "osb_filter.cu", ["-DOSB_FILTER_T=double", "-DOSB_FILTER_NAME=filter_f64"]),
+    ("filter_f32", "osb_filter.cu", ["-DOSB_FILTER_T=float", "-DOSB_FILTER_NAME=filter_f32"] + FAST),
 ] + [
     ("flux_%s_%dd" % (p, nd), "osb_flux.cu",
      ["-DOSB_T=%s" % ("double" if p == "f64" else "float"), "-DOSB_ND=%d" % nd, "-DOSB_NAME=flux_%s_%dd" % (p, nd)]

@@ -5,7 +5,7 @@
 namespace osb {
 namespace {
 
-template <typename T, bool CONV, int VISC, bool FUSE>
+template <typename T, int CONV, int VISC, bool FUSE>
 int launch_central_k(osb_ctx* c, Block& bl, int first, const RkFuse& rf) {
   using Fd = CentralFields<T, CONV, VISC>;
   size_t smem = (size_t)Fd::N * CRING * CPL * sizeof(T);
@@ -45,7 +45,7 @@ int launch_central_k(osb_ctx* c, Block& bl, int first, const RkFuse& rf) {
 }
 
 // With rf (FP32 path) the kernel applies the RK update instead of storing the residual.
-template <typename T, bool CONV, int VISC>
+template <typename T, int CONV, int VISC>
 int launch_central_t(osb_ctx* c, Block& bl, int first, const RkFuse* rf) {
   if constexpr (sizeof(T) == 4) {
     if (rf) return launch_central_k<T, CONV, VISC, true>(c, bl, first, *rf);
@@ -56,13 +56,18 @@ int launch_central_t(osb_ctx* c, Block& bl, int first, const RkFuse* rf) {
 template <typename T>
 int launch_central(osb_ctx* c, Block& bl, bool conv, int first, const RkFuse* rf) {
   const int visc = bl.d.viscous;
-  if (conv) {
-    if (visc == OSB_VISC_SUTHERLAND) return launch_central_t<T, true, 1>(c, bl, first, rf);
-    if (visc == OSB_VISC_CONSTANT) return launch_central_t<T, true, 2>(c, bl, first, rf);
-    return launch_central_t<T, true, 0>(c, bl, first, rf);
+  if (conv && bl.d.split_form == OSB_SPLIT_KGP) {
+    if (visc == OSB_VISC_SUTHERLAND) return launch_central_t<T, 2, 1>(c, bl, first, rf);
+    if (visc == OSB_VISC_CONSTANT) return launch_central_t<T, 2, 2>(c, bl, first, rf);
+    return launch_central_t<T, 2, 0>(c, bl, first, rf);
   }
-  if (visc == OSB_VISC_SUTHERLAND) return launch_central_t<T, false, 1>(c, bl, first, rf);
-  if (visc == OSB_VISC_CONSTANT) return launch_central_t<T, false, 2>(c, bl, first, rf);
+  if (conv) {
+    if (visc == OSB_VISC_SUTHERLAND) return launch_central_t<T, 1, 1>(c, bl, first, rf);
+    if (visc == OSB_VISC_CONSTANT) return launch_central_t<T, 1, 2>(c, bl, first, rf);
+    return launch_central_t<T, 1, 0>(c, bl, first, rf);
+  }
+  if (visc == OSB_VISC_SUTHERLAND) return launch_central_t<T, 0, 1>(c, bl, first, rf);
+  if (visc == OSB_VISC_CONSTANT) return launch_central_t<T, 0, 2>(c, bl, first, rf);
   return OSB_OK;
 }
 

@@ -1,0 +1,369 @@
+// osb_filter.cu -- the non-linear characteristic WENO3 filter applied after every full RK step
+// (filters/WENO_filter.py), as the generated Central4-WENO5 benchmark runs it
+// (apps/performance_benchmark/Central4-WENO5/opensbli.cpp:386-513, kernels 043-049):
+//   1. the filter's own periodic halo exchange (bc_exchanges.h groups 51-56);
+//   2. the Ducros sensor kappa on the interior (kernel 044; its halos stay zero);
+//   3. per direction the filter flux at every interface i+1/2, i = -1..N-1 (kernels 046-048);
+//   4. q += dt * mask * (-sum_d (F_d(i) - F_d(i-1)) / Delta_d), mask = [max kappa over the
+//      point and its neighbours >= Ducros_select] (kernel 049).
+// Compiled once per precision (OSB_FILTER_T).  In the FP32-residual path the filter reads the
+// FP32 state, forms the increment in FP32 and adds it to the FP64 state, then refreshes the
+// FP32 copy of the points it changed.
+#include <algorithm>
+
+#include "osb_internal.h"
+
+#ifndef OSB_FILTER_T
+#define OSB_FILTER_T double
+#define OSB_FILTER_NAME filter_f64
+#endif
+
+namespace osb {
+namespace {
+
+constexpr int FT = 256;  // threads per CTA of the filter kernels
+
+// The exchange before the filter: direction d, both sides (they read and write disjoint
+// points).  Side 0 copies [0, 4) to [N, N+4), side 1 copies [N-4, N) to [-4, 0), over the
+// transverse range [-4, N-4) of the other directions -- the generated iteration range (base
+// -4, extent N); no exchange follows the last RK stage, so the halo points outside that range
+// keep the values of the exchange after the previous stage.
+__global__ void k_filter_halo(BlockK b, int d, int fields) {
+  int ext[3];
+  for (int e = 0; e < 3; ++e) ext[e] = b.n[e];
+  ext[d] = 4;
+  const int per = ext[0] * ext[1] * ext[2];
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < 2 * per; t += gridDim.x * blockDim.x) {
+    const int side = t >= per;
+    const int u = t - side * per;
+    int c[3];
+    c[0] = u % ext[0];
+    c[1] = (u / ext[0]) % ext[1];
+    c[2] = u / (ext[0] * ext[1]);
+    int src[3], dst[3];
+    for (int e = 0; e < 3; ++e) src[e] = dst[e] = c[e] - 4;
+    if (side == 0) {
+      src[d] = c[d];
+      dst[d] = b.n[d] + c[d];
+    } else {
+      src[d] = b.n[d] - 4 + c[d];
+      dst[d] = c[d] - 4;
+    }
+    const int si = lin(b, src[0], src[1], src[2]), di = lin(b, dst[0], dst[1], dst[2]);
+    if (fields & 1)
+      for (int v = 0; v < 5; ++v) b.q[v][di] = b.q[v][si];
+    if ((fields & 2) && b.qf[0])
+      for (int v = 0; v < 5; ++v) b.qf[v][di] = b.qf[v][si];
+  }
+}
+
+// FP32 path: the last RK stage wrote the other buffer of the FP32 ping-pong pair, whose halo
+// shell still holds the state two stages back; the halos the generated step leaves before the
+// filter are those of the exchange after the previous stage, which the buffer that stage read
+// holds.  Copies that shell (depth D, the block's exchange depth) into the current buffer.
+__global__ void k_shell_from(BlockK b, const float* __restrict__ src, int D) {
+  const int n0 = b.n[0], n1 = b.n[1], n2 = b.n[2];
+  const int e0 = n0 + 2 * D, e1 = n1 + 2 * D, e2 = n2 + 2 * D;
+  const int total = e0 * e1 * e2;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+    const int x = t % e0 - D, y = (t / e0) % e1 - D, z = t / (e0 * e1) - D;
+    if (x >= 0 && x < n0 && y >= 0 && y < n1 && z >= 0 && z < n2) continue;
+    const int id = lin(b, x, y, z);
+    for (int v = 0; v < 5; ++v) b.qf[v][id] = src[(size_t)v * b.alloc + id];
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ T vel(const BlockK& b, int i, int id) {
+  return ld_q<T>(b, 1 + i, id) / ld_q<T>(b, 0, id);
+}
+
+// Ducros sensor (kernel 044): (div u)^2 (1/2 - 1/2 tanh(2.5 + 500 div u / |Delta|)) /
+// (1e-40 + |curl u|^2 + (div u)^2), central-4 derivatives.  FP32: the 1e-40 (below the FP32
+// normal range) becomes 1e-30.
+template <typename T>
+__global__ void k_ducros(BlockK b, T* kappa, T inv_h) {
+  const int n0 = b.n[0], n1 = b.n[1], n2 = b.n[2];
+  const int total = n0 * n1 * n2;
+  const T id[3] = {(T)b.invd[0], (T)b.invd[1], (T)b.invd[2]};
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+    const int x = t % n0, y = (t / n0) % n1, z = t / (n0 * n1);
+    const int c = lin(b, x, y, z);
+    T du[3][3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const int s = b.st[j];
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+        du[i][j] = (-L_(2.0 / 3.0) * vel<T>(b, i, c - s) - L_(1.0 / 12.0) * vel<T>(b, i, c + 2 * s) +
+                    L_(1.0 / 12.0) * vel<T>(b, i, c - 2 * s) + L_(2.0 / 3.0) * vel<T>(b, i, c + s)) *
+                   id[j];
+    }
+    const T div = du[0][0] + du[1][1] + du[2][2];
+    const T wz = -du[0][1] + du[1][0], wx = -du[1][2] + du[2][1], wy = -du[2][0] + du[0][2];
+    const T tiny = sizeof(T) == 8 ? L_(1.0e-40) : L_(1.0e-30);
+    kappa[c] = (div * div) * (L_(0.5) - L_(0.5) * tanh(L_(2.5) + L_(500.0) * div * inv_h)) /
+               (tiny + wz * wz + wx * wx + wy * wy + div * div);
+  }
+}
+
+// One side of the WENO3-Z filter reconstruction of a wave: f = the split flux at points
+// i-1..i+2, side + uses {i-1, i, i+1}, side - {i, i+1, i+2}.  Returns the side's
+// contribution to the reconstruction; rj receives its smoothness-sensor term.
+// Smoothness of the two-point stencil {lo, hi} (hi = the higher index), as generated:
+// 1/4 hi^2 + 1/2 (1/2 lo - hi) lo.
+template <typename T>
+__device__ __forceinline__ T beta2(T lo, T hi) {
+  return L_(0.25) * (hi * hi) + L_(0.5) * (L_(0.5) * lo - hi) * lo;
+}
+
+template <typename T, int SIDE>
+__device__ __forceinline__ T weno3_side(const T (&f)[4], T eps32, T& rj) {
+  // stencil values in the side's own order: a = far-upwind, b = centre, c = downwind
+  const T a = SIDE > 0 ? f[0] : f[3], bb = SIDE > 0 ? f[1] : f[2], cc = SIDE > 0 ? f[2] : f[1];
+  const T bd = beta2<T>(f[1], f[2]);                                       // downwind pair {i, i+1}
+  const T bu = SIDE > 0 ? beta2<T>(f[0], f[1]) : beta2<T>(f[2], f[3]);     // upwind pair
+  T ad, au;
+  if (sizeof(T) == 8) {
+    const T t = fabs(bu - bd) * fabs(bu - bd);
+    ad = L_(0.666666666666667) + L_(2.0 / 3.0) * t / ((L_(1.0e-40) + bd) * (L_(1.0e-40) + bd));
+    au = L_(0.333333333333333) + L_(1.0 / 3.0) * t / ((L_(1.0e-40) + bu) * (L_(1.0e-40) + bu));
+  } else {
+    // FP32: epsilon relative to the stencil, and the ratio squared after the division (no
+    // underflow of (eps + beta)^2)
+    const T tau = fabs(bu - bd);
+    const T rd = tau / (eps32 + bd), ru = tau / (eps32 + bu);
+    ad = L_(2.0 / 3.0) * (L_(1.0) + rd * rd);
+    au = L_(1.0 / 3.0) * (L_(1.0) + ru * ru);
+  }
+  const T ia = L_(1.0) / (ad + au);
+  const T wd = ad * ia, wu = au * ia;
+  rj = L_(0.333333333333333) * fabs(-L_(1.0) + L_(3.0) * wu) + L_(0.333333333333333) * fabs(-L_(1.0) + L_(1.5) * wd);
+  return (-L_(0.25) * a + L_(0.75) * bb) * wu + (L_(0.25) * bb + L_(0.25) * cc) * wd;
+}
+
+// Filter flux at interface i+1/2 along direction D (local frame: w[m] = point i-1+m, normal
+// momentum first), kernels 046-048: Roe average of points i, i+1, characteristic projections
+// of Q and F, per wave the WENO3-Z reconstruction of CF +/- lambda CS (both sides) minus the
+// central 4th-order interpolation of CF, scaled by rj, back-projected with the REV columns.
+template <typename T>
+__device__ __forceinline__ void filter_flux(const Pt<T, 3> (&w)[4], const SP<T>& sp, T (&fh)[5]) {
+  constexpr int ND = 3, NV = 5;
+  const T g1 = sp.g1;
+  const Pt<T, 3>& L = w[1];
+  const Pt<T, 3>& R = w[2];
+  const T sL = sqrt(L.q[0]), sR = sqrt(R.q[0]);
+  const T rho = sqrt(L.q[0] * R.q[0]);
+  const T inv = L_(1.0) / (sL + sR);
+  T u[ND], ke = L_(0.0);
+#pragma unroll
+  for (int i = 0; i < ND; ++i) {
+    u[i] = (sL * L.u[i] + sR * R.u[i]) * inv;
+    ke += u[i] * u[i];
+  }
+  const T a = sqrt((-L_(0.5) * ke + ((L.p + L.q[NV - 1]) / sL + (R.p + R.q[NV - 1]) / sR) * inv) * g1);
+  const T sfc = sp.sfc;
+  const T lam_u = sfc * fmax(fabs(R.u[0]), fabs(L.u[0]));
+  const T lam_p = sfc * fmax(fabs(R.u[0] + R.a), fabs(L.u[0] + L.a));
+  const T lam_m = sfc * fmax(fabs(R.u[0] - R.a), fabs(L.u[0] - L.a));
+  const T ia = L_(1.0) / a, ia2 = ia * ia, irho = L_(1.0) / rho;
+  const T phi = g1 * L_(0.5) * ke;
+  const T bta = ia * irho * L_(0.70710678118654752440);
+  const T alf = rho * ia * L_(0.70710678118654752440);
+  T cs[NV][4], cf[NV][4];
+#pragma unroll
+  for (int m = 0; m < 4; ++m) {
+    const Pt<T, 3>& s = w[m];
+    T Fv[NV];
+    Fv[0] = s.q[1];
+    Fv[1] = s.u[0] * s.q[1] + s.p;
+    Fv[2] = s.u[0] * s.q[2];
+    Fv[3] = s.u[0] * s.q[3];
+    Fv[4] = s.u[0] * (s.q[4] + s.p);
+    T o2[2][NV];
+    constexpr int NPASS = sizeof(T) == 4 ? 1 : 2;
+#pragma unroll
+    for (int pass = 0; pass < NPASS; ++pass) {
+      const T* v = pass == 0 ? s.q : Fv;
+      T* o = o2[pass];
+      const T um = u[0] * v[1] + u[1] * v[2] + u[2] * v[3];
+      const T S = phi * v[0] - g1 * um + g1 * v[4];
+      const T D = v[1] - u[0] * v[0];
+      o[0] = v[0] - S * ia2;
+      o[1] = (v[3] - u[2] * v[0]) * irho;
+      o[2] = (u[1] * v[0] - v[2]) * irho;
+      o[3] = bta * (S + a * D);
+      o[4] = bta * (S - a * D);
+    }
+    if (NPASS == 1) {
+      // FP32: L.F = u_n (L.q) + p (L e_1 + u_n L e_E), the two LEV columns in closed form
+      const T un = s.u[0], du = un - u[0];
+      const T pb = s.p * bta, gd = g1 * du;
+      o2[1][0] = un * o2[0][0] - s.p * g1 * ia2 * du;
+      o2[1][1] = un * o2[0][1];
+      o2[1][2] = un * o2[0][2];
+      o2[1][3] = un * o2[0][3] + pb * (a + gd);
+      o2[1][4] = un * o2[0][4] + pb * (gd - a);
+    }
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      cs[k][m] = o2[0][k];
+      cf[k][m] = o2[1][k];  // pass 1 (FP64) or the closed form (FP32)
+    }
+  }
+  T rec[NV];
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    const T lk = k < ND ? lam_u : (k == ND ? lam_p : lam_m);
+    T fp[4], fm[4];
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+      fp[m] = cs[k][m] * lk + cf[k][m];
+      fm[m] = -cs[k][m] * lk + cf[k][m];
+    }
+    T eps32 = L_(0.0);
+    if (sizeof(T) == 4) {
+      const T ms = (cf[k][0] * cf[k][0] + cf[k][1] * cf[k][1] + cf[k][2] * cf[k][2] + cf[k][3] * cf[k][3] +
+                    cs[k][1] * cs[k][1] * lk * lk) * L_(0.25);
+      eps32 = sp.eps32_rel * ms + L_(1e-30);
+    }
+    T rp, rm;
+    const T rcp = weno3_side<T, 1>(fp, eps32, rp);
+    const T rcm = weno3_side<T, -1>(fm, eps32, rm);
+    const T rj = fmax(rp, rm);
+    rec[k] = (L_(1.0 / 12.0) * (-L_(7.0) * cf[k][1] - L_(7.0) * cf[k][2] + cf[k][0] + cf[k][3]) + (rcm + rcp)) * rj;
+  }
+  const T rp = rec[3] + rec[4], rmn = rec[3] - rec[4];
+  const T F0 = rec[0] + alf * rp;
+  fh[0] = F0;
+  fh[1] = u[0] * F0 + alf * a * rmn;
+  fh[2] = u[1] * F0 - rho * rec[2];
+  fh[3] = u[2] * F0 + rho * rec[1];
+  const T h0 = (phi + a * a) / g1;
+  fh[4] = phi / g1 * rec[0] + rho * u[2] * rec[1] - rho * u[1] * rec[2] + alf * h0 * rp + alf * u[0] * a * rmn;
+}
+
+// Filter fluxes along D at interfaces i+1/2, i = -1..N-1, transverse interior; F[v] at the
+// index of point i.  Interfaces whose stencil i-3..i+2 sees no kappa above Ducros_check get 0.
+template <typename T, int D>
+__global__ void k_filter_flux(BlockK b, SchemeParams spd, const T* __restrict__ kappa, T check, T* F0, T* F1, T* F2,
+                              T* F3, T* F4) {
+  const SP<T> sp(spd);
+  int e[3] = {b.n[0], b.n[1], b.n[2]};
+  e[D] += 1;
+  const int total = e[0] * e[1] * e[2];
+  const int s = b.st[D];
+  T* F[5] = {F0, F1, F2, F3, F4};
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+    int c[3] = {t % e[0], (t / e[0]) % e[1], t / (e[0] * e[1])};
+    c[D] -= 1;
+    const int id = lin(b, c[0], c[1], c[2]);
+    T km = kappa[id - 3 * s];
+#pragma unroll
+    for (int m = -2; m <= 2; ++m) km = fmax(km, kappa[id + m * s]);
+    T fh[5] = {L_(0.0), L_(0.0), L_(0.0), L_(0.0), L_(0.0)};
+    if (km > check) {
+      Pt<T, 3> w[4];
+#pragma unroll
+      for (int m = 0; m < 4; ++m) {
+        const int pid = id + (m - 1) * s;
+#pragma unroll
+        for (int lv = 0; lv < 5; ++lv) w[m].q[lv] = ld_q<T>(b, gvar_fwd<3, D>(lv), pid);
+        make_pt<T, 3>(w[m], sp.gama);
+      }
+      filter_flux<T>(w, sp, fh);
+    }
+#pragma unroll
+    for (int lv = 0; lv < 5; ++lv) F[gvar_fwd<3, D>(lv)][id] = fh[lv];
+  }
+}
+
+// q += dt * mask * (-(F_0(i) - F_0(i-1)) / Delta_0 - (F_2 ...) / Delta_2 - (F_1 ...) / Delta_1)
+// on the interior, in the generated operation order (kernel 049).  FP32: the increment is
+// formed in FP32 and added to the FP64 state; the FP32 copy of a changed point is refreshed.
+template <typename T>
+struct FilterFluxes {
+  const T* f[15];  // direction-major: F_d of variable v at f[5 d + v]
+};
+
+template <typename T>
+__global__ void k_filter_apply(BlockK b, const T* __restrict__ kappa, FilterFluxes<T> F, double dt, T select) {
+  const int n0 = b.n[0], n1 = b.n[1], n2 = b.n[2];
+  const int total = n0 * n1 * n2;
+  const int sx = b.st[0], sy = b.st[1], sz = b.st[2];
+  const T i0 = (T)b.invd[0], i1 = (T)b.invd[1], i2 = (T)b.invd[2];
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+    const int x = t % n0, y = (t / n0) % n1, z = t / (n0 * n1);
+    const int c = lin(b, x, y, z);
+    T km = kappa[c];
+    km = fmax(km, kappa[c + sz]);
+    km = fmax(km, kappa[c + 2 * sy]);
+    km = fmax(km, kappa[c + sx]);
+    km = fmax(km, kappa[c - sy]);
+    km = fmax(km, kappa[c - sx]);
+    km = fmax(km, kappa[c + sy]);
+    km = fmax(km, kappa[c + 2 * sz]);
+    km = fmax(km, kappa[c + 2 * sx]);
+    km = fmax(km, kappa[c - sz]);
+    if (!(km >= select)) continue;  // mask 0: the state is unchanged
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      const T* f0 = F.f[v];
+      const T* f1 = F.f[5 + v];
+      const T* f2 = F.f[10 + v];
+      const T inc = -(-f0[c - sx] + f0[c]) * i0 - (-f2[c - sz] + f2[c]) * i2 - (-f1[c - sy] + f1[c]) * i1;
+      if constexpr (sizeof(T) == 8) {
+        b.q[v][c] = inc * dt * 1.0 + b.q[v][c];
+      } else {
+        const double q = __fma_rn(dt, f2d_exact(inc), b.q[v][c]);
+        b.q[v][c] = q;
+        b.qf[v][c] = d2f_rn(q);
+      }
+    }
+  }
+}
+
+template <typename T>
+int filter_t(osb_ctx* c, Block& bl, double dt) {
+  BlockK& k = bl.k;
+  const long n = (long)k.n[0] * k.n[1] * k.n[2];
+  T* base = reinterpret_cast<T*>(bl.filt_ws);
+  T* kappa = base;
+  T* F[15];
+  for (int a = 0; a < 15; ++a) F[a] = base + (size_t)(1 + a) * k.alloc;
+  const int fields = sizeof(T) == 8 ? 1 : 2;
+  timing_begin(c, FAM_FILTER);
+  if (sizeof(T) == 4) {
+    const int D = bl.d.bc_depth[0][0] > 0 ? bl.d.bc_depth[0][0] : 4;
+    const float* prev = c->qf_parity ? bl.qf_base : bl.qf_alt;
+    const long shell = (long)(k.n[0] + 2 * D) * (k.n[1] + 2 * D) * (k.n[2] + 2 * D);
+    k_shell_from<<<grid_for(c, shell, FT), FT, 0, c->stream>>>(k, prev, D);
+    c->launches++;
+  }
+  for (int d = 0; d < 3; ++d) {
+    long per = 8L * (d == 0 ? 1 : k.n[0]) * (d == 1 ? 1 : k.n[1]) * (d == 2 ? 1 : k.n[2]);
+    k_filter_halo<<<grid_for(c, per, FT), FT, 0, c->stream>>>(k, d, fields);
+  }
+  const double h = sqrt(bl.d.delta[0] * bl.d.delta[0] + bl.d.delta[1] * bl.d.delta[1] + bl.d.delta[2] * bl.d.delta[2]);
+  k_ducros<T><<<grid_for(c, n, FT), FT, 0, c->stream>>>(k, kappa, (T)(1.0 / h));
+  SchemeParams sp{bl.d.gama, bl.d.eps, bl.d.teno_ct, bl.d.shock_filter_control, 1e-12};
+  const T check = (T)bl.d.ducros_check;
+  const long nf0 = (long)(k.n[0] + 1) * k.n[1] * k.n[2], nf1 = (long)k.n[0] * (k.n[1] + 1) * k.n[2],
+             nf2 = (long)k.n[0] * k.n[1] * (k.n[2] + 1);
+  k_filter_flux<T, 0><<<grid_for(c, nf0, FT), FT, 0, c->stream>>>(k, sp, kappa, check, F[0], F[1], F[2], F[3], F[4]);
+  k_filter_flux<T, 1><<<grid_for(c, nf1, FT), FT, 0, c->stream>>>(k, sp, kappa, check, F[5], F[6], F[7], F[8], F[9]);
+  k_filter_flux<T, 2><<<grid_for(c, nf2, FT), FT, 0, c->stream>>>(k, sp, kappa, check, F[10], F[11], F[12], F[13],
+                                                                   F[14]);
+  FilterFluxes<T> Fd;
+  for (int a = 0; a < 15; ++a) Fd.f[a] = F[a];
+  k_filter_apply<T><<<grid_for(c, n, FT), FT, 0, c->stream>>>(k, kappa, Fd, dt, (T)bl.d.ducros_select);
+  timing_end(c);
+  c->launches += 8;
+  return OSB_OK;
+}
+
+}  // namespace
+
+int OSB_FILTER_NAME(osb_ctx* c, Block& bl, double dt) { return filter_t<OSB_FILTER_T>(c, bl, dt); }
+
+}  // namespace osb

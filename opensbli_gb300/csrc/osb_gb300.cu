@@ -446,6 +446,12 @@ int fail(int code, const char* fmt, ...) {
   return code;
 }
 
+int grid_for(osb_ctx* c, long n, int threads) {
+  long g = (n + threads - 1) / threads;
+  long cap = (long)c->sm_count * 8;
+  return (int)std::max(1L, std::min(g, cap));
+}
+
 }  // namespace osb
 
 namespace osb {
@@ -535,11 +541,6 @@ int residual(osb_ctx* c, Block& bl) {
                                            : residual_t<double>(c, bl, nullptr, nullptr);
 }
 
-int grid_for(osb_ctx* c, long n, int threads) {
-  long g = (n + threads - 1) / threads;
-  long cap = (long)c->sm_count * 8;
-  return (int)std::max(1L, std::min(g, cap));
-}
 
 // Interface faces of every block: the interior of each face (full = 0) or the face with its
 // transverse halos (full = 1).
@@ -657,7 +658,9 @@ bool use_batch(const osb_ctx* c) {
   return batch_eligible(c, nullptr);
 }
 
-int stage(osb_ctx* c, int s, double dt) {
+// One RK stage of every block; bc = false leaves the boundary treatment after it out (the
+// generated step with a filter exchanges no halos after its last stage).
+int stage(osb_ctx* c, int s, double dt, bool bc = true) {
   if (use_batch(c)) return batch_stage(c, s, dt);
   const int kind = c->rk_kind == OSB_RK_LOW_STORAGE ? 0 : 1;
   if (c->prec == OSB_PREC_FP32_RESIDUAL) {
@@ -689,7 +692,7 @@ int stage(osb_ctx* c, int s, double dt) {
     batch_set_parity(c, c->qf_parity ^ 1);
     // between stages the FP32 kernels read only the FP32 state; the FP64 halos are refreshed
     // when a call returns (osb_step / osb_stage)
-    return apply_bc(c, BC_QF);
+    return bc ? apply_bc(c, BC_QF) : OSB_OK;
   }
   for (auto& bl : c->blocks) {
     int rc = residual(c, bl);
@@ -702,7 +705,13 @@ int stage(osb_ctx* c, int s, double dt) {
     timing_end(c);
     c->launches++;
   }
-  return apply_bc(c);
+  return bc ? apply_bc(c) : OSB_OK;
+}
+
+bool any_filter(const osb_ctx* c) {
+  for (const auto& bl : c->blocks)
+    if (bl.d.filter == OSB_FILTER_WENO3) return true;
+  return false;
 }
 
 // FP32-residual path: refresh the FP32 shadow from the caller's FP64 state (the caller may
@@ -735,10 +744,19 @@ int one_step(osb_ctx* c, double dt) {
       c->launches++;
     }
   }
+  // with a filtered block the last stage exchanges no halos: the filter step's own exchange
+  // follows it (the next step starts with the full exchange)
+  const bool filt = any_filter(c);
   for (int s = 0; s < c->nst; ++s) {
-    rc = stage(c, s, dt);
+    rc = stage(c, s, dt, !(filt && s == c->nst - 1));
     if (rc) return rc;
   }
+  if (filt)
+    for (auto& bl : c->blocks) {
+      if (bl.d.filter != OSB_FILTER_WENO3) continue;
+      rc = c->prec == OSB_PREC_FP32_RESIDUAL ? filter_f32(c, bl, dt) : filter_f64(c, bl, dt);
+      if (rc) return rc;
+    }
   return OSB_OK;
 }
 
@@ -805,6 +823,25 @@ bool check_desc(const osb_block_desc* d, std::string& why) {
       }
       if (f.side != 0 && f.side != 1) { why = "interface side must be 0 or 1"; return false; }
     }
+  if (d->split_form != OSB_SPLIT_FEIEREISEN && d->split_form != OSB_SPLIT_KGP) { why = "unknown split form"; return false; }
+  if (d->split_form == OSB_SPLIT_KGP && d->scheme != OSB_SCHEME_CENTRAL4) {
+    why = "the KGP split form belongs to the central scheme";
+    return false;
+  }
+  if (d->filter != OSB_FILTER_NONE && d->filter != OSB_FILTER_WENO3) { why = "unknown filter"; return false; }
+  if (d->filter == OSB_FILTER_WENO3) {
+    if (d->ndim != 3 || d->scheme != OSB_SCHEME_CENTRAL4 || d->metric[9]) {
+      why = "the WENO filter is implemented for 3D Cartesian blocks of the central scheme";
+      return false;
+    }
+    for (int i = 0; i < 3; ++i)
+      for (int s = 0; s < 2; ++s)
+        if (d->bc[i][s] != OSB_BC_PERIODIC || d->size[i] < 4) {
+          why = "the WENO filter's halo exchange is the periodic one (all faces periodic, >= 4 points)";
+          return false;
+        }
+    if (!(d->ducros_check >= 0.0) || !(d->ducros_select >= 0.0)) { why = "Ducros thresholds must be >= 0"; return false; }
+  }
   return true;
 }
 
@@ -881,6 +918,7 @@ int osb_ctx_destroy(osb_ctx* c) {
     if (bl.qf_base) cudaFree(bl.qf_base);  // k.qf may point at either ping-pong buffer
     if (bl.mf_buf) cudaFree(bl.mf_buf);
     if (bl.qf_alt) cudaFree(bl.qf_alt);
+    if (bl.filt_ws) cudaFree(bl.filt_ws);
   }
   batch_free(c);
   if (c->red) cudaFree(c->red);
@@ -971,6 +1009,19 @@ int osb_block_add(osb_ctx* c, const osb_block_desc* d, int* block_id) {
       c->launches++;
     }
     OSB_CK(cudaGetLastError());
+  }
+  if (d->filter == OSB_FILTER_WENO3) {
+    // kappa (zero halos, written on the interior only) and the 15 filter-flux arrays
+    const size_t bytes = (size_t)16 * k.alloc * (c->prec == OSB_PREC_FP32_RESIDUAL ? sizeof(float) : sizeof(double));
+    cudaError_t e = cudaMalloc(&bl.filt_ws, bytes);
+    if (e != cudaSuccess) {
+      cudaFree(R);
+      if (bl.qf_base) cudaFree(bl.qf_base);
+      if (bl.qf_alt) cudaFree(bl.qf_alt);
+      if (bl.mf_buf) cudaFree(bl.mf_buf);
+      return fail(OSB_ECUDA, "filter workspace: %s", cudaGetErrorString(e));
+    }
+    OSB_CK(cudaMemsetAsync(bl.filt_ws, 0, bytes, c->stream));
   }
   if (c->qf_parity) batch_set_parity(c, 0);  // new tables start from the original buffers
   batch_free(c);
@@ -1298,6 +1349,8 @@ extern "C" int osb_stage_noalloc(const osb_block_desc* d, int rk_kind, double A,
   if (rk_kind != OSB_RK_LOW_STORAGE && rk_kind != OSB_RK_SBLI3) return fail(OSB_EINVAL, "unknown RK kind");
   for (int i = 0; i < 10; ++i)
     if (d->metric[i]) return fail(OSB_ENOTSUP, "osb_stage_noalloc takes Cartesian blocks only");
+  if (d->filter != OSB_FILTER_NONE)
+    return fail(OSB_ENOTSUP, "the WENO filter follows a whole RK step (osb_step), not one stage");
   const int nv = d->ndim + 2;
   size_t alloc = 1;
   for (int i = 0; i < d->ndim; ++i) alloc *= (size_t)(d->size[i] + 2 * d->halo);

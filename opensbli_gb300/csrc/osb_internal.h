@@ -24,10 +24,11 @@ struct Block {
   float* mf_buf = nullptr;   // FP32 copies of the metrics (FP32-residual path, curvilinear)
   float* qf_base = nullptr;  // FP32 state buffer allocated with the block (FP32-residual path)
   float* qf_alt = nullptr;   // second FP32 state buffer of the persistent stage's ping-pong
+  void* filt_ws = nullptr;   // filtered blocks: kappa + 15 filter-flux arrays (residual precision)
 };
 
 // Kernel families for per-kernel timing (osb_timing_report).
-enum { FAM_FLUX_X = 0, FAM_FLUX_Y, FAM_FLUX_Z, FAM_CENTRAL, FAM_RK, FAM_BC, FAM_REDUCE, FAM_PERSISTENT, FAM_N };
+enum { FAM_FLUX_X = 0, FAM_FLUX_Y, FAM_FLUX_Z, FAM_CENTRAL, FAM_RK, FAM_BC, FAM_REDUCE, FAM_PERSISTENT, FAM_FILTER, FAM_N };
 
 struct BatchBlock;
 
@@ -138,6 +139,13 @@ inline int wave_chunks(int n, long ctas_per_chunk, long slots, double overhead, 
   }
   return best;
 }
+
+// Grid size of a grid-stride launch over n items: enough CTAs to cover them, at most 8 per SM.
+int grid_for(osb_ctx* c, long n, int threads);
+
+// Non-linear WENO filter step of a filtered block (osb_filter.cu), after a full RK step.
+int filter_f64(osb_ctx* c, Block& bl, double dt);
+int filter_f32(osb_ctx* c, Block& bl, double dt);
 
 int central_f64(osb_ctx* c, Block& bl, bool conv, int first, const RkFuse* rf);
 int central_f32(osb_ctx* c, Block& bl, bool conv, int first, const RkFuse* rf);

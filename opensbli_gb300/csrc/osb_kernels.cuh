@@ -579,8 +579,10 @@ __global__ void __launch_bounds__(32 * XWARPS) k_flux_x(BlockK b, SchemeParams s
 
 // ---------------------------------------------------------------------------------------
 // Central 4th-order terms on a 3D tile (CX x CY x CZ points, halo 2 with edges).
-//   CONV: skew-symmetric (Feiereisen) convective terms, split_forms.py:111-145 as generated
-//         for the low-Mach TGV ("Convective terms" kernel).
+//   CONV: central convective terms, 1 = skew-symmetric (Feiereisen) form, split_forms.py:111-145
+//         as generated for the low-Mach TGV ("Convective terms" kernel); 2 = Kennedy-Gruber-
+//         Pirozzoli form, split_forms.py:178-236 as generated for the Central4-WENO5 benchmark
+//         (its ring holds H = (rhoE + p) / rho where form 1 holds rhoE).
 //   VISC: viscous stress and heat flux (StoreSome "Viscous terms" kernel), mu from the
 //         modified Sutherland law (VISC == 1) or constant (VISC == 2).
 // Constants of the central kernel, derived once on the host in FP64 and handed over in both
@@ -608,7 +610,7 @@ constexpr int CSX = CX + 2 * CH, CSY = CY + 2 * CH;
 constexpr int CPL = CSX * CSY;  // points of one staged plane
 constexpr int CPP = (CPL + CX * CY - 1) / (CX * CY);  // staged points per thread and plane
 
-template <typename T, bool CONV, int VISC>
+template <typename T, int CONV, int VISC>
 struct CentralFields {
   // indices into the shared-memory field array
   static constexpr int U0 = 0, U1 = 1, U2 = 2, P = 3;
@@ -617,7 +619,7 @@ struct CentralFields {
   static constexpr int N = CONV ? (VISC ? 11 : 9) : 6;
 };
 
-template <typename T, bool CONV, int VISC, bool FUSE>
+template <typename T, int CONV, int VISC, bool FUSE>
 __global__ void __launch_bounds__(CX * CY) k_central3d(BlockK b, CentralParams cp, int first, int czc, RkFuse rf) {
   using Fd = CentralFields<T, CONV, VISC>;
   constexpr int FS = CRING * CPL;  // field stride in shared memory
@@ -671,7 +673,7 @@ __global__ void __launch_bounds__(CX * CY) k_central3d(BlockK b, CentralParams c
         sm[Fd::M0 * FS + at] = m0;
         sm[Fd::M1 * FS + at] = m1;
         sm[Fd::M2 * FS + at] = m2;
-        sm[Fd::E * FS + at] = E;
+        sm[Fd::E * FS + at] = CONV == 2 ? (E + p) / rho : E;
       }
     }
   };
@@ -741,7 +743,7 @@ __global__ void __launch_bounds__(CX * CY) k_central3d(BlockK b, CentralParams c
     const T ID[3] = {id0, id1, id2};
     const T JD[3] = {jd0, jd1, jd2};
     const int UF[3] = {Fd::U0, Fd::U1, Fd::U2};
-    if (CONV) {
+    if (CONV == 1) {
       // R_rho -= sum_j D_j m_j ; R_m_i -= D_i p + 1/2 sum_j [D_j(m_i u_j) + u_i D_j m_j + m_j D_j u_i]
       // R_E -= sum_j [D_j(p u_j) + 1/2 (D_j(E u_j) + m_j D_j(E/rho) + (E/rho) D_j m_j)]
       const int MF[3] = {Fd::M0, Fd::M1, Fd::M2};
@@ -779,6 +781,55 @@ __global__ void __launch_bounds__(CX * CY) k_central3d(BlockK b, CentralParams c
       }
       e += L_(0.5) * divm * Ec;
       racc[4] = -e;
+    }
+    if (CONV == 2) {
+      // Kennedy-Gruber-Pirozzoli form (Fd::E holds H = (rhoE + p) / rho):
+      // R_rho = -1/2 sum_j [D_j m_j + rho du_j/dx_j + u_j D_j rho]
+      // R_m_i = -D_i p - 1/4 sum_j [D_j(u_i m_j) + rho D_j(u_i u_j) + u_i D_j m_j + u_j D_j m_i
+      //                             + m_i du_j/dx_j + m_j du_i/dx_j + u_i u_j D_j rho]
+      // R_E = -1/4 sum_j [D_j(H m_j) + rho D_j(H u_j) + H D_j m_j + u_j D_j(H rho) + m_j D_j H
+      //                   + H rho du_j/dx_j + H u_j D_j rho]
+      const int MF[3] = {Fd::M0, Fd::M1, Fd::M2};
+      auto DP = [&](int f, int g, int s, T inv) -> T {
+        return d1w<T>(F(f, -2 * s) * F(g, -2 * s), F(f, -s) * F(g, -s), F(f, s) * F(g, s), F(f, 2 * s) * F(g, 2 * s)) * inv;
+      };
+      const T rho0 = F(Fd::RHO, 0), H0 = F(Fd::E, 0);
+      T dm[3], drho[3], ujj = L_(0.0), divm = L_(0.0);
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        dm[j] = D1(MF[j], S[j], ID[j]);
+        drho[j] = D1(Fd::RHO, S[j], ID[j]);
+        ujj += D1(UF[j], S[j], ID[j]);
+        divm += dm[j];
+      }
+      T rc = divm + rho0 * ujj;
+#pragma unroll
+      for (int j = 0; j < 3; ++j) rc += F(UF[j], 0) * drho[j];
+      racc[0] = -L_(0.5) * rc;
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        const T ui = F(UF[i], 0), mi = F(MF[i], 0);
+        T acc = L_(0.0);
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          const int s = S[j];
+          const T uj = F(UF[j], 0);
+          acc += DP(UF[i], MF[j], s, ID[j]) + rho0 * DP(UF[i], UF[j], s, ID[j]) + ui * dm[j] +
+                 uj * D1(MF[i], s, ID[j]) + mi * D1(UF[j], s, ID[j]) + F(MF[j], 0) * D1(UF[i], s, ID[j]) +
+                 ui * uj * drho[j];
+        }
+        racc[1 + i] = -(D1(Fd::P, S[i], ID[i]) + L_(0.25) * acc);
+      }
+      T e = L_(0.0);
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        const int s = S[j];
+        const T uj = F(UF[j], 0);
+        e += DP(Fd::E, MF[j], s, ID[j]) + rho0 * DP(Fd::E, UF[j], s, ID[j]) + H0 * dm[j] +
+             uj * DP(Fd::E, Fd::RHO, s, ID[j]) + F(MF[j], 0) * D1(Fd::E, s, ID[j]) +
+             H0 * rho0 * D1(UF[j], s, ID[j]) + H0 * uj * drho[j];
+      }
+      racc[4] = -L_(0.25) * e;
     }
     if (VISC) {
       T du[3][3], lap[3], dmu[3], dT[3], lapT = L_(0.0);
