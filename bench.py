@@ -44,10 +44,11 @@ def parse():
     ap.add_argument("--size", type=int, default=NS)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="tgv", choices=["tgv", "sod", "tgv64", "kh_ensemble", "curv4"],
+    ap.add_argument("--workload", default="tgv", choices=["tgv", "sod", "tgv64", "kh_ensemble", "curv4", "c4w5"],
                     help="tgv: the 256^3 supersonic TGV (headline); sod: the 400-point Sod tube; tgv64: the "
                          "64^3 central TGV; kh_ensemble: 64 uneven 2D Kelvin-Helmholtz instances in one "
-                         "persistent launch per stage; curv4: the 4-block 3D curvilinear TENO5 case")
+                         "persistent launch per stage; curv4: the 4-block 3D curvilinear TENO5 case; c4w5: the "
+                         "Central4-WENO5 benchmark's TGV (central KGP + WENO filter) at --size^3")
     ap.add_argument("--ensemble", type=int, default=64)
     ap.add_argument("--variant", type=int, default=0, help="x-sweep tiling variant when --fuse is given")
     ap.add_argument("--fuse", default="auto", choices=["auto", "0", "1"],
@@ -227,6 +228,23 @@ def cpu_reference_rate(case, env, points, stages, what):
     return {"value": points / per_stage / 1e6, "unit": UNIT, "cores": cores, "kind": "reference",
             "sample": "%d RK stages of %s with the reference's generated OPS solver (OpenMP, -O3); rate from "
                       "the stage timestamps after the first" % (stages, what)}
+
+
+def cpu_port_rate(spec_q, dt, steps, what):
+    """The oracle (the C restatement, one host core, -O2) on a bounded sample: Mpt-RK-stage/s
+    over `steps` whole steps of the block (spec, q)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import harness
+    from opensbli_gb300 import abi, problems
+    spec, q = spec_q
+    ob = harness.OracleBlocks([(spec, q)])
+    ob.apply_bc()
+    t0 = time.perf_counter()
+    ob.step(abi.RK_LOW_STORAGE, problems.RK3_LS_A, problems.RK3_LS_B, dt, steps)
+    secs = time.perf_counter() - t0
+    return {"value": spec.npoints * 3 * steps / secs / 1e6, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": "%d whole steps (3 RK stages + filter) of %s with the oracle (C restatement of the "
+                      "reference path, one core)" % (steps, what)}
 
 
 def reference_arm(args):
@@ -465,7 +483,7 @@ def _merge_errors(per_block):
 
 
 def secondary_arm(args):
-    """kh_ensemble / curv4 workloads: FP32-residual throughput (whole batch per step), the FP64
+    """sod / tgv64 / kh_ensemble / curv4 / c4w5 workloads: FP32-residual throughput (whole batch per step), the FP64
     per-block path beside it, the FP32-vs-FP64 error after the timed steps' count, launches."""
     import torch
     from opensbli_gb300 import abi, autotune, problems
@@ -497,6 +515,15 @@ def secondary_arm(args):
         bytes_pt = 4 * 8 * 4 + 2 * 4 * 4  # q, rk read+write FP64 (4 vars) + FP32 state in/out
         cpu_args = ("kh_weno5z", {"OSB_NP0": 320, "OSB_NP1": 320}, 320 ** 2, 12,
                     "one 320^2 Kelvin-Helmholtz instance (the ensemble's mean size)")
+    elif args.workload == "c4w5":
+        n = args.size
+        blocks = [problems.tgv_filtered(n)]
+        dt = problems.filtered_dt(n)
+        rk = "ls3"
+        work = ("Central4-WENO5 benchmark TGV %d^3, M=1.25, Re=1600, central-4 KGP + Sutherland viscous, "
+                "RK-LS3, non-linear WENO3-Z filter (Ducros 0.05) after every step, periodic" % n)
+        bytes_pt = 4 * 5 * 8
+        cpu_args = None
     else:
         blocks = problems.curvilinear_multiblock_3d(seed=0)
         dt = problems.multiblock_cfl_dt(blocks, CFL)
@@ -511,7 +538,12 @@ def secondary_arm(args):
     log("problem ready: %d blocks, %d points" % (len(blocks), pts))
     if not args.no_cpu:
         try:
-            cpu = cpu_reference_rate(*cpu_args)
+            if args.workload == "c4w5":
+                # the shipped solver's sources are not available to build on this host: the oracle
+                # (pinned to it at 1e-11) times a bounded 48^3 sample
+                cpu = cpu_port_rate(problems.tgv_filtered(48), problems.filtered_dt(48), 2, "the 48^3 filtered TGV")
+            else:
+                cpu = cpu_reference_rate(*cpu_args)
         except Exception as ex:  # the baseline is reported, not required
             cpu = {"value": None, "unit": UNIT, "kind": "reference", "sample": "failed: %s" % str(ex)[:200]}
         log("cpu baseline %s" % json.dumps(cpu))
@@ -543,7 +575,14 @@ def secondary_arm(args):
     dom_ms = rep[dom][0] / max(rep[dom][1], 1)
     hbm, peak_kind = measured_peaks()
     launches_per_stage = rep[dom][1] / 3.0
-    achieved = bytes_pt * pts / launches_per_stage / (dom_ms * 1e-3) / 1e9 if dom == "persistent_stage" else None
+    if dom == "persistent_stage":
+        achieved = bytes_pt * pts / launches_per_stage / (dom_ms * 1e-3) / 1e9
+    elif dom == "central" and len(blocks) == 1:
+        # the central scheme's only residual kernel, RK update fused: FP32 state in and out
+        # (2 x 20 B) plus the FP64 state and register read and written (160 B) per point
+        achieved = 200.0 * pts / (dom_ms * 1e-3) / 1e9
+    else:
+        achieved = None
     # FP64 per-block path and the error after the same number of steps from the same state
     s64 = Solver(blocks, precision="fp64", rk=rk, device=local)
     s64.apply_bc()

@@ -71,6 +71,26 @@ def tgv(n=64, minf=0.1, scheme=abi.SCHEME_CENTRAL4, averaging=abi.AVG_SIMPLE, vi
     return spec, _cons(spec, r, [u0, u1, u2], p)
 
 
+def tgv_filtered(n=128, sizes=None, ducros=0.05):
+    """The supersonic TGV of the reference's Central4-WENO5 benchmark
+    (apps/performance_benchmark/Central4-WENO5; the central branch of
+    apps/compressible_taylor_green_vortex/compressible_TGV.py): M = 1.25, Re = 1600, central-4
+    KGP split convective terms, modified Sutherland viscosity, the non-linear WENO3-Z filter
+    after every step with Ducros_check = Ducros_select = `ducros`; the benchmark's time step is
+    0.00084625 * 256 / n (``filtered_dt``)."""
+    spec, q = tgv(n, minf=1.25, scheme=abi.SCHEME_CENTRAL4, viscous=abi.VISC_SUTHERLAND, sizes=sizes)
+    spec.split_form = abi.SPLIT_KGP
+    spec.filter = abi.FILTER_WENO3
+    spec.ducros_check = ducros
+    spec.ducros_select = ducros
+    return spec, q
+
+
+def filtered_dt(n):
+    """Time step of the Central4-WENO5 benchmark's strong-scaling mode (opensbli.cpp:63)."""
+    return 0.00084625 * 256 / n
+
+
 def kh(n=128, amp=1.0, phase=0.0, sizes=None, scheme=abi.SCHEME_WENO5_Z, averaging=abi.AVG_ROE):
     """2D Kelvin-Helmholtz on the periodic unit square (Delta = 1/N)."""
     sizes = tuple(sizes) if sizes is not None else (n, n)
