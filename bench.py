@@ -121,7 +121,7 @@ class ClockSampler:
 
 def measured_traffic(kernel, fused):
     """DRAM bytes (read + write) per point of one launch of `kernel`, from the ncu capture
-    summarised in profiles/dram_traffic_tgv_fp32.txt (captured at 160^3, above L2; traffic
+    summarised in profiles/dram_traffic_tgv_fp32.txt (captured on the 256^3 block; traffic
     scales with the points of the block), or None."""
     path = os.path.join(ROOT, "profiles", "dram_traffic_tgv_fp32.txt")
     if not os.path.exists(path):
