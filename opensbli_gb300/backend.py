@@ -184,6 +184,62 @@ def _bcs_of(block, central_only):
     return bc, depth
 
 
+def _rhs_names(eqn):
+    """Names of the data objects on the right-hand side of one expanded equation."""
+    return {str(a) for a in eqn.rhs.atoms() if type(a).__name__ in ("DataObject", "Symbol")}
+
+
+def _split_form_of(block):
+    """Convective split form of a central-scheme block (physical_models/split_forms.py), read
+    from its expanded simulation equations.  Over the reference's forms (Divergence, Blaisdell,
+    Feiereisen, Jameson, Kok, KGP, KEEP, each with either energy formulation) the symbol sets
+    of the continuity and energy right-hand sides single out the two implemented ones:
+      Feiereisen: continuity holds only rhou_j; energy holds rhoE, rho, rhou_j, p and neither H
+                  nor e;
+      KGP (enthalpy formulation): continuity holds rho, u_j, rhou_j; energy holds H and rho and
+                  none of p, rhoE, e.
+    Any other form raises NotImplementedError."""
+    from opensbli import SimulationEquations
+    from sympy import flatten
+    eqs = []
+    for ec in block.list_of_equation_classes:
+        if isinstance(ec, SimulationEquations):
+            eqs += flatten(ec.equations)
+    by_lhs = {}
+    for e in eqs:
+        name = str(getattr(e.lhs, "args", [e.lhs])[0]) if getattr(e.lhs, "args", None) else str(e.lhs)
+        by_lhs[name.split("_B")[0]] = e
+    mass, energy = by_lhs.get("rho"), by_lhs.get("rhoE")
+    if mass is None or energy is None:
+        raise NotImplementedError("central scheme: continuity / energy equations not found")
+    m, en = _rhs_names(mass), _rhs_names(energy)
+    nd = block.ndim
+    rhou = {"rhou%d" % i for i in range(nd)}
+    u = {"u%d" % i for i in range(nd)}
+    if m <= rhou and {"rhoE", "rho", "p"} <= en and rhou <= en and not ({"H", "e"} & en):
+        return abi.SPLIT_FEIEREISEN
+    if ({"rho"} | u | rhou) <= m and {"H", "rho"} <= en and not ({"p", "rhoE", "e"} & en):
+        return abi.SPLIT_KGP
+    raise NotImplementedError("central convective split form not supported (Feiereisen and KGP with the enthalpy "
+                              "energy formulation are); continuity uses %s, energy %s" % (sorted(m), sorted(en)))
+
+
+def _check_equation_classes(block):
+    """Fail loudly on equation classes the GB300 path does not run (explicit / non-linear
+    filters and others), instead of ignoring them."""
+    from opensbli import SimulationEquations, ConstituentRelations, GridBasedInitialisation
+    allowed = (SimulationEquations, ConstituentRelations, GridBasedInitialisation)
+    for ec in block.list_of_equation_classes:
+        if isinstance(ec, allowed):
+            continue
+        name = type(ec).__name__
+        if name in ("UserDefinedEquations", "MetricsEquation"):
+            continue  # post-processing reductions (osb_reduce) / metrics passed as arrays
+        raise NotImplementedError("equation class %s is not supported by the GB300 backend%s" % (
+            name, "; the non-linear WENO filter is reached through BlockSpec (problems.tgv_filtered)"
+            if "filter" in name.lower() or "Filter" in name else ""))
+
+
 def block_spec(block, params):
     """BlockSpec of one OpenSBLI SimulationBlock."""
     p = resolve_parameters(params)
@@ -192,9 +248,12 @@ def block_spec(block, params):
     size = tuple(int(_const_value("block%dnp%d" % (b, d), p)) for d in range(nd))
     delta = tuple(float(_const_value("Delta%dblock%d" % (d, b), p)) for d in range(nd))
     scheme, avg, central = _scheme_of(block)
+    _check_equation_classes(block)
     visc = _viscosity_of(block)
     bc, depth = _bcs_of(block, scheme == abi.SCHEME_CENTRAL4)
+    split = _split_form_of(block) if scheme == abi.SCHEME_CENTRAL4 else abi.SPLIT_FEIEREISEN
     return BlockSpec(ndim=nd, size=size, scheme=scheme, averaging=avg, viscous=visc, bc=bc, bc_depth=depth,
+                     split_form=split,
                      gama=_const_value("gama", p), Minf=_const_value("Minf", p, 1.0), Re=_const_value("Re", p, 1.0),
                      Pr=_const_value("Pr", p, 0.71), mu_const=1.0, eps=_const_value("eps", p, 1e-40),
                      teno_ct=_const_value("TENO_CT", p, 1e-6),

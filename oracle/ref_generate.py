@@ -281,6 +281,39 @@ def case_tgv_central():
     return block, _tgv_params(0.1, 16, "0.003385")
 
 
+def central_split_block(form, energy_formulation="none"):
+    """3D supersonic TGV block with the central 4th-order scheme and the convective split form
+    `form` of physical_models/split_forms.py (NS_Split), modified Sutherland viscosity
+    (StoreSome), RK-LS3, periodic -- the central branch of
+    ``apps/compressible_taylor_green_vortex/compressible_TGV.py:66-75, 128-160`` without the
+    filter step."""
+    import copy
+    from opensbli import NS_Split, SimulationEquations, StoreSome, RungeKuttaLS, PeriodicBC
+    ndim = 3
+    constants = ["Re", "Pr", "gama", "Minf", "SuthT", "RefT"]
+    NS = NS_Split(form, ndim, constants, coordinate_symbol="x", conservative=True, viscosity="dynamic",
+                  energy_formulation=energy_formulation, debug=False)
+    sim = SimulationEquations()
+    sim.add_equations(NS.mass)
+    sim.add_equations(NS.momentum)
+    sim.add_equations(NS.energy)
+    cr = _constituents(ndim, viscous=True)
+    block, initial = _tgv_block(ndim)
+    schemes = {}
+    cent = StoreSome(4, "u0 u1 u2")
+    schemes[cent.name] = cent
+    rk = RungeKuttaLS(3)
+    schemes[rk.name] = rk
+    block.set_discretisation_schemes(schemes)
+    bcs = []
+    for d in range(ndim):
+        bcs += [PeriodicBC(d, 0, halos=[-2, 2]), PeriodicBC(d, 1, halos=[-2, 2])]
+    block.set_block_boundaries(bcs)
+    block.set_equations([copy.deepcopy(cr), copy.deepcopy(sim), initial])
+    block.discretise()
+    return block, _tgv_params(1.25, 16, "0.001")
+
+
 def case_kh_weno5z():
     """2D Kelvin-Helmholtz, Euler, characteristic LLF WENO5-Z with Roe average, periodic,
     classic 3-register SBLI RK3 (``apps/kelvin_helmholtz/kelvin_helmholtz.py:20-130``).  The
@@ -397,6 +430,7 @@ CASES = {
     "tgv_weno5z": lambda: case_tgv_shock("weno5z"),
     "tgv_teno6": lambda: case_tgv_shock("teno6"),
     "tgv_central": case_tgv_central,
+    "tgv_kgp": lambda: central_split_block("KGP", "enthalpy"),
     "kh_weno5z": case_kh_weno5z,
     "curv_weno5z": case_curv_weno5z,
 }

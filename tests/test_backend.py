@@ -115,3 +115,28 @@ def test_precision_follows_reference_datatype_knobs():
         assert be.precision == "fp64"
     finally:
         setattr(SimulationDataType, "dtype", saved)
+
+
+TGV_SUPERSONIC = dict(TGV_NUMBERS, Minf="1.25")
+
+
+@needs_ref
+def test_central_split_form_detected():
+    """The central scheme's convective split form is read from the block's equations:
+    Feiereisen (low-Mach TGV app) and KGP with the enthalpy energy formulation (the central
+    branch of compressible_TGV.py) map onto OSB_SPLIT_*; another form fails loudly."""
+    be = _backend_for("tgv_central", dict(TGV_NUMBERS, Minf="0.1"))
+    assert be.specs[0].split_form == abi.SPLIT_FEIEREISEN
+    be = _backend_for("tgv_kgp", TGV_SUPERSONIC)
+    spec = be.specs[0]
+    assert spec.split_form == abi.SPLIT_KGP and spec.scheme == abi.SCHEME_CENTRAL4
+    assert spec.viscous == abi.VISC_SUTHERLAND
+    import contextlib
+    import ref_generate
+    from opensbli import TraditionalAlgorithmRK
+    from opensbli_gb300.backend import GB300Backend
+    with open(os.devnull, "w") as dn, contextlib.redirect_stdout(dn):
+        block, _ = ref_generate.central_split_block("Divergence")
+        alg = TraditionalAlgorithmRK(block)
+    with pytest.raises(NotImplementedError):
+        GB300Backend(alg, TGV_SUPERSONIC)
