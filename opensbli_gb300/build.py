@@ -29,6 +29,9 @@ UNITS = [
     ("central_f64", "osb_central.cu", ["-DOSB_CENTRAL_T=double", "-DOSB_CENTRAL_NAME=central_f64"]),
     ("central_f32", "osb_central.cu", ["-DOSB_CENTRAL_T=float", "-DOSB_CENTRAL_NAME=central_f32"] + FAST),
     ("batch", "osb_batch.cu", FAST),
+    ("resident_f64", "osb_resident.cu", ["-DOSB_RESIDENT_T=double", "-DOSB_RESIDENT_NAME=resident_f64"]),
+    ("resident_f32", "osb_resident.cu", ["-DOSB_RESIDENT_T=float", "-DOSB_RESIDENT_NAME=resident_f32",
+                                          "-DOSB_RESIDENT_F32"] + FAST),
     ("filter_f64", "osb_filter.cu", ["-DOSB_FILTER_T=double", "-DOSB_FILTER_NAME=filter_f64"]),
     ("filter_f32", "osb_filter.cu", ["-DOSB_FILTER_T=float", "-DOSB_FILTER_NAME=filter_f32"] + FAST),
 ] + [

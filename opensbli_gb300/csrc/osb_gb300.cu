@@ -921,6 +921,7 @@ int osb_ctx_destroy(osb_ctx* c) {
     if (bl.filt_ws) cudaFree(bl.filt_ws);
   }
   batch_free(c);
+  if (c->resident) cudaFree(c->resident);
   if (c->red) cudaFree(c->red);
   if (c->bad) cudaFree(c->bad);
   if (c->red_host) cudaFreeHost(c->red_host);
@@ -1077,6 +1078,14 @@ int osb_step(osb_ctx* c, double dt, int nsteps) {
   if (nsteps < 0) return fail(OSB_EINVAL, "nsteps < 0");
   if (c->blocks.empty()) return fail(OSB_EINVAL, "no blocks");
   OSB_CK(cudaSetDevice(c->device));
+  if (resident_eligible(c)) {
+    // small 1D blocks: every stage of every step in one launch (no graph needed; the kernel
+    // derives its FP32 copy of the state itself)
+    int rc = resident_step(c, dt, nsteps);
+    if (rc) return rc;
+    OSB_CK(cudaGetLastError());
+    return OSB_OK;
+  }
   int src = sync_shadow(c);
   if (src) return src;
   const bool batch = use_batch(c);

@@ -63,6 +63,8 @@ struct osb_ctx {
   osb_schedule sched = {OSB_SCHED_AUTO, 16, 2, 1, 0, 1};
   osb::BatchState batch;
   int qf_parity = 0;
+  void* resident = nullptr;  // device table of the resident 1D path (osb_resident.cu)
+  int resident_n = 0;
   double g_dt = 0.0;
   long long g_kernels = 0;
   double* red = nullptr;              // device reduction partials (+ final slot)
@@ -142,6 +144,12 @@ inline int wave_chunks(int n, long ctas_per_chunk, long slots, double overhead, 
 
 // Grid size of a grid-stride launch over n items: enough CTAs to cover them, at most 8 per SM.
 int grid_for(osb_ctx* c, long n, int threads);
+
+// Whole osb_step calls of small 1D blocks in one launch, one CTA per block (osb_resident.cu).
+bool resident_eligible(const osb_ctx* c);
+int resident_step(osb_ctx* c, double dt, int nsteps);
+int resident_f64(osb_ctx* c, double dt, int nsteps);
+int resident_f32(osb_ctx* c, double dt, int nsteps);
 
 // Non-linear WENO filter step of a filtered block (osb_filter.cu), after a full RK step.
 int filter_f64(osb_ctx* c, Block& bl, double dt);
