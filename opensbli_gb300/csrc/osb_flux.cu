@@ -71,10 +71,12 @@ int launch_flux(osb_ctx* c, Block& bl, const SchemeParams& sp, const RkFuse* rf)
       const int nx = wave_chunks(k.n[0], gy, slots, 4.0, 16);
       xseg = (k.n[0] + nx - 1) / nx;
     }
-    xseg = std::max(1, std::min(xseg, k.n[0]));
+    // whole flush tiles per segment (sector-aligned stores), at most the row
+    xseg = std::max(XOUT, (std::min(xseg, k.n[0]) + XOUT - 1) / XOUT * XOUT);
+    // segment 0 also carries the row's head [0, a) before its first sector boundary
     dim3 grid((k.n[0] + xseg - 1) / xseg, (unsigned)gy);
     timing_begin(c, FAM_FLUX_X);
-    kern<<<grid, 32 * XWARPS, smem, st>>>(k, sp, 1, xseg);
+    kern<<<grid, 32 * XWARPS, smem, st>>>(k, sp, 1, xseg, bl.xrows);
     timing_end(c);
     c->launches++;
   }

@@ -18,6 +18,7 @@
 #include <string>
 #include <mutex>
 #include <thread>
+#include <algorithm>
 #include <vector>
 
 #include "osb_internal.h"
@@ -919,6 +920,7 @@ int osb_ctx_destroy(osb_ctx* c) {
     if (bl.mf_buf) cudaFree(bl.mf_buf);
     if (bl.qf_alt) cudaFree(bl.qf_alt);
     if (bl.filt_ws) cudaFree(bl.filt_ws);
+    if (bl.xrows) cudaFree(bl.xrows);
   }
   batch_free(c);
   if (c->resident) cudaFree(c->resident);
@@ -1011,6 +1013,25 @@ int osb_block_add(osb_ctx* c, const osb_block_desc* d, int* block_id) {
     }
     OSB_CK(cudaGetLastError());
   }
+  {
+    // x-sweep row table: the linear index of every row's x = 0 element, rows grouped by the
+    // phase of that element within a 32-byte sector (stable), so each warp's rows share it
+    const int nrows = k.n[1] * k.n[2];
+    std::vector<int> rows(nrows);
+    for (int z = 0, r = 0; z < k.n[2]; ++z)
+      for (int y = 0; y < k.n[1]; ++y) rows[r++] = k.off0 + y * k.st[1] + z * k.st[2];
+    std::stable_sort(rows.begin(), rows.end(), [](int u, int v) { return (u & 7) < (v & 7); });
+    cudaError_t e = cudaMalloc(&bl.xrows, sizeof(int) * nrows);
+    if (e == cudaSuccess) e = cudaMemcpy(bl.xrows, rows.data(), sizeof(int) * nrows, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+      cudaFree(R);
+      if (bl.qf_base) cudaFree(bl.qf_base);
+      if (bl.qf_alt) cudaFree(bl.qf_alt);
+      if (bl.mf_buf) cudaFree(bl.mf_buf);
+      if (bl.xrows) cudaFree(bl.xrows);
+      return fail(OSB_ECUDA, "x-sweep row table: %s", cudaGetErrorString(e));
+    }
+  }
   if (d->filter == OSB_FILTER_WENO3) {
     // kappa (zero halos, written on the interior only) and the 15 filter-flux arrays
     const size_t bytes = (size_t)16 * k.alloc * (c->prec == OSB_PREC_FP32_RESIDUAL ? sizeof(float) : sizeof(double));
@@ -1020,6 +1041,7 @@ int osb_block_add(osb_ctx* c, const osb_block_desc* d, int* block_id) {
       if (bl.qf_base) cudaFree(bl.qf_base);
       if (bl.qf_alt) cudaFree(bl.qf_alt);
       if (bl.mf_buf) cudaFree(bl.mf_buf);
+      cudaFree(bl.xrows);
       return fail(OSB_ECUDA, "filter workspace: %s", cudaGetErrorString(e));
     }
     OSB_CK(cudaMemsetAsync(bl.filt_ws, 0, bytes, c->stream));

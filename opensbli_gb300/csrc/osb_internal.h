@@ -25,6 +25,7 @@ struct Block {
   float* qf_base = nullptr;  // FP32 state buffer allocated with the block (FP32-residual path)
   float* qf_alt = nullptr;   // second FP32 state buffer of the persistent stage's ping-pong
   void* filt_ws = nullptr;   // filtered blocks: kappa + 15 filter-flux arrays (residual precision)
+  int* xrows = nullptr;      // x-sweep rows (linear index of x = 0) grouped by 32-byte-sector phase
 };
 
 // Kernel families for per-kernel timing (osb_timing_report).

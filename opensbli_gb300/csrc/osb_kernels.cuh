@@ -466,7 +466,8 @@ struct XTile {
 };
 
 template <typename T, int ND, int SCH, int AVG, bool CURV>
-__global__ void __launch_bounds__(32 * XWARPS) k_flux_x(BlockK b, SchemeParams spd, int first, int xseg) {
+__global__ void __launch_bounds__(32 * XWARPS) k_flux_x(BlockK b, SchemeParams spd, int first, int xseg,
+                                                         const int* __restrict__ xrows) {
   constexpr int NV = ND + 2;
   constexpr int NF = SweepFields<ND, CURV>::N;
   constexpr int NO = CURV ? NV + 1 : NV;  // curvilinear: the point's 1 / (dx J) rides along
@@ -480,15 +481,25 @@ __global__ void __launch_bounds__(32 * XWARPS) k_flux_x(BlockK b, SchemeParams s
   const int nrows = b.n[1] * b.n[2];
   const int row0 = (blockIdx.y * XWARPS + warp) * 32;
   if (row0 >= nrows) return;  // whole warps only: the lanes below stay converged
-  const int s0 = blockIdx.x * xseg;
-  const int s1 = min(b.n[0], s0 + xseg);
   {
-    // rows past the block end repeat the last row (computed, never stored)
+    // rows past the block end repeat the last row (computed, never stored); with a row table
+    // the rows come grouped by the 32-byte-sector phase of their x = 0 element
     const int row = min(row0 + lane, nrows - 1);
-    const int y = row % b.n[1], z = row / b.n[1];
-    t.rowbase[lane] = lin(b, 0, y, z);
+    t.rowbase[lane] = xrows ? xrows[row] : lin(b, 0, row % b.n[1], row / b.n[1]);
   }
   __syncwarp();
+  // Segment blockIdx.x of this warp: [0, a + xseg) for 0, then [a + k xseg, a + (k+1) xseg),
+  // where x = a is the first point whose element starts a sector in the warp's rows (a = 0
+  // without a row table).  Flush tiles of XOUT points are anchored at o0 = a (mod XOUT), and
+  // xseg is a whole number of tiles, so every tile store covers whole sectors (the row's head
+  // [0, a) is a partial tile of segment 0).
+  constexpr int SEC = 32 / (int)sizeof(T);  // elements per 32-byte sector
+  const int a = xrows ? (SEC - (t.rowbase[0] & (SEC - 1))) & (SEC - 1) : 0;
+  const int kseg = blockIdx.x;
+  const int s0 = kseg == 0 ? 0 : min(b.n[0], a + kseg * xseg);
+  const int s1 = min(b.n[0], a + (kseg + 1) * xseg);
+  if (s0 >= s1) return;  // warp-uniform
+  const int o0 = s0 - (((s0 - a) % XOUT) + XOUT) % XOUT;  // tile origin, <= s0
   const int c0 = s0 - 3;          // global x of input column 0
   const int ncols = s1 - s0 + 6;  // columns s0-3 .. s1+2
   auto issue = [&](int k) {       // input chunk k: columns c0 + XCH k .. c0 + XCH k + XCH - 1
@@ -506,12 +517,12 @@ __global__ void __launch_bounds__(32 * XWARPS) k_flux_x(BlockK b, SchemeParams s
     cp_async_commit();
   };
   const T invd = (T)b.invd[0];
-  // residuals of the points s0 + pb .. s0 + pb + XOUT - 1 (those below s1) from the out tile
-  auto flush = [&](int pb) {
+  // residuals of the tile's points g .. g + XOUT - 1 that lie in [s0, s1), from the out tile
+  auto flush = [&](int g) {
     __syncwarp();
     const int cc = lane % XOUT;
-    const int p = s0 + pb + cc;
-    if (p < s1) {
+    const int p = g + cc;
+    if (p >= s0 && p < s1) {
 #pragma unroll
       for (int rb = 0; rb < XOUT; ++rb) {
         const int r = rb * OPI + lane / XOUT;
@@ -567,13 +578,15 @@ __global__ void __launch_bounds__(32 * XWARPS) k_flux_x(BlockK b, SchemeParams s
     } else {
       char_flux<T, ND, SCH, AVG>(w, sp, fh);
     }
-    // interface j + 1/2 is the right face of point j: out column (j - s0) % XOUT + 1, or the
-    // carry column for the face left of the segment
-    const int oc = j < s0 ? 0 : (j - s0) % XOUT + 1;
+    // interface j + 1/2 is the right face of point j: out column (j - o0) % XOUT + 1; the face
+    // left of the segment lands in the column left of point s0 (the carry column when the
+    // segment starts on the tile grid)
+    const int dj = j - o0;
+    const int oc = dj < 0 ? 0 : dj % XOUT + 1;
 #pragma unroll
     for (int v = 0; v < NV; ++v) t.out[v][lane][oc] = fh[v];
     if constexpr (CURV) t.out[NO - 1][lane][oc] = invd / w[2].J;
-    if (j >= s0 && (oc == XOUT || j == s1 - 1)) flush(j - s0 - (oc - 1));
+    if (j >= s0 && (oc == XOUT || j == s1 - 1)) flush(j - (oc - 1));
   }
 }
 
