@@ -44,11 +44,13 @@ def parse():
     ap.add_argument("--size", type=int, default=NS)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="tgv", choices=["tgv", "sod", "tgv64", "kh_ensemble", "curv4", "c4w5"],
+    ap.add_argument("--workload", default="tgv",
+                    choices=["tgv", "sod", "tgv64", "kh_ensemble", "curv4", "c4w5", "tvd"],
                     help="tgv: the 256^3 supersonic TGV (headline); sod: the 400-point Sod tube; tgv64: the "
                          "64^3 central TGV; kh_ensemble: 64 uneven 2D Kelvin-Helmholtz instances in one "
                          "persistent launch per stage; curv4: the 4-block 3D curvilinear TENO5 case; c4w5: the "
-                         "Central4-WENO5 benchmark's TGV (central KGP + WENO filter) at --size^3")
+                         "Central4-WENO5 benchmark's TGV (central KGP + WENO filter) at --size^3; tvd: the TGV "
+                         "app's TVD branch (central KGP + TVD filter) at --size^3")
     ap.add_argument("--ensemble", type=int, default=64)
     ap.add_argument("--variant", type=int, default=0, help="x-sweep tiling variant when --fuse is given")
     ap.add_argument("--fuse", default="auto", choices=["auto", "0", "1"],
@@ -483,7 +485,7 @@ def _merge_errors(per_block):
 
 
 def secondary_arm(args):
-    """sod / tgv64 / kh_ensemble / curv4 / c4w5 workloads: FP32-residual throughput (whole batch per step), the FP64
+    """sod / tgv64 / kh_ensemble / curv4 / c4w5 / tvd workloads: FP32-residual throughput (whole batch per step), the FP64
     per-block path beside it, the FP32-vs-FP64 error after the timed steps' count, launches."""
     import torch
     from opensbli_gb300 import abi, autotune, problems
@@ -524,6 +526,17 @@ def secondary_arm(args):
                 "RK-LS3, non-linear WENO3-Z filter (Ducros 0.05) after every step, periodic" % n)
         bytes_pt = 4 * 5 * 8
         cpu_args = None
+    elif args.workload == "tvd":
+        n = args.size
+        blocks = [problems.tgv_tvd(n, kappa=1.25)]
+        dt = 0.0005 * 256 / n
+        rk = "ls3"
+        work = ("TGV %d^3 of the TGV app's TVD branch, M=1.25, Re=1600, central-4 KGP + Sutherland viscous, "
+                "RK-LS3, non-linear TVD filter (kappa_TVD 1.25) after every step, periodic" % n)
+        bytes_pt = 4 * 5 * 8
+        cpu_args = ("tgv_kgp_tvd", {"OSB_NP0": 64, "OSB_NP1": 64, "OSB_NP2": 64, "OSB_KAPPA_TVD": 1.25,
+                                    "OSB_DT": 0.0005 * 4}, 64 ** 3, 7,
+                    "the 64^3 TVD-filtered TGV (two whole steps with their filters)")
     else:
         blocks = problems.curvilinear_multiblock_3d(seed=0)
         dt = problems.multiblock_cfl_dt(blocks, CFL)

@@ -68,9 +68,11 @@ extern "C" {
 #define OSB_SPLIT_FEIEREISEN 0 /* skew-symmetric form, split_forms.py:111-145 */
 #define OSB_SPLIT_KGP 1        /* Kennedy-Gruber-Pirozzoli form, split_forms.py:178-236 */
 
-/* Filter applied after every full RK step (filters/WENO_filter.py). */
+/* Filter applied after every full RK step (filters/WENO_filter.py, filters/TVD_filter.py). */
 #define OSB_FILTER_NONE 0
 #define OSB_FILTER_WENO3 1     /* non-linear characteristic WENO3-Z filter with a Ducros sensor */
+#define OSB_FILTER_TVD 2       /* non-linear characteristic TVD filter (Yee-Sandham-Djomehri
+                                  limiter with Harten's switch, shock_capturing.py:619-766) */
 
 /* Residual precision (per context). */
 #define OSB_PREC_FP64 0          /* plain FP64 path, parity with the generated solver */
@@ -120,6 +122,7 @@ typedef struct osb_block_desc {
   int32_t filter;            /* OSB_FILTER_* (3D central scheme only; 0 = none) */
   double ducros_check;       /* filter flux where max kappa over the interface stencil > this */
   double ducros_select;      /* filter applied where max kappa around the point >= this */
+  double tvd_kappa;          /* OSB_FILTER_TVD: the filter strength kappa_TVD */
 } osb_block_desc;
 
 /* ---- library / context ------------------------------------------------------------- */
@@ -244,8 +247,8 @@ int osb_get_stream(osb_ctx* ctx, void** stream);
 int osb_stage_noalloc(const osb_block_desc* desc, int rk_kind, double A, double B, double dt, void* stream);
 
 /* Binding check: writes sizeof(osb_block_desc) and the byte offsets of size, bc, iface, gama,
- * delta, q, rkold, metric, split_form and ducros_check into out[0..10] (n >= 11).  Needs no
- * GPU. */
+ * delta, q, rkold, metric, split_form, ducros_check and tvd_kappa into out[0..11] (n >= 12).
+ * Needs no GPU. */
 int osb_desc_layout(long long* out, int n);
 
 #ifdef __cplusplus

@@ -38,6 +38,7 @@ SPLIT_FEIEREISEN = 0
 SPLIT_KGP = 1
 FILTER_NONE = 0
 FILTER_WENO3 = 1
+FILTER_TVD = 2
 
 PREC_FP64 = 0
 PREC_FP32_RESIDUAL = 1
@@ -102,6 +103,7 @@ class BlockDesc(ctypes.Structure):
         ("filter", ctypes.c_int32),
         ("ducros_check", ctypes.c_double),
         ("ducros_select", ctypes.c_double),
+        ("tvd_kappa", ctypes.c_double),
     ]
 
 
@@ -109,7 +111,7 @@ def layout_signature():
     """(sizeof, offsets...) of BlockDesc, compared with the C side in the tests."""
     offs = [BlockDesc.size.offset, BlockDesc.bc.offset, BlockDesc.iface.offset, BlockDesc.gama.offset,
             BlockDesc.delta.offset, BlockDesc.q.offset, BlockDesc.rkold.offset, BlockDesc.metric.offset,
-            BlockDesc.split_form.offset, BlockDesc.ducros_check.offset]
+            BlockDesc.split_form.offset, BlockDesc.ducros_check.offset, BlockDesc.tvd_kappa.offset]
     return [ctypes.sizeof(BlockDesc)] + offs
 
 
@@ -144,6 +146,7 @@ def make_desc(spec, q_ptrs, rk_ptrs, metric_ptrs=None):
     d.filter = spec.filter
     d.ducros_check = spec.ducros_check
     d.ducros_select = spec.ducros_select
+    d.tvd_kappa = spec.tvd_kappa
     for v, p in enumerate(q_ptrs):
         d.q[v] = p
     for v, p in enumerate(rk_ptrs):

@@ -32,8 +32,10 @@ UNITS = [
     ("resident_f64", "osb_resident.cu", ["-DOSB_RESIDENT_T=double", "-DOSB_RESIDENT_NAME=resident_f64"]),
     ("resident_f32", "osb_resident.cu", ["-DOSB_RESIDENT_T=float", "-DOSB_RESIDENT_NAME=resident_f32",
                                           "-DOSB_RESIDENT_F32"] + FAST),
-    ("filter_f64", "osb_filter.cu", ["-DOSB_FILTER_T=double", "-DOSB_FILTER_NAME=filter_f64"]),
-    ("filter_f32", "osb_filter.cu", ["-DOSB_FILTER_T=float", "-DOSB_FILTER_NAME=filter_f32"] + FAST),
+    ("filter_f64", "osb_filter.cu", ["-DOSB_FILTER_T=double", "-DOSB_FILTER_NAME=filter_f64",
+                                           "-DOSB_TVD_STALE_NAME=tvd_stale_f64"]),
+    ("filter_f32", "osb_filter.cu", ["-DOSB_FILTER_T=float", "-DOSB_FILTER_NAME=filter_f32",
+                                          "-DOSB_TVD_STALE_NAME=tvd_stale_f32"] + FAST),
 ] + [
     ("flux_%s_%dd" % (p, nd), "osb_flux.cu",
      ["-DOSB_T=%s" % ("double" if p == "f64" else "float"), "-DOSB_ND=%d" % nd, "-DOSB_NAME=flux_%s_%dd" % (p, nd)]

@@ -6,6 +6,10 @@
 //   3. per direction the filter flux at every interface i+1/2, i = -1..N-1 (kernels 046-048);
 //   4. q += dt * mask * (-sum_d (F_d(i) - F_d(i-1)) / Delta_d), mask = [max kappa over the
 //      point and its neighbours >= Ducros_select] (kernel 049).
+// The non-linear characteristic TVD filter (filters/TVD_filter.py; the Yee-Sandham-Djomehri
+// limiter with Harten's switch, schemes/spatial/shock_capturing.py:619-766) runs the same
+// exchange, then per direction its flux at interfaces i = -1..N-1 and the same update without a
+// sensor mask, as the generated solver of the TGV app's TVD branch does.
 // Compiled once per precision (OSB_FILTER_T).  In the FP32-residual path the filter reads the
 // FP32 state, forms the increment in FP32 and adds it to the FP64 state, then refreshes the
 // FP32 copy of the points it changed.
@@ -16,6 +20,7 @@
 #ifndef OSB_FILTER_T
 #define OSB_FILTER_T double
 #define OSB_FILTER_NAME filter_f64
+#define OSB_TVD_STALE_NAME tvd_stale_f64
 #endif
 
 namespace osb {
@@ -278,8 +283,199 @@ __global__ void k_filter_flux(BlockK b, SchemeParams spd, const T* __restrict__ 
   }
 }
 
+// ---- TVD filter ---------------------------------------------------------------------------
+
+// A point of the TVD stencil, local frame (normal momentum and velocity first).
+template <typename T>
+struct TvdPt {
+  T r, m[3], e, u[3], a;
+};
+
+// Entropy fix of a wave speed with delta_TVD = 1/2 (shock_capturing.py:681-689, as generated:
+// |z| >= 1/invdelta ? |z| : 1/2 (1/invdelta^2 + z^2) invdelta, invdelta = 2).
+template <typename T>
+__device__ __forceinline__ T tvd_psi(T z) {
+  return fabs(z) >= L_(0.5) ? fabs(z) : L_(0.5) * (L_(0.25) + z * z) * L_(2.0);
+}
+
+// Limiter from the jump of this interface (hi) and the one below (lo) (lines 690-704).
+template <typename T>
+__device__ __forceinline__ T tvd_g(T hi, T lo) {
+  const T S = hi > L_(0.0) ? L_(1.0) : (hi < L_(0.0) ? L_(-1.0) : L_(0.0));
+  const T t1 = fmax(L_(0.0), fmin(S * lo, L_(2.0) * fabs(hi)));
+  const T t2 = fmin(fabs(hi), L_(2.0) * S * lo);
+  return S * fmax(t1, t2);
+}
+
+// TVD filter flux at interface i+1/2 from the points i-1..i+2 (local frame): simple averages
+// over (i-1, i), (i, i+1), (i+1, i+2), the characteristic jumps alpha = LEV (q_hi - q_lo) at
+// each, wave speeds and REV at i+1/2, then per wave sigma = psi(lambda), the limiters g at i and
+// i+1, gamma, phi = 1/2 sigma (g_i + g_i+1) - |sigma + psi(gamma)| alpha, Harten's switch theta
+// = max of ((|a_hi| - |a_lo|) / (|a_hi| + |a_lo| + eps))^2 over the two pairs, and
+// F = 1/2 REV (kappa theta phi), eps_TVD = 1e-8 -- in the operation order of the generated
+// direction-0 kernel.
+template <typename T>
+__device__ __forceinline__ void tvd_flux(const TvdPt<T> (&w)[4], T gm, T kappa, T (&fh)[5]) {
+  const T g1 = gm - L_(1.0), eps = L_(1.0e-8);
+  const T c1 = L_(0.35355339059327373), c2 = L_(0.70710678118654746);
+  T al[5][3];
+  T ws0 = L_(0.0), wsp = L_(0.0), wsm = L_(0.0);
+  T R03 = L_(0.0), R13 = L_(0.0), R14 = L_(0.0), R10 = L_(0.0), R20 = L_(0.0), R22 = L_(0.0), R23 = L_(0.0);
+  T R30 = L_(0.0), R31 = L_(0.0), R33 = L_(0.0), R40 = L_(0.0), R41 = L_(0.0), R42 = L_(0.0), R43 = L_(0.0),
+    R44 = L_(0.0);
+#pragma unroll
+  for (int jb = 0; jb < 3; ++jb) {
+    const TvdPt<T>& lo = w[jb];
+    const TvdPt<T>& hi = w[jb + 1];
+    const T u0 = L_(0.5) * (lo.u[0] + hi.u[0]), u1 = L_(0.5) * (lo.u[1] + hi.u[1]), u2 = L_(0.5) * (lo.u[2] + hi.u[2]);
+    const T a = L_(0.5) * (lo.a + hi.a), rho = L_(0.5) * (lo.r + hi.r);
+    const T ia = L_(1.0) / a, ir = L_(1.0) / rho, ia2 = ia * ia;
+    const T q0 = u0 * u0, q1 = u1 * u1, q2 = u2 * u2;
+    const T L00 = -L_(0.5) * (L_(-2.0) - q0 * ia2 - q1 * ia2 - q2 * ia2 + q0 * ia2 * gm + q1 * ia2 * gm + q2 * ia2 * gm);
+    const T L01 = ia2 * g1 * u0, L02 = ia2 * g1 * u1, L03 = ia2 * g1 * u2, L04 = -ia2 * g1;
+    const T kq = -q0 * ia - q1 * ia - q2 * ia + q0 * gm * ia + q1 * gm * ia + q2 * gm * ia;
+    const T L30 = c1 * (L_(-2.0) * u0 + kq) * ir, L40 = c1 * (L_(2.0) * u0 + kq) * ir;
+    const T L31 = -c2 * (L_(-1.0) - u0 * ia + gm * u0 * ia) * ir, L41 = -c2 * (L_(1.0) - u0 * ia + gm * u0 * ia) * ir;
+    const T L32 = -c2 * g1 * u1 * ia * ir, L33 = -c2 * g1 * u2 * ia * ir, L34 = c2 * g1 * ia * ir;
+    const T dr = -lo.r + hi.r, d0 = -lo.m[0] + hi.m[0], d1 = -lo.m[1] + hi.m[1], d2 = -lo.m[2] + hi.m[2],
+            de = -lo.e + hi.e;
+    al[0][jb] = dr * L00 + de * L04 + d0 * L01 + d1 * L02 + d2 * L03;
+    al[1][jb] = dr * (-u2 * ir) + d2 * ir;
+    al[2][jb] = dr * (u1 * ir) + d1 * (-ir);
+    al[3][jb] = dr * L30 + de * L34 + d0 * L31 + d1 * L32 + d2 * L33;
+    al[4][jb] = dr * L40 + de * L34 + d0 * L41 + d1 * L32 + d2 * L33;
+    if (jb == 1) {
+      ws0 = u0;
+      wsp = a + u0;
+      wsm = -a + u0;
+      R03 = c2 * rho * ia;
+      R10 = u0;
+      R13 = c2 * (a + u0) * rho * ia;
+      R14 = c2 * (-a + u0) * rho * ia;
+      R20 = u1;
+      R22 = -rho;
+      R23 = c2 * rho * u1 * ia;
+      R30 = u2;
+      R31 = rho;
+      R33 = c2 * rho * u2 * ia;
+      R40 = L_(0.5) * q0 + L_(0.5) * q1 + L_(0.5) * q2;
+      R41 = rho * u2;
+      R42 = -rho * u1;
+      const T hq = (a * a + L_(0.5) * g1 * (q0 + q1 + q2)) / g1;
+      R43 = c2 * (hq + a * u0) * rho * ia;
+      R44 = c2 * (hq - a * u0) * rho * ia;
+    }
+  }
+  T ps[5];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    const T s0 = tvd_psi<T>(k < 3 ? ws0 : (k == 3 ? wsp : wsm));
+    const T a0 = al[k][0], a1 = al[k][1], a2 = al[k][2];
+    const T g0 = tvd_g<T>(a1, a0), gg = tvd_g<T>(a2, a1);
+    const T gam = a1 == L_(0.0) ? L_(0.0) : (-g0 + gg) * a1 * s0 / (a1 * a1 + eps);
+    const T phi = -fabs(s0 + tvd_psi<T>(gam)) * a1 + L_(0.5) * (g0 + gg) * s0;
+    T t1 = -fabs(a0) + fabs(a1), t2 = fabs(a0) + fabs(a1) + eps;
+    const T r0 = fabs(t1 / t2);
+    t1 = -fabs(a1) + fabs(a2);
+    t2 = fabs(a1) + fabs(a2) + eps;
+    const T r1 = fabs(t1 / t2);
+    ps[k] = kappa * phi * fmax(r0 * r0, r1 * r1);
+  }
+  fh[0] = L_(0.5) * ps[0] + L_(0.5) * R03 * ps[3] + L_(0.5) * R03 * ps[4];
+  fh[1] = L_(0.5) * R10 * ps[0] + L_(0.5) * R13 * ps[3] + L_(0.5) * R14 * ps[4];
+  fh[2] = L_(0.5) * R20 * ps[0] + L_(0.5) * R22 * ps[2] + L_(0.5) * R23 * ps[3] + L_(0.5) * R23 * ps[4];
+  fh[3] = L_(0.5) * R30 * ps[0] + L_(0.5) * R31 * ps[1] + L_(0.5) * R33 * ps[3] + L_(0.5) * R33 * ps[4];
+  fh[4] = L_(0.5) * R40 * ps[0] + L_(0.5) * R41 * ps[1] + L_(0.5) * R42 * ps[2] + L_(0.5) * R43 * ps[3] +
+          L_(0.5) * R44 * ps[4];
+}
+
+// Face d of the point -2 velocities: the two other directions e1 < e2, index x_e1 + n_e1 x_e2.
+__device__ __forceinline__ void tvd_face_dirs(int d, int& e1, int& e2) {
+  e1 = d == 0 ? 1 : 0;
+  e2 = d == 2 ? 1 : 2;
+}
+
+// u = rhou / rho at index -2 of each direction (the other two interior), from the state the
+// last RK stage reads: the value its constituent relations leave there, which the generated
+// filter reads at that point.  snap[(3 d + c) * fmax + face index].
+template <typename T>
+__global__ void k_tvd_stale(BlockK b, T* __restrict__ snap, int fmax) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < 3 * fmax; t += gridDim.x * blockDim.x) {
+    const int d = t / fmax, f = t - d * fmax;
+    int e1, e2;
+    tvd_face_dirs(d, e1, e2);
+    if (f >= b.n[e1] * b.n[e2]) continue;
+    int c[3];
+    c[d] = -2;
+    c[e1] = f % b.n[e1];
+    c[e2] = f / b.n[e1];
+    const int id = lin(b, c[0], c[1], c[2]);
+    const T r = ld_q<T>(b, 0, id);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) snap[(size_t)(3 * d + k) * fmax + f] = ld_q<T>(b, 1 + k, id) / r;
+  }
+}
+
+// TVD filter fluxes along D at interfaces i+1/2, i = -1..N-1, transverse interior; F[v] at the
+// index of point i.  u and a of each point as the filter's constituent-relation kernel forms
+// them (u = rhou (1/rho), a = sqrt(gama p (1/rho))); at index -2 (the interface at -1) u comes
+// from the stage snapshot and a is 0, as in the generated solver.
+template <typename T, int D>
+__global__ void k_tvd_flux(BlockK b, T gm, T kappa, const T* __restrict__ snap, int fmax, T* F0, T* F1, T* F2, T* F3,
+                           T* F4) {
+  constexpr int T1 = (D + 1) % 3, T2 = (D + 2) % 3;
+  int e1, e2;
+  tvd_face_dirs(D, e1, e2);
+  int e[3] = {b.n[0], b.n[1], b.n[2]};
+  e[D] += 1;
+  const int total = e[0] * e[1] * e[2];
+  const int s = b.st[D];
+  T* F[5] = {F0, F1, F2, F3, F4};
+  const T g1 = gm - L_(1.0);
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+    int c[3] = {t % e[0], (t / e[0]) % e[1], t / (e[0] * e[1])};
+    c[D] -= 1;
+    const int id = lin(b, c[0], c[1], c[2]);
+    TvdPt<T> w[4];
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+      const int p = id + (m - 1) * s;
+      TvdPt<T>& q = w[m];
+      q.r = ld_q<T>(b, 0, p);
+      q.e = ld_q<T>(b, 4, p);
+      const T mx = ld_q<T>(b, 1, p), my = ld_q<T>(b, 2, p), mz = ld_q<T>(b, 3, p);
+      const T mg[3] = {mx, my, mz};
+      q.m[0] = mg[D];
+      q.m[1] = mg[T1];
+      q.m[2] = mg[T2];
+      if (m == 0 && c[D] == -1) {
+        const int f = c[e1] + b.n[e1] * c[e2];
+        q.u[0] = snap[(size_t)(3 * D + D) * fmax + f];
+        q.u[1] = snap[(size_t)(3 * D + T1) * fmax + f];
+        q.u[2] = snap[(size_t)(3 * D + T2) * fmax + f];
+        q.a = L_(0.0);
+      } else {
+        const T ir = L_(1.0) / q.r;
+        q.u[0] = q.m[0] * ir;
+        q.u[1] = q.m[1] * ir;
+        q.u[2] = q.m[2] * ir;
+        const T pr = g1 * (-(L_(0.5) * (mx * mx) + L_(0.5) * (my * my) + L_(0.5) * (mz * mz)) * ir + q.e);
+        q.a = sqrt(gm * pr * ir);
+      }
+    }
+    T fh[5];
+    tvd_flux<T>(w, gm, kappa, fh);
+    F[0][id] = fh[0];
+    F[1 + D][id] = fh[1];
+    F[1 + T1][id] = fh[2];
+    F[1 + T2][id] = fh[3];
+    F[4][id] = fh[4];
+  }
+}
+
 // q += dt * mask * (-(F_0(i) - F_0(i-1)) / Delta_0 - (F_2 ...) / Delta_2 - (F_1 ...) / Delta_1)
-// on the interior, in the generated operation order (kernel 049).  FP32: the increment is
+// on the interior, in the generated operation order (kernel 049); without kappa (TVD filter)
+// the mask is 1.  FP32: the increment is
 // formed in FP32 and added to the FP64 state; the FP32 copy of a changed point is refreshed.
 template <typename T>
 struct FilterFluxes {
@@ -295,17 +491,19 @@ __global__ void k_filter_apply(BlockK b, const T* __restrict__ kappa, FilterFlux
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
     const int x = t % n0, y = (t / n0) % n1, z = t / (n0 * n1);
     const int c = lin(b, x, y, z);
-    T km = kappa[c];
-    km = fmax(km, kappa[c + sz]);
-    km = fmax(km, kappa[c + 2 * sy]);
-    km = fmax(km, kappa[c + sx]);
-    km = fmax(km, kappa[c - sy]);
-    km = fmax(km, kappa[c - sx]);
-    km = fmax(km, kappa[c + sy]);
-    km = fmax(km, kappa[c + 2 * sz]);
-    km = fmax(km, kappa[c + 2 * sx]);
-    km = fmax(km, kappa[c - sz]);
-    if (!(km >= select)) continue;  // mask 0: the state is unchanged
+    if (kappa) {
+      T km = kappa[c];
+      km = fmax(km, kappa[c + sz]);
+      km = fmax(km, kappa[c + 2 * sy]);
+      km = fmax(km, kappa[c + sx]);
+      km = fmax(km, kappa[c - sy]);
+      km = fmax(km, kappa[c - sx]);
+      km = fmax(km, kappa[c + sy]);
+      km = fmax(km, kappa[c + 2 * sz]);
+      km = fmax(km, kappa[c + 2 * sx]);
+      km = fmax(km, kappa[c - sz]);
+      if (!(km >= select)) continue;  // mask 0: the state is unchanged
+    }
 #pragma unroll
     for (int v = 0; v < 5; ++v) {
       const T* f0 = F.f[v];
@@ -323,8 +521,54 @@ __global__ void k_filter_apply(BlockK b, const T* __restrict__ kappa, FilterFlux
   }
 }
 
+// Largest face of a block (the point -2 velocity snapshot of the TVD filter holds 9 of them in
+// the first workspace slot: 9 n_a n_b <= (n_a + 10)(n_b + 10)(n_c + 10), the slot's size).
+inline int tvd_fmax(const BlockK& k) {
+  return std::max(k.n[1] * k.n[2], std::max(k.n[0] * k.n[2], k.n[0] * k.n[1]));
+}
+
+// The TVD filter: its exchange, then per direction the fluxes, then the update (no mask).
+template <typename T>
+int tvd_filter_t(osb_ctx* c, Block& bl, double dt) {
+  BlockK& k = bl.k;
+  const long n = (long)k.n[0] * k.n[1] * k.n[2];
+  T* base = reinterpret_cast<T*>(bl.filt_ws);
+  const T* snap = base;
+  T* F[15];
+  for (int a = 0; a < 15; ++a) F[a] = base + (size_t)(1 + a) * k.alloc;
+  const int fields = sizeof(T) == 8 ? 1 : 2;
+  const int fmax = tvd_fmax(k);
+  timing_begin(c, FAM_FILTER);
+  for (int d = 0; d < 3; ++d) {
+    long per = 8L * (d == 0 ? 1 : k.n[0]) * (d == 1 ? 1 : k.n[1]) * (d == 2 ? 1 : k.n[2]);
+    k_filter_halo<<<grid_for(c, per, FT), FT, 0, c->stream>>>(k, d, fields);
+  }
+  const T gm = (T)bl.d.gama, kap = (T)bl.d.tvd_kappa;
+  const long nf0 = (long)(k.n[0] + 1) * k.n[1] * k.n[2], nf1 = (long)k.n[0] * (k.n[1] + 1) * k.n[2],
+             nf2 = (long)k.n[0] * k.n[1] * (k.n[2] + 1);
+  k_tvd_flux<T, 0><<<grid_for(c, nf0, FT), FT, 0, c->stream>>>(k, gm, kap, snap, fmax, F[0], F[1], F[2], F[3], F[4]);
+  k_tvd_flux<T, 1><<<grid_for(c, nf1, FT), FT, 0, c->stream>>>(k, gm, kap, snap, fmax, F[5], F[6], F[7], F[8], F[9]);
+  k_tvd_flux<T, 2><<<grid_for(c, nf2, FT), FT, 0, c->stream>>>(k, gm, kap, snap, fmax, F[10], F[11], F[12], F[13],
+                                                               F[14]);
+  FilterFluxes<T> Fd;
+  for (int a = 0; a < 15; ++a) Fd.f[a] = F[a];
+  k_filter_apply<T><<<grid_for(c, n, FT), FT, 0, c->stream>>>(k, nullptr, Fd, dt, (T)0);
+  timing_end(c);
+  c->launches += 7;
+  return OSB_OK;
+}
+
+template <typename T>
+int tvd_stale_t(osb_ctx* c, Block& bl) {
+  const int fmax = tvd_fmax(bl.k);
+  k_tvd_stale<T><<<grid_for(c, 3L * fmax, FT), FT, 0, c->stream>>>(bl.k, reinterpret_cast<T*>(bl.filt_ws), fmax);
+  c->launches++;
+  return OSB_OK;
+}
+
 template <typename T>
 int filter_t(osb_ctx* c, Block& bl, double dt) {
+  if (bl.d.filter == OSB_FILTER_TVD) return tvd_filter_t<T>(c, bl, dt);
   BlockK& k = bl.k;
   const long n = (long)k.n[0] * k.n[1] * k.n[2];
   T* base = reinterpret_cast<T*>(bl.filt_ws);
@@ -365,5 +609,6 @@ int filter_t(osb_ctx* c, Block& bl, double dt) {
 }  // namespace
 
 int OSB_FILTER_NAME(osb_ctx* c, Block& bl, double dt) { return filter_t<OSB_FILTER_T>(c, bl, dt); }
+int OSB_TVD_STALE_NAME(osb_ctx* c, Block& bl) { return tvd_stale_t<OSB_FILTER_T>(c, bl); }
 
 }  // namespace osb

@@ -709,9 +709,9 @@ int stage(osb_ctx* c, int s, double dt, bool bc = true) {
   return bc ? apply_bc(c) : OSB_OK;
 }
 
-bool any_filter(const osb_ctx* c) {
+bool any_filter(const osb_ctx* c, int kind) {
   for (const auto& bl : c->blocks)
-    if (bl.d.filter == OSB_FILTER_WENO3) return true;
+    if (bl.d.filter == kind) return true;
   return false;
 }
 
@@ -745,17 +745,25 @@ int one_step(osb_ctx* c, double dt) {
       c->launches++;
     }
   }
-  // with a filtered block the last stage exchanges no halos: the filter step's own exchange
-  // follows it (the next step starts with the full exchange)
-  const bool filt = any_filter(c);
+  // with a WENO-filtered block the last stage exchanges no halos: the filter step's own
+  // exchange follows it (the next step starts with the full exchange); the TVD-filtered step
+  // exchanges after every stage and keeps the velocities at index -2 that its last stage reads
+  const bool fp32 = c->prec == OSB_PREC_FP32_RESIDUAL;
+  const bool weno = any_filter(c, OSB_FILTER_WENO3), tvd = any_filter(c, OSB_FILTER_TVD);
   for (int s = 0; s < c->nst; ++s) {
-    rc = stage(c, s, dt, !(filt && s == c->nst - 1));
+    if (tvd && s == c->nst - 1)
+      for (auto& bl : c->blocks) {
+        if (bl.d.filter != OSB_FILTER_TVD) continue;
+        rc = fp32 ? tvd_stale_f32(c, bl) : tvd_stale_f64(c, bl);
+        if (rc) return rc;
+      }
+    rc = stage(c, s, dt, !(weno && s == c->nst - 1));
     if (rc) return rc;
   }
-  if (filt)
+  if (weno || tvd)
     for (auto& bl : c->blocks) {
-      if (bl.d.filter != OSB_FILTER_WENO3) continue;
-      rc = c->prec == OSB_PREC_FP32_RESIDUAL ? filter_f32(c, bl, dt) : filter_f64(c, bl, dt);
+      if (bl.d.filter == OSB_FILTER_NONE) continue;
+      rc = fp32 ? filter_f32(c, bl, dt) : filter_f64(c, bl, dt);
       if (rc) return rc;
     }
   return OSB_OK;
@@ -829,19 +837,35 @@ bool check_desc(const osb_block_desc* d, std::string& why) {
     why = "the KGP split form belongs to the central scheme";
     return false;
   }
-  if (d->filter != OSB_FILTER_NONE && d->filter != OSB_FILTER_WENO3) { why = "unknown filter"; return false; }
-  if (d->filter == OSB_FILTER_WENO3) {
+  if (d->filter != OSB_FILTER_NONE && d->filter != OSB_FILTER_WENO3 && d->filter != OSB_FILTER_TVD) {
+    why = "unknown filter";
+    return false;
+  }
+  if (d->filter != OSB_FILTER_NONE) {
     if (d->ndim != 3 || d->scheme != OSB_SCHEME_CENTRAL4 || d->metric[9]) {
-      why = "the WENO filter is implemented for 3D Cartesian blocks of the central scheme";
+      why = "the non-linear filters are implemented for 3D Cartesian blocks of the central scheme";
       return false;
     }
     for (int i = 0; i < 3; ++i)
       for (int s = 0; s < 2; ++s)
         if (d->bc[i][s] != OSB_BC_PERIODIC || d->size[i] < 4) {
-          why = "the WENO filter's halo exchange is the periodic one (all faces periodic, >= 4 points)";
+          why = "the filter's halo exchange is the periodic one (all faces periodic, >= 4 points)";
           return false;
         }
-    if (!(d->ducros_check >= 0.0) || !(d->ducros_select >= 0.0)) { why = "Ducros thresholds must be >= 0"; return false; }
+  }
+  if (d->filter == OSB_FILTER_WENO3 && (!(d->ducros_check >= 0.0) || !(d->ducros_select >= 0.0))) {
+    why = "Ducros thresholds must be >= 0";
+    return false;
+  }
+  if (d->filter == OSB_FILTER_TVD) {
+    if (!std::isfinite(d->tvd_kappa)) { why = "kappa_TVD must be finite"; return false; }
+    // the interface at -1 reads index -2, which the stage exchange must fill
+    for (int i = 0; i < 3; ++i)
+      for (int s = 0; s < 2; ++s)
+        if (d->bc_depth[i][s] > 0 && d->bc_depth[i][s] < 2) {
+          why = "the TVD filter needs a periodic exchange of depth >= 2";
+          return false;
+        }
   }
   return true;
 }
@@ -862,7 +886,7 @@ int osb_last_error(char* buf, size_t n) {
 }
 
 int osb_desc_layout(long long* out, int n) {
-  if (!out || n < 11) return fail(OSB_EINVAL, "need 11 slots");
+  if (!out || n < 12) return fail(OSB_EINVAL, "need 12 slots");
   out[0] = sizeof(osb_block_desc);
   out[1] = offsetof(osb_block_desc, size);
   out[2] = offsetof(osb_block_desc, bc);
@@ -874,6 +898,7 @@ int osb_desc_layout(long long* out, int n) {
   out[8] = offsetof(osb_block_desc, metric);
   out[9] = offsetof(osb_block_desc, split_form);
   out[10] = offsetof(osb_block_desc, ducros_check);
+  out[11] = offsetof(osb_block_desc, tvd_kappa);
   return OSB_OK;
 }
 
@@ -1032,8 +1057,9 @@ int osb_block_add(osb_ctx* c, const osb_block_desc* d, int* block_id) {
       return fail(OSB_ECUDA, "x-sweep row table: %s", cudaGetErrorString(e));
     }
   }
-  if (d->filter == OSB_FILTER_WENO3) {
-    // kappa (zero halos, written on the interior only) and the 15 filter-flux arrays
+  if (d->filter != OSB_FILTER_NONE) {
+    // WENO: kappa (zero halos, written on the interior only); TVD: the point -2 velocities;
+    // then the 15 filter-flux arrays
     const size_t bytes = (size_t)16 * k.alloc * (c->prec == OSB_PREC_FP32_RESIDUAL ? sizeof(float) : sizeof(double));
     cudaError_t e = cudaMalloc(&bl.filt_ws, bytes);
     if (e != cudaSuccess) {
@@ -1381,7 +1407,7 @@ extern "C" int osb_stage_noalloc(const osb_block_desc* d, int rk_kind, double A,
   for (int i = 0; i < 10; ++i)
     if (d->metric[i]) return fail(OSB_ENOTSUP, "osb_stage_noalloc takes Cartesian blocks only");
   if (d->filter != OSB_FILTER_NONE)
-    return fail(OSB_ENOTSUP, "the WENO filter follows a whole RK step (osb_step), not one stage");
+    return fail(OSB_ENOTSUP, "the non-linear filter follows a whole RK step (osb_step), not one stage");
   const int nv = d->ndim + 2;
   size_t alloc = 1;
   for (int i = 0; i < d->ndim; ++i) alloc *= (size_t)(d->size[i] + 2 * d->halo);

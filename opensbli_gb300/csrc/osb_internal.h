@@ -155,6 +155,10 @@ int resident_f32(osb_ctx* c, double dt, int nsteps);
 // Non-linear WENO filter step of a filtered block (osb_filter.cu), after a full RK step.
 int filter_f64(osb_ctx* c, Block& bl, double dt);
 int filter_f32(osb_ctx* c, Block& bl, double dt);
+// TVD filter: u at index -2 of each direction from the state the last RK stage reads (launched
+// before that stage)
+int tvd_stale_f64(osb_ctx* c, Block& bl);
+int tvd_stale_f32(osb_ctx* c, Block& bl);
 
 int central_f64(osb_ctx* c, Block& bl, bool conv, int first, const RkFuse* rf);
 int central_f32(osb_ctx* c, Block& bl, bool conv, int first, const RkFuse* rf);

@@ -86,6 +86,21 @@ def tgv_filtered(n=128, sizes=None, ducros=0.05):
     return spec, q
 
 
+def tgv_tvd(n=128, sizes=None, kappa=1.25):
+    """The supersonic TGV of the central branch of
+    apps/compressible_taylor_green_vortex/compressible_TGV.py with its TVD option
+    (``TVD = True``): M = 1.25, Re = 1600, central-4 KGP split convective terms, modified
+    Sutherland viscosity, periodic exchange of depth 2 after every stage, and the non-linear
+    characteristic TVD filter (filters/TVD_filter.py) after every step with strength
+    kappa_TVD = `kappa` (1.25 in apps/turbulent_counter_flow)."""
+    spec, q = tgv(n, minf=1.25, scheme=abi.SCHEME_CENTRAL4, viscous=abi.VISC_SUTHERLAND, sizes=sizes)
+    spec.split_form = abi.SPLIT_KGP
+    spec.filter = abi.FILTER_TVD
+    spec.tvd_kappa = kappa
+    spec.bc_depth = [[2, 2] for _ in range(3)]
+    return spec, q
+
+
 def filtered_dt(n):
     """Time step of the Central4-WENO5 benchmark's strong-scaling mode (opensbli.cpp:63)."""
     return 0.00084625 * 256 / n

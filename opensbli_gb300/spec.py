@@ -39,6 +39,7 @@ class BlockSpec:
     filter: int = abi.FILTER_NONE
     ducros_check: float = 0.05
     ducros_select: float = 0.05
+    tvd_kappa: float = 1.0
 
     def __post_init__(self):
         self.size = tuple(int(s) for s in self.size)

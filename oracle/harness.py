@@ -105,11 +105,14 @@ class OracleBlocks:
     def step(self, rk_kind, A, B, dt, nsteps):
         Aa = (ctypes.c_double * len(A))(*A)
         Bb = (ctypes.c_double * len(B))(*B)
-        oracle().oracle_step(self.desc, len(self.specs), rk_kind, len(A), Aa, Bb, dt, nsteps)
+        if oracle().oracle_step(self.desc, len(self.specs), rk_kind, len(A), Aa, Bb, dt, nsteps):
+            raise RuntimeError("oracle_step refused the blocks")
 
     def filter(self, dt):
-        """The WENO filter step of the filtered blocks (halos must be filled)."""
-        oracle().oracle_filter(self.desc, len(self.specs), dt)
+        """The filter step of the filtered blocks (halos must be filled; the TVD filter takes
+        its point -2 velocities from the current state)."""
+        if oracle().oracle_filter(self.desc, len(self.specs), dt):
+            raise RuntimeError("oracle_filter refused the blocks")
 
     def reduce(self, what):
         out = ctypes.c_double()

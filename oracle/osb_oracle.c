@@ -26,6 +26,8 @@
  *  - Kennedy-Gruber-Pirozzoli central convective terms             (physical_models/split_forms.py:178-236)
  *  - non-linear characteristic WENO3 filter with a Ducros sensor    (filters/WENO_filter.py; generated
  *    kernels of apps/performance_benchmark/Central4-WENO5/opensbliblock00_kernels.h:572-2480)
+ *  - non-linear characteristic TVD filter (Yee-Sandham-Djomehri)   (filters/TVD_filter.py,
+ *    schemes/spatial/shock_capturing.py:619-766)
  *  - low-storage RK3 (rk_LS.py:185-215) and SBLI RK3 (rk_sbli.py:138-154)
  *  - periodic exchange (periodic.py:53-71, opsc.py:1026-1064), zero-gradient
  *    (zero_gradient_outlet.py:11-23), block interfaces (multi_block.py:48-107)
@@ -919,11 +921,8 @@ static void filter_halos(osb_block_desc* b, const geom_t* g) {
     }
 }
 
-int oracle_filter(osb_block_desc* blocks, int nblocks, double dt) {
-  for (int ib = 0; ib < nblocks; ++ib) {
-    osb_block_desc* b = &blocks[ib];
-    if (b->filter != OSB_FILTER_WENO3) continue;
-    if (b->ndim != 3) return -1;
+static void weno_filter_block(osb_block_desc* b, double dt) {
+  {
     geom_t g = geom_of(b);
     const int nv = 5;
     long n = npts_alloc(&g);
@@ -976,8 +975,221 @@ int oracle_filter(osb_block_desc* blocks, int nblocks, double dt) {
     free(kappa);
     cr_free(&c);
   }
+}
+
+/* ---- non-linear TVD filter (filters/TVD_filter.py) ------------------------------------------
+ * The Yee-Sandham-Djomehri characteristic filter of schemes/spatial/shock_capturing.py:619-766
+ * with Harten's switch, applied after every full RK step as the generated solver of the TGV
+ * app's TVD branch runs it (apps/compressible_taylor_green_vortex/compressible_TGV.py:210-222;
+ * kernels "Constituent Relations evaluation", "TVD reconstruction direction d" and
+ * "Non-linear TVD Filter application"): the filter's exchange (filter_halos), u and a on
+ * [-1, N+2) of every direction, per direction the flux at interfaces i+1/2, i = -1..N-1, then
+ * q += dt * (-(F_0(i) - F_0(i-1)) / Delta_0 - (F_2 ..) / Delta_2 - (F_1 ..) / Delta_1).
+ * The interface at -1 reads point -2 of the sweep direction, outside that constituent range:
+ * there a keeps its zero initial value and u the value the last RK stage's constituent
+ * relations left (rhou / rho of the state at the start of that stage), passed in as stale. */
+
+typedef struct {
+  double r, m[3], e, u[3], a; /* local frame: m[0], u[0] normal, then the two transverse */
+} tvd_pt;
+
+/* Entropy fix of a wave speed, delta_TVD = 0.5 (shock_capturing.py:681-689). */
+static double tvd_psi(double z) {
+  const double idl = 1.0 / 0.5; /* invdelta_TVD */
+  return fabs(z) >= 1.0 / idl ? fabs(z) : (1.0 / 2.0) * (1.0 / (idl * idl) + z * z) * idl;
+}
+
+/* Limiter g from the jumps hi (this interface) and lo (the one below) (lines 690-704). */
+static double tvd_g(double hi, double lo) {
+  const double S = hi > 0 ? 1.0 : (hi < 0 ? -1.0 : 0.0);
+  const double t1 = fmax(0.0, fmin(S * lo, 2 * fabs(hi)));
+  const double t2 = fmin(fabs(hi), 2 * S * lo);
+  return S * fmax(t1, t2);
+}
+
+/* Filter flux at interface i+1/2 from points w[0..3] = i-1..i+2 (local frame), in the
+ * operation order of the generated direction-0 kernel: simple averages over (i-1, i), (i, i+1),
+ * (i+1, i+2), alpha = LEV (q_hi - q_lo) at each, wave speeds and REV at i+1/2, sigma, g,
+ * gamma, phi, Harten's theta, phi* = kappa theta phi, F = 1/2 REV phi*. */
+static void tvd_flux(double gm, double kappa, const tvd_pt* w, double* fh) {
+  const double g1 = -1 + gm, eps = 1.0e-8;
+  const double c1 = 0.35355339059327373, c2 = 0.70710678118654746;
+  double al[5][3], ws[5] = {0, 0, 0, 0, 0}, R[5][5];
+  memset(R, 0, sizeof(R));
+  for (int jb = 0; jb < 3; ++jb) {
+    const tvd_pt* lo = &w[jb];
+    const tvd_pt* hi = &w[jb + 1];
+    const double u0 = (1.0 / 2.0) * (lo->u[0] + hi->u[0]), u1 = (1.0 / 2.0) * (lo->u[1] + hi->u[1]),
+                 u2 = (1.0 / 2.0) * (lo->u[2] + hi->u[2]), a = (1.0 / 2.0) * (lo->a + hi->a),
+                 rho = (1.0 / 2.0) * (lo->r + hi->r);
+    const double ia = 1.0 / a, ir = 1.0 / rho, ia2 = ia * ia;
+    const double L00 = -(1.0 / 2.0) * (-2 - (u0 * u0) * ia2 - (u1 * u1) * ia2 - (u2 * u2) * ia2 + (u0 * u0) * ia2 * gm +
+                                        (u1 * u1) * ia2 * gm + (u2 * u2) * ia2 * gm);
+    const double L01 = ia2 * g1 * u0, L02 = ia2 * g1 * u1, L03 = ia2 * g1 * u2, L04 = -ia2 * g1;
+    const double L10 = -u2 * ir, L13 = ir, L20 = u1 * ir, L22 = -ir;
+    const double kq = -(u0 * u0) * ia - (u1 * u1) * ia - (u2 * u2) * ia;
+    const double L30 = c1 * (-2 * u0 + kq + (u0 * u0) * gm * ia + (u1 * u1) * gm * ia + (u2 * u2) * gm * ia) * ir;
+    const double L40 = c1 * (2 * u0 + kq + (u0 * u0) * gm * ia + (u1 * u1) * gm * ia + (u2 * u2) * gm * ia) * ir;
+    const double L31 = -c2 * (-1 - u0 * ia + gm * u0 * ia) * ir, L41 = -c2 * (1 - u0 * ia + gm * u0 * ia) * ir;
+    const double L32 = -c2 * g1 * u1 * ia * ir, L33 = -c2 * g1 * u2 * ia * ir, L34 = c2 * g1 * ia * ir;
+    const double dr = -lo->r + hi->r, d0 = -lo->m[0] + hi->m[0], d1 = -lo->m[1] + hi->m[1],
+                 d2 = -lo->m[2] + hi->m[2], de = -lo->e + hi->e;
+    al[0][jb] = dr * L00 + de * L04 + d0 * L01 + d1 * L02 + d2 * L03;
+    al[1][jb] = dr * L10 + d2 * L13;
+    al[2][jb] = dr * L20 + d1 * L22;
+    al[3][jb] = dr * L30 + de * L34 + d0 * L31 + d1 * L32 + d2 * L33;
+    al[4][jb] = dr * L40 + de * L34 + d0 * L41 + d1 * L32 + d2 * L33;
+    if (jb == 1) {
+      ws[0] = ws[1] = ws[2] = u0;
+      ws[3] = a + u0;
+      ws[4] = -a + u0;
+      R[0][0] = 1;
+      R[0][3] = R[0][4] = c2 * rho * ia;
+      R[1][0] = u0;
+      R[1][3] = c2 * (a + u0) * rho * ia;
+      R[1][4] = c2 * (-a + u0) * rho * ia;
+      R[2][0] = u1;
+      R[2][2] = -rho;
+      R[2][3] = R[2][4] = c2 * rho * u1 * ia;
+      R[3][0] = u2;
+      R[3][1] = rho;
+      R[3][3] = R[3][4] = c2 * rho * u2 * ia;
+      R[4][0] = (1.0 / 2.0) * (u0 * u0) + (1.0 / 2.0) * (u1 * u1) + (1.0 / 2.0) * (u2 * u2);
+      R[4][1] = rho * u2;
+      R[4][2] = -rho * u1;
+      const double hq = ((a * a) + (1.0 / 2.0) * (1 - 1 + g1) * ((u0 * u0) + (u1 * u1) + (u2 * u2))) / (1 - 1 + g1);
+      R[4][3] = c2 * (hq + a * u0) * rho * ia;
+      R[4][4] = c2 * (hq - a * u0) * rho * ia;
+    }
+  }
+  double ps[5];
+  for (int k = 0; k < 5; ++k) {
+    const double s0 = tvd_psi(ws[k]);
+    const double g0 = tvd_g(al[k][1], al[k][0]), gg1 = tvd_g(al[k][2], al[k][1]);
+    const double gam = al[k][1] == 0 ? 0 : (-g0 + gg1) * al[k][1] * s0 / ((al[k][1] * al[k][1]) + eps);
+    const double s1 = tvd_psi(gam);
+    const double phi = -fabs(s0 + s1) * al[k][1] + 0.5 * (g0 + gg1) * s0;
+    double t1 = -fabs(al[k][0]) + fabs(al[k][1]), t2 = fabs(al[k][0]) + fabs(al[k][1]) + eps;
+    const double th0 = fabs(t1 / t2) * fabs(t1 / t2);
+    t1 = -fabs(al[k][1]) + fabs(al[k][2]);
+    t2 = fabs(al[k][1]) + fabs(al[k][2]) + eps;
+    const double th1 = fabs(t1 / t2) * fabs(t1 / t2);
+    ps[k] = kappa * phi * fmax(th0, th1);
+  }
+  fh[0] = 0.5 * R[0][0] * ps[0] + 0.5 * R[0][3] * ps[3] + 0.5 * R[0][4] * ps[4];
+  fh[1] = 0.5 * R[1][0] * ps[0] + 0.5 * R[1][3] * ps[3] + 0.5 * R[1][4] * ps[4];
+  fh[2] = 0.5 * R[2][0] * ps[0] + 0.5 * R[2][2] * ps[2] + 0.5 * R[2][3] * ps[3] + 0.5 * R[2][4] * ps[4];
+  fh[3] = 0.5 * R[3][0] * ps[0] + 0.5 * R[3][1] * ps[1] + 0.5 * R[3][3] * ps[3] + 0.5 * R[3][4] * ps[4];
+  fh[4] = 0.5 * R[4][0] * ps[0] + 0.5 * R[4][1] * ps[1] + 0.5 * R[4][2] * ps[2] + 0.5 * R[4][3] * ps[3] +
+          0.5 * R[4][4] * ps[4];
+}
+
+/* u at index -2 of each direction (the other two interior): rhou / rho of the current state,
+ * one array per velocity component over the whole allocation (only those faces are set). */
+static void tvd_stale_capture(const osb_block_desc* b, const geom_t* g, double* const* st) {
+  for (int d = 0; d < 3; ++d) {
+    int lo[3] = {0, 0, 0}, hi[3] = {g->n[0], g->n[1], g->n[2]};
+    lo[d] = -2;
+    hi[d] = -1;
+    for (int k = lo[2]; k < hi[2]; ++k)
+      for (int j = lo[1]; j < hi[1]; ++j)
+        for (int i = lo[0]; i < hi[0]; ++i) {
+          long id = gid(g, i, j, k);
+          for (int c = 0; c < 3; ++c) st[c][id] = b->q[1 + c][id] / b->q[0][id];
+        }
+  }
+}
+
+static void tvd_filter_block(osb_block_desc* b, double dt, double* const* stale) {
+  geom_t g = geom_of(b);
+  const int nv = 5;
+  const double gm = b->gama;
+  filter_halos(b, &g);
+  double* F[3][NVMAX];
+  for (int d = 0; d < 3; ++d)
+    for (int v = 0; v < nv; ++v) F[d][v] = alloc_like(&g);
+  for (int d = 0; d < 3; ++d) {
+    const int t1 = (d + 1) % 3, t2 = (d + 2) % 3;
+    int lo[3] = {0, 0, 0};
+    lo[d] = -1;
+    for (int k = lo[2]; k < g.n[2]; ++k)
+      for (int j = lo[1]; j < g.n[1]; ++j)
+        for (int i = lo[0]; i < g.n[0]; ++i) {
+          const long id = gid(&g, i, j, k);
+          const int cd = d == 0 ? i : (d == 1 ? j : k);
+          tvd_pt w[4];
+          for (int m = 0; m < 4; ++m) {
+            const long p = id + (long)(m - 1) * g.st[d];
+            const int comp[3] = {d, t1, t2};
+            tvd_pt* s = &w[m];
+            s->r = b->q[0][p];
+            s->e = b->q[4][p];
+            for (int c = 0; c < 3; ++c) s->m[c] = b->q[1 + comp[c]][p];
+            if (cd + m - 1 == -2) {
+              for (int c = 0; c < 3; ++c) s->u[c] = stale[comp[c]][p];
+              s->a = 0.0;
+            } else {
+              /* "Constituent Relations evaluation" of the filter */
+              const double inv_rho = 1.0 / b->q[0][p];
+              for (int c = 0; c < 3; ++c) s->u[c] = b->q[1 + comp[c]][p] * inv_rho;
+              const double p_ = (-1 + gm) * (-(0.5 * (b->q[1][p] * b->q[1][p]) + 0.5 * (b->q[2][p] * b->q[2][p]) +
+                                               0.5 * (b->q[3][p] * b->q[3][p])) * inv_rho + b->q[4][p]);
+              s->a = sqrt(gm * p_ * inv_rho);
+            }
+          }
+          double f[5];
+          tvd_flux(gm, b->tvd_kappa, w, f);
+          F[d][0][id] = f[0];
+          F[d][1 + d][id] = f[1];
+          F[d][1 + t1][id] = f[2];
+          F[d][1 + t2][id] = f[3];
+          F[d][4][id] = f[4];
+        }
+  }
+  const double i0 = 1.0 / b->delta[0], i1 = 1.0 / b->delta[1], i2 = 1.0 / b->delta[2];
+  for (int k = 0; k < g.n[2]; ++k)
+    for (int j = 0; j < g.n[1]; ++j)
+      for (int i = 0; i < g.n[0]; ++i) {
+        const long id = gid(&g, i, j, k);
+        const long sx = g.st[0], sy = g.st[1], sz = g.st[2];
+        for (int v = 0; v < nv; ++v) {
+          const double* f0 = F[0][v];
+          const double* f1 = F[1][v];
+          const double* f2 = F[2][v];
+          b->q[v][id] = (-(-f0[id - sx] + f0[id]) * i0 - (-f2[id - sz] + f2[id]) * i2 - (-f1[id - sy] + f1[id]) * i1 * 1.0) *
+                            dt + b->q[v][id];
+        }
+      }
+  for (int d = 0; d < 3; ++d)
+    for (int v = 0; v < nv; ++v) free(F[d][v]);
+}
+
+/* The filter step of every filtered block.  stale: per block three velocity arrays for the TVD
+ * filter's point -2 (NULL: taken from the current state). */
+static int filter_impl(osb_block_desc* blocks, int nblocks, double dt, double* const* const* stale) {
+  for (int ib = 0; ib < nblocks; ++ib) {
+    osb_block_desc* b = &blocks[ib];
+    if (b->filter == OSB_FILTER_NONE) continue;
+    if (b->ndim != 3) return -1;
+    if (b->filter == OSB_FILTER_WENO3) {
+      weno_filter_block(b, dt);
+    } else if (b->filter == OSB_FILTER_TVD) {
+      geom_t g = geom_of(b);
+      double* own[3] = {NULL, NULL, NULL};
+      if (!stale || !stale[ib]) {
+        for (int c = 0; c < 3; ++c) own[c] = alloc_like(&g);
+        tvd_stale_capture(b, &g, own);
+      }
+      tvd_filter_block(b, dt, (stale && stale[ib]) ? stale[ib] : own);
+      for (int c = 0; c < 3; ++c) free(own[c]);
+    } else {
+      return -1;
+    }
+  }
   return 0;
 }
+
+int oracle_filter(osb_block_desc* blocks, int nblocks, double dt) { return filter_impl(blocks, nblocks, dt, NULL); }
 
 /* ---- boundary conditions ---------------------------------------------------------------- */
 
@@ -1162,6 +1374,8 @@ static int stage_impl(osb_block_desc* blocks, int nblocks, int rk_kind, const do
   return 0;
 }
 
+#define OSB_MAX_BLOCKS_ORACLE 64
+
 int oracle_step(osb_block_desc* blocks, int nblocks, int rk_kind, int nstages, const double* A, const double* B,
                 double dt, int nsteps) {
   for (int it = 0; it < nsteps; ++it) {
@@ -1179,13 +1393,35 @@ int oracle_step(osb_block_desc* blocks, int nblocks, int rk_kind, int nstages, c
               }
       }
     }
-    /* with a filtered block the generated step exchanges no halos after the last stage: the
-     * filter's own exchange (filter_halos) follows it */
-    int filtered = 0;
-    for (int ib = 0; ib < nblocks; ++ib) filtered |= blocks[ib].filter == OSB_FILTER_WENO3;
-    for (int s = 0; s < nstages; ++s)
-      stage_impl(blocks, nblocks, rk_kind, A, B, s, dt, !(filtered && s == nstages - 1));
-    if (filtered && oracle_filter(blocks, nblocks, dt)) return -1;
+    /* with a WENO-filtered block the generated step (the shipped Central4-WENO5 solver)
+     * exchanges no halos after the last stage: the filter's own exchange (filter_halos)
+     * follows it; the TVD-filtered solver exchanges after every stage */
+    int weno = 0, tvd = 0;
+    for (int ib = 0; ib < nblocks; ++ib) {
+      weno |= blocks[ib].filter == OSB_FILTER_WENO3;
+      tvd |= blocks[ib].filter == OSB_FILTER_TVD;
+    }
+    if (tvd && nblocks > OSB_MAX_BLOCKS_ORACLE) return -1;
+    double** stale[OSB_MAX_BLOCKS_ORACLE];
+    for (int ib = 0; ib < nblocks && ib < OSB_MAX_BLOCKS_ORACLE; ++ib) stale[ib] = NULL;
+    for (int s = 0; s < nstages; ++s) {
+      if (tvd && s == nstages - 1)
+        for (int ib = 0; ib < nblocks && ib < OSB_MAX_BLOCKS_ORACLE; ++ib) {
+          if (blocks[ib].filter != OSB_FILTER_TVD) continue;
+          geom_t g = geom_of(&blocks[ib]);
+          stale[ib] = (double**)malloc(3 * sizeof(double*));
+          for (int c = 0; c < 3; ++c) stale[ib][c] = alloc_like(&g);
+          tvd_stale_capture(&blocks[ib], &g, stale[ib]);
+        }
+      stage_impl(blocks, nblocks, rk_kind, A, B, s, dt, !(weno && s == nstages - 1));
+    }
+    int rc = (weno || tvd) ? filter_impl(blocks, nblocks, dt, (double* const* const*)stale) : 0;
+    for (int ib = 0; ib < nblocks && ib < OSB_MAX_BLOCKS_ORACLE; ++ib)
+      if (stale[ib]) {
+        for (int c = 0; c < 3; ++c) free(stale[ib][c]);
+        free(stale[ib]);
+      }
+    if (rc) return -1;
   }
   return 0;
 }

@@ -281,12 +281,13 @@ def case_tgv_central():
     return block, _tgv_params(0.1, 16, "0.003385")
 
 
-def central_split_block(form, energy_formulation="none"):
+def central_split_block(form, energy_formulation="none", extra=None):
     """3D supersonic TGV block with the central 4th-order scheme and the convective split form
     `form` of physical_models/split_forms.py (NS_Split), modified Sutherland viscosity
     (StoreSome), RK-LS3, periodic -- the central branch of
-    ``apps/compressible_taylor_green_vortex/compressible_TGV.py:66-75, 128-160`` without the
-    filter step."""
+    ``apps/compressible_taylor_green_vortex/compressible_TGV.py:66-75, 128-160``.  extra(block),
+    when given, adds a filter's equation classes before discretisation and returns the filter,
+    whose periodic exchange of depth 4 is then added after it (that app's lines 210-222)."""
     import copy
     from opensbli import NS_Split, SimulationEquations, StoreSome, RungeKuttaLS, PeriodicBC
     ndim = 3
@@ -310,8 +311,30 @@ def central_split_block(form, energy_formulation="none"):
         bcs += [PeriodicBC(d, 0, halos=[-2, 2]), PeriodicBC(d, 1, halos=[-2, 2])]
     block.set_block_boundaries(bcs)
     block.set_equations([copy.deepcopy(cr), copy.deepcopy(sim), initial])
+    filt = extra(block) if extra else None
     block.discretise()
+    if filt is not None:
+        filt.update_periodic_boundary(block, halos=[-4, 4])
     return block, _tgv_params(1.25, 16, "0.001")
+
+
+def case_tgv_kgp_tvd():
+    """The central KGP TGV of central_split_block followed, after every full RK step, by the
+    non-linear characteristic TVD filter (``filters/TVD_filter.py``; Yee-Sandham-Djomehri
+    limiter of ``schemes/spatial/shock_capturing.py:619-766``) with its periodic exchange of
+    depth 4 -- the ``TVD = True`` branch of
+    ``apps/compressible_taylor_green_vortex/compressible_TGV.py:210-222``.  The filter's
+    strength kappa_TVD is a run parameter (OSB_KAPPA_TVD)."""
+    from opensbli import TVDFilter
+
+    def with_filter(blk):
+        wf = TVDFilter(blk, airfoil=False)
+        blk.set_equations(wf.equation_classes)
+        return wf
+
+    block, params = central_split_block("KGP", "enthalpy", extra=with_filter)
+    params["kappa_TVD"] = 'osb_env_double("OSB_KAPPA_TVD", 1.0)'
+    return block, params
 
 
 def case_kh_weno5z():
@@ -431,6 +454,7 @@ CASES = {
     "tgv_teno6": lambda: case_tgv_shock("teno6"),
     "tgv_central": case_tgv_central,
     "tgv_kgp": lambda: central_split_block("KGP", "enthalpy"),
+    "tgv_kgp_tvd": case_tgv_kgp_tvd,
     "kh_weno5z": case_kh_weno5z,
     "curv_weno5z": case_curv_weno5z,
 }

@@ -6,6 +6,7 @@ output of the reference solver (OPS C++ generated by OpenSBLI, compiled with
 oracle/ops_compat.h), interior points only, FP64, as a compressed .npz:
 
     python tests/golden/make_golden.py            # all cases
+    python tests/golden/make_golden.py tvd        # the TVD-filtered TGV
 """
 import os
 import subprocess
@@ -117,7 +118,35 @@ def make_shipped_c4w5(n=16, steps=(1, 2, 5)):
     print("wrote shipped_c4w5_%d" % n)
 
 
+def make_tvd(n=12, steps=(1, 2, 4), dt=2e-3, kappa=1.25, pert=(2e-2, 5)):
+    """Golden states of the generated solver of the TGV app's TVD branch (reference case
+    tgv_kgp_tvd: central KGP + Sutherland viscous terms, RK-LS3, TVD filter after every step),
+    dumped at exit after whole steps, from a perturbed TGV state."""
+    spec, q = problems.tgv_tvd(n, kappa=kappa)
+    q = perturb(q, *pert)
+    ob = harness.OracleBlocks([(spec, q)])
+    ob.apply_bc()
+    names = harness.state_names(3)
+    init = {nm: ob.q[0][v] for v, nm in enumerate(names)}
+    sl = spec.interior()
+    out = {"ic": np.stack([ob.q[0][v][sl] for v in range(5)]), "dt": dt, "kappa": kappa,
+           "steps": np.array(steps), "pert": np.array(pert)}
+    for c in steps:
+        env = {"OSB_NP0": n, "OSB_NP1": n, "OSB_NP2": n, "OSB_DT": repr(dt), "OSB_NITER": c,
+               "OSB_KAPPA_TVD": repr(kappa)}
+        r = harness.run_ref("tgv_kgp_tvd", env=env, init=init)
+        out["after_%d" % c] = np.stack([r[nm][sl] for nm in names])
+    name = "tgv_kgp_tvd_%d_perturbed" % n
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    print("wrote", name)
+
+
 def main():
+    if sys.argv[1:] == ["tvd"]:
+        if not harness.ref_available("tgv_kgp_tvd"):
+            subprocess.check_call([sys.executable, os.path.join(ROOT, "oracle", "ref_generate.py"), "tgv_kgp_tvd"])
+        make_tvd()
+        return
     if sys.argv[1:] == ["shipped_teno6"]:
         make_shipped_teno6()
         return

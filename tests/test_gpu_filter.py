@@ -115,3 +115,88 @@ def test_filter_descriptor_checks(built_lib):
     spec.split_form = abi.SPLIT_KGP
     with pytest.raises(abi.OSBError):
         Solver([(spec, q)], precision="fp64", rk="ls3")
+
+
+# ---- non-linear TVD filter (filters/TVD_filter.py) ----------------------------------------
+
+def _tvd_golden():
+    """The perturbed TGV and the golden states of the reference's generated TVD-filtered solver
+    (tests/golden/make_golden.py make_tvd)."""
+    g = np.load(os.path.join(GOLD, "tgv_kgp_tvd_12_perturbed.npz"))
+    spec, q = problems.tgv_tvd(12, kappa=float(g["kappa"]))
+    amp, seed = g["pert"]
+    rng = np.random.default_rng(int(seed))
+    q = [a * (1.0 + float(amp) * rng.standard_normal(a.shape)) for a in q]
+    return spec, q, g
+
+
+@pytest.mark.parametrize("steps", [1, 2, 4])
+def test_tvd_filtered_steps_match_reference_fp64(built_lib, steps):
+    """Whole TVD-filtered steps on the GPU (KGP central step, the filter's exchange, the point -2
+    velocities of the last stage, the three flux directions, the update) against the
+    reference's own generated solver, FP64: 1e-12 of each field's scale.  The filter moves the
+    state by about 2e-3 of its scale per step here."""
+    spec, q, g = _tvd_golden()
+    s = _solver([(spec, q)], precision="fp64", rk="ls3")
+    s.apply_bc()
+    s.step(float(g["dt"]), steps)
+    got = s.state(0)
+    s.close()
+    sl = spec.interior()
+    errs = [harness.rel_err(got[v][sl], g["after_%d" % steps][v]) for v in range(5)]
+    assert max(errs) < 1e-12, errs
+
+
+def test_tvd_filtered_steps_match_oracle_anisotropic_fp64(built_lib, oracle_lib):
+    """A non-cubic TVD-filtered block, 3 steps with CUDA graphs, FP64 against the oracle: 1e-12."""
+    spec, q = problems.tgv_tvd(sizes=(18, 16, 14), kappa=1.25)
+    rng = np.random.default_rng(3)
+    q = [a * (1.0 + 1e-2 * rng.standard_normal(a.shape)) for a in q]
+    dt = 4e-3
+    s = _solver([(spec, q)], precision="fp64", rk="ls3")
+    s.apply_bc()
+    s.step(dt, 3)
+    got = s.state(0)
+    s.close()
+    ob = harness.OracleBlocks([(spec, q)])
+    ob.apply_bc()
+    ob.step(abi.RK_LOW_STORAGE, problems.RK3_LS_A, problems.RK3_LS_B, dt, 3)
+    sl = spec.interior()
+    errs = [harness.rel_err(got[v][sl], ob.q[0][v][sl]) for v in range(5)]
+    assert max(errs) < 1e-12, errs
+
+
+def test_tvd_filtered_steps_fp32_residual(built_lib):
+    """FP32-residual path (FP32 central terms, FP32 TVD filter increment added to the FP64
+    state) against the reference's 4-step state: 1e-5 of each field's scale (the momentum
+    components against the momentum scale), 200x below the filter's own effect."""
+    spec, q, g = _tvd_golden()
+    s = _solver([(spec, q)], precision="fp32", rk="ls3")
+    s.apply_bc()
+    s.step(float(g["dt"]), 4)
+    got = s.state(0)
+    s.close()
+    sl = spec.interior()
+    ref = g["after_4"]
+    mscale = max(float(np.max(np.abs(ref[v]))) for v in (1, 2, 3))
+    errs = []
+    for v in range(5):
+        scale = mscale if v in (1, 2, 3) else float(np.max(np.abs(ref[v])))
+        errs.append(float(np.max(np.abs(got[v][sl] - ref[v]))) / scale)
+    assert max(errs) < 1e-5, errs
+
+
+def test_tvd_descriptor_checks(built_lib):
+    """The TVD filter is refused outside its path: a shock-capturing block, a stage exchange
+    shallower than the point -2 it reads, a non-finite kappa_TVD."""
+    spec, q = problems.tgv(12, minf=1.25, scheme=abi.SCHEME_TENO5, averaging=abi.AVG_ROE)
+    spec.filter = abi.FILTER_TVD
+    with pytest.raises(abi.OSBError):
+        _solver([(spec, q)], precision="fp64", rk="ls3")
+    spec, q = problems.tgv_tvd(12)
+    spec.bc_depth = [[1, 1] for _ in range(3)]
+    with pytest.raises(abi.OSBError):
+        _solver([(spec, q)], precision="fp64", rk="ls3")
+    spec, q = problems.tgv_tvd(12, kappa=float("nan"))
+    with pytest.raises(abi.OSBError):
+        _solver([(spec, q)], precision="fp64", rk="ls3")

@@ -173,3 +173,60 @@ def test_kgp_differs_from_feiereisen(oracle_lib):
     r_f = ob2.residual(0)
     sl = spec.interior()
     assert harness.rel_err(r_kgp[0][sl], r_f[0][sl]) > 1e-3
+
+
+def tvd_case():
+    """The TVD-filtered TGV of tests/golden/make_golden.py make_tvd: the perturbed initial
+    state and the golden states of the reference's generated solver."""
+    g = np.load(os.path.join(GOLD, "tgv_kgp_tvd_12_perturbed.npz"))
+    spec, q = problems.tgv_tvd(12, kappa=float(g["kappa"]))
+    amp, seed = g["pert"]
+    return spec, perturb(q, float(amp), int(seed)), g
+
+
+def test_oracle_matches_reference_tvd_filter(oracle_lib):
+    """The oracle's non-linear TVD filter (with the KGP central step before it) against the
+    reference's own generated solver of the TGV app's TVD branch (oracle/ref_generate.py case
+    tgv_kgp_tvd, compiled with oracle/ops_compat.h), after 1, 2 and 4 whole filtered steps from a
+    perturbed state: 1e-13 of each field's scale.  The filter moves the state by about 2e-3 of
+    its scale per step here, so the comparison sees it (an unfiltered step misses by 1e-3)."""
+    spec, q, g = tvd_case()
+    dt = float(g["dt"])
+    sl = spec.interior()
+    ob = harness.OracleBlocks([(spec, q)])
+    ob.apply_bc()
+    assert np.array_equal(np.stack([ob.q[0][v][sl] for v in range(5)]), g["ic"])
+    for n in g["steps"]:
+        ob = harness.OracleBlocks([(spec, q)])
+        ob.apply_bc()
+        ob.step(abi.RK_LOW_STORAGE, problems.RK3_LS_A, problems.RK3_LS_B, dt, int(n))
+        ref = g["after_%d" % int(n)]
+        errs = [harness.rel_err(ob.q[0][v][sl], ref[v]) for v in range(spec.nvars)]
+        assert max(errs) < 1e-13, (int(n), errs)
+    # the filter is active: the same step without it is far from the reference
+    spec.filter = abi.FILTER_NONE
+    ob = harness.OracleBlocks([(spec, q)])
+    ob.apply_bc()
+    ob.step(abi.RK_LOW_STORAGE, problems.RK3_LS_A, problems.RK3_LS_B, dt, 1)
+    assert max(harness.rel_err(ob.q[0][v][sl], g["after_1"][v]) for v in range(5)) > 1e-4
+
+
+def test_tvd_filter_stale_point_matters(oracle_lib):
+    """The generated filter reads u at index -2 left by the last RK stage and a = 0 there; a
+    filter that recomputes them from the current state differs from the reference on the planes
+    next to the low boundaries (the oracle's standalone filter call takes the current state)."""
+    spec, q, g = tvd_case()
+    dt = float(g["dt"])
+    sl = spec.interior()
+    ob = harness.OracleBlocks([(spec, q)])
+    ob.apply_bc()
+    ob.step(abi.RK_LOW_STORAGE, problems.RK3_LS_A, problems.RK3_LS_B, dt, 1)
+    spec.filter = abi.FILTER_NONE
+    o2 = harness.OracleBlocks([(spec, q)])
+    o2.apply_bc()
+    o2.step(abi.RK_LOW_STORAGE, problems.RK3_LS_A, problems.RK3_LS_B, dt, 1)
+    o2.desc[0].filter = abi.FILTER_TVD
+    o2.filter(dt)
+    d = np.abs(ob.q[0][0][sl] - o2.q[0][0][sl])
+    assert d[:, :, 0].max() > 1e-8          # x = 0 plane: different
+    assert d[2:, 2:, 2:].max() < 1e-13      # away from the low planes: the same
