@@ -224,17 +224,54 @@ def _split_form_of(block):
                               "energy formulation are); continuity uses %s, energy %s" % (sorted(m), sorted(en)))
 
 
+# Kernel names the non-linear filters give their equation classes (filters/TVD_filter.py:66,
+# 91, 142; filters/WENO_filter.py:301-351, 468, 503, 555).
+_TVD_KERNELS = ("TVD reconstruction direction", "Non-linear TVD Filter application")
+_WENO_FILTER_KERNELS = ("WENO reconstruction direction", "Non-linear filter application")
+
+
+def _kernel_names(ec):
+    return [str(getattr(k, "computation_name", "")) for k in getattr(ec, "Kernels", [])]
+
+
+def _filter_of(block, p):
+    """(OSB_FILTER_*, kappa_TVD) of the non-linear filter whose equation classes the block
+    carries.  The TVD filter of filters/TVD_filter.py without its hybrid sensor
+    (optimize=False, the TGV app's TVD branch) maps onto OSB_FILTER_TVD with the run's
+    kappa_TVD; its sensor variant and the WENO filter fail loudly here (the WENO filter's
+    Central4-WENO5 form is reached through BlockSpec, problems.tgv_filtered)."""
+    names = [n for ec in block.list_of_equation_classes for n in _kernel_names(ec)]
+    tvd = any(any(t in n for t in _TVD_KERNELS) for n in names)
+    weno = any(any(t in n for t in _WENO_FILTER_KERNELS) for n in names)
+    if weno:
+        raise NotImplementedError("the WENO filter of filters/WENO_filter.py is not mapped by the backend; "
+                                  "its Central4-WENO5 form is reached through BlockSpec (problems.tgv_filtered)")
+    if not tvd:
+        return abi.FILTER_NONE, 1.0
+    if any("Shock sensor" in n for n in names):
+        raise NotImplementedError("the TVD filter with its Ducros sensor (TVDFilter(optimize=True)) is not "
+                                  "implemented; the unsensored filter is")
+    for name, fixed in (("delta_TVD", 0.5), ("eps_TVD", 1.0e-8)):
+        if name in p and float(p[name]) != fixed:
+            raise NotImplementedError("%s = %s: the TVD filter is implemented for the generator's %s" % (
+                name, p[name], fixed))
+    return abi.FILTER_TVD, float(_const_value("kappa_TVD", p))
+
+
 def _check_equation_classes(block):
-    """Fail loudly on equation classes the GB300 path does not run (explicit / non-linear
-    filters and others), instead of ignoring them."""
+    """Fail loudly on equation classes the GB300 path does not run (explicit filters and
+    others), instead of ignoring them.  The non-linear filters' own classes are recognised by
+    _filter_of."""
     from opensbli import SimulationEquations, ConstituentRelations, GridBasedInitialisation
     allowed = (SimulationEquations, ConstituentRelations, GridBasedInitialisation)
     for ec in block.list_of_equation_classes:
         if isinstance(ec, allowed):
             continue
         name = type(ec).__name__
-        if name in ("UserDefinedEquations", "MetricsEquation"):
-            continue  # post-processing reductions (osb_reduce) / metrics passed as arrays
+        if name == "MetricsEquation":
+            continue  # metrics are passed as arrays
+        if name == "UserDefinedEquations":
+            continue  # a non-linear filter's kernels (_filter_of) or post-processing reductions
         raise NotImplementedError("equation class %s is not supported by the GB300 backend%s" % (
             name, "; the non-linear WENO filter is reached through BlockSpec (problems.tgv_filtered)"
             if "filter" in name.lower() or "Filter" in name else ""))
@@ -252,8 +289,9 @@ def block_spec(block, params):
     visc = _viscosity_of(block)
     bc, depth = _bcs_of(block, scheme == abi.SCHEME_CENTRAL4)
     split = _split_form_of(block) if scheme == abi.SCHEME_CENTRAL4 else abi.SPLIT_FEIEREISEN
+    filt, kappa = _filter_of(block, p)
     return BlockSpec(ndim=nd, size=size, scheme=scheme, averaging=avg, viscous=visc, bc=bc, bc_depth=depth,
-                     split_form=split,
+                     split_form=split, filter=filt, tvd_kappa=kappa,
                      gama=_const_value("gama", p), Minf=_const_value("Minf", p, 1.0), Re=_const_value("Re", p, 1.0),
                      Pr=_const_value("Pr", p, 0.71), mu_const=1.0, eps=_const_value("eps", p, 1e-40),
                      teno_ct=_const_value("TENO_CT", p, 1e-6),

@@ -140,3 +140,20 @@ def test_central_split_form_detected():
         alg = TraditionalAlgorithmRK(block)
     with pytest.raises(NotImplementedError):
         GB300Backend(alg, TGV_SUPERSONIC)
+
+
+@needs_ref
+def test_tvd_filter_detected():
+    """The TVD filter's equation classes (filters/TVD_filter.py, the TGV app's TVD branch) map
+    onto OSB_FILTER_TVD with the run's kappa_TVD and the stage exchange depth of its periodic
+    BCs; without kappa_TVD the backend refuses the block instead of dropping the filter."""
+    be = _backend_for("tgv_kgp_tvd", dict(TGV_SUPERSONIC, kappa_TVD="1.25"))
+    spec = be.specs[0]
+    ref_spec, _ = problems.tgv_tvd(16, kappa=1.25)
+    assert spec.filter == abi.FILTER_TVD and spec.tvd_kappa == 1.25
+    assert spec.split_form == abi.SPLIT_KGP and spec.scheme == abi.SCHEME_CENTRAL4
+    assert spec.bc_depth == ref_spec.bc_depth
+    with pytest.raises(ValueError):
+        _backend_for("tgv_kgp_tvd", TGV_SUPERSONIC)
+    be = _backend_for("tgv_kgp", TGV_SUPERSONIC)
+    assert be.specs[0].filter == abi.FILTER_NONE
