@@ -156,6 +156,18 @@ int osb_set_rk(osb_ctx* ctx, int kind, int nstages, const double* A, const doubl
  * captured once into a CUDA graph and replayed.  Asynchronous: returns after queueing. */
 int osb_step(osb_ctx* ctx, double dt, int nsteps);
 
+/* Host-memory entry point for independent runs of the context's blocks (the reference's
+ * generated solver keeps its state in host memory, opensbli.cpp:86-120 and 206-431): request r
+ * copies the state from host buffer in[r] (every block's variables in block order, each the
+ * whole allocation including halos, the layout the block descriptors' q arrays have,
+ * concatenated), advances it nsteps whole steps (osb_step) and copies the result into out[r].
+ * The host-to-device copy of request r+1 and the device-to-host copy of request r-1 run on two
+ * copy streams while request r computes (pinned host buffers for the overlap).  in[r] may
+ * repeat; out[r] must not be read before the call returns.  Keeps four device staging buffers
+ * of one request's size.  Synchronous: returns when every result is in host memory. */
+int osb_step_requests(osb_ctx* ctx, int count, const double* const* in, double* const* out, double dt,
+                      int nsteps);
+
 /* Runs one RK stage (index `stage`) on every block: residual, update, boundaries. */
 int osb_stage(osb_ctx* ctx, int stage, double dt);
 

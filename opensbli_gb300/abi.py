@@ -186,6 +186,7 @@ def load_library():
     lib.osb_block_add.argtypes = [vp, ctypes.POINTER(BlockDesc), ctypes.POINTER(i32)]
     lib.osb_set_rk.argtypes = [vp, i32, i32, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
     lib.osb_step.argtypes = [vp, ctypes.c_double, i32]
+    lib.osb_step_requests.argtypes = [vp, i32, ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.c_double, i32]
     lib.osb_stage.argtypes = [vp, i32, ctypes.c_double]
     lib.osb_apply_bc.argtypes = [vp]
     lib.osb_residual.argtypes = [vp, i32, ctypes.POINTER(vp)]
@@ -220,7 +221,7 @@ def check(lib, rc, what):
 
 # Exported symbols the header declares (checked by the CPU tests without a GPU).
 EXPORTED = ["osb_version", "osb_last_error", "osb_ctx_create", "osb_ctx_destroy", "osb_block_add",
-            "osb_set_rk", "osb_step", "osb_stage", "osb_apply_bc", "osb_residual", "osb_reduce",
+            "osb_set_rk", "osb_step", "osb_step_requests", "osb_stage", "osb_apply_bc", "osb_residual", "osb_reduce",
             "osb_sync", "osb_set_graphs", "osb_set_variant", "osb_launch_count", "osb_get_stream",
             "osb_desc_layout", "osb_timing", "osb_timing_report", "osb_stage_noalloc", "osb_set_schedule",
             "osb_get_schedule"]

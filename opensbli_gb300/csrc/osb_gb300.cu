@@ -929,6 +929,113 @@ int osb_ctx_create(int device, int precision, osb_ctx** out) {
   return OSB_OK;
 }
 
+namespace {
+
+void requests_free(osb_ctx* c) {
+  for (int k = 0; k < 2; ++k) {
+    if (c->stage_in[k]) cudaFree(c->stage_in[k]);
+    if (c->stage_out[k]) cudaFree(c->stage_out[k]);
+    c->stage_in[k] = c->stage_out[k] = nullptr;
+    for (cudaEvent_t* e : {&c->ev_in[k], &c->ev_used[k], &c->ev_res[k], &c->ev_out[k]})
+      if (*e) {
+        cudaEventDestroy(*e);
+        *e = nullptr;
+      }
+  }
+  if (c->cs_in) cudaStreamDestroy(c->cs_in);
+  if (c->cs_out) cudaStreamDestroy(c->cs_out);
+  c->cs_in = c->cs_out = nullptr;
+  c->stage_bytes = 0;
+}
+
+// Bytes of one request: every block's variables, whole allocations, in block order.
+size_t request_bytes(const osb_ctx* c) {
+  size_t n = 0;
+  for (const auto& bl : c->blocks) n += (size_t)(bl.d.ndim + 2) * bl.k.alloc * sizeof(double);
+  return n;
+}
+
+int requests_setup(osb_ctx* c) {
+  const size_t bytes = request_bytes(c);
+  if (c->stage_bytes == bytes && c->cs_in) return OSB_OK;
+  OSB_CK(cudaStreamSynchronize(c->stream));
+  if (c->cs_in) OSB_CK(cudaStreamSynchronize(c->cs_in));
+  if (c->cs_out) OSB_CK(cudaStreamSynchronize(c->cs_out));
+  requests_free(c);
+  OSB_CK(cudaStreamCreateWithFlags(&c->cs_in, cudaStreamNonBlocking));
+  OSB_CK(cudaStreamCreateWithFlags(&c->cs_out, cudaStreamNonBlocking));
+  for (int k = 0; k < 2; ++k) {
+    cudaError_t e = cudaMalloc(&c->stage_in[k], bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&c->stage_out[k], bytes);
+    if (e != cudaSuccess) {
+      requests_free(c);
+      return fail(OSB_ECUDA, "request staging (%zu bytes x 4): %s", bytes, cudaGetErrorString(e));
+    }
+    for (cudaEvent_t* ev : {&c->ev_in[k], &c->ev_used[k], &c->ev_res[k], &c->ev_out[k]})
+      OSB_CK(cudaEventCreateWithFlags(ev, cudaEventDisableTiming));
+  }
+  c->stage_bytes = bytes;
+  return OSB_OK;
+}
+
+// Copies between the blocks' state arrays and one staging slot (to_state: slot -> state).
+int stage_copy(osb_ctx* c, char* slot, bool to_state) {
+  size_t off = 0;
+  for (auto& bl : c->blocks)
+    for (int v = 0; v < bl.d.ndim + 2; ++v) {
+      const size_t n = (size_t)bl.k.alloc * sizeof(double);
+      if (to_state)
+        OSB_CK(cudaMemcpyAsync(bl.k.q[v], slot + off, n, cudaMemcpyDeviceToDevice, c->stream));
+      else
+        OSB_CK(cudaMemcpyAsync(slot + off, bl.k.q[v], n, cudaMemcpyDeviceToDevice, c->stream));
+      off += n;
+    }
+  return OSB_OK;
+}
+
+}  // namespace
+
+int osb_step_requests(osb_ctx* c, int count, const double* const* in, double* const* out, double dt, int nsteps) {
+  if (!c || (count > 0 && (!in || !out))) return fail(OSB_EINVAL, "null argument");
+  if (count < 0 || nsteps < 0) return fail(OSB_EINVAL, "count or nsteps < 0");
+  if (c->blocks.empty()) return fail(OSB_EINVAL, "no blocks");
+  if (count == 0) return OSB_OK;
+  for (int r = 0; r < count; ++r)
+    if (!in[r] || !out[r]) return fail(OSB_EINVAL, "request %d has a null buffer", r);
+  OSB_CK(cudaSetDevice(c->device));
+  int rc = requests_setup(c);
+  if (rc) return rc;
+  const size_t bytes = c->stage_bytes;
+  // request r uses slot r & 1 in each direction; the copy of request r + 1 in and of r - 1 out
+  // overlap the steps of request r
+  auto h2d = [&](int r) -> int {
+    const int k = r & 1;
+    if (r >= 2) OSB_CK(cudaStreamWaitEvent(c->cs_in, c->ev_used[k], 0));
+    OSB_CK(cudaMemcpyAsync(c->stage_in[k], in[r], bytes, cudaMemcpyHostToDevice, c->cs_in));
+    OSB_CK(cudaEventRecord(c->ev_in[k], c->cs_in));
+    return OSB_OK;
+  };
+  rc = h2d(0);
+  if (rc) return rc;
+  for (int r = 0; r < count; ++r) {
+    const int k = r & 1;
+    if (r + 1 < count && (rc = h2d(r + 1))) return rc;
+    OSB_CK(cudaStreamWaitEvent(c->stream, c->ev_in[k], 0));
+    if ((rc = stage_copy(c, (char*)c->stage_in[k], true))) return rc;
+    OSB_CK(cudaEventRecord(c->ev_used[k], c->stream));
+    if ((rc = osb_step(c, dt, nsteps))) return rc;
+    if (r >= 2) OSB_CK(cudaStreamWaitEvent(c->stream, c->ev_out[k], 0));
+    if ((rc = stage_copy(c, (char*)c->stage_out[k], false))) return rc;
+    OSB_CK(cudaEventRecord(c->ev_res[k], c->stream));
+    OSB_CK(cudaStreamWaitEvent(c->cs_out, c->ev_res[k], 0));
+    OSB_CK(cudaMemcpyAsync(out[r], c->stage_out[k], bytes, cudaMemcpyDeviceToHost, c->cs_out));
+    OSB_CK(cudaEventRecord(c->ev_out[k], c->cs_out));
+  }
+  OSB_CK(cudaStreamSynchronize(c->cs_out));
+  OSB_CK(cudaStreamSynchronize(c->stream));
+  return OSB_OK;
+}
+
 int osb_ctx_destroy(osb_ctx* c) {
   if (!c) return OSB_OK;
   cudaSetDevice(c->device);
@@ -948,6 +1055,7 @@ int osb_ctx_destroy(osb_ctx* c) {
     if (bl.xrows) cudaFree(bl.xrows);
   }
   batch_free(c);
+  requests_free(c);
   if (c->resident) cudaFree(c->resident);
   if (c->red) cudaFree(c->red);
   if (c->bad) cudaFree(c->bad);

@@ -80,6 +80,13 @@ struct osb_ctx {
   std::vector<cudaEvent_t> event_pool;
   double fam_ms[osb::FAM_N] = {0};
   long long fam_count[osb::FAM_N] = {0};
+  // osb_step_requests: copy streams, two device staging slots per direction and their events
+  cudaStream_t cs_in = nullptr, cs_out = nullptr;
+  void* stage_in[2] = {nullptr, nullptr};
+  void* stage_out[2] = {nullptr, nullptr};
+  size_t stage_bytes = 0;
+  cudaEvent_t ev_in[2] = {nullptr, nullptr}, ev_used[2] = {nullptr, nullptr};
+  cudaEvent_t ev_res[2] = {nullptr, nullptr}, ev_out[2] = {nullptr, nullptr};
 };
 
 namespace osb {

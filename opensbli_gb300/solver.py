@@ -117,6 +117,25 @@ class Solver:
     def step(self, dt, nsteps=1):
         abi.check(self.lib, self.lib.osb_step(self.ctx, float(dt), int(nsteps)), "osb_step")
 
+    def step_requests(self, host_in, host_out, dt, nsteps=1):
+        """Independent runs from host memory (osb_step_requests): request r copies its state
+        from host_in[r], advances nsteps steps and leaves the result in host_out[r].  Each
+        buffer is a pinned torch tensor (or anything with data_ptr()) holding every block's
+        variables in block order, whole allocations (the shape of torch.cat of self.q), so the
+        copies overlap the steps.  Returns when every result is in host memory."""
+        n = len(host_in)
+        if len(host_out) != n:
+            raise ValueError("host_in and host_out differ in length")
+        need = sum(q.numel() for q in self.q) * 8
+        for b in list(host_in) + list(host_out):
+            if b.numel() * b.element_size() != need:
+                raise ValueError("request buffer of %d bytes, the blocks need %d" % (b.numel() * b.element_size(), need))
+        vp = ctypes.c_void_p
+        ins = (vp * max(n, 1))(*[b.data_ptr() for b in host_in])
+        outs = (vp * max(n, 1))(*[b.data_ptr() for b in host_out])
+        abi.check(self.lib, self.lib.osb_step_requests(self.ctx, n, ins, outs, float(dt), int(nsteps)),
+                  "osb_step_requests")
+
     def stage(self, s, dt):
         abi.check(self.lib, self.lib.osb_stage(self.ctx, int(s), float(dt)), "osb_stage")
 
