@@ -258,6 +258,19 @@ int osb_get_stream(osb_ctx* ctx, void** stream);
  * No counterpart in the reference (OPS always allocates its own datasets). */
 int osb_stage_noalloc(const osb_block_desc* desc, int rk_kind, double A, double B, double dt, void* stream);
 
+/* ---- curvilinear metrics (equation_types/metric.py:183-327) -------------------------- */
+
+#define OSB_METRIC_PERIODIC 0 /* interior, halos the periodic images (a periodic block) */
+#define OSB_METRIC_EDGE 1     /* where the stencil fits (-3..N+2), outer layers repeat the nearest */
+
+/* Metric arrays of a 2D or 3D block on the device from its grid coordinates x[0..ndim-1]
+ * (device, OPS layout of the descriptor's size and halo, known at every allocated point):
+ * J_ij = d x_i / d xi_j with the generated metric kernel's 4th-order central differences and
+ * operator order, met[3 d + i] = d xi_d / d x_i (J inverted; 2D: the generated closed form),
+ * met[9] = det J -- the arrays osb_block_desc.metric takes.  2D writes slots 0, 1, 3, 4, 9 only.
+ * Reads ndim, size, halo and delta of desc.  Asynchronous on `stream`. */
+int osb_metrics(const osb_block_desc* desc, const double* const* x, double* const* met, int fill, void* stream);
+
 /* Binding check: writes sizeof(osb_block_desc) and the byte offsets of size, bc, iface, gama,
  * delta, q, rkold, metric, split_form, ducros_check and tvd_kappa into out[0..11] (n >= 12).
  * Needs no GPU. */

@@ -40,6 +40,9 @@ FILTER_NONE = 0
 FILTER_WENO3 = 1
 FILTER_TVD = 2
 
+METRIC_PERIODIC = 0
+METRIC_EDGE = 1
+
 PREC_FP64 = 0
 PREC_FP32_RESIDUAL = 1
 
@@ -197,6 +200,7 @@ def load_library():
     lib.osb_launch_count.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong)]
     lib.osb_get_stream.argtypes = [vp, ctypes.POINTER(vp)]
     lib.osb_desc_layout.argtypes = [ctypes.POINTER(ctypes.c_longlong), i32]
+    lib.osb_metrics.argtypes = [ctypes.POINTER(BlockDesc), ctypes.POINTER(vp), ctypes.POINTER(vp), i32, vp]
     lib.osb_stage_noalloc.argtypes = [ctypes.POINTER(BlockDesc), i32, ctypes.c_double, ctypes.c_double,
                                       ctypes.c_double, vp]
     lib.osb_set_schedule.argtypes = [vp, ctypes.POINTER(Schedule)]
@@ -224,7 +228,7 @@ EXPORTED = ["osb_version", "osb_last_error", "osb_ctx_create", "osb_ctx_destroy"
             "osb_set_rk", "osb_step", "osb_step_requests", "osb_stage", "osb_apply_bc", "osb_residual", "osb_reduce",
             "osb_sync", "osb_set_graphs", "osb_set_variant", "osb_launch_count", "osb_get_stream",
             "osb_desc_layout", "osb_timing", "osb_timing_report", "osb_stage_noalloc", "osb_set_schedule",
-            "osb_get_schedule"]
+            "osb_get_schedule", "osb_metrics"]
 
 NOALLOC_MAX_DOUBLES = 4 * 1024 * 1024
 

@@ -291,11 +291,11 @@ struct TvdPt {
   T r, m[3], e, u[3], a;
 };
 
-// Entropy fix of a wave speed with delta_TVD = 1/2 (shock_capturing.py:681-689, as generated:
-// |z| >= 1/invdelta ? |z| : 1/2 (1/invdelta^2 + z^2) invdelta, invdelta = 2).
+// Entropy fix of a wave speed with delta_TVD = 1/2 (shock_capturing.py:681-689; generated as
+// |z| >= 1/invdelta ? |z| : 1/2 (1/invdelta^2 + z^2) invdelta with invdelta = 2).
 template <typename T>
 __device__ __forceinline__ T tvd_psi(T z) {
-  return fabs(z) >= L_(0.5) ? fabs(z) : L_(0.5) * (L_(0.25) + z * z) * L_(2.0);
+  return fabs(z) >= L_(0.5) ? fabs(z) : L_(0.25) + z * z;  // 1/2 (1/4 + z^2) 2, exactly
 }
 
 // Limiter from the jump of this interface (hi) and the one below (lo) (lines 690-704).
@@ -307,85 +307,78 @@ __device__ __forceinline__ T tvd_g(T hi, T lo) {
   return S * fmax(t1, t2);
 }
 
-// TVD filter flux at interface i+1/2 from the points i-1..i+2 (local frame): simple averages
-// over (i-1, i), (i, i+1), (i+1, i+2), the characteristic jumps alpha = LEV (q_hi - q_lo) at
-// each, wave speeds and REV at i+1/2, then per wave sigma = psi(lambda), the limiters g at i and
-// i+1, gamma, phi = 1/2 sigma (g_i + g_i+1) - |sigma + psi(gamma)| alpha, Harten's switch theta
-// = max of ((|a_hi| - |a_lo|) / (|a_hi| + |a_lo| + eps))^2 over the two pairs, and
-// F = 1/2 REV (kappa theta phi), eps_TVD = 1e-8 -- in the operation order of the generated
-// direction-0 kernel.
+// The TVD filter flux at interface i+1/2 follows the generated direction-0 kernel in the local
+// frame of each direction: simple averages of u, a, rho over (i-1, i), (i, i+1), (i+1, i+2); the
+// characteristic jumps alpha = LEV (q_hi - q_lo) at the three half-points; wave speeds and REV
+// at i+1/2; per wave sigma = psi(lambda), the limiters g at i and i+1, gamma, phi =
+// 1/2 sigma (g_i + g_i+1) - |sigma + psi(gamma)| alpha, Harten's switch theta = max of
+// ((|a_hi| - |a_lo|) / (|a_hi| + |a_lo| + eps))^2 over the two pairs, and F = 1/2 REV
+// (kappa theta phi), eps_TVD = 1e-8.  A half-point's jumps serve three interfaces, so they are
+// formed once (tvd_half) and the interface combines three of them (tvd_iface).
+
+// Jumps and averages (u_n, u_t1, u_t2, a, rho) of the half-point between lo and hi.
 template <typename T>
-__device__ __forceinline__ void tvd_flux(const TvdPt<T> (&w)[4], T gm, T kappa, T (&fh)[5]) {
-  const T g1 = gm - L_(1.0), eps = L_(1.0e-8);
+__device__ __forceinline__ void tvd_half(const TvdPt<T>& lo, const TvdPt<T>& hi, T gm, T (&al)[5], T (&av)[5]) {
+  const T g1 = gm - L_(1.0);
   const T c1 = L_(0.35355339059327373), c2 = L_(0.70710678118654746);
-  T al[5][3];
-  T ws0 = L_(0.0), wsp = L_(0.0), wsm = L_(0.0);
-  T R03 = L_(0.0), R13 = L_(0.0), R14 = L_(0.0), R10 = L_(0.0), R20 = L_(0.0), R22 = L_(0.0), R23 = L_(0.0);
-  T R30 = L_(0.0), R31 = L_(0.0), R33 = L_(0.0), R40 = L_(0.0), R41 = L_(0.0), R42 = L_(0.0), R43 = L_(0.0),
-    R44 = L_(0.0);
-#pragma unroll
-  for (int jb = 0; jb < 3; ++jb) {
-    const TvdPt<T>& lo = w[jb];
-    const TvdPt<T>& hi = w[jb + 1];
-    const T u0 = L_(0.5) * (lo.u[0] + hi.u[0]), u1 = L_(0.5) * (lo.u[1] + hi.u[1]), u2 = L_(0.5) * (lo.u[2] + hi.u[2]);
-    const T a = L_(0.5) * (lo.a + hi.a), rho = L_(0.5) * (lo.r + hi.r);
-    const T ia = L_(1.0) / a, ir = L_(1.0) / rho, ia2 = ia * ia;
-    const T q0 = u0 * u0, q1 = u1 * u1, q2 = u2 * u2;
-    const T L00 = -L_(0.5) * (L_(-2.0) - q0 * ia2 - q1 * ia2 - q2 * ia2 + q0 * ia2 * gm + q1 * ia2 * gm + q2 * ia2 * gm);
-    const T L01 = ia2 * g1 * u0, L02 = ia2 * g1 * u1, L03 = ia2 * g1 * u2, L04 = -ia2 * g1;
-    const T kq = -q0 * ia - q1 * ia - q2 * ia + q0 * gm * ia + q1 * gm * ia + q2 * gm * ia;
-    const T L30 = c1 * (L_(-2.0) * u0 + kq) * ir, L40 = c1 * (L_(2.0) * u0 + kq) * ir;
-    const T L31 = -c2 * (L_(-1.0) - u0 * ia + gm * u0 * ia) * ir, L41 = -c2 * (L_(1.0) - u0 * ia + gm * u0 * ia) * ir;
-    const T L32 = -c2 * g1 * u1 * ia * ir, L33 = -c2 * g1 * u2 * ia * ir, L34 = c2 * g1 * ia * ir;
-    const T dr = -lo.r + hi.r, d0 = -lo.m[0] + hi.m[0], d1 = -lo.m[1] + hi.m[1], d2 = -lo.m[2] + hi.m[2],
-            de = -lo.e + hi.e;
-    al[0][jb] = dr * L00 + de * L04 + d0 * L01 + d1 * L02 + d2 * L03;
-    al[1][jb] = dr * (-u2 * ir) + d2 * ir;
-    al[2][jb] = dr * (u1 * ir) + d1 * (-ir);
-    al[3][jb] = dr * L30 + de * L34 + d0 * L31 + d1 * L32 + d2 * L33;
-    al[4][jb] = dr * L40 + de * L34 + d0 * L41 + d1 * L32 + d2 * L33;
-    if (jb == 1) {
-      ws0 = u0;
-      wsp = a + u0;
-      wsm = -a + u0;
-      R03 = c2 * rho * ia;
-      R10 = u0;
-      R13 = c2 * (a + u0) * rho * ia;
-      R14 = c2 * (-a + u0) * rho * ia;
-      R20 = u1;
-      R22 = -rho;
-      R23 = c2 * rho * u1 * ia;
-      R30 = u2;
-      R31 = rho;
-      R33 = c2 * rho * u2 * ia;
-      R40 = L_(0.5) * q0 + L_(0.5) * q1 + L_(0.5) * q2;
-      R41 = rho * u2;
-      R42 = -rho * u1;
-      const T hq = (a * a + L_(0.5) * g1 * (q0 + q1 + q2)) / g1;
-      R43 = c2 * (hq + a * u0) * rho * ia;
-      R44 = c2 * (hq - a * u0) * rho * ia;
-    }
-  }
+  const T u0 = L_(0.5) * (lo.u[0] + hi.u[0]), u1 = L_(0.5) * (lo.u[1] + hi.u[1]), u2 = L_(0.5) * (lo.u[2] + hi.u[2]);
+  const T a = L_(0.5) * (lo.a + hi.a), rho = L_(0.5) * (lo.r + hi.r);
+  const T ia = L_(1.0) / a, ir = L_(1.0) / rho, ia2 = ia * ia;
+  const T q0 = u0 * u0, q1 = u1 * u1, q2 = u2 * u2;
+  const T L00 = -L_(0.5) * (L_(-2.0) - q0 * ia2 - q1 * ia2 - q2 * ia2 + q0 * ia2 * gm + q1 * ia2 * gm + q2 * ia2 * gm);
+  const T L01 = ia2 * g1 * u0, L02 = ia2 * g1 * u1, L03 = ia2 * g1 * u2, L04 = -ia2 * g1;
+  const T kq = -q0 * ia - q1 * ia - q2 * ia + q0 * gm * ia + q1 * gm * ia + q2 * gm * ia;
+  const T L30 = c1 * (L_(-2.0) * u0 + kq) * ir, L40 = c1 * (L_(2.0) * u0 + kq) * ir;
+  const T L31 = -c2 * (L_(-1.0) - u0 * ia + gm * u0 * ia) * ir, L41 = -c2 * (L_(1.0) - u0 * ia + gm * u0 * ia) * ir;
+  const T L32 = -c2 * g1 * u1 * ia * ir, L33 = -c2 * g1 * u2 * ia * ir, L34 = c2 * g1 * ia * ir;
+  const T dr = -lo.r + hi.r, d0 = -lo.m[0] + hi.m[0], d1 = -lo.m[1] + hi.m[1], d2 = -lo.m[2] + hi.m[2],
+          de = -lo.e + hi.e;
+  al[0] = dr * L00 + de * L04 + d0 * L01 + d1 * L02 + d2 * L03;
+  al[1] = dr * (-u2 * ir) + d2 * ir;
+  al[2] = dr * (u1 * ir) + d1 * (-ir);
+  al[3] = dr * L30 + de * L34 + d0 * L31 + d1 * L32 + d2 * L33;
+  al[4] = dr * L40 + de * L34 + d0 * L41 + d1 * L32 + d2 * L33;
+  av[0] = u0;
+  av[1] = u1;
+  av[2] = u2;
+  av[3] = a;
+  av[4] = rho;
+}
+
+// Interface flux from the jumps of the half-points below (a0), at (a1) and above (a2) it and
+// the averages at it.
+template <typename T>
+__device__ __forceinline__ void tvd_iface(const T* a0, const T* a1, const T* a2, const T* av, T gm, T kappa,
+                                          T (&fh)[5]) {
+  const T g1 = gm - L_(1.0), eps = L_(1.0e-8), c2 = L_(0.70710678118654746);
+  const T u0 = av[0], u1 = av[1], u2 = av[2], a = av[3], rho = av[4];
+  const T ia = L_(1.0) / a;
+  const T q0 = u0 * u0, q1 = u1 * u1, q2 = u2 * u2;
+  const T ws0 = u0, wsp = a + u0, wsm = -a + u0;
+  const T R03 = c2 * rho * ia, R13 = c2 * (a + u0) * rho * ia, R14 = c2 * (-a + u0) * rho * ia;
+  const T R23 = c2 * rho * u1 * ia, R33 = c2 * rho * u2 * ia;
+  const T R40 = L_(0.5) * q0 + L_(0.5) * q1 + L_(0.5) * q2;
+  const T hq = (a * a + L_(0.5) * g1 * (q0 + q1 + q2)) / g1;
+  const T R43 = c2 * (hq + a * u0) * rho * ia, R44 = c2 * (hq - a * u0) * rho * ia;
   T ps[5];
 #pragma unroll
   for (int k = 0; k < 5; ++k) {
     const T s0 = tvd_psi<T>(k < 3 ? ws0 : (k == 3 ? wsp : wsm));
-    const T a0 = al[k][0], a1 = al[k][1], a2 = al[k][2];
-    const T g0 = tvd_g<T>(a1, a0), gg = tvd_g<T>(a2, a1);
-    const T gam = a1 == L_(0.0) ? L_(0.0) : (-g0 + gg) * a1 * s0 / (a1 * a1 + eps);
-    const T phi = -fabs(s0 + tvd_psi<T>(gam)) * a1 + L_(0.5) * (g0 + gg) * s0;
-    T t1 = -fabs(a0) + fabs(a1), t2 = fabs(a0) + fabs(a1) + eps;
-    const T r0 = fabs(t1 / t2);
-    t1 = -fabs(a1) + fabs(a2);
-    t2 = fabs(a1) + fabs(a2) + eps;
-    const T r1 = fabs(t1 / t2);
-    ps[k] = kappa * phi * fmax(r0 * r0, r1 * r1);
+    const T b0 = a0[k], b1 = a1[k], b2 = a2[k];
+    const T g0 = tvd_g<T>(b1, b0), gg = tvd_g<T>(b2, b1);
+    const T gam = b1 == L_(0.0) ? L_(0.0) : (-g0 + gg) * b1 * s0 / (b1 * b1 + eps);
+    const T phi = -fabs(s0 + tvd_psi<T>(gam)) * b1 + L_(0.5) * (g0 + gg) * s0;
+    // Harten's switch: the larger of |x0| / y0 and |x1| / y1, squared, with one division
+    const T x0 = fabs(-fabs(b0) + fabs(b1)), y0 = fabs(b0) + fabs(b1) + eps;
+    const T x1 = fabs(-fabs(b1) + fabs(b2)), y1 = fabs(b1) + fabs(b2) + eps;
+    const T th = fmax(x0 * y1, x1 * y0) / (y0 * y1);
+    ps[k] = kappa * phi * (th * th);
   }
   fh[0] = L_(0.5) * ps[0] + L_(0.5) * R03 * ps[3] + L_(0.5) * R03 * ps[4];
-  fh[1] = L_(0.5) * R10 * ps[0] + L_(0.5) * R13 * ps[3] + L_(0.5) * R14 * ps[4];
-  fh[2] = L_(0.5) * R20 * ps[0] + L_(0.5) * R22 * ps[2] + L_(0.5) * R23 * ps[3] + L_(0.5) * R23 * ps[4];
-  fh[3] = L_(0.5) * R30 * ps[0] + L_(0.5) * R31 * ps[1] + L_(0.5) * R33 * ps[3] + L_(0.5) * R33 * ps[4];
-  fh[4] = L_(0.5) * R40 * ps[0] + L_(0.5) * R41 * ps[1] + L_(0.5) * R42 * ps[2] + L_(0.5) * R43 * ps[3] +
+  fh[1] = L_(0.5) * u0 * ps[0] + L_(0.5) * R13 * ps[3] + L_(0.5) * R14 * ps[4];
+  fh[2] = L_(0.5) * u1 * ps[0] + L_(0.5) * (-rho) * ps[2] + L_(0.5) * R23 * ps[3] + L_(0.5) * R23 * ps[4];
+  fh[3] = L_(0.5) * u2 * ps[0] + L_(0.5) * rho * ps[1] + L_(0.5) * R33 * ps[3] + L_(0.5) * R33 * ps[4];
+  fh[4] = L_(0.5) * R40 * ps[0] + L_(0.5) * (rho * u2) * ps[1] + L_(0.5) * (-rho * u1) * ps[2] + L_(0.5) * R43 * ps[3] +
           L_(0.5) * R44 * ps[4];
 }
 
@@ -416,61 +409,115 @@ __global__ void k_tvd_stale(BlockK b, T* __restrict__ snap, int fmax) {
   }
 }
 
-// TVD filter fluxes along D at interfaces i+1/2, i = -1..N-1, transverse interior; F[v] at the
-// index of point i.  u and a of each point as the filter's constituent-relation kernel forms
-// them (u = rhou (1/rho), a = sqrt(gama p (1/rho))); at index -2 (the interface at -1) u comes
-// from the stage snapshot and a is 0, as in the generated solver.
+// Tile of the TVD flux kernel: TA interfaces along D times TB lines, (TA + 2) TB half-points
+// (256: one per thread).  Along x (D = 0) a warp covers consecutive points of a row; along y
+// and z it covers 32 consecutive x of the lines, so the state loads and flux stores are
+// coalesced either way.
+constexpr int TVD_TH = 256;
+template <int D>
+struct TvdTile {
+  static constexpr int TA = D == 0 ? 62 : 8;  // interfaces along D (x: 4 lines of 64 half-points)
+  static constexpr int TB = TVD_TH / TA;      // lines
+  static constexpr int NH = (TA + 2) * TB;    // half-points
+  static constexpr int REC = 11;              // 5 jumps + 5 averages, odd stride
+};
+
+// State of point p (index cD along D) in the local frame, u and a as the filter's
+// constituent-relation kernel forms them (u = rhou (1/rho), a = sqrt(gama p (1/rho))); at
+// index -2 the velocities of the stage snapshot and a = 0, as in the generated solver.
 template <typename T, int D>
-__global__ void k_tvd_flux(BlockK b, T gm, T kappa, const T* __restrict__ snap, int fmax, T* F0, T* F1, T* F2, T* F3,
-                           T* F4) {
+__device__ __forceinline__ void tvd_point(const BlockK& b, int p, bool stale, const T* __restrict__ snap, int fmax,
+                                          int f, T gm, TvdPt<T>& q) {
   constexpr int T1 = (D + 1) % 3, T2 = (D + 2) % 3;
+  q.r = ld_q<T>(b, 0, p);
+  q.e = ld_q<T>(b, 4, p);
+  const T mg[3] = {ld_q<T>(b, 1, p), ld_q<T>(b, 2, p), ld_q<T>(b, 3, p)};
+  q.m[0] = mg[D];
+  q.m[1] = mg[T1];
+  q.m[2] = mg[T2];
+  if (stale) {
+    q.u[0] = snap[(size_t)(3 * D + D) * fmax + f];
+    q.u[1] = snap[(size_t)(3 * D + T1) * fmax + f];
+    q.u[2] = snap[(size_t)(3 * D + T2) * fmax + f];
+    q.a = L_(0.0);
+  } else {
+    const T ir = L_(1.0) / q.r;
+    q.u[0] = q.m[0] * ir;
+    q.u[1] = q.m[1] * ir;
+    q.u[2] = q.m[2] * ir;
+    const T pr =
+        (gm - L_(1.0)) * (-(L_(0.5) * (mg[0] * mg[0]) + L_(0.5) * (mg[1] * mg[1]) + L_(0.5) * (mg[2] * mg[2])) * ir + q.e);
+    q.a = sqrt(gm * pr * ir);
+  }
+}
+
+// TVD filter fluxes along D at interfaces i+1/2, i = -1..N-1, transverse interior; F[v] at the
+// index of point i.  Phase 1: every half-point j = i0-1 .. i0+TA of the tile's lines (the
+// points j, j+1) into shared memory; phase 2: one thread per interface.
+template <typename T, int D>
+__global__ void __launch_bounds__(TVD_TH) k_tvd_flux(BlockK b, T gm, T kappa, const T* __restrict__ snap, int fmax,
+                                                    T* F0, T* F1, T* F2, T* F3, T* F4) {
+  using TT = TvdTile<D>;
+  constexpr int TA = TT::TA, TB = TT::TB, REC = TT::REC;
+  constexpr int T1 = (D + 1) % 3, T2 = (D + 2) % 3;
+  __shared__ T sm[TT::NH * REC];
   int e1, e2;
   tvd_face_dirs(D, e1, e2);
-  int e[3] = {b.n[0], b.n[1], b.n[2]};
-  e[D] += 1;
-  const int total = e[0] * e[1] * e[2];
+  const int N = b.n[D];
+  const int i0 = (int)blockIdx.y * TA - 1;  // first interface of the tile
   const int s = b.st[D];
-  T* F[5] = {F0, F1, F2, F3, F4};
-  const T g1 = gm - L_(1.0);
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
-    int c[3] = {t % e[0], (t / e[0]) % e[1], t / (e[0] * e[1])};
-    c[D] -= 1;
-    const int id = lin(b, c[0], c[1], c[2]);
-    TvdPt<T> w[4];
-#pragma unroll
-    for (int m = 0; m < 4; ++m) {
-      const int p = id + (m - 1) * s;
-      TvdPt<T>& q = w[m];
-      q.r = ld_q<T>(b, 0, p);
-      q.e = ld_q<T>(b, 4, p);
-      const T mx = ld_q<T>(b, 1, p), my = ld_q<T>(b, 2, p), mz = ld_q<T>(b, 3, p);
-      const T mg[3] = {mx, my, mz};
-      q.m[0] = mg[D];
-      q.m[1] = mg[T1];
-      q.m[2] = mg[T2];
-      if (m == 0 && c[D] == -1) {
-        const int f = c[e1] + b.n[e1] * c[e2];
-        q.u[0] = snap[(size_t)(3 * D + D) * fmax + f];
-        q.u[1] = snap[(size_t)(3 * D + T1) * fmax + f];
-        q.u[2] = snap[(size_t)(3 * D + T2) * fmax + f];
-        q.a = L_(0.0);
-      } else {
-        const T ir = L_(1.0) / q.r;
-        q.u[0] = q.m[0] * ir;
-        q.u[1] = q.m[1] * ir;
-        q.u[2] = q.m[2] * ir;
-        const T pr = g1 * (-(L_(0.5) * (mx * mx) + L_(0.5) * (my * my) + L_(0.5) * (mz * mz)) * ir + q.e);
-        q.a = sqrt(gm * pr * ir);
-      }
+  // the tile's line `line` -> transverse coordinates (c[e1], c[e2]); false outside the block
+  auto line_coords = [&](int line, int (&c)[3]) -> bool {
+    if (D == 0) {
+      const long L = (long)blockIdx.x * TB + line;
+      c[1] = (int)(L % b.n[1]);
+      c[2] = (int)(L / b.n[1]);
+      return L < (long)b.n[1] * b.n[2];
     }
-    T fh[5];
-    tvd_flux<T>(w, gm, kappa, fh);
-    F[0][id] = fh[0];
-    F[1 + D][id] = fh[1];
-    F[1 + T1][id] = fh[2];
-    F[1 + T2][id] = fh[3];
-    F[4][id] = fh[4];
+    c[0] = (int)blockIdx.x * TB + line;
+    c[D == 1 ? 2 : 1] = (int)blockIdx.z;
+    return c[0] < b.n[0];
+  };
+  for (int hs = threadIdx.x; hs < TT::NH; hs += TVD_TH) {
+    const int line = D == 0 ? hs / (TA + 2) : hs % TB;
+    const int a = D == 0 ? hs % (TA + 2) : hs / TB;
+    const int j = i0 - 1 + a;  // half-point between points j and j+1
+    int c[3];
+    if (!line_coords(line, c) || j > N) continue;  // beyond the last interface's needs
+    c[D] = j;
+    const int p = lin(b, c[0], c[1], c[2]);
+    const int f = c[e1] + b.n[e1] * c[e2];
+    TvdPt<T> lo, hi;
+    tvd_point<T, D>(b, p, j == -2, snap, fmax, f, gm, lo);
+    tvd_point<T, D>(b, p + s, false, snap, fmax, f, gm, hi);
+    T al[5], av[5];
+    tvd_half<T>(lo, hi, gm, al, av);
+    T* r = sm + (line * (TA + 2) + a) * REC;
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+      r[k] = al[k];
+      r[5 + k] = av[k];
+    }
   }
+  __syncthreads();
+  const int t = threadIdx.x;
+  if (t >= TA * TB) return;  // x tiles: 248 interfaces for 256 threads
+  const int line = D == 0 ? t / TA : t % TB;
+  const int a = D == 0 ? t % TA : t / TB;
+  const int i = i0 + a;
+  int c[3];
+  if (!line_coords(line, c) || i > N - 1) return;
+  c[D] = i;
+  const int id = lin(b, c[0], c[1], c[2]);
+  const T* r = sm + (line * (TA + 2) + a) * REC;
+  T fh[5];
+  tvd_iface<T>(r, r + REC, r + 2 * REC, r + REC + 5, gm, kappa, fh);
+  T* F[5] = {F0, F1, F2, F3, F4};
+  F[0][id] = fh[0];
+  F[1 + D][id] = fh[1];
+  F[1 + T1][id] = fh[2];
+  F[1 + T2][id] = fh[3];
+  F[4][id] = fh[4];
 }
 
 // q += dt * mask * (-(F_0(i) - F_0(i-1)) / Delta_0 - (F_2 ...) / Delta_2 - (F_1 ...) / Delta_1)
@@ -544,12 +591,16 @@ int tvd_filter_t(osb_ctx* c, Block& bl, double dt) {
     k_filter_halo<<<grid_for(c, per, FT), FT, 0, c->stream>>>(k, d, fields);
   }
   const T gm = (T)bl.d.gama, kap = (T)bl.d.tvd_kappa;
-  const long nf0 = (long)(k.n[0] + 1) * k.n[1] * k.n[2], nf1 = (long)k.n[0] * (k.n[1] + 1) * k.n[2],
-             nf2 = (long)k.n[0] * k.n[1] * (k.n[2] + 1);
-  k_tvd_flux<T, 0><<<grid_for(c, nf0, FT), FT, 0, c->stream>>>(k, gm, kap, snap, fmax, F[0], F[1], F[2], F[3], F[4]);
-  k_tvd_flux<T, 1><<<grid_for(c, nf1, FT), FT, 0, c->stream>>>(k, gm, kap, snap, fmax, F[5], F[6], F[7], F[8], F[9]);
-  k_tvd_flux<T, 2><<<grid_for(c, nf2, FT), FT, 0, c->stream>>>(k, gm, kap, snap, fmax, F[10], F[11], F[12], F[13],
-                                                               F[14]);
+  // grids: D = 0 (lines of y, z) x (x tiles); D = 1, 2 (x tiles) x (tiles along D) x (the other)
+  const dim3 g0((unsigned)(((long)k.n[1] * k.n[2] + TvdTile<0>::TB - 1) / TvdTile<0>::TB),
+                (unsigned)((k.n[0] + 1 + TvdTile<0>::TA - 1) / TvdTile<0>::TA));
+  const dim3 g1((unsigned)((k.n[0] + TvdTile<1>::TB - 1) / TvdTile<1>::TB),
+                (unsigned)((k.n[1] + 1 + TvdTile<1>::TA - 1) / TvdTile<1>::TA), (unsigned)k.n[2]);
+  const dim3 g2((unsigned)((k.n[0] + TvdTile<2>::TB - 1) / TvdTile<2>::TB),
+                (unsigned)((k.n[2] + 1 + TvdTile<2>::TA - 1) / TvdTile<2>::TA), (unsigned)k.n[1]);
+  k_tvd_flux<T, 0><<<g0, TVD_TH, 0, c->stream>>>(k, gm, kap, snap, fmax, F[0], F[1], F[2], F[3], F[4]);
+  k_tvd_flux<T, 1><<<g1, TVD_TH, 0, c->stream>>>(k, gm, kap, snap, fmax, F[5], F[6], F[7], F[8], F[9]);
+  k_tvd_flux<T, 2><<<g2, TVD_TH, 0, c->stream>>>(k, gm, kap, snap, fmax, F[10], F[11], F[12], F[13], F[14]);
   FilterFluxes<T> Fd;
   for (int a = 0; a < 15; ++a) Fd.f[a] = F[a];
   k_filter_apply<T><<<grid_for(c, n, FT), FT, 0, c->stream>>>(k, nullptr, Fd, dt, (T)0);

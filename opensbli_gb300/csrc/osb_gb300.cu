@@ -1506,6 +1506,121 @@ int noalloc_scratch(int device, double** out) {
 
 }  // namespace
 
+namespace {
+
+// 4th-order central first derivative of f at linear index id along stride s, the operator
+// order of the generated metric kernel: ((-2/3 f[-1] - 1/12 f[+2]) + 1/12 f[-2] + 2/3 f[+1]) / Delta,
+// rounded operation by operation (no contraction).
+__device__ __forceinline__ double metric_d1(const double* __restrict__ f, int id, int s, double inv) {
+  double t = __dadd_rn(__dmul_rn(-(2.0 / 3.0), f[id - s]), -__dmul_rn(1.0 / 12.0, f[id + 2 * s]));
+  t = __dadd_rn(t, __dmul_rn(1.0 / 12.0, f[id - 2 * s]));
+  t = __dadd_rn(t, __dmul_rn(2.0 / 3.0, f[id + s]));
+  return __dmul_rn(t, inv);
+}
+
+// Metric arrays at every allocated point: the point's metrics are those evaluated at a source
+// point -- the point itself on the interior; its periodic image (fill 0) or the nearest point
+// where the stencil fits, index -3..N+2 of each direction (fill 1), in the halos.  At the
+// source point J_ij = d x_i / d xi_j from central differences of the coordinates;
+// met[3 d + i] = d xi_d / d x_i (the inverse of J), met[9] = det J.
+__global__ void k_metrics(BlockK b, const double* __restrict__ x0, const double* __restrict__ x1,
+                          const double* __restrict__ x2, double* m0, double* m1, double* m2, double* m3, double* m4,
+                          double* m5, double* m6, double* m7, double* m8, double* m9, int fill, int halo) {
+  const int nd = b.ndim;
+  int ext[3];
+  for (int e = 0; e < 3; ++e) ext[e] = e < nd ? b.n[e] + 2 * halo : 1;
+  const long total = (long)ext[0] * ext[1] * ext[2];
+  const double* x[3] = {x0, x1, x2};
+  double* m[10] = {m0, m1, m2, m3, m4, m5, m6, m7, m8, m9};
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+    int c[3] = {(int)(t % ext[0]), (int)((t / ext[0]) % ext[1]), (int)(t / ((long)ext[0] * ext[1]))};
+    int src[3] = {0, 0, 0};
+    for (int e = 0; e < nd; ++e) {
+      c[e] -= halo;
+      const int n = b.n[e];
+      src[e] = fill == OSB_METRIC_PERIODIC ? ((c[e] % n) + n) % n : min(max(c[e], -3), n + 2);
+    }
+    const int dst = lin(b, c[0], c[1], c[2]);
+    const int id = lin(b, src[0], src[1], src[2]);
+    double J[3][3];
+    for (int i = 0; i < nd; ++i)
+      for (int j = 0; j < nd; ++j) J[i][j] = metric_d1(x[i], id, b.st[j], b.invd[j]);
+    if (nd == 2) {
+      const double det = __dadd_rn(__dmul_rn(J[0][0], J[1][1]), -__dmul_rn(J[0][1], J[1][0]));
+      m[0][dst] = __ddiv_rn(J[1][1], det);
+      m[1][dst] = __ddiv_rn(-J[0][1], det);
+      m[3][dst] = __ddiv_rn(-J[1][0], det);
+      m[4][dst] = __ddiv_rn(J[0][0], det);
+      m[9][dst] = det;
+    } else {
+      // cofactors: inv[d][i] = C[i][d] / det
+      double C[3][3];
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+          const int i1 = (i + 1) % 3, i2 = (i + 2) % 3, j1 = (j + 1) % 3, j2 = (j + 2) % 3;
+          C[i][j] = J[i1][j1] * J[i2][j2] - J[i1][j2] * J[i2][j1];
+        }
+      const double det = J[0][0] * C[0][0] + J[0][1] * C[0][1] + J[0][2] * C[0][2];
+      for (int d = 0; d < 3; ++d)
+        for (int i = 0; i < 3; ++i) m[3 * d + i][dst] = C[i][d] / det;
+      m[9][dst] = det;
+    }
+  }
+}
+
+}  // namespace
+
+extern "C" int osb_metrics(const osb_block_desc* d, const double* const* x, double* const* met, int fill,
+                           void* stream) {
+  if (!d || !x || !met) return fail(OSB_EINVAL, "null argument");
+  if (d->ndim != 2 && d->ndim != 3) return fail(OSB_EINVAL, "metrics are defined for 2D and 3D blocks");
+  if (fill != OSB_METRIC_PERIODIC && fill != OSB_METRIC_EDGE) return fail(OSB_EINVAL, "unknown metric fill %d", fill);
+  if (d->halo < 5) return fail(OSB_EINVAL, "halo %d < 5", d->halo);
+  for (int i = 0; i < d->ndim; ++i) {
+    if (!x[i]) return fail(OSB_EINVAL, "coordinate array %d is null", i);
+    if (d->size[i] < (fill == OSB_METRIC_PERIODIC ? d->halo : 1))
+      return fail(OSB_EINVAL, "direction %d has %d points, fewer than the periodic halo", i, d->size[i]);
+    if (!(d->delta[i] > 0.0)) return fail(OSB_EINVAL, "delta[%d] must be > 0", i);
+  }
+  static const int used2[] = {0, 1, 3, 4, 9};
+  if (d->ndim == 2) {
+    for (int k : used2)
+      if (!met[k]) return fail(OSB_EINVAL, "metric array %d is null", k);
+  } else {
+    for (int k = 0; k < 10; ++k)
+      if (!met[k]) return fail(OSB_EINVAL, "metric array %d is null", k);
+  }
+  BlockK k;
+  memset(&k, 0, sizeof k);
+  k.ndim = d->ndim;
+  long ext[3];
+  for (int i = 0; i < 3; ++i) {
+    k.n[i] = i < d->ndim ? d->size[i] : 1;
+    ext[i] = i < d->ndim ? d->size[i] + 2 * d->halo : 1;
+    k.invd[i] = i < d->ndim ? 1.0 / d->delta[i] : 0.0;
+  }
+  if (ext[0] * ext[1] * ext[2] >= (1L << 31)) return fail(OSB_EINVAL, "block too large for 32-bit indexing");
+  k.st[0] = 1;
+  k.st[1] = (int)ext[0];
+  k.st[2] = (int)(ext[0] * ext[1]);
+  k.alloc = ext[0] * ext[1] * ext[2];
+  k.off0 = d->halo + d->halo * k.st[1] + (d->ndim > 2 ? d->halo * k.st[2] : 0);
+  int device = 0, sms = 152;
+  OSB_CK(cudaGetDevice(&device));
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || sms <= 0) sms = 152;
+  const long blocks = std::min<long>((k.alloc + 255) / 256, (long)sms * 16);
+  double* m[10];
+  for (int i = 0; i < 10; ++i) m[i] = met[i];
+  double* dummy = met[9];  // unused 2D slots are never written
+  for (int i = 0; i < 10; ++i)
+    if (!m[i]) m[i] = dummy;
+  k_metrics<<<(unsigned)blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(
+      k, x[0], x[1], d->ndim > 2 ? x[2] : x[0], m[0], m[1], m[2], m[3], m[4], m[5], m[6], m[7], m[8], m[9], fill,
+      d->halo);
+  OSB_CK(cudaGetLastError());
+  return OSB_OK;
+}
+
 extern "C" int osb_stage_noalloc(const osb_block_desc* d, int rk_kind, double A, double B, double dt,
                                  void* stream) {
   if (!d) return fail(OSB_EINVAL, "null descriptor");

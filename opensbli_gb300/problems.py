@@ -249,6 +249,16 @@ def metrics_central4(spec, x, periodic_from_interior=False, extended=False):
     return met
 
 
+def wave_2d_coords(spec):
+    """Grid coordinates of the wavy 2D mesh of curvilinear_wave_2d at every allocated point."""
+    i = spec.grid_index(0).astype(np.float64)
+    j = spec.grid_index(1).astype(np.float64)
+    d0, d1 = spec.delta[0], spec.delta[1]
+    x0 = np.broadcast_to(0.04 * np.sin(3 * math.pi * d1 * j) + d0 * i, spec.shape).copy()
+    x1 = np.broadcast_to(0.04 * np.sin(3 * math.pi * d0 * i) + d1 * j, spec.shape).copy()
+    return x0, x1
+
+
 def curvilinear_wave_2d(n=128, scheme=abi.SCHEME_WENO5_Z, averaging=abi.AVG_ROE):
     """Density wave on a periodic wavy 2D mesh (the reference's curvilinear Euler verification
     case, tests/verification_apps/euler_wave_curvilinear): Delta = 2/N,
@@ -258,11 +268,7 @@ def curvilinear_wave_2d(n=128, scheme=abi.SCHEME_WENO5_Z, averaging=abi.AVG_ROE)
     spec = BlockSpec(ndim=2, size=(n, n), scheme=scheme, averaging=averaging,
                      bc=[[abi.BC_PERIODIC] * 2 for _ in range(2)], bc_depth=[[4, 4], [4, 4]],
                      delta=(2.0 / n, 2.0 / n), gama=1.4)
-    i = spec.grid_index(0).astype(np.float64)
-    j = spec.grid_index(1).astype(np.float64)
-    d0, d1 = spec.delta[0], spec.delta[1]
-    x0 = np.broadcast_to(0.04 * np.sin(3 * math.pi * d1 * j) + d0 * i, spec.shape).copy()
-    x1 = np.broadcast_to(0.04 * np.sin(3 * math.pi * d0 * i) + d1 * j, spec.shape).copy()
+    x0, x1 = wave_2d_coords(spec)
     rho = 1.0 + 0.2 * np.sin(math.pi * (x0 + x1))
     q = _cons(spec, rho, [np.full(spec.shape, 1.0), np.full(spec.shape, -0.5)], 1.0)
     return spec, q, metrics_central4(spec, [x0, x1], periodic_from_interior=True)

@@ -200,3 +200,27 @@ class Solver:
             self.close()
         except Exception:
             pass
+
+
+def device_metrics(spec, x, fill=abi.METRIC_EDGE, device=0):
+    """Metric arrays of a curvilinear block computed on the GPU (osb_metrics) from its grid
+    coordinates x[0..ndim-1] (OPS-layout arrays known at every allocated point, numpy or CUDA
+    tensors): the 10 slots of osb_block_desc.metric as CUDA tensors (None where a 2D block has
+    none).  fill = abi.METRIC_PERIODIC for a periodic block (interior, halos its images),
+    abi.METRIC_EDGE otherwise (where the stencil fits, outer layers the nearest)."""
+    torch = _torch()
+    lib = abi.load_library()
+    dev = torch.device("cuda", device)
+    xs = [torch.as_tensor(np.ascontiguousarray(a, dtype=np.float64) if isinstance(a, np.ndarray) else a,
+                          dtype=torch.float64, device=dev).contiguous() for a in x]
+    used = [0, 1, 3, 4, 9] if spec.ndim == 2 else list(range(10))
+    met = [torch.empty(spec.shape, dtype=torch.float64, device=dev) if k in used else None for k in range(10)]
+    d = abi.make_desc(spec, [0] * 5, [0] * 5)
+    vp = ctypes.c_void_p
+    xp = (vp * 3)(*([t.data_ptr() for t in xs] + [0] * (3 - len(xs))))
+    mp = (vp * 10)(*[0 if m is None else m.data_ptr() for m in met])
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    abi.check(lib, lib.osb_metrics(ctypes.byref(d), xp, mp, int(fill), vp(stream)), "osb_metrics")
+    torch.cuda.synchronize(dev)
+    return met
+
