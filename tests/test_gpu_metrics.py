@@ -56,6 +56,6 @@ def test_metrics_rejects_bad_arguments(built_lib):
     spec = BlockSpec(ndim=3, size=(4, 11, 9), delta=(0.25, 1.0 / 11, 1.0 / 9), scheme=abi.SCHEME_TENO5)
     with pytest.raises(abi.OSBError):  # fewer points than the periodic halo
         device_metrics(spec, _mesh_3d(spec), abi.METRIC_PERIODIC)
-    spec = BlockSpec(ndim=1, size=(16,), delta=(0.1,))
+    spec = BlockSpec(ndim=1, size=(16,), delta=(0.1,), scheme=abi.SCHEME_WENO5_JS)
     with pytest.raises(abi.OSBError):
         device_metrics(spec, [np.zeros(spec.shape)], abi.METRIC_EDGE)
