@@ -45,12 +45,13 @@ def parse():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="tgv",
-                    choices=["tgv", "sod", "tgv64", "kh_ensemble", "curv4", "c4w5", "tvd"],
+                    choices=["tgv", "sod", "tgv64", "kh_ensemble", "curv4", "c4w5", "tvd", "shock"],
                     help="tgv: the 256^3 supersonic TGV (headline); sod: the 400-point Sod tube; tgv64: the "
                          "64^3 central TGV; kh_ensemble: 64 uneven 2D Kelvin-Helmholtz instances in one "
                          "persistent launch per stage; curv4: the 4-block 3D curvilinear TENO5 case; c4w5: the "
                          "Central4-WENO5 benchmark's TGV (central KGP + WENO filter) at --size^3; tvd: the TGV "
-                         "app's TVD branch (central KGP + TVD filter) at --size^3")
+                         "app's TVD branch (central KGP + TVD filter) at --size^3; shock: the 2D inviscid shock "
+                         "reflection app (457 x 255, Dirichlet / extrapolation / symmetry boundaries)")
     ap.add_argument("--ensemble", type=int, default=64)
     ap.add_argument("--variant", type=int, default=0, help="x-sweep tiling variant when --fuse is given")
     ap.add_argument("--fuse", default="auto", choices=["auto", "0", "1"],
@@ -500,7 +501,7 @@ def _merge_errors(per_block):
 
 
 def secondary_arm(args):
-    """sod / tgv64 / kh_ensemble / curv4 / c4w5 / tvd workloads: FP32-residual throughput (whole batch per step), the FP64
+    """sod / tgv64 / kh_ensemble / curv4 / c4w5 / tvd / shock workloads: FP32-residual throughput (whole batch per step), the FP64
     per-block path beside it, the FP32-vs-FP64 error after the timed steps' count, launches."""
     import torch
     from opensbli_gb300 import abi, autotune, problems
@@ -541,6 +542,15 @@ def secondary_arm(args):
                 "RK-LS3, non-linear WENO3-Z filter (Ducros 0.05) after every step, periodic" % n)
         bytes_pt = 4 * 5 * 8
         cpu_args = None
+    elif args.workload == "shock":
+        blocks = [problems.shock_reflection(457, 255)]
+        dt = 0.1
+        rk = "ls3"
+        work = ("2D inviscid shock reflection 457 x 255 (350 x 115, M=2), WENO5-Z (simple average), RK-LS3, "
+                "Dirichlet inlet and top, extrapolation outlet, symmetry wall, dt 0.1 as the app")
+        bytes_pt = 4 * 4 * 8
+        cpu_args = ("shock_reflection", {"OSB_NP0": 457, "OSB_NP1": 255, "OSB_DT": 0.1}, 457 * 255, 30,
+                    "the 457 x 255 shock reflection")
     elif args.workload == "tvd":
         n = args.size
         blocks = [problems.tgv_tvd(n, kappa=1.25)]

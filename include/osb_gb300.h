@@ -63,6 +63,10 @@ extern "C" {
 #define OSB_BC_INTERFACE 2   /* InterfaceBC between blocks (multi_block.py:48-107) */
 #define OSB_BC_EXTRAP0 3     /* ExtrapolationBC order 0 (extrapolation.py:29-38), halo fill only */
 #define OSB_BC_EXTRAP1 4     /* ExtrapolationBC order 1 (extrapolation.py:39-53), halo fill only */
+#define OSB_BC_SYMMETRY 5    /* SymmetryBC, Cartesian (symmetry.py:23-50): halo layer k = the point k
+                                inside, normal momentum negated; the boundary plane unchanged */
+#define OSB_BC_DIRICHLET 6   /* DirichletBC (dirichlet.py:27-41): the boundary plane and its halo
+                                layers set from osb_block_desc.dirichlet */
 
 /* Convective split form of OSB_SCHEME_CENTRAL4 (physical_models/split_forms.py). */
 #define OSB_SPLIT_FEIEREISEN 0 /* skew-symmetric form, split_forms.py:111-145 */
@@ -123,6 +127,11 @@ typedef struct osb_block_desc {
   double ducros_check;       /* filter flux where max kappa over the interface stencil > this */
   double ducros_select;      /* filter applied where max kappa around the point >= this */
   double tvd_kappa;          /* OSB_FILTER_TVD: the filter strength kappa_TVD */
+  /* OSB_BC_DIRICHLET face (d, side): device array of the conserved variables the BC's
+   * equations give on the boundary plane and its bc_depth halo layers, [v][layer][t]: layer l
+   * at index -depth + l (side 0) or N-1 + l (side 1) along d, t over the whole allocated
+   * extent of the other used directions (lower direction fastest).  NULL elsewhere. */
+  const double* dirichlet[3][2];
 } osb_block_desc;
 
 /* ---- library / context ------------------------------------------------------------- */
@@ -272,8 +281,8 @@ int osb_stage_noalloc(const osb_block_desc* desc, int rk_kind, double A, double 
 int osb_metrics(const osb_block_desc* desc, const double* const* x, double* const* met, int fill, void* stream);
 
 /* Binding check: writes sizeof(osb_block_desc) and the byte offsets of size, bc, iface, gama,
- * delta, q, rkold, metric, split_form, ducros_check and tvd_kappa into out[0..11] (n >= 12).
- * Needs no GPU. */
+ * delta, q, rkold, metric, split_form, ducros_check, tvd_kappa and dirichlet into out[0..12]
+ * (n >= 13).  Needs no GPU. */
 int osb_desc_layout(long long* out, int n);
 
 #ifdef __cplusplus

@@ -34,6 +34,8 @@ BC_ZERO_GRAD = 1
 BC_INTERFACE = 2
 BC_EXTRAP0 = 3
 BC_EXTRAP1 = 4
+BC_SYMMETRY = 5
+BC_DIRICHLET = 6
 SPLIT_FEIEREISEN = 0
 SPLIT_KGP = 1
 FILTER_NONE = 0
@@ -107,6 +109,7 @@ class BlockDesc(ctypes.Structure):
         ("ducros_check", ctypes.c_double),
         ("ducros_select", ctypes.c_double),
         ("tvd_kappa", ctypes.c_double),
+        ("dirichlet", (ctypes.c_void_p * 2) * 3),
     ]
 
 
@@ -114,11 +117,12 @@ def layout_signature():
     """(sizeof, offsets...) of BlockDesc, compared with the C side in the tests."""
     offs = [BlockDesc.size.offset, BlockDesc.bc.offset, BlockDesc.iface.offset, BlockDesc.gama.offset,
             BlockDesc.delta.offset, BlockDesc.q.offset, BlockDesc.rkold.offset, BlockDesc.metric.offset,
-            BlockDesc.split_form.offset, BlockDesc.ducros_check.offset, BlockDesc.tvd_kappa.offset]
+            BlockDesc.split_form.offset, BlockDesc.ducros_check.offset, BlockDesc.tvd_kappa.offset,
+            BlockDesc.dirichlet.offset]
     return [ctypes.sizeof(BlockDesc)] + offs
 
 
-def make_desc(spec, q_ptrs, rk_ptrs, metric_ptrs=None):
+def make_desc(spec, q_ptrs, rk_ptrs, metric_ptrs=None, dirichlet_ptrs=None):
     """Fill a BlockDesc from a BlockSpec (see backend.py) and raw array addresses."""
     d = BlockDesc()
     d.ndim = spec.ndim
@@ -157,6 +161,9 @@ def make_desc(spec, q_ptrs, rk_ptrs, metric_ptrs=None):
     if metric_ptrs:
         for i, p in enumerate(metric_ptrs):
             d.metric[i] = p
+    if dirichlet_ptrs:
+        for (i, side), p in dirichlet_ptrs.items():
+            d.dirichlet[i][side] = p
     return d
 
 

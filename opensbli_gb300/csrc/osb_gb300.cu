@@ -295,6 +295,79 @@ __global__ void k_extrap(BlockK b, int nv, int d, int side, int depth, int order
   }
 }
 
+// Transverse point t of a face normal to d over the whole allocated extent of the other used
+// directions (lower direction fastest): its coordinates, halo included.
+__device__ __forceinline__ void face_point(const BlockK& b, int d, int halo, int t, int (&c)[3]) {
+  int r = t;
+  for (int e = 0; e < 3; ++e) {
+    if (e == d) {
+      c[e] = 0;
+      continue;
+    }
+    const int ext = e < b.ndim ? b.n[e] + 2 * halo : 1;
+    c[e] = r % ext - (e < b.ndim ? halo : 0);
+    r /= ext;
+  }
+}
+
+__host__ __device__ inline int face_extent(const BlockK& b, int d, int halo) {
+  int t = 1;
+  for (int e = 0; e < b.ndim; ++e)
+    if (e != d) t *= b.n[e] + 2 * halo;
+  return t;
+}
+
+// Symmetry face (symmetry.py:23-50 as generated for a Cartesian block): halo layer k = 1..depth
+// receives the point k inside the boundary plane (side 0: -k from +k; side 1: N-1+k from
+// N-1-k) with the momentum normal to the face negated; the plane itself is unchanged.  Over the
+// whole transverse allocation.
+__global__ void k_symmetry(BlockK b, int nv, int d, int side, int depth, int halo, int fields) {
+  const int total = face_extent(b, d, halo);
+  const int base = side == 0 ? 0 : b.n[d] - 1;
+  const int o = b.st[d] * (side == 0 ? -1 : 1);
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+    int c[3];
+    face_point(b, d, halo, t, c);
+    c[d] = base;
+    const int id = lin(b, c[0], c[1], c[2]);
+    for (int k = 1; k <= depth; ++k)
+      for (int v = 0; v < nv; ++v) {
+        const bool normal = v == 1 + d;
+        if (fields & BC_Q) {
+          const double x = b.q[v][id - k * o];
+          b.q[v][id + k * o] = normal ? -1.0 * x : x;
+        }
+        if ((fields & BC_QF) && b.qf[0]) {
+          const float x = b.qf[v][id - k * o];
+          b.qf[v][id + k * o] = normal ? -x : x;
+        }
+      }
+  }
+}
+
+// Dirichlet face (dirichlet.py:27-41): the boundary plane and its `depth` halo layers take the
+// values of the BC's equations, vals[v][layer][t] (layer l at -depth + l on side 0, N-1 + l on
+// side 1), over the whole transverse allocation.
+__global__ void k_dirichlet(BlockK b, int nv, int d, int side, int depth, int halo, const double* __restrict__ vals,
+                            int fields) {
+  const int tn = face_extent(b, d, halo);
+  const int layers = depth + 1;
+  const int total = tn * layers;
+  const int c0 = side == 0 ? -depth : b.n[d] - 1;
+  for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < total; u += gridDim.x * blockDim.x) {
+    const int l = u / tn, t = u - l * tn;
+    int c[3];
+    face_point(b, d, halo, t, c);
+    c[d] = c0 + l;
+    const int id = lin(b, c[0], c[1], c[2]);
+    for (int v = 0; v < nv; ++v) {
+      const double x = vals[((size_t)v * layers + l) * tn + t];
+      if (fields & BC_Q) b.q[v][id] = x;
+      if ((fields & BC_QF) && b.qf[0]) b.qf[v][id] = d2f_rn(x);
+    }
+  }
+}
+
 // Block interface (multi_block.py:11-107, InterfaceBC with identity orientation): the halo
 // layers of face (d, side) of dst receive the `depth` layers of src next to its face
 // (d, sside).  The transverse range is the interior of the face (full = 0) or that plus
@@ -642,6 +715,21 @@ int apply_bc(osb_ctx* c, int fields = BC_BOTH) {
                                                                   kind == OSB_BC_EXTRAP1, fields);
             timing_end(c);
             c->launches++;
+          } else if (kind == OSB_BC_SYMMETRY) {
+            const long tr = face_extent(bl.k, d, bl.d.halo);
+            timing_begin(c, FAM_BC);
+            k_symmetry<<<grid_for(c, tr, 128), 128, 0, c->stream>>>(bl.k, nv, d, side, side ? dep1 : dep0,
+                                                                    bl.d.halo, fields);
+            timing_end(c);
+            c->launches++;
+          } else if (kind == OSB_BC_DIRICHLET) {
+            const int dep = side ? dep1 : dep0;
+            const long tr = (long)face_extent(bl.k, d, bl.d.halo) * (dep + 1);
+            timing_begin(c, FAM_BC);
+            k_dirichlet<<<grid_for(c, tr, 128), 128, 0, c->stream>>>(bl.k, nv, d, side, dep, bl.d.halo,
+                                                                     bl.d.dirichlet[d][side], fields);
+            timing_end(c);
+            c->launches++;
           } else if (kind == OSB_BC_PERIODIC) {
             return fail(OSB_EINVAL, "periodic boundary on one side only (block %zu dir %d)", ib, d);
           }
@@ -815,7 +903,20 @@ bool check_desc(const osb_block_desc* d, std::string& why) {
   for (int i = 0; i < d->ndim; ++i)
     for (int s = 0; s < 2; ++s) {
       const int k = d->bc[i][s];
-      if (k < OSB_BC_PERIODIC || k > OSB_BC_EXTRAP1) { why = "unknown boundary kind"; return false; }
+      if (k < OSB_BC_PERIODIC || k > OSB_BC_DIRICHLET) { why = "unknown boundary kind"; return false; }
+      const int dep = d->bc_depth[i][s] > 0 ? d->bc_depth[i][s] : 4;
+      if ((k == OSB_BC_SYMMETRY || k == OSB_BC_DIRICHLET) && (dep > d->halo || dep >= d->size[i])) {
+        why = "symmetry / Dirichlet depth must be below the halo and the block size";
+        return false;
+      }
+      if (k == OSB_BC_SYMMETRY && d->metric[9]) {
+        why = "the symmetry boundary is implemented for Cartesian blocks";
+        return false;
+      }
+      if (k == OSB_BC_DIRICHLET && !d->dirichlet[i][s]) {
+        why = "a Dirichlet face needs its values (osb_block_desc.dirichlet)";
+        return false;
+      }
       if ((k == OSB_BC_EXTRAP0 || k == OSB_BC_EXTRAP1) &&
           (d->scheme == OSB_SCHEME_CENTRAL4 || d->viscous != OSB_VISC_NONE)) {
         why = "extrapolation boundaries with central derivatives need the Carpenter boundary closures";
@@ -886,7 +987,7 @@ int osb_last_error(char* buf, size_t n) {
 }
 
 int osb_desc_layout(long long* out, int n) {
-  if (!out || n < 12) return fail(OSB_EINVAL, "need 12 slots");
+  if (!out || n < 13) return fail(OSB_EINVAL, "need 13 slots");
   out[0] = sizeof(osb_block_desc);
   out[1] = offsetof(osb_block_desc, size);
   out[2] = offsetof(osb_block_desc, bc);
@@ -899,6 +1000,7 @@ int osb_desc_layout(long long* out, int n) {
   out[9] = offsetof(osb_block_desc, split_form);
   out[10] = offsetof(osb_block_desc, ducros_check);
   out[11] = offsetof(osb_block_desc, tvd_kappa);
+  out[12] = offsetof(osb_block_desc, dirichlet);
   return OSB_OK;
 }
 
@@ -1706,6 +1808,13 @@ extern "C" int osb_stage_noalloc(const osb_block_desc* d, int rk_kind, double A,
             if (e != dd) tr *= k.n[e];
           k_extrap<<<grid_for(&c, tr, 128), 128, 0, c.stream>>>(k, nv, dd, side, side ? dep1 : dep0,
                                                                 kind == OSB_BC_EXTRAP1, BC_BOTH);
+        } else if (kind == OSB_BC_SYMMETRY) {
+          k_symmetry<<<grid_for(&c, face_extent(k, dd, d->halo), 128), 128, 0, c.stream>>>(
+              k, nv, dd, side, side ? dep1 : dep0, d->halo, BC_BOTH);
+        } else if (kind == OSB_BC_DIRICHLET) {
+          const int dep = side ? dep1 : dep0;
+          k_dirichlet<<<grid_for(&c, (long)face_extent(k, dd, d->halo) * (dep + 1), 128), 128, 0, c.stream>>>(
+              k, nv, dd, side, dep, d->halo, d->dirichlet[dd][side], BC_BOTH);
         } else if (kind == OSB_BC_PERIODIC) {
           return fail(OSB_EINVAL, "periodic boundary on one side only (dir %d)", dd);
         } else if (kind == OSB_BC_INTERFACE) {

@@ -274,6 +274,51 @@ def curvilinear_wave_2d(n=128, scheme=abi.SCHEME_WENO5_Z, averaging=abi.AVG_ROE)
     return spec, q, metrics_central4(spec, [x0, x1], periodic_from_interior=True)
 
 
+def shock_reflection(n0=457, n1=255, sizes=None):
+    """2D inviscid oblique-shock reflection of apps/inviscid_shock_reflection/inviscid_shock.py
+    on a 350 x 115 box (Delta = 350/(n0-1), 115/(n1-1)), M = 2, gama = 1.4, WENO5-Z (simple
+    average, LLF): uniform free stream (rho = 1, u = (1, 0), p = 1/(gama M^2)); Dirichlet inlet
+    (free stream) on the left over the boundary plane and 3 halo layers, zeroth-order
+    extrapolation on the right, symmetry (inviscid wall) at the bottom, Dirichlet at the top over
+    the plane and 4 halo layers with the post-shock state (rho 1.129734572, u 0.9667023804242755,
+    -0.052106102140246795, p 0.211869) from x = 40 and the free stream (p 0.178571) before it --
+    values, literals and operation order of the generated boundary and initialisation kernels."""
+    if sizes is not None:
+        n0, n1 = sizes
+    gama, minf = 1.4, 2.0
+    spec = BlockSpec(ndim=2, size=(n0, n1), scheme=abi.SCHEME_WENO5_Z, averaging=abi.AVG_SIMPLE,
+                     bc=[[abi.BC_DIRICHLET, abi.BC_EXTRAP0], [abi.BC_SYMMETRY, abi.BC_DIRICHLET]],
+                     bc_depth=[[3, 4], [4, 4]], delta=(350.0 / (n0 - 1), 115.0 / (n1 - 1)), gama=gama, Minf=minf)
+    inv_gm1 = 1.0 / (-1 + gama)
+    p_inf = 1.0 * (1.0 / gama) * (minf ** -2.0)
+
+    def cons(d, u0, u1, p):
+        return [d, d * u0, d * u1, p * inv_gm1 + 0.5 * d * ((u0 * u0) + (u1 * u1))]
+
+    free = cons(1.0, 1.0, 0.0, p_inf)
+    q = [np.full(spec.shape, v) for v in free]
+    h = spec.halo
+    # left inlet: plane x = 0 and 3 halo layers, every allocated y
+    dep0 = spec.bc_depth[0][0]
+    left = np.empty((4, dep0 + 1, n1 + 2 * h))
+    for v in range(4):
+        left[v] = free[v]
+    # top: plane y = n1-1 and 4 halo layers, every allocated x; x = Delta0 * i
+    dep1 = spec.bc_depth[1][1]
+    x = spec.delta[0] * np.arange(-h, n0 + h, dtype=np.float64)
+    pre = x < 40.0
+    d = np.where(pre, 1.0, 1.129734572)
+    u0 = np.where(pre, 1.0, 0.9667023804242755)
+    u1 = np.where(pre, 0.0, -0.052106102140246795)
+    p = np.where(pre, 0.178571, 0.211869)
+    top_row = cons(d, u0, u1, p)
+    top = np.empty((4, dep1 + 1, n0 + 2 * h))
+    for v in range(4):
+        top[v] = top_row[v][None, :]
+    spec.dirichlet = {(0, 0): left, (1, 1): top}
+    return spec, q
+
+
 # ---------------------------------------------------------------------------------------
 # Multi-block topologies
 

@@ -44,6 +44,7 @@ class Solver:
         self.q = []
         self.rk = []
         self.met = []
+        self._dirichlet = []
         self._descs = []
         try:
             for i, item in enumerate(specs_states):
@@ -67,8 +68,14 @@ class Solver:
                           for a in met]
                     mp = [None if a is None else a.data_ptr() for a in mt]
                 self.met.append(mt)
+                dp = None
+                if spec.dirichlet:
+                    dt_ = {k: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).to(self.device)
+                           for k, a in spec.dirichlet.items()}
+                    self._dirichlet.append(dt_)
+                    dp = {k: a.data_ptr() for k, a in dt_.items()}
                 d = abi.make_desc(spec, [q[v].data_ptr() for v in range(spec.nvars)],
-                                  [r[v].data_ptr() for v in range(spec.nvars)], mp)
+                                  [r[v].data_ptr() for v in range(spec.nvars)], mp, dp)
                 self._descs.append(d)
                 bid = ctypes.c_int()
                 torch.cuda.synchronize(self.device)

@@ -40,6 +40,9 @@ class BlockSpec:
     ducros_check: float = 0.05
     ducros_select: float = 0.05
     tvd_kappa: float = 1.0
+    # Dirichlet faces: {(direction, side): array [v][layer][t]} of the values on the boundary
+    # plane and its bc_depth halo layers (osb_block_desc.dirichlet)
+    dirichlet: dict = None
 
     def __post_init__(self):
         self.size = tuple(int(s) for s in self.size)

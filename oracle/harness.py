@@ -82,9 +82,12 @@ class OracleBlocks:
         else:
             self.rk = [[np.ascontiguousarray(a, dtype=np.float64).copy() for a in r] for r in rkold]
         arr = (abi.BlockDesc * len(self.specs))()
+        self.dirichlet = [{k: np.ascontiguousarray(a, dtype=np.float64) for k, a in (s.dirichlet or {}).items()}
+                          for s in self.specs]
         for i, s in enumerate(self.specs):
             mp = None if self.met[i] is None else [None if a is None else _ptr(a) for a in self.met[i]]
-            arr[i] = abi.make_desc(s, [_ptr(a) for a in self.q[i]], [_ptr(a) for a in self.rk[i]], mp)
+            dp = {k: _ptr(a) for k, a in self.dirichlet[i].items()} or None
+            arr[i] = abi.make_desc(s, [_ptr(a) for a in self.q[i]], [_ptr(a) for a in self.rk[i]], mp, dp)
         self.desc = arr
 
     def residual(self, ib=0):

@@ -30,7 +30,8 @@
  *    schemes/spatial/shock_capturing.py:619-766)
  *  - low-storage RK3 (rk_LS.py:185-215) and SBLI RK3 (rk_sbli.py:138-154)
  *  - periodic exchange (periodic.py:53-71, opsc.py:1026-1064), zero-gradient
- *    (zero_gradient_outlet.py:11-23), block interfaces (multi_block.py:48-107)
+ *    (zero_gradient_outlet.py:11-23), extrapolation (extrapolation.py:29-53), symmetry
+ *    (symmetry.py:23-50), Dirichlet (dirichlet.py:27-41), block interfaces (multi_block.py:48-107)
  *  - TGV reductions (compressible_TGV.py:176-206)
  */
 #include <math.h>
@@ -1272,6 +1273,60 @@ static void extrap_face(osb_block_desc* b, const geom_t* g, int d, int side, int
       }
 }
 
+/* Visits the transverse points of a face normal to d over the whole allocation of the other
+ * used directions (lower direction fastest), calling fn with the point's coordinates (the d
+ * coordinate set to `at`) and the transverse index. */
+typedef void (*face_fn)(osb_block_desc* b, const geom_t* g, int d, int side, int depth, const int* c, long t);
+
+static void for_face(osb_block_desc* b, const geom_t* g, int d, int side, int depth, int at, face_fn fn) {
+  const int nd = b->ndim;
+  int lo[3], hi[3];
+  for (int e = 0; e < 3; ++e) {
+    lo[e] = e < nd ? -b->halo : 0;
+    hi[e] = e < nd ? g->n[e] + b->halo : 1;
+  }
+  lo[d] = at;
+  hi[d] = at + 1;
+  long t = 0;
+  for (int k = lo[2]; k < hi[2]; ++k)
+    for (int j = lo[1]; j < hi[1]; ++j)
+      for (int i = lo[0]; i < hi[0]; ++i) {
+        const int c[3] = {i, j, k};
+        fn(b, g, d, side, depth, c, t++);
+      }
+}
+
+/* Symmetry (symmetry.py:23-50 as generated for a Cartesian block): halo layer m = 1..depth
+ * receives the point m inside the boundary plane, the momentum normal to the face times -1.0;
+ * the plane itself is unchanged. */
+static void symmetry_point(osb_block_desc* b, const geom_t* g, int d, int side, int depth, const int* c, long t) {
+  (void)t;
+  const int nv = b->ndim + 2;
+  const long id = gid(g, c[0], c[1], c[2]);
+  const long o = g->st[d] * (side == 0 ? -1 : 1);
+  for (int m = 1; m <= depth; ++m)
+    for (int v = 0; v < nv; ++v) {
+      const double x = b->q[v][id - m * o];
+      b->q[v][id + m * o] = v == 1 + d ? -1.0 * x : x;
+    }
+}
+
+/* Dirichlet (dirichlet.py:27-41): the boundary plane and its depth halo layers take the BC's
+ * values, dirichlet[d][side][v][layer][t], layer l at -depth + l (side 0) or N-1 + l (side 1). */
+static void dirichlet_point(osb_block_desc* b, const geom_t* g, int d, int side, int depth, const int* c, long t) {
+  const int nv = b->ndim + 2;
+  long tn = 1;
+  for (int e = 0; e < b->ndim; ++e)
+    if (e != d) tn *= g->n[e] + 2 * b->halo;
+  const double* vals = b->dirichlet[d][side];
+  for (int l = 0; l <= depth; ++l) {
+    int p[3] = {c[0], c[1], c[2]};
+    p[d] = (side == 0 ? -depth : g->n[d] - 1) + l;
+    const long id = gid(g, p[0], p[1], p[2]);
+    for (int v = 0; v < nv; ++v) b->q[v][id] = vals[((long)v * (depth + 1) + l) * tn + t];
+  }
+}
+
 /* Block interface (multi_block.py:11-107, identity orientation, matching faces normal to the
  * same direction): the halo layers of face (d, side) receive the neighbour's layers adjacent to
  * its face (d, f->side).  `full` = 0 copies the interior of the face only; `full` = 1 also the
@@ -1318,6 +1373,12 @@ int oracle_apply_bc(osb_block_desc* blocks, int nblocks, int zero_grad_only) {
           if (pass == 1 && kind == OSB_BC_ZERO_GRAD) zero_grad_face(b, &g, d, side, depth);
           if (pass == 1 && (kind == OSB_BC_EXTRAP0 || kind == OSB_BC_EXTRAP1))
             extrap_face(b, &g, d, side, depth, kind == OSB_BC_EXTRAP1);
+          if (pass == 1 && kind == OSB_BC_SYMMETRY)
+            for_face(b, &g, d, side, depth, side == 0 ? 0 : g.n[d] - 1, symmetry_point);
+          if (pass == 1 && kind == OSB_BC_DIRICHLET) {
+            if (!b->dirichlet[d][side]) return -1;
+            for_face(b, &g, d, side, depth, 0, dirichlet_point);
+          }
           if (pass != 1 && kind == OSB_BC_INTERFACE && !zero_grad_only)
             interface_face(blocks, b, &g, d, side, depth, pass == 2);
         }

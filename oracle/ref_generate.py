@@ -337,6 +337,57 @@ def case_tgv_kgp_tvd():
     return block, params
 
 
+def case_shock_reflection():
+    """2D inviscid oblique-shock reflection (``apps/inviscid_shock_reflection/inviscid_shock.py``)
+    with the app's boundaries -- Dirichlet free-stream inlet, zeroth-order extrapolation outlet,
+    symmetry (inviscid wall) bottom, Dirichlet top carrying the post-shock state from x = 40 --
+    and its ``weno`` branch with the characteristic LLF WENO5-Z flux (simple average) and the
+    standard RK-LS3 (the app's HLLC-LM flux and SSP coefficients are not on this path)."""
+    import copy
+    from opensbli import (SimulationBlock, GridBasedInitialisation, GridVariable, DataObject, ConstantObject,
+                          parse_expr, SimpleAverage, LFWeno, RungeKuttaLS, DirichletBC, ExtrapolationBC,
+                          SymmetryBC)
+    ndim = 2
+    sim = _euler_equations(ndim, "Weno")
+    cr = _constituents(ndim)
+    block = SimulationBlock(ndim, block_number=0)
+    local_dict = {"block": block, "GridVariable": GridVariable, "DataObject": DataObject}
+    for con in ("gama", "Minf"):
+        local_dict[con] = ConstantObject(con)
+    pe = lambda e: parse_expr(e, local_dict=local_dict)  # noqa: E731
+    x0 = pe("Eq(DataObject(x0), block.deltas[0]*block.grid_indexes[0])")
+    x1 = pe("Eq(DataObject(x1), block.deltas[1]*block.grid_indexes[1])")
+    d_in, u0_in, u1_in = pe("Eq(GridVariable(d), 1.0)"), pe("Eq(GridVariable(u0), 1.0)"), pe("Eq(GridVariable(u1), 0.0)")
+    p_in = pe("Eq(GridVariable(p), 1.0/(gama*Minf**2.0))")
+    rho, rhou0, rhou1 = pe("Eq(DataObject(rho), d)"), pe("Eq(DataObject(rhou0), d*u0)"), pe("Eq(DataObject(rhou1), d*u1)")
+    rhoE = pe("Eq(DataObject(rhoE), p/(gama-1) + 0.5* d *(u0**2+u1**2))")
+    initial = GridBasedInitialisation()
+    initial.add_equations([x0, x1, d_in, u0_in, u1_in, p_in, rho, rhou0, rhou1, rhoE])
+    schemes = {}
+    LF = LFWeno(order=5, formulation="Z", averaging=SimpleAverage([0, 1]), flux_type="LLF")
+    schemes[LF.name] = LF
+    rk = RungeKuttaLS(3)
+    schemes[rk.name] = rk
+    block.set_discretisation_schemes(schemes)
+    pre, post = 1.0 / (1.4 * 4.0), 1.0 / (1.4 * 4.0) * 1.18646663
+    shock_loc = pe("Eq(GridVariable(shock_loc), 40.0)")
+    upper = [pe("Eq(GridVariable(x), DataObject(x0))"), shock_loc,
+             pe("Eq(GridVariable(d), Piecewise((1.0 ,x<shock_loc),(1.129734572, x>=shock_loc),(1.0,True)))"),
+             pe("Eq(GridVariable(u0), Piecewise((1.0 ,x<shock_loc),(0.9667023804242755, x>=shock_loc),(1.0,True)))"),
+             pe("Eq(GridVariable(u1), Piecewise((0.0 ,x<shock_loc),(-0.052106102140246795, x>=shock_loc),(1.0,True)))"),
+             pe("Eq(GridVariable(p), Piecewise( (%f,x<shock_loc),(%f, x>=shock_loc),(1.0,True)))" % (pre, post)),
+             rho, rhou0, rhou1, rhoE]
+    bcs = [DirichletBC(0, 0, [d_in, u0_in, u1_in, p_in, rho, rhou0, rhou1, rhoE]),
+           ExtrapolationBC(0, 1, order=0), SymmetryBC(1, 0), DirichletBC(1, 1, upper)]
+    block.set_block_boundaries(bcs)
+    block.set_equations([copy.deepcopy(cr), copy.deepcopy(sim), initial])
+    block.discretise()
+    p = {"gama": "1.4", "Minf": "2.0", "dt": 'osb_env_double("OSB_DT", 0.1)', "niter": 'osb_env_int("OSB_NITER", 1)',
+         "block0np0": 'osb_env_int("OSB_NP0", 457)', "block0np1": 'osb_env_int("OSB_NP1", 255)',
+         "Delta0block0": "350.0/(block0np0-1)", "Delta1block0": "115.0/(block0np1-1)"}
+    return block, p
+
+
 def case_kh_weno5z():
     """2D Kelvin-Helmholtz, Euler, characteristic LLF WENO5-Z with Roe average, periodic,
     classic 3-register SBLI RK3 (``apps/kelvin_helmholtz/kelvin_helmholtz.py:20-130``).  The
@@ -455,6 +506,7 @@ CASES = {
     "tgv_central": case_tgv_central,
     "tgv_kgp": lambda: central_split_block("KGP", "enthalpy"),
     "tgv_kgp_tvd": case_tgv_kgp_tvd,
+    "shock_reflection": case_shock_reflection,
     "kh_weno5z": case_kh_weno5z,
     "curv_weno5z": case_curv_weno5z,
 }

@@ -44,6 +44,8 @@ CASES = {
                        {"OSB_NP0": 12, "OSB_NP1": 12, "OSB_NP2": 12}, 3.385e-3, [1, 3, 30], None),
     "kh_weno5z_24_perturbed": ("kh_weno5z", lambda: problems.kh(24, amp=1.0, phase=0.0),
                                {"OSB_NP0": 24, "OSB_NP1": 24}, 2e-4, [1, 3, 6], (1e-3, 12)),
+    "shock_reflection_64x32_perturbed": ("shock_reflection", lambda: problems.shock_reflection(64, 32),
+                                         {"OSB_NP0": 64, "OSB_NP1": 32}, 0.5, [1, 3, 30], (1e-2, 4)),
     # the curvilinear solver computes its metrics from its own grid; they match
     # problems.metrics_central4 bit for bit
     "curv_weno5z_32": ("curv_weno5z", lambda: problems.curvilinear_wave_2d(32),

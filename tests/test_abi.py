@@ -26,8 +26,8 @@ def test_library_exports_every_symbol(built_lib):
 
 def test_descriptor_layout(built_lib):
     lib = abi.load_library()
-    out = (ctypes.c_longlong * 12)()
-    assert lib.osb_desc_layout(out, 12) == 0
+    out = (ctypes.c_longlong * 13)()
+    assert lib.osb_desc_layout(out, 13) == 0
     assert list(out) == abi.layout_signature()
 
 
@@ -35,4 +35,4 @@ def test_version_and_errors(built_lib):
     lib = abi.load_library()
     assert lib.osb_version() == 100
     assert lib.osb_desc_layout(None, 0) == abi.OSB_EINVAL
-    assert "12 slots" in abi.last_error(lib)
+    assert "13 slots" in abi.last_error(lib)

@@ -23,6 +23,8 @@ CASES = {
     "tgv_central_12": (lambda: problems.tgv(12, minf=0.1, scheme=abi.SCHEME_CENTRAL4), "ls3", None, 1e-12),
     "kh_weno5z_24_perturbed": (lambda: problems.kh(24, amp=1.0, phase=0.0), "sbli3", (1e-3, 12), 1e-9),
     "curv_weno5z_32": (lambda: problems.curvilinear_wave_2d(32), "ls3", None, 1e-12),
+    # Dirichlet inlet and top (post-shock state from x = 40), extrapolation outlet, symmetry wall
+    "shock_reflection_64x32_perturbed": (lambda: problems.shock_reflection(64, 32), "ls3", (1e-2, 4), 1e-12),
 }
 
 
