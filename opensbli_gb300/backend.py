@@ -179,6 +179,15 @@ def _bcs_of(block, central_only):
                 bc[d][side] = abi.BC_EXTRAP0 if b.order == 0 else abi.BC_EXTRAP1
                 hv = b.get_halo_values(block)
                 depth[d][side] = abs(hv[d][side])
+            elif type(b).__name__ == "SymmetryBC":
+                bc[d][side] = abi.BC_SYMMETRY
+                hv = b.get_halo_values(block)
+                depth[d][side] = abs(hv[d][side])
+            elif type(b).__name__ == "DirichletBC":
+                # the generated kernel covers the plane and the scheme's halo on that side
+                # (dirichlet.py:35-40: block.boundary_halos)
+                bc[d][side] = abi.BC_DIRICHLET
+                depth[d][side] = max(abs(h.get_halos(side)) for h in block.boundary_halos[d][side])
             else:
                 raise NotImplementedError("boundary condition %s is not supported" % type(b).__name__)
     return bc, depth
@@ -290,27 +299,67 @@ def block_spec(block, params):
     bc, depth = _bcs_of(block, scheme == abi.SCHEME_CENTRAL4)
     split = _split_form_of(block) if scheme == abi.SCHEME_CENTRAL4 else abi.SPLIT_FEIEREISEN
     filt, kappa = _filter_of(block, p)
-    return BlockSpec(ndim=nd, size=size, scheme=scheme, averaging=avg, viscous=visc, bc=bc, bc_depth=depth,
+    spec = BlockSpec(ndim=nd, size=size, scheme=scheme, averaging=avg, viscous=visc, bc=bc, bc_depth=depth,
                      split_form=split, filter=filt, tvd_kappa=kappa,
                      gama=_const_value("gama", p), Minf=_const_value("Minf", p, 1.0), Re=_const_value("Re", p, 1.0),
                      Pr=_const_value("Pr", p, 0.71), mu_const=1.0, eps=_const_value("eps", p, 1e-40),
                      teno_ct=_const_value("TENO_CT", p, 1e-6),
                      shock_filter_control=_const_value("shock_filter_control", p, 1.0), delta=delta)
+    if any(k == abi.BC_DIRICHLET for pair in bc for k in pair):
+        spec.dirichlet = dirichlet_faces(block, spec, params)
+    return spec
 
 
 def initial_state(block, spec, params):
     """Evaluate the block's GridBasedInitialisation equations on the host over every allocated
     point (the generated initialisation kernel's range -halo..N+halo), returning the
     conserved variables in OPS layout."""
+    values = _initial_values(block, spec, params)
+    order = ["rho"] + ["rhou%d" % d for d in range(spec.ndim)] + ["rhoE"]
+    return [np.ascontiguousarray(values[n]) for n in order]
+
+
+def dirichlet_faces(block, spec, params):
+    """Values of every DirichletBC face of the block on its boundary plane and halo layers, in
+    the layout osb_block_desc.dirichlet takes ([v][layer][t]): the BC's equations evaluated over
+    the allocation with the data objects the initialisation defines (the grid coordinates x0,
+    x1, ...), as the generated boundary kernel reads them."""
+    faces = {}
+    init = None
+    h = spec.halo
+    for d, pair in enumerate(block.boundary_types):
+        for side, b in enumerate(pair):
+            if spec.bc[d][side] != abi.BC_DIRICHLET:
+                continue
+            if init is None:
+                init = _initial_values(block, spec, params)
+            vals = _initial_values(block, spec, params, equations=b.equations, values=dict(init))
+            order = ["rho"] + ["rhou%d" % e for e in range(spec.ndim)] + ["rhoE"]
+            depth = spec.bc_depth[d][side]
+            ax = spec.ndim - 1 - d
+            n = spec.size[d]
+            first = h - depth if side == 0 else h + n - 1
+            out = []
+            for name in order:
+                a = np.moveaxis(np.asarray(vals[name]), ax, 0)[first:first + depth + 1]
+                # [layer][other axes, slowest first] -> [layer][t] with the lower direction fastest
+                out.append(a.reshape(depth + 1, -1))
+            faces[(d, side)] = np.ascontiguousarray(np.stack(out))
+    return faces
+
+
+def _initial_values(block, spec, params, equations=None, values=None):
+    """Evaluate equations (default: the block's GridBasedInitialisation) over every allocated
+    point with numpy; returns {name: array} of everything they define."""
     import sympy
     from sympy import flatten
     from opensbli.initialisation.gridbasedinit import GridBasedInitialisation
-    from opensbli.core.opensbliobjects import DataObject, ConstantObject
-    from opensbli.core.grid import GridVariable
     p = resolve_parameters(params)
-    inits = [ec for ec in block.list_of_equation_classes if isinstance(ec, GridBasedInitialisation)]
-    if not inits:
-        raise NotImplementedError("block has no GridBasedInitialisation")
+    if equations is None:
+        inits = [ec for ec in block.list_of_equation_classes if isinstance(ec, GridBasedInitialisation)]
+        if not inits:
+            raise NotImplementedError("block has no GridBasedInitialisation")
+        equations = flatten([e.equations for e in inits])
     env = {}
     idx = [spec.grid_index(d).astype(np.float64) for d in range(spec.ndim)]
     for d in range(spec.ndim):
@@ -319,8 +368,8 @@ def initial_state(block, spec, params):
     for k, v in p.items():
         env.setdefault(k, v)
     mods = [{"Abs": np.abs, "Piecewise": _np_piecewise}, "numpy"]
-    values = {}
-    for eq in flatten([e.equations for e in inits]):
+    values = {} if values is None else values
+    for eq in flatten(equations):
         lhs, rhs = eq.lhs, eq.rhs
         indexed = sorted(rhs.atoms(sympy.Indexed), key=str)
         dummies = {ix: sympy.Symbol("_ix%d" % i) for i, ix in enumerate(indexed)}
@@ -346,8 +395,7 @@ def initial_state(block, spec, params):
         name = str(lhs).split("[")[0]
         name = name[:-3] if name.endswith("_B%d" % block.blocknumber) else name
         values[name] = np.broadcast_to(np.asarray(val, dtype=np.float64), spec.shape)
-    order = ["rho"] + ["rhou%d" % d for d in range(spec.ndim)] + ["rhoE"]
-    return [np.ascontiguousarray(values[n]) for n in order]
+    return values
 
 
 def _np_piecewise(*args):

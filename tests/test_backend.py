@@ -157,3 +157,27 @@ def test_tvd_filter_detected():
         _backend_for("tgv_kgp_tvd", TGV_SUPERSONIC)
     be = _backend_for("tgv_kgp", TGV_SUPERSONIC)
     assert be.specs[0].filter == abi.FILTER_NONE
+
+
+@needs_ref
+def test_shock_reflection_boundaries_mapped():
+    """The shock-reflection app's DirichletBC / ExtrapolationBC / SymmetryBC map onto
+    OSB_BC_DIRICHLET (depth = the WENO halo on that side: 3 below, 4 above, as the generated
+    ranges), OSB_BC_EXTRAP0 and OSB_BC_SYMMETRY; the Dirichlet faces' values, evaluated from the
+    BCs' own equations (the top one from the grid coordinate x0), match problems.shock_reflection
+    to rounding (the generated kernel multiplies by 1/(gama-1) where SymPy divides)."""
+    nums = {"gama": "1.4", "Minf": "2.0", "dt": "0.1", "niter": "1", "block0np0": "64", "block0np1": "32",
+            "Delta0block0": "350.0/(block0np0-1)", "Delta1block0": "115.0/(block0np1-1)"}
+    be = _backend_for("shock_reflection", nums)
+    spec = be.specs[0]
+    ref, q = problems.shock_reflection(64, 32)
+    assert spec.bc == ref.bc and spec.bc_depth == ref.bc_depth
+    assert spec.scheme == abi.SCHEME_WENO5_Z and spec.averaging == abi.AVG_SIMPLE
+    assert sorted(spec.dirichlet) == sorted(ref.dirichlet)
+    for k in ref.dirichlet:
+        assert spec.dirichlet[k].shape == ref.dirichlet[k].shape, k
+        assert np.allclose(spec.dirichlet[k], ref.dirichlet[k], rtol=1e-14, atol=0), k
+    from opensbli_gb300.backend import initial_state
+    q0 = initial_state(be.blocks[0], spec, nums)
+    for v in range(4):
+        assert np.allclose(q0[v], q[v], rtol=1e-14, atol=0), v
