@@ -22,6 +22,10 @@ RK3_LS_A = (0.0, -5.0 / 9.0, -153.0 / 128.0)    # rk_LS.py:116-118
 RK3_LS_B = (1.0 / 3.0, 15.0 / 16.0, 8.0 / 15.0)
 RK3_SBLI_NEW = (2.0 / 3.0, 5.0 / 12.0, 3.0 / 5.0)  # rk_sbli.py:75-77 (stage coefficients)
 RK3_SBLI_OLD = (1.0 / 4.0, 3.0 / 20.0, 3.0 / 5.0)  # (solution coefficients)
+# Three-stage third-order SSP coefficients of the low-storage form (rk_LS.py:102-106, Ruuth
+# 2005; the shock-reflection app's RungeKuttaLS(3, formulation='SSP'))
+RK3_SSP_A = (0.0, -2.915493957701923, 0.0)
+RK3_SSP_B = (0.924574112262461, 0.287712943868770, 0.626538293270800)
 
 
 def _cons(spec, rho, u, p):

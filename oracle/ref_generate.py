@@ -337,12 +337,13 @@ def case_tgv_kgp_tvd():
     return block, params
 
 
-def case_shock_reflection():
+def case_shock_reflection(formulation=None):
     """2D inviscid oblique-shock reflection (``apps/inviscid_shock_reflection/inviscid_shock.py``)
     with the app's boundaries -- Dirichlet free-stream inlet, zeroth-order extrapolation outlet,
     symmetry (inviscid wall) bottom, Dirichlet top carrying the post-shock state from x = 40 --
-    and its ``weno`` branch with the characteristic LLF WENO5-Z flux (simple average) and the
-    standard RK-LS3 (the app's HLLC-LM flux and SSP coefficients are not on this path)."""
+    and its ``weno`` branch with the characteristic LLF WENO5-Z flux (simple average; the app's
+    HLLC-LM flux is not on this path) and the standard RK-LS3, or with formulation='SSP' the
+    app's own three-stage SSP coefficients (rk_LS.py:102-106)."""
     import copy
     from opensbli import (SimulationBlock, GridBasedInitialisation, GridVariable, DataObject, ConstantObject,
                           parse_expr, SimpleAverage, LFWeno, RungeKuttaLS, DirichletBC, ExtrapolationBC,
@@ -366,7 +367,7 @@ def case_shock_reflection():
     schemes = {}
     LF = LFWeno(order=5, formulation="Z", averaging=SimpleAverage([0, 1]), flux_type="LLF")
     schemes[LF.name] = LF
-    rk = RungeKuttaLS(3)
+    rk = RungeKuttaLS(3, formulation=formulation)
     schemes[rk.name] = rk
     block.set_discretisation_schemes(schemes)
     pre, post = 1.0 / (1.4 * 4.0), 1.0 / (1.4 * 4.0) * 1.18646663
@@ -507,6 +508,7 @@ CASES = {
     "tgv_kgp": lambda: central_split_block("KGP", "enthalpy"),
     "tgv_kgp_tvd": case_tgv_kgp_tvd,
     "shock_reflection": case_shock_reflection,
+    "shock_reflection_ssp": lambda: case_shock_reflection("SSP"),
     "kh_weno5z": case_kh_weno5z,
     "curv_weno5z": case_curv_weno5z,
 }

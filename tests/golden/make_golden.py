@@ -46,6 +46,9 @@ CASES = {
                                {"OSB_NP0": 24, "OSB_NP1": 24}, 2e-4, [1, 3, 6], (1e-3, 12)),
     "shock_reflection_64x32_perturbed": ("shock_reflection", lambda: problems.shock_reflection(64, 32),
                                          {"OSB_NP0": 64, "OSB_NP1": 32}, 0.5, [1, 3, 30], (1e-2, 4)),
+    # the same with the app's own three-stage SSP coefficients
+    "shock_reflection_ssp_64x32_perturbed": ("shock_reflection_ssp", lambda: problems.shock_reflection(64, 32),
+                                             {"OSB_NP0": 64, "OSB_NP1": 32}, 0.5, [1, 3, 30], (1e-2, 4)),
     # the curvilinear solver computes its metrics from its own grid; they match
     # problems.metrics_central4 bit for bit
     "curv_weno5z_32": ("curv_weno5z", lambda: problems.curvilinear_wave_2d(32),

@@ -116,3 +116,26 @@ def test_dirichlet_needs_values(built_lib):
     spec.dirichlet = {(0, 0): spec.dirichlet[(0, 0)]}  # the top face has none
     with pytest.raises(abi.OSBError):
         Solver([(spec, q)], precision="fp64", rk="ls3")
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("fp32", 1e-6)])
+def test_shock_reflection_ssp_rk3(built_lib, precision, tol):
+    """The shock-reflection app's own time integrator, the three-stage SSP coefficients of the
+    low-storage form (A = 0 on the first and the last stage), 10 steps against the reference's
+    generated solver (golden, 30 stages)."""
+    import os
+    from opensbli_gb300.solver import Solver
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden",
+                             "shock_reflection_ssp_64x32_perturbed.npz"))
+    spec, q = problems.shock_reflection(64, 32)
+    rng = np.random.default_rng(4)
+    q = [a * (1.0 + 1e-2 * rng.standard_normal(a.shape)) for a in q]
+    s = Solver([(spec, q)], precision=precision, rk=(abi.RK_LOW_STORAGE, problems.RK3_SSP_A, problems.RK3_SSP_B))
+    s.apply_bc()
+    s.step(float(g["dt"]), 10)
+    got = s.state(0)
+    s.close()
+    sl = spec.interior()
+    ref = g["after_30"]
+    errs = [float(np.max(np.abs(got[v][sl] - ref[v]))) / float(np.max(np.abs(ref[v]))) for v in range(4)]
+    assert max(errs) < tol, errs

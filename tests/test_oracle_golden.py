@@ -25,6 +25,7 @@ CASES = {
     "curv_weno5z_32": (lambda: problems.curvilinear_wave_2d(32), "ls3", None, 1e-12),
     # Dirichlet inlet and top (post-shock state from x = 40), extrapolation outlet, symmetry wall
     "shock_reflection_64x32_perturbed": (lambda: problems.shock_reflection(64, 32), "ls3", (1e-2, 4), 1e-12),
+    "shock_reflection_ssp_64x32_perturbed": (lambda: problems.shock_reflection(64, 32), "ssp3", (1e-2, 4), 1e-12),
 }
 
 
@@ -44,6 +45,8 @@ def load_case(name):
 def rk_params(rk):
     if rk == "ls3":
         return abi.RK_LOW_STORAGE, problems.RK3_LS_A, problems.RK3_LS_B
+    if rk == "ssp3":
+        return abi.RK_LOW_STORAGE, problems.RK3_SSP_A, problems.RK3_SSP_B
     return abi.RK_SBLI3, problems.RK3_SBLI_NEW, problems.RK3_SBLI_OLD
 
 
