@@ -36,3 +36,23 @@ def test_version_and_errors(built_lib):
     assert lib.osb_version() == 100
     assert lib.osb_desc_layout(None, 0) == abi.OSB_EINVAL
     assert "13 slots" in abi.last_error(lib)
+
+
+def test_new_entry_points_reject_bad_arguments_without_a_gpu(built_lib):
+    """osb_metrics and osb_step_requests validate their arguments before touching the device."""
+    lib = abi.load_library()
+    vp = ctypes.c_void_p
+    assert lib.osb_metrics(None, None, None, 0, None) == abi.OSB_EINVAL
+    from opensbli_gb300 import problems
+    from opensbli_gb300.spec import BlockSpec
+    spec = BlockSpec(ndim=1, size=(16,), delta=(0.1,), scheme=abi.SCHEME_WENO5_JS)
+    d = abi.make_desc(spec, [0] * 5, [0] * 5)
+    xs = (vp * 3)(0, 0, 0)
+    ms = (vp * 10)(*([0] * 10))
+    assert lib.osb_metrics(ctypes.byref(d), xs, ms, abi.METRIC_EDGE, None) == abi.OSB_EINVAL
+    assert "2D and 3D" in abi.last_error(lib)
+    spec, _, _ = problems.curvilinear_wave_2d(16)
+    d = abi.make_desc(spec, [0] * 5, [0] * 5)
+    assert lib.osb_metrics(ctypes.byref(d), xs, ms, 7, None) == abi.OSB_EINVAL
+    assert "fill" in abi.last_error(lib)
+    assert lib.osb_step_requests(None, 1, None, None, 1e-3, 1) == abi.OSB_EINVAL
