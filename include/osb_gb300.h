@@ -173,7 +173,8 @@ int osb_step(osb_ctx* ctx, double dt, int nsteps);
  * The host-to-device copy of request r+1 and the device-to-host copy of request r-1 run on two
  * copy streams while request r computes (pinned host buffers for the overlap).  in[r] may
  * repeat; out[r] must not be read before the call returns.  Keeps four device staging buffers
- * of one request's size.  Synchronous: returns when every result is in host memory. */
+ * of one request's size.  Synchronous: returns when every result is in host memory, and on an
+ * error only after every copy it queued has finished. */
 int osb_step_requests(osb_ctx* ctx, int count, const double* const* in, double* const* out, double dt,
                       int nsteps);
 

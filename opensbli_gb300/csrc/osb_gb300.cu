@@ -1108,30 +1108,42 @@ int osb_step_requests(osb_ctx* c, int count, const double* const* in, double* co
   int rc = requests_setup(c);
   if (rc) return rc;
   const size_t bytes = c->stage_bytes;
+  // once copies are queued, an error waits for every stream before returning: the caller may
+  // free its host buffers as soon as the call returns
+  auto drain = [&](int code) -> int {
+    cudaStreamSynchronize(c->cs_in);
+    cudaStreamSynchronize(c->cs_out);
+    cudaStreamSynchronize(c->stream);
+    return code;
+  };
+  auto ck = [&](cudaError_t e, const char* what) -> int {
+    return e == cudaSuccess ? OSB_OK : drain(fail(OSB_ECUDA, "%s: %s", what, cudaGetErrorString(e)));
+  };
   // request r uses slot r & 1 in each direction; the copy of request r + 1 in and of r - 1 out
   // overlap the steps of request r
   auto h2d = [&](int r) -> int {
     const int k = r & 1;
-    if (r >= 2) OSB_CK(cudaStreamWaitEvent(c->cs_in, c->ev_used[k], 0));
-    OSB_CK(cudaMemcpyAsync(c->stage_in[k], in[r], bytes, cudaMemcpyHostToDevice, c->cs_in));
-    OSB_CK(cudaEventRecord(c->ev_in[k], c->cs_in));
-    return OSB_OK;
+    int e = OSB_OK;
+    if (r >= 2) e = ck(cudaStreamWaitEvent(c->cs_in, c->ev_used[k], 0), "wait");
+    if (!e) e = ck(cudaMemcpyAsync(c->stage_in[k], in[r], bytes, cudaMemcpyHostToDevice, c->cs_in), "copy in");
+    if (!e) e = ck(cudaEventRecord(c->ev_in[k], c->cs_in), "record");
+    return e;
   };
-  rc = h2d(0);
-  if (rc) return rc;
+  if ((rc = h2d(0))) return rc;
   for (int r = 0; r < count; ++r) {
     const int k = r & 1;
     if (r + 1 < count && (rc = h2d(r + 1))) return rc;
-    OSB_CK(cudaStreamWaitEvent(c->stream, c->ev_in[k], 0));
-    if ((rc = stage_copy(c, (char*)c->stage_in[k], true))) return rc;
-    OSB_CK(cudaEventRecord(c->ev_used[k], c->stream));
-    if ((rc = osb_step(c, dt, nsteps))) return rc;
-    if (r >= 2) OSB_CK(cudaStreamWaitEvent(c->stream, c->ev_out[k], 0));
-    if ((rc = stage_copy(c, (char*)c->stage_out[k], false))) return rc;
-    OSB_CK(cudaEventRecord(c->ev_res[k], c->stream));
-    OSB_CK(cudaStreamWaitEvent(c->cs_out, c->ev_res[k], 0));
-    OSB_CK(cudaMemcpyAsync(out[r], c->stage_out[k], bytes, cudaMemcpyDeviceToHost, c->cs_out));
-    OSB_CK(cudaEventRecord(c->ev_out[k], c->cs_out));
+    if ((rc = ck(cudaStreamWaitEvent(c->stream, c->ev_in[k], 0), "wait"))) return rc;
+    if ((rc = stage_copy(c, (char*)c->stage_in[k], true))) return drain(rc);
+    if ((rc = ck(cudaEventRecord(c->ev_used[k], c->stream), "record"))) return rc;
+    if ((rc = osb_step(c, dt, nsteps))) return drain(rc);
+    if (r >= 2 && (rc = ck(cudaStreamWaitEvent(c->stream, c->ev_out[k], 0), "wait"))) return rc;
+    if ((rc = stage_copy(c, (char*)c->stage_out[k], false))) return drain(rc);
+    if ((rc = ck(cudaEventRecord(c->ev_res[k], c->stream), "record"))) return rc;
+    if ((rc = ck(cudaStreamWaitEvent(c->cs_out, c->ev_res[k], 0), "wait"))) return rc;
+    if ((rc = ck(cudaMemcpyAsync(out[r], c->stage_out[k], bytes, cudaMemcpyDeviceToHost, c->cs_out), "copy out")))
+      return rc;
+    if ((rc = ck(cudaEventRecord(c->ev_out[k], c->cs_out), "record"))) return rc;
   }
   OSB_CK(cudaStreamSynchronize(c->cs_out));
   OSB_CK(cudaStreamSynchronize(c->stream));
