@@ -337,7 +337,7 @@ def case_tgv_kgp_tvd():
     return block, params
 
 
-def case_shock_reflection(formulation=None):
+def case_shock_reflection(formulation=None, flux="LLF"):
     """2D inviscid oblique-shock reflection (``apps/inviscid_shock_reflection/inviscid_shock.py``)
     with the app's boundaries -- Dirichlet free-stream inlet, zeroth-order extrapolation outlet,
     symmetry (inviscid wall) bottom, Dirichlet top carrying the post-shock state from x = 40 --
@@ -365,7 +365,11 @@ def case_shock_reflection(formulation=None):
     initial = GridBasedInitialisation()
     initial.add_equations([x0, x1, d_in, u0_in, u1_in, p_in, rho, rhou0, rhou1, rhoE])
     schemes = {}
-    LF = LFWeno(order=5, formulation="Z", averaging=SimpleAverage([0, 1]), flux_type="LLF")
+    if flux == "LLF":
+        LF = LFWeno(order=5, formulation="Z", averaging=SimpleAverage([0, 1]), flux_type="LLF")
+    else:
+        from opensbli import HLLCWeno
+        LF = HLLCWeno(order=5, formulation="Z", averaging=SimpleAverage([0, 1]), flux_type=flux)
     schemes[LF.name] = LF
     rk = RungeKuttaLS(3, formulation=formulation)
     schemes[rk.name] = rk
@@ -509,6 +513,7 @@ CASES = {
     "tgv_kgp_tvd": case_tgv_kgp_tvd,
     "shock_reflection": case_shock_reflection,
     "shock_reflection_ssp": lambda: case_shock_reflection("SSP"),
+    "shock_reflection_hllc": lambda: case_shock_reflection("SSP", "HLLC-LM"),
     "kh_weno5z": case_kh_weno5z,
     "curv_weno5z": case_curv_weno5z,
 }
