@@ -78,6 +78,11 @@ extern "C" {
 #define OSB_FILTER_TVD 2       /* non-linear characteristic TVD filter (Yee-Sandham-Djomehri
                                   limiter with Harten's switch, shock_capturing.py:619-766) */
 
+/* Riemann flux of the characteristic WENO / TENO reconstruction (shock_capturing.py). */
+#define OSB_FLUX_LLF 0         /* flux-split local Lax-Friedrichs (LFWeno / LFTeno) */
+#define OSB_FLUX_HLLC_LM 1     /* HLLC-LM from reconstructed states (HLLCWeno, lines 1031-1256):
+                                  restated in the oracle; the GPU path rejects it (OSB_ENOTSUP) */
+
 /* Residual precision (per context). */
 #define OSB_PREC_FP64 0          /* plain FP64 path, parity with the generated solver */
 #define OSB_PREC_FP32_RESIDUAL 1 /* FP32 residual arithmetic, FP64 state/RK/reductions */
@@ -132,6 +137,7 @@ typedef struct osb_block_desc {
    * at index -depth + l (side 0) or N-1 + l (side 1) along d, t over the whole allocated
    * extent of the other used directions (lower direction fastest).  NULL elsewhere. */
   const double* dirichlet[3][2];
+  int32_t flux_type;         /* OSB_FLUX_* of the shock-capturing schemes (0 = LLF) */
 } osb_block_desc;
 
 /* ---- library / context ------------------------------------------------------------- */
@@ -282,8 +288,8 @@ int osb_stage_noalloc(const osb_block_desc* desc, int rk_kind, double A, double 
 int osb_metrics(const osb_block_desc* desc, const double* const* x, double* const* met, int fill, void* stream);
 
 /* Binding check: writes sizeof(osb_block_desc) and the byte offsets of size, bc, iface, gama,
- * delta, q, rkold, metric, split_form, ducros_check, tvd_kappa and dirichlet into out[0..12]
- * (n >= 13).  Needs no GPU. */
+ * delta, q, rkold, metric, split_form, ducros_check, tvd_kappa, dirichlet and flux_type into
+ * out[0..13] (n >= 14).  Needs no GPU. */
 int osb_desc_layout(long long* out, int n);
 
 #ifdef __cplusplus

@@ -42,6 +42,9 @@ FILTER_NONE = 0
 FILTER_WENO3 = 1
 FILTER_TVD = 2
 
+FLUX_LLF = 0
+FLUX_HLLC_LM = 1
+
 METRIC_PERIODIC = 0
 METRIC_EDGE = 1
 
@@ -110,6 +113,7 @@ class BlockDesc(ctypes.Structure):
         ("ducros_select", ctypes.c_double),
         ("tvd_kappa", ctypes.c_double),
         ("dirichlet", (ctypes.c_void_p * 2) * 3),
+        ("flux_type", ctypes.c_int32),
     ]
 
 
@@ -118,7 +122,7 @@ def layout_signature():
     offs = [BlockDesc.size.offset, BlockDesc.bc.offset, BlockDesc.iface.offset, BlockDesc.gama.offset,
             BlockDesc.delta.offset, BlockDesc.q.offset, BlockDesc.rkold.offset, BlockDesc.metric.offset,
             BlockDesc.split_form.offset, BlockDesc.ducros_check.offset, BlockDesc.tvd_kappa.offset,
-            BlockDesc.dirichlet.offset]
+            BlockDesc.dirichlet.offset, BlockDesc.flux_type.offset]
     return [ctypes.sizeof(BlockDesc)] + offs
 
 
@@ -154,6 +158,7 @@ def make_desc(spec, q_ptrs, rk_ptrs, metric_ptrs=None, dirichlet_ptrs=None):
     d.ducros_check = spec.ducros_check
     d.ducros_select = spec.ducros_select
     d.tvd_kappa = spec.tvd_kappa
+    d.flux_type = spec.flux_type
     for v, p in enumerate(q_ptrs):
         d.q[v] = p
     for v, p in enumerate(rk_ptrs):

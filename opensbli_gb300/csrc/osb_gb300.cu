@@ -933,6 +933,11 @@ bool check_desc(const osb_block_desc* d, std::string& why) {
       }
       if (f.side != 0 && f.side != 1) { why = "interface side must be 0 or 1"; return false; }
     }
+  if (d->flux_type == OSB_FLUX_HLLC_LM) {
+    why = "the HLLC-LM flux is restated in the oracle only; the GPU sweeps implement the LLF flux";
+    return false;
+  }
+  if (d->flux_type != OSB_FLUX_LLF) { why = "unknown flux type"; return false; }
   if (d->split_form != OSB_SPLIT_FEIEREISEN && d->split_form != OSB_SPLIT_KGP) { why = "unknown split form"; return false; }
   if (d->split_form == OSB_SPLIT_KGP && d->scheme != OSB_SCHEME_CENTRAL4) {
     why = "the KGP split form belongs to the central scheme";
@@ -987,7 +992,7 @@ int osb_last_error(char* buf, size_t n) {
 }
 
 int osb_desc_layout(long long* out, int n) {
-  if (!out || n < 13) return fail(OSB_EINVAL, "need 13 slots");
+  if (!out || n < 14) return fail(OSB_EINVAL, "need 14 slots");
   out[0] = sizeof(osb_block_desc);
   out[1] = offsetof(osb_block_desc, size);
   out[2] = offsetof(osb_block_desc, bc);
@@ -1001,6 +1006,7 @@ int osb_desc_layout(long long* out, int n) {
   out[10] = offsetof(osb_block_desc, ducros_check);
   out[11] = offsetof(osb_block_desc, tvd_kappa);
   out[12] = offsetof(osb_block_desc, dirichlet);
+  out[13] = offsetof(osb_block_desc, flux_type);
   return OSB_OK;
 }
 

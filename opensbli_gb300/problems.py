@@ -278,7 +278,7 @@ def curvilinear_wave_2d(n=128, scheme=abi.SCHEME_WENO5_Z, averaging=abi.AVG_ROE)
     return spec, q, metrics_central4(spec, [x0, x1], periodic_from_interior=True)
 
 
-def shock_reflection(n0=457, n1=255, sizes=None):
+def shock_reflection(n0=457, n1=255, sizes=None, flux_type=abi.FLUX_LLF):
     """2D inviscid oblique-shock reflection of apps/inviscid_shock_reflection/inviscid_shock.py
     on a 350 x 115 box (Delta = 350/(n0-1), 115/(n1-1)), M = 2, gama = 1.4, WENO5-Z (simple
     average, LLF): uniform free stream (rho = 1, u = (1, 0), p = 1/(gama M^2)); Dirichlet inlet
@@ -286,13 +286,15 @@ def shock_reflection(n0=457, n1=255, sizes=None):
     extrapolation on the right, symmetry (inviscid wall) at the bottom, Dirichlet at the top over
     the plane and 4 halo layers with the post-shock state (rho 1.129734572, u 0.9667023804242755,
     -0.052106102140246795, p 0.211869) from x = 40 and the free stream (p 0.178571) before it --
-    values, literals and operation order of the generated boundary and initialisation kernels."""
+    values, literals and operation order of the generated boundary and initialisation kernels.
+    flux_type = abi.FLUX_HLLC_LM selects the app's own HLLC-LM flux (oracle only)."""
     if sizes is not None:
         n0, n1 = sizes
     gama, minf = 1.4, 2.0
     spec = BlockSpec(ndim=2, size=(n0, n1), scheme=abi.SCHEME_WENO5_Z, averaging=abi.AVG_SIMPLE,
                      bc=[[abi.BC_DIRICHLET, abi.BC_EXTRAP0], [abi.BC_SYMMETRY, abi.BC_DIRICHLET]],
-                     bc_depth=[[3, 4], [4, 4]], delta=(350.0 / (n0 - 1), 115.0 / (n1 - 1)), gama=gama, Minf=minf)
+                     bc_depth=[[3, 4], [4, 4]], delta=(350.0 / (n0 - 1), 115.0 / (n1 - 1)), gama=gama, Minf=minf,
+                     flux_type=flux_type)
     inv_gm1 = 1.0 / (-1 + gama)
     p_inf = 1.0 * (1.0 / gama) * (minf ** -2.0)
 

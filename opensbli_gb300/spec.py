@@ -43,6 +43,7 @@ class BlockSpec:
     # Dirichlet faces: {(direction, side): array [v][layer][t]} of the values on the boundary
     # plane and its bc_depth halo layers (osb_block_desc.dirichlet)
     dirichlet: dict = None
+    flux_type: int = abi.FLUX_LLF
 
     def __post_init__(self):
         self.size = tuple(int(s) for s in self.size)
@@ -84,8 +85,9 @@ class BlockSpec:
         return idx.reshape(shp)
 
     def same_discretisation(self, other):
-        return (self.ndim, self.scheme, self.averaging, self.viscous, self.split_form, self.filter) == (
-            other.ndim, other.scheme, other.averaging, other.viscous, other.split_form, other.filter)
+        return (self.ndim, self.scheme, self.averaging, self.viscous, self.split_form, self.filter,
+                self.flux_type) == (other.ndim, other.scheme, other.averaging, other.viscous, other.split_form,
+                                    other.filter, other.flux_type)
 
 
 def empty_state(spec):

@@ -20,6 +20,7 @@
  *      f+/- = (CF +/- lambda*CS)/2                                (shock_capturing.py:979-998)
  *      WENO5-JS / WENO5-Z / TENO5 reconstruction                  (weno.py:36-472, teno.py:59-477)
  *      Fhat = REV * (recon(f+) + recon(f-))                       (shock_capturing.py:859-891)
+ *  - HLLC-LM flux from reconstructed states (HLLCWeno)           (shock_capturing.py:1031-1256)
  *  - residual R = -sum_d (Fhat(i+1/2) - Fhat(i-1/2)) / Delta_d    (shock_capturing.py:23-36)
  *  - StoreSome(4) viscous / heat-flux terms, central-4            (optimisations/StoreSome.py, scheme.py:174-258)
  *  - skew-symmetric (Feiereisen) central convective terms         (physical_models/split_forms.py:111-145)
@@ -411,6 +412,119 @@ static void char_flux_cart(const osb_block_desc* b, const geom_t* g, const cr_t*
   }
 }
 
+/* HLLC-LM flux at interface i+1/2 of a Cartesian block (HLLCCharacteristic with flux_type
+ * 'HLLC-LM', shock_capturing.py:1031-1256, as the generated "HLLCWeno_reconstruction" kernel):
+ * the averaged eigensystem; CS = L Q on points i-2..i+3; per wave the scheme's reconstruction of
+ * CS from the left (i-2..i+2) and from the right (i-1..i+3, mirrored); the physical states
+ * qL = R recL, qR = R recR; then u, p, a of each, the wave speeds sL = min(u_av - a_av, uL - aL),
+ * sR = max(u_av + a_av, uR + aR), the contact speed s*, both outer speeds scaled by
+ * phi = sin(pi/2 min(1, 10 M)) with M = max(|uL/aL|, |uR/aR|), and the HLLC flux in the
+ * generated central-plus-dissipation form.  The generated right-state energy term divides pR by
+ * (sL - uR) rho_R, not (sR - uR) rho_R; this follows it. */
+static void hllc_flux_cart(const osb_block_desc* b, const geom_t* g, const cr_t* c, int d, long idc,
+                           double* fhat) {
+  const int nd = b->ndim, nv = nd + 2;
+  const long s = g->st[d];
+  const double gm = b->gama, g1 = -1 + gm;
+  double kt[3] = {0.0, 0.0, 0.0};
+  kt[d] = 1.0;
+  const long iL = idc, iR = idc + s;
+  double rho_av, u_av[3] = {0, 0, 0}, a_av;
+  if (b->averaging == OSB_AVG_ROE) {
+    const double rL = b->q[0][iL], rR = b->q[0][iR];
+    const double sLr = sqrt(rL), sRr = sqrt(rR);
+    rho_av = sqrt(rL * rR);
+    const double inv = 1.0 / (sLr + sRr);
+    double ke = 0.0;
+    for (int i = 0; i < nd; ++i) {
+      u_av[i] = (sLr * c->u[i][iL] + sRr * c->u[i][iR]) * inv;
+      ke += u_av[i] * u_av[i];
+    }
+    const double HL = (b->q[nv - 1][iL] + c->p[iL]) / rL, HR = (b->q[nv - 1][iR] + c->p[iR]) / rR;
+    a_av = sqrt((gm - 1.0) * ((sLr * HL + sRr * HR) * inv - 0.5 * ke));
+  } else {
+    rho_av = (1.0 / 2.0) * (b->q[0][iL] + b->q[0][iR]);
+    for (int i = 0; i < nd; ++i) u_av[i] = (1.0 / 2.0) * (c->u[i][iL] + c->u[i][iR]);
+    a_av = (1.0 / 2.0) * (c->a[iL] + c->a[iR]);
+  }
+  double L[NVMAX][NVMAX], R[NVMAX][NVMAX];
+  eigensystem(nd, gm, kt, rho_av, u_av, a_av, L, R);
+  double cs[NVMAX][6];
+  for (int m = 0; m < 6; ++m) {
+    const long id = idc + (long)(m - 2) * s;
+    for (int w = 0; w < nv; ++w) {
+      double acc = 0.0;
+      for (int v = 0; v < nv; ++v) acc += L[w][v] * b->q[v][id];
+      cs[w][m] = acc;
+    }
+  }
+  double recL[NVMAX], recR[NVMAX];
+  for (int w = 0; w < nv; ++w) {
+    const double mir[5] = {cs[w][5], cs[w][4], cs[w][3], cs[w][2], cs[w][1]};
+    recL[w] = recon5(b->scheme, cs[w], b->eps, b->teno_ct);
+    recR[w] = recon5(b->scheme, mir, b->eps, b->teno_ct);
+  }
+  double qL[NVMAX], qR[NVMAX];
+  for (int v = 0; v < nv; ++v) {
+    double aL_ = 0.0, aR_ = 0.0;
+    for (int w = 0; w < nv; ++w) {
+      aL_ += R[v][w] * recL[w];
+      aR_ += R[v][w] * recR[w];
+    }
+    qL[v] = aL_;
+    qR[v] = aR_;
+  }
+  const double irL = 1.0 / qL[0], irR = 1.0 / qR[0];
+  double uL[3] = {0, 0, 0}, uR[3] = {0, 0, 0}, kL = 0.0, kR = 0.0;
+  for (int i = 0; i < nd; ++i) {
+    uL[i] = irL * qL[1 + i];
+    uR[i] = irR * qR[1 + i];
+    kL += uL[i] * uL[i];
+    kR += uR[i] * uR[i];
+  }
+  const double EL = qL[nv - 1], ER = qR[nv - 1];
+  const double pL = (-0.5 * kL * qL[0] + EL) * g1, pR = (-0.5 * kR * qR[0] + ER) * g1;
+  const double aL = sqrt(gm * irL * pL), aR = sqrt(gm * irR * pR);
+  const double un = u_av[d], uLn = uL[d], uRn = uR[d];
+  double sL = fmin(-a_av + un, -aL + uLn), sR = fmax(a_av + un, aR + uRn);
+  const double ss = (-pL + (-uLn + sL) * qL[0] * uLn - (-uRn + sR) * qR[0] * uRn + pR) /
+                    ((-uLn + sL) * qL[0] - (-uRn + sR) * qR[0]);
+  const double M = fmax(fabs(uLn / aL), fabs(uRn / aR));
+  const double phi = sin((1.0 / 2.0) * M_PI * fmin(1.0, 10.0 * M));
+  sL = phi * sL;
+  sR = phi * sR;
+  const double mL = (-uLn + sL) * qL[0] / (-ss + sL), mR = (-uRn + sR) * qR[0] / (-ss + sR);
+  const double as = fabs(ss);
+  if (sL >= 0) {
+    fhat[0] = qL[1 + d];
+    for (int i = 0; i < nd; ++i) fhat[1 + i] = i == d ? qL[1 + d] * uLn + pL : qL[1 + i] * uLn;
+    fhat[nv - 1] = (pL + EL) * uLn;
+  } else if (sR <= 0) {
+    fhat[0] = qR[1 + d];
+    for (int i = 0; i < nd; ++i) fhat[1 + i] = i == d ? qR[1 + d] * uRn + pR : qR[1 + i] * uRn;
+    fhat[nv - 1] = (pR + ER) * uRn;
+  } else {
+    fhat[0] = (1.0 / 2.0) * qL[1 + d] + (1.0 / 2.0) * qR[1 + d] + (1.0 / 2.0) * (-qL[0] + mL) * sL +
+              (1.0 / 2.0) * (-qR[0] + mR) * sR + (1.0 / 2.0) * (mL - mR) * as;
+    for (int i = 0; i < nd; ++i) {
+      if (i == d) {
+        const double xL = (-uLn + sL) * qL[0] * ss / (-ss + sL), xR = (-uRn + sR) * qR[0] * ss / (-ss + sR);
+        fhat[1 + i] = (1.0 / 2.0) * pL + (1.0 / 2.0) * pR + (1.0 / 2.0) * (-qL[1 + d] + xL) * sL +
+                      (1.0 / 2.0) * (-qR[1 + d] + xR) * sR + (1.0 / 2.0) * (xL - xR) * as +
+                      (1.0 / 2.0) * qL[1 + d] * uLn + (1.0 / 2.0) * qR[1 + d] * uRn;
+      } else {
+        const double xL = (-uLn + sL) * qL[0] * uL[i] / (-ss + sL), xR = (-uRn + sR) * qR[0] * uR[i] / (-ss + sR);
+        fhat[1 + i] = (1.0 / 2.0) * (-qL[1 + i] + xL) * sL + (1.0 / 2.0) * (-qR[1 + i] + xR) * sR +
+                      (1.0 / 2.0) * (xL - xR) * as + (1.0 / 2.0) * qL[1 + i] * uLn + (1.0 / 2.0) * qR[1 + i] * uRn;
+      }
+    }
+    const double eL = (-uLn + sL) * ((-uLn + ss) * (pL / ((-uLn + sL) * qL[0]) + ss) + irL * EL) * qL[0] / (-ss + sL);
+    const double eR = (-uRn + sR) * ((-uRn + ss) * (pR / ((-uRn + sL) * qR[0]) + ss) + irR * ER) * qR[0] / (-ss + sR);
+    fhat[nv - 1] = (1.0 / 2.0) * (-EL + eL) * sL + (1.0 / 2.0) * (-ER + eR) * sR + (1.0 / 2.0) * (eL - eR) * as +
+                   (1.0 / 2.0) * (pL + EL) * uLn + (1.0 / 2.0) * (pR + ER) * uRn;
+  }
+}
+
 /* Curvilinear interface flux (k = D_d averaged, contravariant flux scaled by det J), as the
  * generated "LFWeno_reconstruction" kernel of the curvilinear verification case
  * (euler_eigensystem.py:19-51 apply_direction with metrics; metric.py). */
@@ -623,6 +737,7 @@ int oracle_residual(const osb_block_desc* b, double* const* Rout) {
             long id = gid(&g, i, j, k);
             double f[NVMAX];
             if (b->metric[9]) char_flux_curv(b, &g, &c, d, id, f);
+            else if (b->flux_type == OSB_FLUX_HLLC_LM) hllc_flux_cart(b, &g, &c, d, id, f);
             else char_flux_cart(b, &g, &c, d, id, f);
             for (int v = 0; v < nv; ++v) fh[d][v][id] = f[v];
           }
