@@ -77,16 +77,28 @@ def _const_value(name, params, default=None):
     return default
 
 
+def _flux_of(block):
+    """OSB_FLUX_* of the block's shock-capturing scheme: LLF for LFWeno / LFTeno, HLLC-LM for
+    HLLCWeno with flux_type 'HLLC-LM' (restated in the oracle; the GPU path refuses it)."""
+    from opensbli.schemes.spatial.weno import HLLCWeno
+    for sch in block.discretisation_schemes.values():
+        if isinstance(sch, HLLCWeno):
+            if getattr(sch, "flux_type", None) != "HLLC-LM":
+                raise NotImplementedError("HLLCWeno flux %s is not restated (HLLC-LM is)" % sch.flux_type)
+            return abi.FLUX_HLLC_LM
+    return abi.FLUX_LLF
+
+
 def _scheme_of(block):
     """(scheme, averaging, has_central) from block.discretisation_schemes."""
-    from opensbli.schemes.spatial.weno import LFWeno
+    from opensbli.schemes.spatial.weno import LFWeno, HLLCWeno
     from opensbli.schemes.spatial.teno import LFTeno
     from opensbli.schemes.spatial.scheme import Central
     from opensbli.schemes.spatial.averaging import RoeAverage
     scheme, avg, central = None, abi.AVG_SIMPLE, False
     for sch in block.discretisation_schemes.values():
-        if isinstance(sch, (LFWeno, LFTeno)):
-            if getattr(sch, "flux_type", "LLF") != "LLF":
+        if isinstance(sch, (LFWeno, LFTeno, HLLCWeno)):
+            if isinstance(sch, (LFWeno, LFTeno)) and getattr(sch, "flux_type", "LLF") != "LLF":
                 raise NotImplementedError("only local Lax-Friedrichs splitting is supported (got %s)" % sch.flux_type)
             if getattr(sch, "shock_filter", False):
                 raise NotImplementedError("WENO filter steps are not supported")
@@ -300,7 +312,7 @@ def block_spec(block, params):
     split = _split_form_of(block) if scheme == abi.SCHEME_CENTRAL4 else abi.SPLIT_FEIEREISEN
     filt, kappa = _filter_of(block, p)
     spec = BlockSpec(ndim=nd, size=size, scheme=scheme, averaging=avg, viscous=visc, bc=bc, bc_depth=depth,
-                     split_form=split, filter=filt, tvd_kappa=kappa,
+                     split_form=split, filter=filt, tvd_kappa=kappa, flux_type=_flux_of(block),
                      gama=_const_value("gama", p), Minf=_const_value("Minf", p, 1.0), Re=_const_value("Re", p, 1.0),
                      Pr=_const_value("Pr", p, 0.71), mu_const=1.0, eps=_const_value("eps", p, 1e-40),
                      teno_ct=_const_value("TENO_CT", p, 1e-6),

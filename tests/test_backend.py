@@ -181,3 +181,29 @@ def test_shock_reflection_boundaries_mapped():
     q0 = initial_state(be.blocks[0], spec, nums)
     for v in range(4):
         assert np.allclose(q0[v], q[v], rtol=1e-14, atol=0), v
+
+
+@needs_ref
+def test_hllc_block_maps_and_runs_in_the_oracle():
+    """The shock-reflection app with its HLLCWeno (HLLC-LM) flux and SSP RK3 maps onto a
+    descriptor with OSB_FLUX_HLLC_LM and the SSP coefficients; the oracle run from the backend's
+    own spec and initial state reproduces the reference's generated solver (golden, 30 stages)
+    from the same perturbed state."""
+    import harness
+    nums = {"gama": "1.4", "Minf": "2.0", "dt": "0.5", "niter": "1", "block0np0": "64", "block0np1": "32",
+            "Delta0block0": "350.0/(block0np0-1)", "Delta1block0": "115.0/(block0np1-1)"}
+    be = _backend_for("shock_reflection_hllc", nums)
+    spec = be.specs[0]
+    assert spec.flux_type == abi.FLUX_HLLC_LM and spec.scheme == abi.SCHEME_WENO5_Z
+    assert be.rk[0] == abi.RK_LOW_STORAGE and np.allclose(be.rk[1], problems.RK3_SSP_A)
+    assert np.allclose(be.rk[2], problems.RK3_SSP_B)
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "shock_reflection_hllc_64x32_perturbed.npz"))
+    ref_spec, q = problems.shock_reflection(64, 32, flux_type=abi.FLUX_HLLC_LM)
+    rng = np.random.default_rng(4)
+    q = [a * (1.0 + 1e-2 * rng.standard_normal(a.shape)) for a in q]
+    ob = harness.OracleBlocks([(spec, q)])
+    ob.apply_bc()
+    ob.step(be.rk[0], be.rk[1], be.rk[2], float(g["dt"]), 10)
+    sl = spec.interior()
+    errs = [harness.rel_err(ob.q[0][v][sl], g["after_30"][v]) for v in range(4)]
+    assert max(errs) < 1e-12, errs
