@@ -67,6 +67,8 @@ extern "C" {
                                 inside, normal momentum negated; the boundary plane unchanged */
 #define OSB_BC_DIRICHLET 6   /* DirichletBC (dirichlet.py:27-41): the boundary plane and its halo
                                 layers set from osb_block_desc.dirichlet */
+#define OSB_BC_PRESSURE_OUTLET 7 /* PressureOutletBC (pressure_outlet.py:35-51): restated in the
+                                oracle; the GPU path refuses it (OSB_EINVAL) */
 
 /* Convective split form of OSB_SCHEME_CENTRAL4 (physical_models/split_forms.py). */
 #define OSB_SPLIT_FEIEREISEN 0 /* skew-symmetric form, split_forms.py:111-145 */
@@ -138,6 +140,7 @@ typedef struct osb_block_desc {
    * extent of the other used directions (lower direction fastest).  NULL elsewhere. */
   const double* dirichlet[3][2];
   int32_t flux_type;         /* OSB_FLUX_* of the shock-capturing schemes (0 = LLF) */
+  double back_pressure[3][2]; /* OSB_BC_PRESSURE_OUTLET face (d, side): its back pressure */
 } osb_block_desc;
 
 /* ---- library / context ------------------------------------------------------------- */
@@ -288,8 +291,8 @@ int osb_stage_noalloc(const osb_block_desc* desc, int rk_kind, double A, double 
 int osb_metrics(const osb_block_desc* desc, const double* const* x, double* const* met, int fill, void* stream);
 
 /* Binding check: writes sizeof(osb_block_desc) and the byte offsets of size, bc, iface, gama,
- * delta, q, rkold, metric, split_form, ducros_check, tvd_kappa, dirichlet and flux_type into
- * out[0..13] (n >= 14).  Needs no GPU. */
+ * delta, q, rkold, metric, split_form, ducros_check, tvd_kappa, dirichlet, flux_type and
+ * back_pressure into out[0..14] (n >= 15).  Needs no GPU. */
 int osb_desc_layout(long long* out, int n);
 
 #ifdef __cplusplus

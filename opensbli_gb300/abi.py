@@ -36,6 +36,7 @@ BC_EXTRAP0 = 3
 BC_EXTRAP1 = 4
 BC_SYMMETRY = 5
 BC_DIRICHLET = 6
+BC_PRESSURE_OUTLET = 7
 SPLIT_FEIEREISEN = 0
 SPLIT_KGP = 1
 FILTER_NONE = 0
@@ -114,6 +115,7 @@ class BlockDesc(ctypes.Structure):
         ("tvd_kappa", ctypes.c_double),
         ("dirichlet", (ctypes.c_void_p * 2) * 3),
         ("flux_type", ctypes.c_int32),
+        ("back_pressure", (ctypes.c_double * 2) * 3),
     ]
 
 
@@ -122,7 +124,7 @@ def layout_signature():
     offs = [BlockDesc.size.offset, BlockDesc.bc.offset, BlockDesc.iface.offset, BlockDesc.gama.offset,
             BlockDesc.delta.offset, BlockDesc.q.offset, BlockDesc.rkold.offset, BlockDesc.metric.offset,
             BlockDesc.split_form.offset, BlockDesc.ducros_check.offset, BlockDesc.tvd_kappa.offset,
-            BlockDesc.dirichlet.offset, BlockDesc.flux_type.offset]
+            BlockDesc.dirichlet.offset, BlockDesc.flux_type.offset, BlockDesc.back_pressure.offset]
     return [ctypes.sizeof(BlockDesc)] + offs
 
 
@@ -159,6 +161,8 @@ def make_desc(spec, q_ptrs, rk_ptrs, metric_ptrs=None, dirichlet_ptrs=None):
     d.ducros_select = spec.ducros_select
     d.tvd_kappa = spec.tvd_kappa
     d.flux_type = spec.flux_type
+    for (i, side), bp in (spec.back_pressure or {}).items():
+        d.back_pressure[i][side] = bp
     for v, p in enumerate(q_ptrs):
         d.q[v] = p
     for v, p in enumerate(rk_ptrs):

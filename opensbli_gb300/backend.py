@@ -195,6 +195,10 @@ def _bcs_of(block, central_only):
                 bc[d][side] = abi.BC_SYMMETRY
                 hv = b.get_halo_values(block)
                 depth[d][side] = abs(hv[d][side])
+            elif type(b).__name__ == "PressureOutletBC":
+                bc[d][side] = abi.BC_PRESSURE_OUTLET
+                hv = b.get_halo_values(block)
+                depth[d][side] = abs(hv[d][side])
             elif type(b).__name__ == "DirichletBC":
                 # the generated kernel covers the plane and the scheme's halo on that side
                 # (dirichlet.py:35-40: block.boundary_halos)
@@ -319,6 +323,10 @@ def block_spec(block, params):
                      shock_filter_control=_const_value("shock_filter_control", p, 1.0), delta=delta)
     if any(k == abi.BC_DIRICHLET for pair in bc for k in pair):
         spec.dirichlet = dirichlet_faces(block, spec, params)
+    outlets = {(d, side): float(b.back_pressure) for d, pair in enumerate(block.boundary_types)
+               for side, b in enumerate(pair) if bc[d][side] == abi.BC_PRESSURE_OUTLET}
+    if outlets:
+        spec.back_pressure = outlets
     return spec
 
 

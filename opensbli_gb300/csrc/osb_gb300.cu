@@ -903,6 +903,10 @@ bool check_desc(const osb_block_desc* d, std::string& why) {
   for (int i = 0; i < d->ndim; ++i)
     for (int s = 0; s < 2; ++s) {
       const int k = d->bc[i][s];
+      if (k == OSB_BC_PRESSURE_OUTLET) {
+        why = "the pressure outlet is restated in the oracle only; the GPU path has no kernel for it";
+        return false;
+      }
       if (k < OSB_BC_PERIODIC || k > OSB_BC_DIRICHLET) { why = "unknown boundary kind"; return false; }
       const int dep = d->bc_depth[i][s] > 0 ? d->bc_depth[i][s] : 4;
       if ((k == OSB_BC_SYMMETRY || k == OSB_BC_DIRICHLET) && (dep > d->halo || dep >= d->size[i])) {
@@ -992,7 +996,7 @@ int osb_last_error(char* buf, size_t n) {
 }
 
 int osb_desc_layout(long long* out, int n) {
-  if (!out || n < 14) return fail(OSB_EINVAL, "need 14 slots");
+  if (!out || n < 15) return fail(OSB_EINVAL, "need 15 slots");
   out[0] = sizeof(osb_block_desc);
   out[1] = offsetof(osb_block_desc, size);
   out[2] = offsetof(osb_block_desc, bc);
@@ -1007,6 +1011,7 @@ int osb_desc_layout(long long* out, int n) {
   out[11] = offsetof(osb_block_desc, tvd_kappa);
   out[12] = offsetof(osb_block_desc, dirichlet);
   out[13] = offsetof(osb_block_desc, flux_type);
+  out[14] = offsetof(osb_block_desc, back_pressure);
   return OSB_OK;
 }
 

@@ -278,7 +278,7 @@ def curvilinear_wave_2d(n=128, scheme=abi.SCHEME_WENO5_Z, averaging=abi.AVG_ROE)
     return spec, q, metrics_central4(spec, [x0, x1], periodic_from_interior=True)
 
 
-def shock_reflection(n0=457, n1=255, sizes=None, flux_type=abi.FLUX_LLF):
+def shock_reflection(n0=457, n1=255, sizes=None, flux_type=abi.FLUX_LLF, back_pressure=None):
     """2D inviscid oblique-shock reflection of apps/inviscid_shock_reflection/inviscid_shock.py
     on a 350 x 115 box (Delta = 350/(n0-1), 115/(n1-1)), M = 2, gama = 1.4, WENO5-Z (simple
     average, LLF): uniform free stream (rho = 1, u = (1, 0), p = 1/(gama M^2)); Dirichlet inlet
@@ -287,7 +287,8 @@ def shock_reflection(n0=457, n1=255, sizes=None, flux_type=abi.FLUX_LLF):
     the plane and 4 halo layers with the post-shock state (rho 1.129734572, u 0.9667023804242755,
     -0.052106102140246795, p 0.211869) from x = 40 and the free stream (p 0.178571) before it --
     values, literals and operation order of the generated boundary and initialisation kernels.
-    flux_type = abi.FLUX_HLLC_LM selects the app's own HLLC-LM flux (oracle only)."""
+    flux_type = abi.FLUX_HLLC_LM selects the app's own HLLC-LM flux, back_pressure a
+    PressureOutletBC in place of the extrapolation outlet (both oracle only)."""
     if sizes is not None:
         n0, n1 = sizes
     gama, minf = 1.4, 2.0
@@ -322,6 +323,9 @@ def shock_reflection(n0=457, n1=255, sizes=None, flux_type=abi.FLUX_LLF):
     for v in range(4):
         top[v] = top_row[v][None, :]
     spec.dirichlet = {(0, 0): left, (1, 1): top}
+    if back_pressure is not None:
+        spec.bc[0][1] = abi.BC_PRESSURE_OUTLET
+        spec.back_pressure = {(0, 1): float(back_pressure)}
     return spec, q
 
 

@@ -44,6 +44,8 @@ class BlockSpec:
     # plane and its bc_depth halo layers (osb_block_desc.dirichlet)
     dirichlet: dict = None
     flux_type: int = abi.FLUX_LLF
+    # pressure-outlet faces: {(direction, side): back pressure}
+    back_pressure: dict = None
 
     def __post_init__(self):
         self.size = tuple(int(s) for s in self.size)

@@ -32,7 +32,8 @@
  *  - low-storage RK3 (rk_LS.py:185-215) and SBLI RK3 (rk_sbli.py:138-154)
  *  - periodic exchange (periodic.py:53-71, opsc.py:1026-1064), zero-gradient
  *    (zero_gradient_outlet.py:11-23), extrapolation (extrapolation.py:29-53), symmetry
- *    (symmetry.py:23-50), Dirichlet (dirichlet.py:27-41), block interfaces (multi_block.py:48-107)
+ *    (symmetry.py:23-50), Dirichlet (dirichlet.py:27-41), pressure outlet (pressure_outlet.py:35-51),
+ *    block interfaces (multi_block.py:48-107)
  *  - TGV reductions (compressible_TGV.py:176-206)
  */
 #include <math.h>
@@ -1442,6 +1443,26 @@ static void dirichlet_point(osb_block_desc* b, const geom_t* g, int d, int side,
   }
 }
 
+/* Pressure outlet (pressure_outlet.py:35-51 as generated): the boundary plane and its depth halo
+ * layers take rho and the momentum of the point one inside the plane, and
+ * rhoE = back_pressure / (-1.0 + gama) + (1/2 |rhou|^2) / rho of that point. */
+static void pressure_outlet_point(osb_block_desc* b, const geom_t* g, int d, int side, int depth, const int* c,
+                                  long t) {
+  (void)t;
+  const int nd = b->ndim, nv = nd + 2;
+  const long id = gid(g, c[0], c[1], c[2]);
+  const long o = g->st[d] * (side == 0 ? -1 : 1);
+  const long in = id - o;
+  for (int m = 0; m <= depth; ++m) {
+    const long p = id + m * o;
+    b->q[0][p] = b->q[0][in];
+    for (int i = 0; i < nd; ++i) b->q[1 + i][p] = b->q[1 + i][in];
+    double ke = 0.5 * (b->q[1][in] * b->q[1][in]);
+    for (int i = 1; i < nd; ++i) ke = ke + 0.5 * (b->q[1 + i][in] * b->q[1 + i][in]);
+    b->q[nv - 1][p] = b->back_pressure[d][side] / (-1.0 + b->gama) + ke / b->q[0][in];
+  }
+}
+
 /* Block interface (multi_block.py:11-107, identity orientation, matching faces normal to the
  * same direction): the halo layers of face (d, side) receive the neighbour's layers adjacent to
  * its face (d, f->side).  `full` = 0 copies the interior of the face only; `full` = 1 also the
@@ -1490,6 +1511,8 @@ int oracle_apply_bc(osb_block_desc* blocks, int nblocks, int zero_grad_only) {
             extrap_face(b, &g, d, side, depth, kind == OSB_BC_EXTRAP1);
           if (pass == 1 && kind == OSB_BC_SYMMETRY)
             for_face(b, &g, d, side, depth, side == 0 ? 0 : g.n[d] - 1, symmetry_point);
+          if (pass == 1 && kind == OSB_BC_PRESSURE_OUTLET)
+            for_face(b, &g, d, side, depth, side == 0 ? 0 : g.n[d] - 1, pressure_outlet_point);
           if (pass == 1 && kind == OSB_BC_DIRICHLET) {
             if (!b->dirichlet[d][side]) return -1;
             for_face(b, &g, d, side, depth, 0, dirichlet_point);

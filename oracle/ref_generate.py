@@ -337,7 +337,7 @@ def case_tgv_kgp_tvd():
     return block, params
 
 
-def case_shock_reflection(formulation=None, flux="LLF"):
+def case_shock_reflection(formulation=None, flux="LLF", outlet=None):
     """2D inviscid oblique-shock reflection (``apps/inviscid_shock_reflection/inviscid_shock.py``)
     with the app's boundaries -- Dirichlet free-stream inlet, zeroth-order extrapolation outlet,
     symmetry (inviscid wall) bottom, Dirichlet top carrying the post-shock state from x = 40 --
@@ -382,8 +382,13 @@ def case_shock_reflection(formulation=None, flux="LLF"):
              pe("Eq(GridVariable(u1), Piecewise((0.0 ,x<shock_loc),(-0.052106102140246795, x>=shock_loc),(1.0,True)))"),
              pe("Eq(GridVariable(p), Piecewise( (%f,x<shock_loc),(%f, x>=shock_loc),(1.0,True)))" % (pre, post)),
              rho, rhou0, rhou1, rhoE]
+    if outlet is None:
+        right = ExtrapolationBC(0, 1, order=0)
+    else:
+        from opensbli import PressureOutletBC
+        right = PressureOutletBC(0, 1, back_pressure=outlet)
     bcs = [DirichletBC(0, 0, [d_in, u0_in, u1_in, p_in, rho, rhou0, rhou1, rhoE]),
-           ExtrapolationBC(0, 1, order=0), SymmetryBC(1, 0), DirichletBC(1, 1, upper)]
+           right, SymmetryBC(1, 0), DirichletBC(1, 1, upper)]
     block.set_block_boundaries(bcs)
     block.set_equations([copy.deepcopy(cr), copy.deepcopy(sim), initial])
     block.discretise()
@@ -514,6 +519,8 @@ CASES = {
     "shock_reflection": case_shock_reflection,
     "shock_reflection_ssp": lambda: case_shock_reflection("SSP"),
     "shock_reflection_hllc": lambda: case_shock_reflection("SSP", "HLLC-LM"),
+    # the outlet as PressureOutletBC (pressure_outlet.py) with a back pressure of 0.2
+    "shock_reflection_pout": lambda: case_shock_reflection(outlet=0.2),
     "kh_weno5z": case_kh_weno5z,
     "curv_weno5z": case_curv_weno5z,
 }

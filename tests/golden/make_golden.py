@@ -53,6 +53,10 @@ CASES = {
     "shock_reflection_hllc_64x32_perturbed": ("shock_reflection_hllc",
                                               lambda: problems.shock_reflection(64, 32, flux_type=abi.FLUX_HLLC_LM),
                                               {"OSB_NP0": 64, "OSB_NP1": 32}, 0.5, [1, 3, 30], (1e-2, 4)),
+    # PressureOutletBC (back pressure 0.2) in place of the extrapolation outlet
+    "shock_reflection_pout_64x32_perturbed": ("shock_reflection_pout",
+                                              lambda: problems.shock_reflection(64, 32, back_pressure=0.2),
+                                              {"OSB_NP0": 64, "OSB_NP1": 32}, 0.5, [1, 3, 30], (1e-2, 4)),
     # the curvilinear solver computes its metrics from its own grid; they match
     # problems.metrics_central4 bit for bit
     "curv_weno5z_32": ("curv_weno5z", lambda: problems.curvilinear_wave_2d(32),

@@ -26,8 +26,8 @@ def test_library_exports_every_symbol(built_lib):
 
 def test_descriptor_layout(built_lib):
     lib = abi.load_library()
-    out = (ctypes.c_longlong * 14)()
-    assert lib.osb_desc_layout(out, 14) == 0
+    out = (ctypes.c_longlong * 15)()
+    assert lib.osb_desc_layout(out, 15) == 0
     assert list(out) == abi.layout_signature()
 
 
@@ -35,7 +35,7 @@ def test_version_and_errors(built_lib):
     lib = abi.load_library()
     assert lib.osb_version() == 100
     assert lib.osb_desc_layout(None, 0) == abi.OSB_EINVAL
-    assert "14 slots" in abi.last_error(lib)
+    assert "15 slots" in abi.last_error(lib)
 
 
 def test_new_entry_points_reject_bad_arguments_without_a_gpu(built_lib):
@@ -67,3 +67,15 @@ def test_hllc_descriptor_refused_by_the_gpu_path(built_lib):
     d = abi.make_desc(spec, [1] * 4, [1] * 4, None, {(0, 0): 1, (1, 1): 1})
     assert lib.osb_stage_noalloc(ctypes.byref(d), abi.RK_LOW_STORAGE, 0.0, 0.5, 0.1, None) == abi.OSB_EINVAL
     assert "HLLC" in abi.last_error(lib)
+
+
+def test_pressure_outlet_refused_by_the_gpu_path(built_lib):
+    """The pressure outlet is restated in the oracle (pinned to the reference's generated
+    solver); the GPU path refuses the face instead of leaving its halos unset."""
+    from opensbli_gb300 import problems
+    lib = abi.load_library()
+    spec, _ = problems.shock_reflection(40, 20, back_pressure=0.2)
+    d = abi.make_desc(spec, [1] * 4, [1] * 4, None, {(0, 0): 1, (1, 1): 1})
+    assert d.back_pressure[0][1] == 0.2
+    assert lib.osb_stage_noalloc(ctypes.byref(d), abi.RK_LOW_STORAGE, 0.0, 0.5, 0.1, None) == abi.OSB_EINVAL
+    assert "pressure outlet" in abi.last_error(lib)

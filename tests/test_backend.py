@@ -207,3 +207,25 @@ def test_hllc_block_maps_and_runs_in_the_oracle():
     sl = spec.interior()
     errs = [harness.rel_err(ob.q[0][v][sl], g["after_30"][v]) for v in range(4)]
     assert max(errs) < 1e-12, errs
+
+
+@needs_ref
+def test_pressure_outlet_maps_and_runs_in_the_oracle():
+    """PressureOutletBC maps onto OSB_BC_PRESSURE_OUTLET with its back pressure and depth; the
+    oracle run from the backend's own spec reproduces the reference's generated solver."""
+    import harness
+    nums = {"gama": "1.4", "Minf": "2.0", "dt": "0.5", "niter": "1", "block0np0": "64", "block0np1": "32",
+            "Delta0block0": "350.0/(block0np0-1)", "Delta1block0": "115.0/(block0np1-1)"}
+    be = _backend_for("shock_reflection_pout", nums)
+    spec = be.specs[0]
+    ref, q = problems.shock_reflection(64, 32, back_pressure=0.2)
+    assert spec.bc == ref.bc and spec.bc_depth == ref.bc_depth and spec.back_pressure == {(0, 1): 0.2}
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "shock_reflection_pout_64x32_perturbed.npz"))
+    rng = np.random.default_rng(4)
+    q = [a * (1.0 + 1e-2 * rng.standard_normal(a.shape)) for a in q]
+    ob = harness.OracleBlocks([(spec, q)])
+    ob.apply_bc()
+    ob.step(be.rk[0], be.rk[1], be.rk[2], float(g["dt"]), 10)
+    sl = spec.interior()
+    errs = [harness.rel_err(ob.q[0][v][sl], g["after_30"][v]) for v in range(4)]
+    assert max(errs) < 1e-12, errs

@@ -29,7 +29,13 @@ CASES = {
     # HLLC-LM flux from WENO5-Z reconstructed states (restated in the oracle; not on the GPU yet)
     "shock_reflection_hllc_64x32_perturbed": (lambda: problems.shock_reflection(64, 32, flux_type=abi.FLUX_HLLC_LM),
                                               "ssp3", (1e-2, 4), 1e-12),
+    # pressure outlet (restated in the oracle; not on the GPU yet)
+    "shock_reflection_pout_64x32_perturbed": (lambda: problems.shock_reflection(64, 32, back_pressure=0.2), "ls3",
+                                              (1e-2, 4), 1e-12),
 }
+
+
+OUTLET_PLANE_OVERWRITTEN = {"shock_reflection_pout_64x32_perturbed"}
 
 
 def perturb(q, amp, seed):
@@ -87,8 +93,15 @@ def test_oracle_residual_matches_reference(oracle_lib, name):
         pytest.skip("the reference solver of this case keeps no residual arrays")
     R = ob.residual(0)
     sl = spec.interior()
+    keep = (slice(None),) * spec.ndim
+    if name in OUTLET_PLANE_OVERWRITTEN:
+        # the pressure outlet overwrites its boundary plane after every update, so that plane's
+        # residual is never used; its stencil holds the outlet's replicated state, whose
+        # characteristic jumps are rounding-level, where WENO-Z with epsilon 1e-40 turns
+        # rounding differences into 1e-6 relative ones (the states match to 1e-12 regardless)
+        keep = (slice(None),) * (spec.ndim - 1) + (slice(0, spec.size[0] - 1),)
     for v in range(spec.nvars):
-        assert harness.rel_err(R[v][sl], g["residual_1"][v]) < 10 * tol, v
+        assert harness.rel_err(R[v][sl][keep], g["residual_1"][v][keep]) < 10 * tol, v
 
 
 @pytest.mark.parametrize("name", sorted(CASES))
