@@ -270,10 +270,20 @@ int osb_get_stream(osb_ctx* ctx, void** stream);
  * is a file-scope __device__ array of OSB_NOALLOC_MAX_DOUBLES doubles that every GPU loading
  * the library holds until exit, and blocks whose nvars x allocated points exceed it are
  * rejected with OSB_EINVAL.  The caller passes the state and RK arrays in the descriptor (FP64
- * path only) and, for OSB_RK_SBLI3, copies q into rkold at the start of each step itself.  The
- * first call on a device looks up the workspace address (cudaGetSymbolAddress) and should come
- * before any stream capture on that device.  All calls share the workspace: calls that overlap
- * on the GPU race.  Asynchronous on `stream` (a cudaStream_t, NULL for the default stream).
+ * path only) and, for OSB_RK_SBLI3, copies q into rkold at the start of each step itself.
+ *  - Halos: the stage reads q's halos as they are and applies the block's boundary faces only
+ *    after its update, so before the first call the caller fills them (one osb_apply_bc on a
+ *    context, or its own exchange); later calls leave them filled.
+ *  - Faces: periodic, zero-gradient, extrapolation, symmetry and Dirichlet, with the kernels
+ *    osb_apply_bc uses; a block with an interface face (or one periodic side) is refused with
+ *    OSB_ENOTSUP before anything is launched, so the caller's arrays are untouched.
+ *  - Device: the call runs on the current device; `stream` and every array must belong to it
+ *    (checked: OSB_EINVAL otherwise).  The first call on a device looks up the workspace address
+ *    (cudaGetSymbolAddress) and should come before any stream capture on that device.
+ *  - Non-finite values are not reported by this entry point (the context path reports them
+ *    through osb_sync / OSB_RED_NAN_COUNT).
+ *  - All calls share the workspace: calls that overlap on the GPU race.
+ * Asynchronous on `stream` (a cudaStream_t, NULL for the default stream).
  * No counterpart in the reference (OPS always allocates its own datasets). */
 int osb_stage_noalloc(const osb_block_desc* desc, int rk_kind, double A, double B, double dt, void* stream);
 

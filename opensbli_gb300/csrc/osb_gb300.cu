@@ -578,7 +578,7 @@ int timing_collect(osb_ctx* c) {
 // block.
 template <typename T>
 int residual_t(osb_ctx* c, Block& bl, const RkFuse* rf, bool* fused) {
-  SchemeParams sp{bl.d.gama, bl.d.eps, bl.d.teno_ct, bl.d.shock_filter_control, 1e-12};
+  SchemeParams sp = scheme_params(bl.d.gama, bl.d.eps, bl.d.teno_ct, bl.d.shock_filter_control, 1e-12);
   if (fused) *fused = false;
   int rc;
   if (bl.d.scheme == OSB_SCHEME_CENTRAL4) {
@@ -652,10 +652,103 @@ int apply_interfaces(osb_ctx* c, int full, int fields) {
   return OSB_OK;
 }
 
+// Faces a single block can apply on its own (every kind but interfaces), with the periodic
+// pairing checked: the validation osb_stage_noalloc does before its first launch.
+bool block_faces_ok(const osb_block_desc& d, std::string& why) {
+  for (int dd = 0; dd < d.ndim; ++dd) {
+    const bool p0 = d.bc[dd][0] == OSB_BC_PERIODIC, p1 = d.bc[dd][1] == OSB_BC_PERIODIC;
+    if (p0 != p1) {
+      why = "periodic boundary on one side only (dir " + std::to_string(dd) + ")";
+      return false;
+    }
+    for (int side = 0; side < 2; ++side)
+      if (d.bc[dd][side] == OSB_BC_INTERFACE) {
+        why = "block interfaces need osb_step on a context";
+        return false;
+      }
+  }
+  return true;
+}
+
+// Non-interface boundary faces of one block: the whole periodic halo shell in one launch when
+// every face is periodic with one depth, else direction by direction (transverse ranges include
+// the halos, so corners come from layers filled before) periodic, zero-gradient, extrapolation,
+// symmetry and Dirichlet faces.
+int apply_block_bc(osb_ctx* c, Block& bl, size_t ib, int fields) {
+  const int nv = bl.d.ndim + 2;
+  if (const int D = uniform_periodic_depth(bl)) {
+    long shell = 1, inner = 1;
+    for (int e = 0; e < bl.d.ndim; ++e) {
+      shell *= bl.k.n[e] + 2 * D;
+      inner *= bl.k.n[e];
+    }
+    timing_begin(c, FAM_BC);
+    k_periodic_shell<<<grid_for(c, shell - inner, 256), 256, 0, c->stream>>>(bl.k, nv, D, fields);
+    timing_end(c);
+    c->launches++;
+    return OSB_OK;
+  }
+  for (int d = 0; d < bl.d.ndim; ++d) {
+    int b0 = bl.d.bc[d][0], b1 = bl.d.bc[d][1];
+    int dep0 = bl.d.bc_depth[d][0] > 0 ? bl.d.bc_depth[d][0] : 4;
+    int dep1 = bl.d.bc_depth[d][1] > 0 ? bl.d.bc_depth[d][1] : 4;
+    if (b0 == OSB_BC_PERIODIC && b1 == OSB_BC_PERIODIC) {
+      long tr = 1;
+      for (int e = 0; e < bl.d.ndim; ++e)
+        if (e != d) tr *= bl.k.n[e] + 2 * std::max(dep0, dep1);
+      long per = (long)std::max(dep0, dep1) * tr;
+      timing_begin(c, FAM_BC);
+      k_periodic<<<dim3(std::max(1, grid_for(c, per, 256) / (2 * nv) + 1), 2 * nv), 256, 0, c->stream>>>(
+          bl.k, nv, d, dep0, dep1, fields);
+      timing_end(c);
+      c->launches++;
+      continue;
+    }
+    for (int side = 0; side < 2; ++side) {
+      int kind = bl.d.bc[d][side];
+      if (kind == OSB_BC_ZERO_GRAD) {
+        long tr = 1;
+        for (int e = 0; e < bl.d.ndim; ++e)
+          if (e != d) tr *= bl.k.n[e];
+        timing_begin(c, FAM_BC);
+        k_zero_grad<<<grid_for(c, tr, 128), 128, 0, c->stream>>>(bl.k, nv, d, side, side ? dep1 : dep0, fields);
+        timing_end(c);
+        c->launches++;
+      } else if (kind == OSB_BC_EXTRAP0 || kind == OSB_BC_EXTRAP1) {
+        long tr = 1;
+        for (int e = 0; e < bl.d.ndim; ++e)
+          if (e != d) tr *= bl.k.n[e];
+        timing_begin(c, FAM_BC);
+        k_extrap<<<grid_for(c, tr, 128), 128, 0, c->stream>>>(bl.k, nv, d, side, side ? dep1 : dep0,
+                                                              kind == OSB_BC_EXTRAP1, fields);
+        timing_end(c);
+        c->launches++;
+      } else if (kind == OSB_BC_SYMMETRY) {
+        const long tr = face_extent(bl.k, d, bl.d.halo);
+        timing_begin(c, FAM_BC);
+        k_symmetry<<<grid_for(c, tr, 128), 128, 0, c->stream>>>(bl.k, nv, d, side, side ? dep1 : dep0,
+                                                                bl.d.halo, fields);
+        timing_end(c);
+        c->launches++;
+      } else if (kind == OSB_BC_DIRICHLET) {
+        const int dep = side ? dep1 : dep0;
+        const long tr = (long)face_extent(bl.k, d, bl.d.halo) * (dep + 1);
+        timing_begin(c, FAM_BC);
+        k_dirichlet<<<grid_for(c, tr, 128), 128, 0, c->stream>>>(bl.k, nv, d, side, dep, bl.d.halo,
+                                                                 bl.d.dirichlet[d][side], fields);
+        timing_end(c);
+        c->launches++;
+      } else if (kind == OSB_BC_PERIODIC) {
+        return fail(OSB_EINVAL, "periodic boundary on one side only (block %zu dir %d)", ib, d);
+      }
+    }
+  }
+  return OSB_OK;
+}
+
 // Boundary conditions of all blocks: interface faces (interior of the face), then each
-// block's periodic and zero-gradient faces direction by direction (transverse ranges include
-// the halos, so corners come from layers filled before), then the interface faces again with
-// their transverse halos, which the neighbour has filled by then.
+// block's own faces (apply_block_bc), then the interface faces again with their transverse
+// halos, which the neighbour has filled by then.
 int apply_bc(osb_ctx* c, int fields = BC_BOTH) {
   bool any_iface = false;
   for (auto& bl : c->blocks)
@@ -666,76 +759,8 @@ int apply_bc(osb_ctx* c, int fields = BC_BOTH) {
     if (rc) return rc;
   }
   for (size_t ib = 0; ib < c->blocks.size(); ++ib) {
-    Block& bl = c->blocks[ib];
-    const int nv = bl.d.ndim + 2;
-    if (const int D = uniform_periodic_depth(bl)) {
-      // all faces periodic: the whole halo shell in one launch
-      long shell = 1, inner = 1;
-      for (int e = 0; e < bl.d.ndim; ++e) {
-        shell *= bl.k.n[e] + 2 * D;
-        inner *= bl.k.n[e];
-      }
-      timing_begin(c, FAM_BC);
-      k_periodic_shell<<<grid_for(c, shell - inner, 256), 256, 0, c->stream>>>(bl.k, nv, D, fields);
-      timing_end(c);
-      c->launches++;
-      continue;
-    }
-    for (int d = 0; d < bl.d.ndim; ++d) {
-      int b0 = bl.d.bc[d][0], b1 = bl.d.bc[d][1];
-      int dep0 = bl.d.bc_depth[d][0] > 0 ? bl.d.bc_depth[d][0] : 4;
-      int dep1 = bl.d.bc_depth[d][1] > 0 ? bl.d.bc_depth[d][1] : 4;
-      if (b0 == OSB_BC_PERIODIC && b1 == OSB_BC_PERIODIC) {
-        long tr = 1;
-        for (int e = 0; e < bl.d.ndim; ++e)
-          if (e != d) tr *= bl.k.n[e] + 2 * std::max(dep0, dep1);
-        long per = (long)std::max(dep0, dep1) * tr;
-        timing_begin(c, FAM_BC);
-        k_periodic<<<dim3(std::max(1, grid_for(c, per, 256) / (2 * nv) + 1), 2 * nv), 256, 0, c->stream>>>(
-            bl.k, nv, d, dep0, dep1, fields);
-        timing_end(c);
-        c->launches++;
-      } else {
-        for (int side = 0; side < 2; ++side) {
-          int kind = bl.d.bc[d][side];
-          if (kind == OSB_BC_ZERO_GRAD) {
-            long tr = 1;
-            for (int e = 0; e < bl.d.ndim; ++e)
-              if (e != d) tr *= bl.k.n[e];
-            timing_begin(c, FAM_BC);
-            k_zero_grad<<<grid_for(c, tr, 128), 128, 0, c->stream>>>(bl.k, nv, d, side, side ? dep1 : dep0, fields);
-            timing_end(c);
-            c->launches++;
-          } else if (kind == OSB_BC_EXTRAP0 || kind == OSB_BC_EXTRAP1) {
-            long tr = 1;
-            for (int e = 0; e < bl.d.ndim; ++e)
-              if (e != d) tr *= bl.k.n[e];
-            timing_begin(c, FAM_BC);
-            k_extrap<<<grid_for(c, tr, 128), 128, 0, c->stream>>>(bl.k, nv, d, side, side ? dep1 : dep0,
-                                                                  kind == OSB_BC_EXTRAP1, fields);
-            timing_end(c);
-            c->launches++;
-          } else if (kind == OSB_BC_SYMMETRY) {
-            const long tr = face_extent(bl.k, d, bl.d.halo);
-            timing_begin(c, FAM_BC);
-            k_symmetry<<<grid_for(c, tr, 128), 128, 0, c->stream>>>(bl.k, nv, d, side, side ? dep1 : dep0,
-                                                                    bl.d.halo, fields);
-            timing_end(c);
-            c->launches++;
-          } else if (kind == OSB_BC_DIRICHLET) {
-            const int dep = side ? dep1 : dep0;
-            const long tr = (long)face_extent(bl.k, d, bl.d.halo) * (dep + 1);
-            timing_begin(c, FAM_BC);
-            k_dirichlet<<<grid_for(c, tr, 128), 128, 0, c->stream>>>(bl.k, nv, d, side, dep, bl.d.halo,
-                                                                     bl.d.dirichlet[d][side], fields);
-            timing_end(c);
-            c->launches++;
-          } else if (kind == OSB_BC_PERIODIC) {
-            return fail(OSB_EINVAL, "periodic boundary on one side only (block %zu dir %d)", ib, d);
-          }
-        }
-      }
-    }
+    int rc = apply_block_bc(c, c->blocks[ib], ib, fields);
+    if (rc) return rc;
   }
   if (any_iface) return apply_interfaces(c, 1, fields);
   return OSB_OK;
@@ -1210,6 +1235,7 @@ int osb_block_add(osb_ctx* c, const osb_block_desc* d, int* block_id) {
     k.n[i] = i < d->ndim ? d->size[i] : 1;
     ext[i] = i < d->ndim ? d->size[i] + 2 * d->halo : 1;
     k.invd[i] = i < d->ndim ? 1.0 / d->delta[i] : 0.0;
+    k.invdf[i] = (float)k.invd[i];
     k.inv2d[i] = i < d->ndim ? 1.0 / (d->delta[i] * d->delta[i]) : 0.0;
   }
   if (ext[0] * ext[1] * ext[2] >= (1L << 31)) return fail(OSB_EINVAL, "block too large for 32-bit indexing");
@@ -1723,6 +1749,7 @@ extern "C" int osb_metrics(const osb_block_desc* d, const double* const* x, doub
     k.n[i] = i < d->ndim ? d->size[i] : 1;
     ext[i] = i < d->ndim ? d->size[i] + 2 * d->halo : 1;
     k.invd[i] = i < d->ndim ? 1.0 / d->delta[i] : 0.0;
+    k.invdf[i] = (float)k.invd[i];
   }
   if (ext[0] * ext[1] * ext[2] >= (1L << 31)) return fail(OSB_EINVAL, "block too large for 32-bit indexing");
   k.st[0] = 1;
@@ -1756,6 +1783,7 @@ extern "C" int osb_stage_noalloc(const osb_block_desc* d, int rk_kind, double A,
     if (d->metric[i]) return fail(OSB_ENOTSUP, "osb_stage_noalloc takes Cartesian blocks only");
   if (d->filter != OSB_FILTER_NONE)
     return fail(OSB_ENOTSUP, "the non-linear filter follows a whole RK step (osb_step), not one stage");
+  if (!block_faces_ok(*d, why)) return fail(OSB_ENOTSUP, "osb_stage_noalloc: %s", why.c_str());
   const int nv = d->ndim + 2;
   size_t alloc = 1;
   for (int i = 0; i < d->ndim; ++i) alloc *= (size_t)(d->size[i] + 2 * d->halo);
@@ -1765,6 +1793,22 @@ extern "C" int osb_stage_noalloc(const osb_block_desc* d, int rk_kind, double A,
                 "holds %zu (OSB_NOALLOC_MAX_DOUBLES)", (size_t)nv * alloc, kNoAllocDoubles);
   int device = 0;
   OSB_CK(cudaGetDevice(&device));
+  // the stream and every array must belong to the current device, whose workspace is used
+  if (stream) {
+    int sdev = -1;
+    OSB_CK(cudaStreamGetDevice(static_cast<cudaStream_t>(stream), &sdev));
+    if (sdev != device) return fail(OSB_EINVAL, "stream belongs to device %d, the current device is %d", sdev, device);
+  }
+  for (int v = 0; v < nv; ++v)
+    for (const void* ptr : {(const void*)d->q[v], (const void*)d->rkold[v]}) {
+      cudaPointerAttributes at;
+      OSB_CK(cudaPointerGetAttributes(&at, ptr));
+      if (at.type != cudaMemoryTypeDevice && at.type != cudaMemoryTypeManaged)
+        return fail(OSB_EINVAL, "state / RK array of variable %d is not device memory", v);
+      if (at.type == cudaMemoryTypeDevice && at.device != device)
+        return fail(OSB_EINVAL, "state / RK array of variable %d lives on device %d, the current device is %d", v,
+                    at.device, device);
+    }
   double* scratch = nullptr;
   int rc = noalloc_scratch(device, &scratch);
   if (rc) return rc;
@@ -1788,6 +1832,7 @@ extern "C" int osb_stage_noalloc(const osb_block_desc* d, int rk_kind, double A,
     k.n[i] = i < d->ndim ? d->size[i] : 1;
     ext[i] = i < d->ndim ? d->size[i] + 2 * d->halo : 1;
     k.invd[i] = i < d->ndim ? 1.0 / d->delta[i] : 0.0;
+    k.invdf[i] = (float)k.invd[i];
     k.inv2d[i] = i < d->ndim ? 1.0 / (d->delta[i] * d->delta[i]) : 0.0;
   }
   k.st[0] = 1;
@@ -1805,47 +1850,9 @@ extern "C" int osb_stage_noalloc(const osb_block_desc* d, int rk_kind, double A,
   if (rc) return rc;
   long n = (long)k.n[0] * k.n[1] * k.n[2];
   k_rk<<<grid_for(&c, n, 256), 256, 0, c.stream>>>(k, nv, rk_kind == OSB_RK_LOW_STORAGE ? 0 : 1, A, B, dt, c.bad);
-  // boundary conditions of this block (the same kernels osb_apply_bc launches)
-  for (int dd = 0; dd < d->ndim; ++dd) {
-    int b0 = d->bc[dd][0], b1 = d->bc[dd][1];
-    int dep0 = d->bc_depth[dd][0] > 0 ? d->bc_depth[dd][0] : 4;
-    int dep1 = d->bc_depth[dd][1] > 0 ? d->bc_depth[dd][1] : 4;
-    if (b0 == OSB_BC_PERIODIC && b1 == OSB_BC_PERIODIC) {
-      long tr = 1;
-      for (int e = 0; e < d->ndim; ++e)
-        if (e != dd) tr *= k.n[e] + 2 * std::max(dep0, dep1);
-      long per = (long)std::max(dep0, dep1) * tr;
-      k_periodic<<<dim3(std::max(1, grid_for(&c, per, 256) / (2 * nv) + 1), 2 * nv), 256, 0, c.stream>>>(
-          k, nv, dd, dep0, dep1, BC_BOTH);
-    } else {
-      for (int side = 0; side < 2; ++side) {
-        int kind = d->bc[dd][side];
-        if (kind == OSB_BC_ZERO_GRAD) {
-          long tr = 1;
-          for (int e = 0; e < d->ndim; ++e)
-            if (e != dd) tr *= k.n[e];
-          k_zero_grad<<<grid_for(&c, tr, 128), 128, 0, c.stream>>>(k, nv, dd, side, side ? dep1 : dep0, BC_BOTH);
-        } else if (kind == OSB_BC_EXTRAP0 || kind == OSB_BC_EXTRAP1) {
-          long tr = 1;
-          for (int e = 0; e < d->ndim; ++e)
-            if (e != dd) tr *= k.n[e];
-          k_extrap<<<grid_for(&c, tr, 128), 128, 0, c.stream>>>(k, nv, dd, side, side ? dep1 : dep0,
-                                                                kind == OSB_BC_EXTRAP1, BC_BOTH);
-        } else if (kind == OSB_BC_SYMMETRY) {
-          k_symmetry<<<grid_for(&c, face_extent(k, dd, d->halo), 128), 128, 0, c.stream>>>(
-              k, nv, dd, side, side ? dep1 : dep0, d->halo, BC_BOTH);
-        } else if (kind == OSB_BC_DIRICHLET) {
-          const int dep = side ? dep1 : dep0;
-          k_dirichlet<<<grid_for(&c, (long)face_extent(k, dd, d->halo) * (dep + 1), 128), 128, 0, c.stream>>>(
-              k, nv, dd, side, dep, d->halo, d->dirichlet[dd][side], BC_BOTH);
-        } else if (kind == OSB_BC_PERIODIC) {
-          return fail(OSB_EINVAL, "periodic boundary on one side only (dir %d)", dd);
-        } else if (kind == OSB_BC_INTERFACE) {
-          return fail(OSB_ENOTSUP, "block interfaces need osb_step on a context");
-        }
-      }
-    }
-  }
+  // the block's boundary faces, with the kernels osb_apply_bc launches for them
+  rc = apply_block_bc(&c, bl, 0, BC_BOTH);
+  if (rc) return rc;
   OSB_CK(cudaGetLastError());
   return OSB_OK;
 }
