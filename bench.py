@@ -589,8 +589,7 @@ def secondary_arm(args):
     s32.apply_bc()
     tuned = None
     if args.workload == "kh_ensemble" and not args.no_tune:
-        best, trials = autotune.tune(s32, dt, steps=2, warmup=1, cache=os.path.join(ROOT, "gpurun_out",
-                                                                                     "autotune.json"))
+        best, trials = autotune.tune(s32, dt, steps=2, warmup=1, cache=autotune.DEFAULT_CACHE)
         tuned = {"schedule": best, "trials": len(trials),
                  "per_block_ms": next((t for t, c in trials if c["mode"] == abi.SCHED_PER_BLOCK), None),
                  "best_ms": min((t for t, _ in trials), default=None)}

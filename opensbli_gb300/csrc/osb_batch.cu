@@ -332,7 +332,7 @@ int batch_stage(osb_ctx* c, int s, double dt) {
     if (rc) return rc;
   }
   const Block& f = c->blocks[0];
-  SchemeParams sp{f.d.gama, f.d.eps, f.d.teno_ct, f.d.shock_filter_control, 1e-12};
+  SchemeParams sp = scheme_params(f.d.gama, f.d.eps, f.d.teno_ct, f.d.shock_filter_control, 1e-12);
   const int kind = c->rk_kind == OSB_RK_LOW_STORAGE ? 0 : 1;
   const int save = (kind == 1 && s == 0) ? 1 : 0;
   const BatchBlock* tab = c->batch.tab[c->qf_parity];

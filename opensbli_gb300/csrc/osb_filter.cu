@@ -90,7 +90,7 @@ template <typename T>
 __global__ void k_ducros(BlockK b, T* kappa, T inv_h) {
   const int n0 = b.n[0], n1 = b.n[1], n2 = b.n[2];
   const int total = n0 * n1 * n2;
-  const T id[3] = {(T)b.invd[0], (T)b.invd[1], (T)b.invd[2]};
+  const T id[3] = {inv_delta<T>(b, 0), inv_delta<T>(b, 1), inv_delta<T>(b, 2)};
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
     const int x = t % n0, y = (t / n0) % n1, z = t / (n0 * n1);
     const int c = lin(b, x, y, z);
@@ -534,7 +534,7 @@ __global__ void k_filter_apply(BlockK b, const T* __restrict__ kappa, FilterFlux
   const int n0 = b.n[0], n1 = b.n[1], n2 = b.n[2];
   const int total = n0 * n1 * n2;
   const int sx = b.st[0], sy = b.st[1], sz = b.st[2];
-  const T i0 = (T)b.invd[0], i1 = (T)b.invd[1], i2 = (T)b.invd[2];
+  const T i0 = inv_delta<T>(b, 0), i1 = inv_delta<T>(b, 1), i2 = inv_delta<T>(b, 2);
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
     const int x = t % n0, y = (t / n0) % n1, z = t / (n0 * n1);
     const int c = lin(b, x, y, z);
@@ -641,7 +641,7 @@ int filter_t(osb_ctx* c, Block& bl, double dt) {
   }
   const double h = sqrt(bl.d.delta[0] * bl.d.delta[0] + bl.d.delta[1] * bl.d.delta[1] + bl.d.delta[2] * bl.d.delta[2]);
   k_ducros<T><<<grid_for(c, n, FT), FT, 0, c->stream>>>(k, kappa, (T)(1.0 / h));
-  SchemeParams sp{bl.d.gama, bl.d.eps, bl.d.teno_ct, bl.d.shock_filter_control, 1e-12};
+  SchemeParams sp = scheme_params(bl.d.gama, bl.d.eps, bl.d.teno_ct, bl.d.shock_filter_control, 1e-12);
   const T check = (T)bl.d.ducros_check;
   const long nf0 = (long)(k.n[0] + 1) * k.n[1] * k.n[2], nf1 = (long)k.n[0] * (k.n[1] + 1) * k.n[2],
              nf2 = (long)k.n[0] * k.n[1] * (k.n[2] + 1);

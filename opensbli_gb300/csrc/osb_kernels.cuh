@@ -30,7 +30,16 @@ struct BlockK {
   const float* mf[10];  // FP32 copies of the metrics (FP32-residual path)
   double invd[3];  // 1/Delta
   double inv2d[3]; // 1/Delta^2
+  float invdf[3];  // 1/Delta rounded to FP32 on the host (no conversion in FP32 kernels)
 };
+
+// 1/Delta_d in the arithmetic type of a kernel.
+template <typename T>
+__device__ __forceinline__ T inv_delta(const BlockK& b, int d);
+template <>
+__device__ __forceinline__ double inv_delta<double>(const BlockK& b, int d) { return b.invd[d]; }
+template <>
+__device__ __forceinline__ float inv_delta<float>(const BlockK& b, int d) { return b.invdf[d]; }
 
 // ---- FP32-path helpers: no FP64 arithmetic (the FP64 pipe is 1/64 of FP32 on GB300) ----
 
@@ -350,7 +359,7 @@ __global__ void __launch_bounds__(SWEEP_THREADS, sizeof(T) == 4 ? 4 : 1)
   const int j1 = min(N, j0 + seg);
   if (j0 >= j1) return;
   const T gm = sp.gama;
-  const T invd = (T)b.invd[D];
+  const T invd = inv_delta<T>(b, D);
   const bool rd = !first;
   // iteration it (interface j = j0 - 1 + it) reads the fields of point j + 3 and, for j >= j0,
   // the residual of point j (both inside the 5-point halo / the interior)
@@ -516,7 +525,7 @@ __global__ void __launch_bounds__(32 * XWARPS) k_flux_x(BlockK b, SchemeParams s
     }
     cp_async_commit();
   };
-  const T invd = (T)b.invd[0];
+  const T invd = inv_delta<T>(b, 0);
   // residuals of the tile's points g .. g + XOUT - 1 that lie in [s0, s1), from the out tile
   auto flush = [&](int g) {
     __syncwarp();

@@ -32,16 +32,47 @@ struct SchemeParams {
   double teno_ct;    // TENO cut-off
   double sfc;        // shock_filter_control
   double eps32_rel;  // FP32 path: epsilon relative to the stencil's mean square
+  // the same constants rounded to FP32 on the host (scheme_params): an FP32 kernel that
+  // converted the doubles itself would run the conversions on the FP64 pipe, and under the
+  // sweeps' register cap the compiler re-derives such values inside the loop instead of
+  // keeping them in registers (measured: six FP64-pipe conversions per point in the FP32 y/z
+  // sweeps, 34 % FP64-pipe activity)
+  float gama_f, g1_f, teno_eps_f, teno_ct_f, sfc_f, eps32_rel_f;
 };
 
-// The same constants in the arithmetic type, converted once per thread (a conversion from
-// double runs on the FP64 pipe).
+__host__ __device__ inline SchemeParams scheme_params(double gama, double teno_eps, double teno_ct, double sfc,
+                                                      double eps32_rel) {
+  SchemeParams p;
+  p.gama = gama;
+  p.teno_eps = teno_eps;
+  p.teno_ct = teno_ct;
+  p.sfc = sfc;
+  p.eps32_rel = eps32_rel;
+  p.gama_f = (float)gama;
+  p.g1_f = (float)(gama - 1.0);
+  p.teno_eps_f = (float)teno_eps;
+  p.teno_ct_f = (float)teno_ct;
+  p.sfc_f = (float)sfc;
+  p.eps32_rel_f = (float)eps32_rel;
+  return p;
+}
+
+// The constants in the arithmetic type of a kernel.
 template <typename T>
-struct SP {
-  T gama, g1, teno_eps, teno_ct, sfc, eps32_rel;
+struct SP;
+template <>
+struct SP<double> {
+  double gama, g1, teno_eps, teno_ct, sfc, eps32_rel;
   __device__ __forceinline__ explicit SP(const SchemeParams& p)
-      : gama((T)p.gama), g1((T)(p.gama - 1.0)), teno_eps((T)p.teno_eps), teno_ct((T)p.teno_ct), sfc((T)p.sfc),
-        eps32_rel((T)p.eps32_rel) {}
+      : gama(p.gama), g1(p.gama - 1.0), teno_eps(p.teno_eps), teno_ct(p.teno_ct), sfc(p.sfc),
+        eps32_rel(p.eps32_rel) {}
+};
+template <>
+struct SP<float> {
+  float gama, g1, teno_eps, teno_ct, sfc, eps32_rel;
+  __device__ __forceinline__ explicit SP(const SchemeParams& p)
+      : gama(p.gama_f), g1(p.g1_f), teno_eps(p.teno_eps_f), teno_ct(p.teno_ct_f), sfc(p.sfc_f),
+        eps32_rel(p.eps32_rel_f) {}
 };
 
 // ---------------------------------------------------------------------------------------

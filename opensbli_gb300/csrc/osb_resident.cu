@@ -188,7 +188,7 @@ __global__ void __launch_bounds__(RT) k_resident_1d(const Resident1D* __restrict
 template <typename T, int SCH, int AVG>
 int launch_resident(osb_ctx* c, const Resident1D* dev, int nblocks, int maxE, double dt, int nsteps) {
   const Block& f = c->blocks[0];
-  SchemeParams sp{f.d.gama, f.d.eps, f.d.teno_ct, f.d.shock_filter_control, 1e-12};
+  SchemeParams sp = scheme_params(f.d.gama, f.d.eps, f.d.teno_ct, f.d.shock_filter_control, 1e-12);
   RkCoef rk{};
   rk.kind = c->rk_kind == OSB_RK_LOW_STORAGE ? 0 : 1;
   rk.nst = c->nst;

@@ -153,6 +153,14 @@ SHIPPED_TENO6 = os.path.join("apps", "performance_benchmark", "TENO6")
 SHIPPED = {"teno6": SHIPPED_TENO6, "c4w5": os.path.join("apps", "performance_benchmark", "Central4-WENO5")}
 
 
+def reference_root():
+    """Directory of the upstream OpenSBLI checkout these recipes read (generator and shipped
+    benchmark sources): $OSB_REFERENCE, by default the read-only checkout at /root/reference.
+    None where it is absent (a copy of this tree on another machine)."""
+    root = os.environ.get("OSB_REFERENCE", "/root/reference")
+    return root if os.path.isdir(os.path.join(root, "opensbli")) else None
+
+
 def build_shipped(name, reference=None, force=False):
     """Compile one of the reference's shipped performance-benchmark solvers (bit-exact
     generated code, from where it lies in the reference checkout: TENO6 or Central4-WENO5)
@@ -160,7 +168,9 @@ def build_shipped(name, reference=None, force=False):
     -O1: at -O2 the benchmark's own out-of-bounds read of its run-mode string (see
     shipped_compat.h) is miscompiled; the floating-point semantics are the same (no FMA
     contraction, no fast math)."""
-    reference = reference or os.environ.get("OSB_REFERENCE", "/root/reference")
+    reference = reference or reference_root()
+    if reference is None:
+        raise FileNotFoundError("the upstream checkout is not present (set OSB_REFERENCE)")
     src_dir = os.path.join(reference, SHIPPED[name])
     out_dir = os.path.join(REF, "bench_" + name)
     exe = os.path.join(out_dir, "ref_case")

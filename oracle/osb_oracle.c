@@ -4,8 +4,9 @@
  * TEST INFRASTRUCTURE ONLY.  This file is the checker the GPU path is compared with; it is
  * loaded by tests/, by __graft_entry__.smoke() and by bench.py's CPU-baseline leg, never by
  * the product.  Parity of this restatement with the reference's own generated solver is
- * pinned by tests/test_oracle_ref.py (reference OPS C++ compiled with oracle/ops_compat.h) and
- * by the committed golden vectors under tests/golden/.
+ * pinned by tests/test_oracle_golden.py against the committed golden vectors under tests/golden/
+ * (states of the reference's own generated OPS C++, compiled with oracle/ops_compat.h, and of
+ * its shipped benchmark solvers; tests/golden/make_golden.py writes them).
  *
  * It operates on HOST arrays described by the same osb_block_desc as the CUDA library
  * (include/osb_gb300.h): OPS layout, x fastest, 5 halo points per used direction.

@@ -1,11 +1,11 @@
 """Generate the reference solver sources (OPS C++) for each parity case.
 
 TEST INFRASTRUCTURE ONLY.  This script imports the upstream OpenSBLI generator from a
-read-only checkout (``--reference``, default ``/root/reference``), builds the problem
+read-only checkout (``--reference``, default ``harness.reference_root()``), builds the problem
 definitions below with OpenSBLI's own Python API, and writes the generated OPS C++
 (``opensbli.cpp``, ``opensbliblock00_kernels.h``, ``defdec_data_set.h``, ...) into
 ``oracle/_ref/<case>/``.  Those sources are then compiled against ``oracle/ops_compat.h``
-(see ``oracle/Makefile``) and their output pins the C restatement in ``oracle/osb_oracle.c``.
+(``oracle/harness.py::build_ref``) and their output pins the C restatement in ``oracle/osb_oracle.c``.
 Nothing under ``oracle/_ref`` is committed; it is regenerated from the reference.
 
 The generator pins SymPy 1.1 (``environment_and_run_scripts/InstallPython.sh:50``); only
@@ -25,29 +25,24 @@ several sizes, time steps and step counts from the environment.
 """
 import argparse
 import os
+import subprocess
 import sys
 import contextlib
 
 
 HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+sys.path.insert(0, os.path.dirname(HERE))
+import harness  # noqa: E402  (same directory: where the upstream checkout lies)
 
 
 def apply_compat_patches():
+    """The three SymPy-1.14 shims of the module docstring: the first is the package's front-end
+    shim (opensbli_gb300.compat.apply, which a problem script run through GB300Backend needs
+    too), the other two concern only the OPS printer."""
     import sympy
-    from sympy import Indexed
-
-    base_prop = sympy.Basic.is_commutative
-
-    def _get(self):
-        d = getattr(self, "__dict__", None)
-        if d is not None and "_osb_is_comm" in d:
-            return d["_osb_is_comm"]
-        return base_prop.fget(self)
-
-    def _set(self, value):
-        self.__dict__["_osb_is_comm"] = value
-
-    Indexed.is_commutative = property(_get, _set)
+    from opensbli_gb300 import compat
+    compat.apply()
 
     from opensbli.code_generation import opsc as opsc_mod
     from opensbli.core.opensbliobjects import GroupedPiecewise
@@ -529,7 +524,9 @@ CASES = {
 def build_case(name, reference=None):
     """Build the OpenSBLI block of one case (discretised, no code printed); for tests of the
     drop-in backend.  Returns (block, generator parameter dict)."""
-    reference = reference or os.environ.get("OSB_REFERENCE", "/root/reference")
+    reference = reference or harness.reference_root()
+    if reference is None:
+        raise FileNotFoundError("the upstream checkout is not present (set OSB_REFERENCE)")
     if reference not in sys.path:
         sys.path.insert(0, reference)
     apply_compat_patches()
@@ -540,12 +537,21 @@ def build_case(name, reference=None):
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("cases", nargs="*", default=sorted(CASES))
-    ap.add_argument("--reference", default=os.environ.get("OSB_REFERENCE", "/root/reference"))
+    ap.add_argument("--reference", default=harness.reference_root())
     ap.add_argument("--out", default=os.path.join(HERE, "_ref"))
     args = ap.parse_args(argv)
-    if not os.path.isdir(os.path.join(args.reference, "opensbli")):
+    if not args.reference or not os.path.isdir(os.path.join(args.reference, "opensbli")):
         print("reference checkout not found at %s; nothing generated" % args.reference)
         return 1
+    if len(args.cases) > 1:
+        # one interpreter per case: the generator keeps module-level state (the constants to
+        # declare, the grid objects), so a case generated after another would inherit its
+        # constants; the cases run in parallel
+        import concurrent.futures as cf
+        cmd = [sys.executable, os.path.abspath(__file__), "--reference", args.reference, "--out", args.out]
+        with cf.ThreadPoolExecutor(max_workers=max(1, min(len(args.cases), os.cpu_count() or 1))) as ex:
+            rcs = list(ex.map(lambda c: subprocess.call(cmd + [c]), args.cases))
+        return max(rcs)
     sys.path.insert(0, args.reference)
     apply_compat_patches()
     for name in args.cases:

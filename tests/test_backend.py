@@ -7,9 +7,10 @@ import pytest
 
 from opensbli_gb300 import abi, problems
 
-REF = os.environ.get("OSB_REFERENCE", "/root/reference")
-needs_ref = pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "opensbli")),
-                               reason="upstream OpenSBLI checkout not available")
+import harness  # oracle/ (on the path through conftest): where the upstream checkout lies
+
+REF = harness.reference_root()
+needs_ref = pytest.mark.skipif(REF is None, reason="upstream OpenSBLI checkout not available")
 
 
 def _backend_for(case, numbers):
