@@ -294,12 +294,43 @@ def _check_equation_classes(block):
             continue
         name = type(ec).__name__
         if name == "MetricsEquation":
-            continue  # metrics are passed as arrays
+            continue  # evaluated by metrics_of: the block becomes curvilinear, its metrics computed on the GPU
         if name == "UserDefinedEquations":
             continue  # a non-linear filter's kernels (_filter_of) or post-processing reductions
         raise NotImplementedError("equation class %s is not supported by the GB300 backend%s" % (
             name, "; the non-linear WENO filter is reached through BlockSpec (problems.tgv_filtered)"
             if "filter" in name.lower() or "Filter" in name else ""))
+
+
+def metrics_of(block):
+    """Coordinate names (x0, x1[, x2]) of a block that carries a MetricsEquation
+    (equation_types/metric.py:24-451), None for a Cartesian block.
+
+    The supported form is the one the curvilinear apps use: every direction curvilinear
+    (generate_transformations(ndim, 'x', [(True, True)] * ndim, order), so the ten arrays are
+    D = adj(J) / det J and det J of J_ij = d x_i / d xi_j, metric.py:183-197), the non-conservative
+    metrics, on a block whose faces are all periodic (the metric kernel runs over the interior and
+    the arrays are exchanged like the state).  Stretched-only or Cartesian directions, the
+    conservative metrics, and non-periodic curvilinear blocks (whose metric derivatives take the
+    one-sided boundary closures of Carpenter_scheme.py) raise NotImplementedError."""
+    mets = [ec for ec in block.list_of_equation_classes if type(ec).__name__ == "MetricsEquation"]
+    if not mets:
+        return None
+    me = mets[0]
+    if not all(getattr(me, "curvilinear_metric", [])) or len(me.curvilinear_metric) != block.ndim:
+        raise NotImplementedError("MetricsEquation with stretched-only or Cartesian directions (%s) is not supported; "
+                                  "every direction must be curvilinear" % (getattr(me, "curvilinear_metric", None),))
+    if getattr(me, "conservative_metrics", False):
+        raise NotImplementedError("conservative metrics are not supported")
+    from opensbli.core.boundary_conditions.periodic import PeriodicBC
+    for d, pair in enumerate(block.boundary_types):
+        for side, b in enumerate(pair):
+            if not isinstance(b, PeriodicBC):
+                raise NotImplementedError(
+                    "curvilinear block with a %s face (direction %d side %d): the metric derivatives at non-periodic "
+                    "boundaries need the one-sided Carpenter closures, which are not implemented" % (
+                        type(b).__name__, d, side))
+    return [str(c) for c in me.cartesian_coordinates]
 
 
 def block_spec(block, params):
@@ -311,7 +342,11 @@ def block_spec(block, params):
     delta = tuple(float(_const_value("Delta%dblock%d" % (d, b), p)) for d in range(nd))
     scheme, avg, central = _scheme_of(block)
     _check_equation_classes(block)
+    coords = metrics_of(block)
     visc = _viscosity_of(block)
+    if coords is not None and (visc != abi.VISC_NONE or scheme == abi.SCHEME_CENTRAL4):
+        raise NotImplementedError("curvilinear blocks take the characteristic Euler flux only (the metric-"
+                                  "transformed central and viscous terms are not implemented)")
     bc, depth = _bcs_of(block, scheme == abi.SCHEME_CENTRAL4)
     split = _split_form_of(block) if scheme == abi.SCHEME_CENTRAL4 else abi.SPLIT_FEIEREISEN
     filt, kappa = _filter_of(block, p)
@@ -320,7 +355,8 @@ def block_spec(block, params):
                      gama=_const_value("gama", p), Minf=_const_value("Minf", p, 1.0), Re=_const_value("Re", p, 1.0),
                      Pr=_const_value("Pr", p, 0.71), mu_const=1.0, eps=_const_value("eps", p, 1e-40),
                      teno_ct=_const_value("TENO_CT", p, 1e-6),
-                     shock_filter_control=_const_value("shock_filter_control", p, 1.0), delta=delta)
+                     shock_filter_control=_const_value("shock_filter_control", p, 1.0), delta=delta,
+                     curvilinear=coords is not None)
     if any(k == abi.BC_DIRICHLET for pair in bc for k in pair):
         spec.dirichlet = dirichlet_faces(block, spec, params)
     outlets = {(d, side): float(b.back_pressure) for d, pair in enumerate(block.boundary_types)
@@ -464,11 +500,82 @@ def precision_of(mixed_precision_config=None):
     return "fp32" if any(isinstance(t, type) and issubclass(t, FloatC) for t in types) else "fp64"
 
 
+def coordinates(block, spec, params, names):
+    """Grid coordinates (the DataObjects the block's GridBasedInitialisation defines under the
+    MetricsEquation's coordinate names) at every allocated point, OPS layout."""
+    values = _initial_values(block, spec, params)
+    missing = [n for n in names if n not in values]
+    if missing:
+        raise NotImplementedError("curvilinear block: the initialisation does not define the coordinates %s" % missing)
+    return [np.ascontiguousarray(values[n], dtype=np.float64) for n in names]
+
+
+class BackendPlan:
+    """What GB300Backend derives from an OpenSBLI algorithm: per block its BlockSpec, its initial
+    state (the GridBasedInitialisation evaluated over the allocation) and, for a curvilinear
+    block, its grid coordinates; the time integrator (kind, A, B); dt, niter and the precision.
+    It holds plain arrays only, so it can be written to a file (save) and run where the
+    OpenSBLI generator is not installed (GB300Backend.from_plan)."""
+
+    def __init__(self, specs, states, coords, rk, dt=None, niter=None, precision="fp64"):
+        self.specs = list(specs)
+        self.states = [None if q is None else [np.ascontiguousarray(a, dtype=np.float64) for a in q] for q in states]
+        self.coords = [None if x is None else [np.ascontiguousarray(a, dtype=np.float64) for a in x] for x in coords]
+        kind, A, B = rk
+        self.rk = (int(kind), tuple(float(x) for x in A), tuple(float(x) for x in B))
+        self.dt = None if dt is None else float(dt)
+        self.niter = None if niter is None else int(niter)
+        self.precision = precision
+
+    def save(self, path):
+        """One .npz: a JSON record of the specs and scalars plus the arrays."""
+        import json
+        arrays = {}
+        recs = []
+        for ib, spec in enumerate(self.specs):
+            rec, arr = spec.to_record()
+            recs.append(rec)
+            for k, a in arr.items():
+                arrays["b%d_%s" % (ib, k)] = a
+            for v, a in enumerate(self.states[ib] or []):
+                arrays["b%d_q%d" % (ib, v)] = a
+            for d, a in enumerate(self.coords[ib] or []):
+                arrays["b%d_x%d" % (ib, d)] = a
+        meta = {"specs": recs, "rk": [self.rk[0], list(self.rk[1]), list(self.rk[2])], "dt": self.dt,
+                "niter": self.niter, "precision": self.precision,
+                "ncoords": [0 if x is None else len(x) for x in self.coords]}
+        np.savez_compressed(path, meta=np.array(json.dumps(meta)), **arrays)
+
+    @classmethod
+    def load(cls, path):
+        import json
+        with np.load(path) as f:
+            meta = json.loads(str(f["meta"]))
+            specs, states, coords = [], [], []
+            for ib, rec in enumerate(meta["specs"]):
+                pre = "b%d_" % ib
+                arr = {k[len(pre):]: f[k] for k in f.files if k.startswith(pre + "dirichlet_")}
+                spec = BlockSpec.from_record(rec, arr)
+                specs.append(spec)
+                states.append([f[pre + "q%d" % v] for v in range(spec.nvars)])
+                nc = meta["ncoords"][ib]
+                coords.append([f[pre + "x%d" % d] for d in range(nc)] if nc else None)
+        rk = (meta["rk"][0], meta["rk"][1], meta["rk"][2])
+        return cls(specs, states, coords, rk, meta["dt"], meta["niter"], meta["precision"])
+
+
 class GB300Backend:
     """Stands in for OPSC(alg): owns the GPU state of every block of ``alg`` and runs its
     time loop on the GB300 kernels.  ``precision`` is "fp64" or "fp32" (FP32 residual, FP64
     state); left as None it follows the script's SimulationDataType and the optional
-    ``mixed_precision_config`` of OPSC (see precision_of)."""
+    ``mixed_precision_config`` of OPSC (see precision_of).
+
+    A curvilinear block (a MetricsEquation, see metrics_of) gets its ten metric arrays computed
+    on the GPU from the grid coordinates its initialisation defines (osb_metrics, the generated
+    metric kernel's central differences, halos from the periodic images) and passed with the
+    block; it is never run as a Cartesian block.  ``plan()`` returns everything the backend
+    derived from the algorithm as a BackendPlan; ``GB300Backend.from_plan`` runs such a plan
+    without the OpenSBLI generator (initialise and run are the same code)."""
 
     def __init__(self, alg, parameters, precision=None, device=0, graphs=True, mixed_precision_config=None):
         if precision is None:
@@ -483,6 +590,7 @@ class GB300Backend:
         for s in self.specs[1:]:
             if not s.same_discretisation(self.specs[0]):
                 raise NotImplementedError("blocks with different discretisations")
+        self.coord_names = [metrics_of(b) for b in self.blocks]
         self.rk = _rk_of(self.blocks[0])
         self.precision = precision
         self.device = device
@@ -490,16 +598,59 @@ class GB300Backend:
         self.dt = float(self.numbers["dt"]) if "dt" in self.numbers else None
         self.niter = int(self.numbers["niter"]) if "niter" in self.numbers else None
         self.solver = None
+        self.metrics = None
         self.iteration = 0
+        self._plan = None
+
+    @classmethod
+    def from_plan(cls, plan, precision=None, device=0, graphs=True):
+        """A backend that runs a BackendPlan (plan.precision unless precision is given)."""
+        be = cls.__new__(cls)
+        be.alg = None
+        be.params = {}
+        be.numbers = {}
+        be.blocks = []
+        be.specs = list(plan.specs)
+        be.coord_names = [None if x is None else ["x%d" % d for d in range(len(x))] for x in plan.coords]
+        be.rk = plan.rk
+        be.precision = precision or plan.precision
+        if be.precision not in ("fp64", "fp32"):
+            raise ValueError("precision must be 'fp64' or 'fp32', not %r" % (be.precision,))
+        be.device = device
+        be.graphs = graphs
+        be.dt = plan.dt
+        be.niter = plan.niter
+        be.solver = None
+        be.metrics = None
+        be.iteration = 0
+        be._plan = plan
+        return be
+
+    def plan(self):
+        """The BackendPlan of this algorithm: specs, initial states, coordinates, RK, dt, niter."""
+        if self._plan is None:
+            states = [initial_state(b, s, self.params) for b, s in zip(self.blocks, self.specs)]
+            coords = [None if names is None else coordinates(b, s, self.params, names)
+                      for b, s, names in zip(self.blocks, self.specs, self.coord_names)]
+            self._plan = BackendPlan(self.specs, states, coords, self.rk, self.dt, self.niter, self.precision)
+        return self._plan
 
     def initialise(self, states=None):
         """Upload the initial state (default: the scripts' GridBasedInitialisation evaluated on the
-        host) and apply the boundary conditions once, as the generated code does before its time loop."""
-        from .solver import Solver
+        host), compute the metric arrays of curvilinear blocks on the GPU, and apply the boundary
+        conditions once, as the generated code does before its time loop."""
+        from .solver import Solver, device_metrics
+        plan = self.plan()
         if states is None:
-            states = [initial_state(b, s, self.params) for b, s in zip(self.blocks, self.specs)]
-        self.solver = Solver(list(zip(self.specs, states)), precision=self.precision, rk=self.rk,
-                             device=self.device, graphs=self.graphs)
+            states = plan.states
+        self.metrics = []
+        for spec, x in zip(self.specs, plan.coords):
+            if spec.curvilinear != (x is not None):
+                raise abi.OSBError("block curvilinear flag and coordinates disagree")
+            self.metrics.append(None if x is None else
+                                device_metrics(spec, x, fill=abi.METRIC_PERIODIC, device=self.device))
+        items = [(s, q) if m is None else (s, q, m) for s, q, m in zip(self.specs, states, self.metrics)]
+        self.solver = Solver(items, precision=self.precision, rk=self.rk, device=self.device, graphs=self.graphs)
         self.solver.apply_bc()
         return self
 

@@ -271,11 +271,42 @@ def curvilinear_wave_2d(n=128, scheme=abi.SCHEME_WENO5_Z, averaging=abi.AVG_ROE)
     differences on the interior, exchanged periodically.  Returns (spec, state, metrics)."""
     spec = BlockSpec(ndim=2, size=(n, n), scheme=scheme, averaging=averaging,
                      bc=[[abi.BC_PERIODIC] * 2 for _ in range(2)], bc_depth=[[4, 4], [4, 4]],
-                     delta=(2.0 / n, 2.0 / n), gama=1.4)
+                     delta=(2.0 / n, 2.0 / n), gama=1.4, curvilinear=True)
     x0, x1 = wave_2d_coords(spec)
     rho = 1.0 + 0.2 * np.sin(math.pi * (x0 + x1))
     q = _cons(spec, rho, [np.full(spec.shape, 1.0), np.full(spec.shape, -0.5)], 1.0)
     return spec, q, metrics_central4(spec, [x0, x1], periodic_from_interior=True)
+
+
+def wave_3d_coords(spec, amp=0.05):
+    """Grid coordinates of the periodic wavy 3D mesh of curvilinear_wave_3d at every allocated
+    point: x_i = eta_i + amp sin(2 pi eta_j) sin(2 pi eta_k), (i, j, k) cyclic, eta_d = index_d
+    Delta_d."""
+    eta = [spec.delta[d] * spec.grid_index(d).astype(np.float64) for d in range(3)]
+    out = []
+    for i in range(3):
+        j, k = (i + 1) % 3, (i + 2) % 3
+        x = eta[i] + amp * np.sin(2.0 * math.pi * eta[j]) * np.sin(2.0 * math.pi * eta[k])
+        out.append(np.ascontiguousarray(np.broadcast_to(x, spec.shape)))
+    return out
+
+
+def curvilinear_wave_3d(sizes=(16, 12, 10), scheme=abi.SCHEME_TENO5, averaging=abi.AVG_ROE, minf=0.7):
+    """Euler on a periodic wavy 3D mesh over the unit box (Delta_d = 1/N_d): coordinates
+    wave_3d_coords, rho = 1 + 0.1 sin(2 pi (x0 + x1 + x2)), u = (0.7, -0.3, 0.2),
+    p = 1/(gama Minf^2) + 0.1 sin(2 pi (x0 - x1)); metrics from 4th-order central differences on
+    the interior, exchanged periodically -- the single-block problem the generated reference case
+    curv3d_teno5 solves.  Returns (spec, state, metrics, coordinates)."""
+    spec = BlockSpec(ndim=3, size=tuple(sizes), scheme=scheme, averaging=averaging, viscous=abi.VISC_NONE,
+                     bc=[[abi.BC_PERIODIC] * 2 for _ in range(3)], bc_depth=[[4, 4] for _ in range(3)],
+                     delta=tuple(1.0 / n for n in sizes), gama=1.4, Minf=minf, curvilinear=True)
+    x = wave_3d_coords(spec)
+    g = spec.gama
+    rho = 1.0 + 0.1 * np.sin(2.0 * math.pi * (x[0] + x[1] + x[2]))
+    p = 1.0 / (g * minf * minf) + 0.1 * np.sin(2.0 * math.pi * (x[0] - x[1]))
+    u = [np.full(spec.shape, c) for c in (0.7, -0.3, 0.2)]
+    q = _cons(spec, rho, u, p)
+    return spec, q, metrics_central4(spec, x, periodic_from_interior=True), x
 
 
 def shock_reflection(n0=457, n1=255, sizes=None, flux_type=abi.FLUX_LLF, back_pressure=None):
@@ -412,7 +443,8 @@ def curvilinear_multiblock_3d(sizes=None, seed=0, amp=0.05, mach=0.7, pulse=1e-2
         size = sizes[name]
         org, bc, iface = layout[name]
         spec = BlockSpec(ndim=3, size=size, scheme=scheme, averaging=averaging, viscous=abi.VISC_NONE,
-                         bc=bc, bc_depth=[[4, 4] for _ in range(3)], iface=iface, delta=(dl, dl, dl), gama=g)
+                         bc=bc, bc_depth=[[4, 4] for _ in range(3)], iface=iface, delta=(dl, dl, dl), gama=g,
+                         curvilinear=True)
         # index coordinates on the allocation grown by 2 (for the metric stencil)
         grids = []
         for d in range(3):

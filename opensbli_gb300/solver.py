@@ -25,7 +25,8 @@ class Solver:
 
     specs_states: list of (BlockSpec, [nv arrays in OPS layout]) pairs, or triples whose third
         item is the list of 10 metric arrays of a curvilinear block (osb_block_desc.metric
-        order: D_di at 3*d + i, det J at 9; None where unused).
+        order: D_di at 3*d + i, det J at 9; None where unused; numpy arrays or CUDA tensors).
+        A spec marked curvilinear must come with its metric arrays.
     precision: "fp64" (parity path) or "fp32" (FP32 residual, FP64 state).
     rk: "ls3" (RungeKuttaLS(3)), "sbli3" (RungeKutta(3)) or (kind, A, B).
     """
@@ -59,12 +60,16 @@ class Solver:
                 self.q.append(q)
                 self.rk.append(r)
                 mt, mp = None, None
+                if met is None and getattr(spec, "curvilinear", False):
+                    raise abi.OSBError("block %d is curvilinear: its metric arrays must be given" % i)
                 if met is not None:
                     for a in met:
-                        if a is not None and tuple(np.shape(a)) != tuple(spec.shape):
+                        if a is not None and tuple(a.shape) != tuple(spec.shape):
                             raise abi.OSBError("metric array of shape %s, block allocation is %s"
-                                               % (np.shape(a), spec.shape))
-                    mt = [None if a is None else torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).to(self.device)
+                                               % (tuple(a.shape), spec.shape))
+                    mt = [None if a is None else
+                          (a.to(device=self.device, dtype=torch.float64).contiguous() if torch.is_tensor(a) else
+                           torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).to(self.device))
                           for a in met]
                     mp = [None if a is None else a.data_ptr() for a in mt]
                 self.met.append(mt)

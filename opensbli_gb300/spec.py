@@ -46,6 +46,9 @@ class BlockSpec:
     flux_type: int = abi.FLUX_LLF
     # pressure-outlet faces: {(direction, side): back pressure}
     back_pressure: dict = None
+    # a curvilinear block: its metric arrays (osb_block_desc.metric) must be supplied; a
+    # curvilinear block without them is refused instead of being run as a Cartesian one
+    curvilinear: bool = False
 
     def __post_init__(self):
         self.size = tuple(int(s) for s in self.size)
@@ -85,6 +88,47 @@ class BlockSpec:
         shp = [1] * self.ndim
         shp[self.ndim - 1 - d] = n
         return idx.reshape(shp)
+
+    # ---- serialisation (the backend's plan files): scalars and lists as plain values, the
+    # Dirichlet face arrays separately
+    _SCALARS = ("ndim", "scheme", "averaging", "viscous", "gama", "Minf", "Re", "Pr", "mu_const", "eps", "teno_ct",
+                "shock_filter_control", "halo", "split_form", "filter", "ducros_check", "ducros_select", "tvd_kappa",
+                "flux_type", "curvilinear")
+
+    def to_record(self):
+        """(dict of plain values, {name: array}) that from_record turns back into this spec."""
+        rec = {k: getattr(self, k) for k in self._SCALARS}
+        rec["curvilinear"] = bool(self.curvilinear)
+        rec["size"] = list(self.size)
+        rec["delta"] = [float(x) for x in self.delta]
+        rec["bc"] = [list(map(int, r)) for r in self.bc]
+        rec["bc_depth"] = [list(map(int, r)) for r in self.bc_depth]
+        rec["iface"] = None if self.iface is None else [[None if f is None else list(map(int, f)) for f in r]
+                                                        for r in self.iface]
+        rec["back_pressure"] = None if not self.back_pressure else [[d, s, float(v)] for (d, s), v in
+                                                                     sorted(self.back_pressure.items())]
+        arrays = {"dirichlet_%d_%d" % k: np.ascontiguousarray(a) for k, a in (self.dirichlet or {}).items()}
+        return rec, arrays
+
+    @classmethod
+    def from_record(cls, rec, arrays=None):
+        kw = {k: rec[k] for k in cls._SCALARS if k in rec}
+        kw["size"] = tuple(rec["size"])
+        kw["delta"] = tuple(rec["delta"])
+        kw["bc"] = [list(r) for r in rec["bc"]]
+        kw["bc_depth"] = [list(r) for r in rec["bc_depth"]]
+        if rec.get("iface") is not None:
+            kw["iface"] = [[None if f is None else tuple(f) for f in r] for r in rec["iface"]]
+        if rec.get("back_pressure"):
+            kw["back_pressure"] = {(int(d), int(s)): float(v) for d, s, v in rec["back_pressure"]}
+        dirichlet = {}
+        for name, a in (arrays or {}).items():
+            if name.startswith("dirichlet_"):
+                _, d, s = name.split("_")
+                dirichlet[(int(d), int(s))] = np.asarray(a, dtype=np.float64)
+        if dirichlet:
+            kw["dirichlet"] = dirichlet
+        return cls(**kw)
 
     def same_discretisation(self, other):
         return (self.ndim, self.scheme, self.averaging, self.viscous, self.split_form, self.filter,

@@ -230,3 +230,78 @@ def test_pressure_outlet_maps_and_runs_in_the_oracle():
     sl = spec.interior()
     errs = [harness.rel_err(ob.q[0][v][sl], g["after_30"][v]) for v in range(4)]
     assert max(errs) < 1e-12, errs
+
+
+PLANS = ["sod400", "tgv_teno5_12", "curv128", "curv3d_16x12x10", "shock_64x32", "kh_32"]
+
+
+@needs_ref
+@pytest.mark.parametrize("name", PLANS)
+def test_backend_plan_matches_committed_fixture(name):
+    """GB300Backend still derives, from the reference's own problem definition, exactly the plan
+    committed under tests/golden/ (specs, initial state, coordinates, RK, dt, niter), which the
+    GPU tests run through GB300Backend.from_plan.  One interpreter per case: the generator keeps
+    module-level state between problems."""
+    import subprocess
+    import sys
+    script = os.path.join(os.path.dirname(__file__), "golden", "make_backend_plans.py")
+    r = subprocess.run([sys.executable, script, "--check", name], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+
+
+@needs_ref
+def test_curvilinear_script_is_curvilinear():
+    """The reference's curvilinear case (MetricsEquation + LFWeno) maps onto a curvilinear spec
+    whose coordinates come from its initialisation; the Solver refuses such a spec without
+    metric arrays instead of running it as a Cartesian block."""
+    be = _backend_for("curv_weno5z", {"gama": "1.4", "dt": "0.0005", "niter": "10", "block0np0": "32",
+                                      "block0np1": "32", "Delta0block0": "2.0/(block0np0)",
+                                      "Delta1block0": "2.0/(block0np1)"})
+    spec = be.specs[0]
+    assert spec.curvilinear and be.coord_names[0] == ["x0", "x1"]
+    plan = be.plan()
+    ref_spec, ref_q, _ = problems.curvilinear_wave_2d(32)
+    x0, x1 = problems.wave_2d_coords(ref_spec)
+    assert np.array_equal(plan.coords[0][0], x0) and np.array_equal(plan.coords[0][1], x1)
+    for v in range(4):
+        assert np.array_equal(plan.states[0][v], ref_q[v]), v
+
+
+@needs_ref
+def test_curvilinear_with_non_periodic_faces_refused():
+    """A curvilinear block with a non-periodic face needs the one-sided metric closures, which are
+    not implemented: the backend refuses it."""
+    import contextlib
+    import ref_generate
+    block, _ = ref_generate.build_case("curv_weno5z", REF)
+    from opensbli import TraditionalAlgorithmRK
+    from opensbli.core.boundary_conditions.zero_gradient_outlet import ZeroGradientOutletBC
+    from opensbli_gb300.backend import GB300Backend
+    bts = [list(pair) for pair in block.boundary_types]
+    bts[0][1] = ZeroGradientOutletBC(0, 1)
+    block.boundary_types = bts
+    with open(os.devnull, "w") as dn, contextlib.redirect_stdout(dn):
+        alg = TraditionalAlgorithmRK(block)
+    with pytest.raises(NotImplementedError, match="Carpenter"):
+        GB300Backend(alg, {"gama": "1.4", "block0np0": "32", "block0np1": "32", "Delta0block0": "2.0/(block0np0)",
+                           "Delta1block0": "2.0/(block0np1)"})
+
+
+def test_plan_file_round_trip(tmp_path):
+    """BackendPlan.save / load keep every spec field, the Dirichlet faces and the arrays."""
+    from opensbli_gb300.backend import BackendPlan
+    spec, q = problems.shock_reflection(64, 32)
+    cspec, cq, _, x = problems.curvilinear_wave_3d((8, 8, 8))
+    plan = BackendPlan([spec, cspec], [q, cq], [None, x], (abi.RK_LOW_STORAGE, problems.RK3_SSP_A,
+                                                           problems.RK3_SSP_B), 0.5, 7, "fp32")
+    plan.save(str(tmp_path / "p.npz"))
+    back = BackendPlan.load(str(tmp_path / "p.npz"))
+    assert back.rk == plan.rk and (back.dt, back.niter, back.precision) == (0.5, 7, "fp32")
+    for a, b in zip(plan.specs, back.specs):
+        ra, xa = a.to_record()
+        rb, xb = b.to_record()
+        assert ra == rb and sorted(xa) == sorted(xb)
+        assert all(np.array_equal(xa[k], xb[k]) for k in xa)
+    assert back.specs[1].curvilinear and back.coords[0] is None
+    assert all(np.array_equal(u, v) for u, v in zip(back.coords[1], x))
+    assert all(np.array_equal(u, v) for u, v in zip(back.states[0], q))
