@@ -99,6 +99,7 @@ static void cr_compute(const osb_block_desc* b, const geom_t* g, cr_t* c) {
   const int nd = b->ndim, nv = nd + 2;
   const double gm = b->gama;
   long n = npts_alloc(g);
+#pragma omp parallel for schedule(static)
   for (long id = 0; id < n; ++id) {
     double rho = b->q[0][id];
     if (rho == 0.0) continue;
@@ -716,6 +717,7 @@ int oracle_residual(const osb_block_desc* b, double* const* Rout) {
   if (b->scheme == OSB_SCHEME_CENTRAL4) {
     /* quadratic products needed by the split form (precomputed over the extent) */
     double* tmp[1] = {NULL};
+#pragma omp parallel for schedule(static)
     for (int k = 0; k < g.n[2]; ++k)
       for (int j = 0; j < g.n[1]; ++j)
         for (int i = 0; i < g.n[0]; ++i) {
@@ -730,9 +732,12 @@ int oracle_residual(const osb_block_desc* b, double* const* Rout) {
     double* fh[3][NVMAX];
     for (int d = 0; d < nd; ++d)
       for (int v = 0; v < nv; ++v) fh[d][v] = (double*)calloc(n, sizeof(double));
+    /* every loop below writes each point from its own inputs only: the OpenMP split over the
+     * outer index leaves the results bit-identical to a serial run */
     for (int d = 0; d < nd; ++d) {
       int lo[3] = {0, 0, 0};
       lo[d] = -1;
+#pragma omp parallel for schedule(static)
       for (int k = lo[2]; k < g.n[2]; ++k)
         for (int j = lo[1]; j < g.n[1]; ++j)
           for (int i = lo[0]; i < g.n[0]; ++i) {
@@ -744,6 +749,7 @@ int oracle_residual(const osb_block_desc* b, double* const* Rout) {
             for (int v = 0; v < nv; ++v) fh[d][v][id] = f[v];
           }
     }
+#pragma omp parallel for schedule(static)
     for (int k = 0; k < g.n[2]; ++k)
       for (int j = 0; j < g.n[1]; ++j)
         for (int i = 0; i < g.n[0]; ++i) {
@@ -764,6 +770,7 @@ int oracle_residual(const osb_block_desc* b, double* const* Rout) {
       for (int v = 0; v < nv; ++v) free(fh[d][v]);
   }
   if (b->viscous != OSB_VISC_NONE) {
+#pragma omp parallel for schedule(static)
     for (int k = 0; k < g.n[2]; ++k)
       for (int j = 0; j < g.n[1]; ++j)
         for (int i = 0; i < g.n[0]; ++i) {
@@ -1554,6 +1561,7 @@ static int stage_impl(osb_block_desc* blocks, int nblocks, int rk_kind, const do
       double* q = b->q[v];
       double* o = b->rkold[v];
       const double* r = R[ib * NVMAX + v];
+#pragma omp parallel for schedule(static)
       for (int k = 0; k < g.n[2]; ++k)
         for (int j = 0; j < g.n[1]; ++j)
           for (int i = 0; i < g.n[0]; ++i) {

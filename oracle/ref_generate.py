@@ -440,6 +440,75 @@ def case_kh_weno5z():
     return block, params
 
 
+def case_curv3d_teno5():
+    """3D curvilinear Euler on a periodic wavy mesh, characteristic LLF TENO5 (Roe average) with
+    4th-order central metrics (MetricsEquation, every direction curvilinear), RK-LS3: the
+    single-block form of the 4-block curvilinear configuration's discretisation.  Mesh
+    x_i = xi_i Delta_i + 0.05 sin(2 pi eta_j) sin(2 pi eta_k) over the unit box ((i, j, k) cyclic,
+    eta = index x Delta), a density / pressure wave rho = 1 + 0.1 sin(2 pi (x0 + x1 + x2)),
+    p = 1 / (gama Minf^2) + 0.1 sin(2 pi (x0 - x1)), u = (0.7, -0.3, 0.2)."""
+    from sympy import pi, sin, Eq
+    from opensbli import (MetricsEquation, EinsteinEquation, SimulationEquations, ConstituentRelations,
+                          SimulationBlock, RoeAverage, LFTeno, StoreSome, RungeKuttaLS, GridVariable, DataObject,
+                          ConstantObject, parse_expr, GridBasedInitialisation, PeriodicBC)
+    ndim = 3
+    metriceq = MetricsEquation()
+    metriceq.generate_transformations(ndim, "x", [(True, True)] * 3, 2)
+    sc1 = "**{'scheme':'Teno'}"
+    mass = "Eq(Der(rho,t), - Conservative(detJ * rho*U_j,xi_j,%s)/detJ)" % sc1
+    momentum = "Eq(Der(rhou_i,t) , -  Conservative(detJ * (rhou_i*U_j + p*D_j_i), xi_j , %s)/detJ)" % sc1
+    energy = "Eq(Der(rhoE,t), - Conservative(detJ * (p+rhoE)*U_j,xi_j, %s)/detJ)" % sc1
+    constants_eqns = ["gama", "Minf"]
+    einstein = EinsteinEquation()
+    einstein.optional_subs_dict = metriceq.metric_subs
+    sim = SimulationEquations()
+    cr = ConstituentRelations()
+    for base in (mass, momentum, energy):
+        e = einstein.expand(base, ndim, "xi", [], constants_eqns)
+        if base == momentum:
+            e = [Eq(x.lhs, x.rhs) for x in e]
+        elif base == energy:
+            e = Eq(e.lhs, e.rhs)
+        sim.add_equations(e)
+    for c in ["Eq(u_i, rhou_i/rho)", "Eq(p, (gama-1)*(rhoE-rho*(1/2)*(KD(_i,_j)*u_i*u_j)))",
+              "Eq(a, (gama*p/rho)**0.5)", "Eq(U_i, D_i_j*u_j)"]:
+        cr.add_equations(einstein.expand(c, ndim, "xi", [], constants_eqns))
+    block = SimulationBlock(ndim, block_number=0)
+    schemes = {}
+    LF = LFTeno(order=5, averaging=RoeAverage([0, 1]), flux_type="LLF")
+    schemes[LF.name] = LF
+    cent = StoreSome(4, "u0 u1 u2")  # the metric derivatives' central scheme
+    schemes[cent.name] = cent
+    rk = RungeKuttaLS(3)
+    schemes[rk.name] = rk
+    block.set_discretisation_schemes(schemes)
+    local_dict = {"block": block, "GridVariable": GridVariable, "DataObject": DataObject,
+                  "gama": ConstantObject("gama"), "Minf": ConstantObject("Minf")}
+    (i, j, k) = block.grid_indexes
+    (dx, dy, dz) = block.deltas
+    x0 = Eq(DataObject("x0"), i * dx + 0.05 * sin(2.0 * pi * j * dy) * sin(2.0 * pi * k * dz), evaluate=False)
+    x1 = Eq(DataObject("x1"), j * dy + 0.05 * sin(2.0 * pi * k * dz) * sin(2.0 * pi * i * dx), evaluate=False)
+    x2 = Eq(DataObject("x2"), k * dz + 0.05 * sin(2.0 * pi * i * dx) * sin(2.0 * pi * j * dy), evaluate=False)
+    eqs = [parse_expr(e, local_dict=local_dict) for e in [
+        "Eq(GridVariable(d), 1+0.1*sin(2*pi*(DataObject(x0)+DataObject(x1)+DataObject(x2))))",
+        "Eq(GridVariable(u0), 0.7)", "Eq(GridVariable(u1), -0.3)", "Eq(GridVariable(u2), 0.2)",
+        "Eq(GridVariable(p), 1/(gama*Minf**2) + 0.1*sin(2*pi*(DataObject(x0)-DataObject(x1))))",
+        "Eq(DataObject(rho), d)", "Eq(DataObject(rhou0), d*u0)", "Eq(DataObject(rhou1), d*u1)",
+        "Eq(DataObject(rhou2), d*u2)",
+        "Eq(DataObject(rhoE), p/(gama-1) + 0.5* d *(u0**2+u1**2+u2**2))"]]
+    initial = GridBasedInitialisation()
+    initial.add_equations([x0, x1, x2] + eqs)
+    block.set_block_boundaries([[PeriodicBC(d, 0), PeriodicBC(d, 1)] for d in range(ndim)])
+    block.set_equations([cr, initial, sim, metriceq])
+    block.discretise()
+    params = {"gama": "1.4", "Minf": "0.7", "dt": 'osb_env_double("OSB_DT", 0.002)',
+              "niter": 'osb_env_int("OSB_NITER", 10)', "TENO_CT": 'osb_env_double("OSB_TENO_CT", 1e-6)'}
+    for d, n in enumerate((16, 12, 10)):
+        params["block0np%d" % d] = 'osb_env_int("OSB_NP%d", %d)' % (d, n)
+        params["Delta%dblock0" % d] = "1.0/(block0np%d)" % d
+    return block, params
+
+
 def case_curv_weno5z():
     """2D curvilinear wavy-mesh Euler wave, characteristic LLF WENO5-Z (Roe average) with
     4th-order central metrics, periodic, RK-LS3: the reference's verification case
@@ -518,6 +587,7 @@ CASES = {
     "shock_reflection_pout": lambda: case_shock_reflection(outlet=0.2),
     "kh_weno5z": case_kh_weno5z,
     "curv_weno5z": case_curv_weno5z,
+    "curv3d_teno5": case_curv3d_teno5,
 }
 
 

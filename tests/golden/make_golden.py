@@ -61,7 +61,14 @@ CASES = {
     # problems.metrics_central4 bit for bit
     "curv_weno5z_32": ("curv_weno5z", lambda: problems.curvilinear_wave_2d(32),
                        {"OSB_NP0": 32, "OSB_NP1": 32}, 5e-4, [1, 3, 30], None),
+    # 3D curvilinear TENO5 (MetricsEquation, every direction curvilinear); the solver's own metric
+    # arrays are stored with the states (interior; their halos are the periodic images)
+    "curv3d_teno5_16x12x10_perturbed": ("curv3d_teno5", lambda: problems.curvilinear_wave_3d((16, 12, 10)),
+                                        {"OSB_NP0": 16, "OSB_NP1": 12, "OSB_NP2": 10}, 2e-3, [1, 3, 30],
+                                        (1e-3, 21)),
 }
+
+METRIC_NAMES = ["D00", "D01", "D02", "D10", "D11", "D12", "D20", "D21", "D22", "detJ"]
 
 
 def make(name):
@@ -84,6 +91,14 @@ def make(name):
         out["after_%d" % n] = np.stack([r[nm][sl] for nm in names])
         if n == 1 and "Residual0_B0" in r:
             out["residual_1"] = np.stack([r["Residual%d_B0" % v][sl] for v in range(spec.nvars)])
+        if n == 1 and spec.ndim == 3 and "detJ_B0" in r:
+            mets = [r[m + "_B0"] for m in METRIC_NAMES]
+            for m in mets:  # the generated solver exchanges its metrics periodically
+                b = np.zeros_like(m)
+                b[sl] = m[sl]
+                problems._periodic_fill(spec, b, spec.halo)
+                assert np.array_equal(b[2:-2, 2:-2, 2:-2], m[2:-2, 2:-2, 2:-2])
+            out["metrics"] = np.stack([m[sl] for m in mets])
     np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
     print("wrote", name)
 

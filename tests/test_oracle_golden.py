@@ -10,6 +10,29 @@ from opensbli_gb300 import abi, problems
 
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
+CURV3D = "curv3d_teno5_16x12x10_perturbed"
+
+
+def reference_metrics(spec, name=CURV3D):
+    """The generated solver's own metric arrays of a golden case (stored on the interior), with
+    the periodic halos its exchange gives them."""
+    g = np.load(os.path.join(GOLD, name + ".npz"))
+    out = []
+    for m in g["metrics"]:
+        a = np.zeros(spec.shape)
+        a[spec.interior()] = m
+        problems._periodic_fill(spec, a, spec.halo)
+        out.append(a)
+    return out
+
+
+def _curv3d():
+    """3D curvilinear TENO5 with the reference solver's own metrics (so the flux path is pinned
+    on identical inputs; the metric arrays themselves are compared separately)."""
+    spec, q, _, _ = problems.curvilinear_wave_3d((16, 12, 10))
+    return spec, q, reference_metrics(spec)
+
+
 CASES = {
     "sod_weno5js_400": (lambda: problems.sod(400), "ls3", None, 1e-12),
     "sod_extrap_200_perturbed": (lambda: problems.sod(200, bc=(abi.BC_EXTRAP1, abi.BC_EXTRAP0)), "ls3", (1e-2, 13),
@@ -23,6 +46,8 @@ CASES = {
     "tgv_central_12": (lambda: problems.tgv(12, minf=0.1, scheme=abi.SCHEME_CENTRAL4), "ls3", None, 1e-12),
     "kh_weno5z_24_perturbed": (lambda: problems.kh(24, amp=1.0, phase=0.0), "sbli3", (1e-3, 12), 1e-9),
     "curv_weno5z_32": (lambda: problems.curvilinear_wave_2d(32), "ls3", None, 1e-12),
+    # 3D curvilinear TENO5 (MetricsEquation + LFTeno(5)), the 4-block configuration's discretisation
+    CURV3D: (_curv3d, "ls3", (1e-3, 21), 1e-12),
     # Dirichlet inlet and top (post-shock state from x = 40), extrapolation outlet, symmetry wall
     "shock_reflection_64x32_perturbed": (lambda: problems.shock_reflection(64, 32), "ls3", (1e-2, 4), 1e-12),
     "shock_reflection_ssp_64x32_perturbed": (lambda: problems.shock_reflection(64, 32), "ssp3", (1e-2, 4), 1e-12),
@@ -251,3 +276,15 @@ def test_tvd_filter_stale_point_matters(oracle_lib):
     d = np.abs(ob.q[0][0][sl] - o2.q[0][0][sl])
     assert d[:, :, 0].max() > 1e-8          # x = 0 plane: different
     assert d[2:, 2:, 2:].max() < 1e-13      # away from the low planes: the same
+
+
+def test_host_metrics_match_reference_3d():
+    """The 3D metric arrays from 4th-order central differences of the coordinates
+    (problems.metrics_central4: J, then its inverse) against the reference solver's own
+    (adj(J) / det J in its generated operation order): equal to rounding, 1e-13 relative."""
+    spec, _, met, _ = problems.curvilinear_wave_3d((16, 12, 10))
+    ref = reference_metrics(spec)
+    sl = spec.interior()
+    for k in range(10):
+        scale = float(np.max(np.abs(ref[k][sl])))
+        assert float(np.max(np.abs(met[k][sl] - ref[k][sl]))) < 1e-13 * scale, k
