@@ -79,7 +79,7 @@ def _const_value(name, params, default=None):
 
 def _flux_of(block):
     """OSB_FLUX_* of the block's shock-capturing scheme: LLF for LFWeno / LFTeno, HLLC-LM for
-    HLLCWeno with flux_type 'HLLC-LM' (restated in the oracle; the GPU path refuses it)."""
+    HLLCWeno with flux_type 'HLLC-LM' (Cartesian 2D / 3D blocks)."""
     from opensbli.schemes.spatial.weno import HLLCWeno
     for sch in block.discretisation_schemes.values():
         if isinstance(sch, HLLCWeno):
@@ -600,6 +600,7 @@ class GB300Backend:
         self.solver = None
         self.metrics = None
         self.iteration = 0
+        self.simulation_time = 0.0
         self._plan = None
 
     @classmethod
@@ -623,6 +624,7 @@ class GB300Backend:
         be.solver = None
         be.metrics = None
         be.iteration = 0
+        be.simulation_time = 0.0
         be._plan = plan
         return be
 
@@ -635,10 +637,12 @@ class GB300Backend:
             self._plan = BackendPlan(self.specs, states, coords, self.rk, self.dt, self.niter, self.precision)
         return self._plan
 
-    def initialise(self, states=None):
+    def initialise(self, states=None, restart=None):
         """Upload the initial state (default: the scripts' GridBasedInitialisation evaluated on the
         host), compute the metric arrays of curvilinear blocks on the GPU, and apply the boundary
-        conditions once, as the generated code does before its time loop."""
+        conditions once, as the generated code does before its time loop.  restart: a file
+        written by save(); its state, RK register, iteration and simulation time replace the
+        initialisation (the generated code's restart == 1 branch, opsc.py:962-977)."""
         from .solver import Solver, device_metrics
         plan = self.plan()
         if states is None:
@@ -651,8 +655,14 @@ class GB300Backend:
                                 device_metrics(spec, x, fill=abi.METRIC_PERIODIC, device=self.device))
         items = [(s, q) if m is None else (s, q, m) for s, q, m in zip(self.specs, states, self.metrics)]
         self.solver = Solver(items, precision=self.precision, rk=self.rk, device=self.device, graphs=self.graphs)
+        if restart is not None:
+            self.iteration, self.simulation_time = self.solver.load_restart(restart)
         self.solver.apply_bc()
         return self
+
+    def save(self, path):
+        """Write a restart file (state, RK register, iteration, simulation time of every block)."""
+        self.solver.save_restart(path, self.iteration, self.simulation_time)
 
     def run(self, niter=None, dt=None):
         niter = self.niter if niter is None else niter
@@ -661,6 +671,7 @@ class GB300Backend:
             raise ValueError("niter and dt must be given (as parameters or arguments)")
         self.solver.step(dt, niter)
         self.iteration += niter
+        self.simulation_time += niter * dt
         self.solver.sync()
         return self
 

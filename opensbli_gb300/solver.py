@@ -148,6 +148,29 @@ class Solver:
         abi.check(self.lib, self.lib.osb_step_requests(self.ctx, n, ins, outs, float(dt), int(nsteps)),
                   "osb_step_requests")
 
+    # -- checkpoint / restart (restart.py: the reference's restart content, .npz layout) ---
+    def save_restart(self, path, iteration, simulation_time):
+        """Write every block's FP64 state and RK register (whole allocations) with the
+        iteration count and simulation time."""
+        from . import restart
+        self.sync()
+        restart.write(path, self.specs, [[a.cpu().numpy() for a in q] for q in self.q],
+                      [[a.cpu().numpy() for a in r] for r in self.rk], iteration, simulation_time)
+
+    def load_restart(self, path):
+        """Load state and RK register of every block from a restart file written for the same
+        blocks; returns (iteration, simulation_time).  The next step continues exactly as the
+        run that wrote the file."""
+        from . import restart
+        data = restart.read(path)
+        restart.check_compatible(self.specs, data)
+        self.sync()
+        for q, r, blk in zip(self.q, self.rk, data["blocks"]):
+            q.copy_(self.torch.from_numpy(np.ascontiguousarray(np.stack(blk["state"]))))
+            r.copy_(self.torch.from_numpy(np.ascontiguousarray(np.stack(blk["register"]))))
+        self.torch.cuda.synchronize(self.device)
+        return data["iter"], data["simulation_time"]
+
     def stage(self, s, dt):
         abi.check(self.lib, self.lib.osb_stage(self.ctx, int(s), float(dt)), "osb_stage")
 
