@@ -67,8 +67,9 @@ extern "C" {
                                 inside, normal momentum negated; the boundary plane unchanged */
 #define OSB_BC_DIRICHLET 6   /* DirichletBC (dirichlet.py:27-41): the boundary plane and its halo
                                 layers set from osb_block_desc.dirichlet */
-#define OSB_BC_PRESSURE_OUTLET 7 /* PressureOutletBC (pressure_outlet.py:35-51): restated in the
-                                oracle; the GPU path refuses it (OSB_EINVAL) */
+#define OSB_BC_PRESSURE_OUTLET 7 /* PressureOutletBC (pressure_outlet.py:35-51), Cartesian: the
+                                boundary plane and its halo layers take rho and momentum of the
+                                point inside, rhoE from osb_block_desc.back_pressure */
 
 /* Convective split form of OSB_SCHEME_CENTRAL4 (physical_models/split_forms.py). */
 #define OSB_SPLIT_FEIEREISEN 0 /* skew-symmetric form, split_forms.py:111-145 */
@@ -83,7 +84,7 @@ extern "C" {
 /* Riemann flux of the characteristic WENO / TENO reconstruction (shock_capturing.py). */
 #define OSB_FLUX_LLF 0         /* flux-split local Lax-Friedrichs (LFWeno / LFTeno) */
 #define OSB_FLUX_HLLC_LM 1     /* HLLC-LM from reconstructed states (HLLCWeno, lines 1031-1256):
-                                  restated in the oracle; the GPU path rejects it (OSB_ENOTSUP) */
+                                  Cartesian 2D / 3D blocks, WENO5-JS / WENO5-Z / TENO5 */
 
 /* Residual precision (per context). */
 #define OSB_PREC_FP64 0          /* plain FP64 path, parity with the generated solver */

@@ -226,8 +226,8 @@ bool batch_eligible(const osb_ctx* c, std::string* why) {
   for (const auto& bl : c->blocks) {
     if (bl.d.ndim != 2) return no("the persistent stage takes 2D blocks");
     if (bl.k.m[9]) return no("the persistent stage takes Cartesian blocks");
-    if (bl.d.scheme == OSB_SCHEME_CENTRAL4 || bl.d.viscous != OSB_VISC_NONE)
-      return no("the persistent stage takes the characteristic Euler flux");
+    if (bl.d.scheme == OSB_SCHEME_CENTRAL4 || bl.d.viscous != OSB_VISC_NONE || bl.d.flux_type != OSB_FLUX_LLF)
+      return no("the persistent stage takes the characteristic LLF Euler flux");
     for (int d = 0; d < 2; ++d)
       if (bl.d.bc[d][0] != OSB_BC_PERIODIC || bl.d.bc[d][1] != OSB_BC_PERIODIC)
         return no("the persistent stage takes fully periodic blocks");

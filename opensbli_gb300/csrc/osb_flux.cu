@@ -22,9 +22,9 @@ namespace {
 // One y or z sweep over `lines` lines of N interfaces: the lines are cut into segments so the
 // CTAs fill the resident slots in nearly whole waves (a segment costs one extra interface and
 // the start of its 6-point window, about 1.5 interfaces).
-template <typename T, int ND, int D, int SCH, int AVG, bool CURV, bool FUSE>
+template <typename T, int ND, int D, int SCH, int AVG, bool CURV, bool FUSE, int FLX>
 int launch_sweep_k(osb_ctx* c, const BlockK& k, const SchemeParams& sp, int N, int other, const RkFuse& rf) {
-  auto kern = k_flux_sweep<T, ND, D, SCH, AVG, CURV, FUSE>;
+  auto kern = k_flux_sweep<T, ND, D, SCH, AVG, CURV, FUSE, FLX>;
   const long slots = (long)resident_ctas(kern, SWEEP_THREADS, 0) * c->sm_count;
   const long gx = (k.n[0] + SWEEP_THREADS - 1) / SWEEP_THREADS;
   int nseg = wave_chunks(N, gx * other, slots, 1.5, 8);
@@ -37,17 +37,17 @@ int launch_sweep_k(osb_ctx* c, const BlockK& k, const SchemeParams& sp, int N, i
   return OSB_OK;
 }
 
-template <typename T, int ND, int D, int SCH, int AVG, bool CURV>
+template <typename T, int ND, int D, int SCH, int AVG, bool CURV, int FLX>
 int launch_sweep(osb_ctx* c, const BlockK& k, const SchemeParams& sp, int N, int other, const RkFuse* rf) {
-  if constexpr (sizeof(T) == 4) {
-    if (rf) return launch_sweep_k<T, ND, D, SCH, AVG, CURV, true>(c, k, sp, N, other, *rf);
+  if constexpr (sizeof(T) == 4 && FLX == 0) {
+    if (rf) return launch_sweep_k<T, ND, D, SCH, AVG, CURV, true, FLX>(c, k, sp, N, other, *rf);
   }
-  return launch_sweep_k<T, ND, D, SCH, AVG, CURV, false>(c, k, sp, N, other, RkFuse{});
+  return launch_sweep_k<T, ND, D, SCH, AVG, CURV, false, FLX>(c, k, sp, N, other, RkFuse{});
 }
 
 // x sweep (writes R), then y[, z] sweeps (accumulate); with rf (FP32 path, 2D/3D) the last
 // sweep applies the RK update instead of storing the residual.
-template <typename T, int ND, int SCH, int AVG, bool CURV>
+template <typename T, int ND, int SCH, int AVG, bool CURV, int FLX = 0>
 int launch_flux(osb_ctx* c, Block& bl, const SchemeParams& sp, const RkFuse* rf) {
   BlockK& k = bl.k;
   cudaStream_t st = c->stream;
@@ -55,7 +55,7 @@ int launch_flux(osb_ctx* c, Block& bl, const SchemeParams& sp, const RkFuse* rf)
   {
     constexpr int NF = SweepFields<ND, CURV>::N;
     const size_t smem = (size_t)XWARPS * sizeof(XTile<T, NF, CURV ? ND + 3 : ND + 2>);
-    auto kern = k_flux_x<T, ND, SCH, AVG, CURV>;
+    auto kern = k_flux_x<T, ND, SCH, AVG, CURV, FLX>;
     OSB_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int nrows = k.n[1] * k.n[2];
     const long gy = (nrows + 32 * XWARPS - 1) / (32 * XWARPS);
@@ -87,8 +87,8 @@ int launch_flux(osb_ctx* c, Block& bl, const SchemeParams& sp, const RkFuse* rf)
     timing_begin(c, D == 1 ? FAM_FLUX_Y : FAM_FLUX_Z);
     const RkFuse* f = D == ND - 1 ? rf : nullptr;
     int rc = OSB_OK;
-    if (D == 1) rc = launch_sweep<T, ND, 1, SCH, AVG, CURV>(c, k, sp, N, other, f);
-    else if (ND == 3) rc = launch_sweep<T, ND, (ND == 3 ? 2 : 1), SCH, AVG, CURV>(c, k, sp, N, other, f);
+    if (D == 1) rc = launch_sweep<T, ND, 1, SCH, AVG, CURV, FLX>(c, k, sp, N, other, f);
+    else if (ND == 3) rc = launch_sweep<T, ND, (ND == 3 ? 2 : 1), SCH, AVG, CURV, FLX>(c, k, sp, N, other, f);
     timing_end(c);
     if (rc != OSB_OK) return rc;
     c->launches++;
@@ -96,9 +96,30 @@ int launch_flux(osb_ctx* c, Block& bl, const SchemeParams& sp, const RkFuse* rf)
   return OSB_OK;
 }
 
+// HLLC-LM flux (Cartesian 2D / 3D blocks, fifth-order reconstructions): the sweeps do not carry
+// the RK update for it
+template <typename T, int ND>
+int dispatch_hllc(osb_ctx* c, Block& bl, const SchemeParams& sp) {
+  const int sch = bl.d.scheme, avg = bl.d.averaging;
+  if (avg == OSB_AVG_ROE) {
+    if (sch == OSB_SCHEME_WENO5_JS) return launch_flux<T, ND, SCH_WENO5_JS, AVG_ROE, false, 1>(c, bl, sp, nullptr);
+    if (sch == OSB_SCHEME_WENO5_Z) return launch_flux<T, ND, SCH_WENO5_Z, AVG_ROE, false, 1>(c, bl, sp, nullptr);
+    if (sch == OSB_SCHEME_TENO5) return launch_flux<T, ND, SCH_TENO5, AVG_ROE, false, 1>(c, bl, sp, nullptr);
+  } else {
+    if (sch == OSB_SCHEME_WENO5_JS) return launch_flux<T, ND, SCH_WENO5_JS, AVG_SIMPLE, false, 1>(c, bl, sp, nullptr);
+    if (sch == OSB_SCHEME_WENO5_Z) return launch_flux<T, ND, SCH_WENO5_Z, AVG_SIMPLE, false, 1>(c, bl, sp, nullptr);
+    if (sch == OSB_SCHEME_TENO5) return launch_flux<T, ND, SCH_TENO5, AVG_SIMPLE, false, 1>(c, bl, sp, nullptr);
+  }
+  return fail(OSB_ENOTSUP, "the HLLC-LM flux takes the fifth-order WENO / TENO reconstructions");
+}
+
 template <typename T, int ND, bool CURV>
 int dispatch_flux_nd(osb_ctx* c, Block& bl, const SchemeParams& sp, const RkFuse* rf) {
   const int sch = bl.d.scheme, avg = bl.d.averaging;
+  if (bl.d.flux_type == OSB_FLUX_HLLC_LM) {
+    if constexpr (!CURV && ND >= 2) return dispatch_hllc<T, ND>(c, bl, sp);
+    return fail(OSB_ENOTSUP, "the HLLC-LM flux is implemented for Cartesian 2D and 3D blocks");
+  }
   if (avg == OSB_AVG_ROE) {
     if (sch == OSB_SCHEME_WENO5_JS) return launch_flux<T, ND, SCH_WENO5_JS, AVG_ROE, CURV>(c, bl, sp, rf);
     if (sch == OSB_SCHEME_WENO5_Z) return launch_flux<T, ND, SCH_WENO5_Z, AVG_ROE, CURV>(c, bl, sp, rf);

@@ -345,6 +345,55 @@ __global__ void k_symmetry(BlockK b, int nv, int d, int side, int depth, int hal
   }
 }
 
+// Pressure outlet (pressure_outlet.py:35-51 as generated): the boundary plane and its `depth`
+// halo layers take the density and momentum of the point one inside the plane, and the total
+// energy pback / (gama - 1) + (sum_i 1/2 m_i^2) / rho of that point, over the whole transverse
+// allocation; the generated operation order, rounded operation by operation.  The FP32 copy
+// (between stages of the FP32-residual path) is formed the same way from the FP32 neighbour.
+__device__ __forceinline__ double pout_energy(double pback, double gama, const double* m, int nd, double rho) {
+  double ke = __dmul_rn(0.5, __dmul_rn(m[0], m[0]));
+  for (int i = 1; i < nd; ++i) ke = __dadd_rn(ke, __dmul_rn(0.5, __dmul_rn(m[i], m[i])));
+  return __dadd_rn(__ddiv_rn(pback, __dadd_rn(-1.0, gama)), __ddiv_rn(ke, rho));
+}
+__global__ void k_pressure_outlet(BlockK b, int nv, int d, int side, int depth, int halo, double pback, double gama,
+                                  int fields) {
+  const int total = face_extent(b, d, halo);
+  const int base = side == 0 ? 0 : b.n[d] - 1;
+  const int o = b.st[d] * (side == 0 ? -1 : 1);
+  const int nd = nv - 2;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+    int c[3];
+    face_point(b, d, halo, t, c);
+    c[d] = base;
+    const int id = lin(b, c[0], c[1], c[2]);
+    const int in = id - o;
+    if (fields & BC_Q) {
+      double m[3];
+      for (int i = 0; i < nd; ++i) m[i] = b.q[1 + i][in];
+      const double rho = b.q[0][in];
+      const double E = pout_energy(pback, gama, m, nd, rho);
+      for (int k = 0; k <= depth; ++k) {
+        const int p = id + k * o;
+        b.q[0][p] = rho;
+        for (int i = 0; i < nd; ++i) b.q[1 + i][p] = m[i];
+        b.q[nv - 1][p] = E;
+      }
+    }
+    if ((fields & BC_QF) && b.qf[0]) {
+      double m[3];
+      for (int i = 0; i < nd; ++i) m[i] = f2d_exact(b.qf[1 + i][in]);
+      const float rho = b.qf[0][in];
+      const float E = d2f_rn(pout_energy(pback, gama, m, nd, f2d_exact(rho)));
+      for (int k = 0; k <= depth; ++k) {
+        const int p = id + k * o;
+        b.qf[0][p] = rho;
+        for (int i = 0; i < nd; ++i) b.qf[1 + i][p] = b.qf[1 + i][in];
+        b.qf[nv - 1][p] = E;
+      }
+    }
+  }
+}
+
 // Dirichlet face (dirichlet.py:27-41): the boundary plane and its `depth` halo layers take the
 // values of the BC's equations, vals[v][layer][t] (layer l at -depth + l on side 0, N-1 + l on
 // side 1), over the whole transverse allocation.
@@ -738,6 +787,13 @@ int apply_block_bc(osb_ctx* c, Block& bl, size_t ib, int fields) {
                                                                  bl.d.dirichlet[d][side], fields);
         timing_end(c);
         c->launches++;
+      } else if (kind == OSB_BC_PRESSURE_OUTLET) {
+        const long tr = face_extent(bl.k, d, bl.d.halo);
+        timing_begin(c, FAM_BC);
+        k_pressure_outlet<<<grid_for(c, tr, 128), 128, 0, c->stream>>>(
+            bl.k, nv, d, side, side ? dep1 : dep0, bl.d.halo, bl.d.back_pressure[d][side], bl.d.gama, fields);
+        timing_end(c);
+        c->launches++;
       } else if (kind == OSB_BC_PERIODIC) {
         return fail(OSB_EINVAL, "periodic boundary on one side only (block %zu dir %d)", ib, d);
       }
@@ -928,18 +984,19 @@ bool check_desc(const osb_block_desc* d, std::string& why) {
   for (int i = 0; i < d->ndim; ++i)
     for (int s = 0; s < 2; ++s) {
       const int k = d->bc[i][s];
-      if (k == OSB_BC_PRESSURE_OUTLET) {
-        why = "the pressure outlet is restated in the oracle only; the GPU path has no kernel for it";
-        return false;
-      }
-      if (k < OSB_BC_PERIODIC || k > OSB_BC_DIRICHLET) { why = "unknown boundary kind"; return false; }
+      if (k < OSB_BC_PERIODIC || k > OSB_BC_PRESSURE_OUTLET) { why = "unknown boundary kind"; return false; }
       const int dep = d->bc_depth[i][s] > 0 ? d->bc_depth[i][s] : 4;
-      if ((k == OSB_BC_SYMMETRY || k == OSB_BC_DIRICHLET) && (dep > d->halo || dep >= d->size[i])) {
-        why = "symmetry / Dirichlet depth must be below the halo and the block size";
+      if ((k == OSB_BC_SYMMETRY || k == OSB_BC_DIRICHLET || k == OSB_BC_PRESSURE_OUTLET) &&
+          (dep > d->halo || dep >= d->size[i])) {
+        why = "symmetry / Dirichlet / pressure-outlet depth must be below the halo and the block size";
         return false;
       }
-      if (k == OSB_BC_SYMMETRY && d->metric[9]) {
-        why = "the symmetry boundary is implemented for Cartesian blocks";
+      if ((k == OSB_BC_SYMMETRY || k == OSB_BC_PRESSURE_OUTLET) && d->metric[9]) {
+        why = "the symmetry and pressure-outlet boundaries are implemented for Cartesian blocks";
+        return false;
+      }
+      if (k == OSB_BC_PRESSURE_OUTLET && !(d->back_pressure[i][s] > 0.0)) {
+        why = "a pressure outlet needs a positive back pressure";
         return false;
       }
       if (k == OSB_BC_DIRICHLET && !d->dirichlet[i][s]) {
@@ -962,11 +1019,13 @@ bool check_desc(const osb_block_desc* d, std::string& why) {
       }
       if (f.side != 0 && f.side != 1) { why = "interface side must be 0 or 1"; return false; }
     }
-  if (d->flux_type == OSB_FLUX_HLLC_LM) {
-    why = "the HLLC-LM flux is restated in the oracle only; the GPU sweeps implement the LLF flux";
+  if (d->flux_type == OSB_FLUX_HLLC_LM &&
+      (d->ndim < 2 || curv || !(d->scheme == OSB_SCHEME_WENO5_JS || d->scheme == OSB_SCHEME_WENO5_Z ||
+                                d->scheme == OSB_SCHEME_TENO5))) {
+    why = "the HLLC-LM flux is implemented for Cartesian 2D / 3D blocks with WENO5-JS, WENO5-Z or TENO5";
     return false;
   }
-  if (d->flux_type != OSB_FLUX_LLF) { why = "unknown flux type"; return false; }
+  if (d->flux_type != OSB_FLUX_LLF && d->flux_type != OSB_FLUX_HLLC_LM) { why = "unknown flux type"; return false; }
   if (d->split_form != OSB_SPLIT_FEIEREISEN && d->split_form != OSB_SPLIT_KGP) { why = "unknown split form"; return false; }
   if (d->split_form == OSB_SPLIT_KGP && d->scheme != OSB_SCHEME_CENTRAL4) {
     why = "the KGP split form belongs to the central scheme";

@@ -332,7 +332,7 @@ constexpr int SWEEP_THREADS = 128, SWEEP_RING = 3;
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
 
-template <typename T, int ND, int D, int SCH, int AVG, bool CURV, bool FUSE>
+template <typename T, int ND, int D, int SCH, int AVG, bool CURV, bool FUSE, int FLX = 0>
 __global__ void __launch_bounds__(SWEEP_THREADS, sizeof(T) == 4 ? 4 : 1)
     k_flux_sweep(BlockK b, SchemeParams spd, int seg, int nseg, int first, RkFuse rf) {
   constexpr int NV = ND + 2;
@@ -428,7 +428,7 @@ __global__ void __launch_bounds__(SWEEP_THREADS, sizeof(T) == 4 ? 4 : 1)
       char_flux_curv<T, ND, SCH, AVG>(w, sp, fh);
       sc = invd / w[2].J;
     } else {
-      char_flux<T, ND, SCH, AVG>(w, sp, fh);
+      cart_flux<T, ND, SCH, AVG, FLX>(w, sp, fh);
     }
     if (j >= j0) {
       if constexpr (FUSE) {
@@ -474,7 +474,7 @@ struct XTile {
   int rowbase[32];
 };
 
-template <typename T, int ND, int SCH, int AVG, bool CURV>
+template <typename T, int ND, int SCH, int AVG, bool CURV, int FLX = 0>
 __global__ void __launch_bounds__(32 * XWARPS) k_flux_x(BlockK b, SchemeParams spd, int first, int xseg,
                                                          const int* __restrict__ xrows) {
   constexpr int NV = ND + 2;
@@ -585,7 +585,7 @@ __global__ void __launch_bounds__(32 * XWARPS) k_flux_x(BlockK b, SchemeParams s
     if constexpr (CURV) {
       char_flux_curv<T, ND, SCH, AVG>(w, sp, fh);
     } else {
-      char_flux<T, ND, SCH, AVG>(w, sp, fh);
+      cart_flux<T, ND, SCH, AVG, FLX>(w, sp, fh);
     }
     // interface j + 1/2 is the right face of point j: out column (j - o0) % XOUT + 1; the face
     // left of the segment lands in the column left of point s0 (the carry column when the

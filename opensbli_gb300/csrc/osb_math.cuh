@@ -416,6 +416,164 @@ __device__ __forceinline__ void char_flux(const Pt<T, ND> (&w)[6], const SP<T>& 
   }
 }
 
+// HLLC-LM flux at the interface between w[2] and w[3] of a 6-point window (offsets -2..+3),
+// Cartesian local frame (HLLCWeno with flux_type 'HLLC-LM', shock_capturing.py:1031-1256):
+// the averaged state and eigensystem as char_flux; the characteristic projections CS = L q of
+// the six points; per wave the scheme's fifth-order reconstruction from the left (points
+// i-2..i+2) and from the right (i+3..i-1, mirrored); back to physical left and right states with
+// the REV columns; then u, p, a of each side, the outer wave speeds sL = min(u_av - a_av,
+// uL - aL), sR = max(u_av + a_av, uR + aR), the contact speed s*, both outer speeds scaled by
+// phi = sin(pi/2 min(1, 10 M)) with M = max |u/a| of the two sides (the low-Mach correction),
+// and the flux in the generated central-plus-dissipation form.  The generated right-state
+// energy term divides pR by (sL - uR) rho_R, not (sR - uR) rho_R; this follows it.
+template <typename T>
+__device__ __forceinline__ T lm_sin(T x);
+template <>
+__device__ __forceinline__ double lm_sin<double>(double x) { return sin(x); }
+template <>
+__device__ __forceinline__ float lm_sin<float>(float x) { return sinf(x); }
+
+template <typename T, int ND, int SCH, int AVG>
+__device__ __forceinline__ void hllc_flux(const Pt<T, ND> (&w)[6], const SP<T>& sp, T (&fh)[ND + 2]) {
+  constexpr int NV = ND + 2;
+  const T g1 = sp.g1;
+  const Pt<T, ND>& L = w[2];
+  const Pt<T, ND>& R = w[3];
+  T rho, u[ND], a;
+  if (AVG == AVG_ROE) {
+    T sL = sqrt(L.q[0]), sR = sqrt(R.q[0]);
+    rho = sqrt(L.q[0] * R.q[0]);
+    T inv = L_(1.0) / (sL + sR);
+    T ke = L_(0.0);
+#pragma unroll
+    for (int i = 0; i < ND; ++i) {
+      u[i] = (sL * L.u[i] + sR * R.u[i]) * inv;
+      ke += u[i] * u[i];
+    }
+    T H = ((L.q[NV - 1] + L.p) / sL + (R.q[NV - 1] + R.p) / sR) * inv;
+    a = sqrt(g1 * (H - L_(0.5) * ke));
+  } else {
+    rho = L_(0.5) * (L.q[0] + R.q[0]);
+#pragma unroll
+    for (int i = 0; i < ND; ++i) u[i] = L_(0.5) * (L.u[i] + R.u[i]);
+    a = L_(0.5) * (L.a + R.a);
+  }
+  const T ia = L_(1.0) / a, ia2 = ia * ia, irho = L_(1.0) / rho;
+  T ke = L_(0.0);
+#pragma unroll
+  for (int i = 0; i < ND; ++i) ke += u[i] * u[i];
+  const T phi = g1 * L_(0.5) * ke;
+  const T bta = ia * irho * L_(0.70710678118654752440);
+  const T alf = rho * ia * L_(0.70710678118654752440);
+  T cs[NV][6];
+#pragma unroll
+  for (int m = 0; m < 6; ++m) {
+    const T* v = w[m].q;
+    T um = L_(0.0);
+#pragma unroll
+    for (int i = 0; i < ND; ++i) um += u[i] * v[1 + i];
+    T S = phi * v[0] - g1 * um + g1 * v[NV - 1];
+    T D = v[1] - u[0] * v[0];
+    cs[0][m] = v[0] - S * ia2;
+    if (ND == 2) {
+      cs[1][m] = (u[1] * v[0] - v[2]) * irho;
+    } else {
+      cs[1][m] = (v[3] - u[2] * v[0]) * irho;
+      cs[2][m] = (u[1] * v[0] - v[2]) * irho;
+    }
+    cs[ND][m] = bta * (S + a * D);
+    cs[ND + 1][m] = bta * (S - a * D);
+  }
+  T rl[NV], rr[NV];
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    rl[k] = recon5<T, SCH>(cs[k][0], cs[k][1], cs[k][2], cs[k][3], cs[k][4], sp);
+    rr[k] = recon5<T, SCH>(cs[k][5], cs[k][4], cs[k][3], cs[k][2], cs[k][1], sp);
+  }
+  // REV columns (k = e_0): characteristic -> conserved, both sides
+  T qL[NV], qR[NV];
+  const T h0 = (phi + a * a) / g1;
+  auto rev = [&](const T (&c)[NV], T (&o)[NV]) {
+    const T rp = c[ND] + c[ND + 1], rm = c[ND] - c[ND + 1];
+    const T F0 = c[0] + alf * rp;
+    o[0] = F0;
+    o[1] = u[0] * F0 + alf * a * rm;
+    if (ND == 2) {
+      o[2] = u[1] * F0 - rho * c[1];
+      o[3] = phi / g1 * c[0] - rho * u[1] * c[1] + alf * h0 * rp + alf * u[0] * a * rm;
+    } else {
+      o[2] = u[1] * F0 - rho * c[2];
+      o[3] = u[2] * F0 + rho * c[1];
+      o[4] = phi / g1 * c[0] + rho * u[2] * c[1] - rho * u[1] * c[2] + alf * h0 * rp + alf * u[0] * a * rm;
+    }
+  };
+  rev(rl, qL);
+  rev(rr, qR);
+  const T gm = sp.gama;
+  const T irL = L_(1.0) / qL[0], irR = L_(1.0) / qR[0];
+  T uL[ND], uR[ND], kL = L_(0.0), kR = L_(0.0);
+#pragma unroll
+  for (int i = 0; i < ND; ++i) {
+    uL[i] = irL * qL[1 + i];
+    uR[i] = irR * qR[1 + i];
+    kL += uL[i] * uL[i];
+    kR += uR[i] * uR[i];
+  }
+  const T EL = qL[NV - 1], ER = qR[NV - 1];
+  const T pL = (-L_(0.5) * kL * qL[0] + EL) * g1, pR = (-L_(0.5) * kR * qR[0] + ER) * g1;
+  const T aL = sqrt(gm * irL * pL), aR = sqrt(gm * irR * pR);
+  const T un = u[0], uLn = uL[0], uRn = uR[0];
+  T sL = fmin(-a + un, -aL + uLn), sR = fmax(a + un, aR + uRn);
+  const T ss = (-pL + (-uLn + sL) * qL[0] * uLn - (-uRn + sR) * qR[0] * uRn + pR) /
+               ((-uLn + sL) * qL[0] - (-uRn + sR) * qR[0]);
+  const T M = fmax(fabs(uLn / aL), fabs(uRn / aR));
+  const T lm = lm_sin<T>(L_(0.5) * L_(3.14159265358979323846) * fmin(L_(1.0), L_(10.0) * M));
+  sL = lm * sL;
+  sR = lm * sR;
+  const T mL = (-uLn + sL) * qL[0] / (-ss + sL), mR = (-uRn + sR) * qR[0] / (-ss + sR);
+  const T as = fabs(ss);
+  if (sL >= L_(0.0)) {
+    fh[0] = qL[1];
+#pragma unroll
+    for (int i = 0; i < ND; ++i) fh[1 + i] = i == 0 ? qL[1] * uLn + pL : qL[1 + i] * uLn;
+    fh[NV - 1] = (pL + EL) * uLn;
+  } else if (sR <= L_(0.0)) {
+    fh[0] = qR[1];
+#pragma unroll
+    for (int i = 0; i < ND; ++i) fh[1 + i] = i == 0 ? qR[1] * uRn + pR : qR[1 + i] * uRn;
+    fh[NV - 1] = (pR + ER) * uRn;
+  } else {
+    const T hf = L_(0.5);
+    fh[0] = hf * qL[1] + hf * qR[1] + hf * (-qL[0] + mL) * sL + hf * (-qR[0] + mR) * sR + hf * (mL - mR) * as;
+#pragma unroll
+    for (int i = 0; i < ND; ++i) {
+      if (i == 0) {
+        const T xL = (-uLn + sL) * qL[0] * ss / (-ss + sL), xR = (-uRn + sR) * qR[0] * ss / (-ss + sR);
+        fh[1] = hf * pL + hf * pR + hf * (-qL[1] + xL) * sL + hf * (-qR[1] + xR) * sR + hf * (xL - xR) * as +
+                hf * qL[1] * uLn + hf * qR[1] * uRn;
+      } else {
+        const T xL = (-uLn + sL) * qL[0] * uL[i] / (-ss + sL), xR = (-uRn + sR) * qR[0] * uR[i] / (-ss + sR);
+        fh[1 + i] = hf * (-qL[1 + i] + xL) * sL + hf * (-qR[1 + i] + xR) * sR + hf * (xL - xR) * as +
+                    hf * qL[1 + i] * uLn + hf * qR[1 + i] * uRn;
+      }
+    }
+    const T eL = (-uLn + sL) * ((-uLn + ss) * (pL / ((-uLn + sL) * qL[0]) + ss) + irL * EL) * qL[0] / (-ss + sL);
+    const T eR = (-uRn + sR) * ((-uRn + ss) * (pR / ((-uRn + sL) * qR[0]) + ss) + irR * ER) * qR[0] / (-ss + sR);
+    fh[NV - 1] = hf * (-EL + eL) * sL + hf * (-ER + eR) * sR + hf * (eL - eR) * as + hf * (pL + EL) * uLn +
+                 hf * (pR + ER) * uRn;
+  }
+}
+
+// Interface flux of a Cartesian sweep: characteristic LLF (FLX 0) or HLLC-LM (FLX 1).
+template <typename T, int ND, int SCH, int AVG, int FLX>
+__device__ __forceinline__ void cart_flux(const Pt<T, ND> (&w)[6], const SP<T>& sp, T (&fh)[ND + 2]) {
+  if constexpr (FLX == 1) {
+    hllc_flux<T, ND, SCH, AVG>(w, sp, fh);
+  } else {
+    char_flux<T, ND, SCH, AVG>(w, sp, fh);
+  }
+}
+
 // ---------------------------------------------------------------------------------------
 // Curvilinear sweeps work in the global frame.  A point carries its conserved state and
 // primitives plus the metric row of the sweep direction d, k_i = D_di = d xi_d / d x_i, and

@@ -223,8 +223,10 @@ bool resident_eligible(const osb_ctx* c) {
     if (d.scheme != f.scheme || d.averaging != f.averaging) return false;
     if (bl.k.alloc > RESIDENT_MAX_E) return false;
     for (int s = 0; s < 2; ++s)
-      if (d.bc[0][s] == OSB_BC_INTERFACE || d.bc[0][s] == OSB_BC_SYMMETRY || d.bc[0][s] == OSB_BC_DIRICHLET)
+      if (d.bc[0][s] == OSB_BC_INTERFACE || d.bc[0][s] == OSB_BC_SYMMETRY || d.bc[0][s] == OSB_BC_DIRICHLET ||
+          d.bc[0][s] == OSB_BC_PRESSURE_OUTLET)
         return false;
+    if (d.flux_type != OSB_FLUX_LLF) return false;
     if ((d.bc[0][0] == OSB_BC_PERIODIC) != (d.bc[0][1] == OSB_BC_PERIODIC)) return false;
   }
   return true;

@@ -319,7 +319,7 @@ def shock_reflection(n0=457, n1=255, sizes=None, flux_type=abi.FLUX_LLF, back_pr
     -0.052106102140246795, p 0.211869) from x = 40 and the free stream (p 0.178571) before it --
     values, literals and operation order of the generated boundary and initialisation kernels.
     flux_type = abi.FLUX_HLLC_LM selects the app's own HLLC-LM flux, back_pressure a
-    PressureOutletBC in place of the extrapolation outlet (both oracle only)."""
+    PressureOutletBC in place of the extrapolation outlet."""
     if sizes is not None:
         n0, n1 = sizes
     gama, minf = 1.4, 2.0

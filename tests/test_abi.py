@@ -58,24 +58,27 @@ def test_new_entry_points_reject_bad_arguments_without_a_gpu(built_lib):
     assert lib.osb_step_requests(None, 1, None, None, 1e-3, 1) == abi.OSB_EINVAL
 
 
-def test_hllc_descriptor_refused_by_the_gpu_path(built_lib):
-    """The HLLC-LM flux is restated in the oracle (pinned to the reference's generated solver);
-    the GPU path refuses such a block loudly instead of running the LLF flux in its place."""
+def test_hllc_descriptor_outside_the_gpu_flux_refused(built_lib):
+    """The GPU HLLC-LM flux covers Cartesian 2D / 3D blocks with the fifth-order WENO / TENO
+    reconstructions; any other combination (here TENO6) is refused loudly, before any device
+    work, instead of running the LLF flux in its place."""
     from opensbli_gb300 import problems
     lib = abi.load_library()
     spec, _ = problems.shock_reflection(40, 20, flux_type=abi.FLUX_HLLC_LM)
+    spec.scheme = abi.SCHEME_TENO6
     d = abi.make_desc(spec, [1] * 4, [1] * 4, None, {(0, 0): 1, (1, 1): 1})
     assert lib.osb_stage_noalloc(ctypes.byref(d), abi.RK_LOW_STORAGE, 0.0, 0.5, 0.1, None) == abi.OSB_EINVAL
     assert "HLLC" in abi.last_error(lib)
 
 
-def test_pressure_outlet_refused_by_the_gpu_path(built_lib):
-    """The pressure outlet is restated in the oracle (pinned to the reference's generated
-    solver); the GPU path refuses the face instead of leaving its halos unset."""
+def test_pressure_outlet_without_back_pressure_refused(built_lib):
+    """A pressure-outlet face needs its back pressure (osb_block_desc.back_pressure); a face left
+    at zero is refused before any device work."""
     from opensbli_gb300 import problems
     lib = abi.load_library()
     spec, _ = problems.shock_reflection(40, 20, back_pressure=0.2)
     d = abi.make_desc(spec, [1] * 4, [1] * 4, None, {(0, 0): 1, (1, 1): 1})
     assert d.back_pressure[0][1] == 0.2
+    d.back_pressure[0][1] = 0.0
     assert lib.osb_stage_noalloc(ctypes.byref(d), abi.RK_LOW_STORAGE, 0.0, 0.5, 0.1, None) == abi.OSB_EINVAL
-    assert "pressure outlet" in abi.last_error(lib)
+    assert "back pressure" in abi.last_error(lib)

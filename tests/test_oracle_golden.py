@@ -51,10 +51,10 @@ CASES = {
     # Dirichlet inlet and top (post-shock state from x = 40), extrapolation outlet, symmetry wall
     "shock_reflection_64x32_perturbed": (lambda: problems.shock_reflection(64, 32), "ls3", (1e-2, 4), 1e-12),
     "shock_reflection_ssp_64x32_perturbed": (lambda: problems.shock_reflection(64, 32), "ssp3", (1e-2, 4), 1e-12),
-    # HLLC-LM flux from WENO5-Z reconstructed states (restated in the oracle; not on the GPU yet)
+    # HLLC-LM flux from WENO5-Z reconstructed states (the app's own flux)
     "shock_reflection_hllc_64x32_perturbed": (lambda: problems.shock_reflection(64, 32, flux_type=abi.FLUX_HLLC_LM),
                                               "ssp3", (1e-2, 4), 1e-12),
-    # pressure outlet (restated in the oracle; not on the GPU yet)
+    # pressure outlet (back pressure 0.2) in place of the extrapolation outlet
     "shock_reflection_pout_64x32_perturbed": (lambda: problems.shock_reflection(64, 32, back_pressure=0.2), "ls3",
                                               (1e-2, 4), 1e-12),
 }
