@@ -33,6 +33,19 @@ NS = 256
 MINF = 1.25
 CFL = 0.5
 BYTES_PER_PT_STAGE = 160.0  # fully fused algorithmic traffic: q and RKold read+written once, FP64
+# FP32-residual vs FP64 after the configuration's own 1000 steps (256^3, CFL 0.5), measured by
+# `python -m opensbli_gb300.accuracy --size 256 --steps 1000` (profiles/accuracy_tgv256_fp32_vs_fp64.md);
+# too long (about 9 minutes of FP64 steps) to repeat inside the bench
+ACCURACY_1000 = {
+    "source": "profiles/accuracy_tgv256_fp32_vs_fp64.md (python -m opensbli_gb300.accuracy --size 256 --steps 1000)",
+    "teno5_roe": {"rho": {"rel_l2": 1.16e-4, "rel_linf": 1.03e-2}, "rhoE": {"rel_l2": 1.41e-4, "rel_linf": 6.73e-3},
+                  "ke_max_rel_dev": 1.61e-6,
+                  "fp64_with_1e-8_input_perturbation": {"rho_rel_l2": 1.10e-4, "rhoE_rel_l2": 1.33e-4}},
+    "weno5z_simple": {"rho": {"rel_l2": 3.53e-7, "rel_linf": 9.58e-6},
+                      "rhoE": {"rel_l2": 1.69e-6, "rel_linf": 1.44e-5}, "ke_max_rel_dev": 1.71e-6},
+    "target_rel_l2": 1e-5,
+    "target_met": {"teno5_roe": False, "weno5z_simple": True},
+}
 
 
 def parse():
@@ -172,16 +185,26 @@ def make_problem(n):
     return spec, q, dt
 
 
-def kernel_bytes(fused):
-    """Algorithmic bytes per point of one launch of each FP32-path kernel of the 3D block: its
-    own minimal inputs and outputs (FP32 state 5 x 4 B, float-float residual 5 x 8 B, FP64
-    state and RK register 5 x 8 B each)."""
-    return {"flux_x": 20.0 + 40.0,                 # read FP32 state, write residual
-            "flux_y": 20.0 + 80.0,                 # read FP32 state, read + write residual
-            "flux_z": 20.0 + 80.0,
-            "central": (20.0 + 40.0 + 160.0 + 20.0) if fused else (20.0 + 80.0),
-            "rk_update": 40.0 + 160.0 + 20.0,      # residual, state + register read/write, FP32 out
-            "boundary": 0.0, "reduce": 40.0, "persistent_stage": 0.0}
+def kernel_bytes(fused, nv=5, ndim=3, curvilinear=False, a_zero_stages=1, nstages=3, central_only=False):
+    """Algorithmic bytes per point of one launch of each FP32-path kernel, averaged over the
+    stages of a step: its own minimal inputs and outputs (FP32 state nv x 4 B, float-float
+    residual nv x 8 B, FP64 state and RK register nv x 8 B each; a curvilinear sweep also reads
+    its metric row and det J in FP32, (ndim + 1) x 4 B).  The first low-storage stage (A = 0)
+    does not read the register: a_zero_stages of the nstages read nv x 8 B less.  central_only:
+    the central kernel is the block's only residual kernel (central scheme), so it reads no
+    partial residual."""
+    st = 4.0 * nv
+    res = 8.0 * nv
+    met = 4.0 * (ndim + 1) if curvilinear else 0.0
+    reg_read = 8.0 * nv * (nstages - a_zero_stages) / nstages
+    upd = 8.0 * nv + reg_read + 16.0 * nv + st  # state read, register read, both written, FP32 out
+    return {"flux_x": st + met + res,              # read FP32 state, write residual
+            "flux_y": st + met + 2 * res,          # read FP32 state, read + write residual
+            "flux_z": st + met + 2 * res,
+            "central": (st + (0.0 if central_only else res) + upd) if fused else
+                       (st + (res if central_only else 2 * res)),
+            "rk_update": res + upd,                # residual in, the update's arrays
+            "boundary": 0.0, "reduce": 8.0 * nv, "persistent_stage": 0.0}
 
 
 def time_steps(solver, dt, steps):
@@ -234,8 +257,8 @@ def cpu_reference_rate(case, env, points, stages, what):
 
 
 def cpu_port_rate(spec_q, dt, steps, what):
-    """The oracle (the C restatement, one host core, -O2) on a bounded sample: Mpt-RK-stage/s
-    over `steps` whole steps of the block (spec, q)."""
+    """The oracle (the C restatement, -O2, OpenMP over its per-point loops) on a bounded sample:
+    Mpt-RK-stage/s over `steps` whole steps of the block (spec, q)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import harness
     from opensbli_gb300 import abi, problems
@@ -245,9 +268,11 @@ def cpu_port_rate(spec_q, dt, steps, what):
     t0 = time.perf_counter()
     ob.step(abi.RK_LOW_STORAGE, problems.RK3_LS_A, problems.RK3_LS_B, dt, steps)
     secs = time.perf_counter() - t0
-    return {"value": spec.npoints * 3 * steps / secs / 1e6, "unit": UNIT, "cores": 1, "kind": "port",
+    return {"value": spec.npoints * 3 * steps / secs / 1e6, "unit": UNIT, "cores": os.cpu_count() or 1,
+            "kind": "port",
             "sample": "%d whole steps (3 RK stages + filter) of %s with the oracle (C restatement of the "
-                      "reference path, one core)" % (steps, what)}
+                      "reference path; its residual and update loops on all host cores with OpenMP, the filter "
+                      "serial)" % (steps, what)}
 
 
 def reference_arm(args):
@@ -338,7 +363,8 @@ def our_arm(args):
     dom = max(rep, key=lambda k: rep[k][0])
     dom_ms = rep[dom][0] / max(rep[dom][1], 1)
     fused = rep["rk_update"][1] == 0
-    alg_bytes = kernel_bytes(fused)[dom] * pts
+    alg_bytes_pt = kernel_bytes(fused)[dom]
+    alg_bytes = alg_bytes_pt * pts
     hbm, peak_kind = measured_peaks()
     achieved = alg_bytes / (dom_ms * 1e-3) / 1e9
     step_bytes_gbs = BYTES_PER_PT_STAGE * pts * 3 * args.steps / secs / 1e9
@@ -459,12 +485,17 @@ def our_arm(args):
             "fp64": {"value": fp64, "unit": UNIT,
                      "fp32_over_fp64": (value / world / fp64) if fp64 else None},
             "error_vs_fp64": err,
+            "error_vs_fp64_1000_steps": ACCURACY_1000,
             "clocks": clk,
             "gpu_launches": launches,
             "schedule": sched,
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
                          "per_launch_ms": dom_ms, "share": rep[dom][0] / tot,
+                         "algorithmic_bytes_per_point": alg_bytes_pt,
+                         "traffic_source": "constant: DRAM bytes per point of this kernel from the ncu capture in "
+                                           "profiles/dram_traffic_tgv_fp32.txt, times the points; not measured "
+                                           "in this run",
                          "note": "the reconstruction sweeps are FP32-pipe bound; compute roof below"},
             "compute": {"fp32_peak_tflops": fp32_peak, "fp64_peak_tflops": fp64_peak},
             "step_hbm_gbs_at_160B": step_bytes_gbs,
@@ -568,10 +599,10 @@ def secondary_arm(args):
         rk = "ls3"
         work = ("4-block 3D curvilinear Euler (512x256x32, 384x256x32, 512x192x32, 256x256x32), TENO5 (Roe), "
                 "interfaces + periodic, Mach 0.7 + Gaussian pulse, RK-LS3, CFL %.1f" % CFL)
-        bytes_pt = 4 * 5 * 8
-        cpu_args = ("curv_weno5z", {"OSB_NP0": 1024, "OSB_NP1": 1024}, 1024 ** 2, 12,
-                    "the reference's 2D curvilinear WENO5-Z case at 1024^2 (no 3D multi-block curvilinear "
-                    "reference case is generated)")
+        bytes_pt = 4 * 5 * 8 + 10 * 8  # fused stage plus the ten FP64 metric arrays read
+        cpu_args = ("curv3d_teno5", {"OSB_NP0": 256, "OSB_NP1": 256, "OSB_NP2": 32}, 256 * 256 * 32, 6,
+                    "a 256x256x32 block of the reference's generated 3D curvilinear TENO5 solver (MetricsEquation "
+                    "+ LFTeno(5), RK-LS3; the 4-block case's discretisation on one block of its sizes)")
     pts = sum(b[0].npoints for b in blocks)
     log("problem ready: %d blocks, %d points" % (len(blocks), pts))
     if not args.no_cpu:
@@ -612,14 +643,18 @@ def secondary_arm(args):
     dom_ms = rep[dom][0] / max(rep[dom][1], 1)
     hbm, peak_kind = measured_peaks()
     launches_per_stage = rep[dom][1] / 3.0
+    spec0 = blocks[0][0]
+    table = kernel_bytes(rep["rk_update"][1] == 0, nv=spec0.nvars, ndim=spec0.ndim,
+                         curvilinear=len(blocks[0]) > 2 and blocks[0][2] is not None,
+                         central_only=spec0.scheme == abi.SCHEME_CENTRAL4)
     if dom == "persistent_stage":
-        achieved = bytes_pt * pts / launches_per_stage / (dom_ms * 1e-3) / 1e9
-    elif dom == "central" and len(blocks) == 1:
-        # the central scheme's only residual kernel, RK update fused: FP32 state in and out
-        # (2 x 20 B) plus the FP64 state and register read and written (160 B) per point
-        achieved = 200.0 * pts / (dom_ms * 1e-3) / 1e9
+        dom_bytes_pt = bytes_pt
+    elif dom in ("flux_x", "flux_y", "flux_z", "central", "rk_update"):
+        dom_bytes_pt = table[dom]
     else:
-        achieved = None
+        dom_bytes_pt = None
+    # bytes of one launch: every block's points, over the launches of one stage of that family
+    achieved = (dom_bytes_pt * pts / launches_per_stage / (dom_ms * 1e-3) / 1e9) if dom_bytes_pt else None
     # FP64 per-block path and the error after the same number of steps from the same state
     s64 = Solver(blocks, precision="fp64", rk=rk, device=local)
     s64.apply_bc()
@@ -657,7 +692,9 @@ def secondary_arm(args):
             "schedule": sched,
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm if achieved else None, "peak_kind": peak_kind,
-                         "per_launch_ms": dom_ms}}
+                         "per_launch_ms": dom_ms, "algorithmic_bytes_per_point": dom_bytes_pt,
+                         "traffic": None},
+            "step_hbm_gbs_at_fused_bytes": bytes_pt * pts * 3 * args.steps / secs / 1e9}
     print(json.dumps(line), flush=True)
     return 0
 

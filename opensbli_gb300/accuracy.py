@@ -1,15 +1,23 @@
-"""FP32-residual accuracy against the FP64 path on the supersonic Taylor-Green vortex.
+"""FP32-residual accuracy against the FP64 path, at each benchmark configuration's own horizon.
 
     python -m opensbli_gb300.accuracy --size 256 --steps 1000 --every 50 --out result.json
+    python -m opensbli_gb300.accuracy --workload tgv64 --steps 500 --every 50
+    python -m opensbli_gb300.accuracy --workload kh_ensemble --steps 2000 --every 200
+    python -m opensbli_gb300.accuracy --workload curv4 --steps 500 --every 50
 
 Advances, in lockstep from the same initial state, the FP64 path (the reference solution),
 the FP32-residual path (FP64 state, RK register and reductions) and -- with --floor -- a second
 FP64 run whose initial state carries a relative perturbation of `floor_amp` (seeded), for
-`steps` RK3 steps at the CFL-0.5 time step of t = 0.  Every `every` steps it records the
-relative L2 / Linf differences of rho and rhoE against the FP64 run and the kinetic energy of
-every run.  The perturbed FP64 run measures how fast this flow amplifies any difference at
-rounding level: it is the floor that no implementation differing from the FP64 path by
-rounding can stay under.
+`steps` RK3 steps.  Every `every` steps it records the relative L2 / Linf differences of rho and
+rhoE against the FP64 run (L2 over the interior points of every block; Linf = max |diff| over
+max |field|) and the kinetic energy of every run.  The perturbed FP64 run measures how fast the
+flow amplifies any difference at rounding level: the floor that no implementation differing
+from the FP64 path by rounding can stay under.
+
+Workloads: tgv (the supersonic TGV at --size^3, CFL 0.5 at t = 0, --scheme), tgv64 (the 64^3
+low-Mach TGV with the central scheme, dt 3.385e-3), kh_ensemble (the 64 seeded Kelvin-Helmholtz
+instances, dt 2e-4, the FP32 run on the persistent batched stage), curv4 (the 4-block 3D
+curvilinear case, CFL 0.5 at t = 0).
 """
 import argparse
 import json
@@ -21,31 +29,56 @@ from . import abi, problems
 from .solver import Solver
 
 
-def _diff(torch, a, b, sl):
+def _diff(torch, runs_a, runs_b, specs):
+    """rel L2 / Linf of rho and rhoE of run a against run b over all blocks."""
     out = {}
-    for v, name in ((0, "rho"), (a.shape[0] - 1, "rhoE")):
-        x = a[v][sl]
-        y = b[v][sl]
-        d = x - y
-        out[name] = {"rel_l2": float(torch.linalg.vector_norm(d) / torch.linalg.vector_norm(y)),
-                     "rel_linf": float(d.abs().max() / y.abs().max())}
+    for name in ("rho", "rhoE"):
+        num = den = 0.0
+        dmax = fmax = 0.0
+        for ib, spec in enumerate(specs):
+            v = 0 if name == "rho" else spec.nvars - 1
+            sl = spec.interior()
+            x = runs_a[ib][v][sl]
+            y = runs_b[ib][v][sl]
+            d = x - y
+            num += float(torch.sum(d * d))
+            den += float(torch.sum(y * y))
+            dmax = max(dmax, float(d.abs().max()))
+            fmax = max(fmax, float(y.abs().max()))
+        out[name] = {"rel_l2": (num / den) ** 0.5, "rel_linf": dmax / fmax}
     return out
 
 
+def workload(name, size=256, scheme=abi.SCHEME_TENO5, averaging=abi.AVG_ROE, minf=1.25, cfl=0.5):
+    """(blocks, dt, rk, description) of a benchmark configuration."""
+    if name == "tgv":
+        spec, q = problems.tgv(size, minf=minf, scheme=scheme, averaging=averaging)
+        return [(spec, q)], problems.cfl_dt(spec, q, cfl), "ls3", "supersonic TGV %d^3 (CFL %.1f)" % (size, cfl)
+    if name == "tgv64":
+        return ([problems.tgv(64, minf=0.1, scheme=abi.SCHEME_CENTRAL4)], 3.385e-3, "ls3",
+                "TGV 64^3, M=0.1, central-4 Feiereisen + viscous, dt 3.385e-3")
+    if name == "kh_ensemble":
+        return (problems.kh_ensemble(64, seed=0), 2e-4, "ls3",
+                "64 Kelvin-Helmholtz instances (seed 0), WENO5-Z (Roe), dt 2e-4")
+    if name == "curv4":
+        blocks = problems.curvilinear_multiblock_3d(seed=0)
+        return blocks, problems.multiblock_cfl_dt(blocks, cfl), "ls3", "4-block 3D curvilinear TENO5 (CFL 0.5)"
+    raise ValueError("unknown workload %s" % name)
+
+
 def run(size=256, steps=1000, every=50, scheme=abi.SCHEME_TENO5, averaging=abi.AVG_ROE, minf=1.25, cfl=0.5,
-        floor=False, floor_amp=1e-12, seed=0, fp32=True):
-    spec, q = problems.tgv(size, minf=minf, scheme=scheme, averaging=averaging)
-    dt = problems.cfl_dt(spec, q, cfl)
-    runs = {"fp64": Solver([(spec, q)], precision="fp64", rk="ls3")}
+        floor=False, floor_amp=1e-12, seed=0, fp32=True, name="tgv"):
+    blocks, dt, rk, desc = workload(name, size, scheme, averaging, minf, cfl)
+    specs = [b[0] for b in blocks]
+    runs = {"fp64": Solver(blocks, precision="fp64", rk=rk)}
     if fp32:
-        runs["fp32"] = Solver([(spec, q)], precision="fp32", rk="ls3")
+        runs["fp32"] = Solver(blocks, precision="fp32", rk=rk)
     if floor:
         rng = np.random.default_rng(seed)
-        qp = [a * (1.0 + floor_amp * rng.standard_normal(a.shape)) for a in q]
-        runs["fp64_perturbed"] = Solver([(spec, qp)], precision="fp64", rk="ls3")
+        pert = [(b[0], [a * (1.0 + floor_amp * rng.standard_normal(a.shape)) for a in b[1]]) + tuple(b[2:])
+                for b in blocks]
+        runs["fp64_perturbed"] = Solver(pert, precision="fp64", rk=rk)
     torch = runs["fp64"].torch
-    h = spec.halo
-    sl = tuple(slice(h, h + spec.size[d]) for d in reversed(range(spec.ndim)))
     for s in runs.values():
         s.apply_bc()
     hist = {"steps": [0], "ke": {k: [s.reduce(abi.RED_KE)] for k, s in runs.items()},
@@ -63,12 +96,13 @@ def run(size=256, steps=1000, every=50, scheme=abi.SCHEME_TENO5, averaging=abi.A
         hist["steps"].append(done)
         for k, s in runs.items():
             hist["ke"][k].append(s.reduce(abi.RED_KE))
-        ref = runs["fp64"].q[0]
         for k in hist["diff"]:
-            hist["diff"][k].append(_diff(torch, runs[k].q[0], ref, sl))
-    out = {"size": size, "steps": steps, "dt": dt, "scheme": scheme, "averaging": averaging, "minf": minf,
+            hist["diff"][k].append(_diff(torch, runs[k].q, runs["fp64"].q, specs))
+    npts = sum(s.npoints for s in specs)
+    out = {"workload": name, "description": desc, "points": npts, "size": size, "steps": steps, "dt": dt,
+           "scheme": scheme, "averaging": averaging, "minf": minf,
            "floor_amp": floor_amp if floor else None, "history": hist, "seconds": secs,
-           "mpt_stage_per_s": {k: spec.npoints * 3 * steps / secs[k] / 1e6 for k in secs}}
+           "mpt_stage_per_s": {k: npts * 3 * steps / secs[k] / 1e6 for k in secs}}
     out["errors"] = {k: v[-1] for k, v in hist["diff"].items()}
     ke64 = np.array(hist["ke"]["fp64"])
     out["ke_max_rel_dev"] = {k: float(np.max(np.abs(np.array(v) - ke64) / np.abs(ke64)))
@@ -80,6 +114,7 @@ def run(size=256, steps=1000, every=50, scheme=abi.SCHEME_TENO5, averaging=abi.A
 
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--workload", default="tgv", choices=["tgv", "tgv64", "kh_ensemble", "curv4"])
     ap.add_argument("--size", type=int, default=256)
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--every", type=int, default=50)
@@ -92,9 +127,9 @@ def main():
     scheme = abi.SCHEME_NAMES[args.scheme]
     avg = abi.AVG_ROE if scheme == abi.SCHEME_TENO5 else abi.AVG_SIMPLE
     res = run(args.size, args.steps, args.every, scheme=scheme, averaging=avg, floor=args.floor,
-              floor_amp=args.floor_amp, fp32=not args.no_fp32)
+              floor_amp=args.floor_amp, fp32=not args.no_fp32, name=args.workload)
     txt = json.dumps(res)
-    print(json.dumps({"errors": res["errors"], "ke_max_rel_dev": res["ke_max_rel_dev"],
+    print(json.dumps({"workload": args.workload, "errors": res["errors"], "ke_max_rel_dev": res["ke_max_rel_dev"],
                       "mpt_stage_per_s": res["mpt_stage_per_s"]}))
     if args.out:
         with open(args.out, "w") as f:
