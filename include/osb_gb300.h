@@ -108,7 +108,9 @@ typedef struct osb_interface {
   int32_t block;   /* index (osb_block_add order) of the neighbouring block */
   int32_t dir;     /* its direction that faces this one */
   int32_t side;    /* its side (0 = low, 1 = high) */
-  int32_t flip;    /* 1 if the transverse index runs backwards across the interface */
+  int32_t flip;    /* 1: InterfaceBC match flag (opsc.py:1043-1045): the normal index of the
+                      neighbour runs the other way, so its layers are copied in reverse order
+                      (faces of equal sides, e.g. both low faces of a C-mesh wake cut) */
 } osb_interface;
 
 typedef struct osb_block_desc {

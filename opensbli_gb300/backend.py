@@ -172,6 +172,7 @@ def _bcs_of(block, central_only):
     from opensbli.core.boundary_conditions.extrapolation import ExtrapolationBC
     bc = [[None, None] for _ in range(block.ndim)]
     depth = [[4, 4] for _ in range(block.ndim)]
+    flips = [[None, None] for _ in range(block.ndim)]
     for d, pair in enumerate(block.boundary_types):
         for side, b in enumerate(pair):
             if isinstance(b, PeriodicBC):
@@ -199,6 +200,23 @@ def _bcs_of(block, central_only):
                 bc[d][side] = abi.BC_PRESSURE_OUTLET
                 hv = b.get_halo_values(block)
                 depth[d][side] = abs(hv[d][side])
+            elif type(b).__name__ == "SharedInterfaceBC":
+                raise NotImplementedError("SharedInterfaceBC (interfaces sharing their boundary points) is not "
+                                          "implemented; InterfaceBC is")
+            elif type(b).__name__ == "InterfaceBC":
+                # multi_block.py:48-107: the neighbour's layers next to its face fill this face's
+                # halos, in reverse order along the normal when the match flag is set
+                # (opsc.py:1043-1045); depth = the neighbour's scheme halo on that side
+                match = tuple(b.match)
+                if len(match) < 3 or match[1] != d:
+                    raise NotImplementedError("interface of direction %d matched to direction %s of block %s: only "
+                                              "faces normal to the same direction are implemented" % (
+                                                  d, match[1] if len(match) > 1 else None, match[0]))
+                bc[d][side] = abi.BC_INTERFACE
+                flips[d][side] = (int(match[0]), int(match[1]), int(match[2]),
+                                  1 if len(match) > 3 and match[3] else 0)
+                hv = b.get_halo_values(block)
+                depth[d][side] = abs(hv[d][side])
             elif type(b).__name__ == "DirichletBC":
                 # the generated kernel covers the plane and the scheme's halo on that side
                 # (dirichlet.py:35-40: block.boundary_halos)
@@ -206,7 +224,7 @@ def _bcs_of(block, central_only):
                 depth[d][side] = max(abs(h.get_halos(side)) for h in block.boundary_halos[d][side])
             else:
                 raise NotImplementedError("boundary condition %s is not supported" % type(b).__name__)
-    return bc, depth
+    return bc, depth, flips
 
 
 def _rhs_names(eqn):
@@ -347,10 +365,11 @@ def block_spec(block, params):
     if coords is not None and (visc != abi.VISC_NONE or scheme == abi.SCHEME_CENTRAL4):
         raise NotImplementedError("curvilinear blocks take the characteristic Euler flux only (the metric-"
                                   "transformed central and viscous terms are not implemented)")
-    bc, depth = _bcs_of(block, scheme == abi.SCHEME_CENTRAL4)
+    bc, depth, iface = _bcs_of(block, scheme == abi.SCHEME_CENTRAL4)
     split = _split_form_of(block) if scheme == abi.SCHEME_CENTRAL4 else abi.SPLIT_FEIEREISEN
     filt, kappa = _filter_of(block, p)
     spec = BlockSpec(ndim=nd, size=size, scheme=scheme, averaging=avg, viscous=visc, bc=bc, bc_depth=depth,
+                     iface=iface if any(f is not None for pair in iface for f in pair) else None,
                      split_form=split, filter=filt, tvd_kappa=kappa, flux_type=_flux_of(block),
                      gama=_const_value("gama", p), Minf=_const_value("Minf", p, 1.0), Re=_const_value("Re", p, 1.0),
                      Pr=_const_value("Pr", p, 0.71), mu_const=1.0, eps=_const_value("eps", p, 1e-40),
@@ -577,7 +596,11 @@ class GB300Backend:
     derived from the algorithm as a BackendPlan; ``GB300Backend.from_plan`` runs such a plan
     without the OpenSBLI generator (initialise and run are the same code)."""
 
-    def __init__(self, alg, parameters, precision=None, device=0, graphs=True, mixed_precision_config=None):
+    def __init__(self, alg, parameters, precision=None, device=0, graphs=True, mixed_precision_config=None,
+                 blocks=None):
+        """alg: what the script would hand to OPSC -- TraditionalAlgorithmRK(block), or for a
+        MultiBlock problem the MultiBlock itself or TraditionalAlgorithmRKMB(multi_block) with
+        blocks=multi_block (that algorithm object keeps no reference to its blocks)."""
         if precision is None:
             precision = precision_of(mixed_precision_config)
         if precision not in ("fp64", "fp32"):
@@ -585,7 +608,12 @@ class GB300Backend:
         self.alg = alg
         self.params = dict(parameters)
         self.numbers = resolve_parameters(self.params)
-        self.blocks = list(alg.blocks)
+        if blocks is not None:
+            self.blocks = list(getattr(blocks, "blocks", blocks))
+        elif hasattr(alg, "blocks"):
+            self.blocks = list(alg.blocks)
+        else:
+            raise ValueError("a multi-block algorithm keeps no reference to its blocks: pass blocks=multi_block")
         self.specs = [block_spec(b, self.params) for b in self.blocks]
         for s in self.specs[1:]:
             if not s.same_discretisation(self.specs[0]):

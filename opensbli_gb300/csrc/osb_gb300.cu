@@ -417,12 +417,12 @@ __global__ void k_dirichlet(BlockK b, int nv, int d, int side, int depth, int ha
   }
 }
 
-// Block interface (multi_block.py:11-107, InterfaceBC with identity orientation): the halo
-// layers of face (d, side) of dst receive the `depth` layers of src next to its face
-// (d, sside).  The transverse range is the interior of the face (full = 0) or that plus
-// `depth` halo points on each side (full = 1).
-__global__ void k_interface(BlockK dst, BlockK src, int nv, int d, int side, int sside, int depth, int full,
-                            int fields) {
+// Block interface (multi_block.py:11-107, InterfaceBC): the halo layers of face (d, side) of dst
+// receive the `depth` layers of src next to its face (d, sside), in reverse order along the
+// normal when flip is set (the match flag, opsc.py:1043-1045).  The transverse range is the
+// interior of the face (full = 0) or that plus `depth` halo points on each side (full = 1).
+__global__ void k_interface(BlockK dst, BlockK src, int nv, int d, int side, int sside, int flip, int depth,
+                            int full, int fields) {
   int ext[3], lo[3];
   for (int e = 0; e < 3; ++e) {
     if (e < dst.ndim && e != d) {
@@ -445,7 +445,9 @@ __global__ void k_interface(BlockK dst, BlockK src, int nv, int d, int side, int
     int di[3], si[3];
     for (int e = 0; e < 3; ++e) di[e] = si[e] = c[e] + lo[e];
     di[d] = side == 0 ? -depth + c[d] : dst.n[d] + c[d];
-    si[d] = sside == 1 ? src.n[d] - depth + c[d] : c[d];
+    // flipped (the neighbour's normal index runs the other way): the layers in reverse order
+    const int sl = flip ? depth - 1 - c[d] : c[d];
+    si[d] = sside == 1 ? src.n[d] - depth + sl : sl;
     const int a = lin(dst, di[0], di[1], di[2]), bsrc = lin(src, si[0], si[1], si[2]);
     if (fields & BC_Q) dst.q[v][a] = src.q[v][bsrc];
     if ((fields & BC_QF) && dst.qf[0]) dst.qf[v][a] = src.qf[v][bsrc];
@@ -692,8 +694,8 @@ int apply_interfaces(osb_ctx* c, int full, int fields) {
         for (int e = 0; e < bl.d.ndim; ++e)
           if (e != d) total *= bl.k.n[e] + (full ? 2 * depth : 0);
         timing_begin(c, FAM_BC);
-        k_interface<<<grid_for(c, total, 256), 256, 0, c->stream>>>(bl.k, nb.k, nv, d, side, f.side, depth, full,
-                                                                     fields);
+        k_interface<<<grid_for(c, total, 256), 256, 0, c->stream>>>(bl.k, nb.k, nv, d, side, f.side, f.flip, depth,
+                                                                     full, fields);
         timing_end(c);
         c->launches++;
       }
@@ -1013,8 +1015,8 @@ bool check_desc(const osb_block_desc* d, std::string& why) {
     for (int s = 0; s < 2; ++s) {
       if (d->bc[i][s] != OSB_BC_INTERFACE) continue;
       const osb_interface& f = d->iface[i][s];
-      if (f.dir != i || f.flip != 0) {
-        why = "interfaces connect faces normal to the same direction without flips";
+      if (f.dir != i || (f.flip != 0 && f.flip != 1)) {
+        why = "interfaces connect faces normal to the same direction (flip 0 or 1)";
         return false;
       }
       if (f.side != 0 && f.side != 1) { why = "interface side must be 0 or 1"; return false; }

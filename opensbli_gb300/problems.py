@@ -363,6 +363,34 @@ def shock_reflection(n0=457, n1=255, sizes=None, flux_type=abi.FLUX_LLF, back_pr
 # ---------------------------------------------------------------------------------------
 # Multi-block topologies
 
+def flipped_pair_2d(sizes=(24, 20)):
+    """Two 2D Euler blocks (WENO5-Z, simple average) joined along x by two flipped interfaces --
+    block 0's low-x face to block 1's low-x face and the two high-x faces (InterfaceBC with the
+    match flag set, as a C-mesh wake cut) -- and periodic in y (depth 4 everywhere), with a
+    different smooth state on each block over x0 = i / N0, x1 = j / N1: the problem of the
+    generated multi-block reference case mb2_flip.  Returns [(spec, state)] for blocks 0 and 1."""
+    forms = [(lambda x0, x1: 1.0 + 0.2 * np.sin(2 * math.pi * (x0 + x1)),
+              lambda x0, x1: 0.4 + 0.1 * np.cos(2 * math.pi * x1),
+              lambda x0, x1: -0.2 + 0.1 * np.sin(2 * math.pi * x0),
+              lambda x0, x1: 1.0 + 0.1 * np.cos(2 * math.pi * (x0 - x1))),
+             (lambda x0, x1: 1.1 + 0.15 * np.cos(2 * math.pi * (x0 - 2 * x1)),
+              lambda x0, x1: -0.3 + 0.1 * np.sin(2 * math.pi * (x0 + x1)),
+              lambda x0, x1: 0.25 + 0.1 * np.cos(2 * math.pi * x0),
+              lambda x0, x1: 0.9 + 0.1 * np.sin(2 * math.pi * x1))]
+    out = []
+    for b in range(2):
+        o = 1 - b
+        spec = BlockSpec(ndim=2, size=tuple(sizes), scheme=abi.SCHEME_WENO5_Z, averaging=abi.AVG_SIMPLE,
+                         bc=[[abi.BC_INTERFACE, abi.BC_INTERFACE], [abi.BC_PERIODIC, abi.BC_PERIODIC]],
+                         bc_depth=[[4, 4], [4, 4]], iface=[[(o, 0, 0, 1), (o, 0, 1, 1)], [None, None]],
+                         delta=(1.0 / sizes[0], 1.0 / sizes[1]), gama=1.4)
+        x0 = spec.delta[0] * spec.grid_index(0)
+        x1 = spec.delta[1] * spec.grid_index(1)
+        d, u0, u1, p = (f(x0, x1) for f in forms[b])
+        out.append((spec, _cons(spec, d, [u0, u1], p)))
+    return out
+
+
 def split_block(spec, state, cuts, d=0, metrics=None):
     """Split one block along direction d at the interior indices `cuts` into blocks joined by
     interfaces (periodic faces along d become an interface between the last and the first

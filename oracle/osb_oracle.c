@@ -1494,8 +1494,11 @@ static void interface_face(osb_block_desc* blocks, osb_block_desc* b, const geom
         for (int i = lo[0]; i < hi[0]; ++i) {
           int dst[3] = {i, j, k}, src[3] = {i, j, k};
           int layer = (d == 0 ? i : (d == 1 ? j : k));
+          /* a flipped interface (opsc.py:1043-1045: to_dir of the normal direction negated)
+           * copies the layers in reverse order along the normal */
+          int sl = f->flip ? depth - 1 - layer : layer;
           dst[d] = side == 0 ? -depth + layer : g->n[d] + layer;
-          src[d] = f->side == 1 ? Nn - depth + layer : layer;
+          src[d] = f->side == 1 ? Nn - depth + sl : sl;
           b->q[v][gid(g, dst[0], dst[1], dst[2])] = nb->q[v][gid(&ng, src[0], src[1], src[2])];
         }
 }

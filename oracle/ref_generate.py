@@ -128,7 +128,11 @@ def _constituents(ndim, viscous=False, sutherland=True, with_T=None):
 def _finish(block, alg_kwargs, params):
     from opensbli import TraditionalAlgorithmRK, SimulationDataType, Double, OPSC
     from opensbli.utilities.helperfunctions import substitute_simulation_parameters
-    alg = TraditionalAlgorithmRK(block, **alg_kwargs)
+    if hasattr(block, "nblocks"):  # a MultiBlock: the multi-block time loop (multiblock/algorithm.py)
+        from opensbli.multiblock.algorithm import TraditionalAlgorithmRKMB
+        alg = TraditionalAlgorithmRKMB(block, **alg_kwargs)
+    else:
+        alg = TraditionalAlgorithmRK(block, **alg_kwargs)
     SimulationDataType.set_datatype(Double)
     OPSC(alg)
     names, values = zip(*params.items())
@@ -509,6 +513,60 @@ def case_curv3d_teno5():
     return block, params
 
 
+def case_mb2_flip():
+    """Two 2D Euler blocks (characteristic LLF WENO5-Z, simple average, RK-LS3) joined along x by
+    two flipped interfaces -- block 0's low-x face to block 1's low-x face and the two high-x
+    faces, InterfaceBC(match=(other, 0, side, True)) as the C-mesh wake cut of
+    apps/aerofoils/multi_block/2D/airfoil_MB_2D.py:160,170 -- and periodic in y; a different
+    smooth state on each block (MultiBlock, TraditionalAlgorithmRKMB)."""
+    from opensbli import (MultiBlock, GridBasedInitialisation, GridVariable, DataObject, parse_expr, SimpleAverage,
+                          LFWeno, RungeKuttaLS, PeriodicBC, InterfaceBC)
+    ndim = 2
+    sim = _euler_equations(ndim, "Weno")
+    cr = _constituents(ndim)
+    mb = MultiBlock(ndim, 2)
+    schemes = {}
+    LF = LFWeno(order=5, formulation="Z", averaging=SimpleAverage([0, 1]), flux_type="LLF")
+    schemes[LF.name] = LF
+    rk = RungeKuttaLS(3)
+    schemes[rk.name] = rk
+    mb.set_discretisation_schemes(schemes)
+    bcs = {}
+    for b in range(2):
+        o = 1 - b
+        bcs[b] = [InterfaceBC(direction=0, side=0, halos=[-4, 4], name="b%d_low_x" % b, match=(o, 0, 0, True)),
+                  InterfaceBC(direction=0, side=1, halos=[-4, 4], name="b%d_high_x" % b, match=(o, 0, 1, True)),
+                  PeriodicBC(1, 0), PeriodicBC(1, 1)]
+    mb.set_block_boundaries(bcs)
+    inits = {}
+    forms = [("1.0 + 0.2*sin(2*pi*(x0 + x1))", "0.4 + 0.1*cos(2*pi*x1)", "-0.2 + 0.1*sin(2*pi*x0)",
+              "1.0 + 0.1*cos(2*pi*(x0 - x1))"),
+             ("1.1 + 0.15*cos(2*pi*(x0 - 2*x1))", "-0.3 + 0.1*sin(2*pi*(x0 + x1))", "0.25 + 0.1*cos(2*pi*x0)",
+              "0.9 + 0.1*sin(2*pi*x1)")]
+    for b, blk in enumerate(mb.blocks):
+        local_dict = {"block": blk, "GridVariable": GridVariable, "DataObject": DataObject}
+        d, u0, u1, p = forms[b]
+        eqns = ["Eq(GridVariable(x0), block.deltas[0]*block.grid_indexes[0])",
+                "Eq(GridVariable(x1), block.deltas[1]*block.grid_indexes[1])",
+                "Eq(GridVariable(d), %s)" % d, "Eq(GridVariable(u0), %s)" % u0, "Eq(GridVariable(u1), %s)" % u1,
+                "Eq(GridVariable(p), %s)" % p,
+                "Eq(DataObject(rho), d)", "Eq(DataObject(rhou0), d*u0)", "Eq(DataObject(rhou1), d*u1)",
+                "Eq(DataObject(rhoE), p/(gama-1.0) + 0.5*d*(u0**2 + u1**2))"]
+        init = GridBasedInitialisation()
+        init.add_equations([parse_expr(e, local_dict=local_dict) for e in eqns])
+        inits[b] = init
+    mb.set_equations([cr, sim])
+    mb.set_initial_conditions(inits)
+    mb.discretise()
+    params = {"gama": "1.4", "dt": 'osb_env_double("OSB_DT", 0.0005)', "niter": 'osb_env_int("OSB_NITER", 1)'}
+    for b in range(2):
+        for d in range(2):
+            params["block%dnp%d" % (b, d)] = 'osb_env_int("OSB_NP%d", %d)' % (d, 24 if d == 0 else 20)
+            params["Delta%dblock%d" % (d, b)] = "1.0/block%dnp%d" % (b, d)
+        params["block%dnp2" % b] = "1"
+    return mb, params
+
+
 def case_curv_weno5z():
     """2D curvilinear wavy-mesh Euler wave, characteristic LLF WENO5-Z (Roe average) with
     4th-order central metrics, periodic, RK-LS3: the reference's verification case
@@ -588,6 +646,7 @@ CASES = {
     "kh_weno5z": case_kh_weno5z,
     "curv_weno5z": case_curv_weno5z,
     "curv3d_teno5": case_curv3d_teno5,
+    "mb2_flip": case_mb2_flip,
 }
 
 

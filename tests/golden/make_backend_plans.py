@@ -48,6 +48,11 @@ CASES = {
     "shock_64x32": ("shock_reflection", {"gama": "1.4", "Minf": "2.0", "dt": "0.5", "niter": "10",
                                          "block0np0": "64", "block0np1": "32",
                                          "Delta0block0": "350.0/(block0np0-1)", "Delta1block0": "115.0/(block0np1-1)"}),
+    # two blocks joined by flipped interfaces (MultiBlock, TraditionalAlgorithmRKMB)
+    "mb2_flip": ("mb2_flip", {"gama": "1.4", "dt": "0.0005", "niter": "10",
+                              "block0np0": "24", "block0np1": "20", "Delta0block0": "1.0/block0np0",
+                              "Delta1block0": "1.0/block0np1", "block1np0": "24", "block1np1": "20",
+                              "Delta0block1": "1.0/block1np0", "Delta1block1": "1.0/block1np1"}),
     # Kelvin-Helmholtz with the classic SBLI RK3
     "kh_32": ("kh_weno5z", {"gama": "1.4", "dt": "0.0002", "niter": "6", "block0np0": "32", "block0np1": "32",
                             "Delta0block0": "1.0/block0np0", "Delta1block0": "1.0/block0np1", "khamp": "1.0",
@@ -67,6 +72,9 @@ def build_plan(name):
     from opensbli import TraditionalAlgorithmRK
     from opensbli_gb300.backend import GB300Backend
     with open(os.devnull, "w") as dn, contextlib.redirect_stdout(dn):
+        if hasattr(block, "nblocks"):  # a MultiBlock: the script's TraditionalAlgorithmRKMB
+            from opensbli.multiblock.algorithm import TraditionalAlgorithmRKMB
+            return GB300Backend(TraditionalAlgorithmRKMB(block), params, precision="fp64", blocks=block).plan()
         alg = TraditionalAlgorithmRK(block)
     return GB300Backend(alg, params, precision="fp64").plan()
 

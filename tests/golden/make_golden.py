@@ -169,7 +169,36 @@ def make_tvd(n=12, steps=(1, 2, 4), dt=2e-3, kappa=1.25, pert=(2e-2, 5)):
     print("wrote", name)
 
 
+def make_mb2_flip(sizes=(24, 20), counts=(1, 3, 30), dt=5e-4, pert=(1e-3, 31)):
+    """Golden states of the generated two-block case with flipped interfaces (reference case
+    mb2_flip: MultiBlock, TraditionalAlgorithmRKMB), from perturbed states of both blocks."""
+    blocks = problems.flipped_pair_2d(sizes)
+    blocks = [(s, perturb(q, *pert)) for s, q in blocks]
+    ob = harness.OracleBlocks(blocks)
+    ob.apply_bc()
+    init = {}
+    for b in range(2):
+        for v, nm in enumerate(["rho", "rhou0", "rhou1", "rhoE"]):
+            init["%s_B%d" % (nm, b)] = ob.q[b][v]
+    out = {"dt": dt, "counts": np.array(counts), "pert": np.array(pert)}
+    sl = blocks[0][0].interior()
+    for b in range(2):
+        out["ic_%d" % b] = np.stack([ob.q[b][v][sl] for v in range(4)])
+    env = {"OSB_NP0": sizes[0], "OSB_NP1": sizes[1], "OSB_DT": repr(dt), "OSB_NITER": max(counts) // 3 + 1}
+    for n in counts:
+        # the harness counts every block's update: a stage of the two blocks is two updates
+        r = harness.run_ref("mb2_flip", env=env, init=init, stop_after_rk=2 * n)
+        for b in range(2):
+            out["after_%d_%d" % (n, b)] = np.stack([r["%s_B%d" % (nm, b)][sl] for nm in ["rho", "rhou0", "rhou1", "rhoE"]])
+    name = "mb2_flip_%dx%d_perturbed" % sizes
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    print("wrote", name)
+
+
 def main():
+    if sys.argv[1:] == ["mb2_flip"]:
+        make_mb2_flip()
+        return
     if sys.argv[1:] == ["tvd"]:
         if not harness.ref_available("tgv_kgp_tvd"):
             subprocess.check_call([sys.executable, os.path.join(ROOT, "oracle", "ref_generate.py"), "tgv_kgp_tvd"])

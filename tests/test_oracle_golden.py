@@ -288,3 +288,57 @@ def test_host_metrics_match_reference_3d():
     for k in range(10):
         scale = float(np.max(np.abs(ref[k][sl])))
         assert float(np.max(np.abs(met[k][sl] - ref[k][sl]))) < 1e-13 * scale, k
+
+
+MB2 = "mb2_flip_24x20_perturbed"
+
+
+def _mb2_blocks():
+    g = np.load(os.path.join(GOLD, MB2 + ".npz"))
+    blocks = problems.flipped_pair_2d((24, 20))
+    amp, seed = float(g["pert"][0]), int(g["pert"][1])
+    blocks = [(s, perturb(q, amp, seed)) for s, q in blocks]
+    return blocks, g
+
+
+def test_flipped_interfaces_match_reference():
+    """Two blocks joined by flipped interfaces (InterfaceBC match flag: the neighbour's layers in
+    reverse order along the normal), periodic in y: the oracle against the reference's generated
+    multi-block solver (MultiBlock + TraditionalAlgorithmRKMB, bc_exchanges with a negative
+    to_dir) after 1, 3 and 30 stages, both blocks, 1e-12."""
+    blocks, g = _mb2_blocks()
+    blocks = [(s, [a for a in q]) for s, q in blocks]
+    for n in g["counts"]:
+        n = int(n)
+        ob = harness.OracleBlocks(blocks)
+        ob.apply_bc()
+        sl = blocks[0][0].interior()
+        if n == 1:
+            for b in range(2):
+                assert np.array_equal(np.stack([ob.q[b][v][sl] for v in range(4)]), g["ic_%d" % b])
+        advance_mb(ob, "ls3", float(g["dt"]), n)
+        for b in range(2):
+            ref = g["after_%d_%d" % (n, b)]
+            errs = [harness.rel_err(ob.q[b][v][sl], ref[v]) for v in range(4)]
+            assert max(errs) < 1e-12, (n, b, errs)
+
+
+def test_flip_matters():
+    """Without the flip the same two blocks end elsewhere (the golden states are sensitive to it)."""
+    blocks, g = _mb2_blocks()
+    for s, _ in blocks:
+        s.iface = [[(f[0], f[1], f[2], 0) for f in s.iface[0]], [None, None]]
+    ob = harness.OracleBlocks(blocks)
+    ob.apply_bc()
+    advance_mb(ob, "ls3", float(g["dt"]), 3)
+    sl = blocks[0][0].interior()
+    assert harness.rel_err(ob.q[0][0][sl], g["after_3_0"][0]) > 1e-6
+
+
+def advance_mb(ob, rk, dt, nstages):
+    kind, A, B = rk_params(rk)
+    nsteps, rest = divmod(nstages, 3)
+    if nsteps:
+        ob.step(kind, A, B, dt, nsteps)
+    for st in range(rest):
+        ob.stage(kind, A, B, st, dt)
