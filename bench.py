@@ -574,14 +574,15 @@ def secondary_arm(args):
         bytes_pt = 4 * 5 * 8
         cpu_args = None
     elif args.workload == "shock":
-        blocks = [problems.shock_reflection(457, 255)]
+        # the app as written: its own HLLC-LM flux from WENO5-Z states and its SSP RK3
+        blocks = [problems.shock_reflection(457, 255, flux_type=abi.FLUX_HLLC_LM)]
         dt = 0.1
-        rk = "ls3"
-        work = ("2D inviscid shock reflection 457 x 255 (350 x 115, M=2), WENO5-Z (simple average), RK-LS3, "
-                "Dirichlet inlet and top, extrapolation outlet, symmetry wall, dt 0.1 as the app")
+        rk = (abi.RK_LOW_STORAGE, problems.RK3_SSP_A, problems.RK3_SSP_B)
+        work = ("2D inviscid shock reflection 457 x 255 (350 x 115, M=2), HLLC-LM flux from WENO5-Z states (simple "
+                "average), SSP RK3, Dirichlet inlet and top, extrapolation outlet, symmetry wall, dt 0.1 as the app")
         bytes_pt = 4 * 4 * 8
-        cpu_args = ("shock_reflection", {"OSB_NP0": 457, "OSB_NP1": 255, "OSB_DT": 0.1}, 457 * 255, 30,
-                    "the 457 x 255 shock reflection")
+        cpu_args = ("shock_reflection_hllc", {"OSB_NP0": 457, "OSB_NP1": 255, "OSB_DT": 0.1}, 457 * 255, 30,
+                    "the 457 x 255 shock reflection with the app's HLLC-LM flux and SSP RK3")
     elif args.workload == "tvd":
         n = args.size
         blocks = [problems.tgv_tvd(n, kappa=1.25)]
