@@ -5,11 +5,11 @@
 namespace osb {
 namespace {
 
-template <typename T, int CONV, int VISC, bool FUSE>
+template <typename T, int CONV, int VISC, bool FUSE, int CY>
 int launch_central_k(osb_ctx* c, Block& bl, int first, const RkFuse& rf) {
   using Fd = CentralFields<T, CONV, VISC>;
-  size_t smem = (size_t)Fd::N * CRING * CPL * sizeof(T);
-  auto kern = k_central3d<T, CONV, VISC, FUSE>;
+  size_t smem = (size_t)Fd::N * CRING * CTile<CY>::CPL * sizeof(T);
+  auto kern = k_central3d<T, CONV, VISC, FUSE, CY>;
   OSB_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   CentralParams cp{};
   const osb_block_desc& d = bl.d;
@@ -34,7 +34,7 @@ int launch_central_k(osb_ctx* c, Block& bl, int first, const RkFuse& rf) {
   // (two of halo) at about a third of the cost of a computed plane each
   const long cols = (long)((k.n[0] + CX - 1) / CX) * ((k.n[1] + CY - 1) / CY);
   const long slots = (long)resident_ctas(kern, CX * CY, smem) * c->sm_count;
-  const int nz = wave_chunks(k.n[2], cols, slots, 1.4, 8);
+  const int nz = wave_chunks(k.n[2], cols, slots, 1.4, 4);
   const int czc = (k.n[2] + nz - 1) / nz;
   dim3 grid((k.n[0] + CX - 1) / CX, (k.n[1] + CY - 1) / CY, (k.n[2] + czc - 1) / czc);
   timing_begin(c, FAM_CENTRAL);
@@ -44,13 +44,26 @@ int launch_central_k(osb_ctx* c, Block& bl, int first, const RkFuse& rf) {
   return OSB_OK;
 }
 
+// Tile height of the FP32 kernels: 8 rows unless the ring holds the KGP form's eleven fields of a
+// block whose cross-section already gives every SM several columns (measured: 8 rows are 37 %
+// faster on the 64^3 central TGV and equal on the 256^3 TENO5 one; 4 rows are 1.4 % faster for
+// the 256^3 KGP form).  The FP64 kernels (FP64-pipe bound, a ring twice as large) keep 4 rows.
+template <typename T, int CONV, int VISC, bool FUSE>
+int launch_central_h(osb_ctx* c, Block& bl, int first, const RkFuse& rf) {
+  const long cols4 = (long)((bl.k.n[0] + CX - 1) / CX) * ((bl.k.n[1] + 3) / 4);
+  if (sizeof(T) == 8 || (CONV == 2 && cols4 >= 2L * c->sm_count))
+    return launch_central_k<T, CONV, VISC, FUSE, 4>(c, bl, first, rf);
+  if constexpr (sizeof(T) == 4) return launch_central_k<T, CONV, VISC, FUSE, 8>(c, bl, first, rf);
+  return OSB_OK;
+}
+
 // With rf (FP32 path) the kernel applies the RK update instead of storing the residual.
 template <typename T, int CONV, int VISC>
 int launch_central_t(osb_ctx* c, Block& bl, int first, const RkFuse* rf) {
   if constexpr (sizeof(T) == 4) {
-    if (rf) return launch_central_k<T, CONV, VISC, true>(c, bl, first, *rf);
+    if (rf) return launch_central_h<T, CONV, VISC, true>(c, bl, first, *rf);
   }
-  return launch_central_k<T, CONV, VISC, false>(c, bl, first, RkFuse{});
+  return launch_central_h<T, CONV, VISC, false>(c, bl, first, RkFuse{});
 }
 
 template <typename T>

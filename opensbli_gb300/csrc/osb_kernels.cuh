@@ -627,10 +627,17 @@ __device__ __forceinline__ float cpar<float>(double, float f) { return f; }
 // z-2 .. z+2 around the current one sit in a 5-plane ring in shared memory (halo 2 in x and y,
 // edges included), the raw state of plane z+3 is loaded into registers while plane z is
 // computed, then converted to primitives into the slot plane z-2 vacates.
-constexpr int CX = 32, CY = 4, CH = 2, CRING = 5;
-constexpr int CSX = CX + 2 * CH, CSY = CY + 2 * CH;
-constexpr int CPL = CSX * CSY;  // points of one staged plane
-constexpr int CPP = (CPL + CX * CY - 1) / (CX * CY);  // staged points per thread and plane
+// The tile height CY is a template argument: 8 rows stage fewer halo points per computed point
+// (36 x 12 / 256 against 36 x 8 / 128) and give small blocks more threads per column, 4 rows keep
+// the shared-memory ring small when it holds many fields (the KGP form with viscous terms).
+constexpr int CX = 32, CH = 2, CRING = 5;
+constexpr int CSX = CX + 2 * CH;
+template <int CY>
+struct CTile {
+  static constexpr int CSY = CY + 2 * CH;
+  static constexpr int CPL = CSX * CSY;                        // points of one staged plane
+  static constexpr int CPP = (CPL + CX * CY - 1) / (CX * CY);  // staged points per thread and plane
+};
 
 template <typename T, int CONV, int VISC>
 struct CentralFields {
@@ -641,8 +648,9 @@ struct CentralFields {
   static constexpr int N = CONV ? (VISC ? 11 : 9) : 6;
 };
 
-template <typename T, int CONV, int VISC, bool FUSE>
+template <typename T, int CONV, int VISC, bool FUSE, int CY>
 __global__ void __launch_bounds__(CX * CY) k_central3d(BlockK b, CentralParams cp, int first, int czc, RkFuse rf) {
+  constexpr int CPL = CTile<CY>::CPL, CPP = CTile<CY>::CPP;
   using Fd = CentralFields<T, CONV, VISC>;
   constexpr int FS = CRING * CPL;  // field stride in shared memory
   extern __shared__ __align__(16) unsigned char osb_smem[];
