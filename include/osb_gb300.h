@@ -216,6 +216,15 @@ int osb_set_graphs(osb_ctx* ctx, int enable);
  * 5 = 48 points. */
 int osb_set_variant(osb_ctx* ctx, int variant);
 
+/* Selects how the FP32-residual path's central kernel (fused RK update) stages the raw state of
+ * its z planes: 0 (default) per-thread register loads one plane ahead, 1 bulk copies through the
+ * TMA engine (one cp.async.bulk per staged row and variable, completion on an mbarrier per slot,
+ * two planes ahead; 20-35 % slower on GB300: the OPS row pitch allows no tiled tensor map, so a
+ * plane takes 60 copies of 160 bytes).  Both give bit-identical results.  A bulk-copy wait that
+ * runs out (about 0.2 s) ends the kernel's use of the copies and makes the next osb_sync return
+ * OSB_ECUDA. */
+int osb_set_central_staging(osb_ctx* ctx, int bulk);
+
 /* Stage schedule.  OSB_SCHED_PER_BLOCK runs every block's sweeps, RK update and boundary
  * kernels as separate launches; OSB_SCHED_PERSISTENT runs one fused persistent launch per RK
  * stage over all blocks (FP32-residual path, 2D fully periodic blocks with the characteristic

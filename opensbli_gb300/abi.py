@@ -213,6 +213,7 @@ def load_library():
     lib.osb_sync.argtypes = [vp, i32]
     lib.osb_set_graphs.argtypes = [vp, i32]
     lib.osb_set_variant.argtypes = [vp, i32]
+    lib.osb_set_central_staging.argtypes = [vp, i32]
     lib.osb_launch_count.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong)]
     lib.osb_get_stream.argtypes = [vp, ctypes.POINTER(vp)]
     lib.osb_desc_layout.argtypes = [ctypes.POINTER(ctypes.c_longlong), i32]
@@ -242,7 +243,7 @@ def check(lib, rc, what):
 # Exported symbols the header declares (checked by the CPU tests without a GPU).
 EXPORTED = ["osb_version", "osb_last_error", "osb_ctx_create", "osb_ctx_destroy", "osb_block_add",
             "osb_set_rk", "osb_step", "osb_step_requests", "osb_stage", "osb_apply_bc", "osb_residual", "osb_reduce",
-            "osb_sync", "osb_set_graphs", "osb_set_variant", "osb_launch_count", "osb_get_stream",
+            "osb_sync", "osb_set_graphs", "osb_set_variant", "osb_set_central_staging", "osb_launch_count", "osb_get_stream",
             "osb_desc_layout", "osb_timing", "osb_timing_report", "osb_stage_noalloc", "osb_set_schedule",
             "osb_get_schedule", "osb_metrics"]
 

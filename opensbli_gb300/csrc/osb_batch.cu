@@ -157,11 +157,7 @@ __global__ void __launch_bounds__(BTHREADS) k_batch2d(const BatchBlock* __restri
         float h = __fadd_rn(p1, e1);
         float l = __fsub_rn(e1, __fsub_rn(h, p1));
         ff_add(h, l, p2, e2);
-        // dt * residual as a float-float product, one conversion (as rk_point_ff)
-        const float pp = __fmul_rn(h, dt_h);
-        float ee = __fmaf_rn(h, dt_h, -pp);
-        ee = __fmaf_rn(h, dt_l, __fmaf_rn(l, dt_h, ee));
-        const double x = f2d_exact(pp) + f2d_exact(ee);
+        const double x = dt_residual(h, l, dt_h, dt_l);  // as rk_point_ff
         double q = bk.q[v][id];
         double o;
         if (kind == 0) {

@@ -5,11 +5,12 @@
 namespace osb {
 namespace {
 
-template <typename T, int CONV, int VISC, bool FUSE, int CY>
+template <typename T, int CONV, int VISC, bool FUSE, int CY, bool BULK>
 int launch_central_k(osb_ctx* c, Block& bl, int first, const RkFuse& rf) {
   using Fd = CentralFields<T, CONV, VISC>;
   size_t smem = (size_t)Fd::N * CRING * CTile<CY>::CPL * sizeof(T);
-  auto kern = k_central3d<T, CONV, VISC, FUSE, CY>;
+  if (BULK) smem += CTile<CY>::RAW * sizeof(float) + 2 * sizeof(unsigned long long);
+  auto kern = k_central3d<T, CONV, VISC, FUSE, CY, BULK>;
   OSB_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   CentralParams cp{};
   const osb_block_desc& d = bl.d;
@@ -48,22 +49,24 @@ int launch_central_k(osb_ctx* c, Block& bl, int first, const RkFuse& rf) {
 // block whose cross-section already gives every SM several columns (measured: 8 rows are 37 %
 // faster on the 64^3 central TGV and equal on the 256^3 TENO5 one; 4 rows are 1.4 % faster for
 // the 256^3 KGP form).  The FP64 kernels (FP64-pipe bound, a ring twice as large) keep 4 rows.
-template <typename T, int CONV, int VISC, bool FUSE>
+template <typename T, int CONV, int VISC, bool FUSE, bool BULK>
 int launch_central_h(osb_ctx* c, Block& bl, int first, const RkFuse& rf) {
   const long cols4 = (long)((bl.k.n[0] + CX - 1) / CX) * ((bl.k.n[1] + 3) / 4);
   if (sizeof(T) == 8 || (CONV == 2 && cols4 >= 2L * c->sm_count))
-    return launch_central_k<T, CONV, VISC, FUSE, 4>(c, bl, first, rf);
-  if constexpr (sizeof(T) == 4) return launch_central_k<T, CONV, VISC, FUSE, 8>(c, bl, first, rf);
+    return launch_central_k<T, CONV, VISC, FUSE, 4, BULK>(c, bl, first, rf);
+  if constexpr (sizeof(T) == 4) return launch_central_k<T, CONV, VISC, FUSE, 8, BULK>(c, bl, first, rf);
   return OSB_OK;
 }
 
-// With rf (FP32 path) the kernel applies the RK update instead of storing the residual.
+// With rf (FP32 path) the kernel applies the RK update instead of storing the residual; its
+// planes come in by register loads or, after osb_set_central_staging(1), by bulk copies.
 template <typename T, int CONV, int VISC>
 int launch_central_t(osb_ctx* c, Block& bl, int first, const RkFuse* rf) {
   if constexpr (sizeof(T) == 4) {
-    if (rf) return launch_central_h<T, CONV, VISC, true>(c, bl, first, *rf);
+    if (rf && c->central_bulk) return launch_central_h<T, CONV, VISC, true, true>(c, bl, first, *rf);
+    if (rf) return launch_central_h<T, CONV, VISC, true, false>(c, bl, first, *rf);
   }
-  return launch_central_h<T, CONV, VISC, false>(c, bl, first, RkFuse{});
+  return launch_central_h<T, CONV, VISC, false, false>(c, bl, first, RkFuse{});
 }
 
 template <typename T>

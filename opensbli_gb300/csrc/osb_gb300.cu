@@ -848,6 +848,7 @@ int stage(osb_ctx* c, int s, double dt, bool bc = true) {
       rf.B = c->B[s];
       rf.dt = dt;
       rf.bad = c->bad;
+      rf.stall = c->bad + 1;
       float* out = c->qf_parity ? bl.qf_base : bl.qf_alt;
       for (int v = 0; v < bl.d.ndim + 2; ++v) rf.qout[v] = out + (size_t)v * bl.k.alloc;
       bool fused = false;
@@ -1117,9 +1118,9 @@ int osb_ctx_create(int device, int precision, osb_ctx** out) {
   if (e != cudaSuccess) { delete c; return fail(OSB_ECUDA, "stream: %s", cudaGetErrorString(e)); }
   c->red_slots = c->sm_count * 8 + 1;
   e = cudaMalloc(&c->red, sizeof(double) * (c->red_slots + 8) * 64);
-  if (e == cudaSuccess) e = cudaMalloc(&c->bad, sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMalloc(&c->bad, 2 * sizeof(unsigned long long));
   if (e == cudaSuccess) e = cudaMallocHost(&c->red_host, sizeof(double) * 8);
-  if (e == cudaSuccess) e = cudaMemset(c->bad, 0, sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMemset(c->bad, 0, 2 * sizeof(unsigned long long));
   if (e != cudaSuccess) {
     osb_ctx_destroy(c);
     return fail(OSB_ECUDA, "workspace: %s", cudaGetErrorString(e));
@@ -1595,11 +1596,13 @@ int osb_sync(osb_ctx* c, int timeout_ms) {
     if (timeout_ms >= 0 && ms > timeout_ms) return fail(OSB_ETIMEDOUT, "stream not idle after %d ms", timeout_ms);
     std::this_thread::sleep_for(std::chrono::microseconds(50));
   }
-  unsigned long long bad = 0;
-  OSB_CK(cudaMemcpy(&bad, c->bad, sizeof bad, cudaMemcpyDeviceToHost));
-  if (bad) {
+  unsigned long long bad[2] = {0, 0};
+  OSB_CK(cudaMemcpy(bad, c->bad, sizeof bad, cudaMemcpyDeviceToHost));
+  if (bad[0] || bad[1]) {
     OSB_CK(cudaMemset(c->bad, 0, sizeof bad));
-    return fail(OSB_ENAN, "%llu non-finite values produced by the RK update", bad);
+    if (bad[1])
+      return fail(OSB_ECUDA, "%llu thread blocks of the central kernel gave up waiting for their bulk copies", bad[1]);
+    return fail(OSB_ENAN, "%llu non-finite values produced by the RK update", bad[0]);
   }
   return OSB_OK;
 }
@@ -1641,6 +1644,14 @@ int osb_get_schedule(osb_ctx* c, int* mode_out, osb_schedule* sched_out) {
 int osb_set_variant(osb_ctx* c, int variant) {
   if (!c) return fail(OSB_EINVAL, "null ctx");
   c->variant = variant;
+  drop_graph(c);
+  return OSB_OK;
+}
+
+int osb_set_central_staging(osb_ctx* c, int bulk) {
+  if (!c) return fail(OSB_EINVAL, "null ctx");
+  if (bulk != 0 && bulk != 1) return fail(OSB_EINVAL, "central staging %d (0 register loads, 1 bulk copies)", bulk);
+  c->central_bulk = bulk;
   drop_graph(c);
   return OSB_OK;
 }

@@ -70,10 +70,11 @@ struct osb_ctx {
   long long g_kernels = 0;
   double* red = nullptr;              // device reduction partials (+ final slot)
   double* red_host = nullptr;         // pinned
-  unsigned long long* bad = nullptr;  // non-finite counter
+  unsigned long long* bad = nullptr;  // [0] non-finite values, [1] staging waits that ran out
   int red_slots = 0;
   long long launches = 0;
   int variant = -1;
+  int central_bulk = 0;  // FP32 central kernel: raw planes by register loads (0) or bulk copies (1)
   int sm_count = 152;
   bool timing = false;                    // per-kernel CUDA-event timing (graphs bypassed)
   std::vector<osb::TimedEvent> events;    // pending timed launches

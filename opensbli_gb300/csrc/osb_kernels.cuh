@@ -259,18 +259,26 @@ struct RkFuse {
   float dt_h, dt_l;  // dt as a float-float pair
   float* qout[5];
   unsigned long long* bad;
+  unsigned long long* stall;  // bulk-staging waits that ran out (k_central3d BULK)
 };
 
-// RK update of one variable from the float-float residual (h, l): dt * (h + l) is formed as a
-// float-float product (exact TwoProduct plus the cross terms, relative error ~2^-48, the
-// precision of the residual itself) and converted once, so the update costs three FP64
-// operations (two on the first low-storage stage) instead of four.
+// The increment dt * R of the FP32-residual path's RK update, from the float-float residual
+// (h, l) and dt as a float-float pair: the cross terms h dt_l + l dt_h (relative size 2^-24,
+// formed to ~2^-48) are added to h dt_h by one FMA, so the result is dt (h + l) rounded once
+// to FP32, |error| <= 2^-24 |dt R| (plus ~2^-47), then widened exactly with integer operations.
+// The single rounding is below the residual's own FP32 error: each flux difference in R
+// carries ~2^-24 of the flux, and |R| is at most the flux differences it sums.  An FP64
+// addition of the pair's two parts would cost more than the two FMAs of the update itself
+// on GB300's FP64 pipe.
+__device__ __forceinline__ double dt_residual(float h, float l, float dt_h, float dt_l) {
+  return f2d_exact(__fmaf_rn(h, dt_h, __fmaf_rn(h, dt_l, __fmul_rn(l, dt_h))));
+}
+
+// RK update of one variable from the float-float residual (h, l) with x = dt_residual: two
+// FP64 FMAs, the register and the state (rk_LS.py:204-215; rk_sbli.py:138-145).
 __device__ __forceinline__ unsigned rk_point_ff(const BlockK& b, const RkFuse& rf, int v, int id, float h, float l,
                                                 double q, double o) {
-  const float p = __fmul_rn(h, rf.dt_h);
-  float e = __fmaf_rn(h, rf.dt_h, -p);
-  e = __fmaf_rn(h, rf.dt_l, __fmaf_rn(l, rf.dt_h, e));
-  const double x = f2d_exact(p) + f2d_exact(e);  // dt * residual
+  const double x = dt_residual(h, l, rf.dt_h, rf.dt_l);
   if (rf.kind == 0) {
     o = rf.a_zero ? x : __fma_rn(rf.A, o, x);
     q = __fma_rn(rf.B, o, q);
@@ -279,6 +287,17 @@ __device__ __forceinline__ unsigned rk_point_ff(const BlockK& b, const RkFuse& r
     o = __fma_rn(rf.B, x, o);
   }
   b.rk[v][id] = o;
+  b.q[v][id] = q;
+  rf.qout[v][id] = d2f_rn(q);
+  return ((((unsigned)__double2hiint(q) >> 20) & 0x7ffu) == 0x7ffu) ? 1u : 0u;
+}
+// The first low-storage stage (A = 0): the register becomes x, one FP64 FMA.  Callers take
+// this path under a uniform branch; the select in rk_point_ff gives the same values.
+__device__ __forceinline__ unsigned rk_point_a0(const BlockK& b, const RkFuse& rf, int v, int id, float h, float l,
+                                                double q) {
+  const double x = dt_residual(h, l, rf.dt_h, rf.dt_l);
+  q = __fma_rn(rf.B, x, q);
+  b.rk[v][id] = x;
   b.q[v][id] = q;
   rf.qout[v][id] = d2f_rn(q);
   return ((((unsigned)__double2hiint(q) >> 20) & 0x7ffu) == 0x7ffu) ? 1u : 0u;
@@ -622,7 +641,7 @@ __device__ __forceinline__ double cpar<double>(double d, float) { return d; }
 template <>
 __device__ __forceinline__ float cpar<float>(double, float f) { return f; }
 
-// A CTA owns a 32 x 4 column of points and streams it through czc planes of z (a launch
+// A CTA owns a 32 x CY column of points and streams it through czc planes of z (a launch
 // argument, chosen on the host so the CTAs fill whole waves): the planes
 // z-2 .. z+2 around the current one sit in a 5-plane ring in shared memory (halo 2 in x and y,
 // edges included), the raw state of plane z+3 is loaded into registers while plane z is
@@ -630,14 +649,67 @@ __device__ __forceinline__ float cpar<float>(double, float f) { return f; }
 // The tile height CY is a template argument: 8 rows stage fewer halo points per computed point
 // (36 x 12 / 256 against 36 x 8 / 128) and give small blocks more threads per column, 4 rows keep
 // the shared-memory ring small when it holds many fields (the KGP form with viscous terms).
+// BULK (FP32 state only): the raw planes come in through the bulk-copy (TMA) engine instead --
+// one cp.async.bulk per staged row and variable into a two-slot raw buffer in shared memory,
+// completion counted on an mbarrier per slot, two planes ahead of the computed one.  The OPS
+// row pitch (n + 10 elements) is not a multiple of 16 bytes, which a tiled tensor map needs,
+// so each row copy starts at the 16-byte boundary at or below the row's first staged element
+// and moves CRW elements; the lead (0..3 elements) is recomputed by the reading thread.
 constexpr int CX = 32, CH = 2, CRING = 5;
 constexpr int CSX = CX + 2 * CH;
+constexpr int CRW = 40;  // elements per bulk row copy: CSX plus a lead of up to 3, in 16-byte units
 template <int CY>
 struct CTile {
   static constexpr int CSY = CY + 2 * CH;
   static constexpr int CPL = CSX * CSY;                        // points of one staged plane
   static constexpr int CPP = (CPL + CX * CY - 1) / (CX * CY);  // staged points per thread and plane
+  static constexpr int RAW = 2 * 5 * CSY * CRW;                // floats of the two raw plane slots
 };
+
+// ---- bulk-copy (TMA) staging: mbarrier and cp.async.bulk wrappers ----
+__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_init_fence() { asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory"); }
+__device__ __forceinline__ void mbar_arrive_expect(unsigned long long* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_test(unsigned long long* bar, unsigned parity) {
+  unsigned done;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, 1000;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(done)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;\n" : "=l"(t));
+  return t;
+}
+// Waits for the phase of the given parity to complete; gives up after about 0.2 s (false).
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity) {
+  if (mbar_test(bar, parity)) return true;
+  const unsigned long long t0 = global_ns();
+  for (int i = 0; i < (1 << 22); ++i) {
+    if (mbar_test(bar, parity)) return true;
+    if (global_ns() - t0 > 200000000ull) return false;
+  }
+  return false;
+}
+// Orders this thread's earlier generic-proxy accesses of shared memory before its later bulk
+// copies into it.
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
+// Global -> shared bulk copy of `bytes` (16-byte aligned addresses, a multiple of 16 bytes),
+// counted on mbarrier `bar`.
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                   smem_addr(dst)),
+               "l"(src), "r"(bytes), "r"(smem_addr(bar))
+               : "memory");
+}
 
 template <typename T, int CONV, int VISC>
 struct CentralFields {
@@ -648,13 +720,26 @@ struct CentralFields {
   static constexpr int N = CONV ? (VISC ? 11 : 9) : 6;
 };
 
-template <typename T, int CONV, int VISC, bool FUSE, int CY>
-__global__ void __launch_bounds__(CX * CY) k_central3d(BlockK b, CentralParams cp, int first, int czc, RkFuse rf) {
-  constexpr int CPL = CTile<CY>::CPL, CPP = CTile<CY>::CPP;
+// BULK: at least as many CTAs per SM as its shared memory (ring, raw slots, mbarriers; 228 KB per
+// SM, 1 KB reserved per CTA) admits, so the register allocation does not lower the occupancy.
+// Without BULK the minimum is 0 (none declared): an explicit 1 lets the compiler spend twice the
+// registers at half the occupancy.
+template <int NF, int CY, bool BULK>
+constexpr int bulk_ctas() {
+  return BULK ? (228 * 1024) / (NF * CRING * CTile<CY>::CPL * 4 + CTile<CY>::RAW * 4 + 16 + 1024) : 0;
+}
+template <typename T, int CONV, int VISC, bool FUSE, int CY, bool BULK = false>
+__global__ void __launch_bounds__(CX * CY, bulk_ctas<CentralFields<T, CONV, VISC>::N, CY, BULK>()) k_central3d(BlockK b, CentralParams cp, int first, int czc, RkFuse rf) {
+  static_assert(!BULK || (sizeof(T) == 4 && FUSE), "bulk staging: FP32 state, fused update (error counter)");
+  constexpr int CPL = CTile<CY>::CPL, CPP = CTile<CY>::CPP, CSY = CTile<CY>::CSY;
   using Fd = CentralFields<T, CONV, VISC>;
   constexpr int FS = CRING * CPL;  // field stride in shared memory
   extern __shared__ __align__(16) unsigned char osb_smem[];
   T* sm = reinterpret_cast<T*>(osb_smem);
+  // BULK: raw plane slots after the ring (16-byte aligned: FS * 4 bytes is a multiple of 16),
+  // then one mbarrier per slot
+  float* raw = reinterpret_cast<float*>(sm + Fd::N * FS);
+  unsigned long long* bar = reinterpret_cast<unsigned long long*>(raw + CTile<CY>::RAW);
   const int tx = threadIdx.x % CX, ty = threadIdx.x / CX;
   const int x0 = blockIdx.x * CX, y0 = blockIdx.y * CY;
   const int zb = blockIdx.z * czc, ze = min(b.n[2], zb + czc);
@@ -708,12 +793,99 @@ __global__ void __launch_bounds__(CX * CY) k_central3d(BlockK b, CentralParams c
     }
   };
   auto slot_of = [](int gz) { return (gz + 2 * CRING) % CRING; };
-  // prologue: planes zb-2 .. zb+1 into the ring, plane zb+2 into registers
-  for (int gz = zb - CH; gz < zb + CH; ++gz) {
-    load_plane(gz);
-    store_plane(slot_of(gz));
+  // BULK: plane gz goes to raw slot (gz - zb + CH) & 1 and completes that slot's phase of
+  // parity ((gz - zb + CH) >> 1) & 1; rows past y = n1 + CH are not copied.  A wait that runs
+  // out marks the CTA broken (uniformly, through the next barrier): it issues no further copies,
+  // counts the event in *rf.stall, and before returning waits (bounded) for the copies it issued.
+  const int nrow = min(CSY, b.n[1] + 2 * CH + 1 - y0);
+  bool broken = false;
+  unsigned pend = 0, ppar = 0;  // raw slots with a copy in flight no wait has seen complete, its parity
+  auto rslot = [&](int gz) { return (gz - zb + CH) & 1; };
+  auto rpar = [&](int gz) { return (unsigned)((gz - zb + CH) >> 1) & 1u; };
+  // The copies of a plane are spread over lanes 0..7 of every warp (one warp issuing all of them
+  // measured 10 % slower); thread 0 arms the slot's next phase (arrive + expected bytes) as soon
+  // as its wait saw the previous one complete, so the copies need no extra barrier.
+  const unsigned plane_bytes = (unsigned)(nrow * 5 * CRW * 4);
+  auto issue = [&](int gz) {  // the bookkeeping is uniform
+    if (!BULK || broken || gz > ze + CH - 1) return;
+    const int s = rslot(gz);
+    pend |= 1u << s;
+    ppar = (ppar & ~(1u << s)) | (rpar(gz) << s);
+    const int lane = threadIdx.x & 31;
+    if (lane >= 8) return;
+    fence_async_smem();
+    for (int c = (threadIdx.x >> 5) * 8 + lane; c < 5 * nrow; c += CY * 8) {
+      const int v = c / nrow, r = c - v * nrow;
+      const float* src = b.qf[v] + lin(b, x0 - CH, y0 - CH + r, gz);
+      const float* al = reinterpret_cast<const float*>(reinterpret_cast<size_t>(src) & ~(size_t)15);
+      bulk_copy_g2s(raw + ((s * 5 + v) * CSY + r) * CRW, al, CRW * 4, &bar[s]);
+    }
+  };
+  // the 16-byte phase (0..3 elements) of each variable's array, two bits per variable: a row
+  // copy's lead is that phase plus the row's linear index, mod 4
+  unsigned phase = 0;
+  if constexpr (BULK) {
+#pragma unroll
+    for (int v = 0; v < 5; ++v) phase |= (unsigned)((reinterpret_cast<size_t>(b.qf[v]) >> 2) & 3) << (2 * v);
   }
-  load_plane(zb + CH);
+  // raw plane gz from its slot into the registers of the staged points (waits for the copy)
+  auto fetch_plane = [&](int gz) -> int {
+    const int s = rslot(gz);
+    int late = 0;
+    if (!broken) {
+      late = mbar_wait_bounded(&bar[s], rpar(gz)) ? 0 : 1;
+      if (!late) pend &= ~(1u << s);
+      if (!late && threadIdx.x == 0 && gz + 2 <= ze + CH - 1) mbar_arrive_expect(&bar[s], plane_bytes);
+    }
+#pragma unroll
+    for (int u = 0; u < CPP; ++u) {
+      const int idx = threadIdx.x + u * CX * CY;
+      const int ry = idx / CSX, cx = idx % CSX;
+      if (idx < CPL && x0 - CH + cx <= b.n[0] + CH && y0 - CH + ry <= b.n[1] + CH) {
+        const unsigned rl = (unsigned)lin(b, x0 - CH, y0 - CH + ry, gz);
+        const float* rrow = raw + (s * 5 * CSY + ry) * CRW + cx;
+#pragma unroll
+        for (int v = 0; v < 5; ++v) qv[u][v] = rrow[v * CSY * CRW + (int)(((phase >> (2 * v)) + rl) & 3u)];
+      }
+    }
+    return late;
+  };
+  // the barrier after a staged plane; BULK: also makes `broken` uniform
+  auto plane_barrier = [&](int late) {
+    if constexpr (BULK) {
+      const bool was = broken;
+      broken = __syncthreads_or(late) != 0 || was;
+      if (broken && !was && threadIdx.x == 0) atomicAdd(rf.stall, 1ull);
+    } else {
+      __syncthreads();
+    }
+  };
+  if constexpr (BULK) {
+    if (threadIdx.x == 0) {
+      mbar_init(&bar[0], 1);
+      mbar_init(&bar[1], 1);
+      mbar_init_fence();
+      mbar_arrive_expect(&bar[0], plane_bytes);  // planes zb-2 and zb-1
+      mbar_arrive_expect(&bar[1], plane_bytes);
+    }
+    __syncthreads();
+    issue(zb - CH);
+    issue(zb - CH + 1);
+    // prologue: planes zb-2 .. zb+1 into the ring, each slot refilled two planes ahead
+    for (int gz = zb - CH; gz < zb + CH; ++gz) {
+      const int late = fetch_plane(gz);
+      store_plane(slot_of(gz));
+      plane_barrier(late);
+      issue(gz + 2);
+    }
+  } else {
+    // prologue: planes zb-2 .. zb+1 into the ring, plane zb+2 into registers
+    for (int gz = zb - CH; gz < zb + CH; ++gz) {
+      load_plane(gz);
+      store_plane(slot_of(gz));
+    }
+    load_plane(zb + CH);
+  }
   const int gx = x0 + tx, gy = y0 + ty;
   const bool active = gx < b.n[0] && gy < b.n[1];
   const T id0 = cpar<T>(cp.invd[0], cp.invd_f[0]), id1 = cpar<T>(cp.invd[1], cp.invd_f[1]),
@@ -725,9 +897,16 @@ __global__ void __launch_bounds__(CX * CY) k_central3d(BlockK b, CentralParams c
   const int sx = 1, sy = CSX, sz = CPL;
   const int cxy = (ty + CH) * CSX + (tx + CH);
   for (int gz = zb; gz < ze; ++gz) {
-    store_plane(slot_of(gz + CH));  // plane gz+2, loaded during the previous iteration
-    __syncthreads();
-    if (gz + CH + 1 < ze + CH) load_plane(gz + CH + 1);
+    if constexpr (BULK) {
+      const int late = fetch_plane(gz + CH);  // copied during iteration gz - 2
+      store_plane(slot_of(gz + CH));
+      plane_barrier(late);
+      issue(gz + CH + 2);
+    } else {
+      store_plane(slot_of(gz + CH));  // plane gz+2, loaded during the previous iteration
+      __syncthreads();
+      if (gz + CH + 1 < ze + CH) load_plane(gz + CH + 1);
+    }
     int pbase[2 * CH + 1];
 #pragma unroll
     for (int k = 0; k <= 2 * CH; ++k) pbase[k] = slot_of(gz + k - CH) * CPL;
@@ -916,11 +1095,20 @@ __global__ void __launch_bounds__(CX * CY) k_central3d(BlockK b, CentralParams c
     if constexpr (FUSE) {
       // a first (only) residual kernel starts from zero; otherwise from the partial residual
       unsigned nb = 0;
+      if (rf.kind == 0 && rf.a_zero) {  // uniform: the first low-storage stage, one FMA per variable
 #pragma unroll
-      for (int v = 0; v < 5; ++v) {
-        float h = first ? racc[v] : oh[v], l = first ? 0.f : ol[v];
-        if (!first && v >= v0) rp_final(racc[v], h, l);
-        nb += rk_point_ff(b, rf, v, gid, h, l, fq[v], fo[v]);
+        for (int v = 0; v < 5; ++v) {
+          float h = first ? racc[v] : oh[v], l = first ? 0.f : ol[v];
+          if (!first && v >= v0) rp_final(racc[v], h, l);
+          nb += rk_point_a0(b, rf, v, gid, h, l, fq[v]);
+        }
+      } else {
+#pragma unroll
+        for (int v = 0; v < 5; ++v) {
+          float h = first ? racc[v] : oh[v], l = first ? 0.f : ol[v];
+          if (!first && v >= v0) rp_final(racc[v], h, l);
+          nb += rk_point_ff(b, rf, v, gid, h, l, fq[v], fo[v]);
+        }
       }
       if (nb) atomicAdd(rf.bad, (unsigned long long)nb);
     } else if (first) {
@@ -932,6 +1120,13 @@ __global__ void __launch_bounds__(CX * CY) k_central3d(BlockK b, CentralParams c
     }
     }  // active
     __syncthreads();  // the next iteration overwrites the slot of plane gz-2
+  }
+  if constexpr (BULK) {
+    // only a broken CTA can end with copies in flight: wait for them (bounded) before its
+    // shared memory is released
+#pragma unroll
+    for (int s2 = 0; s2 < 2; ++s2)
+      if (pend & (1u << s2)) mbar_wait_bounded(&bar[s2], (ppar >> s2) & 1u);
   }
 }
 

@@ -70,9 +70,9 @@ __device__ void bc_1d(double* q, int E, int h, int N, const Resident1D& r) {
 
 // T = double: the FP64 path.  T = float: the FP32-residual path -- the state and RK register
 // stay FP64 in shared memory next to an FP32 copy of the state; the fluxes come from the FP32
-// copy, the residual is the compensated (float-float) flux difference and the update forms
-// dt x residual as a float-float product and applies it in FP64, as the fused RK epilogue of
-// the per-block path does.
+// copy, the residual is the compensated (float-float) flux difference and the update takes
+// dt x residual rounded once to FP32 (dt_residual) and applies it with FP64 FMAs, as the fused
+// RK epilogue of the per-block path does.
 template <typename T, int SCH, int AVG>
 __global__ void __launch_bounds__(RT) k_resident_1d(const Resident1D* __restrict__ blocks, SchemeParams spd, RkCoef rk,
                                                     double dt, int nsteps, unsigned long long* bad) {
@@ -143,10 +143,7 @@ __global__ void __launch_bounds__(RT) k_resident_1d(const Resident1D* __restrict
             ff_flux_diff((float)F[id], (float)F[id - 1], invd_f, p, pe);
             const float hh = __fadd_rn(p, pe);
             const float ll = __fsub_rn(pe, __fsub_rn(hh, p));
-            const float pp = __fmul_rn(hh, dt_h);
-            float e = __fmaf_rn(hh, dt_h, -pp);
-            e = __fmaf_rn(hh, dt_l, __fmaf_rn(ll, dt_h, e));
-            const double x = f2d_exact(pp) + f2d_exact(e);  // dt * residual
+            const double x = dt_residual(hh, ll, dt_h, dt_l);  // as rk_point_ff
             if (rk.kind == 0) {
               ov = a_zero ? x : __fma_rn(A, ov, x);
               qv = __fma_rn(B, ov, qv);

@@ -5,12 +5,15 @@ quick checks; the throughput measurement with its roofline and baselines is benc
     python -m opensbli_gb300.run curv4 --xy-scale 2 --precision fp32 --steps 1
     python -m opensbli_gb300.run kh --count 16 --steps 1
     python -m opensbli_gb300.run sod --precision fp64 --steps 50
+    python -m opensbli_gb300.run tgv --size 160 --central-staging 1 --steps 1
 
 tgv: the supersonic TGV (TENO5, Roe average, central viscous terms) at --size^3, dt 1e-3;
 curv4: the 4-block curvilinear case with its x and y sizes divided by --xy-scale;
 kh: the first --count instances of the seeded KH ensemble on the persistent stage;
 sod: the 400-point Sod tube (one osb_step call, the resident path).
-Graphs are off and the FP32 per-block path applies the RK update in its last kernel.
+Graphs are off and the FP32 per-block path applies the RK update in its last kernel, whose
+central kernel stages its planes by register loads (--central-staging 0, the default) or bulk
+copies (1).
 """
 import argparse
 import sys
@@ -43,12 +46,14 @@ def main(argv=None):
     ap.add_argument("--count", type=int, default=16)
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--steps", type=int, default=1)
+    ap.add_argument("--central-staging", type=int, default=0, choices=[0, 1])
     args = ap.parse_args(argv)
     blocks, dt, sched = build(args)
     precision = "fp32" if args.workload == "kh" else args.precision
     s = Solver(blocks, precision=precision, rk="ls3", graphs=False)
     if sched is not None:
         s.set_schedule(**sched)
+    s.set_central_staging(args.central_staging)
     s.apply_bc()
     s.step(dt, args.steps)
     s.sync()

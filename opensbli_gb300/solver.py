@@ -114,6 +114,10 @@ class Solver:
         """Tiling variant of the x reconstruction sweep (osb_set_variant)."""
         abi.check(self.lib, self.lib.osb_set_variant(self.ctx, int(variant)), "osb_set_variant")
 
+    def set_central_staging(self, bulk):
+        """Plane staging of the FP32 central kernel: bulk copies (1) or register loads (0)."""
+        abi.check(self.lib, self.lib.osb_set_central_staging(self.ctx, int(bulk)), "osb_set_central_staging")
+
     def schedule(self):
         """(resolved mode, settings dict) of osb_get_schedule."""
         mode = ctypes.c_int()
