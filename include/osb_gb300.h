@@ -70,6 +70,14 @@ extern "C" {
 #define OSB_BC_PRESSURE_OUTLET 7 /* PressureOutletBC (pressure_outlet.py:35-51), Cartesian: the
                                 boundary plane and its halo layers take rho and momentum of the
                                 point inside, rhoE from osb_block_desc.back_pressure */
+#define OSB_BC_ISOTHERMAL_WALL 8 /* IsothermalWallBC (isothermal_wall.py:62-131) with the wall
+                                energy rhoE = Twall rho / (gama Minf^2 (gama - 1)), Twall from
+                                osb_block_desc.wall_temperature: no-slip wall plane, halo layer
+                                k with T = (k+1) Twall - k T(inside), the wall pressure and the
+                                mirrored velocity of the point k inside; the central derivatives
+                                of the viscous terms take the one-sided Carpenter closures at the
+                                four points next to the wall (Carpenter_scheme.py).  3D
+                                Cartesian blocks, walls on y faces, shock-capturing schemes. */
 
 /* Convective split form of OSB_SCHEME_CENTRAL4 (physical_models/split_forms.py). */
 #define OSB_SPLIT_FEIEREISEN 0 /* skew-symmetric form, split_forms.py:111-145 */
@@ -144,6 +152,7 @@ typedef struct osb_block_desc {
   const double* dirichlet[3][2];
   int32_t flux_type;         /* OSB_FLUX_* of the shock-capturing schemes (0 = LLF) */
   double back_pressure[3][2]; /* OSB_BC_PRESSURE_OUTLET face (d, side): its back pressure */
+  double wall_temperature[3][2]; /* OSB_BC_ISOTHERMAL_WALL face (d, side): Twall */
 } osb_block_desc;
 
 /* ---- library / context ------------------------------------------------------------- */

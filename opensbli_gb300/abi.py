@@ -37,6 +37,7 @@ BC_EXTRAP1 = 4
 BC_SYMMETRY = 5
 BC_DIRICHLET = 6
 BC_PRESSURE_OUTLET = 7
+BC_ISOTHERMAL_WALL = 8
 SPLIT_FEIEREISEN = 0
 SPLIT_KGP = 1
 FILTER_NONE = 0
@@ -116,6 +117,7 @@ class BlockDesc(ctypes.Structure):
         ("dirichlet", (ctypes.c_void_p * 2) * 3),
         ("flux_type", ctypes.c_int32),
         ("back_pressure", (ctypes.c_double * 2) * 3),
+        ("wall_temperature", (ctypes.c_double * 2) * 3),
     ]
 
 
@@ -124,7 +126,8 @@ def layout_signature():
     offs = [BlockDesc.size.offset, BlockDesc.bc.offset, BlockDesc.iface.offset, BlockDesc.gama.offset,
             BlockDesc.delta.offset, BlockDesc.q.offset, BlockDesc.rkold.offset, BlockDesc.metric.offset,
             BlockDesc.split_form.offset, BlockDesc.ducros_check.offset, BlockDesc.tvd_kappa.offset,
-            BlockDesc.dirichlet.offset, BlockDesc.flux_type.offset, BlockDesc.back_pressure.offset]
+            BlockDesc.dirichlet.offset, BlockDesc.flux_type.offset, BlockDesc.back_pressure.offset,
+            BlockDesc.wall_temperature.offset]
     return [ctypes.sizeof(BlockDesc)] + offs
 
 
@@ -163,6 +166,8 @@ def make_desc(spec, q_ptrs, rk_ptrs, metric_ptrs=None, dirichlet_ptrs=None):
     d.flux_type = spec.flux_type
     for (i, side), bp in (spec.back_pressure or {}).items():
         d.back_pressure[i][side] = bp
+    for (i, side), tw in (spec.wall_temperature or {}).items():
+        d.wall_temperature[i][side] = tw
     for v, p in enumerate(q_ptrs):
         d.q[v] = p
     for v, p in enumerate(rk_ptrs):

@@ -200,6 +200,11 @@ def _bcs_of(block, central_only):
                 bc[d][side] = abi.BC_PRESSURE_OUTLET
                 hv = b.get_halo_values(block)
                 depth[d][side] = abs(hv[d][side])
+            elif type(b).__name__ == "IsothermalWallBC":
+                # isothermal_wall.py:62-131; its wall energy equation is read by wall_temperature
+                bc[d][side] = abi.BC_ISOTHERMAL_WALL
+                hv = b.get_halo_values(block)
+                depth[d][side] = abs(hv[d][side])
             elif type(b).__name__ == "SharedInterfaceBC":
                 raise NotImplementedError("SharedInterfaceBC (interfaces sharing their boundary points) is not "
                                           "implemented; InterfaceBC is")
@@ -382,7 +387,48 @@ def block_spec(block, params):
                for side, b in enumerate(pair) if bc[d][side] == abi.BC_PRESSURE_OUTLET}
     if outlets:
         spec.back_pressure = outlets
+    walls = {(d, side): wall_temperature(b, spec, params) for d, pair in enumerate(block.boundary_types)
+             for side, b in enumerate(pair) if bc[d][side] == abi.BC_ISOTHERMAL_WALL}
+    if walls:
+        spec.wall_temperature = walls
     return spec
+
+
+def wall_temperature(bc, spec, params):
+    """Twall of an IsothermalWallBC whose equation sets the wall energy to
+    rhoE = Twall rho / (gama Minf^2 (gama - 1)) (the wall of the channel and SBLI apps, e.g.
+    apps/channel_flow/compressible_TCF_Central/turbulent_channel.py:118-131): the equation is
+    evaluated at two wall densities and must be that linear law; other wall equations raise."""
+    import sympy
+    from opensbli.core.opensbliobjects import DataSet, ConstantObject
+    eqs = list(bc.equations)
+    if len(eqs) != 1 or not str(getattr(eqs[0].lhs, "base", eqs[0].lhs)).startswith("rhoE"):
+        raise NotImplementedError("IsothermalWallBC: only the wall-energy equation rhoE = Twall*rho/(gama*Minf**2*"
+                                  "(gama-1)) is supported")
+    rhs = eqs[0].rhs
+    p = resolve_parameters(params)
+    rho = [a for a in rhs.atoms(DataSet) if str(a.base).split("_")[0] == "rho"]
+    other = [a for a in rhs.atoms(DataSet) if a not in rho]
+    if len(rho) != 1 or other:
+        raise NotImplementedError("IsothermalWallBC: the wall energy must depend on the wall density alone")
+
+    def at(r):  # the wall energy at wall density r (the data set first: its indices hold constants)
+        e = rhs.subs(rho[0], r)
+        return float(e.subs({a: _const_value(str(a), p) for a in e.atoms(ConstantObject)}))
+    scale = spec.gama * spec.Minf ** 2 * (spec.gama - 1.0)
+    t1 = at(1.0) * scale
+    t2 = at(2.0) * scale / 2.0
+    if not (t1 > 0.0) or abs(t1 - t2) > 1e-12 * abs(t1) or not sympy.Float(t1).is_finite:
+        raise NotImplementedError("IsothermalWallBC: the wall energy is not Twall*rho/(gama*Minf**2*(gama-1))")
+    # the value of the equation's temperature constant itself (t1 carries the rounding of the
+    # evaluation above)
+    for a in rhs.atoms(ConstantObject):
+        if str(a) in ("gama", "Minf"):
+            continue
+        v = _const_value(str(a), p, default=float("nan"))
+        if abs(v - t1) <= 1e-12 * abs(t1):
+            return float(v)
+    return t1
 
 
 def initial_state(block, spec, params):

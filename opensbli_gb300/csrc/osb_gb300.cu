@@ -394,6 +394,78 @@ __global__ void k_pressure_outlet(BlockK b, int nv, int d, int side, int depth, 
   }
 }
 
+// Isothermal no-slip wall (isothermal_wall.py:62-131 as generated for conservative variables,
+// wall energy rhoE = Twall rho / (gama Minf^2 (gama - 1))): the wall plane takes zero momentum and
+// that energy (its density stays the one the RK update gave it); with the wall pressure
+// Pw = (gama - 1) rhoE(wall) and the temperature T1 = Minf^2 gama (gama - 1) (rhoE - |rhou|^2 /
+// (2 rho)) / rho of the point next to the wall, halo layer k = 1..depth takes
+// T_k = (k+1) Twall - k T1, rho_k = Minf^2 gama Pw / T_k, momentum -rho_k u(k) and energy
+// Pw / (gama - 1) + rho_k |u(k)|^2 / 2, u(k) the velocity of the point k inside.  Over the whole
+// transverse allocation.  The FP32 shadow is filled from its own values (FP64 arithmetic on the
+// exactly widened floats, rounded once); with BC_QF alone the FP64 wall plane is reset too, so
+// the FP64 state's wall momentum and energy stay the wall's between the FP32 path's stages.
+template <typename S>
+__device__ __forceinline__ double wall_ld(const S* a, int i);
+template <>
+__device__ __forceinline__ double wall_ld<double>(const double* a, int i) { return a[i]; }
+template <>
+__device__ __forceinline__ double wall_ld<float>(const float* a, int i) { return f2d_exact(a[i]); }
+__device__ __forceinline__ void wall_st(double* a, int i, double x) { a[i] = x; }
+__device__ __forceinline__ void wall_st(float* a, int i, double x) { a[i] = d2f_rn(x); }
+
+template <typename S>
+__device__ void wall_point(S* const* q, int nd, int w, int o, int depth, double gm, double M2, double Tw) {
+  const int nv = nd + 2;
+  for (int i = 0; i < nd; ++i) wall_st(q[1 + i], w, 0.0);
+  const double Ew = __ddiv_rn(__dmul_rn(Tw, wall_ld(q[0], w)), __dmul_rn(__dmul_rn(gm, M2), __dadd_rn(gm, -1.0)));
+  wall_st(q[nv - 1], w, Ew);
+  const double pw = __dmul_rn(__dadd_rn(gm, -1.0), wall_ld(q[nv - 1], w));
+  const int a = w + o;
+  double ke = 0.0;
+  for (int i = 0; i < nd; ++i) {
+    const double m = wall_ld(q[1 + i], a);
+    ke = __dadd_rn(ke, __dmul_rn(0.5, __dmul_rn(m, m)));
+  }
+  const double ra = wall_ld(q[0], a);
+  const double Ta =
+      __ddiv_rn(__dmul_rn(__dmul_rn(__dmul_rn(M2, __dadd_rn(gm, -1.0)), __dadd_rn(wall_ld(q[nv - 1], a), -__ddiv_rn(ke, ra))), gm), ra);
+  for (int k = 1; k <= depth; ++k) {
+    const int in = w + k * o, h = w - k * o;
+    double u[3], u2 = 0.0;
+    for (int i = 0; i < nd; ++i) {
+      u[i] = __ddiv_rn(wall_ld(q[1 + i], in), wall_ld(q[0], in));
+      u2 = __dadd_rn(u2, __dmul_rn(u[i], u[i]));
+    }
+    const double Tk = __dadd_rn(__dmul_rn(-(double)k, Ta), __dmul_rn((double)(k + 1), Tw));
+    const double rk = __ddiv_rn(__dmul_rn(__dmul_rn(M2, gm), pw), Tk);
+    wall_st(q[0], h, rk);
+    for (int i = 0; i < nd; ++i) wall_st(q[1 + i], h, -__dmul_rn(rk, u[i]));
+    wall_st(q[nv - 1], h, __dadd_rn(__ddiv_rn(pw, __dadd_rn(gm, -1.0)), __dmul_rn(__dmul_rn(0.5, u2), rk)));
+  }
+}
+
+__global__ void k_isothermal_wall(BlockK b, int nv, int d, int side, int depth, int halo, double gama, double Minf,
+                                  double Tw, int fields) {
+  const int total = face_extent(b, d, halo);
+  const int base = side == 0 ? 0 : b.n[d] - 1;
+  const int o = b.st[d] * (side == 0 ? 1 : -1);  // towards the inside
+  const int nd = nv - 2;
+  const double M2 = __dmul_rn(Minf, Minf);
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+    int c[3];
+    face_point(b, d, halo, t, c);
+    c[d] = base;
+    const int w = lin(b, c[0], c[1], c[2]);
+    if (fields & BC_Q) {
+      wall_point<double>(b.q, nd, w, o, depth, gama, M2, Tw);
+    } else if (b.qf[0]) {  // FP64 wall plane only (the halos follow when the call returns)
+      for (int i = 0; i < nd; ++i) b.q[1 + i][w] = 0.0;
+      b.q[nv - 1][w] = __ddiv_rn(__dmul_rn(Tw, b.q[0][w]), __dmul_rn(__dmul_rn(gama, M2), __dadd_rn(gama, -1.0)));
+    }
+    if ((fields & BC_QF) && b.qf[0]) wall_point<float>(b.qf, nd, w, o, depth, gama, M2, Tw);
+  }
+}
+
 // Dirichlet face (dirichlet.py:27-41): the boundary plane and its `depth` halo layers take the
 // values of the BC's equations, vals[v][layer][t] (layer l at -depth + l on side 0, N-1 + l on
 // side 1), over the whole transverse allocation.
@@ -796,6 +868,14 @@ int apply_block_bc(osb_ctx* c, Block& bl, size_t ib, int fields) {
             bl.k, nv, d, side, side ? dep1 : dep0, bl.d.halo, bl.d.back_pressure[d][side], bl.d.gama, fields);
         timing_end(c);
         c->launches++;
+      } else if (kind == OSB_BC_ISOTHERMAL_WALL) {
+        const long tr = face_extent(bl.k, d, bl.d.halo);
+        timing_begin(c, FAM_BC);
+        k_isothermal_wall<<<grid_for(c, tr, 128), 128, 0, c->stream>>>(
+            bl.k, nv, d, side, side ? dep1 : dep0, bl.d.halo, bl.d.gama, bl.d.Minf, bl.d.wall_temperature[d][side],
+            fields);
+        timing_end(c);
+        c->launches++;
       } else if (kind == OSB_BC_PERIODIC) {
         return fail(OSB_EINVAL, "periodic boundary on one side only (block %zu dir %d)", ib, d);
       }
@@ -987,7 +1067,19 @@ bool check_desc(const osb_block_desc* d, std::string& why) {
   for (int i = 0; i < d->ndim; ++i)
     for (int s = 0; s < 2; ++s) {
       const int k = d->bc[i][s];
-      if (k < OSB_BC_PERIODIC || k > OSB_BC_PRESSURE_OUTLET) { why = "unknown boundary kind"; return false; }
+      if (k < OSB_BC_PERIODIC || k > OSB_BC_ISOTHERMAL_WALL) { why = "unknown boundary kind"; return false; }
+      if (k == OSB_BC_ISOTHERMAL_WALL) {
+        if (d->ndim != 3 || i != 1 || d->metric[9] || d->scheme == OSB_SCHEME_CENTRAL4) {
+          why = "isothermal walls are implemented on the y faces of 3D Cartesian blocks with a shock-capturing scheme";
+          return false;
+        }
+        if (!(d->wall_temperature[i][s] > 0.0)) { why = "an isothermal wall needs a positive wall temperature"; return false; }
+        const int wd = d->bc_depth[i][s] > 0 ? d->bc_depth[i][s] : 4;
+        if (wd > d->halo || d->size[i] < 12) {
+          why = "isothermal walls: depth up to the halo, at least 12 points between the walls";
+          return false;
+        }
+      }
       const int dep = d->bc_depth[i][s] > 0 ? d->bc_depth[i][s] : 4;
       if ((k == OSB_BC_SYMMETRY || k == OSB_BC_DIRICHLET || k == OSB_BC_PRESSURE_OUTLET) &&
           (dep > d->halo || dep >= d->size[i])) {
@@ -1083,7 +1175,7 @@ int osb_last_error(char* buf, size_t n) {
 }
 
 int osb_desc_layout(long long* out, int n) {
-  if (!out || n < 15) return fail(OSB_EINVAL, "need 15 slots");
+  if (!out || n < 16) return fail(OSB_EINVAL, "need 16 slots");
   out[0] = sizeof(osb_block_desc);
   out[1] = offsetof(osb_block_desc, size);
   out[2] = offsetof(osb_block_desc, bc);
@@ -1099,6 +1191,7 @@ int osb_desc_layout(long long* out, int n) {
   out[12] = offsetof(osb_block_desc, dirichlet);
   out[13] = offsetof(osb_block_desc, flux_type);
   out[14] = offsetof(osb_block_desc, back_pressure);
+  out[15] = offsetof(osb_block_desc, wall_temperature);
   return OSB_OK;
 }
 

@@ -633,6 +633,12 @@ struct CentralParams {
   float gama_f, M2_f, mu_c_f, invRe_f, kheat_f;
   double invd[3], inv2d[3];
   float invd_f[3], inv2d_f[3];
+  // isothermal-wall y faces (WALL kernels): low / high face present, and the one-sided
+  // closures of the first (rows 0..3, six points from m - r) and second (rows 0..1, five
+  // points) derivatives next to a wall (Carpenter_scheme.py)
+  int wall_lo, wall_hi;
+  double c1[4][6], c2[2][5];
+  float c1f[4][6], c2f[2][5];
 };
 template <typename T>
 __device__ __forceinline__ T cpar(double d, float f);
@@ -658,9 +664,9 @@ __device__ __forceinline__ float cpar<float>(double, float f) { return f; }
 constexpr int CX = 32, CH = 2, CRING = 5;
 constexpr int CSX = CX + 2 * CH;
 constexpr int CRW = 40;  // elements per bulk row copy: CSX plus a lead of up to 3, in 16-byte units
-template <int CY>
+template <int CY, int HY = CH>
 struct CTile {
-  static constexpr int CSY = CY + 2 * CH;
+  static constexpr int CSY = CY + 2 * HY;  // HY: staged rows above and below the tile
   static constexpr int CPL = CSX * CSY;                        // points of one staged plane
   static constexpr int CPP = (CPL + CX * CY - 1) / (CX * CY);  // staged points per thread and plane
   static constexpr int RAW = 2 * 5 * CSY * CRW;                // floats of the two raw plane slots
@@ -728,10 +734,15 @@ template <int NF, int CY, bool BULK>
 constexpr int bulk_ctas() {
   return BULK ? (228 * 1024) / (NF * CRING * CTile<CY>::CPL * 4 + CTile<CY>::RAW * 4 + 16 + 1024) : 0;
 }
-template <typename T, int CONV, int VISC, bool FUSE, int CY, bool BULK = false>
+// WALL: isothermal-wall y faces (cp.wall_lo / cp.wall_hi) -- the tile stages 4 rows above and
+// below instead of 2, and the y derivatives of the points next to a wall take the one-sided
+// closures (viscous terms of a shock-capturing block; CONV == 0).
+template <typename T, int CONV, int VISC, bool FUSE, int CY, bool BULK = false, bool WALL = false>
 __global__ void __launch_bounds__(CX * CY, bulk_ctas<CentralFields<T, CONV, VISC>::N, CY, BULK>()) k_central3d(BlockK b, CentralParams cp, int first, int czc, RkFuse rf) {
   static_assert(!BULK || (sizeof(T) == 4 && FUSE), "bulk staging: FP32 state, fused update (error counter)");
-  constexpr int CPL = CTile<CY>::CPL, CPP = CTile<CY>::CPP, CSY = CTile<CY>::CSY;
+  static_assert(!WALL || (CONV == 0 && !BULK), "wall closures: viscous terms of shock-capturing blocks");
+  constexpr int CHY = WALL ? 4 : CH;  // staged rows above and below the tile
+  constexpr int CPL = CTile<CY, CHY>::CPL, CPP = CTile<CY, CHY>::CPP, CSY = CTile<CY, CHY>::CSY;
   using Fd = CentralFields<T, CONV, VISC>;
   constexpr int FS = CRING * CPL;  // field stride in shared memory
   extern __shared__ __align__(16) unsigned char osb_smem[];
@@ -754,8 +765,8 @@ __global__ void __launch_bounds__(CX * CY, bulk_ctas<CentralFields<T, CONV, VISC
 #pragma unroll
     for (int u = 0; u < CPP; ++u) {
       const int idx = threadIdx.x + u * CX * CY;
-      const int gx = x0 - CH + idx % CSX, gy = y0 - CH + idx / CSX;
-      if (idx < CPL && gx <= b.n[0] + CH && gy <= b.n[1] + CH) {
+      const int gx = x0 - CH + idx % CSX, gy = y0 - CHY + idx / CSX;
+      if (idx < CPL && gx <= b.n[0] + CH && gy <= b.n[1] + CHY) {
         const int id = lin(b, gx, gy, gz);
 #pragma unroll
         for (int v = 0; v < 5; ++v) qv[u][v] = ld_q<T>(b, v, id);
@@ -767,8 +778,8 @@ __global__ void __launch_bounds__(CX * CY, bulk_ctas<CentralFields<T, CONV, VISC
 #pragma unroll
     for (int u = 0; u < CPP; ++u) {
       const int idx = threadIdx.x + u * CX * CY;
-      const int gx = x0 - CH + idx % CSX, gy = y0 - CH + idx / CSX;
-      if (!(idx < CPL && gx <= b.n[0] + CH && gy <= b.n[1] + CH)) continue;
+      const int gx = x0 - CH + idx % CSX, gy = y0 - CHY + idx / CSX;
+      if (!(idx < CPL && gx <= b.n[0] + CH && gy <= b.n[1] + CHY)) continue;
       const int at = slot * CPL + idx;
       const T rho = qv[u][0], m0 = qv[u][1], m1 = qv[u][2], m2 = qv[u][3], E = qv[u][4];
       T ir = L_(1.0) / rho;
@@ -895,7 +906,37 @@ __global__ void __launch_bounds__(CX * CY, bulk_ctas<CentralFields<T, CONV, VISC
   // offsets are written as linear offsets of a virtual (x, y, z) tile with z stride CPL and
   // decoded into (plane, in-plane) parts; they are compile-time constants after unrolling
   const int sx = 1, sy = CSX, sz = CPL;
-  const int cxy = (ty + CH) * CSX + (tx + CH);
+  const int cxy = (ty + CHY) * CSX + (tx + CH);
+  // WALL: the closure rows of this thread's point (wr1: first derivatives, rows 0..3 from a
+  // wall; wr2: second derivatives, rows 0..1; -1 the central rule), its weights with the sign of
+  // the face applied, and the y offsets m -> yb + ys m of the stencil points
+  int wr1 = -1, wr2 = -1, yb1 = 0, ys1 = 1, yb2 = 0, ys2 = 1;
+  T cw1[6], cw2[5];
+  if constexpr (WALL) {
+    const int ny = b.n[1];
+    if (gy < ny) {
+      if (cp.wall_lo && gy < 4) wr1 = gy;
+      else if (cp.wall_hi && gy > ny - 5) wr1 = 4 + (ny - 1 - gy);
+      if (cp.wall_lo && gy < 2) wr2 = gy;
+      else if (cp.wall_hi && gy > ny - 3) wr2 = 4 + (ny - 1 - gy);
+    }
+    const int r1 = wr1 & 3, r2 = wr2 & 1;
+    const bool hi1 = wr1 >= 4, hi2 = wr2 >= 4;
+    yb1 = hi1 ? r1 : -r1;
+    ys1 = hi1 ? -1 : 1;
+    yb2 = hi2 ? r2 : -r2;
+    ys2 = hi2 ? -1 : 1;
+#pragma unroll
+    for (int m = 0; m < 6; ++m) {
+      const T c = r1 == 0 ? cpar<T>(cp.c1[0][m], cp.c1f[0][m])
+                  : r1 == 1 ? cpar<T>(cp.c1[1][m], cp.c1f[1][m])
+                  : r1 == 2 ? cpar<T>(cp.c1[2][m], cp.c1f[2][m])
+                            : cpar<T>(cp.c1[3][m], cp.c1f[3][m]);
+      cw1[m] = hi1 ? -c : c;
+    }
+#pragma unroll
+    for (int m = 0; m < 5; ++m) cw2[m] = r2 == 0 ? cpar<T>(cp.c2[0][m], cp.c2f[0][m]) : cpar<T>(cp.c2[1][m], cp.c2f[1][m]);
+  }
   for (int gz = zb; gz < ze; ++gz) {
     if constexpr (BULK) {
       const int late = fetch_plane(gz + CH);  // copied during iteration gz - 2
@@ -914,13 +955,59 @@ __global__ void __launch_bounds__(CX * CY, bulk_ctas<CentralFields<T, CONV, VISC
       const int dz = (o + 2 * sz + sz / 2) / sz - 2;
       return sm[f * FS + pbase[dz + CH] + cxy + (o - dz * sz)];
     };
-    auto D1 = [&](int f, int s, T inv) -> T { return d1w<T>(F(f, -2 * s), F(f, -s), F(f, s), F(f, 2 * s)) * inv; };
-    auto D2 = [&](int f, int s, T inv) -> T { return d2w<T>(F(f, -2 * s), F(f, -s), F(f, 0), F(f, s), F(f, 2 * s)) * inv; };
-    // mixed derivative: central-4 along sb of the central-4 derivative along sa
+    // a staged value by plane offset dz and in-plane offset (the closures' y offsets reach 4 rows)
+    auto Fp = [&](int f, int dz, int ip) -> T { return sm[f * FS + pbase[dz + CH] + cxy + ip]; };
+    // closure sums of the first / second y derivative (without 1/Delta) at plane dz, x offset ox;
+    // the first-derivative row 0 has four points (its last two weights are zero and the rows
+    // beyond may not be staged)
+    auto Y1 = [&](int f, int dz, int ox) -> T {
+      T acc = L_(0.0);
+#pragma unroll
+      for (int m = 0; m < 4; ++m) acc += cw1[m] * Fp(f, dz, ox + (yb1 + ys1 * m) * sy);
+      if ((wr1 & 3) != 0) {
+#pragma unroll
+        for (int m = 4; m < 6; ++m) acc += cw1[m] * Fp(f, dz, ox + (yb1 + ys1 * m) * sy);
+      }
+      return acc;
+    };
+    auto Y2 = [&](int f) -> T {
+      T acc = L_(0.0);
+#pragma unroll
+      for (int m = 0; m < 5; ++m) acc += cw2[m] * Fp(f, 0, (yb2 + ys2 * m) * sy);
+      return acc;
+    };
+    auto D1 = [&](int f, int s, T inv) -> T {
+      if (WALL && s == sy && wr1 >= 0) return Y1(f, 0, 0) * inv;
+      return d1w<T>(F(f, -2 * s), F(f, -s), F(f, s), F(f, 2 * s)) * inv;
+    };
+    auto D2 = [&](int f, int s, T inv) -> T {
+      if (WALL && s == sy && wr2 >= 0) return Y2(f) * inv;
+      return d2w<T>(F(f, -2 * s), F(f, -s), F(f, 0), F(f, s), F(f, 2 * s)) * inv;
+    };
+    // mixed derivative: central-4 along sb of the central-4 derivative along sa (WALL: the
+    // closures where sa or sb is y; moving along sb keeps the point's row along sa)
     auto DM = [&](int f, int sa, int sb, T ia, T ib) -> T {
       const T cw[4] = {L_(1.0 / 12.0), -L_(2.0 / 3.0), L_(2.0 / 3.0), -L_(1.0 / 12.0)};
       const int off[4] = {-2, -1, 1, 2};
       T r = L_(0.0);
+      if (WALL && sb == sy && wr1 >= 0) {  // closure along y of the x (sa) derivatives
+        auto dx = [&](int dy) -> T {
+          const int o = dy * sy;
+          return d1w<T>(Fp(f, 0, o - 2 * sa), Fp(f, 0, o - sa), Fp(f, 0, o + sa), Fp(f, 0, o + 2 * sa)) * ia;
+        };
+#pragma unroll
+        for (int m = 0; m < 4; ++m) r += cw1[m] * dx(yb1 + ys1 * m);
+        if ((wr1 & 3) != 0) {
+#pragma unroll
+          for (int m = 4; m < 6; ++m) r += cw1[m] * dx(yb1 + ys1 * m);
+        }
+        return r * ib;
+      }
+      if (WALL && sa == sy && wr1 >= 0) {  // central along sb (z) of the closure y derivatives
+#pragma unroll
+        for (int m = 0; m < 4; ++m) r += cw[m] * (Y1(f, off[m] * (sb / sz), 0) * ia);
+        return r * ib;
+      }
 #pragma unroll
       for (int m = 0; m < 4; ++m) {
         int o = off[m] * sb;

@@ -75,6 +75,37 @@ def tgv(n=64, minf=0.1, scheme=abi.SCHEME_CENTRAL4, averaging=abi.AVG_SIMPLE, vi
     return spec, _cons(spec, r, [u0, u1, u2], p)
 
 
+def channel_iso(sizes=(16, 17, 8), twall=1.0, minf=0.5, re=100.0):
+    """3D channel between isothermal no-slip walls at y = -1 and y = 1 (IsothermalWallBC on both
+    y faces, Twall = `twall`), periodic in x on [0, 2pi) and z on [0, 2pi), uniform grid with the
+    walls on the first and last points in y (Delta_y = 2 / (N_y - 1)), characteristic LLF TENO5
+    (Roe average) with central-4 viscous terms (modified Sutherland law), Minf = 0.5, Re = 100:
+    the shock-capturing wall-bounded form of the SBLI apps with the walls of
+    apps/channel_flow/compressible_TCF_Central/turbulent_channel.py:118-131.  Initial state: a
+    perturbed parabolic profile, u0 = (1 - y^2)(1 + 0.1 sin x cos z), u1 = 0.05 sin x (1 - y^2)^2,
+    u2 = 0.05 cos x sin z (1 - y^2), p = (1 + 0.02 cos x cos z) / (gama Minf^2),
+    rho = 1 + 0.02 sin x y."""
+    n0, n1, n2 = sizes
+    spec = BlockSpec(ndim=3, size=sizes, scheme=abi.SCHEME_TENO5, averaging=abi.AVG_ROE,
+                     viscous=abi.VISC_SUTHERLAND,
+                     bc=[[abi.BC_PERIODIC] * 2, [abi.BC_ISOTHERMAL_WALL] * 2, [abi.BC_PERIODIC] * 2],
+                     bc_depth=[[4, 4] for _ in range(3)],
+                     delta=(2.0 * math.pi / n0, 2.0 / (n1 - 1), 2.0 * math.pi / n2), gama=1.4, Minf=minf, Re=re,
+                     Pr=0.71, mu_const=1.0, eps=1e-40, teno_ct=1e-6,
+                     wall_temperature={(1, 0): float(twall), (1, 1): float(twall)})
+    x0 = spec.delta[0] * spec.grid_index(0)
+    x1 = -1.0 + spec.delta[1] * spec.grid_index(1)
+    x2 = spec.delta[2] * spec.grid_index(2)
+    g = spec.gama
+    w = 1.0 - x1 * x1
+    u0 = w * (1.0 + 0.1 * np.sin(x0) * np.cos(x2))
+    u1 = 0.05 * np.sin(x0) * w * w
+    u2 = 0.05 * np.cos(x0) * np.sin(x2) * w
+    p = 1.0 / (g * minf * minf) * (1.0 + 0.02 * np.cos(x0) * np.cos(x2))
+    r = 1.0 + 0.02 * np.sin(x0) * x1
+    return spec, _cons(spec, r, [u0, u1, u2], p)
+
+
 def tgv_filtered(n=128, sizes=None, ducros=0.05):
     """The supersonic TGV of the reference's Central4-WENO5 benchmark
     (apps/performance_benchmark/Central4-WENO5; the central branch of

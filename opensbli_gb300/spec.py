@@ -46,6 +46,8 @@ class BlockSpec:
     flux_type: int = abi.FLUX_LLF
     # pressure-outlet faces: {(direction, side): back pressure}
     back_pressure: dict = None
+    # isothermal-wall faces: {(direction, side): wall temperature Twall}
+    wall_temperature: dict = None
     # a curvilinear block: its metric arrays (osb_block_desc.metric) must be supplied; a
     # curvilinear block without them is refused instead of being run as a Cartesian one
     curvilinear: bool = False
@@ -107,6 +109,8 @@ class BlockSpec:
                                                         for r in self.iface]
         rec["back_pressure"] = None if not self.back_pressure else [[d, s, float(v)] for (d, s), v in
                                                                      sorted(self.back_pressure.items())]
+        if self.wall_temperature:  # (absent otherwise: records of blocks without walls are unchanged)
+            rec["wall_temperature"] = [[d, s, float(v)] for (d, s), v in sorted(self.wall_temperature.items())]
         arrays = {"dirichlet_%d_%d" % k: np.ascontiguousarray(a) for k, a in (self.dirichlet or {}).items()}
         return rec, arrays
 
@@ -121,6 +125,8 @@ class BlockSpec:
             kw["iface"] = [[None if f is None else tuple(f) for f in r] for r in rec["iface"]]
         if rec.get("back_pressure"):
             kw["back_pressure"] = {(int(d), int(s)): float(v) for d, s, v in rec["back_pressure"]}
+        if rec.get("wall_temperature"):
+            kw["wall_temperature"] = {(int(d), int(s)): float(v) for d, s, v in rec["wall_temperature"]}
         dirichlet = {}
         for name, a in (arrays or {}).items():
             if name.startswith("dirichlet_"):

@@ -57,6 +57,7 @@ def oracle():
                                     P(ctypes.c_double), ctypes.c_double, ctypes.c_int]
         lib.oracle_reduce.argtypes = [P(abi.BlockDesc), ctypes.c_int, ctypes.c_int, P(ctypes.c_double)]
         lib.oracle_filter.argtypes = [P(abi.BlockDesc), ctypes.c_int, ctypes.c_double]
+        lib.oracle_carpenter.argtypes = [ctypes.c_int, ctypes.c_int, P(ctypes.c_double)]
         _olib = lib
     return _olib
 

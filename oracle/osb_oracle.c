@@ -628,31 +628,167 @@ static inline double dmix(const double* f, long id, long sa, long sb, double inv
   return acc * invb;
 }
 
+/* ---- one-sided boundary closures of the central derivatives at isothermal-wall faces ----
+ * The fourth-order closure of Carpenter, Gottlieb and Abarbanel (J. Comput. Phys. 1998,
+ * doi:10.1006/jcph.1998.6114) that Carpenter_scheme.py:91-111 forms as inv(A_L) A_R: its row r
+ * (r = 0..3, the points 0..3 next to the wall) weighs the six points r' = m - r (m = 0..5) from
+ * the wall plane; row 0 is the exact third-order one-sided rule [-11/6, 3, -3/2, 1/3] (the
+ * reference rationalises it).  The second derivative takes the two rows of
+ * Carpenter_scheme.py:79-86 at the points 0 and 1 (five points from m - r).  On the far side the
+ * rows are mirrored: offsets r - m, first-derivative weights negated. */
+static double carp1[4][6];
+static const double carp2[2][5] = {{35.0 / 12.0, -104.0 / 12.0, 114.0 / 12.0, -56.0 / 12.0, 11.0 / 12.0},
+                                   {11.0 / 12.0, -20.0 / 12.0, 6.0 / 12.0, 4.0 / 12.0, -1.0 / 12.0}};
+static int carp_ready = 0;
+
+static void carpenter_init(void) {
+  if (carp_ready) return;
+  const double R1 = -(2177.0 * sqrt(295369.0) - 1166427.0) / 25488.0;
+  const double R2 = (66195.0 * sqrt(53.0) * sqrt(5573.0) - 35909375.0) / 101952.0;
+  double AL[4][4] = {
+      {-(216.0 * R2 + 2160.0 * R1 - 2125.0) / 12960.0, (81.0 * R2 + 675.0 * R1 + 415.0) / 540.0,
+       -(72.0 * R2 + 720.0 * R1 + 445.0) / 1440.0, -(108.0 * R2 + 756.0 * R1 + 421.0) / 1296.0},
+      {(81.0 * R2 + 675.0 * R1 + 415.0) / 540.0, -(4104.0 * R2 + 32400.0 * R1 + 11225.0) / 4320.0,
+       (1836.0 * R2 + 14580.0 * R1 + 7295.0) / 2160.0, -(216.0 * R2 + 2160.0 * R1 + 655.0) / 4320.0},
+      {-(72.0 * R2 + 720.0 * R1 + 445.0) / 1440.0, (1836.0 * R2 + 14580.0 * R1 + 7295.0) / 2160.0,
+       -(4104.0 * R2 + 32400.0 * R1 + 12785.0) / 4320.0, (81.0 * R2 + 675.0 * R1 + 335.0) / 540.0},
+      {-(108.0 * R2 + 756.0 * R1 + 421.0) / 1296.0, -(216.0 * R2 + 2160.0 * R1 + 655.0) / 4320.0,
+       (81.0 * R2 + 675.0 * R1 + 335.0) / 540.0, -(216.0 * R2 + 2160.0 * R1 - 12085.0) / 12960.0}};
+  double AR[4][6] = {
+      {-0.5, -(864.0 * R2 + 6480.0 * R1 + 305.0) / 4320.0, (216.0 * R2 + 1620.0 * R1 + 725.0) / 540.0,
+       -(864.0 * R2 + 6480.0 * R1 + 3335.0) / 4320.0, 0.0, 0.0},
+      {(864.0 * R2 + 6480.0 * R1 + 305.0) / 4320.0, 0.0, -(864.0 * R2 + 6480.0 * R1 + 2315.0) / 1440.0,
+       (108.0 * R2 + 810.0 * R1 + 415.0) / 270.0, 0.0, 0.0},
+      {-(216.0 * R2 + 1620.0 * R1 + 725.0) / 540.0, (864.0 * R2 + 6480.0 * R1 + 2315.0) / 1440.0, 0.0,
+       -(864.0 * R2 + 6480.0 * R1 + 785.0) / 4320.0, -1.0 / 12.0, 0.0},
+      {(864.0 * R2 + 6480.0 * R1 + 3335.0) / 4320.0, -(108.0 * R2 + 810.0 * R1 + 415.0) / 270.0,
+       (864.0 * R2 + 6480.0 * R1 + 785.0) / 4320.0, 0.0, 8.0 / 12.0, -1.0 / 12.0}};
+  /* solve A_L X = A_R by Gauss-Jordan elimination with partial pivoting */
+  for (int col = 0; col < 4; ++col) {
+    int piv = col;
+    for (int r = col + 1; r < 4; ++r)
+      if (fabs(AL[r][col]) > fabs(AL[piv][col])) piv = r;
+    for (int k = 0; k < 4; ++k) { double t = AL[col][k]; AL[col][k] = AL[piv][k]; AL[piv][k] = t; }
+    for (int k = 0; k < 6; ++k) { double t = AR[col][k]; AR[col][k] = AR[piv][k]; AR[piv][k] = t; }
+    const double inv = 1.0 / AL[col][col];
+    for (int k = 0; k < 4; ++k) AL[col][k] *= inv;
+    for (int k = 0; k < 6; ++k) AR[col][k] *= inv;
+    for (int r = 0; r < 4; ++r) {
+      if (r == col) continue;
+      const double f = AL[r][col];
+      for (int k = 0; k < 4; ++k) AL[r][k] -= f * AL[col][k];
+      for (int k = 0; k < 6; ++k) AR[r][k] -= f * AR[col][k];
+    }
+  }
+  for (int r = 0; r < 4; ++r)
+    for (int m = 0; m < 6; ++m) carp1[r][m] = fabs(AR[r][m]) < 1e-14 ? 0.0 : AR[r][m];
+  const double row0[6] = {-11.0 / 6.0, 3.0, -1.5, 1.0 / 3.0, 0.0, 0.0};
+  for (int m = 0; m < 6; ++m) carp1[0][m] = row0[m];
+  carp_ready = 1;
+}
+
+/* The closure weights (for tests): row r of the first (order 1, 6 weights) or second (order 2,
+ * 5 weights) derivative closure. */
+int oracle_carpenter(int order, int r, double* w) {
+  carpenter_init();
+  if (order == 1 && r >= 0 && r < 4) { for (int m = 0; m < 6; ++m) w[m] = carp1[r][m]; return 0; }
+  if (order == 2 && r >= 0 && r < 2) { for (int m = 0; m < 5; ++m) w[m] = carp2[r][m]; return 0; }
+  return -1;
+}
+
+/* Closure row of the point with index i along d for derivatives of `order`: 0..3 (first) or
+ * 0..1 (second) next to a low wall face, 4 + r next to a high one, -1 for the central rule. */
+static int closure_row(const osb_block_desc* b, const geom_t* g, int d, int i, int order) {
+  const int rows = order == 1 ? 4 : 2;
+  if (b->bc[d][0] == OSB_BC_ISOTHERMAL_WALL && i < rows) return i;
+  if (b->bc[d][1] == OSB_BC_ISOTHERMAL_WALL && i > g->n[d] - 1 - rows) return 4 + (g->n[d] - 1 - i);
+  return -1;
+}
+
+/* Closure sums (without the 1/Delta factors): row code cr of closure_row */
+static inline double c1sum(const double* f, long id, long s, int cr) {
+  const int r = cr & 3, hi = cr >= 4;
+  double acc = 0.0;
+  for (int m = 0; m < 6; ++m) {
+    if (carp1[r][m] == 0.0) continue;
+    const long o = hi ? (long)(r - m) : (long)(m - r);
+    acc += (hi ? -carp1[r][m] : carp1[r][m]) * f[id + o * s];
+  }
+  return acc;
+}
+static inline double c2sum(const double* f, long id, long s, int cr) {
+  const int r = cr & 3, hi = cr >= 4;
+  double acc = 0.0;
+  for (int m = 0; m < 5; ++m) {
+    const long o = hi ? (long)(r - m) : (long)(m - r);
+    acc += carp2[r][m] * f[id + o * s];
+  }
+  return acc;
+}
+
+/* First / second derivative along d at the point with coordinates c (index id) */
+static inline double d1at(const osb_block_desc* b, const geom_t* g, const double* f, long id, const int* c, int d,
+                          double invd) {
+  const int cr = closure_row(b, g, d, c[d], 1);
+  if (cr < 0) return d1c(f, id, g->st[d], invd);
+  return c1sum(f, id, g->st[d], cr) * invd;
+}
+static inline double d2at(const osb_block_desc* b, const geom_t* g, const double* f, long id, const int* c, int d,
+                          double inv2d) {
+  const int cr = closure_row(b, g, d, c[d], 2);
+  if (cr < 0) return d2c(f, id, g->st[d], inv2d);
+  return c2sum(f, id, g->st[d], cr) * inv2d;
+}
+/* d^2 f / dx_a dx_b: the first derivative along b of the first derivative along a (each with
+ * its closure; moving along b keeps the point's index along a) */
+static inline double dmixat(const osb_block_desc* b, const geom_t* g, const double* f, long id, const int* c, int a,
+                            int bb, double inva, double invb) {
+  const int cb = closure_row(b, g, bb, c[bb], 1);
+  if (cb < 0) {
+    double acc = 0.0;
+    for (int m = 0; m < 5; ++m) {
+      if (m == 2) continue;
+      const long idb = id + (long)(m - 2) * g->st[bb];
+      acc += C1[m] * d1at(b, g, f, idb, c, a, inva);
+    }
+    return acc * invb;
+  }
+  const int r = cb & 3, hi = cb >= 4;
+  double acc = 0.0;
+  for (int m = 0; m < 6; ++m) {
+    if (carp1[r][m] == 0.0) continue;
+    const long o = hi ? (long)(r - m) : (long)(m - r);
+    acc += (hi ? -carp1[r][m] : carp1[r][m]) * d1at(b, g, f, id + o * g->st[bb], c, a, inva);
+  }
+  return acc * invb;
+}
+
 /* Viscous stress and heat-flux residual terms (generated "Viscous terms" kernel of the
- * supersonic TGV, Residual1..4 += ...). */
-static void viscous_point(const osb_block_desc* b, const geom_t* g, const cr_t* c, long id, double* r) {
+ * supersonic TGV, Residual1..4 += ...); at isothermal-wall faces the derivatives take the
+ * closures above (the generated kernels' idx-conditional branches). */
+static void viscous_point(const osb_block_desc* b, const geom_t* g, const cr_t* c, long id, const int* pc, double* r) {
   const int nd = b->ndim;
   double inv[3], inv2[3];
   for (int d = 0; d < nd; ++d) { inv[d] = 1.0 / b->delta[d]; inv2[d] = 1.0 / (b->delta[d] * b->delta[d]); }
   double du[3][3], lap[3], dmu[3], dT[3], lapT = 0.0;
   for (int i = 0; i < nd; ++i)
-    for (int j = 0; j < nd; ++j) du[i][j] = d1c(c->u[i], id, g->st[j], inv[j]);
+    for (int j = 0; j < nd; ++j) du[i][j] = d1at(b, g, c->u[i], id, pc, j, inv[j]);
   double div = 0.0;
   for (int i = 0; i < nd; ++i) div += du[i][i];
   for (int j = 0; j < nd; ++j) {
-    dmu[j] = d1c(c->mu, id, g->st[j], inv[j]);
-    dT[j] = d1c(c->T, id, g->st[j], inv[j]);
-    lapT += d2c(c->T, id, g->st[j], inv2[j]);
+    dmu[j] = d1at(b, g, c->mu, id, pc, j, inv[j]);
+    dT[j] = d1at(b, g, c->T, id, pc, j, inv[j]);
+    lapT += d2at(b, g, c->T, id, pc, j, inv2[j]);
   }
   /* lap_i = sum_j d2u_i/dx_j^2 + 1/3 d/dx_i (div u) */
   for (int i = 0; i < nd; ++i) {
     double s = 0.0;
-    for (int j = 0; j < nd; ++j) s += d2c(c->u[i], id, g->st[j], inv2[j]);
-    s += (1.0 / 3.0) * d2c(c->u[i], id, g->st[i], inv2[i]);
+    for (int j = 0; j < nd; ++j) s += d2at(b, g, c->u[i], id, pc, j, inv2[j]);
+    s += (1.0 / 3.0) * d2at(b, g, c->u[i], id, pc, i, inv2[i]);
     for (int j = 0; j < nd; ++j) {
       if (j == i) continue;
       int a = i < j ? i : j, bb = i < j ? j : i;
-      s += (1.0 / 3.0) * dmix(c->u[j], id, g->st[a], g->st[bb], inv[a], inv[bb]);
+      s += (1.0 / 3.0) * dmixat(b, g, c->u[j], id, pc, a, bb, inv[a], inv[bb]);
     }
     lap[i] = s;
   }
@@ -704,6 +840,7 @@ typedef struct {
 } set_t;
 
 int oracle_residual(const osb_block_desc* b, double* const* Rout) {
+  carpenter_init();
   geom_t g = geom_of(b);
   const int nd = b->ndim, nv = nd + 2;
   long n = npts_alloc(&g);
@@ -776,7 +913,8 @@ int oracle_residual(const osb_block_desc* b, double* const* Rout) {
         for (int i = 0; i < g.n[0]; ++i) {
           long id = gid(&g, i, j, k);
           double r[NVMAX] = {0, 0, 0, 0, 0};
-          viscous_point(b, &g, &c, id, r);
+          const int pc[3] = {i, j, k};
+          viscous_point(b, &g, &c, id, pc, r);
           for (int v = 1; v < nv; ++v) Rout[v][id] += r[v];
         }
   }
@@ -1471,6 +1609,42 @@ static void pressure_outlet_point(osb_block_desc* b, const geom_t* g, int d, int
   }
 }
 
+/* Isothermal wall (isothermal_wall.py:62-131 as generated for conservative variables, with the
+ * wall energy rhoE = Twall rho / (gama Minf^2 (gama - 1))): the wall plane takes zero momentum
+ * and that energy; with the wall pressure Pw = (gama - 1) rhoE(wall) and the temperature
+ * T1 = Minf^2 gama (gama - 1) (rhoE - |rhou|^2 / (2 rho)) / rho of the point next to the wall,
+ * halo layer k = 1..depth takes T_k = (k+1) Twall - k T1, rho_k = Minf^2 gama Pw / T_k, the
+ * momentum -rho_k u(k) and the energy Pw / (gama - 1) + rho_k |u(k)|^2 / 2, u(k) the velocity of
+ * the point k inside the wall. */
+static void isothermal_wall_point(osb_block_desc* b, const geom_t* g, int d, int side, int depth, const int* c,
+                                  long t) {
+  (void)t;
+  const int nd = b->ndim, nv = nd + 2;
+  const long w = gid(g, c[0], c[1], c[2]);
+  const long o = g->st[d] * (side == 0 ? 1 : -1); /* towards the inside */
+  const double gm = b->gama, M2 = b->Minf * b->Minf, Tw = b->wall_temperature[d][side];
+  for (int i = 0; i < nd; ++i) b->q[1 + i][w] = 0.0;
+  b->q[nv - 1][w] = Tw * b->q[0][w] / (gm * M2 * (gm - 1.0));
+  const double pw = (gm - 1.0) * b->q[nv - 1][w];
+  const long a = w + o;
+  double ke = 0.0;
+  for (int i = 0; i < nd; ++i) ke += 0.5 * (b->q[1 + i][a] * b->q[1 + i][a]);
+  const double Ta = M2 * (gm - 1.0) * (b->q[nv - 1][a] - ke / b->q[0][a]) * gm / b->q[0][a];
+  for (int k = 1; k <= depth; ++k) {
+    const long in = w + k * o, h = w - k * o;
+    double u[3], u2 = 0.0;
+    for (int i = 0; i < nd; ++i) {
+      u[i] = b->q[1 + i][in] / b->q[0][in];
+      u2 += u[i] * u[i];
+    }
+    const double Tk = -(double)k * Ta + (double)(k + 1) * Tw;
+    const double rk = M2 * gm * pw / Tk;
+    b->q[0][h] = rk;
+    for (int i = 0; i < nd; ++i) b->q[1 + i][h] = -rk * u[i];
+    b->q[nv - 1][h] = pw / (gm - 1.0) + 0.5 * u2 * rk;
+  }
+}
+
 /* Block interface (multi_block.py:11-107, identity orientation, matching faces normal to the
  * same direction): the halo layers of face (d, side) receive the neighbour's layers adjacent to
  * its face (d, f->side).  `full` = 0 copies the interior of the face only; `full` = 1 also the
@@ -1524,6 +1698,8 @@ int oracle_apply_bc(osb_block_desc* blocks, int nblocks, int zero_grad_only) {
             for_face(b, &g, d, side, depth, side == 0 ? 0 : g.n[d] - 1, symmetry_point);
           if (pass == 1 && kind == OSB_BC_PRESSURE_OUTLET)
             for_face(b, &g, d, side, depth, side == 0 ? 0 : g.n[d] - 1, pressure_outlet_point);
+          if (pass == 1 && kind == OSB_BC_ISOTHERMAL_WALL)
+            for_face(b, &g, d, side, depth, side == 0 ? 0 : g.n[d] - 1, isothermal_wall_point);
           if (pass == 1 && kind == OSB_BC_DIRICHLET) {
             if (!b->dirichlet[d][side]) return -1;
             for_face(b, &g, d, side, depth, 0, dirichlet_point);

@@ -317,6 +317,66 @@ def central_split_block(form, energy_formulation="none", extra=None):
     return block, _tgv_params(1.25, 16, "0.001")
 
 
+def case_channel_iso():
+    """3D channel between isothermal no-slip walls: characteristic LLF TENO5 (Roe average) plus
+    4th-order central viscous terms (StoreSome), the shock-capturing form of the SBLI apps, on a
+    uniform grid; IsothermalWallBC on both y faces with the wall energy of
+    ``apps/channel_flow/compressible_TCF_Central/turbulent_channel.py:118-131`` (no forcing
+    terms), periodic in x and z, RK-LS3.  The wall faces take the reference's default Carpenter
+    closures of the central derivatives (core/boundary_conditions/Carpenter_scheme.py)."""
+    import copy
+    from opensbli import (RoeAverage, LFTeno, StoreSome, RungeKuttaLS, PeriodicBC, IsothermalWallBC,
+                          SimulationBlock, GridBasedInitialisation, GridVariable, DataObject, parse_expr,
+                          ConstantObject, Eq)
+    ndim = 3
+    sim = _euler_equations(ndim, "Teno", viscous=True)
+    cr = _constituents(ndim, viscous=True)
+    block = SimulationBlock(ndim, block_number=0)
+    local_dict = {"block": block, "GridVariable": GridVariable, "DataObject": DataObject}
+    eqns = ["Eq(GridVariable(x0), block.deltas[0]*block.grid_indexes[0])",
+            "Eq(GridVariable(x1), -1.0 + block.deltas[1]*block.grid_indexes[1])",
+            "Eq(GridVariable(x2), block.deltas[2]*block.grid_indexes[2])",
+            "Eq(GridVariable(u0), (1.0 - x1*x1)*(1.0 + 0.1*sin(x0)*cos(x2)))",
+            "Eq(GridVariable(u1), 0.05*sin(x0)*(1.0 - x1*x1)*(1.0 - x1*x1))",
+            "Eq(GridVariable(u2), 0.05*cos(x0)*sin(x2)*(1.0 - x1*x1))",
+            "Eq(GridVariable(p), 1.0/(gama*Minf*Minf)*(1.0 + 0.02*cos(x0)*cos(x2)))",
+            "Eq(GridVariable(r), 1.0 + 0.02*sin(x0)*x1)",
+            "Eq(DataObject(rho), r)", "Eq(DataObject(rhou0), r*u0)", "Eq(DataObject(rhou1), r*u1)",
+            "Eq(DataObject(rhou2), r*u2)",
+            "Eq(DataObject(rhoE), p/(gama-1) + 0.5* r *(u0**2+ u1**2 + u2**2))"]
+    initial = GridBasedInitialisation()
+    initial.add_equations([parse_expr(e, local_dict=local_dict) for e in eqns])
+    schemes = {}
+    LF = LFTeno(order=5, averaging=RoeAverage([0, 1]), flux_type="LLF")
+    schemes[LF.name] = LF
+    cent = StoreSome(4, "u0 u1 u2")
+    schemes[cent.name] = cent
+    rk = RungeKuttaLS(3)
+    schemes[rk.name] = rk
+    block.set_discretisation_schemes(schemes)
+    q = flatten_q(sim)
+    gama, Minf, Twall = ConstantObject("gama"), ConstantObject("Minf"), ConstantObject("Twall")
+    wall = [Eq(q[4], Twall * q[0] / (gama * Minf ** 2.0 * (gama - 1)))]
+    bcs = [PeriodicBC(0, 0, halos=[-4, 4]), PeriodicBC(0, 1, halos=[-4, 4]),
+           IsothermalWallBC(1, 0, wall[:]), IsothermalWallBC(1, 1, wall[:]),
+           PeriodicBC(2, 0, halos=[-4, 4]), PeriodicBC(2, 1, halos=[-4, 4])]
+    block.set_block_boundaries(bcs)
+    block.set_equations([copy.deepcopy(cr), copy.deepcopy(sim), initial])
+    block.discretise()
+    p = {"Re": "100.0", "gama": "1.4", "Minf": "0.5", "Pr": "0.71", "Twall": "1.0",
+         "dt": 'osb_env_double("OSB_DT", 0.001)', "niter": 'osb_env_int("OSB_NITER", 1)',
+         "TENO_CT": 'osb_env_double("OSB_TENO_CT", 1e-6)'}
+    for d, (n, dl) in enumerate([(16, "2*M_PI/block0np0"), (17, "2.0/(block0np1-1)"), (8, "2*M_PI/block0np2")]):
+        p["block0np%d" % d] = 'osb_env_int("OSB_NP%d", %d)' % (d, n)
+        p["Delta%dblock0" % d] = dl
+    return block, p
+
+
+def flatten_q(sim):
+    from sympy import flatten
+    return flatten(sim.time_advance_arrays)
+
+
 def case_tgv_kgp_tvd():
     """The central KGP TGV of central_split_block followed, after every full RK step, by the
     non-linear characteristic TVD filter (``filters/TVD_filter.py``; Yee-Sandham-Djomehri
@@ -647,6 +707,7 @@ CASES = {
     "curv_weno5z": case_curv_weno5z,
     "curv3d_teno5": case_curv3d_teno5,
     "mb2_flip": case_mb2_flip,
+    "channel_iso": case_channel_iso,
 }
 
 

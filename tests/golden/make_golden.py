@@ -61,6 +61,10 @@ CASES = {
     # problems.metrics_central4 bit for bit
     "curv_weno5z_32": ("curv_weno5z", lambda: problems.curvilinear_wave_2d(32),
                        {"OSB_NP0": 32, "OSB_NP1": 32}, 5e-4, [1, 3, 30], None),
+    # isothermal no-slip walls on both y faces with the Carpenter closures of the viscous terms
+    "channel_iso_16x17x8_perturbed": ("channel_iso", lambda: problems.channel_iso((16, 17, 8)),
+                                      {"OSB_NP0": 16, "OSB_NP1": 17, "OSB_NP2": 8}, 1e-3, [1, 3, 30],
+                                      (1e-3, 41)),
     # 3D curvilinear TENO5 (MetricsEquation, every direction curvilinear); the solver's own metric
     # arrays are stored with the states (interior; their halos are the periodic images)
     "curv3d_teno5_16x12x10_perturbed": ("curv3d_teno5", lambda: problems.curvilinear_wave_3d((16, 12, 10)),

@@ -230,3 +230,85 @@ def test_pressure_outlet_matches_reference_solver(built_lib, oracle_lib, precisi
         box = (slice(h, h + n1), slice(h, h + n0 + 4))  # interior rows, through the outlet's 4 halo layers
         for v in range(4):
             assert np.max(np.abs(got[v][box] - ob.q[0][v][box])) < 1e-12 * np.max(np.abs(ob.q[0][v])), v
+
+
+def _golden_channel():
+    import os
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "channel_iso_16x17x8_perturbed.npz"))
+    spec, q = problems.channel_iso((16, 17, 8))
+    rng = np.random.default_rng(41)
+    q = [a * (1.0 + 1e-3 * rng.standard_normal(a.shape)) for a in q]
+    return spec, q, g
+
+
+def _channel_errors(got, ref, sl):
+    """Max error of each field over its scale, the momentum components over the momentum scale."""
+    mscale = max(float(np.max(np.abs(ref[v]))) for v in (1, 2, 3))
+    return [float(np.max(np.abs(got[v][sl] - ref[v]))) / (mscale if v in (1, 2, 3) else float(np.max(np.abs(ref[v]))))
+            for v in range(5)]
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("fp32", 1e-5)])
+def test_isothermal_wall_channel_matches_reference_solver(built_lib, oracle_lib, precision, tol):
+    """The 3D channel between isothermal no-slip walls (TENO5 + viscous terms with the Carpenter
+    closures at both walls) on the GPU: 10 steps against the reference's generated solver
+    (golden, 30 stages) and, in FP64, against the oracle on the interior and the walls' halo
+    layers (1e-12)."""
+    from opensbli_gb300.solver import Solver
+    spec, q, g = _golden_channel()
+    s = Solver([(spec, q)], precision=precision, rk="ls3")
+    s.apply_bc()
+    s.step(float(g["dt"]), 10)
+    got = s.state(0)
+    s.close()
+    sl = spec.interior()
+    errs = _channel_errors(got, g["after_30"], sl)
+    assert max(errs) < tol, errs
+    if precision == "fp64":
+        ob = harness.OracleBlocks([(spec, q)])
+        ob.apply_bc()
+        ob.step(abi.RK_LOW_STORAGE, problems.RK3_LS_A, problems.RK3_LS_B, float(g["dt"]), 10)
+        h, (n0, n1, n2) = spec.halo, spec.size
+        box = (slice(h, h + n2), slice(h - 4, h + n1 + 4), slice(h, h + n0))  # interior x, z; y through the walls' halos
+        for v in range(5):
+            assert np.max(np.abs(got[v][box] - ob.q[0][v][box])) < 1e-12 * np.max(np.abs(ob.q[0][v][box])), v
+
+
+def test_isothermal_wall_residual_matches_oracle(built_lib, oracle_lib):
+    """The residual of one stage (sweeps plus the viscous terms with the wall closures) of the
+    golden channel state, FP64 GPU against the oracle: 1e-12 of each field's scale."""
+    from opensbli_gb300.solver import Solver
+    spec, q, _ = _golden_channel()
+    s = Solver([(spec, q)], precision="fp64", rk="ls3")
+    s.apply_bc()
+    R = s.residual(0)
+    s.close()
+    ob = harness.OracleBlocks([(spec, q)])
+    ob.apply_bc()
+    Ro = ob.residual(0)
+    sl = spec.interior()
+    mscale = max(float(np.max(np.abs(Ro[v][sl]))) for v in (1, 2, 3))
+    for v in range(5):
+        sc = mscale if v in (1, 2, 3) else float(np.max(np.abs(Ro[v][sl])))
+        assert float(np.max(np.abs(R[v][sl] - Ro[v][sl]))) < 1e-12 * sc, v
+
+
+def test_isothermal_wall_refused_outside_its_scope(built_lib):
+    """Walls on a face other than y, on a central-scheme block, or without a wall temperature
+    are refused at osb_block_add."""
+    from opensbli_gb300.solver import Solver
+    spec, q = problems.channel_iso((16, 17, 8))
+    bad = []
+    s1 = problems.channel_iso((16, 17, 8))[0]
+    s1.wall_temperature = {(1, 0): 0.0, (1, 1): 1.0}
+    bad.append(s1)
+    s2 = problems.channel_iso((16, 17, 8))[0]
+    s2.scheme = abi.SCHEME_CENTRAL4
+    bad.append(s2)
+    s3 = problems.channel_iso((16, 17, 8))[0]
+    s3.bc = [[abi.BC_ISOTHERMAL_WALL] * 2, [abi.BC_PERIODIC] * 2, [abi.BC_PERIODIC] * 2]
+    s3.wall_temperature = {(0, 0): 1.0, (0, 1): 1.0}
+    bad.append(s3)
+    for sp in bad:
+        with pytest.raises(abi.OSBError):
+            Solver([(sp, q)], precision="fp64", rk="ls3")

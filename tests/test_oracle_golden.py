@@ -57,6 +57,8 @@ CASES = {
     # pressure outlet (back pressure 0.2) in place of the extrapolation outlet
     "shock_reflection_pout_64x32_perturbed": (lambda: problems.shock_reflection(64, 32, back_pressure=0.2), "ls3",
                                               (1e-2, 4), 1e-12),
+    # isothermal no-slip walls (both y faces) with the Carpenter closures of the viscous terms
+    "channel_iso_16x17x8_perturbed": (lambda: problems.channel_iso((16, 17, 8)), "ls3", (1e-3, 41), 1e-12),
 }
 
 
