@@ -78,6 +78,11 @@ extern "C" {
                                 of the viscous terms take the one-sided Carpenter closures at the
                                 four points next to the wall (Carpenter_scheme.py).  3D
                                 Cartesian blocks, walls on y faces, shock-capturing schemes. */
+#define OSB_BC_ADIABATIC_WALL 9  /* AdiabaticWallBC (adiabatic_wall.py:28-69): no-slip wall plane with
+                                the energy of the wall temperature that makes the one-sided
+                                third-order dT/dn vanish, T_w = (18 T1 - 9 T2 + 2 T3) / 11; halo
+                                layer k mirrors the point k inside (momentum negated); the same
+                                Carpenter closures and scope as OSB_BC_ISOTHERMAL_WALL. */
 
 /* Convective split form of OSB_SCHEME_CENTRAL4 (physical_models/split_forms.py). */
 #define OSB_SPLIT_FEIEREISEN 0 /* skew-symmetric form, split_forms.py:111-145 */

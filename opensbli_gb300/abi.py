@@ -38,6 +38,7 @@ BC_SYMMETRY = 5
 BC_DIRICHLET = 6
 BC_PRESSURE_OUTLET = 7
 BC_ISOTHERMAL_WALL = 8
+BC_ADIABATIC_WALL = 9
 SPLIT_FEIEREISEN = 0
 SPLIT_KGP = 1
 FILTER_NONE = 0

@@ -205,6 +205,10 @@ def _bcs_of(block, central_only):
                 bc[d][side] = abi.BC_ISOTHERMAL_WALL
                 hv = b.get_halo_values(block)
                 depth[d][side] = abs(hv[d][side])
+            elif type(b).__name__ == "AdiabaticWallBC":
+                bc[d][side] = abi.BC_ADIABATIC_WALL  # adiabatic_wall.py:28-69
+                hv = b.get_halo_values(block)
+                depth[d][side] = abs(hv[d][side])
             elif type(b).__name__ == "SharedInterfaceBC":
                 raise NotImplementedError("SharedInterfaceBC (interfaces sharing their boundary points) is not "
                                           "implemented; InterfaceBC is")

@@ -70,6 +70,9 @@ const Closures& closures() {
   return cl;
 }
 
+// Faces whose central derivatives take the one-sided closures (ModifyCentralDerivative walls).
+inline bool is_wall(int kind) { return kind == OSB_BC_ISOTHERMAL_WALL || kind == OSB_BC_ADIABATIC_WALL; }
+
 template <typename T, int CONV, int VISC, bool FUSE, int CY, bool BULK, bool WALL = false>
 int launch_central_k(osb_ctx* c, Block& bl, int first, const RkFuse& rf) {
   using Fd = CentralFields<T, CONV, VISC>;
@@ -96,8 +99,8 @@ int launch_central_k(osb_ctx* c, Block& bl, int first, const RkFuse& rf) {
     cp.inv2d_f[i] = (float)cp.inv2d[i];
   }
   if (WALL) {
-    cp.wall_lo = bl.d.bc[1][0] == OSB_BC_ISOTHERMAL_WALL;
-    cp.wall_hi = bl.d.bc[1][1] == OSB_BC_ISOTHERMAL_WALL;
+    cp.wall_lo = is_wall(bl.d.bc[1][0]);
+    cp.wall_hi = is_wall(bl.d.bc[1][1]);
     const Closures& cl = closures();
     for (int r = 0; r < 4; ++r)
       for (int m = 0; m < 6; ++m) {
@@ -132,7 +135,7 @@ int launch_central_k(osb_ctx* c, Block& bl, int first, const RkFuse& rf) {
 template <typename T, int CONV, int VISC, bool FUSE, bool BULK>
 int launch_central_h(osb_ctx* c, Block& bl, int first, const RkFuse& rf) {
   if constexpr (CONV == 0 && !BULK) {
-    if (bl.d.bc[1][0] == OSB_BC_ISOTHERMAL_WALL || bl.d.bc[1][1] == OSB_BC_ISOTHERMAL_WALL)
+    if (is_wall(bl.d.bc[1][0]) || is_wall(bl.d.bc[1][1]))
       return launch_central_k<T, CONV, VISC, FUSE, 4, false, true>(c, bl, first, rf);
   }
   const long cols4 = (long)((bl.k.n[0] + CX - 1) / CX) * ((bl.k.n[1] + 3) / 4);
@@ -147,7 +150,7 @@ int launch_central_h(osb_ctx* c, Block& bl, int first, const RkFuse& rf) {
 template <typename T, int CONV, int VISC>
 int launch_central_t(osb_ctx* c, Block& bl, int first, const RkFuse* rf) {
   if constexpr (sizeof(T) == 4) {
-    const bool wall = bl.d.bc[1][0] == OSB_BC_ISOTHERMAL_WALL || bl.d.bc[1][1] == OSB_BC_ISOTHERMAL_WALL;
+    const bool wall = is_wall(bl.d.bc[1][0]) || is_wall(bl.d.bc[1][1]);
     if (rf && c->central_bulk && !wall) return launch_central_h<T, CONV, VISC, true, true>(c, bl, first, *rf);
     if (rf) return launch_central_h<T, CONV, VISC, true, false>(c, bl, first, *rf);
   }

@@ -444,25 +444,66 @@ __device__ void wall_point(S* const* q, int nd, int w, int o, int depth, double 
   }
 }
 
-__global__ void k_isothermal_wall(BlockK b, int nv, int d, int side, int depth, int halo, double gama, double Minf,
-                                  double Tw, int fields) {
+// Adiabatic wall (adiabatic_wall.py:28-69 as generated): halo layer k takes the density and
+// energy of the point k inside and its momentum negated; the wall plane zero momentum and
+// rhoE = rho(wall) T_w / (gama Minf^2 (gama - 1)), T_w = (18 T1 - 9 T2 + 2 T3) / 11 the wall
+// temperature of a vanishing one-sided third-order dT/dn (T_k of the point k inside).  `halos`
+// false: the wall plane only.
+template <typename S>
+__device__ void adiabatic_point(S* const* q, int nd, int w, int o, int depth, double gm, double M2, bool halos) {
+  const int nv = nd + 2;
+  if (halos)
+    for (int k = 1; k <= depth; ++k) wall_st(q[0], w - k * o, wall_ld(q[0], w + k * o));
+  for (int i = 0; i < nd; ++i) wall_st(q[1 + i], w, 0.0);
+  if (halos)
+    for (int k = 1; k <= depth; ++k)
+      for (int i = 0; i < nd; ++i) wall_st(q[1 + i], w - k * o, -wall_ld(q[1 + i], w + k * o));
+  double T[4];
+  for (int k = 1; k <= 3; ++k) {
+    const int a = w + k * o;
+    double ke = 0.0;
+    for (int i = 0; i < nd; ++i) {
+      const double m = wall_ld(q[1 + i], a);
+      ke = __dadd_rn(ke, __dmul_rn(0.5, __dmul_rn(m, m)));
+    }
+    const double ra = wall_ld(q[0], a);
+    T[k] = __ddiv_rn(__dmul_rn(__dmul_rn(__dmul_rn(M2, __dadd_rn(gm, -1.0)), __dadd_rn(wall_ld(q[nv - 1], a), -__ddiv_rn(ke, ra))), gm), ra);
+  }
+  const double Tw = __dadd_rn(__dadd_rn(__dmul_rn(18.0 / 11.0, T[1]), -__dmul_rn(9.0 / 11.0, T[2])), __dmul_rn(2.0 / 11.0, T[3]));
+  wall_st(q[nv - 1], w, __ddiv_rn(__dmul_rn(Tw, wall_ld(q[0], w)), __dmul_rn(__dmul_rn(gm, M2), __dadd_rn(gm, -1.0))));
+  if (halos)
+    for (int k = 1; k <= depth; ++k) wall_st(q[nv - 1], w - k * o, wall_ld(q[nv - 1], w + k * o));
+}
+
+// Both wall kinds over the whole transverse allocation of face (d, side).
+__global__ void k_wall(BlockK b, int nv, int kind, int d, int side, int depth, int halo, double gama, double Minf,
+                       double Tw, int fields) {
   const int total = face_extent(b, d, halo);
   const int base = side == 0 ? 0 : b.n[d] - 1;
   const int o = b.st[d] * (side == 0 ? 1 : -1);  // towards the inside
   const int nd = nv - 2;
   const double M2 = __dmul_rn(Minf, Minf);
+  const bool iso = kind == OSB_BC_ISOTHERMAL_WALL;
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
     int c[3];
     face_point(b, d, halo, t, c);
     c[d] = base;
     const int w = lin(b, c[0], c[1], c[2]);
     if (fields & BC_Q) {
-      wall_point<double>(b.q, nd, w, o, depth, gama, M2, Tw);
+      if (iso) wall_point<double>(b.q, nd, w, o, depth, gama, M2, Tw);
+      else adiabatic_point<double>(b.q, nd, w, o, depth, gama, M2, true);
     } else if (b.qf[0]) {  // FP64 wall plane only (the halos follow when the call returns)
-      for (int i = 0; i < nd; ++i) b.q[1 + i][w] = 0.0;
-      b.q[nv - 1][w] = __ddiv_rn(__dmul_rn(Tw, b.q[0][w]), __dmul_rn(__dmul_rn(gama, M2), __dadd_rn(gama, -1.0)));
+      if (iso) {
+        for (int i = 0; i < nd; ++i) b.q[1 + i][w] = 0.0;
+        b.q[nv - 1][w] = __ddiv_rn(__dmul_rn(Tw, b.q[0][w]), __dmul_rn(__dmul_rn(gama, M2), __dadd_rn(gama, -1.0)));
+      } else {
+        adiabatic_point<double>(b.q, nd, w, o, depth, gama, M2, false);
+      }
     }
-    if ((fields & BC_QF) && b.qf[0]) wall_point<float>(b.qf, nd, w, o, depth, gama, M2, Tw);
+    if ((fields & BC_QF) && b.qf[0]) {
+      if (iso) wall_point<float>(b.qf, nd, w, o, depth, gama, M2, Tw);
+      else adiabatic_point<float>(b.qf, nd, w, o, depth, gama, M2, true);
+    }
   }
 }
 
@@ -868,12 +909,12 @@ int apply_block_bc(osb_ctx* c, Block& bl, size_t ib, int fields) {
             bl.k, nv, d, side, side ? dep1 : dep0, bl.d.halo, bl.d.back_pressure[d][side], bl.d.gama, fields);
         timing_end(c);
         c->launches++;
-      } else if (kind == OSB_BC_ISOTHERMAL_WALL) {
+      } else if (kind == OSB_BC_ISOTHERMAL_WALL || kind == OSB_BC_ADIABATIC_WALL) {
         const long tr = face_extent(bl.k, d, bl.d.halo);
         timing_begin(c, FAM_BC);
-        k_isothermal_wall<<<grid_for(c, tr, 128), 128, 0, c->stream>>>(
-            bl.k, nv, d, side, side ? dep1 : dep0, bl.d.halo, bl.d.gama, bl.d.Minf, bl.d.wall_temperature[d][side],
-            fields);
+        k_wall<<<grid_for(c, tr, 128), 128, 0, c->stream>>>(bl.k, nv, kind, d, side, side ? dep1 : dep0, bl.d.halo,
+                                                           bl.d.gama, bl.d.Minf, bl.d.wall_temperature[d][side],
+                                                           fields);
         timing_end(c);
         c->launches++;
       } else if (kind == OSB_BC_PERIODIC) {
@@ -1067,16 +1108,19 @@ bool check_desc(const osb_block_desc* d, std::string& why) {
   for (int i = 0; i < d->ndim; ++i)
     for (int s = 0; s < 2; ++s) {
       const int k = d->bc[i][s];
-      if (k < OSB_BC_PERIODIC || k > OSB_BC_ISOTHERMAL_WALL) { why = "unknown boundary kind"; return false; }
-      if (k == OSB_BC_ISOTHERMAL_WALL) {
+      if (k < OSB_BC_PERIODIC || k > OSB_BC_ADIABATIC_WALL) { why = "unknown boundary kind"; return false; }
+      if (k == OSB_BC_ISOTHERMAL_WALL || k == OSB_BC_ADIABATIC_WALL) {
         if (d->ndim != 3 || i != 1 || d->metric[9] || d->scheme == OSB_SCHEME_CENTRAL4) {
-          why = "isothermal walls are implemented on the y faces of 3D Cartesian blocks with a shock-capturing scheme";
+          why = "walls are implemented on the y faces of 3D Cartesian blocks with a shock-capturing scheme";
           return false;
         }
-        if (!(d->wall_temperature[i][s] > 0.0)) { why = "an isothermal wall needs a positive wall temperature"; return false; }
+        if (k == OSB_BC_ISOTHERMAL_WALL && !(d->wall_temperature[i][s] > 0.0)) {
+          why = "an isothermal wall needs a positive wall temperature";
+          return false;
+        }
         const int wd = d->bc_depth[i][s] > 0 ? d->bc_depth[i][s] : 4;
         if (wd > d->halo || d->size[i] < 12) {
-          why = "isothermal walls: depth up to the halo, at least 12 points between the walls";
+          why = "walls: depth up to the halo, at least 12 points between the walls";
           return false;
         }
       }

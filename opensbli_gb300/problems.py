@@ -75,7 +75,7 @@ def tgv(n=64, minf=0.1, scheme=abi.SCHEME_CENTRAL4, averaging=abi.AVG_SIMPLE, vi
     return spec, _cons(spec, r, [u0, u1, u2], p)
 
 
-def channel_iso(sizes=(16, 17, 8), twall=1.0, minf=0.5, re=100.0):
+def channel_iso(sizes=(16, 17, 8), twall=1.0, minf=0.5, re=100.0, upper="isothermal"):
     """3D channel between isothermal no-slip walls at y = -1 and y = 1 (IsothermalWallBC on both
     y faces, Twall = `twall`), periodic in x on [0, 2pi) and z on [0, 2pi), uniform grid with the
     walls on the first and last points in y (Delta_y = 2 / (N_y - 1)), characteristic LLF TENO5
@@ -84,15 +84,19 @@ def channel_iso(sizes=(16, 17, 8), twall=1.0, minf=0.5, re=100.0):
     apps/channel_flow/compressible_TCF_Central/turbulent_channel.py:118-131.  Initial state: a
     perturbed parabolic profile, u0 = (1 - y^2)(1 + 0.1 sin x cos z), u1 = 0.05 sin x (1 - y^2)^2,
     u2 = 0.05 cos x sin z (1 - y^2), p = (1 + 0.02 cos x cos z) / (gama Minf^2),
-    rho = 1 + 0.02 sin x y."""
+    rho = 1 + 0.02 sin x y.  upper = "adiabatic" makes the upper wall an AdiabaticWallBC (the
+    alternative upper wall of apps/channel_flow/laminar_2D/laminar_channel.py:104-113)."""
     n0, n1, n2 = sizes
     spec = BlockSpec(ndim=3, size=sizes, scheme=abi.SCHEME_TENO5, averaging=abi.AVG_ROE,
                      viscous=abi.VISC_SUTHERLAND,
-                     bc=[[abi.BC_PERIODIC] * 2, [abi.BC_ISOTHERMAL_WALL] * 2, [abi.BC_PERIODIC] * 2],
+                     bc=[[abi.BC_PERIODIC] * 2,
+                         [abi.BC_ISOTHERMAL_WALL, abi.BC_ISOTHERMAL_WALL if upper == "isothermal" else abi.BC_ADIABATIC_WALL],
+                         [abi.BC_PERIODIC] * 2],
                      bc_depth=[[4, 4] for _ in range(3)],
                      delta=(2.0 * math.pi / n0, 2.0 / (n1 - 1), 2.0 * math.pi / n2), gama=1.4, Minf=minf, Re=re,
                      Pr=0.71, mu_const=1.0, eps=1e-40, teno_ct=1e-6,
-                     wall_temperature={(1, 0): float(twall), (1, 1): float(twall)})
+                     wall_temperature={(1, 0): float(twall), (1, 1): float(twall)} if upper == "isothermal"
+                     else {(1, 0): float(twall)})
     x0 = spec.delta[0] * spec.grid_index(0)
     x1 = -1.0 + spec.delta[1] * spec.grid_index(1)
     x2 = spec.delta[2] * spec.grid_index(2)

@@ -698,10 +698,11 @@ int oracle_carpenter(int order, int r, double* w) {
 
 /* Closure row of the point with index i along d for derivatives of `order`: 0..3 (first) or
  * 0..1 (second) next to a low wall face, 4 + r next to a high one, -1 for the central rule. */
+static inline int is_wall(int kind) { return kind == OSB_BC_ISOTHERMAL_WALL || kind == OSB_BC_ADIABATIC_WALL; }
 static int closure_row(const osb_block_desc* b, const geom_t* g, int d, int i, int order) {
   const int rows = order == 1 ? 4 : 2;
-  if (b->bc[d][0] == OSB_BC_ISOTHERMAL_WALL && i < rows) return i;
-  if (b->bc[d][1] == OSB_BC_ISOTHERMAL_WALL && i > g->n[d] - 1 - rows) return 4 + (g->n[d] - 1 - i);
+  if (is_wall(b->bc[d][0]) && i < rows) return i;
+  if (is_wall(b->bc[d][1]) && i > g->n[d] - 1 - rows) return 4 + (g->n[d] - 1 - i);
   return -1;
 }
 
@@ -1645,6 +1646,34 @@ static void isothermal_wall_point(osb_block_desc* b, const geom_t* g, int d, int
   }
 }
 
+/* Adiabatic wall (adiabatic_wall.py:28-69 as generated): halo layer k takes the density and the
+ * energy of the point k inside and its momentum negated; the wall plane takes zero momentum and
+ * rhoE = rho(wall) T_w / (gama Minf^2 (gama - 1)) with T_w = (18 T1 - 9 T2 + 2 T3) / 11 the
+ * wall temperature of a vanishing one-sided third-order dT/dn, T_k = Minf^2 gama (gama - 1)
+ * (rhoE - |rhou|^2 / (2 rho)) / rho of the point k inside. */
+static void adiabatic_wall_point(osb_block_desc* b, const geom_t* g, int d, int side, int depth, const int* c,
+                                 long t) {
+  (void)t;
+  const int nd = b->ndim, nv = nd + 2;
+  const long w = gid(g, c[0], c[1], c[2]);
+  const long o = g->st[d] * (side == 0 ? 1 : -1); /* towards the inside */
+  const double gm = b->gama, M2 = b->Minf * b->Minf;
+  for (int k = 1; k <= depth; ++k) b->q[0][w - k * o] = b->q[0][w + k * o];
+  for (int i = 0; i < nd; ++i) b->q[1 + i][w] = 0.0;
+  for (int k = 1; k <= depth; ++k)
+    for (int i = 0; i < nd; ++i) b->q[1 + i][w - k * o] = -b->q[1 + i][w + k * o];
+  double T[4];
+  for (int k = 1; k <= 3; ++k) {
+    const long a = w + k * o;
+    double ke = 0.0;
+    for (int i = 0; i < nd; ++i) ke += 0.5 * (b->q[1 + i][a] * b->q[1 + i][a]);
+    T[k] = M2 * (gm - 1.0) * (b->q[nv - 1][a] - ke / b->q[0][a]) * gm / b->q[0][a];
+  }
+  const double Tw = (18.0 / 11.0) * T[1] - (9.0 / 11.0) * T[2] + (2.0 / 11.0) * T[3];
+  b->q[nv - 1][w] = Tw * b->q[0][w] / (gm * M2 * (gm - 1.0));
+  for (int k = 1; k <= depth; ++k) b->q[nv - 1][w - k * o] = b->q[nv - 1][w + k * o];
+}
+
 /* Block interface (multi_block.py:11-107, identity orientation, matching faces normal to the
  * same direction): the halo layers of face (d, side) receive the neighbour's layers adjacent to
  * its face (d, f->side).  `full` = 0 copies the interior of the face only; `full` = 1 also the
@@ -1700,6 +1729,8 @@ int oracle_apply_bc(osb_block_desc* blocks, int nblocks, int zero_grad_only) {
             for_face(b, &g, d, side, depth, side == 0 ? 0 : g.n[d] - 1, pressure_outlet_point);
           if (pass == 1 && kind == OSB_BC_ISOTHERMAL_WALL)
             for_face(b, &g, d, side, depth, side == 0 ? 0 : g.n[d] - 1, isothermal_wall_point);
+          if (pass == 1 && kind == OSB_BC_ADIABATIC_WALL)
+            for_face(b, &g, d, side, depth, side == 0 ? 0 : g.n[d] - 1, adiabatic_wall_point);
           if (pass == 1 && kind == OSB_BC_DIRICHLET) {
             if (!b->dirichlet[d][side]) return -1;
             for_face(b, &g, d, side, depth, 0, dirichlet_point);

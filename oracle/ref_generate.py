@@ -317,7 +317,13 @@ def central_split_block(form, energy_formulation="none", extra=None):
     return block, _tgv_params(1.25, 16, "0.001")
 
 
-def case_channel_iso():
+def case_channel_adi():
+    """The channel of case_channel_iso with the upper wall adiabatic (AdiabaticWallBC, the
+    alternative upper wall of ``apps/channel_flow/laminar_2D/laminar_channel.py:104-113``)."""
+    return case_channel_iso(upper="adiabatic")
+
+
+def case_channel_iso(upper="isothermal"):
     """3D channel between isothermal no-slip walls: characteristic LLF TENO5 (Roe average) plus
     4th-order central viscous terms (StoreSome), the shock-capturing form of the SBLI apps, on a
     uniform grid; IsothermalWallBC on both y faces with the wall energy of
@@ -326,8 +332,8 @@ def case_channel_iso():
     closures of the central derivatives (core/boundary_conditions/Carpenter_scheme.py)."""
     import copy
     from opensbli import (RoeAverage, LFTeno, StoreSome, RungeKuttaLS, PeriodicBC, IsothermalWallBC,
-                          SimulationBlock, GridBasedInitialisation, GridVariable, DataObject, parse_expr,
-                          ConstantObject, Eq)
+                          AdiabaticWallBC, SimulationBlock, GridBasedInitialisation, GridVariable, DataObject,
+                          parse_expr, ConstantObject, Eq)
     ndim = 3
     sim = _euler_equations(ndim, "Teno", viscous=True)
     cr = _constituents(ndim, viscous=True)
@@ -358,7 +364,8 @@ def case_channel_iso():
     gama, Minf, Twall = ConstantObject("gama"), ConstantObject("Minf"), ConstantObject("Twall")
     wall = [Eq(q[4], Twall * q[0] / (gama * Minf ** 2.0 * (gama - 1)))]
     bcs = [PeriodicBC(0, 0, halos=[-4, 4]), PeriodicBC(0, 1, halos=[-4, 4]),
-           IsothermalWallBC(1, 0, wall[:]), IsothermalWallBC(1, 1, wall[:]),
+           IsothermalWallBC(1, 0, wall[:]),
+           IsothermalWallBC(1, 1, wall[:]) if upper == "isothermal" else AdiabaticWallBC(1, 1),
            PeriodicBC(2, 0, halos=[-4, 4]), PeriodicBC(2, 1, halos=[-4, 4])]
     block.set_block_boundaries(bcs)
     block.set_equations([copy.deepcopy(cr), copy.deepcopy(sim), initial])
@@ -708,6 +715,7 @@ CASES = {
     "curv3d_teno5": case_curv3d_teno5,
     "mb2_flip": case_mb2_flip,
     "channel_iso": case_channel_iso,
+    "channel_adi": case_channel_adi,
 }
 
 

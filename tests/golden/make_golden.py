@@ -65,6 +65,10 @@ CASES = {
     "channel_iso_16x17x8_perturbed": ("channel_iso", lambda: problems.channel_iso((16, 17, 8)),
                                       {"OSB_NP0": 16, "OSB_NP1": 17, "OSB_NP2": 8}, 1e-3, [1, 3, 30],
                                       (1e-3, 41)),
+    # the same with the upper wall adiabatic
+    "channel_adi_16x17x8_perturbed": ("channel_adi", lambda: problems.channel_iso((16, 17, 8), upper="adiabatic"),
+                                      {"OSB_NP0": 16, "OSB_NP1": 17, "OSB_NP2": 8}, 1e-3, [1, 3, 30],
+                                      (1e-3, 42)),
     # 3D curvilinear TENO5 (MetricsEquation, every direction curvilinear); the solver's own metric
     # arrays are stored with the states (interior; their halos are the periodic images)
     "curv3d_teno5_16x12x10_perturbed": ("curv3d_teno5", lambda: problems.curvilinear_wave_3d((16, 12, 10)),

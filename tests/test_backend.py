@@ -232,7 +232,7 @@ def test_pressure_outlet_maps_and_runs_in_the_oracle():
     assert max(errs) < 1e-12, errs
 
 
-PLANS = ["sod400", "tgv_teno5_12", "curv128", "curv3d_16x12x10", "shock_64x32", "kh_32", "mb2_flip", "channel_iso"]
+PLANS = ["sod400", "tgv_teno5_12", "curv128", "curv3d_16x12x10", "shock_64x32", "kh_32", "mb2_flip", "channel_iso", "channel_adi"]
 
 
 @needs_ref

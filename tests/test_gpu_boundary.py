@@ -232,11 +232,17 @@ def test_pressure_outlet_matches_reference_solver(built_lib, oracle_lib, precisi
             assert np.max(np.abs(got[v][box] - ob.q[0][v][box])) < 1e-12 * np.max(np.abs(ob.q[0][v])), v
 
 
-def _golden_channel():
+CHANNELS = {"iso": ("channel_iso_16x17x8_perturbed.npz", "isothermal", 41),
+            "adi": ("channel_adi_16x17x8_perturbed.npz", "adiabatic", 42)}
+
+
+def _golden_channel(kind="iso"):
+    """The golden channel: isothermal walls on both y faces ("iso"), or the upper one adiabatic ("adi")."""
     import os
-    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "channel_iso_16x17x8_perturbed.npz"))
-    spec, q = problems.channel_iso((16, 17, 8))
-    rng = np.random.default_rng(41)
+    name, upper, seed = CHANNELS[kind]
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", name))
+    spec, q = problems.channel_iso((16, 17, 8), upper=upper)
+    rng = np.random.default_rng(seed)
     q = [a * (1.0 + 1e-3 * rng.standard_normal(a.shape)) for a in q]
     return spec, q, g
 
@@ -251,14 +257,15 @@ def _channel_errors(got, ref, sl):
 # FP32: the golden state carries 1e-3 relative noise, on which TENO5's binary cut-off decisions
 # sit near their threshold, so FP32 rounding flips some of them: 2.6e-5 of the momentum scale
 # after 30 stages, the same as the perturbed curvilinear TENO5 case (test_gpu_fullsize.py)
+@pytest.mark.parametrize("kind", sorted(CHANNELS))
 @pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("fp32", 5e-5)])
-def test_isothermal_wall_channel_matches_reference_solver(built_lib, oracle_lib, precision, tol):
+def test_wall_channel_matches_reference_solver(built_lib, oracle_lib, kind, precision, tol):
     """The 3D channel between isothermal no-slip walls (TENO5 + viscous terms with the Carpenter
     closures at both walls) on the GPU: 10 steps against the reference's generated solver
     (golden, 30 stages) and, in FP64, against the oracle on the interior and the walls' halo
-    layers (1e-12)."""
+    layers (1e-12); with the upper wall adiabatic as well."""
     from opensbli_gb300.solver import Solver
-    spec, q, g = _golden_channel()
+    spec, q, g = _golden_channel(kind)
     s = Solver([(spec, q)], precision=precision, rk="ls3")
     s.apply_bc()
     s.step(float(g["dt"]), 10)
@@ -277,11 +284,12 @@ def test_isothermal_wall_channel_matches_reference_solver(built_lib, oracle_lib,
             assert np.max(np.abs(got[v][box] - ob.q[0][v][box])) < 1e-12 * np.max(np.abs(ob.q[0][v][box])), v
 
 
-def test_isothermal_wall_residual_matches_oracle(built_lib, oracle_lib):
+@pytest.mark.parametrize("kind", sorted(CHANNELS))
+def test_wall_residual_matches_oracle(built_lib, oracle_lib, kind):
     """The residual of one stage (sweeps plus the viscous terms with the wall closures) of the
     golden channel state, FP64 GPU against the oracle: 1e-12 of each field's scale."""
     from opensbli_gb300.solver import Solver
-    spec, q, _ = _golden_channel()
+    spec, q, _ = _golden_channel(kind)
     s = Solver([(spec, q)], precision="fp64", rk="ls3")
     s.apply_bc()
     R = s.residual(0)

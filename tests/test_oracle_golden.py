@@ -59,6 +59,8 @@ CASES = {
                                               (1e-2, 4), 1e-12),
     # isothermal no-slip walls (both y faces) with the Carpenter closures of the viscous terms
     "channel_iso_16x17x8_perturbed": (lambda: problems.channel_iso((16, 17, 8)), "ls3", (1e-3, 41), 1e-12),
+    "channel_adi_16x17x8_perturbed": (lambda: problems.channel_iso((16, 17, 8), upper="adiabatic"), "ls3",
+                                      (1e-3, 42), 1e-12),
 }
 
 
