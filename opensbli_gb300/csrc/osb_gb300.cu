@@ -401,46 +401,50 @@ __global__ void k_pressure_outlet(BlockK b, int nv, int d, int side, int depth, 
 // (2 rho)) / rho of the point next to the wall, halo layer k = 1..depth takes
 // T_k = (k+1) Twall - k T1, rho_k = Minf^2 gama Pw / T_k, momentum -rho_k u(k) and energy
 // Pw / (gama - 1) + rho_k |u(k)|^2 / 2, u(k) the velocity of the point k inside.  Over the whole
-// transverse allocation.  The FP32 shadow is filled from its own values (FP64 arithmetic on the
-// exactly widened floats, rounded once); with BC_QF alone the FP64 wall plane is reset too, so
-// the FP64 state's wall momentum and energy stay the wall's between the FP32 path's stages.
-template <typename S>
-__device__ __forceinline__ double wall_ld(const S* a, int i);
+// transverse allocation.  The FP32 shadow is filled from its own values in FP32 arithmetic (its
+// halos feed FP32 kernels only); with BC_QF alone the FP64 wall plane is reset too, so the FP64
+// state's wall momentum and energy stay the wall's between the FP32 path's stages.
+// Explicitly rounded operations in the arithmetic of the array a wall kernel fills.
+template <typename A>
+struct WOp;
 template <>
-__device__ __forceinline__ double wall_ld<double>(const double* a, int i) { return a[i]; }
+struct WOp<double> {
+  static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+  static __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+  static __device__ __forceinline__ double div(double a, double b) { return __ddiv_rn(a, b); }
+};
 template <>
-__device__ __forceinline__ double wall_ld<float>(const float* a, int i) { return f2d_exact(a[i]); }
-__device__ __forceinline__ void wall_st(double* a, int i, double x) { a[i] = x; }
-__device__ __forceinline__ void wall_st(float* a, int i, double x) { a[i] = d2f_rn(x); }
+struct WOp<float> {
+  static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
+  static __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+  static __device__ __forceinline__ float div(float a, float b) { return __fdiv_rn(a, b); }
+};
 
-template <typename S>
-__device__ void wall_point(S* const* q, int nd, int w, int o, int depth, double gm, double M2, double Tw) {
+template <typename A>
+__device__ void wall_point(A* const* q, int nd, int w, int o, int depth, A gm, A M2, A Tw) {
+  using O = WOp<A>;
   const int nv = nd + 2;
-  for (int i = 0; i < nd; ++i) wall_st(q[1 + i], w, 0.0);
-  const double Ew = __ddiv_rn(__dmul_rn(Tw, wall_ld(q[0], w)), __dmul_rn(__dmul_rn(gm, M2), __dadd_rn(gm, -1.0)));
-  wall_st(q[nv - 1], w, Ew);
-  const double pw = __dmul_rn(__dadd_rn(gm, -1.0), wall_ld(q[nv - 1], w));
+  const A g1 = O::add(gm, A(-1));
+  for (int i = 0; i < nd; ++i) q[1 + i][w] = A(0);
+  q[nv - 1][w] = O::div(O::mul(Tw, q[0][w]), O::mul(O::mul(gm, M2), g1));
+  const A pw = O::mul(g1, q[nv - 1][w]);
   const int a = w + o;
-  double ke = 0.0;
-  for (int i = 0; i < nd; ++i) {
-    const double m = wall_ld(q[1 + i], a);
-    ke = __dadd_rn(ke, __dmul_rn(0.5, __dmul_rn(m, m)));
-  }
-  const double ra = wall_ld(q[0], a);
-  const double Ta =
-      __ddiv_rn(__dmul_rn(__dmul_rn(__dmul_rn(M2, __dadd_rn(gm, -1.0)), __dadd_rn(wall_ld(q[nv - 1], a), -__ddiv_rn(ke, ra))), gm), ra);
+  A ke = A(0);
+  for (int i = 0; i < nd; ++i) ke = O::add(ke, O::mul(A(0.5), O::mul(q[1 + i][a], q[1 + i][a])));
+  const A ra = q[0][a];
+  const A Ta = O::div(O::mul(O::mul(O::mul(M2, g1), O::add(q[nv - 1][a], -O::div(ke, ra))), gm), ra);
   for (int k = 1; k <= depth; ++k) {
     const int in = w + k * o, h = w - k * o;
-    double u[3], u2 = 0.0;
+    A u[3], u2 = A(0);
     for (int i = 0; i < nd; ++i) {
-      u[i] = __ddiv_rn(wall_ld(q[1 + i], in), wall_ld(q[0], in));
-      u2 = __dadd_rn(u2, __dmul_rn(u[i], u[i]));
+      u[i] = O::div(q[1 + i][in], q[0][in]);
+      u2 = O::add(u2, O::mul(u[i], u[i]));
     }
-    const double Tk = __dadd_rn(__dmul_rn(-(double)k, Ta), __dmul_rn((double)(k + 1), Tw));
-    const double rk = __ddiv_rn(__dmul_rn(__dmul_rn(M2, gm), pw), Tk);
-    wall_st(q[0], h, rk);
-    for (int i = 0; i < nd; ++i) wall_st(q[1 + i], h, -__dmul_rn(rk, u[i]));
-    wall_st(q[nv - 1], h, __dadd_rn(__ddiv_rn(pw, __dadd_rn(gm, -1.0)), __dmul_rn(__dmul_rn(0.5, u2), rk)));
+    const A Tk = O::add(O::mul(A(-k), Ta), O::mul(A(k + 1), Tw));
+    const A rk = O::div(O::mul(O::mul(M2, gm), pw), Tk);
+    q[0][h] = rk;
+    for (int i = 0; i < nd; ++i) q[1 + i][h] = -O::mul(rk, u[i]);
+    q[nv - 1][h] = O::add(O::div(pw, g1), O::mul(O::mul(A(0.5), u2), rk));
   }
 }
 
@@ -449,35 +453,34 @@ __device__ void wall_point(S* const* q, int nd, int w, int o, int depth, double 
 // rhoE = rho(wall) T_w / (gama Minf^2 (gama - 1)), T_w = (18 T1 - 9 T2 + 2 T3) / 11 the wall
 // temperature of a vanishing one-sided third-order dT/dn (T_k of the point k inside).  `halos`
 // false: the wall plane only.
-template <typename S>
-__device__ void adiabatic_point(S* const* q, int nd, int w, int o, int depth, double gm, double M2, bool halos) {
+template <typename A>
+__device__ void adiabatic_point(A* const* q, int nd, int w, int o, int depth, A gm, A M2, bool halos) {
+  using O = WOp<A>;
   const int nv = nd + 2;
+  const A g1 = O::add(gm, A(-1));
   if (halos)
-    for (int k = 1; k <= depth; ++k) wall_st(q[0], w - k * o, wall_ld(q[0], w + k * o));
-  for (int i = 0; i < nd; ++i) wall_st(q[1 + i], w, 0.0);
+    for (int k = 1; k <= depth; ++k) q[0][w - k * o] = q[0][w + k * o];
+  for (int i = 0; i < nd; ++i) q[1 + i][w] = A(0);
   if (halos)
     for (int k = 1; k <= depth; ++k)
-      for (int i = 0; i < nd; ++i) wall_st(q[1 + i], w - k * o, -wall_ld(q[1 + i], w + k * o));
-  double T[4];
+      for (int i = 0; i < nd; ++i) q[1 + i][w - k * o] = -q[1 + i][w + k * o];
+  A T[4];
   for (int k = 1; k <= 3; ++k) {
     const int a = w + k * o;
-    double ke = 0.0;
-    for (int i = 0; i < nd; ++i) {
-      const double m = wall_ld(q[1 + i], a);
-      ke = __dadd_rn(ke, __dmul_rn(0.5, __dmul_rn(m, m)));
-    }
-    const double ra = wall_ld(q[0], a);
-    T[k] = __ddiv_rn(__dmul_rn(__dmul_rn(__dmul_rn(M2, __dadd_rn(gm, -1.0)), __dadd_rn(wall_ld(q[nv - 1], a), -__ddiv_rn(ke, ra))), gm), ra);
+    A ke = A(0);
+    for (int i = 0; i < nd; ++i) ke = O::add(ke, O::mul(A(0.5), O::mul(q[1 + i][a], q[1 + i][a])));
+    const A ra = q[0][a];
+    T[k] = O::div(O::mul(O::mul(O::mul(M2, g1), O::add(q[nv - 1][a], -O::div(ke, ra))), gm), ra);
   }
-  const double Tw = __dadd_rn(__dadd_rn(__dmul_rn(18.0 / 11.0, T[1]), -__dmul_rn(9.0 / 11.0, T[2])), __dmul_rn(2.0 / 11.0, T[3]));
-  wall_st(q[nv - 1], w, __ddiv_rn(__dmul_rn(Tw, wall_ld(q[0], w)), __dmul_rn(__dmul_rn(gm, M2), __dadd_rn(gm, -1.0))));
+  const A Tw = O::add(O::add(O::mul(A(18.0 / 11.0), T[1]), -O::mul(A(9.0 / 11.0), T[2])), O::mul(A(2.0 / 11.0), T[3]));
+  q[nv - 1][w] = O::div(O::mul(Tw, q[0][w]), O::mul(O::mul(gm, M2), g1));
   if (halos)
-    for (int k = 1; k <= depth; ++k) wall_st(q[nv - 1], w - k * o, wall_ld(q[nv - 1], w + k * o));
+    for (int k = 1; k <= depth; ++k) q[nv - 1][w - k * o] = q[nv - 1][w + k * o];
 }
 
 // Both wall kinds over the whole transverse allocation of face (d, side).
 __global__ void k_wall(BlockK b, int nv, int kind, int d, int side, int depth, int halo, double gama, double Minf,
-                       double Tw, int fields) {
+                       double Tw, float gf, float M2f, float Twf, int fields) {
   const int total = face_extent(b, d, halo);
   const int base = side == 0 ? 0 : b.n[d] - 1;
   const int o = b.st[d] * (side == 0 ? 1 : -1);  // towards the inside
@@ -501,8 +504,8 @@ __global__ void k_wall(BlockK b, int nv, int kind, int d, int side, int depth, i
       }
     }
     if ((fields & BC_QF) && b.qf[0]) {
-      if (iso) wall_point<float>(b.qf, nd, w, o, depth, gama, M2, Tw);
-      else adiabatic_point<float>(b.qf, nd, w, o, depth, gama, M2, true);
+      if (iso) wall_point<float>(b.qf, nd, w, o, depth, gf, M2f, Twf);
+      else adiabatic_point<float>(b.qf, nd, w, o, depth, gf, M2f, true);
     }
   }
 }
@@ -912,9 +915,9 @@ int apply_block_bc(osb_ctx* c, Block& bl, size_t ib, int fields) {
       } else if (kind == OSB_BC_ISOTHERMAL_WALL || kind == OSB_BC_ADIABATIC_WALL) {
         const long tr = face_extent(bl.k, d, bl.d.halo);
         timing_begin(c, FAM_BC);
-        k_wall<<<grid_for(c, tr, 128), 128, 0, c->stream>>>(bl.k, nv, kind, d, side, side ? dep1 : dep0, bl.d.halo,
-                                                           bl.d.gama, bl.d.Minf, bl.d.wall_temperature[d][side],
-                                                           fields);
+        k_wall<<<grid_for(c, tr, 128), 128, 0, c->stream>>>(
+            bl.k, nv, kind, d, side, side ? dep1 : dep0, bl.d.halo, bl.d.gama, bl.d.Minf, bl.d.wall_temperature[d][side],
+            (float)bl.d.gama, (float)(bl.d.Minf * bl.d.Minf), (float)bl.d.wall_temperature[d][side], fields);
         timing_end(c);
         c->launches++;
       } else if (kind == OSB_BC_PERIODIC) {

@@ -6,11 +6,14 @@ quick checks; the throughput measurement with its roofline and baselines is benc
     python -m opensbli_gb300.run kh --count 16 --steps 1
     python -m opensbli_gb300.run sod --precision fp64 --steps 50
     python -m opensbli_gb300.run tgv --size 160 --central-staging 1 --steps 1
+    python -m opensbli_gb300.run channel --size 128 --steps 1
 
 tgv: the supersonic TGV (TENO5, Roe average, central viscous terms) at --size^3, dt 1e-3;
 curv4: the 4-block curvilinear case with its x and y sizes divided by --xy-scale;
 kh: the first --count instances of the seeded KH ensemble on the persistent stage;
-sod: the 400-point Sod tube (one osb_step call, the resident path).
+sod: the 400-point Sod tube (one osb_step call, the resident path);
+channel: the channel between isothermal walls (TENO5 + viscous, Carpenter closures) of
+--size x (--size + 1) x --size/2 points, dt 2e-4.
 Graphs are off and the FP32 per-block path applies the RK update in its last kernel, whose
 central kernel stages its planes by register loads (--central-staging 0, the default) or bulk
 copies (1).
@@ -35,12 +38,15 @@ def build(args):
                 {"mode": abi.SCHED_PERSISTENT, "tile_y": 16, "ctas_per_sm": 2, "dynamic": 1, "order": 0})
     if args.workload == "sod":
         return [problems.sod(400)], 2e-4, None
+    if args.workload == "channel":
+        n = args.size
+        return [problems.channel_iso((n, n + 1, n // 2))], 2e-4, {"mode": abi.SCHED_PER_BLOCK, "fuse_update": 1}
     raise ValueError(args.workload)
 
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("workload", choices=["tgv", "curv4", "kh", "sod"])
+    ap.add_argument("workload", choices=["tgv", "curv4", "kh", "sod", "channel"])
     ap.add_argument("--size", type=int, default=160)
     ap.add_argument("--xy-scale", type=int, default=1)
     ap.add_argument("--count", type=int, default=16)
