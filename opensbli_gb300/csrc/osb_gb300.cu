@@ -755,9 +755,11 @@ int residual_t(osb_ctx* c, Block& bl, const RkFuse* rf, bool* fused) {
   } else {
     const int nd = bl.d.ndim;
     const bool visc = bl.d.viscous != OSB_VISC_NONE;
-    // the sweeps do not carry the update: at their 128-register cap the extra FP64 state and
-    // register loads cannot be hidden (measured slower than the separate k_rk32)
-    const RkFuse* rs = nullptr;
+    // the last sweep of a 3D Cartesian block carries the update (z sweep + update 4.34 against
+    // 4.53 ms per step of the 256^3 Euler TGV with the separate k_rk32); the curvilinear sweeps
+    // (168 registers) do not: there the extra FP64 state and register loads are not hidden
+    // (5.60 against 5.01 ms per step of the 4-block case), nor in 2D, which is unmeasured
+    const RkFuse* rs = (sizeof(T) == 4 && !visc && nd == 3 && !bl.k.m[9]) ? rf : nullptr;
     if (bl.k.m[9]) {
       if (sizeof(T) == 4) rc = nd == 2 ? flux_curv_f32_2d(c, bl, sp, rs) : flux_curv_f32_3d(c, bl, sp, rs);
       else rc = nd == 2 ? flux_curv_f64_2d(c, bl, sp, nullptr) : flux_curv_f64_3d(c, bl, sp, nullptr);
