@@ -533,40 +533,53 @@ __global__ void k_dirichlet(BlockK b, int nv, int d, int side, int depth, int ha
   }
 }
 
-// Block interface (multi_block.py:11-107, InterfaceBC): the halo layers of face (d, side) of dst
-// receive the `depth` layers of src next to its face (d, sside), in reverse order along the
-// normal when flip is set (the match flag, opsc.py:1043-1045).  The transverse range is the
-// interior of the face (full = 0) or that plus `depth` halo points on each side (full = 1).
-__global__ void k_interface(BlockK dst, BlockK src, int nv, int d, int side, int sside, int flip, int depth,
-                            int full, int fields) {
-  int ext[3], lo[3];
-  for (int e = 0; e < 3; ++e) {
-    if (e < dst.ndim && e != d) {
-      lo[e] = full ? -depth : 0;
-      ext[e] = dst.n[e] + (full ? 2 * depth : 0);
-    } else {
-      lo[e] = 0;
-      ext[e] = 1;
-    }
-  }
-  ext[d] = depth;
-  const long total = (long)ext[0] * ext[1] * ext[2] * nv;
-  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
-    long r = t;
+
+// Block interfaces (multi_block.py:11-107, InterfaceBC): the halo layers of face (d, side) of a
+// block receive the `depth` layers of its neighbour next to the neighbour's face (d, sside), in
+// reverse order along the normal when flip is set (the match flag, opsc.py:1043-1045); the
+// transverse range is the interior of the face (full = 0) or that plus `depth` halo points on
+// each side (full = 1).  Every interface face of one boundary pass goes in one launch: the faces
+// travel by value in the kernel's parameters (their FP32 pointers are the ping-pong buffers
+// current at launch time, so a captured graph keeps the right ones per parity), and each thread
+// finds its face from the faces' starting offsets.
+constexpr int kIfMax = 24;
+struct IfFace {
+  long begin;                  // first element of this face in the launch's index space
+  int d, side, sside, flip, depth, nv;
+  int ext[3], lo[3];           // copied box: extents and lower corner (transverse), layers along d
+  int dn[3], dst_st[3], dst_off0;
+  int sn[3], src_st[3], src_off0;
+  double* dq[5];
+  const double* sq[5];
+  float* dqf[5];
+  const float* sqf[5];
+};
+struct IfBatch {
+  int nfaces;
+  long total;
+  IfFace f[kIfMax];
+};
+
+__global__ void k_interface(const __grid_constant__ IfBatch batch, int fields) {
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < batch.total; t += (long)gridDim.x * blockDim.x) {
+    int i = 0;
+    while (i + 1 < batch.nfaces && batch.f[i + 1].begin <= t) ++i;
+    const IfFace& F = batch.f[i];
+    long r = t - F.begin;
     int c[3];
-    c[0] = (int)(r % ext[0]); r /= ext[0];
-    c[1] = (int)(r % ext[1]); r /= ext[1];
-    c[2] = (int)(r % ext[2]);
-    const int v = (int)(r / ext[2]);
+    c[0] = (int)(r % F.ext[0]); r /= F.ext[0];
+    c[1] = (int)(r % F.ext[1]); r /= F.ext[1];
+    c[2] = (int)(r % F.ext[2]);
+    const int v = (int)(r / F.ext[2]);
     int di[3], si[3];
-    for (int e = 0; e < 3; ++e) di[e] = si[e] = c[e] + lo[e];
-    di[d] = side == 0 ? -depth + c[d] : dst.n[d] + c[d];
-    // flipped (the neighbour's normal index runs the other way): the layers in reverse order
-    const int sl = flip ? depth - 1 - c[d] : c[d];
-    si[d] = sside == 1 ? src.n[d] - depth + sl : sl;
-    const int a = lin(dst, di[0], di[1], di[2]), bsrc = lin(src, si[0], si[1], si[2]);
-    if (fields & BC_Q) dst.q[v][a] = src.q[v][bsrc];
-    if ((fields & BC_QF) && dst.qf[0]) dst.qf[v][a] = src.qf[v][bsrc];
+    for (int e = 0; e < 3; ++e) di[e] = si[e] = c[e] + F.lo[e];
+    di[F.d] = F.side == 0 ? -F.depth + c[F.d] : F.dn[F.d] + c[F.d];
+    const int sl = F.flip ? F.depth - 1 - c[F.d] : c[F.d];
+    si[F.d] = F.sside == 1 ? F.sn[F.d] - F.depth + sl : sl;
+    const int a = F.dst_off0 + di[0] * F.dst_st[0] + di[1] * F.dst_st[1] + di[2] * F.dst_st[2];
+    const int bs = F.src_off0 + si[0] * F.src_st[0] + si[1] * F.src_st[1] + si[2] * F.src_st[2];
+    if (fields & BC_Q) F.dq[v][a] = F.sq[v][bs];
+    if ((fields & BC_QF) && F.dqf[0]) F.dqf[v][a] = F.sqf[v][bs];
   }
 }
 
@@ -788,6 +801,16 @@ int residual(osb_ctx* c, Block& bl) {
 // Interface faces of every block: the interior of each face (full = 0) or the face with its
 // transverse halos (full = 1).
 int apply_interfaces(osb_ctx* c, int full, int fields) {
+  IfBatch batch{};
+  auto flush = [&]() {
+    if (batch.nfaces == 0) return;
+    timing_begin(c, FAM_BC);
+    k_interface<<<grid_for(c, batch.total, 256), 256, 0, c->stream>>>(batch, fields);
+    timing_end(c);
+    c->launches++;
+    batch.nfaces = 0;
+    batch.total = 0;
+  };
   for (size_t ib = 0; ib < c->blocks.size(); ++ib) {
     Block& bl = c->blocks[ib];
     const int nv = bl.d.ndim + 2;
@@ -808,16 +831,43 @@ int apply_interfaces(osb_ctx* c, int full, int fields) {
           return fail(OSB_EINVAL, "interface depth %d exceeds the %d points of block %d", depth, nb.k.n[d], f.block);
         if ((bl.k.qf[0] != nullptr) != (nb.k.qf[0] != nullptr))
           return fail(OSB_EINVAL, "interface between blocks of different precision");
-        long total = (long)depth * nv;
-        for (int e = 0; e < bl.d.ndim; ++e)
-          if (e != d) total *= bl.k.n[e] + (full ? 2 * depth : 0);
-        timing_begin(c, FAM_BC);
-        k_interface<<<grid_for(c, total, 256), 256, 0, c->stream>>>(bl.k, nb.k, nv, d, side, f.side, f.flip, depth,
-                                                                     full, fields);
-        timing_end(c);
-        c->launches++;
+        IfFace& F = batch.f[batch.nfaces];
+        F.begin = batch.total;
+        F.d = d;
+        F.side = side;
+        F.sside = f.side;
+        F.flip = f.flip;
+        F.depth = depth;
+        F.nv = nv;
+        long total = nv;
+        for (int e = 0; e < 3; ++e) {
+          if (e < bl.d.ndim && e != d) {
+            F.lo[e] = full ? -depth : 0;
+            F.ext[e] = bl.k.n[e] + (full ? 2 * depth : 0);
+          } else {
+            F.lo[e] = 0;
+            F.ext[e] = 1;
+          }
+          F.dn[e] = bl.k.n[e];
+          F.sn[e] = nb.k.n[e];
+          F.dst_st[e] = bl.k.st[e];
+          F.src_st[e] = nb.k.st[e];
+        }
+        F.ext[d] = depth;
+        for (int e = 0; e < 3; ++e) total *= F.ext[e];
+        F.dst_off0 = bl.k.off0;
+        F.src_off0 = nb.k.off0;
+        for (int v = 0; v < 5; ++v) {
+          F.dq[v] = v < nv ? bl.k.q[v] : nullptr;
+          F.sq[v] = v < nv ? nb.k.q[v] : nullptr;
+          F.dqf[v] = v < nv ? bl.k.qf[v] : nullptr;
+          F.sqf[v] = v < nv ? nb.k.qf[v] : nullptr;
+        }
+        batch.total += total;
+        if (++batch.nfaces == kIfMax) flush();
       }
   }
+  flush();
   return OSB_OK;
 }
 
