@@ -400,8 +400,8 @@ __global__ void k_pressure_outlet(BlockK b, int nv, int d, int side, int depth, 
 // Pw = (gama - 1) rhoE(wall) and the temperature T1 = Minf^2 gama (gama - 1) (rhoE - |rhou|^2 /
 // (2 rho)) / rho of the point next to the wall, halo layer k = 1..depth takes
 // T_k = (k+1) Twall - k T1, rho_k = Minf^2 gama Pw / T_k, momentum -rho_k u(k) and energy
-// Pw / (gama - 1) + rho_k |u(k)|^2 / 2, u(k) the velocity of the point k inside.  Over the whole
-// transverse allocation.  The FP32 shadow is filled from its own values in FP32 arithmetic (its
+// Pw / (gama - 1) + rho_k |u(k)|^2 / 2, u(k) the velocity of the point k inside.  Over the
+// transverse range the other faces fill (their layers' depth).  The FP32 shadow is filled from its own values in FP32 arithmetic (its
 // halos feed FP32 kernels only); with BC_QF alone the FP64 wall plane is reset too, so the FP64
 // state's wall momentum and energy stay the wall's between the FP32 path's stages.
 // Explicitly rounded operations in the arithmetic of the array a wall kernel fills.
@@ -478,7 +478,7 @@ __device__ void adiabatic_point(A* const* q, int nd, int w, int o, int depth, A 
     for (int k = 1; k <= depth; ++k) q[nv - 1][w - k * o] = q[nv - 1][w + k * o];
 }
 
-// Both wall kinds over the whole transverse allocation of face (d, side).
+// Both wall kinds over the transverse range of face (d, side), `halo` points beyond the face.
 __global__ void k_wall(BlockK b, int nv, int kind, int d, int side, int depth, int halo, double gama, double Minf,
                        double Tw, float gf, float M2f, float Twf, int fields) {
   const int total = face_extent(b, d, halo);
@@ -965,10 +965,16 @@ int apply_block_bc(osb_ctx* c, Block& bl, size_t ib, int fields) {
         timing_end(c);
         c->launches++;
       } else if (kind == OSB_BC_ISOTHERMAL_WALL || kind == OSB_BC_ADIABATIC_WALL) {
-        const long tr = face_extent(bl.k, d, bl.d.halo);
+        // over the transverse range the other faces' layers fill (the points beyond them hold
+        // whatever the caller left, and a wall point there would divide by their density)
+        int th = 1;
+        for (int e = 0; e < bl.d.ndim; ++e)
+          if (e != d) th = std::max(th, std::max(bl.d.bc_depth[e][0], bl.d.bc_depth[e][1]));
+        th = std::min(th, bl.d.halo);
+        const long tr = face_extent(bl.k, d, th);
         timing_begin(c, FAM_BC);
         k_wall<<<grid_for(c, tr, 128), 128, 0, c->stream>>>(
-            bl.k, nv, kind, d, side, side ? dep1 : dep0, bl.d.halo, bl.d.gama, bl.d.Minf, bl.d.wall_temperature[d][side],
+            bl.k, nv, kind, d, side, side ? dep1 : dep0, th, bl.d.gama, bl.d.Minf, bl.d.wall_temperature[d][side],
             (float)bl.d.gama, (float)(bl.d.Minf * bl.d.Minf), (float)bl.d.wall_temperature[d][side], fields);
         timing_end(c);
         c->launches++;

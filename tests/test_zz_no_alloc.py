@@ -6,7 +6,8 @@ synchronise the device or fail under memory pressure in the middle of a run).  T
 keeps its residual workspace in a fixed-size static device array instead, and the caller passes
 its own state and RK arrays.  These tests call it through the C ABI and compare it with the
 context-based entry point (osb_stage) on two consecutive stages, for a periodic 3D TENO5 block,
-a 2D block with Dirichlet, symmetry and extrapolation faces, and the SBLI RK3 integrator.
+a 2D block with Dirichlet, symmetry and extrapolation faces, a channel between an isothermal
+and an adiabatic wall, and the SBLI RK3 integrator.
 Collected last on purpose.
 """
 import ctypes
@@ -104,6 +105,15 @@ def test_stage_noalloc_dirichlet_symmetry_extrapolation(built_lib):
     rng = np.random.default_rng(3)
     q = [a * (1.0 + 1e-3 * rng.standard_normal(a.shape)) for a in q]
     _check(spec, q, "ssp3", [0, 1], 0.1)
+
+
+def test_stage_noalloc_walls(built_lib):
+    """Isothermal and adiabatic no-slip walls (y faces) with the Carpenter closures of the
+    viscous terms: the wall kernels and the closure-aware central kernel on the noalloc path."""
+    spec, q = problems.channel_iso((16, 17, 8), upper="adiabatic")
+    rng = np.random.default_rng(5)
+    q = [a * (1.0 + 1e-3 * rng.standard_normal(a.shape)) for a in q]
+    _check(spec, q, "ls3", [0, 1], 1e-3)
 
 
 def test_stage_noalloc_sbli3(built_lib):
