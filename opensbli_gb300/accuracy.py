@@ -4,6 +4,7 @@
     python -m opensbli_gb300.accuracy --workload tgv64 --steps 500 --every 50
     python -m opensbli_gb300.accuracy --workload kh_ensemble --steps 2000 --every 200
     python -m opensbli_gb300.accuracy --workload curv4 --steps 500 --every 50
+    python -m opensbli_gb300.accuracy --workload channel --steps 500 --every 50
 
 Advances, in lockstep from the same initial state, the FP64 path (the reference solution),
 the FP32-residual path (FP64 state, RK register and reductions) and -- with --floor -- a second
@@ -17,7 +18,8 @@ from the FP64 path by rounding can stay under.
 Workloads: tgv (the supersonic TGV at --size^3, CFL 0.5 at t = 0, --scheme), tgv64 (the 64^3
 low-Mach TGV with the central scheme, dt 3.385e-3), kh_ensemble (the 64 seeded Kelvin-Helmholtz
 instances, dt 2e-4, the FP32 run on the persistent batched stage), curv4 (the 4-block 3D
-curvilinear case, CFL 0.5 at t = 0).
+curvilinear case, CFL 0.5 at t = 0), channel (the 256 x 257 x 128 channel between isothermal
+walls, dt 2e-4).
 """
 import argparse
 import json
@@ -63,6 +65,9 @@ def workload(name, size=256, scheme=abi.SCHEME_TENO5, averaging=abi.AVG_ROE, min
     if name == "curv4":
         blocks = problems.curvilinear_multiblock_3d(seed=0)
         return blocks, problems.multiblock_cfl_dt(blocks, cfl), "ls3", "4-block 3D curvilinear TENO5 (CFL 0.5)"
+    if name == "channel":
+        return ([problems.channel_iso((256, 257, 128))], 2e-4, "ls3",
+                "channel 256 x 257 x 128 between isothermal walls, TENO5 + viscous (Carpenter closures), dt 2e-4")
     raise ValueError("unknown workload %s" % name)
 
 
@@ -114,7 +119,7 @@ def run(size=256, steps=1000, every=50, scheme=abi.SCHEME_TENO5, averaging=abi.A
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", default="tgv", choices=["tgv", "tgv64", "kh_ensemble", "curv4"])
+    ap.add_argument("--workload", default="tgv", choices=["tgv", "tgv64", "kh_ensemble", "curv4", "channel"])
     ap.add_argument("--size", type=int, default=256)
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--every", type=int, default=50)

@@ -959,21 +959,25 @@ __global__ void __launch_bounds__(CX * CY, bulk_ctas<CentralFields<T, CONV, VISC
     auto Fp = [&](int f, int dz, int ip) -> T { return sm[f * FS + pbase[dz + CH] + cxy + ip]; };
     // closure sums of the first / second y derivative (without 1/Delta) at plane dz, x offset ox;
     // the first-derivative row 0 has four points (its last two weights are zero and the rows
-    // beyond may not be staged)
+    // beyond may not be staged).  Every closure row sums to zero, so the sums run over the
+    // differences from the stencil's wall-side point m = 0, whose weight drops out: the FP32
+    // weights then stay exactly consistent, as in d1w / d2w.
     auto Y1 = [&](int f, int dz, int ox) -> T {
+      const T fw = Fp(f, dz, ox + yb1 * sy);
       T acc = L_(0.0);
 #pragma unroll
-      for (int m = 0; m < 4; ++m) acc += cw1[m] * Fp(f, dz, ox + (yb1 + ys1 * m) * sy);
+      for (int m = 1; m < 4; ++m) acc += cw1[m] * (Fp(f, dz, ox + (yb1 + ys1 * m) * sy) - fw);
       if ((wr1 & 3) != 0) {
 #pragma unroll
-        for (int m = 4; m < 6; ++m) acc += cw1[m] * Fp(f, dz, ox + (yb1 + ys1 * m) * sy);
+        for (int m = 4; m < 6; ++m) acc += cw1[m] * (Fp(f, dz, ox + (yb1 + ys1 * m) * sy) - fw);
       }
       return acc;
     };
     auto Y2 = [&](int f) -> T {
+      const T fw = Fp(f, 0, yb2 * sy);
       T acc = L_(0.0);
 #pragma unroll
-      for (int m = 0; m < 5; ++m) acc += cw2[m] * Fp(f, 0, (yb2 + ys2 * m) * sy);
+      for (int m = 1; m < 5; ++m) acc += cw2[m] * (Fp(f, 0, (yb2 + ys2 * m) * sy) - fw);
       return acc;
     };
     auto D1 = [&](int f, int s, T inv) -> T {
@@ -987,34 +991,30 @@ __global__ void __launch_bounds__(CX * CY, bulk_ctas<CentralFields<T, CONV, VISC
     // mixed derivative: central-4 along sb of the central-4 derivative along sa (WALL: the
     // closures where sa or sb is y; moving along sb keeps the point's row along sa)
     auto DM = [&](int f, int sa, int sb, T ia, T ib) -> T {
-      const T cw[4] = {L_(1.0 / 12.0), -L_(2.0 / 3.0), L_(2.0 / 3.0), -L_(1.0 / 12.0)};
-      const int off[4] = {-2, -1, 1, 2};
-      T r = L_(0.0);
       if (WALL && sb == sy && wr1 >= 0) {  // closure along y of the x (sa) derivatives
         auto dx = [&](int dy) -> T {
           const int o = dy * sy;
           return d1w<T>(Fp(f, 0, o - 2 * sa), Fp(f, 0, o - sa), Fp(f, 0, o + sa), Fp(f, 0, o + 2 * sa)) * ia;
         };
+        const T gw = dx(yb1);
+        T r = L_(0.0);
 #pragma unroll
-        for (int m = 0; m < 4; ++m) r += cw1[m] * dx(yb1 + ys1 * m);
+        for (int m = 1; m < 4; ++m) r += cw1[m] * (dx(yb1 + ys1 * m) - gw);
         if ((wr1 & 3) != 0) {
 #pragma unroll
-          for (int m = 4; m < 6; ++m) r += cw1[m] * dx(yb1 + ys1 * m);
+          for (int m = 4; m < 6; ++m) r += cw1[m] * (dx(yb1 + ys1 * m) - gw);
         }
         return r * ib;
       }
       if (WALL && sa == sy && wr1 >= 0) {  // central along sb (z) of the closure y derivatives
-#pragma unroll
-        for (int m = 0; m < 4; ++m) r += cw[m] * (Y1(f, off[m] * (sb / sz), 0) * ia);
-        return r * ib;
+        const int k = sb / sz;
+        return d1w<T>(Y1(f, -2 * k, 0) * ia, Y1(f, -k, 0) * ia, Y1(f, k, 0) * ia, Y1(f, 2 * k, 0) * ia) * ib;
       }
-#pragma unroll
-      for (int m = 0; m < 4; ++m) {
-        int o = off[m] * sb;
-        T dv = d1w<T>(F(f, o - 2 * sa), F(f, o - sa), F(f, o + sa), F(f, o + 2 * sa)) * ia;
-        r += cw[m] * dv;
-      }
-      return r * ib;
+      auto dv = [&](int m) -> T {
+        const int o = m * sb;
+        return d1w<T>(F(f, o - 2 * sa), F(f, o - sa), F(f, o + sa), F(f, o + 2 * sa)) * ia;
+      };
+      return d1w<T>(dv(-2), dv(-1), dv(1), dv(2)) * ib;
     };
     // every thread reaches both barriers of an iteration at the same call sites: the point
     // update is guarded, never skipped with a jump past a barrier
