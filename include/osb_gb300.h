@@ -158,6 +158,14 @@ typedef struct osb_block_desc {
   int32_t flux_type;         /* OSB_FLUX_* of the shock-capturing schemes (0 = LLF) */
   double back_pressure[3][2]; /* OSB_BC_PRESSURE_OUTLET face (d, side): its back pressure */
   double wall_temperature[3][2]; /* OSB_BC_ISOTHERMAL_WALL face (d, side): Twall */
+  /* Stretched wall-normal grid (a MetricsEquation with direction 1 stretched only, applied to the
+   * equations: equation_types/metric.py:183-240): D11 = d xi_1 / d x_1 (ystretch[0]) and
+   * SD111 = d D11 / d xi_1 (ystretch[1]) of every interior row j = 0 .. size[1]-1, as
+   * osb_ystretch_metrics computes them (device arrays of size[1] doubles; host arrays for the
+   * oracle); delta[1] is the spacing of xi_1.  The y flux difference and every y derivative of the
+   * viscous terms take them: d/dx_1 = D11 d/dxi_1, d2/dx_1^2 = D11^2 d2/dxi_1^2 + D11 SD111 d/dxi_1.
+   * NULL for a uniform y grid.  3D Cartesian viscous blocks with wall faces on both y sides only. */
+  const double* ystretch[2];
 } osb_block_desc;
 
 /* ---- library / context ------------------------------------------------------------- */
@@ -300,9 +308,10 @@ int osb_get_stream(osb_ctx* ctx, void** stream);
  *  - Halos: the stage reads q's halos as they are and applies the block's boundary faces only
  *    after its update, so before the first call the caller fills them (one osb_apply_bc on a
  *    context, or its own exchange); later calls leave them filled.
- *  - Faces: periodic, zero-gradient, extrapolation, symmetry and Dirichlet, with the kernels
- *    osb_apply_bc uses; a block with an interface face (or one periodic side) is refused with
- *    OSB_ENOTSUP before anything is launched, so the caller's arrays are untouched.
+ *  - Faces: periodic, zero-gradient, extrapolation, symmetry, Dirichlet, pressure outlet and
+ *    isothermal / adiabatic wall, with the kernels osb_apply_bc uses; a block with an interface
+ *    face (or one periodic side) is refused with OSB_ENOTSUP before anything is launched, so the
+ *    caller's arrays are untouched.
  *  - Device: the call runs on the current device; `stream` and every array must belong to it
  *    (checked: OSB_EINVAL otherwise).  The first call on a device looks up the workspace address
  *    (cudaGetSymbolAddress) and should come before any stream capture on that device.
@@ -312,6 +321,18 @@ int osb_get_stream(osb_ctx* ctx, void** stream);
  * Asynchronous on `stream` (a cudaStream_t, NULL for the default stream).
  * No counterpart in the reference (OPS always allocates its own datasets). */
 int osb_stage_noalloc(const osb_block_desc* desc, int rk_kind, double A, double B, double dt, void* stream);
+
+/* ---- stretched wall-normal grid ------------------------------------------------------ */
+
+/* Metrics of a wall-normal grid line x1[j], j = 0 .. n-1 (the generated "MetricsEquation
+ * evaluation" kernels of a MetricsEquation with direction 1 stretched only,
+ * equation_types/metric.py:183-240, with the Carpenter closures of
+ * core/boundary_conditions/Carpenter_scheme.py in the four rows next to a wall face): with
+ * x1' the 4th-order derivative of x1 along xi_1 (spacing delta), d11[j] = 1 / x1'[j] and
+ * sd111[j] the same derivative of d11.  wall_lo / wall_hi: 1 where that y face is a wall (the
+ * closures apply; the channel apps have walls on both).  Host arrays, no GPU work; n >= 12. */
+int osb_ystretch_metrics(int32_t n, double delta, const double* x1, int32_t wall_lo, int32_t wall_hi, double* d11,
+                         double* sd111);
 
 /* ---- curvilinear metrics (equation_types/metric.py:183-327) -------------------------- */
 
@@ -327,8 +348,8 @@ int osb_stage_noalloc(const osb_block_desc* desc, int rk_kind, double A, double 
 int osb_metrics(const osb_block_desc* desc, const double* const* x, double* const* met, int fill, void* stream);
 
 /* Binding check: writes sizeof(osb_block_desc) and the byte offsets of size, bc, iface, gama,
- * delta, q, rkold, metric, split_form, ducros_check, tvd_kappa, dirichlet, flux_type and
- * back_pressure into out[0..14] (n >= 15).  Needs no GPU. */
+ * delta, q, rkold, metric, split_form, ducros_check, tvd_kappa, dirichlet, flux_type,
+ * back_pressure, wall_temperature and ystretch into out[0..16] (n >= 17).  Needs no GPU. */
 int osb_desc_layout(long long* out, int n);
 
 #ifdef __cplusplus

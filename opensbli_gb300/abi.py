@@ -119,6 +119,7 @@ class BlockDesc(ctypes.Structure):
         ("flux_type", ctypes.c_int32),
         ("back_pressure", (ctypes.c_double * 2) * 3),
         ("wall_temperature", (ctypes.c_double * 2) * 3),
+        ("ystretch", ctypes.c_void_p * 2),
     ]
 
 
@@ -128,12 +129,13 @@ def layout_signature():
             BlockDesc.delta.offset, BlockDesc.q.offset, BlockDesc.rkold.offset, BlockDesc.metric.offset,
             BlockDesc.split_form.offset, BlockDesc.ducros_check.offset, BlockDesc.tvd_kappa.offset,
             BlockDesc.dirichlet.offset, BlockDesc.flux_type.offset, BlockDesc.back_pressure.offset,
-            BlockDesc.wall_temperature.offset]
+            BlockDesc.wall_temperature.offset, BlockDesc.ystretch.offset]
     return [ctypes.sizeof(BlockDesc)] + offs
 
 
-def make_desc(spec, q_ptrs, rk_ptrs, metric_ptrs=None, dirichlet_ptrs=None):
-    """Fill a BlockDesc from a BlockSpec (see backend.py) and raw array addresses."""
+def make_desc(spec, q_ptrs, rk_ptrs, metric_ptrs=None, dirichlet_ptrs=None, ystretch_ptrs=None):
+    """Fill a BlockDesc from a BlockSpec (see backend.py) and raw array addresses
+    (ystretch_ptrs: the D11 and SD111 rows of a stretched wall-normal grid)."""
     d = BlockDesc()
     d.ndim = spec.ndim
     for i in range(3):
@@ -179,6 +181,8 @@ def make_desc(spec, q_ptrs, rk_ptrs, metric_ptrs=None, dirichlet_ptrs=None):
     if dirichlet_ptrs:
         for (i, side), p in dirichlet_ptrs.items():
             d.dirichlet[i][side] = p
+    if ystretch_ptrs:
+        d.ystretch[0], d.ystretch[1] = ystretch_ptrs
     return d
 
 
@@ -224,6 +228,8 @@ def load_library():
     lib.osb_get_stream.argtypes = [vp, ctypes.POINTER(vp)]
     lib.osb_desc_layout.argtypes = [ctypes.POINTER(ctypes.c_longlong), i32]
     lib.osb_metrics.argtypes = [ctypes.POINTER(BlockDesc), ctypes.POINTER(vp), ctypes.POINTER(vp), i32, vp]
+    dp = ctypes.POINTER(ctypes.c_double)
+    lib.osb_ystretch_metrics.argtypes = [i32, ctypes.c_double, dp, i32, i32, dp, dp]
     lib.osb_stage_noalloc.argtypes = [ctypes.POINTER(BlockDesc), i32, ctypes.c_double, ctypes.c_double,
                                       ctypes.c_double, vp]
     lib.osb_set_schedule.argtypes = [vp, ctypes.POINTER(Schedule)]
@@ -240,6 +246,20 @@ def last_error(lib):
     return buf.value.decode(errors="replace")
 
 
+def ystretch_metrics(x1, delta, wall_lo=True, wall_hi=True):
+    """(D11, SD111) of a wall-normal grid line x1 (its interior rows) by osb_ystretch_metrics:
+    host work of the library, no GPU needed."""
+    import numpy as np
+    lib = load_library()
+    x = np.ascontiguousarray(x1, dtype=np.float64)
+    n = x.shape[0]
+    d11, sd = np.zeros(n), np.zeros(n)
+    dp = ctypes.POINTER(ctypes.c_double)
+    check(lib, lib.osb_ystretch_metrics(n, float(delta), x.ctypes.data_as(dp), int(wall_lo), int(wall_hi),
+                                        d11.ctypes.data_as(dp), sd.ctypes.data_as(dp)), "osb_ystretch_metrics")
+    return d11, sd
+
+
 def check(lib, rc, what):
     if rc != OSB_OK:
         raise OSBError("%s failed (%d): %s" % (what, rc, last_error(lib)))
@@ -251,7 +271,7 @@ EXPORTED = ["osb_version", "osb_last_error", "osb_ctx_create", "osb_ctx_destroy"
             "osb_set_rk", "osb_step", "osb_step_requests", "osb_stage", "osb_apply_bc", "osb_residual", "osb_reduce",
             "osb_sync", "osb_set_graphs", "osb_set_variant", "osb_set_central_staging", "osb_launch_count", "osb_get_stream",
             "osb_desc_layout", "osb_timing", "osb_timing_report", "osb_stage_noalloc", "osb_set_schedule",
-            "osb_get_schedule", "osb_metrics"]
+            "osb_get_schedule", "osb_metrics", "osb_ystretch_metrics"]
 
 NOALLOC_MAX_DOUBLES = 4 * 1024 * 1024
 

@@ -21,6 +21,7 @@
 #include <algorithm>
 #include <vector>
 
+#include "osb_closures.h"
 #include "osb_internal.h"
 
 using namespace osb;
@@ -593,10 +594,12 @@ __global__ void k_metric_f32(const double* m, float* out, long n) {
 // Reductions (compressible_TGV.py:176-206 and the CFL / NaN checks), FP64.
 __device__ __forceinline__ double uval(const BlockK& b, int v, long id) { return b.q[v][id] / b.q[0][id]; }
 
-__device__ __forceinline__ double d1g(const BlockK& b, int v, long id, int d) {
+// d u_v / dx_d at the point (row j); a stretched y grid scales the y derivative by D11 of the row
+__device__ __forceinline__ double d1g(const BlockK& b, int v, long id, int d, int j) {
   long s = b.st[d];
+  const double inv = (d == 1 && b.ys[0]) ? b.invd[1] * b.ys[0][j] : b.invd[d];
   return ((1.0 / 12.0) * uval(b, v, id - 2 * s) - (2.0 / 3.0) * uval(b, v, id - s) + (2.0 / 3.0) * uval(b, v, id + s) -
-          (1.0 / 12.0) * uval(b, v, id + 2 * s)) * b.invd[d];
+          (1.0 / 12.0) * uval(b, v, id + 2 * s)) * inv;
 }
 
 struct RedParams {
@@ -631,12 +634,12 @@ __global__ void k_reduce(BlockK b, RedParams rp, double* partial, int slot) {
       case 1: {
         double w2 = 0.0;
         if (nd == 3) {
-          double wx = d1g(b, 3, id, 1) - d1g(b, 2, id, 2);
-          double wy = d1g(b, 1, id, 2) - d1g(b, 3, id, 0);
-          double wz = d1g(b, 2, id, 0) - d1g(b, 1, id, 1);
+          double wx = d1g(b, 3, id, 1, j) - d1g(b, 2, id, 2, j);
+          double wy = d1g(b, 1, id, 2, j) - d1g(b, 3, id, 0, j);
+          double wz = d1g(b, 2, id, 0, j) - d1g(b, 1, id, 1, j);
           w2 = wx * wx + wy * wy + wz * wz;
         } else if (nd == 2) {
-          double wz = d1g(b, 2, id, 0) - d1g(b, 1, id, 1);
+          double wz = d1g(b, 2, id, 0, j) - d1g(b, 1, id, 1, j);
           w2 = wz * wz;
         }
         c = w2 * mu;
@@ -644,7 +647,7 @@ __global__ void k_reduce(BlockK b, RedParams rp, double* partial, int slot) {
       }
       case 2: {
         double div = 0.0;
-        for (int e = 0; e < nd; ++e) div += d1g(b, 1 + e, id, e);
+        for (int e = 0; e < nd; ++e) div += d1g(b, 1 + e, id, e, j);
         c = (4.0 / 3.0) * div * div * mu;
         break;
       }
@@ -652,7 +655,7 @@ __global__ void k_reduce(BlockK b, RedParams rp, double* partial, int slot) {
       case 4: {
         double a = sqrt(rp.gama * p / rho);
         double s = 0.0;
-        for (int e = 0; e < nd; ++e) s += (fabs(u[e]) + a) * b.invd[e];
+        for (int e = 0; e < nd; ++e) s += (fabs(u[e]) + a) * ((e == 1 && b.ys[0]) ? b.invd[1] * b.ys[0][j] : b.invd[e]);
         c = 1.0 / s;
         break;
       }
@@ -892,7 +895,7 @@ bool block_faces_ok(const osb_block_desc& d, std::string& why) {
 // Non-interface boundary faces of one block: the whole periodic halo shell in one launch when
 // every face is periodic with one depth, else direction by direction (transverse ranges include
 // the halos, so corners come from layers filled before) periodic, zero-gradient, extrapolation,
-// symmetry and Dirichlet faces.
+// symmetry, Dirichlet, pressure-outlet and wall faces.
 int apply_block_bc(osb_ctx* c, Block& bl, size_t ib, int fields) {
   const int nv = bl.d.ndim + 2;
   if (const int D = uniform_periodic_depth(bl)) {
@@ -1209,6 +1212,17 @@ bool check_desc(const osb_block_desc* d, std::string& why) {
         return false;
       }
     }
+  if ((d->ystretch[0] != nullptr) != (d->ystretch[1] != nullptr)) {
+    why = "a stretched y grid needs both D11 and SD111 (osb_block_desc.ystretch)";
+    return false;
+  }
+  if (d->ystretch[0]) {
+    auto wall = [](int k) { return k == OSB_BC_ISOTHERMAL_WALL || k == OSB_BC_ADIABATIC_WALL; };
+    if (d->ndim != 3 || d->metric[9] || d->viscous == OSB_VISC_NONE || !wall(d->bc[1][0]) || !wall(d->bc[1][1])) {
+      why = "a stretched y grid is implemented for 3D Cartesian viscous blocks with walls on both y faces";
+      return false;
+    }
+  }
   for (int i = 0; i < d->ndim; ++i)
     for (int s = 0; s < 2; ++s) {
       if (d->bc[i][s] != OSB_BC_INTERFACE) continue;
@@ -1280,7 +1294,7 @@ int osb_last_error(char* buf, size_t n) {
 }
 
 int osb_desc_layout(long long* out, int n) {
-  if (!out || n < 16) return fail(OSB_EINVAL, "need 16 slots");
+  if (!out || n < 17) return fail(OSB_EINVAL, "need 17 slots");
   out[0] = sizeof(osb_block_desc);
   out[1] = offsetof(osb_block_desc, size);
   out[2] = offsetof(osb_block_desc, bc);
@@ -1297,6 +1311,55 @@ int osb_desc_layout(long long* out, int n) {
   out[13] = offsetof(osb_block_desc, flux_type);
   out[14] = offsetof(osb_block_desc, back_pressure);
   out[15] = offsetof(osb_block_desc, wall_temperature);
+  out[16] = offsetof(osb_block_desc, ystretch);
+  return OSB_OK;
+}
+
+// Stretched wall-normal metrics of a grid line (the generated "MetricsEquation evaluation"
+// kernels of a y-stretched MetricsEquation: x1' and D11 = 1 / x1', then SD111 = D11'; each
+// derivative the central 4th-order rule, or the Carpenter closure rows in the four rows next to
+// a wall face).  Host work only.
+int osb_ystretch_metrics(int32_t n, double delta, const double* x1, int32_t wall_lo, int32_t wall_hi, double* d11,
+                         double* sd111) {
+  if (!x1 || !d11 || !sd111) return fail(OSB_EINVAL, "null argument");
+  if (n < 12) return fail(OSB_EINVAL, "a stretched line needs at least 12 points (got %d)", n);
+  if (!(delta > 0.0)) return fail(OSB_EINVAL, "delta must be positive");
+  const Closures& cl = closures();
+  const double inv = 1.0 / delta;
+  // derivative of f at row j: closure rows next to a wall, the central rule elsewhere (which
+  // needs j -2 .. j +2 inside the line: a line without walls is refused below)
+  auto der = [&](const std::vector<double>& f, int j, double& out) -> bool {
+    int r = -1;
+    bool hi = false;
+    if (wall_lo && j < 4) r = j;
+    else if (wall_hi && j > n - 5) { r = n - 1 - j; hi = true; }
+    double acc = 0.0;
+    if (r >= 0) {
+      for (int m = 0; m < 6; ++m) {
+        if (cl.c1[r][m] == 0.0) continue;
+        const int o = hi ? r - m : m - r;
+        acc += (hi ? -cl.c1[r][m] : cl.c1[r][m]) * f[j + o];
+      }
+    } else {
+      if (j < 2 || j > n - 3) return false;
+      acc = (1.0 / 12.0) * f[j - 2] - (2.0 / 3.0) * f[j - 1] + (2.0 / 3.0) * f[j + 1] - (1.0 / 12.0) * f[j + 2];
+    }
+    out = acc * inv;
+    return true;
+  };
+  std::vector<double> xl(x1, x1 + n), dl(n);
+  for (int j = 0; j < n; ++j) {
+    double xd = 0.0;
+    if (!der(xl, j, xd)) return fail(OSB_EINVAL, "row %d: a stretched line needs wall faces at both ends", j);
+    if (xd == 0.0 || !std::isfinite(xd)) return fail(OSB_EINVAL, "row %d: the grid line is not strictly monotone", j);
+    dl[j] = 1.0 / xd;
+    d11[j] = dl[j];
+  }
+  for (int j = 0; j < n; ++j) {
+    double v = 0.0;
+    der(dl, j, v);
+    sd111[j] = v;
+  }
   return OSB_OK;
 }
 
@@ -1463,6 +1526,7 @@ int osb_ctx_destroy(osb_ctx* c) {
     if (bl.qf_alt) cudaFree(bl.qf_alt);
     if (bl.filt_ws) cudaFree(bl.filt_ws);
     if (bl.xrows) cudaFree(bl.xrows);
+    if (bl.ys_buf) cudaFree(bl.ys_buf);
   }
   batch_free(c);
   requests_free(c);
@@ -1590,6 +1654,32 @@ int osb_block_add(osb_ctx* c, const osb_block_desc* d, int* block_id) {
       return fail(OSB_ECUDA, "filter workspace: %s", cudaGetErrorString(e));
     }
     OSB_CK(cudaMemsetAsync(bl.filt_ws, 0, bytes, c->stream));
+  }
+  if (d->ystretch[0]) {
+    // the stretched grid's D11 and SD111 rows, then their FP32 copies
+    const int n1 = k.n[1];
+    cudaError_t e = cudaMalloc(&bl.ys_buf, (sizeof(double) + sizeof(float)) * 2 * n1);
+    double* yd = static_cast<double*>(bl.ys_buf);
+    float* yf = reinterpret_cast<float*>(yd + 2 * n1);
+    for (int i = 0; i < 2 && e == cudaSuccess; ++i)
+      e = cudaMemcpyAsync(yd + i * n1, d->ystretch[i], sizeof(double) * n1, cudaMemcpyDefault, c->stream);
+    if (e != cudaSuccess) {
+      cudaFree(R);
+      if (bl.qf_base) cudaFree(bl.qf_base);
+      if (bl.qf_alt) cudaFree(bl.qf_alt);
+      if (bl.mf_buf) cudaFree(bl.mf_buf);
+      if (bl.filt_ws) cudaFree(bl.filt_ws);
+      if (bl.ys_buf) cudaFree(bl.ys_buf);
+      cudaFree(bl.xrows);
+      return fail(OSB_ECUDA, "stretched-grid rows: %s", cudaGetErrorString(e));
+    }
+    k_metric_f32<<<grid_for(c, 2 * n1, 256), 256, 0, c->stream>>>(yd, yf, 2 * n1);
+    c->launches++;
+    OSB_CK(cudaGetLastError());
+    k.ys[0] = yd;
+    k.ys[1] = yd + n1;
+    k.ysf[0] = yf;
+    k.ysf[1] = yf + n1;
   }
   if (c->qf_parity) batch_set_parity(c, 0);  // new tables start from the original buffers
   batch_free(c);
@@ -2079,6 +2169,14 @@ extern "C" int osb_stage_noalloc(const osb_block_desc* d, int rk_kind, double A,
         return fail(OSB_EINVAL, "state / RK array of variable %d lives on device %d, the current device is %d", v,
                     at.device, device);
     }
+  for (int w = 0; w < 2; ++w) {
+    if (!d->ystretch[w]) continue;
+    cudaPointerAttributes at;
+    OSB_CK(cudaPointerGetAttributes(&at, d->ystretch[w]));
+    if ((at.type != cudaMemoryTypeDevice && at.type != cudaMemoryTypeManaged) ||
+        (at.type == cudaMemoryTypeDevice && at.device != device))
+      return fail(OSB_EINVAL, "stretched-grid rows %d are not device memory of the current device", w);
+  }
   double* scratch = nullptr;
   int rc = noalloc_scratch(device, &scratch);
   if (rc) return rc;
@@ -2115,6 +2213,8 @@ extern "C" int osb_stage_noalloc(const osb_block_desc* d, int rk_kind, double A,
     k.rk[v] = d->rkold[v];
     k.R[v] = scratch + (size_t)v * k.alloc;
   }
+  k.ys[0] = d->ystretch[0];  // FP64 path: the caller's rows directly
+  k.ys[1] = d->ystretch[1];
   OSB_CK(cudaMemsetAsync(c.bad, 0, sizeof(unsigned long long), c.stream));
   rc = residual(&c, bl);
   if (rc) return rc;

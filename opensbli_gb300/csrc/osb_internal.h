@@ -22,6 +22,7 @@ struct Block {
   osb_block_desc d;
   BlockK k;
   float* mf_buf = nullptr;   // FP32 copies of the metrics (FP32-residual path, curvilinear)
+  void* ys_buf = nullptr;    // stretched y grid: D11, SD111 rows (FP64) and their FP32 copies
   float* qf_base = nullptr;  // FP32 state buffer allocated with the block (FP32-residual path)
   float* qf_alt = nullptr;   // second FP32 state buffer of the persistent stage's ping-pong
   void* filt_ws = nullptr;   // filtered blocks: kappa + 15 filter-flux arrays (residual precision)

@@ -28,10 +28,20 @@ struct BlockK {
   float* Rl[5];    // ... stored in the same bytes as the FP64 residual
   const double* m[10];  // curvilinear metrics (D_di at 3*d+i, det J at 9); null: Cartesian
   const float* mf[10];  // FP32 copies of the metrics (FP32-residual path)
+  const double* ys[2];  // stretched y grid: D11 and SD111 of the interior rows j; null: uniform
+  const float* ysf[2];  // their FP32 copies (FP32-residual path)
   double invd[3];  // 1/Delta
   double inv2d[3]; // 1/Delta^2
   float invdf[3];  // 1/Delta rounded to FP32 on the host (no conversion in FP32 kernels)
 };
+
+// Stretched y grid: D11 (w = 0) or SD111 (w = 1) of interior row j in the kernel's type.
+template <typename T>
+__device__ __forceinline__ T ystr(const BlockK& b, int w, int j);
+template <>
+__device__ __forceinline__ double ystr<double>(const BlockK& b, int w, int j) { return b.ys[w][j]; }
+template <>
+__device__ __forceinline__ float ystr<float>(const BlockK& b, int w, int j) { return b.ysf[w][j]; }
 
 // 1/Delta_d in the arithmetic type of a kernel.
 template <typename T>
@@ -450,6 +460,9 @@ __global__ void __launch_bounds__(SWEEP_THREADS, sizeof(T) == 4 ? 4 : 1)
       cart_flux<T, ND, SCH, AVG, FLX>(w, sp, fh);
     }
     if (j >= j0) {
+      // stretched y grid: -(F_j+1/2 - F_j-1/2) / Delta_1 * D11_j (the generated residual's order)
+      if constexpr (D == 1 && !CURV)
+        if (b.ys[0]) sc = invd * ystr<T>(b, 0, j);
       if constexpr (FUSE) {
 #pragma unroll
         for (int lv = 0; lv < NV; ++lv) {
@@ -899,10 +912,22 @@ __global__ void __launch_bounds__(CX * CY, bulk_ctas<CentralFields<T, CONV, VISC
   }
   const int gx = x0 + tx, gy = y0 + ty;
   const bool active = gx < b.n[0] && gy < b.n[1];
-  const T id0 = cpar<T>(cp.invd[0], cp.invd_f[0]), id1 = cpar<T>(cp.invd[1], cp.invd_f[1]),
-          id2 = cpar<T>(cp.invd[2], cp.invd_f[2]);
-  const T jd0 = cpar<T>(cp.inv2d[0], cp.inv2d_f[0]), jd1 = cpar<T>(cp.inv2d[1], cp.inv2d_f[1]),
-          jd2 = cpar<T>(cp.inv2d[2], cp.inv2d_f[2]);
+  const T id0 = cpar<T>(cp.invd[0], cp.invd_f[0]), id2 = cpar<T>(cp.invd[2], cp.invd_f[2]);
+  const T jd0 = cpar<T>(cp.inv2d[0], cp.inv2d_f[0]), jd2 = cpar<T>(cp.inv2d[2], cp.inv2d_f[2]);
+  T id1 = cpar<T>(cp.invd[1], cp.invd_f[1]), jd1 = cpar<T>(cp.inv2d[1], cp.inv2d_f[1]);
+  // WALL on a stretched y grid (metric.py:199-240, SD111 the only second-derivative metric):
+  // every y derivative of this thread's row takes D11 (d/dx_1 = D11 d/dxi_1, so 1/Delta_1 and
+  // 1/Delta_1^2 scale by D11 and D11^2), and the second ones add D11 SD111 d/dxi_1 = SD111 times
+  // the scaled first derivative
+  T sdy = L_(0.0);
+  if constexpr (WALL) {
+    if (b.ys[0] && gy < b.n[1]) {
+      const T d11 = ystr<T>(b, 0, gy);
+      id1 = id1 * d11;
+      jd1 = jd1 * (d11 * d11);
+      sdy = ystr<T>(b, 1, gy);
+    }
+  }
   // offsets are written as linear offsets of a virtual (x, y, z) tile with z stride CPL and
   // decoded into (plane, in-plane) parts; they are compile-time constants after unrolling
   const int sx = 1, sy = CSX, sz = CPL;
@@ -1140,12 +1165,18 @@ __global__ void __launch_bounds__(CX * CY, bulk_ctas<CentralFields<T, CONV, VISC
         dT[j] = D1(Fd::TT, S[j], ID[j]);
         lapT += D2(Fd::TT, S[j], JD[j]);
       }
+      if constexpr (WALL) lapT += dT[1] * sdy;
 #pragma unroll
       for (int i = 0; i < 3; ++i) {
         T s = L_(0.0);
 #pragma unroll
         for (int j = 0; j < 3; ++j) s += D2(UF[i], S[j], JD[j]);
-        s += L_(1.0 / 3.0) * D2(UF[i], S[i], JD[i]);
+        if constexpr (WALL) {
+          s += du[i][1] * sdy;
+          s += L_(1.0 / 3.0) * (i == 1 ? D2(UF[i], S[i], JD[i]) + du[1][1] * sdy : D2(UF[i], S[i], JD[i]));
+        } else {
+          s += L_(1.0 / 3.0) * D2(UF[i], S[i], JD[i]);
+        }
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
           if (j == i) continue;

@@ -75,7 +75,15 @@ def tgv(n=64, minf=0.1, scheme=abi.SCHEME_CENTRAL4, averaging=abi.AVG_SIMPLE, vi
     return spec, _cons(spec, r, [u0, u1, u2], p)
 
 
-def channel_iso(sizes=(16, 17, 8), twall=1.0, minf=0.5, re=100.0, upper="isothermal"):
+def stretched_line(n, stretch, j=None):
+    """Wall-normal coordinate y = -tanh(s (1 - 2 j / (n - 1))) / tanh(s) of the rows j (default
+    the interior rows 0..n-1), the generated grid kernel's operation order
+    (apps/channel_flow/compressible_TCF_TENO/turbulent_channel.py:178)."""
+    j = np.arange(n) if j is None else j
+    return -1.0 * np.tanh((1.0 - 2.0 * j / (-1.0 + n)) * stretch) / np.tanh(stretch)
+
+
+def channel_iso(sizes=(16, 17, 8), twall=1.0, minf=0.5, re=100.0, upper="isothermal", stretch=None):
     """3D channel between isothermal no-slip walls at y = -1 and y = 1 (IsothermalWallBC on both
     y faces, Twall = `twall`), periodic in x on [0, 2pi) and z on [0, 2pi), uniform grid with the
     walls on the first and last points in y (Delta_y = 2 / (N_y - 1)), characteristic LLF TENO5
@@ -85,7 +93,11 @@ def channel_iso(sizes=(16, 17, 8), twall=1.0, minf=0.5, re=100.0, upper="isother
     perturbed parabolic profile, u0 = (1 - y^2)(1 + 0.1 sin x cos z), u1 = 0.05 sin x (1 - y^2)^2,
     u2 = 0.05 cos x sin z (1 - y^2), p = (1 + 0.02 cos x cos z) / (gama Minf^2),
     rho = 1 + 0.02 sin x y.  upper = "adiabatic" makes the upper wall an AdiabaticWallBC (the
-    alternative upper wall of apps/channel_flow/laminar_2D/laminar_channel.py:104-113)."""
+    alternative upper wall of apps/channel_flow/laminar_2D/laminar_channel.py:104-113).
+
+    stretch = s (e.g. 1.7): the wall-normal grid of apps/channel_flow/compressible_TCF_TENO/
+    turbulent_channel.py:170-232, y = -tanh(s (1 - 2 j / (N_y - 1))) / tanh(s) on xi_1 in [0, 1]
+    (Delta_1 = 1 / (N_y - 1)), whose metrics D11 / SD111 (osb_ystretch_metrics) the spec carries."""
     n0, n1, n2 = sizes
     spec = BlockSpec(ndim=3, size=sizes, scheme=abi.SCHEME_TENO5, averaging=abi.AVG_ROE,
                      viscous=abi.VISC_SUTHERLAND,
@@ -93,12 +105,17 @@ def channel_iso(sizes=(16, 17, 8), twall=1.0, minf=0.5, re=100.0, upper="isother
                          [abi.BC_ISOTHERMAL_WALL, abi.BC_ISOTHERMAL_WALL if upper == "isothermal" else abi.BC_ADIABATIC_WALL],
                          [abi.BC_PERIODIC] * 2],
                      bc_depth=[[4, 4] for _ in range(3)],
-                     delta=(2.0 * math.pi / n0, 2.0 / (n1 - 1), 2.0 * math.pi / n2), gama=1.4, Minf=minf, Re=re,
+                     delta=(2.0 * math.pi / n0, (1.0 if stretch else 2.0) / (n1 - 1), 2.0 * math.pi / n2),
+                     gama=1.4, Minf=minf, Re=re,
                      Pr=0.71, mu_const=1.0, eps=1e-40, teno_ct=1e-6,
                      wall_temperature={(1, 0): float(twall), (1, 1): float(twall)} if upper == "isothermal"
                      else {(1, 0): float(twall)})
     x0 = spec.delta[0] * spec.grid_index(0)
-    x1 = -1.0 + spec.delta[1] * spec.grid_index(1)
+    if stretch:
+        x1 = stretched_line(n1, stretch, spec.grid_index(1))
+        spec.ystretch = abi.ystretch_metrics(stretched_line(n1, stretch), spec.delta[1])
+    else:
+        x1 = -1.0 + spec.delta[1] * spec.grid_index(1)
     x2 = spec.delta[2] * spec.grid_index(2)
     g = spec.gama
     w = 1.0 - x1 * x1

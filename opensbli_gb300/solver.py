@@ -46,6 +46,7 @@ class Solver:
         self.rk = []
         self.met = []
         self._dirichlet = []
+        self._ystretch = []
         self._descs = []
         try:
             for i, item in enumerate(specs_states):
@@ -79,8 +80,14 @@ class Solver:
                            for k, a in spec.dirichlet.items()}
                     self._dirichlet.append(dt_)
                     dp = {k: a.data_ptr() for k, a in dt_.items()}
+                yp = None
+                if spec.ystretch is not None:  # the library copies the rows at osb_block_add
+                    ys = [torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).to(self.device)
+                          for a in spec.ystretch]
+                    self._ystretch.append(ys)
+                    yp = [a.data_ptr() for a in ys]
                 d = abi.make_desc(spec, [q[v].data_ptr() for v in range(spec.nvars)],
-                                  [r[v].data_ptr() for v in range(spec.nvars)], mp, dp)
+                                  [r[v].data_ptr() for v in range(spec.nvars)], mp, dp, yp)
                 self._descs.append(d)
                 bid = ctypes.c_int()
                 torch.cuda.synchronize(self.device)

@@ -51,6 +51,9 @@ class BlockSpec:
     # a curvilinear block: its metric arrays (osb_block_desc.metric) must be supplied; a
     # curvilinear block without them is refused instead of being run as a Cartesian one
     curvilinear: bool = False
+    # a stretched wall-normal grid: (D11, SD111) of the interior rows (osb_block_desc.ystretch,
+    # abi.ystretch_metrics); delta[1] is then the spacing of xi_1
+    ystretch: tuple = None
 
     def __post_init__(self):
         self.size = tuple(int(s) for s in self.size)
@@ -112,6 +115,8 @@ class BlockSpec:
         if self.wall_temperature:  # (absent otherwise: records of blocks without walls are unchanged)
             rec["wall_temperature"] = [[d, s, float(v)] for (d, s), v in sorted(self.wall_temperature.items())]
         arrays = {"dirichlet_%d_%d" % k: np.ascontiguousarray(a) for k, a in (self.dirichlet or {}).items()}
+        if self.ystretch is not None:
+            arrays["ystretch_d11"], arrays["ystretch_sd111"] = (np.ascontiguousarray(a) for a in self.ystretch)
         return rec, arrays
 
     @classmethod
@@ -134,6 +139,9 @@ class BlockSpec:
                 dirichlet[(int(d), int(s))] = np.asarray(a, dtype=np.float64)
         if dirichlet:
             kw["dirichlet"] = dirichlet
+        if arrays is not None and "ystretch_d11" in arrays:
+            kw["ystretch"] = (np.asarray(arrays["ystretch_d11"], dtype=np.float64),
+                              np.asarray(arrays["ystretch_sd111"], dtype=np.float64))
         return cls(**kw)
 
     def same_discretisation(self, other):

@@ -58,6 +58,8 @@ def oracle():
         lib.oracle_reduce.argtypes = [P(abi.BlockDesc), ctypes.c_int, ctypes.c_int, P(ctypes.c_double)]
         lib.oracle_filter.argtypes = [P(abi.BlockDesc), ctypes.c_int, ctypes.c_double]
         lib.oracle_carpenter.argtypes = [ctypes.c_int, ctypes.c_int, P(ctypes.c_double)]
+        lib.oracle_ystretch_metrics.argtypes = [ctypes.c_int, ctypes.c_double, P(ctypes.c_double), ctypes.c_int,
+                                                ctypes.c_int, P(ctypes.c_double), P(ctypes.c_double)]
         _olib = lib
     return _olib
 
@@ -65,6 +67,19 @@ def oracle():
 def _ptr(a):
     assert a.dtype == np.float64 and a.flags.c_contiguous
     return a.ctypes.data
+
+
+def ystretch_metrics(x1, delta, wall_lo=True, wall_hi=True):
+    """(D11, SD111) of a wall-normal grid line by the oracle's restatement of the generated
+    metric kernels (oracle_ystretch_metrics)."""
+    x = np.ascontiguousarray(x1, dtype=np.float64)
+    n = x.shape[0]
+    d11, sd = np.zeros(n), np.zeros(n)
+    P = ctypes.POINTER(ctypes.c_double)
+    if oracle().oracle_ystretch_metrics(n, float(delta), x.ctypes.data_as(P), int(wall_lo), int(wall_hi),
+                                        d11.ctypes.data_as(P), sd.ctypes.data_as(P)):
+        raise ValueError("oracle_ystretch_metrics refused the line")
+    return d11, sd
 
 
 class OracleBlocks:
@@ -85,10 +100,13 @@ class OracleBlocks:
         arr = (abi.BlockDesc * len(self.specs))()
         self.dirichlet = [{k: np.ascontiguousarray(a, dtype=np.float64) for k, a in (s.dirichlet or {}).items()}
                           for s in self.specs]
+        self.ys = [None if s.ystretch is None else [np.ascontiguousarray(a, dtype=np.float64) for a in s.ystretch]
+                   for s in self.specs]
         for i, s in enumerate(self.specs):
             mp = None if self.met[i] is None else [None if a is None else _ptr(a) for a in self.met[i]]
             dp = {k: _ptr(a) for k, a in self.dirichlet[i].items()} or None
-            arr[i] = abi.make_desc(s, [_ptr(a) for a in self.q[i]], [_ptr(a) for a in self.rk[i]], mp, dp)
+            yp = None if self.ys[i] is None else [_ptr(a) for a in self.ys[i]]
+            arr[i] = abi.make_desc(s, [_ptr(a) for a in self.q[i]], [_ptr(a) for a in self.rk[i]], mp, dp, yp)
         self.desc = arr
 
     def residual(self, ib=0):

@@ -696,6 +696,53 @@ int oracle_carpenter(int order, int r, double* w) {
   return -1;
 }
 
+/* Wall-normal stretching metrics of a grid line x1[j], j = 0..n-1: the generated "MetricsEquation
+ * evaluation" kernels of a MetricsEquation with direction 1 stretched only (metric.py:183-197,
+ * transform_second_derivative metric.py:199-240): x1' = d x1 / d xi_1 by the central 4th-order
+ * rule, or the closure rows above in the four rows next to a wall face; D11 = 1 / x1' (and
+ * det J = x1'); SD111 = d D11 / d xi_1 by the same rules.  Returns -1 when a row has no rule
+ * (no wall at an end) or the line is not strictly monotone. */
+int oracle_ystretch_metrics(int n, double delta, const double* x1, int wall_lo, int wall_hi, double* d11,
+                            double* sd111) {
+  carpenter_init();
+  if (n < 12) return -1;
+  const double inv = 1.0 / delta;
+  for (int pass = 0; pass < 2; ++pass) {
+    const double* f = pass == 0 ? x1 : d11;
+    double* out = pass == 0 ? d11 : sd111;
+    double* tmp = (double*)malloc(sizeof(double) * n);
+    for (int j = 0; j < n; ++j) {
+      int r = -1, hi = 0;
+      if (wall_lo && j < 4) r = j;
+      else if (wall_hi && j > n - 5) { r = n - 1 - j; hi = 1; }
+      double acc;
+      if (r >= 0) {
+        acc = 0.0;
+        for (int m = 0; m < 6; ++m) {
+          if (carp1[r][m] == 0.0) continue;
+          const int o = hi ? r - m : m - r;
+          acc += (hi ? -carp1[r][m] : carp1[r][m]) * f[j + o];
+        }
+        acc *= inv;
+      } else {
+        if (j < 2 || j > n - 3) { free(tmp); return -1; }
+        acc = d1c(f, j, 1, inv);
+      }
+      tmp[j] = acc;
+    }
+    for (int j = 0; j < n; ++j) {
+      if (pass == 0) {
+        if (tmp[j] == 0.0 || !isfinite(tmp[j])) { free(tmp); return -1; }
+        out[j] = 1.0 / tmp[j];
+      } else {
+        out[j] = tmp[j];
+      }
+    }
+    free(tmp);
+  }
+  return 0;
+}
+
 /* Closure row of the point with index i along d for derivatives of `order`: 0..3 (first) or
  * 0..1 (second) next to a low wall face, 4 + r next to a high one, -1 for the central rule. */
 static inline int is_wall(int kind) { return kind == OSB_BC_ISOTHERMAL_WALL || kind == OSB_BC_ADIABATIC_WALL; }
@@ -771,6 +818,16 @@ static void viscous_point(const osb_block_desc* b, const geom_t* g, const cr_t* 
   const int nd = b->ndim;
   double inv[3], inv2[3];
   for (int d = 0; d < nd; ++d) { inv[d] = 1.0 / b->delta[d]; inv2[d] = 1.0 / (b->delta[d] * b->delta[d]); }
+  /* stretched y (metric.py:199-240 with only SD111 non-zero): d/dx_1 = D11 d/dxi_1 and
+   * d2/dx_1^2 = D11^2 d2/dxi_1^2 + D11 SD111 d/dxi_1 (the generated viscous kernel's
+   * D11*D11*d2_u_dy + D11*wk*SD111); mixed derivatives take D11 once */
+  double sd = 0.0;
+  if (b->ystretch[0]) {
+    const double d11 = b->ystretch[0][pc[1]];
+    inv[1] *= d11;
+    inv2[1] *= d11 * d11;
+    sd = b->ystretch[1][pc[1]];
+  }
   double du[3][3], lap[3], dmu[3], dT[3], lapT = 0.0;
   for (int i = 0; i < nd; ++i)
     for (int j = 0; j < nd; ++j) du[i][j] = d1at(b, g, c->u[i], id, pc, j, inv[j]);
@@ -781,11 +838,13 @@ static void viscous_point(const osb_block_desc* b, const geom_t* g, const cr_t* 
     dT[j] = d1at(b, g, c->T, id, pc, j, inv[j]);
     lapT += d2at(b, g, c->T, id, pc, j, inv2[j]);
   }
+  lapT += dT[1] * sd;
   /* lap_i = sum_j d2u_i/dx_j^2 + 1/3 d/dx_i (div u) */
   for (int i = 0; i < nd; ++i) {
     double s = 0.0;
     for (int j = 0; j < nd; ++j) s += d2at(b, g, c->u[i], id, pc, j, inv2[j]);
-    s += (1.0 / 3.0) * d2at(b, g, c->u[i], id, pc, i, inv2[i]);
+    s += du[i][1] * sd;
+    s += (1.0 / 3.0) * (d2at(b, g, c->u[i], id, pc, i, inv2[i]) + (i == 1 ? du[1][1] * sd : 0.0));
     for (int j = 0; j < nd; ++j) {
       if (j == i) continue;
       int a = i < j ? i : j, bb = i < j ? j : i;
@@ -899,7 +958,11 @@ int oracle_residual(const osb_block_desc* b, double* const* Rout) {
               for (int d = 0; d < nd; ++d) r += (fh[d][v][id] - fh[d][v][id - g.st[d]]) * (1.0 / b->delta[d]);
               r = -r / b->metric[9][id];
             } else {
-              for (int d = 0; d < nd; ++d) r -= (fh[d][v][id] - fh[d][v][id - g.st[d]]) * (1.0 / b->delta[d]);
+              for (int d = 0; d < nd; ++d) {
+                /* stretched y: the generated residual's -(F_j - F_j-1) invDelta1 D11 */
+                const double sc = (d == 1 && b->ystretch[0]) ? b->ystretch[0][j] : 1.0;
+                r -= (fh[d][v][id] - fh[d][v][id - g.st[d]]) * (1.0 / b->delta[d]) * sc;
+              }
             }
             Rout[v][id] = r;
           }
@@ -1856,12 +1919,13 @@ int oracle_reduce(const osb_block_desc* blocks, int nblocks, int what, double* o
     cr_t c;
     cr_alloc(&c, n);
     cr_compute(b, &g, &c);
-    double inv[3];
-    for (int d = 0; d < nd; ++d) inv[d] = 1.0 / b->delta[d];
+    double inv0[3], inv[3];
+    for (int d = 0; d < nd; ++d) inv0[d] = inv[d] = 1.0 / b->delta[d];
     for (int k = 0; k < g.n[2]; ++k)
       for (int j = 0; j < g.n[1]; ++j)
         for (int i = 0; i < g.n[0]; ++i) {
           long id = gid(&g, i, j, k);
+          if (b->ystretch[0]) inv[1] = inv0[1] * b->ystretch[0][j]; /* d/dx_1 = D11 d/dxi_1 */
           double rho = b->q[0][id];
           if (what == OSB_RED_RHO_SUM) acc += rho;
           else if (what == OSB_RED_KE) {

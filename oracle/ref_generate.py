@@ -323,39 +323,61 @@ def case_channel_adi():
     return case_channel_iso(upper="adiabatic")
 
 
-def case_channel_iso(upper="isothermal"):
+def case_channel_iso(upper="isothermal", stretch=False):
     """3D channel between isothermal no-slip walls: characteristic LLF TENO5 (Roe average) plus
     4th-order central viscous terms (StoreSome), the shock-capturing form of the SBLI apps, on a
     uniform grid; IsothermalWallBC on both y faces with the wall energy of
     ``apps/channel_flow/compressible_TCF_Central/turbulent_channel.py:118-131`` (no forcing
     terms), periodic in x and z, RK-LS3.  The wall faces take the reference's default Carpenter
-    closures of the central derivatives (core/boundary_conditions/Carpenter_scheme.py)."""
+    closures of the central derivatives (core/boundary_conditions/Carpenter_scheme.py).
+
+    stretch=True: the wall-normal grid of ``apps/channel_flow/compressible_TCF_TENO/
+    turbulent_channel.py:170-232``, x1 = -tanh(stretch (1 - 2 j / (N_y - 1))) / tanh(stretch) with
+    stretch = 1.7 on xi_1 in [0, 1] (Delta_1 = 1 / (N_y - 1)), transformed by a MetricsEquation
+    with direction 1 stretched only and applied to the equations (``apply_metrics``); the
+    velocity, pressure and density fields take the grid's x0, x1, x2."""
     import copy
     from opensbli import (RoeAverage, LFTeno, StoreSome, RungeKuttaLS, PeriodicBC, IsothermalWallBC,
                           AdiabaticWallBC, SimulationBlock, GridBasedInitialisation, GridVariable, DataObject,
-                          parse_expr, ConstantObject, Eq)
+                          parse_expr, ConstantObject, Eq, MetricsEquation)
     ndim = 3
     sim = _euler_equations(ndim, "Teno", viscous=True)
     cr = _constituents(ndim, viscous=True)
     block = SimulationBlock(ndim, block_number=0)
     local_dict = {"block": block, "GridVariable": GridVariable, "DataObject": DataObject}
-    eqns = ["Eq(GridVariable(x0), block.deltas[0]*block.grid_indexes[0])",
-            "Eq(GridVariable(x1), -1.0 + block.deltas[1]*block.grid_indexes[1])",
-            "Eq(GridVariable(x2), block.deltas[2]*block.grid_indexes[2])",
-            "Eq(GridVariable(u0), (1.0 - x1*x1)*(1.0 + 0.1*sin(x0)*cos(x2)))",
-            "Eq(GridVariable(u1), 0.05*sin(x0)*(1.0 - x1*x1)*(1.0 - x1*x1))",
-            "Eq(GridVariable(u2), 0.05*cos(x0)*sin(x2)*(1.0 - x1*x1))",
-            "Eq(GridVariable(p), 1.0/(gama*Minf*Minf)*(1.0 + 0.02*cos(x0)*cos(x2)))",
-            "Eq(GridVariable(r), 1.0 + 0.02*sin(x0)*x1)",
-            "Eq(DataObject(rho), r)", "Eq(DataObject(rhou0), r*u0)", "Eq(DataObject(rhou1), r*u1)",
-            "Eq(DataObject(rhou2), r*u2)",
-            "Eq(DataObject(rhoE), p/(gama-1) + 0.5* r *(u0**2+ u1**2 + u2**2))"]
+    fields = ["Eq(GridVariable(u0), (1.0 - x1*x1)*(1.0 + 0.1*sin(x0)*cos(x2)))",
+              "Eq(GridVariable(u1), 0.05*sin(x0)*(1.0 - x1*x1)*(1.0 - x1*x1))",
+              "Eq(GridVariable(u2), 0.05*cos(x0)*sin(x2)*(1.0 - x1*x1))",
+              "Eq(GridVariable(p), 1.0/(gama*Minf*Minf)*(1.0 + 0.02*cos(x0)*cos(x2)))",
+              "Eq(GridVariable(r), 1.0 + 0.02*sin(x0)*x1)",
+              "Eq(DataObject(rho), r)", "Eq(DataObject(rhou0), r*u0)", "Eq(DataObject(rhou1), r*u1)",
+              "Eq(DataObject(rhou2), r*u2)",
+              "Eq(DataObject(rhoE), p/(gama-1) + 0.5* r *(u0**2+ u1**2 + u2**2))"]
     initial = GridBasedInitialisation()
-    initial.add_equations([parse_expr(e, local_dict=local_dict) for e in eqns])
+    if stretch:
+        from sympy import tanh
+        (i, j, k) = block.grid_indexes
+        (dx, dy, dz) = block.deltas
+        ny, st = ConstantObject("block0np1"), ConstantObject("stretch")
+        x1 = 0.5 * 2 * (1.0 - tanh(st * (1.0 - 2.0 * (j / (ny - 1.0)))) / tanh(st)) - 1.0
+        grid = [Eq(DataObject("x0"), i * dx), Eq(DataObject("x1"), x1), Eq(DataObject("x2"), k * dz)]
+        fields = [f.replace("x0", "DataObject(x0)").replace("x1", "DataObject(x1)").replace("x2", "DataObject(x2)")
+                  for f in fields]
+        initial.add_equations(grid + [parse_expr(e, local_dict=local_dict) for e in fields])
+        metriceq = MetricsEquation()
+        metriceq.generate_transformations(ndim, "x", [(False, False), (True, False), (False, False)], 2)
+        sim.apply_metrics(metriceq)
+        equations = [copy.deepcopy(cr), sim, initial, metriceq]
+    else:
+        eqns = ["Eq(GridVariable(x0), block.deltas[0]*block.grid_indexes[0])",
+                "Eq(GridVariable(x1), -1.0 + block.deltas[1]*block.grid_indexes[1])",
+                "Eq(GridVariable(x2), block.deltas[2]*block.grid_indexes[2])"] + fields
+        initial.add_equations([parse_expr(e, local_dict=local_dict) for e in eqns])
+        equations = [copy.deepcopy(cr), copy.deepcopy(sim), initial]
     schemes = {}
     LF = LFTeno(order=5, averaging=RoeAverage([0, 1]), flux_type="LLF")
     schemes[LF.name] = LF
-    cent = StoreSome(4, "u0 u1 u2")
+    cent = StoreSome(4, "u0 u1 u2 T" if stretch else "u0 u1 u2")
     schemes[cent.name] = cent
     rk = RungeKuttaLS(3)
     schemes[rk.name] = rk
@@ -368,12 +390,15 @@ def case_channel_iso(upper="isothermal"):
            IsothermalWallBC(1, 1, wall[:]) if upper == "isothermal" else AdiabaticWallBC(1, 1),
            PeriodicBC(2, 0, halos=[-4, 4]), PeriodicBC(2, 1, halos=[-4, 4])]
     block.set_block_boundaries(bcs)
-    block.set_equations([copy.deepcopy(cr), copy.deepcopy(sim), initial])
+    block.set_equations(equations)
     block.discretise()
     p = {"Re": "100.0", "gama": "1.4", "Minf": "0.5", "Pr": "0.71", "Twall": "1.0",
          "dt": 'osb_env_double("OSB_DT", 0.001)', "niter": 'osb_env_int("OSB_NITER", 1)',
          "TENO_CT": 'osb_env_double("OSB_TENO_CT", 1e-6)'}
-    for d, (n, dl) in enumerate([(16, "2*M_PI/block0np0"), (17, "2.0/(block0np1-1)"), (8, "2*M_PI/block0np2")]):
+    if stretch:
+        p["stretch"] = "1.7"
+    d1 = "1.0/(block0np1-1)" if stretch else "2.0/(block0np1-1)"
+    for d, (n, dl) in enumerate([(16, "2*M_PI/block0np0"), (17, d1), (8, "2*M_PI/block0np2")]):
         p["block0np%d" % d] = 'osb_env_int("OSB_NP%d", %d)' % (d, n)
         p["Delta%dblock0" % d] = dl
     return block, p
@@ -716,6 +741,7 @@ CASES = {
     "mb2_flip": case_mb2_flip,
     "channel_iso": case_channel_iso,
     "channel_adi": case_channel_adi,
+    "channel_str": lambda: case_channel_iso(stretch=True),
 }
 
 

@@ -69,6 +69,12 @@ CASES = {
     "channel_adi_16x17x8_perturbed": ("channel_adi", lambda: problems.channel_iso((16, 17, 8), upper="adiabatic"),
                                       {"OSB_NP0": 16, "OSB_NP1": 17, "OSB_NP2": 8}, 1e-3, [1, 3, 30],
                                       (1e-3, 42)),
+    # the isothermal channel on the stretched wall-normal grid of the TENO turbulent-channel app
+    # (MetricsEquation stretched in y, applied to the equations); the solver's own D11 / SD111
+    # rows are stored with the states
+    "channel_str_16x17x8_perturbed": ("channel_str", lambda: problems.channel_iso((16, 17, 8), stretch=1.7),
+                                      {"OSB_NP0": 16, "OSB_NP1": 17, "OSB_NP2": 8}, 1e-3, [1, 3, 30],
+                                      (1e-3, 43)),
     # 3D curvilinear TENO5 (MetricsEquation, every direction curvilinear); the solver's own metric
     # arrays are stored with the states (interior; their halos are the periodic images)
     "curv3d_teno5_16x12x10_perturbed": ("curv3d_teno5", lambda: problems.curvilinear_wave_3d((16, 12, 10)),
@@ -99,7 +105,14 @@ def make(name):
         out["after_%d" % n] = np.stack([r[nm][sl] for nm in names])
         if n == 1 and "Residual0_B0" in r:
             out["residual_1"] = np.stack([r["Residual%d_B0" % v][sl] for v in range(spec.nvars)])
-        if n == 1 and spec.ndim == 3 and "detJ_B0" in r:
+        if n == 1 and spec.ystretch is not None:
+            h = spec.halo
+            line = (slice(h, h + 1), slice(h, h + spec.size[1]), slice(h, h + 1))
+            out["ystretch"] = np.stack([r[m][line].reshape(-1) for m in ("D11_B0", "SD111_B0")])
+            for m in ("D11_B0", "SD111_B0"):  # a function of the row only
+                a = r[m][sl]
+                assert np.array_equal(a, np.broadcast_to(a[:1, :, :1], a.shape))
+        elif n == 1 and spec.ndim == 3 and "detJ_B0" in r:
             mets = [r[m + "_B0"] for m in METRIC_NAMES]
             for m in mets:  # the generated solver exchanges its metrics periodically
                 b = np.zeros_like(m)

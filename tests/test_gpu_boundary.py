@@ -232,16 +232,18 @@ def test_pressure_outlet_matches_reference_solver(built_lib, oracle_lib, precisi
             assert np.max(np.abs(got[v][box] - ob.q[0][v][box])) < 1e-12 * np.max(np.abs(ob.q[0][v])), v
 
 
-CHANNELS = {"iso": ("channel_iso_16x17x8_perturbed.npz", "isothermal", 41),
-            "adi": ("channel_adi_16x17x8_perturbed.npz", "adiabatic", 42)}
+CHANNELS = {"iso": ("channel_iso_16x17x8_perturbed.npz", "isothermal", 41, None),
+            "adi": ("channel_adi_16x17x8_perturbed.npz", "adiabatic", 42, None),
+            "str": ("channel_str_16x17x8_perturbed.npz", "isothermal", 43, 1.7)}
 
 
 def _golden_channel(kind="iso"):
-    """The golden channel: isothermal walls on both y faces ("iso"), or the upper one adiabatic ("adi")."""
+    """The golden channel: isothermal walls on both y faces ("iso"), the upper one adiabatic
+    ("adi"), or isothermal walls on the stretched wall-normal grid of the TENO channel app ("str")."""
     import os
-    name, upper, seed = CHANNELS[kind]
+    name, upper, seed, stretch = CHANNELS[kind]
     g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", name))
-    spec, q = problems.channel_iso((16, 17, 8), upper=upper)
+    spec, q = problems.channel_iso((16, 17, 8), upper=upper, stretch=stretch)
     rng = np.random.default_rng(seed)
     q = [a * (1.0 + 1e-3 * rng.standard_normal(a.shape)) for a in q]
     return spec, q, g
@@ -263,7 +265,8 @@ def test_wall_channel_matches_reference_solver(built_lib, oracle_lib, kind, prec
     """The 3D channel between isothermal no-slip walls (TENO5 + viscous terms with the Carpenter
     closures at both walls) on the GPU: 10 steps against the reference's generated solver
     (golden, 30 stages) and, in FP64, against the oracle on the interior and the walls' halo
-    layers (1e-12); with the upper wall adiabatic as well."""
+    layers (1e-12); with the upper wall adiabatic, and on the stretched wall-normal grid (the y
+    flux difference and every y derivative of the viscous terms scaled by D11, SD111 terms)."""
     from opensbli_gb300.solver import Solver
     spec, q, g = _golden_channel(kind)
     s = Solver([(spec, q)], precision=precision, rk="ls3")
@@ -305,8 +308,9 @@ def test_wall_residual_matches_oracle(built_lib, oracle_lib, kind):
 
 
 def test_isothermal_wall_refused_outside_its_scope(built_lib):
-    """Walls on a face other than y, on a central-scheme block, or without a wall temperature
-    are refused at osb_block_add."""
+    """Walls on a face other than y, on a central-scheme block, or without a wall temperature,
+    and a stretched y grid without walls on both y faces or without viscous terms, are refused
+    at osb_block_add."""
     from opensbli_gb300.solver import Solver
     spec, q = problems.channel_iso((16, 17, 8))
     bad = []
@@ -320,6 +324,13 @@ def test_isothermal_wall_refused_outside_its_scope(built_lib):
     s3.bc = [[abi.BC_ISOTHERMAL_WALL] * 2, [abi.BC_PERIODIC] * 2, [abi.BC_PERIODIC] * 2]
     s3.wall_temperature = {(0, 0): 1.0, (0, 1): 1.0}
     bad.append(s3)
+    # a stretched y grid needs walls on both y faces and viscous terms
+    s4 = problems.channel_iso((16, 17, 8), stretch=1.7)[0]
+    s4.bc = [[abi.BC_PERIODIC] * 2, [abi.BC_PERIODIC] * 2, [abi.BC_PERIODIC] * 2]
+    bad.append(s4)
+    s5 = problems.channel_iso((16, 17, 8), stretch=1.7)[0]
+    s5.viscous = abi.VISC_NONE
+    bad.append(s5)
     for sp in bad:
         with pytest.raises(abi.OSBError):
             Solver([(sp, q)], precision="fp64", rk="ls3")

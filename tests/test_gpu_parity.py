@@ -227,6 +227,21 @@ def test_reductions(built_lib, oracle_lib, what):
     assert abs(got - ref) <= 1e-12 * max(abs(ref), 1.0), (got, ref)
 
 
+@pytest.mark.parametrize("what", [abi.RED_KE, abi.RED_ENSTROPHY_DISS, abi.RED_DILATATION_DISS, abi.RED_CFL_DT])
+def test_reductions_stretched_grid(built_lib, oracle_lib, what):
+    """Reductions on the stretched wall-normal grid: the y derivatives and the CFL's y term take
+    D11 of the row."""
+    spec, q = problems.channel_iso((16, 17, 8), stretch=1.7)
+    s = _solver([(spec, q)], precision="fp64")
+    s.apply_bc()
+    got = s.reduce(what)
+    s.close()
+    ob = harness.OracleBlocks([(spec, q)])
+    ob.apply_bc()
+    ref = ob.reduce(what)
+    assert abs(got - ref) <= 1e-12 * max(abs(ref), 1.0), (got, ref)
+
+
 # ---- FP32 residual path ---------------------------------------------------------------
 
 def test_fp32_residual_tgv_teno5_one_step(built_lib, oracle_lib):

@@ -61,10 +61,38 @@ CASES = {
     "channel_iso_16x17x8_perturbed": (lambda: problems.channel_iso((16, 17, 8)), "ls3", (1e-3, 41), 1e-12),
     "channel_adi_16x17x8_perturbed": (lambda: problems.channel_iso((16, 17, 8), upper="adiabatic"), "ls3",
                                       (1e-3, 42), 1e-12),
+    # the same on the stretched wall-normal grid of the TENO turbulent-channel app (D11 / SD111)
+    "channel_str_16x17x8_perturbed": (lambda: _channel_str(), "ls3", (1e-3, 43), 1e-12),
 }
 
 
 OUTLET_PLANE_OVERWRITTEN = {"shock_reflection_pout_64x32_perturbed"}
+
+
+def _channel_str(sizes=(16, 17, 8), stretch=1.7):
+    """The stretched channel with the oracle's own wall-normal metrics (oracle_ystretch_metrics
+    of the grid line) in place of the library's."""
+    spec, q = problems.channel_iso(sizes, stretch=stretch)
+    spec.ystretch = harness.ystretch_metrics(problems.stretched_line(sizes[1], stretch), spec.delta[1])
+    return spec, q
+
+
+def test_ystretch_metrics_match_reference(oracle_lib, built_lib):
+    """D11 / SD111 of the stretched grid: the oracle's restatement against the reference solver's
+    own arrays (1e-12: the grid line's tanh and the summation order differ at rounding level,
+    which the two differentiations amplify to ~1e-13), and the library's osb_ystretch_metrics
+    against the oracle (identical)."""
+    g = np.load(os.path.join(GOLD, "channel_str_16x17x8_perturbed.npz"))
+    line = problems.stretched_line(17, 1.7)
+    d = 1.0 / 16.0
+    ours = harness.ystretch_metrics(line, d)
+    for a, b in zip(ours, g["ystretch"]):
+        assert harness.rel_err(a, b) < 1e-12
+    lib = abi.ystretch_metrics(line, d)
+    for a, b in zip(lib, ours):
+        assert np.array_equal(a, b)
+    with pytest.raises(ValueError):
+        harness.ystretch_metrics(line, d, wall_lo=False)  # no rule for the rows next to a free end
 
 
 def perturb(q, amp, seed):

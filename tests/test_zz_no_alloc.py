@@ -77,8 +77,12 @@ def _check(spec, q, rk, stages, dt):
         keep = {k: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).to(dev)
                 for k, a in spec.dirichlet.items()}
         dp = {k: a.data_ptr() for k, a in keep.items()}
+    yp = None
+    if spec.ystretch is not None:
+        keep_ys = [torch.from_numpy(np.ascontiguousarray(a)).to(dev) for a in spec.ystretch]
+        yp = [a.data_ptr() for a in keep_ys]
     d = abi.make_desc(spec, [qd[v].data_ptr() for v in range(spec.nvars)],
-                      [rkd[v].data_ptr() for v in range(spec.nvars)], None, dp)
+                      [rkd[v].data_ptr() for v in range(spec.nvars)], None, dp, yp)
     torch.cuda.synchronize()
     for st in stages:
         rc = lib.osb_stage_noalloc(ctypes.byref(d), kind, A[st], B[st], dt, None)
@@ -112,6 +116,14 @@ def test_stage_noalloc_walls(built_lib):
     viscous terms: the wall kernels and the closure-aware central kernel on the noalloc path."""
     spec, q = problems.channel_iso((16, 17, 8), upper="adiabatic")
     rng = np.random.default_rng(5)
+    q = [a * (1.0 + 1e-3 * rng.standard_normal(a.shape)) for a in q]
+    _check(spec, q, "ls3", [0, 1], 1e-3)
+
+
+def test_stage_noalloc_stretched_walls(built_lib):
+    """The walls on the stretched wall-normal grid (osb_block_desc.ystretch rows on the device)."""
+    spec, q = problems.channel_iso((16, 17, 8), stretch=1.7)
+    rng = np.random.default_rng(6)
     q = [a * (1.0 + 1e-3 * rng.standard_normal(a.shape)) for a in q]
     _check(spec, q, "ls3", [0, 1], 1e-3)
 
