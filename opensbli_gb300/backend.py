@@ -344,6 +344,8 @@ def metrics_of(block):
     if not mets:
         return None
     me = mets[0]
+    if ystretch_of(block) is not None:
+        return None  # the stretched wall-normal grid: a Cartesian block with D11 / SD111 rows
     if not all(getattr(me, "curvilinear_metric", [])) or len(me.curvilinear_metric) != block.ndim:
         raise NotImplementedError("MetricsEquation with stretched-only or Cartesian directions (%s) is not supported; "
                                   "every direction must be curvilinear" % (getattr(me, "curvilinear_metric", None),))
@@ -358,6 +360,34 @@ def metrics_of(block):
                     "boundaries need the one-sided Carpenter closures, which are not implemented" % (
                         type(b).__name__, d, side))
     return [str(c) for c in me.cartesian_coordinates]
+
+
+def ystretch_of(block):
+    """Coordinate name of the wall-normal direction (x1) of a 3D block whose MetricsEquation
+    stretches direction 1 only (generate_transformations(3, 'x', [(False, False), (True, False),
+    (False, False)], 2), metric.py:43-64, applied to the equations: the form of
+    apps/channel_flow/compressible_TCF_TENO/turbulent_channel.py:225-228), None otherwise."""
+    mets = [ec for ec in block.list_of_equation_classes if type(ec).__name__ == "MetricsEquation"]
+    if not mets or block.ndim != 3:
+        return None
+    me = mets[0]
+    if any(getattr(me, "curvilinear_metric", [True])) or list(getattr(me, "stretching_metric", [])) != [False, True,
+                                                                                                         False]:
+        return None
+    return str(me.cartesian_coordinates[1])
+
+
+def _ystretch_rows(block, spec, params, name):
+    """(D11, SD111) of the wall-normal grid line the block's initialisation defines
+    (abi.ystretch_metrics, the generated metric kernels); the line must not vary in x or z."""
+    x1 = coordinates(block, spec, params, [name])[0]
+    sl = spec.interior()
+    h = spec.halo
+    line = np.ascontiguousarray(x1[h, h:h + spec.size[1], h])
+    if not np.array_equal(x1[sl], np.broadcast_to(line[None, :, None], x1[sl].shape)):
+        raise NotImplementedError("a stretched y grid whose %s varies in x or z is not supported" % name)
+    return abi.ystretch_metrics(line, spec.delta[1], spec.bc[1][0] in (abi.BC_ISOTHERMAL_WALL, abi.BC_ADIABATIC_WALL),
+                                spec.bc[1][1] in (abi.BC_ISOTHERMAL_WALL, abi.BC_ADIABATIC_WALL))
 
 
 def block_spec(block, params):
@@ -395,6 +425,12 @@ def block_spec(block, params):
              for side, b in enumerate(pair) if bc[d][side] == abi.BC_ISOTHERMAL_WALL}
     if walls:
         spec.wall_temperature = walls
+    ycoord = ystretch_of(block)
+    if ycoord is not None:
+        wall = (abi.BC_ISOTHERMAL_WALL, abi.BC_ADIABATIC_WALL)
+        if visc == abi.VISC_NONE or bc[1][0] not in wall or bc[1][1] not in wall:
+            raise NotImplementedError("a stretched y grid is implemented for viscous blocks with walls on both y faces")
+        spec.ystretch = _ystretch_rows(block, spec, params, ycoord)
     return spec
 
 
@@ -623,7 +659,8 @@ class BackendPlan:
             specs, states, coords = [], [], []
             for ib, rec in enumerate(meta["specs"]):
                 pre = "b%d_" % ib
-                arr = {k[len(pre):]: f[k] for k in f.files if k.startswith(pre + "dirichlet_")}
+                arr = {k[len(pre):]: f[k] for k in f.files
+                       if k.startswith(pre + "dirichlet_") or k.startswith(pre + "ystretch_")}
                 spec = BlockSpec.from_record(rec, arr)
                 specs.append(spec)
                 states.append([f[pre + "q%d" % v] for v in range(spec.nvars)])

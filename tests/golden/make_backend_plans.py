@@ -63,6 +63,13 @@ CASES = {
                                     "dt": "0.001", "niter": "10", "TENO_CT": "1e-6", "block0np0": "16",
                                     "block0np1": "17", "block0np2": "8", "Delta0block0": "2*M_PI/block0np0",
                                     "Delta1block0": "2.0/(block0np1-1)", "Delta2block0": "2*M_PI/block0np2"}),
+    # the isothermal channel on the stretched wall-normal grid of the TENO turbulent-channel app
+    # (MetricsEquation stretched in y, applied to the equations)
+    "channel_str": ("channel_str", {"Re": "100.0", "gama": "1.4", "Minf": "0.5", "Pr": "0.71", "Twall": "1.0",
+                                    "stretch": "1.7", "dt": "0.001", "niter": "10", "TENO_CT": "1e-6",
+                                    "block0np0": "16", "block0np1": "17", "block0np2": "8",
+                                    "Delta0block0": "2*M_PI/block0np0", "Delta1block0": "1.0/(block0np1-1)",
+                                    "Delta2block0": "2*M_PI/block0np2"}),
     # Kelvin-Helmholtz with the classic SBLI RK3
     "kh_32": ("kh_weno5z", {"gama": "1.4", "dt": "0.0002", "niter": "6", "block0np0": "32", "block0np1": "32",
                             "Delta0block0": "1.0/block0np0", "Delta1block0": "1.0/block0np1", "khamp": "1.0",

@@ -232,7 +232,8 @@ def test_pressure_outlet_maps_and_runs_in_the_oracle():
     assert max(errs) < 1e-12, errs
 
 
-PLANS = ["sod400", "tgv_teno5_12", "curv128", "curv3d_16x12x10", "shock_64x32", "kh_32", "mb2_flip", "channel_iso", "channel_adi"]
+PLANS = ["sod400", "tgv_teno5_12", "curv128", "curv3d_16x12x10", "shock_64x32", "kh_32", "mb2_flip", "channel_iso",
+         "channel_adi", "channel_str"]
 
 
 @needs_ref
@@ -247,6 +248,26 @@ def test_backend_plan_matches_committed_fixture(name):
     script = os.path.join(os.path.dirname(__file__), "golden", "make_backend_plans.py")
     r = subprocess.run([sys.executable, script, "--check", name], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+
+
+def test_stretched_channel_plan_is_the_stretched_channel(built_lib):
+    """The TENO channel app's stretched wall-normal grid (MetricsEquation stretched in y, applied
+    to the equations) as the backend maps it (the committed plan, which
+    test_backend_plan_matches_committed_fixture pins to the script): a Cartesian block with the
+    D11 / SD111 rows of its grid line, identical to problems.channel_iso(stretch=1.7), and the
+    same initial state to rounding."""
+    from opensbli_gb300.backend import BackendPlan
+    plan = BackendPlan.load(os.path.join(os.path.dirname(__file__), "golden", "plan_channel_str.npz"))
+    sp = plan.specs[0]
+    spec, q = problems.channel_iso((16, 17, 8), stretch=1.7)
+    assert not sp.curvilinear and plan.coords == [None]
+    for a, b in zip(sp.ystretch, spec.ystretch):
+        assert np.array_equal(a, b)
+    for k in ("size", "scheme", "averaging", "viscous", "bc", "bc_depth", "delta", "wall_temperature", "Re", "Minf"):
+        assert getattr(sp, k) == getattr(spec, k), k
+    sl = spec.interior()
+    for v in range(spec.nvars):
+        assert np.max(np.abs(plan.states[0][v][sl] - q[v][sl])) <= 1e-15 * np.max(np.abs(q[v][sl])), v
 
 
 @needs_ref
