@@ -51,11 +51,14 @@ extern "C" {
 #define OSB_AVG_SIMPLE 0
 #define OSB_AVG_ROE 1
 
-/* Viscous terms: none (Euler), modified Sutherland law mu(T) (compressible_TGV.py:82), or
- * constant viscosity (split_forms.py viscosity='constant'). */
+/* Viscous terms: none (Euler), modified Sutherland law mu(T) (compressible_TGV.py:82),
+ * constant viscosity (split_forms.py viscosity='constant'), or the power law mu = T^visc_power
+ * of apps/channel_flow/compressible_TCF_TENO/turbulent_channel.py:93 (restated in the oracle;
+ * the GPU kernels refuse it with OSB_EINVAL at osb_block_add). */
 #define OSB_VISC_NONE 0
 #define OSB_VISC_SUTHERLAND 1
 #define OSB_VISC_CONSTANT 2
+#define OSB_VISC_POWER_LAW 3
 
 /* Boundary conditions per face (core/boundary_conditions/). */
 #define OSB_BC_PERIODIC 0    /* PeriodicBC -> ExchangeSelf (periodic.py:25-71) */
@@ -166,6 +169,12 @@ typedef struct osb_block_desc {
    * viscous terms take them: d/dx_1 = D11 d/dxi_1, d2/dx_1^2 = D11^2 d2/dxi_1^2 + D11 SD111 d/dxi_1.
    * NULL for a uniform y grid.  3D Cartesian viscous blocks with wall faces on both y sides only. */
   const double* ystretch[2];
+  double visc_power;         /* OSB_VISC_POWER_LAW: the exponent (0.7 in the channel app) */
+  /* Constant source terms of the channel apps' momentum and energy equations
+   * (turbulent_channel.py:38-39, "- KD(_i,_j)*c_j" and "- Dot(c_j, u_j)"): R(rhou_i) -= c_i,
+   * R(rhoE) -= sum_j c_j u_j.  Restated in the oracle; the GPU kernels refuse non-zero values
+   * with OSB_EINVAL at osb_block_add. */
+  double forcing[3];
 } osb_block_desc;
 
 /* ---- library / context ------------------------------------------------------------- */
@@ -349,7 +358,8 @@ int osb_metrics(const osb_block_desc* desc, const double* const* x, double* cons
 
 /* Binding check: writes sizeof(osb_block_desc) and the byte offsets of size, bc, iface, gama,
  * delta, q, rkold, metric, split_form, ducros_check, tvd_kappa, dirichlet, flux_type,
- * back_pressure, wall_temperature and ystretch into out[0..16] (n >= 17).  Needs no GPU. */
+ * back_pressure, wall_temperature, ystretch, visc_power and forcing into out[0..18] (n >= 19).
+ * Needs no GPU. */
 int osb_desc_layout(long long* out, int n);
 
 #ifdef __cplusplus

@@ -28,6 +28,7 @@ AVG_ROE = 1
 VISC_NONE = 0
 VISC_SUTHERLAND = 1
 VISC_CONSTANT = 2
+VISC_POWER_LAW = 3  # mu = T^visc_power: oracle only (the GPU path refuses it)
 
 BC_PERIODIC = 0
 BC_ZERO_GRAD = 1
@@ -120,6 +121,8 @@ class BlockDesc(ctypes.Structure):
         ("back_pressure", (ctypes.c_double * 2) * 3),
         ("wall_temperature", (ctypes.c_double * 2) * 3),
         ("ystretch", ctypes.c_void_p * 2),
+        ("visc_power", ctypes.c_double),
+        ("forcing", ctypes.c_double * 3),
     ]
 
 
@@ -129,7 +132,8 @@ def layout_signature():
             BlockDesc.delta.offset, BlockDesc.q.offset, BlockDesc.rkold.offset, BlockDesc.metric.offset,
             BlockDesc.split_form.offset, BlockDesc.ducros_check.offset, BlockDesc.tvd_kappa.offset,
             BlockDesc.dirichlet.offset, BlockDesc.flux_type.offset, BlockDesc.back_pressure.offset,
-            BlockDesc.wall_temperature.offset, BlockDesc.ystretch.offset]
+            BlockDesc.wall_temperature.offset, BlockDesc.ystretch.offset, BlockDesc.visc_power.offset,
+            BlockDesc.forcing.offset]
     return [ctypes.sizeof(BlockDesc)] + offs
 
 
@@ -167,6 +171,9 @@ def make_desc(spec, q_ptrs, rk_ptrs, metric_ptrs=None, dirichlet_ptrs=None, ystr
     d.ducros_select = spec.ducros_select
     d.tvd_kappa = spec.tvd_kappa
     d.flux_type = spec.flux_type
+    d.visc_power = spec.visc_power
+    for i, c in enumerate(spec.forcing or (0.0, 0.0, 0.0)):
+        d.forcing[i] = c
     for (i, side), bp in (spec.back_pressure or {}).items():
         d.back_pressure[i][side] = bp
     for (i, side), tw in (spec.wall_temperature or {}).items():

@@ -390,6 +390,18 @@ def _ystretch_rows(block, spec, params, name):
                                 spec.bc[1][1] in (abi.BC_ISOTHERMAL_WALL, abi.BC_ADIABATIC_WALL))
 
 
+def _teno_eps(p):
+    """The TENO epsilon of the generated code: LFTeno gives its 'eps' constant the value 1e-40
+    (teno.py:368-371), which the code printer writes as a literal; parameter substitution only
+    fills constants declared without a value ('=Input', helperfunctions.py:150-175), so a script's
+    own 'eps' parameter (the TENO channel app passes 1e-15) does not reach the solver."""
+    from opensbli.core.kernel import ConstantsToDeclare
+    for c in ConstantsToDeclare.constants:
+        if str(c) == "eps" and getattr(c, "value", None) is not None:
+            return float(c.value)
+    return _const_value("eps", p, 1e-40)
+
+
 def block_spec(block, params):
     """BlockSpec of one OpenSBLI SimulationBlock."""
     p = resolve_parameters(params)
@@ -411,7 +423,7 @@ def block_spec(block, params):
                      iface=iface if any(f is not None for pair in iface for f in pair) else None,
                      split_form=split, filter=filt, tvd_kappa=kappa, flux_type=_flux_of(block),
                      gama=_const_value("gama", p), Minf=_const_value("Minf", p, 1.0), Re=_const_value("Re", p, 1.0),
-                     Pr=_const_value("Pr", p, 0.71), mu_const=1.0, eps=_const_value("eps", p, 1e-40),
+                     Pr=_const_value("Pr", p, 0.71), mu_const=1.0, eps=_teno_eps(p),
                      teno_ct=_const_value("TENO_CT", p, 1e-6),
                      shock_filter_control=_const_value("shock_filter_control", p, 1.0), delta=delta,
                      curvilinear=coords is not None)

@@ -1148,6 +1148,11 @@ bool check_desc(const osb_block_desc* d, std::string& why) {
   if (!(d->scheme == OSB_SCHEME_WENO5_JS || d->scheme == OSB_SCHEME_WENO5_Z || d->scheme == OSB_SCHEME_TENO5 ||
         d->scheme == OSB_SCHEME_TENO6 || d->scheme == OSB_SCHEME_CENTRAL4)) { why = "unknown scheme"; return false; }
   if (d->averaging != OSB_AVG_SIMPLE && d->averaging != OSB_AVG_ROE) { why = "unknown averaging"; return false; }
+  if (d->viscous == OSB_VISC_POWER_LAW || d->forcing[0] != 0.0 || d->forcing[1] != 0.0 || d->forcing[2] != 0.0) {
+    why = "the power-law viscosity and the constant forcing terms are restated in the oracle only (no GPU kernels)";
+    return false;
+  }
+  if (d->viscous < OSB_VISC_NONE || d->viscous > OSB_VISC_CONSTANT) { why = "unknown viscosity law"; return false; }
   for (int v = 0; v < d->ndim + 2; ++v)
     if (!d->q[v] || !d->rkold[v]) { why = "null state or RK array"; return false; }
   for (int i = 0; i < d->ndim; ++i)
@@ -1294,7 +1299,7 @@ int osb_last_error(char* buf, size_t n) {
 }
 
 int osb_desc_layout(long long* out, int n) {
-  if (!out || n < 17) return fail(OSB_EINVAL, "need 17 slots");
+  if (!out || n < 19) return fail(OSB_EINVAL, "need 19 slots");
   out[0] = sizeof(osb_block_desc);
   out[1] = offsetof(osb_block_desc, size);
   out[2] = offsetof(osb_block_desc, bc);
@@ -1312,6 +1317,8 @@ int osb_desc_layout(long long* out, int n) {
   out[14] = offsetof(osb_block_desc, back_pressure);
   out[15] = offsetof(osb_block_desc, wall_temperature);
   out[16] = offsetof(osb_block_desc, ystretch);
+  out[17] = offsetof(osb_block_desc, visc_power);
+  out[18] = offsetof(osb_block_desc, forcing);
   return OSB_OK;
 }
 

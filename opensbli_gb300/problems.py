@@ -127,6 +127,38 @@ def channel_iso(sizes=(16, 17, 8), twall=1.0, minf=0.5, re=100.0, upper="isother
     return spec, _cons(spec, r, [u0, u1, u2], p)
 
 
+def channel_tcf(sizes=(16, 17, 8), stretch=1.7):
+    """The discretisation and parameters of apps/channel_flow/compressible_TCF_TENO/
+    turbulent_channel.py: characteristic LLF TENO6 (Roe average) + central-4 viscous terms with
+    the power-law viscosity mu = T^0.7, the constant forcing c = (-1, 0, 0) (-c_i in the momentum
+    equations, -c_j u_j in the energy equation), isothermal walls (Twall 1) on the tanh-stretched
+    wall-normal grid (xi_1 in [0, 2], stretch 1.7), periodic x on [0, 4 pi) and z on
+    [0, 4 pi / 3), Re 190.71, Minf 0.0955, Pr 0.7, TENO_CT 1e-7, and the TENO epsilon 1e-40 that
+    the generated code uses (the app's eps = 1e-15 parameter does not reach it: LFTeno fixes the
+    value, teno.py:368-371); the initial fields of channel_iso on that grid.  The power law and
+    the forcing are restated in the oracle only: the GPU path refuses this spec."""
+    n0, n1, n2 = sizes
+    spec = BlockSpec(ndim=3, size=sizes, scheme=abi.SCHEME_TENO6, averaging=abi.AVG_ROE,
+                     viscous=abi.VISC_POWER_LAW, visc_power=0.7, forcing=(-1.0, 0.0, 0.0),
+                     bc=[[abi.BC_PERIODIC] * 2, [abi.BC_ISOTHERMAL_WALL] * 2, [abi.BC_PERIODIC] * 2],
+                     bc_depth=[[4, 4] for _ in range(3)],
+                     delta=(4.0 * math.pi / n0, 2.0 / (n1 - 1), (4.0 * math.pi / 3.0) / n2),
+                     gama=1.4, Minf=0.0955, Re=190.71, Pr=0.7, mu_const=1.0, eps=1e-40, teno_ct=1e-7,
+                     wall_temperature={(1, 0): 1.0, (1, 1): 1.0})
+    x0 = spec.delta[0] * spec.grid_index(0)
+    x1 = stretched_line(n1, stretch, spec.grid_index(1))
+    spec.ystretch = abi.ystretch_metrics(stretched_line(n1, stretch), spec.delta[1])
+    x2 = spec.delta[2] * spec.grid_index(2)
+    g = spec.gama
+    w = 1.0 - x1 * x1
+    u0 = w * (1.0 + 0.1 * np.sin(x0) * np.cos(x2))
+    u1 = 0.05 * np.sin(x0) * w * w
+    u2 = 0.05 * np.cos(x0) * np.sin(x2) * w
+    p = 1.0 / (g * spec.Minf * spec.Minf) * (1.0 + 0.02 * np.cos(x0) * np.cos(x2))
+    r = 1.0 + 0.02 * np.sin(x0) * x1
+    return spec, _cons(spec, r, [u0, u1, u2], p)
+
+
 def tgv_filtered(n=128, sizes=None, ducros=0.05):
     """The supersonic TGV of the reference's Central4-WENO5 benchmark
     (apps/performance_benchmark/Central4-WENO5; the central branch of

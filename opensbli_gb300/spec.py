@@ -54,6 +54,10 @@ class BlockSpec:
     # a stretched wall-normal grid: (D11, SD111) of the interior rows (osb_block_desc.ystretch,
     # abi.ystretch_metrics); delta[1] is then the spacing of xi_1
     ystretch: tuple = None
+    # OSB_VISC_POWER_LAW exponent, and the constant source terms c_j of the channel apps
+    # (osb_block_desc.visc_power / forcing; both restated in the oracle, refused by the GPU path)
+    visc_power: float = 0.0
+    forcing: tuple = None
 
     def __post_init__(self):
         self.size = tuple(int(s) for s in self.size)
@@ -112,6 +116,10 @@ class BlockSpec:
                                                         for r in self.iface]
         rec["back_pressure"] = None if not self.back_pressure else [[d, s, float(v)] for (d, s), v in
                                                                      sorted(self.back_pressure.items())]
+        if self.visc_power:  # (absent otherwise, like the wall temperatures)
+            rec["visc_power"] = float(self.visc_power)
+        if self.forcing and any(self.forcing):
+            rec["forcing"] = [float(c) for c in self.forcing]
         if self.wall_temperature:  # (absent otherwise: records of blocks without walls are unchanged)
             rec["wall_temperature"] = [[d, s, float(v)] for (d, s), v in sorted(self.wall_temperature.items())]
         arrays = {"dirichlet_%d_%d" % k: np.ascontiguousarray(a) for k, a in (self.dirichlet or {}).items()}
@@ -132,6 +140,10 @@ class BlockSpec:
             kw["back_pressure"] = {(int(d), int(s)): float(v) for d, s, v in rec["back_pressure"]}
         if rec.get("wall_temperature"):
             kw["wall_temperature"] = {(int(d), int(s)): float(v) for d, s, v in rec["wall_temperature"]}
+        if rec.get("visc_power"):
+            kw["visc_power"] = float(rec["visc_power"])
+        if rec.get("forcing"):
+            kw["forcing"] = tuple(float(c) for c in rec["forcing"])
         dirichlet = {}
         for name, a in (arrays or {}).items():
             if name.startswith("dirichlet_"):

@@ -116,6 +116,8 @@ static void cr_compute(const osb_block_desc* b, const geom_t* g, cr_t* c) {
     c->T[id] = T;
     if (b->viscous == OSB_VISC_SUTHERLAND)
       c->mu[id] = 1.4042 * T * sqrt(T) / (0.40417 + T);
+    else if (b->viscous == OSB_VISC_POWER_LAW) /* turbulent_channel.py:93, mu = T**0.7 */
+      c->mu[id] = pow(T, b->visc_power);
     else
       c->mu[id] = b->mu_const;
   }
@@ -980,6 +982,22 @@ int oracle_residual(const osb_block_desc* b, double* const* Rout) {
           const int pc[3] = {i, j, k};
           viscous_point(b, &g, &c, id, pc, r);
           for (int v = 1; v < nv; ++v) Rout[v][id] += r[v];
+        }
+  }
+  if (b->forcing[0] != 0.0 || b->forcing[1] != 0.0 || b->forcing[2] != 0.0) {
+    /* the channel apps' constant sources (turbulent_channel.py:38-39): -c_i in the momentum
+     * equations, -sum_j c_j u_j in the energy equation */
+#pragma omp parallel for schedule(static)
+    for (int k = 0; k < g.n[2]; ++k)
+      for (int j = 0; j < g.n[1]; ++j)
+        for (int i = 0; i < g.n[0]; ++i) {
+          long id = gid(&g, i, j, k);
+          double w = 0.0;
+          for (int e = 0; e < nd; ++e) {
+            Rout[1 + e][id] -= b->forcing[e];
+            w += b->forcing[e] * c.u[e][id];
+          }
+          Rout[nv - 1][id] -= w;
         }
   }
   cr_free(&c);

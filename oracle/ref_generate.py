@@ -404,6 +404,86 @@ def case_channel_iso(upper="isothermal", stretch=False):
     return block, p
 
 
+def case_channel_tcf():
+    """The equations and schemes of ``apps/channel_flow/compressible_TCF_TENO/turbulent_channel.py``
+    (lines 35-93, 139-246): Navier-Stokes with the constant forcing terms -KD(_i,_j) c_j and
+    -Dot(c_j, u_j), power-law viscosity mu = T^0.7, characteristic LLF TENO6 (Roe average),
+    StoreSome(4, 'u0 u1 u2 T'), the SSP RK3, isothermal walls on both y faces (Twall), periodic x
+    and z, and the tanh-stretched wall-normal grid on xi_1 in [0, 2] transformed by a
+    MetricsEquation stretched in y; the app's parameters (Re 190.71, Minf 0.0955, Pr 0.7,
+    c = (-1, 0, 0), stretch 1.7, TENO_CT 1e-7, eps 1e-15) on a 16 x 17 x 8 block.  The
+    initial fields are the channel cases' (the golden runs replace them); the statistics
+    classes and the HDF5 output of the app are not part of the residual path."""
+    import copy
+    from sympy import tanh
+    from opensbli import (EinsteinEquation, SimulationEquations, ConstituentRelations, RoeAverage, LFTeno,
+                          StoreSome, RungeKuttaLS, PeriodicBC, IsothermalWallBC, SimulationBlock,
+                          GridBasedInitialisation, GridVariable, DataObject, parse_expr, ConstantObject, Eq,
+                          MetricsEquation)
+    ndim = 3
+    sc1 = "**{'scheme':'Teno'}"
+    mass = "Eq(Der(rho,t), - Conservative(rhou_j,x_j,%s))" % sc1
+    momentum = ("Eq(Der(rhou_i,t) , -Conservative(rhou_i*u_j + KD(_i,_j)*p,x_j , %s) + Der(tau_i_j,x_j) "
+                "- KD(_i,_j)*c_j )" % sc1)
+    energy = ("Eq(Der(rhoE,t), - Conservative((p+rhoE)*u_j,x_j, %s) - Der(q_j,x_j) + Der(u_i*tau_i_j ,x_j) "
+              "- Dot(c_j, u_j))" % sc1)
+    subs = ["Eq(tau_i_j, (mu/Re)*(Der(u_i,x_j)+ Der(u_j,x_i) - (2/3)* KD(_i,_j)* Der(u_k,x_k)))",
+            "Eq(q_j, (-mu/((gama-1)*Minf*Minf*Pr*Re))*Der(T,x_j))"]
+    constants = ["Re", "Pr", "gama", "Minf", "c_j"]
+    eq = EinsteinEquation()
+    sim = SimulationEquations()
+    for base in (mass, momentum, energy):
+        sim.add_equations(eq.expand(base, ndim, "x", subs, constants))
+    cr = ConstituentRelations()
+    for r in ["Eq(u_i, rhou_i/rho)", "Eq(p, (gama-1)*(rhoE - rho*(1/2)*(KD(_i,_j)*u_i*u_j)))",
+              "Eq(a, (gama*p/rho)**0.5)", "Eq(T, p*gama*Minf*Minf/(rho))", "Eq(mu, (T**0.7))"]:
+        cr.add_equations(eq.expand(r, ndim, "x", subs, constants))
+    block = SimulationBlock(ndim, block_number=0)
+    local_dict = {"block": block, "GridVariable": GridVariable, "DataObject": DataObject}
+    (i, j, k) = block.grid_indexes
+    (dx, dy, dz) = block.deltas
+    ny, st = ConstantObject("block0np1"), ConstantObject("stretch")
+    x1 = 0.5 * 2 * (1.0 - tanh(st * (1.0 - 2.0 * (j / (ny - 1.0)))) / tanh(st)) - 1.0
+    grid = [Eq(DataObject("x0"), i * dx), Eq(DataObject("x1"), x1), Eq(DataObject("x2"), k * dz)]
+    fields = ["Eq(GridVariable(u0), (1.0 - DataObject(x1)*DataObject(x1))*(1.0 + 0.1*sin(DataObject(x0))*cos(DataObject(x2))))",
+              "Eq(GridVariable(u1), 0.05*sin(DataObject(x0))*(1.0 - DataObject(x1)*DataObject(x1))*(1.0 - DataObject(x1)*DataObject(x1)))",
+              "Eq(GridVariable(u2), 0.05*cos(DataObject(x0))*sin(DataObject(x2))*(1.0 - DataObject(x1)*DataObject(x1)))",
+              "Eq(GridVariable(p), 1.0/(gama*Minf*Minf)*(1.0 + 0.02*cos(DataObject(x0))*cos(DataObject(x2))))",
+              "Eq(GridVariable(r), 1.0 + 0.02*sin(DataObject(x0))*DataObject(x1))",
+              "Eq(DataObject(rho), r)", "Eq(DataObject(rhou0), r*u0)", "Eq(DataObject(rhou1), r*u1)",
+              "Eq(DataObject(rhou2), r*u2)",
+              "Eq(DataObject(rhoE), p/(gama-1) + 0.5* r *(u0**2+ u1**2 + u2**2))"]
+    initial = GridBasedInitialisation()
+    initial.add_equations(grid + [parse_expr(e, local_dict=local_dict) for e in fields])
+    metriceq = MetricsEquation()
+    metriceq.generate_transformations(ndim, "x", [(False, False), (True, False), (False, False)], 2)
+    sim.apply_metrics(metriceq)
+    schemes = {}
+    LF = LFTeno(order=6, averaging=RoeAverage([0, 1]), flux_type="LLF")
+    schemes[LF.name] = LF
+    cent = StoreSome(4, "u0 u1 u2 T")
+    schemes[cent.name] = cent
+    rk = RungeKuttaLS(3, formulation="SSP")
+    schemes[rk.name] = rk
+    block.set_discretisation_schemes(schemes)
+    q = flatten_q(sim)
+    gama, Minf, Twall = ConstantObject("gama"), ConstantObject("Minf"), ConstantObject("Twall")
+    wall = [Eq(q[4], Twall * q[0] / (gama * Minf ** 2.0 * (gama - 1)))]
+    bcs = [PeriodicBC(0, 0), PeriodicBC(0, 1), IsothermalWallBC(1, 0, wall[:]), IsothermalWallBC(1, 1, wall[:]),
+           PeriodicBC(2, 0), PeriodicBC(2, 1)]
+    block.set_block_boundaries(bcs)
+    block.set_equations([copy.deepcopy(cr), sim, initial, metriceq])
+    block.discretise()
+    p = {"Re": "190.71", "gama": "1.4", "Minf": "0.0955", "Pr": "0.7", "Twall": "1.0", "stretch": "1.7",
+         "c0": "-1", "c1": "0", "c2": "0", "eps": "1e-15",
+         "dt": 'osb_env_double("OSB_DT", 0.0002)', "niter": 'osb_env_int("OSB_NITER", 1)',
+         "TENO_CT": 'osb_env_double("OSB_TENO_CT", 1e-7)'}
+    for d, (n, dl) in enumerate([(16, "4.0*M_PI/block0np0"), (17, "2.0/(block0np1-1)"), (8, "(4.0*M_PI/3.0)/block0np2")]):
+        p["block0np%d" % d] = 'osb_env_int("OSB_NP%d", %d)' % (d, n)
+        p["Delta%dblock0" % d] = dl
+    return block, p
+
+
 def flatten_q(sim):
     from sympy import flatten
     return flatten(sim.time_advance_arrays)
@@ -742,6 +822,7 @@ CASES = {
     "channel_iso": case_channel_iso,
     "channel_adi": case_channel_adi,
     "channel_str": lambda: case_channel_iso(stretch=True),
+    "channel_tcf": case_channel_tcf,
 }
 
 

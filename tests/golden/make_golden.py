@@ -75,6 +75,11 @@ CASES = {
     "channel_str_16x17x8_perturbed": ("channel_str", lambda: problems.channel_iso((16, 17, 8), stretch=1.7),
                                       {"OSB_NP0": 16, "OSB_NP1": 17, "OSB_NP2": 8}, 1e-3, [1, 3, 30],
                                       (1e-3, 43)),
+    # the TENO turbulent-channel app's discretisation (TENO6, power-law viscosity, constant
+    # forcing, stretched wall-normal grid, SSP RK3)
+    "channel_tcf_16x17x8_perturbed": ("channel_tcf", lambda: problems.channel_tcf((16, 17, 8)),
+                                      {"OSB_NP0": 16, "OSB_NP1": 17, "OSB_NP2": 8}, 2e-4, [1, 3, 30],
+                                      (1e-3, 44)),
     # 3D curvilinear TENO5 (MetricsEquation, every direction curvilinear); the solver's own metric
     # arrays are stored with the states (interior; their halos are the periodic images)
     "curv3d_teno5_16x12x10_perturbed": ("curv3d_teno5", lambda: problems.curvilinear_wave_3d((16, 12, 10)),

@@ -63,6 +63,9 @@ CASES = {
                                       (1e-3, 42), 1e-12),
     # the same on the stretched wall-normal grid of the TENO turbulent-channel app (D11 / SD111)
     "channel_str_16x17x8_perturbed": (lambda: _channel_str(), "ls3", (1e-3, 43), 1e-12),
+    # the TENO turbulent-channel app's discretisation: TENO6, power-law viscosity, constant
+    # forcing, stretched wall-normal grid, SSP RK3
+    "channel_tcf_16x17x8_perturbed": (lambda: _channel_tcf(), "ssp3", (1e-3, 44), 1e-12),
 }
 
 
@@ -73,6 +76,13 @@ def _channel_str(sizes=(16, 17, 8), stretch=1.7):
     """The stretched channel with the oracle's own wall-normal metrics (oracle_ystretch_metrics
     of the grid line) in place of the library's."""
     spec, q = problems.channel_iso(sizes, stretch=stretch)
+    spec.ystretch = harness.ystretch_metrics(problems.stretched_line(sizes[1], stretch), spec.delta[1])
+    return spec, q
+
+
+def _channel_tcf(sizes=(16, 17, 8), stretch=1.7):
+    """The TENO channel app's case with the oracle's own wall-normal metrics."""
+    spec, q = problems.channel_tcf(sizes, stretch=stretch)
     spec.ystretch = harness.ystretch_metrics(problems.stretched_line(sizes[1], stretch), spec.delta[1])
     return spec, q
 
