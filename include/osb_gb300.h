@@ -53,8 +53,7 @@ extern "C" {
 
 /* Viscous terms: none (Euler), modified Sutherland law mu(T) (compressible_TGV.py:82),
  * constant viscosity (split_forms.py viscosity='constant'), or the power law mu = T^visc_power
- * of apps/channel_flow/compressible_TCF_TENO/turbulent_channel.py:93 (restated in the oracle;
- * the GPU kernels refuse it with OSB_EINVAL at osb_block_add). */
+ * of apps/channel_flow/compressible_TCF_TENO/turbulent_channel.py:93. */
 #define OSB_VISC_NONE 0
 #define OSB_VISC_SUTHERLAND 1
 #define OSB_VISC_CONSTANT 2
@@ -172,8 +171,8 @@ typedef struct osb_block_desc {
   double visc_power;         /* OSB_VISC_POWER_LAW: the exponent (0.7 in the channel app) */
   /* Constant source terms of the channel apps' momentum and energy equations
    * (turbulent_channel.py:38-39, "- KD(_i,_j)*c_j" and "- Dot(c_j, u_j)"): R(rhou_i) -= c_i,
-   * R(rhoE) -= sum_j c_j u_j.  Restated in the oracle; the GPU kernels refuse non-zero values
-   * with OSB_EINVAL at osb_block_add. */
+   * R(rhoE) -= sum_j c_j u_j, applied by the central viscous kernel (3D Cartesian viscous
+   * blocks; OSB_EINVAL otherwise). */
   double forcing[3];
 } osb_block_desc;
 

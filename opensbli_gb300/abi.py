@@ -28,7 +28,7 @@ AVG_ROE = 1
 VISC_NONE = 0
 VISC_SUTHERLAND = 1
 VISC_CONSTANT = 2
-VISC_POWER_LAW = 3  # mu = T^visc_power: oracle only (the GPU path refuses it)
+VISC_POWER_LAW = 3  # mu = T^visc_power (the TENO channel app)
 
 BC_PERIODIC = 0
 BC_ZERO_GRAD = 1

@@ -22,6 +22,8 @@ raises ``NotImplementedError``; there is no fallback.
 """
 import math
 
+import re
+
 import numpy as np
 
 from . import abi
@@ -125,28 +127,69 @@ def _scheme_of(block):
     return scheme, avg, central
 
 
-def _viscosity_of(block):
-    """OSB_VISC_* from the block's equations: a Sutherland-type mu(T) constituent relation, a
-    constant viscosity (viscous terms without a mu relation), or inviscid."""
-    from opensbli.equation_types.opensbliequations import ConstituentRelations, SimulationEquations
-    from sympy import flatten
-    has_mu = False
-    viscous = False
+def _mu_law(block):
+    """(OSB_VISC_SUTHERLAND, 0) for the modified Sutherland mu(T) relation, (OSB_VISC_POWER_LAW,
+    e) for mu = T**e (turbulent_channel.py:93), None without a mu relation."""
+    from opensbli.equation_types.opensbliequations import ConstituentRelations
+    from sympy import flatten, Pow
     for ec in block.list_of_equation_classes:
         if isinstance(ec, ConstituentRelations):
             for eq in flatten(ec.equations):
                 if str(eq.lhs).startswith("mu"):
-                    rhs = str(eq.rhs)
-                    if "1.4042" not in rhs or "0.40417" not in rhs:
-                        raise NotImplementedError("viscosity law %s is not supported" % rhs)
-                    has_mu = True
+                    rhs = eq.rhs
+                    if "1.4042" in str(rhs) and "0.40417" in str(rhs):
+                        return abi.VISC_SUTHERLAND, 0.0
+                    if isinstance(rhs, Pow) and str(rhs.base).startswith("T") and rhs.exp.is_number:
+                        return abi.VISC_POWER_LAW, float(rhs.exp)
+                    raise NotImplementedError("viscosity law %s is not supported" % rhs)
+    return None
+
+
+def _viscosity_of(block):
+    """OSB_VISC_* from the block's equations: a Sutherland-type or power-law mu(T) constituent
+    relation, a constant viscosity (viscous terms without a mu relation), or inviscid."""
+    from opensbli.equation_types.opensbliequations import SimulationEquations
+    from sympy import flatten
+    viscous = False
+    for ec in block.list_of_equation_classes:
         if isinstance(ec, SimulationEquations):
             for eq in flatten(ec.equations):
                 if "Re" in str(eq.rhs):
                     viscous = True
+    law = _mu_law(block)
     if not viscous:
         return abi.VISC_NONE
-    return abi.VISC_SUTHERLAND if has_mu else abi.VISC_CONSTANT
+    return abi.VISC_CONSTANT if law is None else law[0]
+
+
+def _forcing_of(block, p):
+    """(c0, c1, c2) of the channel apps' constant sources (turbulent_channel.py:38-39: "-
+    KD(_i,_j)*c_j" in the momentum equations, "- Dot(c_j, u_j)" in the energy equation), None
+    when the equations carry no c_j.  Any other use of c_j is refused."""
+    from opensbli.equation_types.opensbliequations import SimulationEquations
+    from sympy import flatten
+    nd = block.ndim
+    names = ["c%d" % i for i in range(nd)]
+    eqs = [eq for ec in block.list_of_equation_classes if isinstance(ec, SimulationEquations)
+           for eq in flatten(ec.equations)]
+    syms = {str(x): x for eq in eqs for x in eq.rhs.free_symbols if str(x) in names}
+    if not syms:
+        return None
+    for eq in eqs:
+        lhs = str(eq.lhs)
+        for i, n in enumerate(names):
+            if n not in syms:
+                continue
+            cf = eq.rhs.expand().coeff(syms[n])
+            if "rhoE" in lhs:
+                want = r"-u%d(_B\d+)?" % i  # energy (u_i, or its dataset once discretised)
+            elif "rhou%d" % i in lhs:
+                want = "-1"  # momentum i
+            else:
+                want = "0"  # mass, the other momentum components
+            if not re.fullmatch(want, str(cf)):
+                raise NotImplementedError("source term %s * %s in %s is not the channel apps' forcing" % (cf, n, lhs))
+    return tuple(float(_const_value(n, p, 0.0)) for n in names) + (0.0,) * (3 - nd)
 
 
 def _rk_of(block):
@@ -437,6 +480,12 @@ def block_spec(block, params):
              for side, b in enumerate(pair) if bc[d][side] == abi.BC_ISOTHERMAL_WALL}
     if walls:
         spec.wall_temperature = walls
+    law = _mu_law(block)
+    if visc == abi.VISC_POWER_LAW:
+        spec.visc_power = law[1]
+    forcing = _forcing_of(block, p)
+    if forcing is not None and any(forcing):
+        spec.forcing = forcing
     ycoord = ystretch_of(block)
     if ycoord is not None:
         wall = (abi.BC_ISOTHERMAL_WALL, abi.BC_ADIABATIC_WALL)

@@ -31,6 +31,13 @@ int launch_central_k(osb_ctx* c, Block& bl, int first, const RkFuse& rf) {
   cp.mu_c_f = (float)cp.mu_c;
   cp.invRe_f = (float)cp.invRe;
   cp.kheat_f = (float)cp.kheat;
+  cp.mu_pow = d.viscous == OSB_VISC_POWER_LAW ? d.visc_power : 0.0;
+  cp.mu_pow_f = (float)cp.mu_pow;
+  cp.forced = d.forcing[0] != 0.0 || d.forcing[1] != 0.0 || d.forcing[2] != 0.0;
+  for (int i = 0; i < 3; ++i) {
+    cp.force[i] = d.forcing[i];
+    cp.force_f[i] = (float)d.forcing[i];
+  }
   for (int i = 0; i < 3; ++i) {
     cp.invd[i] = bl.k.invd[i];
     cp.inv2d[i] = bl.k.inv2d[i];
@@ -100,16 +107,16 @@ template <typename T>
 int launch_central(osb_ctx* c, Block& bl, bool conv, int first, const RkFuse* rf) {
   const int visc = bl.d.viscous;
   if (conv && bl.d.split_form == OSB_SPLIT_KGP) {
-    if (visc == OSB_VISC_SUTHERLAND) return launch_central_t<T, 2, 1>(c, bl, first, rf);
+    if (visc == OSB_VISC_SUTHERLAND || visc == OSB_VISC_POWER_LAW) return launch_central_t<T, 2, 1>(c, bl, first, rf);
     if (visc == OSB_VISC_CONSTANT) return launch_central_t<T, 2, 2>(c, bl, first, rf);
     return launch_central_t<T, 2, 0>(c, bl, first, rf);
   }
   if (conv) {
-    if (visc == OSB_VISC_SUTHERLAND) return launch_central_t<T, 1, 1>(c, bl, first, rf);
+    if (visc == OSB_VISC_SUTHERLAND || visc == OSB_VISC_POWER_LAW) return launch_central_t<T, 1, 1>(c, bl, first, rf);
     if (visc == OSB_VISC_CONSTANT) return launch_central_t<T, 1, 2>(c, bl, first, rf);
     return launch_central_t<T, 1, 0>(c, bl, first, rf);
   }
-  if (visc == OSB_VISC_SUTHERLAND) return launch_central_t<T, 0, 1>(c, bl, first, rf);
+  if (visc == OSB_VISC_SUTHERLAND || visc == OSB_VISC_POWER_LAW) return launch_central_t<T, 0, 1>(c, bl, first, rf);
   if (visc == OSB_VISC_CONSTANT) return launch_central_t<T, 0, 2>(c, bl, first, rf);
   return OSB_OK;
 }

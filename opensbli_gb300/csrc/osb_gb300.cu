@@ -604,7 +604,7 @@ __device__ __forceinline__ double d1g(const BlockK& b, int v, long id, int d, in
 
 struct RedParams {
   int what, nv, visc;
-  double gama, Minf, mu_const;
+  double gama, Minf, mu_const, mu_pow;  // mu_pow: OSB_VISC_POWER_LAW exponent
 };
 
 __global__ void k_reduce(BlockK b, RedParams rp, double* partial, int slot) {
@@ -624,9 +624,9 @@ __global__ void k_reduce(BlockK b, RedParams rp, double* partial, int slot) {
     for (int e = 0; e < nd; ++e) { u[e] = b.q[1 + e][id] / rho; ke += u[e] * u[e]; }
     double p = (rp.gama - 1.0) * (b.q[rp.nv - 1][id] - 0.5 * rho * ke);
     double mu = rp.mu_const;
-    if (rp.visc == 1) {
+    if (rp.visc == OSB_VISC_SUTHERLAND || rp.visc == OSB_VISC_POWER_LAW) {
       double T = rp.Minf * rp.Minf * rp.gama * p / rho;
-      mu = 1.4042 * T * sqrt(T) / (0.40417 + T);
+      mu = rp.visc == OSB_VISC_POWER_LAW ? pow(T, rp.mu_pow) : 1.4042 * T * sqrt(T) / (0.40417 + T);
     }
     double c = 0.0;
     switch (rp.what) {
@@ -1148,11 +1148,16 @@ bool check_desc(const osb_block_desc* d, std::string& why) {
   if (!(d->scheme == OSB_SCHEME_WENO5_JS || d->scheme == OSB_SCHEME_WENO5_Z || d->scheme == OSB_SCHEME_TENO5 ||
         d->scheme == OSB_SCHEME_TENO6 || d->scheme == OSB_SCHEME_CENTRAL4)) { why = "unknown scheme"; return false; }
   if (d->averaging != OSB_AVG_SIMPLE && d->averaging != OSB_AVG_ROE) { why = "unknown averaging"; return false; }
-  if (d->viscous == OSB_VISC_POWER_LAW || d->forcing[0] != 0.0 || d->forcing[1] != 0.0 || d->forcing[2] != 0.0) {
-    why = "the power-law viscosity and the constant forcing terms are restated in the oracle only (no GPU kernels)";
+  if (d->viscous < OSB_VISC_NONE || d->viscous > OSB_VISC_POWER_LAW) { why = "unknown viscosity law"; return false; }
+  if (d->viscous == OSB_VISC_POWER_LAW && !(d->visc_power > 0.0)) {
+    why = "the power-law viscosity needs a positive exponent (visc_power)";
     return false;
   }
-  if (d->viscous < OSB_VISC_NONE || d->viscous > OSB_VISC_CONSTANT) { why = "unknown viscosity law"; return false; }
+  if ((d->forcing[0] != 0.0 || d->forcing[1] != 0.0 || d->forcing[2] != 0.0) &&
+      (d->ndim != 3 || d->viscous == OSB_VISC_NONE || d->metric[9])) {
+    why = "the constant forcing terms are applied by the central viscous kernel of 3D Cartesian blocks";
+    return false;
+  }
   for (int v = 0; v < d->ndim + 2; ++v)
     if (!d->q[v] || !d->rkold[v]) { why = "null state or RK array"; return false; }
   for (int i = 0; i < d->ndim; ++i)
@@ -1865,7 +1870,7 @@ int osb_reduce(osb_ctx* c, int what, double* host_out) {
     long n = (long)bl.k.n[0] * bl.k.n[1] * bl.k.n[2];
     int grid = std::min(grid_for(c, n, threads), 64);
     if (slot + grid > (c->red_slots + 8) * 64 - 1) return fail(OSB_ENOTSUP, "too many blocks for the reduction");
-    RedParams rp{what, bl.d.ndim + 2, bl.d.viscous, bl.d.gama, bl.d.Minf, bl.d.mu_const};
+    RedParams rp{what, bl.d.ndim + 2, bl.d.viscous, bl.d.gama, bl.d.Minf, bl.d.mu_const, bl.d.visc_power};
     k_reduce<<<grid, threads, 0, c->stream>>>(bl.k, rp, c->red, slot);
     c->launches++;
     slot += grid;

@@ -652,6 +652,11 @@ struct CentralParams {
   int wall_lo, wall_hi;
   double c1[4][6], c2[2][5];
   float c1f[4][6], c2f[2][5];
+  // VISC == 1 with mu_pow > 0: the power law mu = T^mu_pow (turbulent_channel.py:93) in place of
+  // the modified Sutherland law; forced: the constant sources -c_i (momentum), -c_j u_j (energy)
+  double mu_pow, force[3];
+  float mu_pow_f, force_f[3];
+  int forced;
 };
 template <typename T>
 __device__ __forceinline__ T cpar(double d, float f);
@@ -770,6 +775,7 @@ __global__ void __launch_bounds__(CX * CY, bulk_ctas<CentralFields<T, CONV, VISC
   const T gm = cpar<T>(cp.gama, cp.gama_f);
   const T M2 = cpar<T>(cp.M2, cp.M2_f);
   const T mu_c = cpar<T>(cp.mu_c, cp.mu_c_f);
+  const T mu_pw = cpar<T>(cp.mu_pow, cp.mu_pow_f);
   const T invRe = cpar<T>(cp.invRe, cp.invRe_f);
   const T kheat = cpar<T>(cp.kheat, cp.kheat_f);
   // raw state of one plane, CPP points per thread
@@ -805,7 +811,9 @@ __global__ void __launch_bounds__(CX * CY, bulk_ctas<CentralFields<T, CONV, VISC
       if (VISC) {
         T Tt = M2 * gm * p * ir;
         sm[Fd::TT * FS + at] = Tt;
-        sm[Fd::MU * FS + at] = (VISC == 1) ? L_(1.4042) * Tt * sqrt(Tt) / (L_(0.40417) + Tt) : mu_c;
+        sm[Fd::MU * FS + at] = (VISC == 1) ? (mu_pw > L_(0.0) ? pow(Tt, mu_pw)
+                                                              : L_(1.4042) * Tt * sqrt(Tt) / (L_(0.40417) + Tt))
+                                           : mu_c;
       }
       if (CONV) {
         sm[Fd::RHO * FS + at] = rho;
@@ -1208,6 +1216,16 @@ __global__ void __launch_bounds__(CX * CY, bulk_ctas<CentralFields<T, CONV, VISC
 #pragma unroll
       for (int j = 0; j < 3; ++j) h += dT[j] * dmu[j];
       racc[4] += e * invRe + h * kheat;
+      if (cp.forced) {
+        T w = L_(0.0);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+          const T fi = cpar<T>(cp.force[i], cp.force_f[i]);
+          racc[1 + i] -= fi;
+          w += fi * F(UF[i], 0);
+        }
+        racc[4] -= w;
+      }
     }
     const int v0 = CONV ? 0 : 1;
     if constexpr (FUSE) {

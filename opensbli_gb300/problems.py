@@ -135,8 +135,7 @@ def channel_tcf(sizes=(16, 17, 8), stretch=1.7):
     wall-normal grid (xi_1 in [0, 2], stretch 1.7), periodic x on [0, 4 pi) and z on
     [0, 4 pi / 3), Re 190.71, Minf 0.0955, Pr 0.7, TENO_CT 1e-7, and the TENO epsilon 1e-40 that
     the generated code uses (the app's eps = 1e-15 parameter does not reach it: LFTeno fixes the
-    value, teno.py:368-371); the initial fields of channel_iso on that grid.  The power law and
-    the forcing are restated in the oracle only: the GPU path refuses this spec."""
+    value, teno.py:368-371); the initial fields of channel_iso on that grid."""
     n0, n1, n2 = sizes
     spec = BlockSpec(ndim=3, size=sizes, scheme=abi.SCHEME_TENO6, averaging=abi.AVG_ROE,
                      viscous=abi.VISC_POWER_LAW, visc_power=0.7, forcing=(-1.0, 0.0, 0.0),

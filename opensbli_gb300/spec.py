@@ -55,7 +55,7 @@ class BlockSpec:
     # abi.ystretch_metrics); delta[1] is then the spacing of xi_1
     ystretch: tuple = None
     # OSB_VISC_POWER_LAW exponent, and the constant source terms c_j of the channel apps
-    # (osb_block_desc.visc_power / forcing; both restated in the oracle, refused by the GPU path)
+    # (osb_block_desc.visc_power / forcing)
     visc_power: float = 0.0
     forcing: tuple = None
 

@@ -70,6 +70,15 @@ CASES = {
                                     "block0np0": "16", "block0np1": "17", "block0np2": "8",
                                     "Delta0block0": "2*M_PI/block0np0", "Delta1block0": "1.0/(block0np1-1)",
                                     "Delta2block0": "2*M_PI/block0np2"}),
+    # the TENO turbulent-channel app's discretisation: TENO6, power-law viscosity, constant
+    # forcing, stretched wall-normal grid, SSP RK3 (the app's own parameters; its eps is the
+    # generator's fixed 1e-40)
+    "channel_tcf": ("channel_tcf", {"Re": "190.71", "gama": "1.4", "Minf": "0.0955", "Pr": "0.7", "Twall": "1.0",
+                                    "dt": "0.0002", "niter": "10", "block0np0": "16", "block0np1": "17",
+                                    "block0np2": "8", "Delta0block0": "4.0*M_PI/block0np0",
+                                    "Delta1block0": "2.0/(block0np1-1)", "Delta2block0": "(4.0*M_PI/3.0)/block0np2",
+                                    "c0": "-1", "c1": "0", "c2": "0", "stretch": "1.7", "TENO_CT": "1e-7",
+                                    "eps": "1e-15"}),
     # Kelvin-Helmholtz with the classic SBLI RK3
     "kh_32": ("kh_weno5z", {"gama": "1.4", "dt": "0.0002", "niter": "6", "block0np0": "32", "block0np1": "32",
                             "Delta0block0": "1.0/block0np0", "Delta1block0": "1.0/block0np1", "khamp": "1.0",

@@ -233,7 +233,7 @@ def test_pressure_outlet_maps_and_runs_in_the_oracle():
 
 
 PLANS = ["sod400", "tgv_teno5_12", "curv128", "curv3d_16x12x10", "shock_64x32", "kh_32", "mb2_flip", "channel_iso",
-         "channel_adi", "channel_str"]
+         "channel_adi", "channel_str", "channel_tcf"]
 
 
 @needs_ref
@@ -265,6 +265,26 @@ def test_stretched_channel_plan_is_the_stretched_channel(built_lib):
         assert np.array_equal(a, b)
     for k in ("size", "scheme", "averaging", "viscous", "bc", "bc_depth", "delta", "wall_temperature", "Re", "Minf"):
         assert getattr(sp, k) == getattr(spec, k), k
+    sl = spec.interior()
+    for v in range(spec.nvars):
+        assert np.max(np.abs(plan.states[0][v][sl] - q[v][sl])) <= 1e-15 * np.max(np.abs(q[v][sl])), v
+
+
+def test_teno_channel_app_plan_is_the_teno_channel(built_lib):
+    """The TENO turbulent-channel app's equations as the backend maps them (the committed plan):
+    TENO6, the power law mu = T^0.7, the forcing c = (-1, 0, 0) read from its -KD(_i,_j) c_j and
+    -Dot(c_j, u_j) terms, the stretched wall-normal grid, the SSP RK3, and the TENO epsilon of the
+    generated code (1e-40, not the script's eps parameter): identical to problems.channel_tcf."""
+    from opensbli_gb300.backend import BackendPlan
+    plan = BackendPlan.load(os.path.join(os.path.dirname(__file__), "golden", "plan_channel_tcf.npz"))
+    sp = plan.specs[0]
+    spec, q = problems.channel_tcf((16, 17, 8))
+    for k in ("size", "scheme", "averaging", "viscous", "visc_power", "forcing", "bc", "delta", "wall_temperature",
+              "Re", "Minf", "Pr", "eps", "teno_ct"):
+        assert getattr(sp, k) == getattr(spec, k), k
+    assert plan.rk[1] == tuple(problems.RK3_SSP_A) and plan.rk[2] == tuple(problems.RK3_SSP_B)
+    for a, b in zip(sp.ystretch, spec.ystretch):
+        assert np.array_equal(a, b)
     sl = spec.interior()
     for v in range(spec.nvars):
         assert np.max(np.abs(plan.states[0][v][sl] - q[v][sl])) <= 1e-15 * np.max(np.abs(q[v][sl])), v

@@ -41,7 +41,7 @@ def _oracle(plan, met):
 
 
 @pytest.mark.parametrize("name", ["sod400", "tgv_teno5_12", "curv128", "curv3d_16x12x10", "shock_64x32", "kh_32",
-                                  "mb2_flip", "channel_iso", "channel_adi", "channel_str"])
+                                  "mb2_flip", "channel_iso", "channel_adi", "channel_str", "channel_tcf"])
 def test_backend_plan_runs_like_the_oracle(built_lib, oracle_lib, name):
     import harness
     plan, got, met = _run(name)

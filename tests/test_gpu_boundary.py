@@ -287,6 +287,39 @@ def test_wall_channel_matches_reference_solver(built_lib, oracle_lib, kind, prec
             assert np.max(np.abs(got[v][box] - ob.q[0][v][box])) < 1e-12 * np.max(np.abs(ob.q[0][v][box])), v
 
 
+def test_teno_channel_app_matches_reference_solver(built_lib, oracle_lib):
+    """The TENO turbulent-channel app's discretisation (TENO6, power-law viscosity mu = T^0.7,
+    the constant forcing -c_i / -c_j u_j, isothermal walls on the stretched wall-normal grid, SSP
+    RK3), FP64 on the GPU: 10 steps against the reference's generated solver (golden, 30 stages)
+    and the oracle, through the walls' halo layers, at 1e-12; the residual of one stage at 1e-12."""
+    import os
+    from opensbli_gb300.solver import Solver
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "channel_tcf_16x17x8_perturbed.npz"))
+    spec, q = problems.channel_tcf((16, 17, 8))
+    rng = np.random.default_rng(44)
+    q = [a * (1.0 + 1e-3 * rng.standard_normal(a.shape)) for a in q]
+    rk = (abi.RK_LOW_STORAGE, problems.RK3_SSP_A, problems.RK3_SSP_B)
+    s = Solver([(spec, q)], precision="fp64", rk=rk)
+    s.apply_bc()
+    R = s.residual(0)
+    s.step(float(g["dt"]), 10)
+    got = s.state(0)
+    s.close()
+    sl = spec.interior()
+    errs = _channel_errors(got, g["after_30"], sl)
+    assert max(errs) < 1e-12, errs
+    ob = harness.OracleBlocks([(spec, q)])
+    ob.apply_bc()
+    Ro = ob.residual(0)
+    for v in range(5):
+        assert harness.rel_err(R[v][sl], Ro[v][sl]) < 1e-12, ("residual", v)
+    ob.step(*rk, float(g["dt"]), 10)
+    h, (n0, n1, n2) = spec.halo, spec.size
+    box = (slice(h, h + n2), slice(h - 4, h + n1 + 4), slice(h, h + n0))
+    for v in range(5):
+        assert np.max(np.abs(got[v][box] - ob.q[0][v][box])) < 1e-12 * np.max(np.abs(ob.q[0][v][box])), v
+
+
 @pytest.mark.parametrize("kind", sorted(CHANNELS))
 def test_wall_residual_matches_oracle(built_lib, oracle_lib, kind):
     """The residual of one stage (sweeps plus the viscous terms with the wall closures) of the
