@@ -85,6 +85,12 @@ extern "C" {
                                 third-order dT/dn vanish, T_w = (18 T1 - 9 T2 + 2 T3) / 11; halo
                                 layer k mirrors the point k inside (momentum negated); the same
                                 Carpenter closures and scope as OSB_BC_ISOTHERMAL_WALL. */
+#define OSB_BC_INLET_PRESSURE_EXTRAP 10 /* InletPressureExtrapolateBC (inlet_pressure_extrapolate.py:11-
+                                  73), low x face: where |u_n| >= a at the boundary plane it takes
+                                  the inflow state the halo holds, else rhoE of the plane is copied
+                                  into the bc_depth halo layers; a ModifyCentralDerivative face
+                                  (the viscous terms' Carpenter closures apply).  Restated in the
+                                  oracle; the GPU path refuses it (OSB_EINVAL at osb_block_add). */
 
 /* Convective split form of OSB_SCHEME_CENTRAL4 (physical_models/split_forms.py). */
 #define OSB_SPLIT_FEIEREISEN 0 /* skew-symmetric form, split_forms.py:111-145 */

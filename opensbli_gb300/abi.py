@@ -40,6 +40,7 @@ BC_DIRICHLET = 6
 BC_PRESSURE_OUTLET = 7
 BC_ISOTHERMAL_WALL = 8
 BC_ADIABATIC_WALL = 9
+BC_INLET_PRESSURE_EXTRAP = 10  # oracle only (the GPU path refuses it)
 SPLIT_FEIEREISEN = 0
 SPLIT_KGP = 1
 FILTER_NONE = 0

@@ -1182,6 +1182,10 @@ bool check_desc(const osb_block_desc* d, std::string& why) {
   for (int i = 0; i < d->ndim; ++i)
     for (int s = 0; s < 2; ++s) {
       const int k = d->bc[i][s];
+      if (k == OSB_BC_INLET_PRESSURE_EXTRAP) {
+        why = "the pressure-extrapolation inlet is restated in the oracle only (no GPU kernel)";
+        return false;
+      }
       if (k < OSB_BC_PERIODIC || k > OSB_BC_ADIABATIC_WALL) { why = "unknown boundary kind"; return false; }
       if (k == OSB_BC_ISOTHERMAL_WALL || k == OSB_BC_ADIABATIC_WALL) {
         if (d->ndim != 3 || i != 1 || d->metric[9] || d->scheme == OSB_SCHEME_CENTRAL4) {

@@ -158,6 +158,37 @@ def channel_tcf(sizes=(16, 17, 8), stretch=1.7):
     return spec, _cons(spec, r, [u0, u1, u2], p)
 
 
+def duct_inlet(sizes=(20, 17, 8), minf=0.5, re=100.0):
+    """The inflow / outflow faces of the SBLI apps (apps/katzer_SBLI/katzer_SBLI.py:131-160) on a
+    3D duct x in [0, 4], y in [-1, 1] (walls), z in [0, 2 pi) (periodic): the pressure-extrapolation
+    inlet at x = 0, zeroth-order extrapolation at x = 4, isothermal walls (Twall 1) on both y faces;
+    characteristic LLF TENO5 (Roe) + central viscous terms (modified Sutherland), Re 100.  Initial
+    state (over the whole allocation: the inlet's halos keep it as the inflow)
+    u0 = (1 - y^2)(1 + 0.05 sin z), u1 = 0.05 sin x (1 - y^2)^2, u2 = 0.05 cos x sin z (1 - y^2),
+    p = (1 + 0.02 cos x cos z) / (gama Minf^2), rho = 1 + 0.02 sin x y.  minf 0.5 takes the
+    inlet's subsonic branch, 2 its supersonic one.  The inlet is restated in the oracle only: the
+    GPU path refuses this spec."""
+    n0, n1, n2 = sizes
+    spec = BlockSpec(ndim=3, size=sizes, scheme=abi.SCHEME_TENO5, averaging=abi.AVG_ROE,
+                     viscous=abi.VISC_SUTHERLAND,
+                     bc=[[abi.BC_INLET_PRESSURE_EXTRAP, abi.BC_EXTRAP0], [abi.BC_ISOTHERMAL_WALL] * 2,
+                         [abi.BC_PERIODIC] * 2],
+                     bc_depth=[[4, 4] for _ in range(3)],
+                     delta=(4.0 / (n0 - 1), 2.0 / (n1 - 1), 2.0 * math.pi / n2), gama=1.4, Minf=minf, Re=re,
+                     Pr=0.71, mu_const=1.0, eps=1e-40, teno_ct=1e-6, wall_temperature={(1, 0): 1.0, (1, 1): 1.0})
+    x0 = spec.delta[0] * spec.grid_index(0)
+    x1 = -1.0 + spec.delta[1] * spec.grid_index(1)
+    x2 = spec.delta[2] * spec.grid_index(2)
+    g = spec.gama
+    w = 1.0 - x1 * x1
+    u0 = w * (1.0 + 0.05 * np.sin(x2))
+    u1 = 0.05 * np.sin(x0) * w * w
+    u2 = 0.05 * np.cos(x0) * np.sin(x2) * w
+    p = 1.0 / (g * minf * minf) * (1.0 + 0.02 * np.cos(x0) * np.cos(x2))
+    r = 1.0 + 0.02 * np.sin(x0) * x1
+    return spec, _cons(spec, r, [u0, u1, u2], p)
+
+
 def tgv_filtered(n=128, sizes=None, ducros=0.05):
     """The supersonic TGV of the reference's Central4-WENO5 benchmark
     (apps/performance_benchmark/Central4-WENO5; the central branch of

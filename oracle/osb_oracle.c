@@ -747,11 +747,18 @@ int oracle_ystretch_metrics(int n, double delta, const double* x1, int wall_lo, 
 
 /* Closure row of the point with index i along d for derivatives of `order`: 0..3 (first) or
  * 0..1 (second) next to a low wall face, 4 + r next to a high one, -1 for the central rule. */
-static inline int is_wall(int kind) { return kind == OSB_BC_ISOTHERMAL_WALL || kind == OSB_BC_ADIABATIC_WALL; }
+static inline int modifies_central(int kind) {
+  /* every ModifyCentralDerivative face kind (bc_core.py:15-17): walls, the pressure-extrapolation
+   * inlet, extrapolation, Dirichlet and pressure-outlet faces; their central derivatives only
+   * occur on viscous blocks */
+  return kind == OSB_BC_ISOTHERMAL_WALL || kind == OSB_BC_ADIABATIC_WALL || kind == OSB_BC_INLET_PRESSURE_EXTRAP ||
+         kind == OSB_BC_EXTRAP0 || kind == OSB_BC_EXTRAP1 || kind == OSB_BC_DIRICHLET ||
+         kind == OSB_BC_PRESSURE_OUTLET;
+}
 static int closure_row(const osb_block_desc* b, const geom_t* g, int d, int i, int order) {
   const int rows = order == 1 ? 4 : 2;
-  if (is_wall(b->bc[d][0]) && i < rows) return i;
-  if (is_wall(b->bc[d][1]) && i > g->n[d] - 1 - rows) return 4 + (g->n[d] - 1 - i);
+  if (modifies_central(b->bc[d][0]) && i < rows) return i;
+  if (modifies_central(b->bc[d][1]) && i > g->n[d] - 1 - rows) return 4 + (g->n[d] - 1 - i);
   return -1;
 }
 
@@ -1759,6 +1766,32 @@ static void adiabatic_wall_point(osb_block_desc* b, const geom_t* g, int d, int 
  * same direction): the halo layers of face (d, side) receive the neighbour's layers adjacent to
  * its face (d, f->side).  `full` = 0 copies the interior of the face only; `full` = 1 also the
  * transverse halos (depth of this face), which the neighbour has filled by then. */
+/* InletPressureExtrapolateBC at a low face (inlet_pressure_extrapolate.py:33-73, the generated
+ * "InletPressureExtrapolate boundary" kernel): from the boundary-plane state, |u_i| and the sound
+ * speed; where the normal |u| >= a the plane takes the state of halo layer 1 (the inflow the
+ * initialisation left there), otherwise the plane keeps its state and rhoE of the plane is
+ * copied into the halo layers. */
+static void inlet_point(osb_block_desc* b, const geom_t* g, int d, int side, int depth, const int* c, long t) {
+  (void)side;
+  (void)t;
+  const int nd = b->ndim, nv = nd + 2;
+  const long id = gid(g, c[0], c[1], c[2]);
+  const long s = g->st[d];
+  const double gm = b->gama, rhob = b->q[0][id];
+  double ub[3] = {0.0, 0.0, 0.0}, usq = 0.0;
+  for (int e = 0; e < nd; ++e) {
+    ub[e] = fabs(b->q[1 + e][id] / b->q[0][id]);
+    usq += ub[e] * ub[e];
+  }
+  const double pb = (gm - 1.0) * (-0.5 * usq * rhob + b->q[nv - 1][id]);
+  const double ab = sqrt(gm * pb / rhob);
+  if (ub[d] >= ab) {
+    for (int v = 0; v < nv; ++v) b->q[v][id] = b->q[v][id - s];
+  } else {
+    for (int m = 1; m <= depth; ++m) b->q[nv - 1][id - m * s] = b->q[nv - 1][id];
+  }
+}
+
 static void interface_face(osb_block_desc* blocks, osb_block_desc* b, const geom_t* g, int d, int side, int depth,
                            int full) {
   const osb_interface* f = &b->iface[d][side];
@@ -1812,6 +1845,10 @@ int oracle_apply_bc(osb_block_desc* blocks, int nblocks, int zero_grad_only) {
             for_face(b, &g, d, side, depth, side == 0 ? 0 : g.n[d] - 1, isothermal_wall_point);
           if (pass == 1 && kind == OSB_BC_ADIABATIC_WALL)
             for_face(b, &g, d, side, depth, side == 0 ? 0 : g.n[d] - 1, adiabatic_wall_point);
+          if (pass == 1 && kind == OSB_BC_INLET_PRESSURE_EXTRAP) {
+            if (side != 0) return -1; /* the reference implements the inlet on low faces only */
+            for_face(b, &g, d, side, depth, 0, inlet_point);
+          }
           if (pass == 1 && kind == OSB_BC_DIRICHLET) {
             if (!b->dirichlet[d][side]) return -1;
             for_face(b, &g, d, side, depth, 0, dirichlet_point);

@@ -484,6 +484,64 @@ def case_channel_tcf():
     return block, p
 
 
+def case_duct_inlet(minf=0.5):
+    """The inflow / outflow faces of the SBLI apps (apps/katzer_SBLI/katzer_SBLI.py:131-160) on a
+    3D duct: InletPressureExtrapolateBC at x = 0 and ExtrapolationBC(order=0) at the far x face,
+    isothermal no-slip walls on both y faces, periodic z; characteristic LLF TENO5 (Roe average)
+    plus central viscous terms, RK-LS3, Minf = `minf` (0.5: the subsonic branch of the inlet, the
+    pressure extrapolated into its halos; 2: the supersonic branch).  The inlet, outlet and wall
+    faces are ModifyCentralDerivative boundaries: the viscous terms take the Carpenter closures
+    at all four.  The inflow state is what the initialisation left in the inlet's halos."""
+    import copy
+    from opensbli import (RoeAverage, LFTeno, StoreSome, RungeKuttaLS, PeriodicBC, IsothermalWallBC,
+                          SimulationBlock, GridBasedInitialisation, GridVariable, DataObject, parse_expr,
+                          ConstantObject, Eq)
+    from opensbli.core.boundary_conditions.inlet_pressure_extrapolate import InletPressureExtrapolateBC
+    from opensbli.core.boundary_conditions.extrapolation import ExtrapolationBC
+    ndim = 3
+    sim = _euler_equations(ndim, "Teno", viscous=True)
+    cr = _constituents(ndim, viscous=True)
+    block = SimulationBlock(ndim, block_number=0)
+    local_dict = {"block": block, "GridVariable": GridVariable, "DataObject": DataObject}
+    eqns = ["Eq(GridVariable(x0), block.deltas[0]*block.grid_indexes[0])",
+            "Eq(GridVariable(x1), -1.0 + block.deltas[1]*block.grid_indexes[1])",
+            "Eq(GridVariable(x2), block.deltas[2]*block.grid_indexes[2])",
+            "Eq(GridVariable(u0), (1.0 - x1*x1)*(1.0 + 0.05*sin(x2)))",
+            "Eq(GridVariable(u1), 0.05*sin(x0)*(1.0 - x1*x1)*(1.0 - x1*x1))",
+            "Eq(GridVariable(u2), 0.05*cos(x0)*sin(x2)*(1.0 - x1*x1))",
+            "Eq(GridVariable(p), 1.0/(gama*Minf*Minf)*(1.0 + 0.02*cos(x0)*cos(x2)))",
+            "Eq(GridVariable(r), 1.0 + 0.02*sin(x0)*x1)",
+            "Eq(DataObject(rho), r)", "Eq(DataObject(rhou0), r*u0)", "Eq(DataObject(rhou1), r*u1)",
+            "Eq(DataObject(rhou2), r*u2)",
+            "Eq(DataObject(rhoE), p/(gama-1) + 0.5* r *(u0**2+ u1**2 + u2**2))"]
+    initial = GridBasedInitialisation()
+    initial.add_equations([parse_expr(e, local_dict=local_dict) for e in eqns])
+    schemes = {}
+    LF = LFTeno(order=5, averaging=RoeAverage([0, 1]), flux_type="LLF")
+    schemes[LF.name] = LF
+    cent = StoreSome(4, "u0 u1 u2")
+    schemes[cent.name] = cent
+    rk = RungeKuttaLS(3)
+    schemes[rk.name] = rk
+    block.set_discretisation_schemes(schemes)
+    q = flatten_q(sim)
+    gama, Minf, Twall = ConstantObject("gama"), ConstantObject("Minf"), ConstantObject("Twall")
+    wall = [Eq(q[4], Twall * q[0] / (gama * Minf ** 2.0 * (gama - 1)))]
+    bcs = [InletPressureExtrapolateBC(0, 0), ExtrapolationBC(0, 1, order=0),
+           IsothermalWallBC(1, 0, wall[:]), IsothermalWallBC(1, 1, wall[:]),
+           PeriodicBC(2, 0, halos=[-4, 4]), PeriodicBC(2, 1, halos=[-4, 4])]
+    block.set_block_boundaries(bcs)
+    block.set_equations([copy.deepcopy(cr), copy.deepcopy(sim), initial])
+    block.discretise()
+    p = {"Re": "100.0", "gama": "1.4", "Minf": repr(float(minf)), "Pr": "0.71", "Twall": "1.0",
+         "dt": 'osb_env_double("OSB_DT", 0.0005)', "niter": 'osb_env_int("OSB_NITER", 1)',
+         "TENO_CT": 'osb_env_double("OSB_TENO_CT", 1e-6)'}
+    for d, (n, dl) in enumerate([(20, "4.0/(block0np0-1)"), (17, "2.0/(block0np1-1)"), (8, "2*M_PI/block0np2")]):
+        p["block0np%d" % d] = 'osb_env_int("OSB_NP%d", %d)' % (d, n)
+        p["Delta%dblock0" % d] = dl
+    return block, p
+
+
 def flatten_q(sim):
     from sympy import flatten
     return flatten(sim.time_advance_arrays)
@@ -823,6 +881,8 @@ CASES = {
     "channel_adi": case_channel_adi,
     "channel_str": lambda: case_channel_iso(stretch=True),
     "channel_tcf": case_channel_tcf,
+    "duct_inlet_sub": lambda: case_duct_inlet(0.5),
+    "duct_inlet_sup": lambda: case_duct_inlet(2.0),
 }
 
 

@@ -80,6 +80,14 @@ CASES = {
     "channel_tcf_16x17x8_perturbed": ("channel_tcf", lambda: problems.channel_tcf((16, 17, 8)),
                                       {"OSB_NP0": 16, "OSB_NP1": 17, "OSB_NP2": 8}, 2e-4, [1, 3, 30],
                                       (1e-3, 44)),
+    # the SBLI apps' inflow / outflow faces: the pressure-extrapolation inlet (subsonic and
+    # supersonic branch) and the extrapolation outlet, with the viscous terms' closures at both
+    "duct_inlet_sub_20x17x8_perturbed": ("duct_inlet_sub", lambda: problems.duct_inlet((20, 17, 8), minf=0.5),
+                                         {"OSB_NP0": 20, "OSB_NP1": 17, "OSB_NP2": 8}, 5e-4, [1, 3, 30],
+                                         (1e-3, 45)),
+    "duct_inlet_sup_20x17x8_perturbed": ("duct_inlet_sup", lambda: problems.duct_inlet((20, 17, 8), minf=2.0),
+                                         {"OSB_NP0": 20, "OSB_NP1": 17, "OSB_NP2": 8}, 5e-4, [1, 3, 30],
+                                         (1e-3, 46)),
     # 3D curvilinear TENO5 (MetricsEquation, every direction curvilinear); the solver's own metric
     # arrays are stored with the states (interior; their halos are the periodic images)
     "curv3d_teno5_16x12x10_perturbed": ("curv3d_teno5", lambda: problems.curvilinear_wave_3d((16, 12, 10)),

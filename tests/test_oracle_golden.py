@@ -66,6 +66,12 @@ CASES = {
     # the TENO turbulent-channel app's discretisation: TENO6, power-law viscosity, constant
     # forcing, stretched wall-normal grid, SSP RK3
     "channel_tcf_16x17x8_perturbed": (lambda: _channel_tcf(), "ssp3", (1e-3, 44), 1e-12),
+    # the SBLI apps' pressure-extrapolation inlet (subsonic / supersonic branch) and extrapolation
+    # outlet on a walled duct, the viscous terms' closures at all four faces
+    "duct_inlet_sub_20x17x8_perturbed": (lambda: problems.duct_inlet((20, 17, 8), minf=0.5), "ls3", (1e-3, 45),
+                                         1e-12),
+    "duct_inlet_sup_20x17x8_perturbed": (lambda: problems.duct_inlet((20, 17, 8), minf=2.0), "ls3", (1e-3, 46),
+                                         1e-12),
 }
 
 
