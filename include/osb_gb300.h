@@ -53,11 +53,14 @@ extern "C" {
 
 /* Viscous terms: none (Euler), modified Sutherland law mu(T) (compressible_TGV.py:82),
  * constant viscosity (split_forms.py viscosity='constant'), or the power law mu = T^visc_power
- * of apps/channel_flow/compressible_TCF_TENO/turbulent_channel.py:93. */
+ * of apps/channel_flow/compressible_TCF_TENO/turbulent_channel.py:93, or Sutherland's law with
+ * its ratio S = SuthT / RefT, mu = T^1.5 (1 + S) / (T + S) (apps/katzer_SBLI/katzer_SBLI.py:67;
+ * restated in the oracle, refused by the GPU path). */
 #define OSB_VISC_NONE 0
 #define OSB_VISC_SUTHERLAND 1
 #define OSB_VISC_CONSTANT 2
 #define OSB_VISC_POWER_LAW 3
+#define OSB_VISC_SUTHERLAND_RATIO 4
 
 /* Boundary conditions per face (core/boundary_conditions/). */
 #define OSB_BC_PERIODIC 0    /* PeriodicBC -> ExchangeSelf (periodic.py:25-71) */
@@ -180,6 +183,7 @@ typedef struct osb_block_desc {
    * R(rhoE) -= sum_j c_j u_j, applied by the central viscous kernel (3D Cartesian viscous
    * blocks; OSB_EINVAL otherwise). */
   double forcing[3];
+  double sutherland_s;       /* OSB_VISC_SUTHERLAND_RATIO: S = SuthT / RefT */
 } osb_block_desc;
 
 /* ---- library / context ------------------------------------------------------------- */
@@ -363,8 +367,8 @@ int osb_metrics(const osb_block_desc* desc, const double* const* x, double* cons
 
 /* Binding check: writes sizeof(osb_block_desc) and the byte offsets of size, bc, iface, gama,
  * delta, q, rkold, metric, split_form, ducros_check, tvd_kappa, dirichlet, flux_type,
- * back_pressure, wall_temperature, ystretch, visc_power and forcing into out[0..18] (n >= 19).
- * Needs no GPU. */
+ * back_pressure, wall_temperature, ystretch, visc_power, forcing and sutherland_s into
+ * out[0..19] (n >= 20).  Needs no GPU. */
 int osb_desc_layout(long long* out, int n);
 
 #ifdef __cplusplus

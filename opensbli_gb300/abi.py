@@ -29,6 +29,7 @@ VISC_NONE = 0
 VISC_SUTHERLAND = 1
 VISC_CONSTANT = 2
 VISC_POWER_LAW = 3  # mu = T^visc_power (the TENO channel app)
+VISC_SUTHERLAND_RATIO = 4  # mu = T^1.5 (1 + S) / (T + S), S = SuthT / RefT: oracle only
 
 BC_PERIODIC = 0
 BC_ZERO_GRAD = 1
@@ -124,6 +125,7 @@ class BlockDesc(ctypes.Structure):
         ("ystretch", ctypes.c_void_p * 2),
         ("visc_power", ctypes.c_double),
         ("forcing", ctypes.c_double * 3),
+        ("sutherland_s", ctypes.c_double),
     ]
 
 
@@ -134,7 +136,7 @@ def layout_signature():
             BlockDesc.split_form.offset, BlockDesc.ducros_check.offset, BlockDesc.tvd_kappa.offset,
             BlockDesc.dirichlet.offset, BlockDesc.flux_type.offset, BlockDesc.back_pressure.offset,
             BlockDesc.wall_temperature.offset, BlockDesc.ystretch.offset, BlockDesc.visc_power.offset,
-            BlockDesc.forcing.offset]
+            BlockDesc.forcing.offset, BlockDesc.sutherland_s.offset]
     return [ctypes.sizeof(BlockDesc)] + offs
 
 
@@ -173,6 +175,7 @@ def make_desc(spec, q_ptrs, rk_ptrs, metric_ptrs=None, dirichlet_ptrs=None, ystr
     d.tvd_kappa = spec.tvd_kappa
     d.flux_type = spec.flux_type
     d.visc_power = spec.visc_power
+    d.sutherland_s = spec.sutherland_s
     for i, c in enumerate(spec.forcing or (0.0, 0.0, 0.0)):
         d.forcing[i] = c
     for (i, side), bp in (spec.back_pressure or {}).items():

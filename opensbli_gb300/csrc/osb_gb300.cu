@@ -1148,6 +1148,10 @@ bool check_desc(const osb_block_desc* d, std::string& why) {
   if (!(d->scheme == OSB_SCHEME_WENO5_JS || d->scheme == OSB_SCHEME_WENO5_Z || d->scheme == OSB_SCHEME_TENO5 ||
         d->scheme == OSB_SCHEME_TENO6 || d->scheme == OSB_SCHEME_CENTRAL4)) { why = "unknown scheme"; return false; }
   if (d->averaging != OSB_AVG_SIMPLE && d->averaging != OSB_AVG_ROE) { why = "unknown averaging"; return false; }
+  if (d->viscous == OSB_VISC_SUTHERLAND_RATIO) {
+    why = "Sutherland's law with a SuthT / RefT ratio is restated in the oracle only (no GPU kernel)";
+    return false;
+  }
   if (d->viscous < OSB_VISC_NONE || d->viscous > OSB_VISC_POWER_LAW) { why = "unknown viscosity law"; return false; }
   if (d->viscous == OSB_VISC_POWER_LAW && !(d->visc_power > 0.0)) {
     why = "the power-law viscosity needs a positive exponent (visc_power)";
@@ -1308,7 +1312,7 @@ int osb_last_error(char* buf, size_t n) {
 }
 
 int osb_desc_layout(long long* out, int n) {
-  if (!out || n < 19) return fail(OSB_EINVAL, "need 19 slots");
+  if (!out || n < 20) return fail(OSB_EINVAL, "need 20 slots");
   out[0] = sizeof(osb_block_desc);
   out[1] = offsetof(osb_block_desc, size);
   out[2] = offsetof(osb_block_desc, bc);
@@ -1328,6 +1332,7 @@ int osb_desc_layout(long long* out, int n) {
   out[16] = offsetof(osb_block_desc, ystretch);
   out[17] = offsetof(osb_block_desc, visc_power);
   out[18] = offsetof(osb_block_desc, forcing);
+  out[19] = offsetof(osb_block_desc, sutherland_s);
   return OSB_OK;
 }
 

@@ -189,6 +189,58 @@ def duct_inlet(sizes=(20, 17, 8), minf=0.5, re=100.0):
     return spec, _cons(spec, r, [u0, u1, u2], p)
 
 
+def katzer_line(n1, lx1=115.0, by=5.0, j=None):
+    """Wall-normal coordinate of the Katzer SBLI grid, Lx1 sinh(by xi_1 / Lx1) / sinh(by) with
+    xi_1 = Delta_1 j, Delta_1 = Lx1 / (n1 - 1), in the generated grid kernel's operation order
+    (apps/katzer_SBLI/katzer_SBLI.py:185)."""
+    j = np.arange(n1) if j is None else j
+    d1 = lx1 / (n1 - 1)
+    inv = 1.0 / lx1
+    return np.sinh(by * inv * d1 * j) / (inv * np.sinh(by))
+
+
+def katzer(sizes=(24, 17)):
+    """The discretisation of apps/katzer_SBLI/katzer_SBLI.py (direct shock-capturing branch) on
+    a small block: 2D, WENO5-Z (simple average, LLF) + central viscous terms with Sutherland's
+    law (S = SuthT / RefT = 110.4 / 288), Minf 2, Re 950, Pr 0.72, the SSP RK3; x in [0, 400]
+    (Delta_0 = 400 / (n0 - 1)) with the pressure-extrapolation inlet at x = 0 and zeroth-order
+    extrapolation at x = 400; the sinh-stretched wall-normal grid y in [0, 115] (katzer_line)
+    with an isothermal wall (Twall 1.67619431) at y = 0 and the app's Dirichlet shock-generator
+    state (post-shock where x0 > 40) over the top plane and its 4 halo layers.  Initial fields
+    (the app's similarity solution replaced): w = tanh(y / 5), u0 = w (1 + 0.01 sin(0.05 x)),
+    u1 = 0.01 w sin(0.1 x), T = Twall + (1 - Twall) w, p = 1 / (gama Minf^2), rho = gama Minf^2 p / T.
+    Sutherland's ratio form and the inlet are restated in the oracle only: the GPU path refuses
+    this spec."""
+    n0, n1 = sizes
+    gama, minf, tw = 1.4, 2.0, 1.67619431
+    spec = BlockSpec(ndim=2, size=sizes, scheme=abi.SCHEME_WENO5_Z, averaging=abi.AVG_SIMPLE,
+                     viscous=abi.VISC_SUTHERLAND_RATIO, sutherland_s=110.4 * (1.0 / 288.0),
+                     bc=[[abi.BC_INLET_PRESSURE_EXTRAP, abi.BC_EXTRAP0], [abi.BC_ISOTHERMAL_WALL, abi.BC_DIRICHLET]],
+                     bc_depth=[[4, 4], [4, 4]], delta=(400.0 / (n0 - 1), 115.0 / (n1 - 1)), gama=gama, Minf=minf,
+                     Re=950.0, Pr=0.72, eps=1e-40, wall_temperature={(1, 0): tw})
+    x0 = spec.delta[0] * spec.grid_index(0)
+    x1 = katzer_line(n1, j=spec.grid_index(1))
+    spec.ystretch = abi.ystretch_metrics(katzer_line(n1), spec.delta[1])
+    w = np.tanh(x1 / 5.0)
+    u0 = w * (1.0 + 0.01 * np.sin(0.05 * x0))
+    u1 = 0.01 * w * np.sin(0.1 * x0)
+    T = tw + (1.0 - tw) * w
+    p = 1.0 / (gama * minf * minf) + 0.0 * T
+    r = gama * minf * minf * p / T
+    q = _cons(spec, r, [u0, u1], p)
+    h = spec.halo
+    x = spec.delta[0] * np.arange(-h, n0 + h, dtype=np.float64)
+    post = x > 40.0
+    top_row = [np.where(post, 1.129734572, 1.00000596004), np.where(post, 1.0921171, 1.00000268202),
+               np.where(post, -0.058866065, 0.00565001630205), np.where(post, 1.0590824, 0.94644428042)]
+    dep = spec.bc_depth[1][1]
+    top = np.empty((4, dep + 1, n0 + 2 * h))
+    for v in range(4):
+        top[v] = top_row[v][None, :]
+    spec.dirichlet = {(1, 1): top}
+    return spec, q
+
+
 def tgv_filtered(n=128, sizes=None, ducros=0.05):
     """The supersonic TGV of the reference's Central4-WENO5 benchmark
     (apps/performance_benchmark/Central4-WENO5; the central branch of

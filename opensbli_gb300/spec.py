@@ -58,6 +58,8 @@ class BlockSpec:
     # (osb_block_desc.visc_power / forcing)
     visc_power: float = 0.0
     forcing: tuple = None
+    # OSB_VISC_SUTHERLAND_RATIO: S = SuthT / RefT
+    sutherland_s: float = 0.0
 
     def __post_init__(self):
         self.size = tuple(int(s) for s in self.size)
@@ -120,6 +122,8 @@ class BlockSpec:
             rec["visc_power"] = float(self.visc_power)
         if self.forcing and any(self.forcing):
             rec["forcing"] = [float(c) for c in self.forcing]
+        if self.sutherland_s:
+            rec["sutherland_s"] = float(self.sutherland_s)
         if self.wall_temperature:  # (absent otherwise: records of blocks without walls are unchanged)
             rec["wall_temperature"] = [[d, s, float(v)] for (d, s), v in sorted(self.wall_temperature.items())]
         arrays = {"dirichlet_%d_%d" % k: np.ascontiguousarray(a) for k, a in (self.dirichlet or {}).items()}
@@ -144,6 +148,8 @@ class BlockSpec:
             kw["visc_power"] = float(rec["visc_power"])
         if rec.get("forcing"):
             kw["forcing"] = tuple(float(c) for c in rec["forcing"])
+        if rec.get("sutherland_s"):
+            kw["sutherland_s"] = float(rec["sutherland_s"])
         dirichlet = {}
         for name, a in (arrays or {}).items():
             if name.startswith("dirichlet_"):

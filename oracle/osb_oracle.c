@@ -118,6 +118,8 @@ static void cr_compute(const osb_block_desc* b, const geom_t* g, cr_t* c) {
       c->mu[id] = 1.4042 * T * sqrt(T) / (0.40417 + T);
     else if (b->viscous == OSB_VISC_POWER_LAW) /* turbulent_channel.py:93, mu = T**0.7 */
       c->mu[id] = pow(T, b->visc_power);
+    else if (b->viscous == OSB_VISC_SUTHERLAND_RATIO) /* katzer_SBLI.py:67 */
+      c->mu[id] = pow(T, 1.5) * (1.0 + b->sutherland_s) / (b->sutherland_s + T);
     else
       c->mu[id] = b->mu_const;
   }

@@ -542,6 +542,93 @@ def case_duct_inlet(minf=0.5):
     return block, p
 
 
+def case_katzer():
+    """The discretisation of ``apps/katzer_SBLI/katzer_SBLI.py`` (its direct shock-capturing
+    branch, lines 30-160): 2D Navier-Stokes with WENO5-Z (simple average, LLF), StoreSome(4,
+    'u0 u1 T'), the Sutherland law mu = T^1.5 (1 + SuthT/RefT) / (T + SuthT/RefT), the SSP RK3, a
+    sinh-stretched wall-normal grid (Lx1 sinh(by xi_1 / Lx1) / sinh(by)) transformed by a
+    MetricsEquation stretched in y, the pressure-extrapolation inlet at x = 0, zeroth-order
+    extrapolation at the far x face, an isothermal wall (Twall 1.67619431) at y = 0 and the app's
+    Dirichlet shock-generator state at the top (post-shock where x0 > 40); the app's parameters
+    (Minf 2, Re 950, Pr 0.72) on a 24 x 17 block.  The app's similarity-solution initialisation
+    (Initialise_Katzer) is replaced by analytic fields: the golden runs replace the state anyway."""
+    import copy
+    from sympy import sinh
+    from opensbli import (EinsteinEquation, SimulationEquations, ConstituentRelations, SimpleAverage, LFWeno,
+                          StoreSome, RungeKuttaLS, IsothermalWallBC, DirichletBC, SimulationBlock,
+                          GridBasedInitialisation, GridVariable, DataObject, parse_expr, ConstantObject, Eq,
+                          MetricsEquation)
+    from opensbli.core.boundary_conditions.inlet_pressure_extrapolate import InletPressureExtrapolateBC
+    from opensbli.core.boundary_conditions.extrapolation import ExtrapolationBC
+    ndim = 2
+    eq = EinsteinEquation()
+    constants = ["Re", "Pr", "gama", "Minf", "SuthT", "RefT"]
+    sc1 = "**{'scheme':'Weno'}"
+    mass = "Eq(Der(rho,t), - Conservative(rhou_j,x_j,%s))" % sc1
+    momentum = "Eq(Der(rhou_i,t) , -Conservative(rhou_i*u_j + KD(_i,_j)*p,x_j , %s) + Der(tau_i_j,x_j) )" % sc1
+    energy = "Eq(Der(rhoE,t), - Conservative((p+rhoE)*u_j,x_j, %s) - Der(q_j,x_j) + Der(u_i*tau_i_j ,x_j) )" % sc1
+    subs = ["Eq(tau_i_j, (mu/Re)*(Der(u_i,x_j)+ Der(u_j,x_i) - (2/3)* KD(_i,_j)* Der(u_k,x_k)))",
+            "Eq(q_j, (-mu/((gama-1)*Minf*Minf*Pr*Re))*Der(T,x_j))"]
+    sim = SimulationEquations()
+    for base in (mass, momentum, energy):
+        sim.add_equations(eq.expand(base, ndim, "x", subs, constants))
+    cr = ConstituentRelations()
+    for r in ["Eq(u_i, rhou_i/rho)", "Eq(p, (gama-1)*(rhoE - rho*(1/2)*(KD(_i,_j)*u_i*u_j)))",
+              "Eq(a, (gama*p/rho)**0.5)", "Eq(T, p*gama*Minf*Minf/(rho))",
+              "Eq(mu, (T**(1.5)*(1.0+SuthT/RefT)/(T+SuthT/RefT)))"]:
+        cr.add_equations(eq.expand(r, ndim, "x", [], constants))
+    block = SimulationBlock(ndim, block_number=0)
+    metriceq = MetricsEquation()
+    metriceq.generate_transformations(ndim, "x", [(False, False), (True, False)], 2)
+    sim.apply_metrics(metriceq)
+    schemes = {}
+    LF = LFWeno(order=5, formulation="Z", averaging=SimpleAverage([0, 1]), flux_type="LLF")
+    schemes[LF.name] = LF
+    cent = StoreSome(4, "u0 u1 T")
+    schemes[cent.name] = cent
+    rk = RungeKuttaLS(3, formulation="SSP")
+    schemes[rk.name] = rk
+    block.set_discretisation_schemes(schemes)
+    local_dict = {"block": block, "GridVariable": GridVariable, "DataObject": DataObject}
+    for con in ["Minf", "Twall", "Lx1", "by"]:
+        local_dict[con] = ConstantObject(con)
+    x_loc = parse_expr("Eq(GridVariable(x0), block.deltas[0]*block.grid_indexes[0])", local_dict=local_dict)
+    q = flatten_q(sim)
+    rhoE_wall = parse_expr("Eq(DataObject(rhoE), DataObject(rho)*Twall/(gama*(gama-1.0)*Minf**2.0))",
+                           local_dict=local_dict)
+    top = [parse_expr(e, local_dict=local_dict) for e in [
+        "Eq(DataObject(rho), Piecewise((1.129734572, (x0)>40.0), (1.00000596004, True)))",
+        "Eq(DataObject(rhou0), Piecewise((1.0921171, (x0)>40.0), (1.00000268202, True)))",
+        "Eq(DataObject(rhou1), Piecewise((-0.058866065, (x0)>40.0), (0.00565001630205, True)))",
+        "Eq(DataObject(rhoE), Piecewise((1.0590824, (x0)>40.0), (0.94644428042, True)))"]]
+    bcs = [[InletPressureExtrapolateBC(0, 0), ExtrapolationBC(0, 1, order=0)],
+           [IsothermalWallBC(1, 0, [rhoE_wall]), DirichletBC(1, 1, [x_loc] + top)]]
+    block.set_block_boundaries(bcs)
+    grid = [parse_expr("Eq(DataObject(x0), block.deltas[0]*block.grid_indexes[0])", local_dict=local_dict),
+            parse_expr("Eq(DataObject(x1), Lx1*sinh(by*block.deltas[1]*block.grid_indexes[1]/Lx1)/sinh(by))",
+                       local_dict=local_dict)]
+    fields = ["Eq(GridVariable(w), tanh(DataObject(x1)/5.0))",
+              "Eq(GridVariable(u0), w*(1.0 + 0.01*sin(0.05*DataObject(x0))))",
+              "Eq(GridVariable(u1), 0.01*w*sin(0.1*DataObject(x0)))",
+              "Eq(GridVariable(T), Twall + (1.0 - Twall)*w)",
+              "Eq(GridVariable(p), 1.0/(gama*Minf*Minf))",
+              "Eq(GridVariable(r), gama*Minf*Minf*p/T)",
+              "Eq(DataObject(rho), r)", "Eq(DataObject(rhou0), r*u0)", "Eq(DataObject(rhou1), r*u1)",
+              "Eq(DataObject(rhoE), p/(gama-1) + 0.5* r *(u0**2+ u1**2))"]
+    local_dict["gama"] = ConstantObject("gama")
+    initial = GridBasedInitialisation()
+    initial.add_equations(grid + [parse_expr(e, local_dict=local_dict) for e in fields])
+    block.set_equations([copy.deepcopy(cr), sim, initial, metriceq])
+    block.discretise()
+    p = {"gama": "1.4", "Minf": "2.0", "Pr": "0.72", "Re": "950.0", "Twall": "1.67619431",
+         "SuthT": "110.4", "RefT": "288.0", "Lx1": "115.0", "by": "5.0",
+         "dt": 'osb_env_double("OSB_DT", 0.04)', "niter": 'osb_env_int("OSB_NITER", 1)'}
+    for d, (n, dl) in enumerate([(24, "400.0/(block0np0-1)"), (17, "115.0/(block0np1-1)")]):
+        p["block0np%d" % d] = 'osb_env_int("OSB_NP%d", %d)' % (d, n)
+        p["Delta%dblock0" % d] = dl
+    return block, p
+
+
 def flatten_q(sim):
     from sympy import flatten
     return flatten(sim.time_advance_arrays)
@@ -883,6 +970,7 @@ CASES = {
     "channel_tcf": case_channel_tcf,
     "duct_inlet_sub": lambda: case_duct_inlet(0.5),
     "duct_inlet_sup": lambda: case_duct_inlet(2.0),
+    "katzer": case_katzer,
 }
 
 

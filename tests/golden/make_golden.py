@@ -88,6 +88,10 @@ CASES = {
     "duct_inlet_sup_20x17x8_perturbed": ("duct_inlet_sup", lambda: problems.duct_inlet((20, 17, 8), minf=2.0),
                                          {"OSB_NP0": 20, "OSB_NP1": 17, "OSB_NP2": 8}, 5e-4, [1, 3, 30],
                                          (1e-3, 46)),
+    # the Katzer SBLI app's discretisation: 2D WENO5-Z + viscous terms (Sutherland ratio law),
+    # inlet, extrapolation outlet, isothermal wall, Dirichlet top, sinh-stretched y, SSP RK3
+    "katzer_24x17_perturbed": ("katzer", lambda: problems.katzer((24, 17)), {"OSB_NP0": 24, "OSB_NP1": 17}, 0.04,
+                               [1, 3, 30], (1e-3, 47)),
     # 3D curvilinear TENO5 (MetricsEquation, every direction curvilinear); the solver's own metric
     # arrays are stored with the states (interior; their halos are the periodic images)
     "curv3d_teno5_16x12x10_perturbed": ("curv3d_teno5", lambda: problems.curvilinear_wave_3d((16, 12, 10)),
@@ -120,11 +124,13 @@ def make(name):
             out["residual_1"] = np.stack([r["Residual%d_B0" % v][sl] for v in range(spec.nvars)])
         if n == 1 and spec.ystretch is not None:
             h = spec.halo
-            line = (slice(h, h + 1), slice(h, h + spec.size[1]), slice(h, h + 1))
+            rows = slice(h, h + spec.size[1])
+            line = (slice(h, h + 1), rows, slice(h, h + 1)) if spec.ndim == 3 else (rows, slice(h, h + 1))
             out["ystretch"] = np.stack([r[m][line].reshape(-1) for m in ("D11_B0", "SD111_B0")])
             for m in ("D11_B0", "SD111_B0"):  # a function of the row only
                 a = r[m][sl]
-                assert np.array_equal(a, np.broadcast_to(a[:1, :, :1], a.shape))
+                first = a[:1, :, :1] if spec.ndim == 3 else a[:, :1]
+                assert np.array_equal(a, np.broadcast_to(first, a.shape))
         elif n == 1 and spec.ndim == 3 and "detJ_B0" in r:
             mets = [r[m + "_B0"] for m in METRIC_NAMES]
             for m in mets:  # the generated solver exchanges its metrics periodically

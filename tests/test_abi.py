@@ -26,8 +26,8 @@ def test_library_exports_every_symbol(built_lib):
 
 def test_descriptor_layout(built_lib):
     lib = abi.load_library()
-    out = (ctypes.c_longlong * 19)()
-    assert lib.osb_desc_layout(out, 19) == 0
+    out = (ctypes.c_longlong * 20)()
+    assert lib.osb_desc_layout(out, 20) == 0
     assert list(out) == abi.layout_signature()
 
 
@@ -35,7 +35,7 @@ def test_version_and_errors(built_lib):
     lib = abi.load_library()
     assert lib.osb_version() == 100
     assert lib.osb_desc_layout(None, 0) == abi.OSB_EINVAL
-    assert "19 slots" in abi.last_error(lib)
+    assert "20 slots" in abi.last_error(lib)
 
 
 def test_new_entry_points_reject_bad_arguments_without_a_gpu(built_lib):

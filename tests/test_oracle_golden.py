@@ -72,6 +72,9 @@ CASES = {
                                          1e-12),
     "duct_inlet_sup_20x17x8_perturbed": (lambda: problems.duct_inlet((20, 17, 8), minf=2.0), "ls3", (1e-3, 46),
                                          1e-12),
+    # the Katzer SBLI app's discretisation (2D; inlet, extrapolation outlet, isothermal wall and
+    # Dirichlet top, all with closures; sinh-stretched y; Sutherland's ratio law; SSP RK3)
+    "katzer_24x17_perturbed": (lambda: _katzer(), "ssp3", (1e-3, 47), 1e-12),
 }
 
 
@@ -90,6 +93,13 @@ def _channel_tcf(sizes=(16, 17, 8), stretch=1.7):
     """The TENO channel app's case with the oracle's own wall-normal metrics."""
     spec, q = problems.channel_tcf(sizes, stretch=stretch)
     spec.ystretch = harness.ystretch_metrics(problems.stretched_line(sizes[1], stretch), spec.delta[1])
+    return spec, q
+
+
+def _katzer(sizes=(24, 17)):
+    """The Katzer SBLI case with the oracle's own wall-normal metrics."""
+    spec, q = problems.katzer(sizes)
+    spec.ystretch = harness.ystretch_metrics(problems.katzer_line(sizes[1]), spec.delta[1])
     return spec, q
 
 
