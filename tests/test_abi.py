@@ -82,3 +82,25 @@ def test_pressure_outlet_without_back_pressure_refused(built_lib):
     d.back_pressure[0][1] = 0.0
     assert lib.osb_stage_noalloc(ctypes.byref(d), abi.RK_LOW_STORAGE, 0.0, 0.5, 0.1, None) == abi.OSB_EINVAL
     assert "back pressure" in abi.last_error(lib)
+
+
+def test_ystretch_metrics_host_function(built_lib):
+    """osb_ystretch_metrics (host work, no GPU): a uniform line gives D11 = 1 / x' and SD111 = 0
+    to rounding; short, non-monotone and wall-less lines are refused with OSB_EINVAL."""
+    import numpy as np
+    import pytest
+    n, d = 17, 1.0 / 16.0
+    x = -1.0 + 2.0 * np.arange(n) / (n - 1)  # x' = 2 on xi in [0, 1]
+    d11, sd = abi.ystretch_metrics(x, d)
+    assert np.max(np.abs(d11 - 0.5)) < 1e-13 and np.max(np.abs(sd)) < 1e-11
+    with pytest.raises(abi.OSBError):
+        abi.ystretch_metrics(x[:10], d)  # fewer than 12 rows
+    bad = x.copy()
+    bad[5] = bad[4]
+    bad[6] = bad[4]
+    bad[7] = bad[4]
+    bad[3] = bad[4]
+    with pytest.raises(abi.OSBError):
+        abi.ystretch_metrics(bad, d)  # a flat stretch: x' = 0 somewhere
+    with pytest.raises(abi.OSBError):
+        abi.ystretch_metrics(x, d, wall_lo=False)  # no rule for the rows next to a free end
