@@ -1345,6 +1345,10 @@ int osb_ystretch_metrics(int32_t n, double delta, const double* x1, int32_t wall
   if (!x1 || !d11 || !sd111) return fail(OSB_EINVAL, "null argument");
   if (n < 12) return fail(OSB_EINVAL, "a stretched line needs at least 12 points (got %d)", n);
   if (!(delta > 0.0)) return fail(OSB_EINVAL, "delta must be positive");
+  const bool inc = x1[1] > x1[0];
+  for (int j = 0; j + 1 < n; ++j)
+    if (inc ? !(x1[j + 1] > x1[j]) : !(x1[j + 1] < x1[j]))
+      return fail(OSB_EINVAL, "the grid line is not strictly monotone (rows %d, %d)", j, j + 1);
   const Closures& cl = closures();
   const double inv = 1.0 / delta;
   // derivative of f at row j: closure rows next to a wall, the central rule elsewhere (which
