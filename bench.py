@@ -61,7 +61,7 @@ def parse():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="tgv",
-                    choices=["tgv", "sod", "tgv64", "kh_ensemble", "curv4", "c4w5", "tvd", "shock", "channel"],
+                    choices=["tgv", "sod", "tgv64", "kh_ensemble", "curv4", "c4w5", "tvd", "shock", "channel", "tcf"],
                     help="tgv: the 256^3 supersonic TGV (headline); sod: the 400-point Sod tube; tgv64: the "
                          "64^3 central TGV; kh_ensemble: 64 uneven 2D Kelvin-Helmholtz instances in one "
                          "persistent launch per stage; curv4: the 4-block 3D curvilinear TENO5 case; c4w5: the "
@@ -69,7 +69,8 @@ def parse():
                          "app's TVD branch (central KGP + TVD filter) at --size^3; shock: the 2D inviscid shock "
                          "reflection app (457 x 255, Dirichlet / extrapolation / symmetry boundaries); channel: a "
                          "3D channel between isothermal no-slip walls (TENO5 + viscous terms with the Carpenter "
-                         "closures), 256 x 257 x 128")
+                         "closures), 256 x 257 x 128; tcf: the TENO turbulent-channel app's discretisation at its "
+                         "129^3 (TENO6, power-law viscosity, forcing, stretched walls, SSP RK3)")
     ap.add_argument("--ensemble", type=int, default=64)
     ap.add_argument("--variant", type=int, default=0, help="x-sweep tiling variant when --fuse is given")
     ap.add_argument("--fuse", default="auto", choices=["auto", "0", "1"],
@@ -544,7 +545,7 @@ def _merge_errors(per_block):
 
 
 def secondary_arm(args):
-    """sod / tgv64 / kh_ensemble / curv4 / c4w5 / tvd / shock / channel workloads: FP32-residual throughput (whole batch per step), the FP64
+    """sod / tgv64 / kh_ensemble / curv4 / c4w5 / tvd / shock / channel / tcf workloads: FP32-residual throughput (whole batch per step), the FP64
     per-block path beside it, the FP32-vs-FP64 error after the timed steps' count, launches."""
     import torch
     from opensbli_gb300 import abi, autotune, problems
@@ -604,6 +605,16 @@ def secondary_arm(args):
         bytes_pt = 4 * 5 * 8
         cpu_args = ("channel_iso", {"OSB_NP0": 64, "OSB_NP1": 65, "OSB_NP2": 32, "OSB_DT": 2e-4}, 64 * 65 * 32, 12,
                     "a 64 x 65 x 32 channel of the reference's generated solver (the same discretisation)")
+    elif args.workload == "tcf":
+        blocks = [problems.channel_tcf((129, 129, 129))]
+        dt = 2e-4
+        rk = (abi.RK_LOW_STORAGE, problems.RK3_SSP_A, problems.RK3_SSP_B)
+        work = ("the TENO turbulent-channel app's discretisation at its 129^3: TENO6 (Roe) + central-4 viscous "
+                "terms with mu = T^0.7, forcing c = (-1, 0, 0), isothermal walls on the tanh-stretched y grid "
+                "(stretch 1.7), Re 190.71, Minf 0.0955, SSP RK3, dt 2e-4 as the app")
+        bytes_pt = 4 * 5 * 8
+        cpu_args = ("channel_tcf", {"OSB_NP0": 64, "OSB_NP1": 65, "OSB_NP2": 32, "OSB_DT": 2e-4}, 64 * 65 * 32, 12,
+                    "a 64 x 65 x 32 block of the reference's generated solver of the app's discretisation")
     elif args.workload == "tvd":
         n = args.size
         blocks = [problems.tgv_tvd(n, kappa=1.25)]

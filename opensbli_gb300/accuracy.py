@@ -68,6 +68,11 @@ def workload(name, size=256, scheme=abi.SCHEME_TENO5, averaging=abi.AVG_ROE, min
     if name == "channel":
         return ([problems.channel_iso((256, 257, 128))], 2e-4, "ls3",
                 "channel 256 x 257 x 128 between isothermal walls, TENO5 + viscous (Carpenter closures), dt 2e-4")
+    if name == "tcf":
+        return ([problems.channel_tcf((129, 129, 129))], 2e-4, (abi.RK_LOW_STORAGE, problems.RK3_SSP_A,
+                                                               problems.RK3_SSP_B),
+                "the TENO turbulent-channel app's discretisation at 129^3 (TENO6, mu = T^0.7, forcing, "
+                "stretched walls, SSP RK3), dt 2e-4")
     raise ValueError("unknown workload %s" % name)
 
 
@@ -119,7 +124,7 @@ def run(size=256, steps=1000, every=50, scheme=abi.SCHEME_TENO5, averaging=abi.A
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", default="tgv", choices=["tgv", "tgv64", "kh_ensemble", "curv4", "channel"])
+    ap.add_argument("--workload", default="tgv", choices=["tgv", "tgv64", "kh_ensemble", "curv4", "channel", "tcf"])
     ap.add_argument("--size", type=int, default=256)
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--every", type=int, default=50)
