@@ -1224,9 +1224,13 @@ bool check_desc(const osb_block_desc* d, std::string& why) {
         why = "a Dirichlet face needs its values (osb_block_desc.dirichlet)";
         return false;
       }
-      if ((k == OSB_BC_EXTRAP0 || k == OSB_BC_EXTRAP1) &&
+      // ExtrapolationBC, DirichletBC and PressureOutletBC are ModifyCentralDerivative faces
+      // (bc_core.py:15-17): the reference's central derivatives take the Carpenter closures next
+      // to them, which the central kernel implements at y walls only
+      if ((k == OSB_BC_EXTRAP0 || k == OSB_BC_EXTRAP1 || k == OSB_BC_DIRICHLET || k == OSB_BC_PRESSURE_OUTLET) &&
           (d->scheme == OSB_SCHEME_CENTRAL4 || d->viscous != OSB_VISC_NONE)) {
-        why = "extrapolation boundaries with central derivatives need the Carpenter boundary closures";
+        why = "extrapolation, Dirichlet and pressure-outlet faces with central derivatives need the Carpenter "
+              "boundary closures (implemented at y walls only)";
         return false;
       }
     }
