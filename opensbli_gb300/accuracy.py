@@ -5,6 +5,7 @@
     python -m opensbli_gb300.accuracy --workload kh_ensemble --steps 2000 --every 200
     python -m opensbli_gb300.accuracy --workload curv4 --steps 500 --every 50
     python -m opensbli_gb300.accuracy --workload channel --steps 500 --every 50
+    python -m opensbli_gb300.accuracy --workload tcf --steps 500 --every 50
 
 Advances, in lockstep from the same initial state, the FP64 path (the reference solution),
 the FP32-residual path (FP64 state, RK register and reductions) and -- with --floor -- a second
@@ -19,7 +20,8 @@ Workloads: tgv (the supersonic TGV at --size^3, CFL 0.5 at t = 0, --scheme), tgv
 low-Mach TGV with the central scheme, dt 3.385e-3), kh_ensemble (the 64 seeded Kelvin-Helmholtz
 instances, dt 2e-4, the FP32 run on the persistent batched stage), curv4 (the 4-block 3D
 curvilinear case, CFL 0.5 at t = 0), channel (the 256 x 257 x 128 channel between isothermal
-walls, dt 2e-4).
+walls, dt 2e-4), tcf (the TENO turbulent-channel app's discretisation at its 129^3, SSP RK3,
+dt 2e-4).
 """
 import argparse
 import json
